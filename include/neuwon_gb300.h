@@ -1,0 +1,166 @@
+/*
+ * neuwon_gb300 -- C ABI of the GB300 (sm_103a) implementation of NEUWON's
+ * per-time-step hot path, the staggered Model.advance().
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status: NW_OK (0) or a negative NW_ERR_* code.  After an
+ * error, nw_last_error() gives a one-line description.  A context owns one
+ * CUDA device, one stream and the device mirror of the model's
+ * structure-of-arrays; calls on one context are not thread-safe (the
+ * reference is single-threaded too).  Host pointers passed in are only read
+ * during the call unless stated otherwise.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the reference project).
+ */
+#ifndef NEUWON_GB300_H
+#define NEUWON_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nw_ctx nw_ctx;
+
+/* Status codes. */
+#define NW_OK            0
+#define NW_ERR_ARG      -1   /* bad argument (size, name, range)             */
+#define NW_ERR_CUDA     -2   /* CUDA runtime error                           */
+#define NW_ERR_STATE    -3   /* call made in the wrong order                 */
+#define NW_ERR_NOMEM    -4   /* device allocation failed                     */
+#define NW_ERR_NUMERIC  -5   /* a kernel flagged a non-finite voltage        */
+#define NW_ERR_LIMIT    -6   /* a size exceeds what this build supports      */
+
+/* Arithmetic precision of a context's state and step kernels. */
+#define NW_F32 4
+#define NW_F64 8
+
+/* Element types for nw_set_data / nw_get_data. */
+#define NW_DTYPE_F64 1
+#define NW_DTYPE_F32 2
+#define NW_DTYPE_I64 3
+#define NW_DTYPE_I32 4
+#define NW_DTYPE_U32 5
+#define NW_DTYPE_U8  6
+
+/* Step implementations for nw_advance. */
+#define NW_PATH_BATCHED 0   /* persistent fused K-step kernel, one CTA per neuron */
+#define NW_PATH_PLAIN   1   /* per-neuron launches, one thread per row/instance  */
+
+/* ---- context -------------------------------------------------------- */
+
+/* Replaces the reference's memory-space switch (neuwon/database/memory_spaces.py:14-35,
+ * Database.using_memory_space database.py:122-154): one device, one stream. */
+int nw_ctx_create(int device, int precision, nw_ctx** out);
+int nw_ctx_destroy(nw_ctx* ctx);
+/* Copies the last error message (NUL-terminated, truncated to len). */
+int nw_last_error(nw_ctx* ctx, char* buf, int len);
+/* Version of this library (major*10000 + minor*100 + patch). */
+int nw_version(void);
+/* The context's CUDA stream, as a cudaStream_t stored into *stream. */
+int nw_get_stream(nw_ctx* ctx, void** stream);
+int nw_synchronize(nw_ctx* ctx);
+
+/* ---- model structure ------------------------------------------------ */
+
+/* Segment tree of all neurons (neuwon/rxd/neuron/segment.py:11-25 "parent",
+ * neuron.py:119-137 sort_key='neuron').  Segments are in the reference's sorted
+ * order: neurons contiguous, neuron k owning [neuron_start[k], neuron_start[k+1]).
+ * parent[i] is a global segment index or -1 for a root; parents precede children.
+ * time_step is the model dt in ms (rxd_model.py:9); the electric half step is dt/2. */
+int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
+                  const int64_t* neuron_start, const int64_t* parent,
+                  double time_step_ms, double celsius);
+
+/* Replaces Database.get_data / set_data (database.py, data_components.py:318-333)
+ * for the device-resident attributes.  name is "Class.attribute":
+ *   Segment.voltage, Segment.integral_voltage, Segment.capacitance,
+ *   Segment.axial_resistance, Segment.nonspecific_current,
+ *   hh.m, hh.h, hh.n (instance order as registered),
+ *   Neuron.AP_detected, Neuron.spike_count.
+ * Values are converted between dtype and the context precision. */
+int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int64_t count);
+int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t count);
+
+/* ---- propagator ----------------------------------------------------- */
+
+/* Replaces Segment._compute_propagator_matrix (neuwon/rxd/neuron/electric.py:78-117):
+ * builds expm(coef * dt/2) for every neuron in FP64 on the GPU from the device copies
+ * of parent, axial_resistance and capacitance, prunes |p| < prune_tolerance (the
+ * reference hard-codes machine epsilon, electric.py:114), and stores it for both
+ * step paths.  *nnz_out receives the number of kept entries (diagonal included). */
+int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out);
+
+/* Replaces DB_Class "electric_propagator_matrix" set_data (data_components.py:611-622):
+ * install an FP64 CSR propagator computed elsewhere (global indices, n x n). */
+int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr,
+                          const int64_t* col, const double* val, int64_t nnz);
+
+/* Reads the FP64 propagator back as CSR (rowptr[n+1], col[nnz], val[nnz]);
+ * pass NULL arrays to query *nnz_out only. */
+int nw_propagator_get_csr(nw_ctx* ctx, int64_t* rowptr, int64_t* col, double* val,
+                          int64_t* nnz_out);
+
+/* ---- mechanisms ----------------------------------------------------- */
+
+/* Registers the instances of the Hodgkin-Huxley mechanism
+ * (nmodl_library/artificial/hh.mod as compiled by neuwon/rxd/nmodl/__init__.py:28-63,
+ * Mechanism API neuwon/rxd/mechanisms.py:4-54).  segment[i] is instance i's segment;
+ * g*_coef[i] are its conductance coefficients in siemens (gbar[S/cm2] * 1e-8 *
+ * magnitude[um2], nmodl/__init__.py:99-107, 404-406); e* are the reversal potentials
+ * of the three nonspecific conductances (mV).  Gates start at their steady state at
+ * v_init, as the INITIAL block does. */
+int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
+                   const double* gna_coef, const double* gk_coef, const double* gl_coef,
+                   double ena, double ek, double el, double v_init);
+
+/* ---- stimulus, detection, recording --------------------------------- */
+
+/* Current clamps: replaces Segment.inject_current + TimeSeries.play on the
+ * half-step input clock (electric.py:119-125, database/time.py:245-302).
+ * Clamp k adds amps[k] (A) to its segment's sum_current on input ticks
+ * first_tick[k] <= t < first_tick[k] + num_ticks[k] (tick 1 = first half step). */
+int nw_clamps_set(nw_ctx* ctx, int64_t count, const int64_t* segment, const double* amps,
+                  const int64_t* first_tick, const int64_t* num_ticks);
+
+/* AP detectors, one per neuron (neuwon/rxd/neuron/neuron.py:139-146, 184-188). */
+int nw_detectors_set(nw_ctx* ctx, const int64_t* segment, const double* threshold_mV);
+
+/* Voltage probes: replaces TimeSeries.record of Segment.voltage after each
+ * advance (database/time.py:189-231).  Up to max_steps samples are kept. */
+int nw_probes_set(nw_ctx* ctx, int64_t count, const int64_t* segment, int64_t max_steps);
+/* Copies the recorded samples, row-major [steps][count]; *steps_out gets the row count. */
+int nw_probes_read(nw_ctx* ctx, void* host, int dtype, int64_t max_rows, int64_t* steps_out);
+
+/* ---- time stepping -------------------------------------------------- */
+
+/* Replaces RxD_Model.advance (neuwon/rxd/rxd_model.py:63-80) called k_steps times:
+ * species(dt/2) -> mechanisms(dt) -> species(dt/2) -> AP detector, per step.
+ * path selects NW_PATH_BATCHED (fused persistent kernel) or NW_PATH_PLAIN. */
+int nw_advance(nw_ctx* ctx, int32_t k_steps, int path);
+
+/* End-to-end step with host buffers: copies stim_amps (one value per clamp, A, or
+ * NULL to keep the clamps' amplitudes) from host, advances k_steps, and copies all
+ * segment voltages (context precision as dtype) back into v_out (may be NULL). */
+int nw_advance_host(nw_ctx* ctx, int32_t k_steps, const double* stim_amps,
+                    void* v_out, int v_dtype);
+
+/* Simulation clock (rxd_model.py:22-23): completed steps and input ticks. */
+int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks);
+
+/* Tuning of the batched path: lanes per propagator row (4, 8, 16 or 32, 0 = auto),
+ * threads per CTA (128..1024), CTAs per SM (0 = occupancy maximum). */
+int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm);
+int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm);
+
+/* Statistics of the installed propagator: rows, kept entries (with diagonal),
+ * stored off-diagonal entries including padding, bytes of the batched format. */
+int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* stored,
+                        int64_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEUWON_GB300_H */

@@ -1,0 +1,14 @@
+"""neuwon_gb300: GB300-native (sm_103a) implementation of NEUWON's Model.advance() hot path.
+
+The host API mirrors the reference's RxD_Model / Neuron / Segment / Mechanism
+interface; every time step runs in hand-written CUDA kernels behind the C ABI
+declared in include/neuwon_gb300.h (loaded with ctypes, no CPU fallback).
+"""
+from .mechanisms import HH, Mechanism, NMODL
+from .model import Clock, Model, Neuron, RxD_Model, Segment, TimeSeries
+from .morphology import EPSILON, Tree, geometry, neuron_sizes, passive_electric, random_tree
+
+__all__ = ["HH", "Mechanism", "NMODL", "Clock", "Model", "Neuron", "RxD_Model", "Segment",
+           "TimeSeries", "EPSILON", "Tree", "geometry", "neuron_sizes", "passive_electric",
+           "random_tree"]
+__version__ = "0.1.0"

@@ -1,0 +1,759 @@
+// C-ABI entry points of neuwon_gb300: contexts, model structure, attribute
+// transfer, mechanisms, stimulus, detectors, probes and stepping dispatch.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+
+#include "nw_internal.cuh"
+
+namespace nw {
+
+int fail(nw_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_fail(nw_ctx* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(ctx, e == cudaErrorMemoryAllocation ? NW_ERR_NOMEM : NW_ERR_CUDA, m);
+}
+
+int dev_alloc(nw_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (b.ptr && b.bytes == bytes) return NW_OK;
+    dev_free(b);
+    if (bytes == 0) return NW_OK;
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        return fail(ctx, NW_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) +
+                                       " bytes failed: " + cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    return NW_OK;
+}
+
+void dev_free(DevBuf& b) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+size_t dtype_size(int dtype) {
+    switch (dtype) {
+        case NW_DTYPE_F64: case NW_DTYPE_I64: return 8;
+        case NW_DTYPE_F32: case NW_DTYPE_I32: case NW_DTYPE_U32: return 4;
+        case NW_DTYPE_U8: return 1;
+    }
+    return 0;
+}
+
+static double read_as_double(const void* p, int dtype, int64_t i) {
+    switch (dtype) {
+        case NW_DTYPE_F64: return static_cast<const double*>(p)[i];
+        case NW_DTYPE_F32: return static_cast<const float*>(p)[i];
+        case NW_DTYPE_I64: return (double)static_cast<const int64_t*>(p)[i];
+        case NW_DTYPE_I32: return static_cast<const int32_t*>(p)[i];
+        case NW_DTYPE_U32: return static_cast<const uint32_t*>(p)[i];
+        case NW_DTYPE_U8: return static_cast<const uint8_t*>(p)[i];
+    }
+    return 0.0;
+}
+
+static void write_from_double(void* p, int dtype, int64_t i, double v) {
+    switch (dtype) {
+        case NW_DTYPE_F64: static_cast<double*>(p)[i] = v; break;
+        case NW_DTYPE_F32: static_cast<float*>(p)[i] = (float)v; break;
+        case NW_DTYPE_I64: static_cast<int64_t*>(p)[i] = (int64_t)v; break;
+        case NW_DTYPE_I32: static_cast<int32_t*>(p)[i] = (int32_t)v; break;
+        case NW_DTYPE_U32: static_cast<uint32_t*>(p)[i] = (uint32_t)v; break;
+        case NW_DTYPE_U8: static_cast<uint8_t*>(p)[i] = (uint8_t)(v != 0.0); break;
+    }
+}
+
+// Host-side conversion, then one synchronous copy (set-up data only).
+int upload_convert(nw_ctx* ctx, void* dst, int dst_dtype, const void* host, int src_dtype,
+                   int64_t count) {
+    if (count == 0) return NW_OK;
+    size_t es = dtype_size(dst_dtype);
+    if (!es || !dtype_size(src_dtype)) return fail(ctx, NW_ERR_ARG, "unknown dtype");
+    if (dst_dtype == src_dtype) {
+        NW_CUDA(ctx, cudaMemcpyAsync(dst, host, es * count, cudaMemcpyHostToDevice, ctx->stream));
+        NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return NW_OK;
+    }
+    std::vector<unsigned char> tmp(es * count);
+    for (int64_t i = 0; i < count; ++i)
+        write_from_double(tmp.data(), dst_dtype, i, read_as_double(host, src_dtype, i));
+    NW_CUDA(ctx, cudaMemcpyAsync(dst, tmp.data(), es * count, cudaMemcpyHostToDevice, ctx->stream));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return NW_OK;
+}
+
+int download_convert(nw_ctx* ctx, void* host, int dst_dtype, const void* src, int src_dtype,
+                     int64_t count) {
+    if (count == 0) return NW_OK;
+    size_t es = dtype_size(src_dtype);
+    if (!es || !dtype_size(dst_dtype)) return fail(ctx, NW_ERR_ARG, "unknown dtype");
+    if (dst_dtype == src_dtype) {
+        NW_CUDA(ctx, cudaMemcpyAsync(host, src, es * count, cudaMemcpyDeviceToHost, ctx->stream));
+        NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return NW_OK;
+    }
+    std::vector<unsigned char> tmp(es * count);
+    NW_CUDA(ctx, cudaMemcpyAsync(tmp.data(), src, es * count, cudaMemcpyDeviceToHost, ctx->stream));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t i = 0; i < count; ++i)
+        write_from_double(host, dst_dtype, i, read_as_double(tmp.data(), src_dtype, i));
+    return NW_OK;
+}
+
+static int real_dtype(nw_ctx* ctx) { return ctx->precision == NW_F64 ? NW_DTYPE_F64 : NW_DTYPE_F32; }
+
+// kI = (dt/2)/C [ms/F], kG = (dt/2 * 1e-3)/C [s/F]  (neuwon/rxd/neuron/electric.py:60-72).
+template <typename real>
+__global__ void k_factors(const double* cap, real* kI, real* kG, double h_ms, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double c = cap[i];
+    kI[i] = (real)(h_ms / c);
+    kG[i] = (real)(h_ms * 1e-3 / c);
+}
+
+static int refresh_k(nw_ctx* ctx) {
+    if (!ctx->have_cap) return NW_OK;
+    int64_t n = ctx->n_seg;
+    int threads = 256;
+    int64_t blocks = (n + threads - 1) / threads;
+    double h = 0.5 * ctx->time_step;
+    if (ctx->precision == NW_F64)
+        k_factors<double><<<blocks, threads, 0, ctx->stream>>>(
+            ctx->cap64.as<double>(), ctx->kI.as<double>(), ctx->kG.as<double>(), h, n);
+    else
+        k_factors<float><<<blocks, threads, 0, ctx->stream>>>(
+            ctx->cap64.as<double>(), ctx->kI.as<float>(), ctx->kG.as<float>(), h, n);
+    NW_CUDA(ctx, cudaGetLastError());
+    return NW_OK;
+}
+
+template <typename real>
+__global__ void fill_real(real* p, real v, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+static int fill(nw_ctx* ctx, DevBuf& b, double v, int64_t n) {
+    if (n == 0) return NW_OK;
+    int threads = 256;
+    int64_t blocks = (n + threads - 1) / threads;
+    if (ctx->precision == NW_F64)
+        fill_real<double><<<blocks, threads, 0, ctx->stream>>>(b.as<double>(), v, n);
+    else
+        fill_real<float><<<blocks, threads, 0, ctx->stream>>>(b.as<float>(), (float)v, n);
+    NW_CUDA(ctx, cudaGetLastError());
+    return NW_OK;
+}
+
+static int64_t neuron_of(const nw_ctx* ctx, int64_t seg) {
+    const auto& s = ctx->h_neuron_start;
+    return (int64_t)(std::upper_bound(s.begin(), s.end(), seg) - s.begin()) - 1;
+}
+
+// HH steady state at v (nmodl_library/artificial/hh.mod:48-53, 62-94).
+static void hh_steady(double v, double* m, double* h, double* n) {
+    auto vtrap = [](double x, double y) {
+        return std::fabs(x / y) < 1e-6 ? y * (1 - x / y / 2) : x / (std::exp(x / y) - 1);
+    };
+    double a = .1 * vtrap(-(v + 40), 10), b = 4 * std::exp(-(v + 65) / 18);
+    *m = a / (a + b);
+    a = .07 * std::exp(-(v + 65) / 20); b = 1 / (std::exp(-(v + 35) / 10) + 1);
+    *h = a / (a + b);
+    a = .01 * vtrap(-(v + 55), 10); b = .125 * std::exp(-(v + 65) / 80);
+    *n = a / (a + b);
+}
+
+// Scatters user-order clamp amplitudes (staged as f64) into the neuron-sorted array.
+template <typename real>
+__global__ void stage_clamp_amps(const double* stage, const int64_t* sorted_to_user, real* amp, int64_t n) {
+    int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s < n) amp[s] = (real)stage[sorted_to_user[s]];
+}
+
+}  // namespace nw
+
+using namespace nw;
+
+extern "C" {
+
+int nw_version(void) { return 100; }
+
+int nw_ctx_create(int device, int precision, nw_ctx** out) {
+    if (!out) return NW_ERR_ARG;
+    *out = nullptr;
+    if (precision != NW_F32 && precision != NW_F64) return NW_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return NW_ERR_CUDA;
+    }
+    nw_ctx* ctx = new nw_ctx();
+    ctx->device = device;
+    ctx->precision = precision;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    int sms = 0, optin = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e != cudaSuccess) { delete ctx; return NW_ERR_CUDA; }
+    ctx->num_sms = sms;
+    ctx->smem_optin = (size_t)optin;
+    if (dev_alloc(ctx, ctx->work_counter, 64) != NW_OK ||
+        dev_alloc(ctx, ctx->status, 64) != NW_OK) { delete ctx; return NW_ERR_NOMEM; }
+    cudaMemsetAsync(ctx->status.ptr, 0, 64, ctx->stream);
+    *out = ctx;
+    return NW_OK;
+}
+
+int nw_ctx_destroy(nw_ctx* ctx) {
+    if (!ctx) return NW_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec,
+                      &ctx->kI, &ctx->kG, &ctx->cap64, &ctx->res64, &ctx->p_rowptr, &ctx->p_col,
+                      &ctx->p_val, &ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak,
+                      &ctx->hh.seg, &ctx->hh.gm, &ctx->hh.gh, &ctx->hh.gn, &ctx->hh.cna,
+                      &ctx->hh.ck, &ctx->hh.cl, &ctx->hh.seg_ptr, &ctx->hh.neuron_ptr,
+                      &ctx->clamp_seg, &ctx->clamp_amp, &ctx->clamp_first, &ctx->clamp_count,
+                      &ctx->clamp_neuron_ptr, &ctx->clamp_amp_stage, &ctx->det_seg, &ctx->det_thr,
+                      &ctx->ap_detected, &ctx->ap_state, &ctx->spike_count, &ctx->probe_seg,
+                      &ctx->probe_neuron_ptr, &ctx->probe_slot, &ctx->trace, &ctx->neuron_order,
+                      &ctx->work_counter, &ctx->status, &ctx->plain_x};
+    for (DevBuf* b : bufs) dev_free(*b);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return NW_OK;
+}
+
+int nw_last_error(nw_ctx* ctx, char* buf, int len) {
+    if (!buf || len <= 0) return NW_ERR_ARG;
+    const char* m = ctx ? ctx->err.c_str() : "no context";
+    std::strncpy(buf, m, (size_t)len - 1);
+    buf[len - 1] = '\0';
+    return NW_OK;
+}
+
+int nw_get_stream(nw_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return NW_ERR_ARG;
+    *stream = (void*)ctx->stream;
+    return NW_OK;
+}
+
+int nw_synchronize(nw_ctx* ctx) {
+    if (!ctx) return NW_ERR_ARG;
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return NW_OK;
+}
+
+int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
+                  const int64_t* neuron_start, const int64_t* parent,
+                  double time_step_ms, double celsius) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (num_segments <= 0 || num_neurons <= 0 || !neuron_start || !parent)
+        return fail(ctx, NW_ERR_ARG, "nw_model_init: empty model or null arrays");
+    if (!(time_step_ms > 0.0)) return fail(ctx, NW_ERR_ARG, "nw_model_init: time_step must be > 0");
+    if (neuron_start[0] != 0 || neuron_start[num_neurons] != num_segments)
+        return fail(ctx, NW_ERR_ARG, "nw_model_init: neuron_start must span [0, num_segments]");
+    int64_t maxn = 0;
+    for (int64_t k = 0; k < num_neurons; ++k) {
+        int64_t a = neuron_start[k], b = neuron_start[k + 1];
+        if (b <= a) return fail(ctx, NW_ERR_ARG, "nw_model_init: empty or unordered neuron range");
+        maxn = std::max(maxn, b - a);
+        for (int64_t i = a; i < b; ++i) {
+            int64_t p = parent[i];
+            if (p >= 0 && (p < a || p >= i))
+                return fail(ctx, NW_ERR_ARG, "nw_model_init: parent of segment " + std::to_string(i) +
+                                             " must be an earlier segment of the same neuron");
+        }
+    }
+    if (maxn > 65535)
+        return fail(ctx, NW_ERR_LIMIT, "nw_model_init: neurons larger than 65535 segments are not supported");
+    ctx->n_seg = num_segments;
+    ctx->n_neuron = num_neurons;
+    ctx->max_neuron = maxn;
+    ctx->time_step = time_step_ms;
+    ctx->celsius = celsius;
+    ctx->h_neuron_start.assign(neuron_start, neuron_start + num_neurons + 1);
+    ctx->h_parent.assign(parent, parent + num_segments);
+    ctx->prop_valid = false;
+    ctx->have_cap = ctx->have_res = false;
+    ctx->nonspec_nonzero = false;
+    ctx->g_valid = false;
+    ctx->input_ticks = ctx->steps = 0;
+    ctx->have_detectors = false;
+    ctx->n_clamps = 0;
+    ctx->n_probes = 0;
+    ctx->hh = HHState();
+    size_t rs = (size_t)ctx->precision;
+    NW_CHECK(dev_alloc(ctx, ctx->neuron_start, 8 * (num_neurons + 1)));
+    NW_CHECK(dev_alloc(ctx, ctx->parent, 8 * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->V, rs * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->Vint, rs * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->Inonspec, rs * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->kI, rs * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->kG, rs * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->cap64, 8 * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->res64, 8 * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->plain_x, rs * num_segments));
+    NW_CUDA(ctx, cudaMemcpyAsync(ctx->neuron_start.ptr, neuron_start, 8 * (num_neurons + 1),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    NW_CUDA(ctx, cudaMemcpyAsync(ctx->parent.ptr, parent, 8 * num_segments,
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    NW_CHECK(fill(ctx, ctx->V, -70.0, num_segments));   // rxd_model.py:12 initial_voltage
+    NW_CUDA(ctx, cudaMemsetAsync(ctx->Vint.ptr, 0, rs * num_segments, ctx->stream));
+    NW_CUDA(ctx, cudaMemsetAsync(ctx->Inonspec.ptr, 0, rs * num_segments, ctx->stream));
+    // Default AP detectors: each neuron's first segment (its root), 20 mV (neuron.py:141,156).
+    std::vector<int64_t> dseg(num_neurons);
+    std::vector<double> dthr(num_neurons, 20.0);
+    for (int64_t k = 0; k < num_neurons; ++k) dseg[k] = neuron_start[k];
+    NW_CHECK(nw_detectors_set(ctx, dseg.data(), dthr.data()));
+    // Work order: largest neurons first (longest-processing-time-first).
+    std::vector<int32_t> order(num_neurons);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+        return (neuron_start[a + 1] - neuron_start[a]) > (neuron_start[b + 1] - neuron_start[b]);
+    });
+    NW_CHECK(dev_alloc(ctx, ctx->neuron_order, 4 * num_neurons));
+    NW_CUDA(ctx, cudaMemcpyAsync(ctx->neuron_order.ptr, order.data(), 4 * num_neurons,
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return NW_OK;
+}
+
+int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int64_t count) {
+    if (!ctx || !name || (!host && count)) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    std::string nm(name);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_set_data before nw_model_init");
+    auto need = [&](int64_t n) {
+        return count == n ? NW_OK : fail(ctx, NW_ERR_ARG, nm + ": expected " + std::to_string(n) +
+                                                           " values, got " + std::to_string(count));
+    };
+    int rd = real_dtype(ctx);
+    if (nm == "Segment.voltage") {
+        NW_CHECK(need(ctx->n_seg));
+        return upload_convert(ctx, ctx->V.ptr, rd, host, dtype, count);
+    }
+    if (nm == "Segment.integral_voltage") {
+        NW_CHECK(need(ctx->n_seg));
+        return upload_convert(ctx, ctx->Vint.ptr, rd, host, dtype, count);
+    }
+    if (nm == "Segment.nonspecific_current") {
+        NW_CHECK(need(ctx->n_seg));
+        bool nz = false;
+        for (int64_t i = 0; i < count && !nz; ++i) nz = read_as_double(host, dtype, i) != 0.0;
+        ctx->nonspec_nonzero = nz;
+        return upload_convert(ctx, ctx->Inonspec.ptr, rd, host, dtype, count);
+    }
+    if (nm == "Segment.capacitance" || nm == "Segment.axial_resistance") {
+        NW_CHECK(need(ctx->n_seg));
+        bool cap = nm == "Segment.capacitance";
+        for (int64_t i = 0; i < count; ++i) {
+            double v = read_as_double(host, dtype, i);
+            if (!(v > 0.0) || !std::isfinite(v)) {
+                if (!cap && ctx->h_parent[i] < 0) continue;   // a root's resistance is unused
+                return fail(ctx, NW_ERR_ARG, nm + " must be finite and > 0 (segment " + std::to_string(i) + ")");
+            }
+        }
+        NW_CHECK(upload_convert(ctx, cap ? ctx->cap64.ptr : ctx->res64.ptr, NW_DTYPE_F64, host, dtype, count));
+        if (cap) { ctx->have_cap = true; NW_CHECK(refresh_k(ctx)); }
+        else ctx->have_res = true;
+        ctx->prop_valid = false;
+        NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return NW_OK;
+    }
+    if (nm == "hh.m" || nm == "hh.h" || nm == "hh.n") {
+        NW_CHECK(need(ctx->hh.m));
+        std::vector<double> sorted(count);
+        for (int64_t i = 0; i < count; ++i) sorted[ctx->hh.user_to_sorted[i]] = read_as_double(host, dtype, i);
+        DevBuf& b = nm == "hh.m" ? ctx->hh.gm : (nm == "hh.h" ? ctx->hh.gh : ctx->hh.gn);
+        return upload_convert(ctx, b.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
+    }
+    if (nm == "Neuron.AP_detected") {
+        NW_CHECK(need(ctx->n_neuron));
+        return upload_convert(ctx, ctx->ap_detected.ptr, NW_DTYPE_U8, host, dtype, count);
+    }
+    if (nm == "Neuron.spike_count") {
+        NW_CHECK(need(ctx->n_neuron));
+        return upload_convert(ctx, ctx->spike_count.ptr, NW_DTYPE_U32, host, dtype, count);
+    }
+    return fail(ctx, NW_ERR_ARG, "nw_set_data: unknown attribute " + nm);
+}
+
+int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t count) {
+    if (!ctx || !name || (!host && count)) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    std::string nm(name);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_get_data before nw_model_init");
+    auto need = [&](int64_t n) {
+        return count == n ? NW_OK : fail(ctx, NW_ERR_ARG, nm + ": expected " + std::to_string(n) +
+                                                           " values, got " + std::to_string(count));
+    };
+    int rd = real_dtype(ctx);
+    if (nm == "Segment.voltage") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->V.ptr, rd, count); }
+    if (nm == "Segment.integral_voltage") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->Vint.ptr, rd, count); }
+    if (nm == "Segment.nonspecific_current") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->Inonspec.ptr, rd, count); }
+    if (nm == "Segment.capacitance") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->cap64.ptr, NW_DTYPE_F64, count); }
+    if (nm == "Segment.axial_resistance") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->res64.ptr, NW_DTYPE_F64, count); }
+    if (nm == "hh.m" || nm == "hh.h" || nm == "hh.n") {
+        NW_CHECK(need(ctx->hh.m));
+        const DevBuf& b = nm == "hh.m" ? ctx->hh.gm : (nm == "hh.h" ? ctx->hh.gh : ctx->hh.gn);
+        std::vector<double> sorted(count);
+        NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, b.ptr, rd, count));
+        for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[ctx->hh.user_to_sorted[i]]);
+        return NW_OK;
+    }
+    if (nm == "Neuron.AP_detected") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->ap_detected.ptr, NW_DTYPE_U8, count); }
+    if (nm == "Neuron.spike_count") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->spike_count.ptr, NW_DTYPE_U32, count); }
+    return fail(ctx, NW_ERR_ARG, "nw_get_data: unknown attribute " + nm);
+}
+
+int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_propagator_build before nw_model_init");
+    if (!ctx->have_cap || !ctx->have_res)
+        return fail(ctx, NW_ERR_STATE, "nw_propagator_build needs Segment.capacitance and Segment.axial_resistance");
+    if (!(prune_tolerance >= 0.0)) return fail(ctx, NW_ERR_ARG, "prune_tolerance must be >= 0");
+    NW_CHECK(propagator_build(ctx, prune_tolerance, nnz_out));
+    NW_CHECK(propagator_to_batched(ctx));
+    ctx->prop_valid = true;
+    return NW_OK;
+}
+
+int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr, const int64_t* col,
+                          const double* val, int64_t nnz) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_propagator_set_csr before nw_model_init");
+    if (n != ctx->n_seg || !rowptr || (nnz && (!col || !val)))
+        return fail(ctx, NW_ERR_ARG, "nw_propagator_set_csr: shape does not match the model");
+    if (rowptr[0] != 0 || rowptr[n] != nnz) return fail(ctx, NW_ERR_ARG, "nw_propagator_set_csr: bad rowptr");
+    for (int64_t k = 0; k < ctx->n_neuron; ++k) {
+        int64_t a = ctx->h_neuron_start[k], b = ctx->h_neuron_start[k + 1];
+        for (int64_t i = a; i < b; ++i) {
+            if (rowptr[i + 1] < rowptr[i]) return fail(ctx, NW_ERR_ARG, "nw_propagator_set_csr: rowptr decreases");
+            for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+                if (col[e] < a || col[e] >= b)
+                    return fail(ctx, NW_ERR_ARG, "nw_propagator_set_csr: entry couples two neurons (row " +
+                                                 std::to_string(i) + ")");
+        }
+    }
+    NW_CHECK(propagator_from_host(ctx, rowptr, col, val, nnz));
+    NW_CHECK(propagator_to_batched(ctx));
+    ctx->prop_valid = true;
+    return NW_OK;
+}
+
+int nw_propagator_get_csr(nw_ctx* ctx, int64_t* rowptr, int64_t* col, double* val, int64_t* nnz_out) {
+    if (!ctx) return NW_ERR_ARG;
+    if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");
+    if (nnz_out) *nnz_out = ctx->nnz64;
+    if (!rowptr) return NW_OK;
+    NW_CUDA(ctx, cudaMemcpyAsync(rowptr, ctx->p_rowptr.ptr, 8 * (ctx->n_seg + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<int32_t> c32(ctx->nnz64);
+    if (ctx->nnz64) {
+        NW_CUDA(ctx, cudaMemcpyAsync(c32.data(), ctx->p_col.ptr, 4 * ctx->nnz64, cudaMemcpyDeviceToHost, ctx->stream));
+        NW_CUDA(ctx, cudaMemcpyAsync(val, ctx->p_val.ptr, 8 * ctx->nnz64, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t e = 0; e < ctx->nnz64; ++e) col[e] = c32[e];
+    return NW_OK;
+}
+
+int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* stored, int64_t* bytes) {
+    if (!ctx) return NW_ERR_ARG;
+    if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");
+    if (rows) *rows = ctx->n_seg;
+    if (nnz) *nnz = ctx->nnz64;
+    if (stored) *stored = ctx->nnz_b;
+    if (bytes) *bytes = ctx->nnz_b * (2 + ctx->precision) + ctx->n_seg * (8 + ctx->precision);
+    return NW_OK;
+}
+
+int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
+                   const double* gna_coef, const double* gk_coef, const double* gl_coef,
+                   double ena, double ek, double el, double v_init) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_hh_register before nw_model_init");
+    if (num_instances < 0 || (num_instances && (!segment || !gna_coef || !gk_coef || !gl_coef)))
+        return fail(ctx, NW_ERR_ARG, "nw_hh_register: null arrays");
+    const int64_t m = num_instances, n = ctx->n_seg;
+    for (int64_t i = 0; i < m; ++i)
+        if (segment[i] < 0 || segment[i] >= n)
+            return fail(ctx, NW_ERR_ARG, "nw_hh_register: segment index out of range");
+    // Segment-sorted order (stable), so every segment's instances are contiguous
+    // and every neuron's instances form one range.
+    std::vector<int64_t> order(m);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return segment[a] < segment[b]; });
+    HHState& hh = ctx->hh;
+    hh = HHState();
+    hh.m = m;
+    hh.ena = ena; hh.ek = ek; hh.el = el; hh.v_init = v_init;
+    hh.user_to_sorted.assign(m, 0);
+    for (int64_t s = 0; s < m; ++s) hh.user_to_sorted[order[s]] = s;
+    hh.identity = (m == n);
+    for (int64_t s = 0; s < m && hh.identity; ++s) hh.identity = segment[order[s]] == s;
+    std::vector<uint32_t> seg(m), seg_ptr(n + 1, 0);
+    std::vector<double> cna(m), ck(m), cl(m), g0(m);
+    std::vector<int64_t> nptr(ctx->n_neuron + 1, 0);
+    for (int64_t s = 0; s < m; ++s) {
+        int64_t u = order[s];
+        seg[s] = (uint32_t)segment[u];
+        cna[s] = gna_coef[u]; ck[s] = gk_coef[u]; cl[s] = gl_coef[u];
+        seg_ptr[segment[u] + 1]++;
+        nptr[neuron_of(ctx, segment[u]) + 1]++;
+    }
+    for (int64_t i = 0; i < n; ++i) seg_ptr[i + 1] += seg_ptr[i];
+    for (int64_t k = 0; k < ctx->n_neuron; ++k) nptr[k + 1] += nptr[k];
+    double m0, h0, n0;
+    hh_steady(v_init, &m0, &h0, &n0);
+    size_t rs = (size_t)ctx->precision;
+    int rd = real_dtype(ctx);
+    NW_CHECK(dev_alloc(ctx, hh.seg, 4 * std::max<int64_t>(m, 1)));
+    NW_CHECK(dev_alloc(ctx, hh.seg_ptr, 4 * (n + 1)));
+    NW_CHECK(dev_alloc(ctx, hh.neuron_ptr, 8 * (ctx->n_neuron + 1)));
+    for (DevBuf* b : {&hh.gm, &hh.gh, &hh.gn, &hh.cna, &hh.ck, &hh.cl})
+        NW_CHECK(dev_alloc(ctx, *b, rs * std::max<int64_t>(m, 1)));
+    NW_CHECK(upload_convert(ctx, hh.seg.ptr, NW_DTYPE_U32, seg.data(), NW_DTYPE_U32, m));
+    NW_CHECK(upload_convert(ctx, hh.seg_ptr.ptr, NW_DTYPE_U32, seg_ptr.data(), NW_DTYPE_U32, n + 1));
+    NW_CHECK(upload_convert(ctx, hh.neuron_ptr.ptr, NW_DTYPE_I64, nptr.data(), NW_DTYPE_I64, ctx->n_neuron + 1));
+    NW_CHECK(upload_convert(ctx, hh.cna.ptr, rd, cna.data(), NW_DTYPE_F64, m));
+    NW_CHECK(upload_convert(ctx, hh.ck.ptr, rd, ck.data(), NW_DTYPE_F64, m));
+    NW_CHECK(upload_convert(ctx, hh.cl.ptr, rd, cl.data(), NW_DTYPE_F64, m));
+    std::fill(g0.begin(), g0.end(), m0);
+    NW_CHECK(upload_convert(ctx, hh.gm.ptr, rd, g0.data(), NW_DTYPE_F64, m));
+    std::fill(g0.begin(), g0.end(), h0);
+    NW_CHECK(upload_convert(ctx, hh.gh.ptr, rd, g0.data(), NW_DTYPE_F64, m));
+    std::fill(g0.begin(), g0.end(), n0);
+    NW_CHECK(upload_convert(ctx, hh.gn.ptr, rd, g0.data(), NW_DTYPE_F64, m));
+    ctx->g_valid = false;
+    return NW_OK;
+}
+
+int nw_clamps_set(nw_ctx* ctx, int64_t count, const int64_t* segment, const double* amps,
+                  const int64_t* first_tick, const int64_t* num_ticks) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_clamps_set before nw_model_init");
+    if (count < 0 || (count && (!segment || !amps || !first_tick || !num_ticks)))
+        return fail(ctx, NW_ERR_ARG, "nw_clamps_set: null arrays");
+    std::vector<int64_t> nb(count);
+    std::vector<int32_t> per(ctx->n_neuron + 1, 0);
+    for (int64_t c = 0; c < count; ++c) {
+        if (segment[c] < 0 || segment[c] >= ctx->n_seg || num_ticks[c] < 0)
+            return fail(ctx, NW_ERR_ARG, "nw_clamps_set: bad clamp " + std::to_string(c));
+        nb[c] = neuron_of(ctx, segment[c]);
+        if (++per[nb[c] + 1] > kMaxClampsPerNeuron)
+            return fail(ctx, NW_ERR_LIMIT, "nw_clamps_set: more than " + std::to_string(kMaxClampsPerNeuron) +
+                                           " clamps on one neuron");
+    }
+    for (int64_t k = 0; k < ctx->n_neuron; ++k) per[k + 1] += per[k];
+    std::vector<int64_t> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return nb[a] < nb[b]; });
+    std::vector<uint32_t> seg(count);
+    std::vector<double> amp(count);
+    std::vector<int64_t> first(count), cnt(count);
+    ctx->clamp_user_to_sorted.assign(count, 0);
+    for (int64_t s = 0; s < count; ++s) {
+        int64_t u = order[s];
+        ctx->clamp_user_to_sorted[u] = s;
+        seg[s] = (uint32_t)segment[u]; amp[s] = amps[u]; first[s] = first_tick[u]; cnt[s] = num_ticks[u];
+    }
+    size_t n1 = (size_t)std::max<int64_t>(count, 1);
+    NW_CHECK(dev_alloc(ctx, ctx->clamp_seg, 4 * n1));
+    NW_CHECK(dev_alloc(ctx, ctx->clamp_amp, (size_t)ctx->precision * n1));
+    NW_CHECK(dev_alloc(ctx, ctx->clamp_amp_stage, 16 * n1));
+    NW_CHECK(dev_alloc(ctx, ctx->clamp_first, 8 * n1));
+    NW_CHECK(dev_alloc(ctx, ctx->clamp_count, 8 * n1));
+    NW_CHECK(dev_alloc(ctx, ctx->clamp_neuron_ptr, 4 * (ctx->n_neuron + 1)));
+    NW_CHECK(upload_convert(ctx, ctx->clamp_seg.ptr, NW_DTYPE_U32, seg.data(), NW_DTYPE_U32, count));
+    NW_CHECK(upload_convert(ctx, ctx->clamp_amp.ptr, real_dtype(ctx), amp.data(), NW_DTYPE_F64, count));
+    NW_CHECK(upload_convert(ctx, ctx->clamp_first.ptr, NW_DTYPE_I64, first.data(), NW_DTYPE_I64, count));
+    NW_CHECK(upload_convert(ctx, ctx->clamp_count.ptr, NW_DTYPE_I64, cnt.data(), NW_DTYPE_I64, count));
+    NW_CHECK(upload_convert(ctx, ctx->clamp_neuron_ptr.ptr, NW_DTYPE_I32, per.data(), NW_DTYPE_I32, ctx->n_neuron + 1));
+    // Second half of the staging buffer: sorted position -> user index, used by
+    // nw_advance_host to scatter user-order amplitudes.
+    NW_CHECK(upload_convert(ctx, (char*)ctx->clamp_amp_stage.ptr + 8 * n1, NW_DTYPE_I64, order.data(),
+                            NW_DTYPE_I64, count));
+    ctx->n_clamps = count;
+    return NW_OK;
+}
+
+int nw_detectors_set(nw_ctx* ctx, const int64_t* segment, const double* threshold_mV) {
+    if (!ctx || !segment || !threshold_mV) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_detectors_set before nw_model_init");
+    int64_t nn = ctx->n_neuron;
+    std::vector<uint32_t> seg(nn);
+    for (int64_t k = 0; k < nn; ++k) {
+        if (segment[k] < ctx->h_neuron_start[k] || segment[k] >= ctx->h_neuron_start[k + 1])
+            return fail(ctx, NW_ERR_ARG, "nw_detectors_set: detector of neuron " + std::to_string(k) +
+                                         " is not one of its segments");
+        seg[k] = (uint32_t)segment[k];
+    }
+    NW_CHECK(dev_alloc(ctx, ctx->det_seg, 4 * nn));
+    NW_CHECK(dev_alloc(ctx, ctx->det_thr, (size_t)ctx->precision * nn));
+    NW_CHECK(dev_alloc(ctx, ctx->ap_detected, nn));
+    NW_CHECK(dev_alloc(ctx, ctx->ap_state, nn));
+    NW_CHECK(dev_alloc(ctx, ctx->spike_count, 4 * nn));
+    NW_CHECK(upload_convert(ctx, ctx->det_seg.ptr, NW_DTYPE_U32, seg.data(), NW_DTYPE_U32, nn));
+    NW_CHECK(upload_convert(ctx, ctx->det_thr.ptr, real_dtype(ctx), threshold_mV, NW_DTYPE_F64, nn));
+    NW_CUDA(ctx, cudaMemsetAsync(ctx->ap_detected.ptr, 0, nn, ctx->stream));
+    NW_CUDA(ctx, cudaMemsetAsync(ctx->ap_state.ptr, 0, nn, ctx->stream));
+    NW_CUDA(ctx, cudaMemsetAsync(ctx->spike_count.ptr, 0, 4 * nn, ctx->stream));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->have_detectors = true;
+    return NW_OK;
+}
+
+int nw_probes_set(nw_ctx* ctx, int64_t count, const int64_t* segment, int64_t max_steps) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_probes_set before nw_model_init");
+    if (count < 0 || max_steps < 0 || (count && !segment)) return fail(ctx, NW_ERR_ARG, "nw_probes_set: bad arguments");
+    std::vector<int64_t> nb(count);
+    std::vector<int32_t> per(ctx->n_neuron + 1, 0);
+    for (int64_t p = 0; p < count; ++p) {
+        if (segment[p] < 0 || segment[p] >= ctx->n_seg) return fail(ctx, NW_ERR_ARG, "nw_probes_set: bad segment");
+        nb[p] = neuron_of(ctx, segment[p]);
+        if (++per[nb[p] + 1] > kMaxProbesPerNeuron)
+            return fail(ctx, NW_ERR_LIMIT, "nw_probes_set: more than " + std::to_string(kMaxProbesPerNeuron) +
+                                           " probes on one neuron");
+    }
+    for (int64_t k = 0; k < ctx->n_neuron; ++k) per[k + 1] += per[k];
+    std::vector<int64_t> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return nb[a] < nb[b]; });
+    std::vector<uint32_t> seg(count), slot(count);
+    for (int64_t s = 0; s < count; ++s) { seg[s] = (uint32_t)segment[order[s]]; slot[s] = (uint32_t)order[s]; }
+    size_t n1 = (size_t)std::max<int64_t>(count, 1);
+    NW_CHECK(dev_alloc(ctx, ctx->probe_seg, 4 * n1));
+    NW_CHECK(dev_alloc(ctx, ctx->probe_slot, 4 * n1));
+    NW_CHECK(dev_alloc(ctx, ctx->probe_neuron_ptr, 4 * (ctx->n_neuron + 1)));
+    NW_CHECK(dev_alloc(ctx, ctx->trace, (size_t)ctx->precision * n1 * (size_t)std::max<int64_t>(max_steps, 1)));
+    NW_CHECK(upload_convert(ctx, ctx->probe_seg.ptr, NW_DTYPE_U32, seg.data(), NW_DTYPE_U32, count));
+    NW_CHECK(upload_convert(ctx, ctx->probe_slot.ptr, NW_DTYPE_U32, slot.data(), NW_DTYPE_U32, count));
+    NW_CHECK(upload_convert(ctx, ctx->probe_neuron_ptr.ptr, NW_DTYPE_I32, per.data(), NW_DTYPE_I32, ctx->n_neuron + 1));
+    ctx->n_probes = count;
+    ctx->probe_cap = max_steps;
+    ctx->probe_len = 0;
+    return NW_OK;
+}
+
+int nw_probes_read(nw_ctx* ctx, void* host, int dtype, int64_t max_rows, int64_t* steps_out) {
+    if (!ctx) return NW_ERR_ARG;
+    int64_t rows = std::min(max_rows, ctx->probe_len);
+    if (steps_out) *steps_out = ctx->probe_len;
+    if (!host || rows <= 0 || ctx->n_probes == 0) return NW_OK;
+    return download_convert(ctx, host, dtype, ctx->trace.ptr, real_dtype(ctx), rows * ctx->n_probes);
+}
+
+static int check_ready(nw_ctx* ctx, int k_steps) {
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_advance before nw_model_init");
+    if (!ctx->have_cap) return fail(ctx, NW_ERR_STATE, "nw_advance: Segment.capacitance not set");
+    if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "nw_advance: no valid propagator (build or install one)");
+    if (k_steps < 0) return fail(ctx, NW_ERR_ARG, "nw_advance: negative step count");
+    if (ctx->n_probes && ctx->probe_len + k_steps > ctx->probe_cap)
+        return fail(ctx, NW_ERR_LIMIT, "nw_advance: probe buffer full (" + std::to_string(ctx->probe_cap) + " steps)");
+    return NW_OK;
+}
+
+static int read_status(nw_ctx* ctx) {
+    int st = 0;
+    NW_CUDA(ctx, cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (st & kStatusNonFinite) {
+        cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+        return fail(ctx, NW_ERR_NUMERIC, "a segment voltage became non-finite");
+    }
+    return NW_OK;
+}
+
+int nw_advance(nw_ctx* ctx, int32_t k_steps, int path) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    NW_CHECK(check_ready(ctx, k_steps));
+    if (k_steps == 0) return NW_OK;
+    if (path == NW_PATH_BATCHED) NW_CHECK(advance_batched(ctx, k_steps));
+    else if (path == NW_PATH_PLAIN) NW_CHECK(advance_plain(ctx, k_steps));
+    else return fail(ctx, NW_ERR_ARG, "nw_advance: unknown path");
+    return read_status(ctx);
+}
+
+int nw_advance_host(nw_ctx* ctx, int32_t k_steps, const double* stim_amps, void* v_out, int v_dtype) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    NW_CHECK(check_ready(ctx, k_steps));
+    if (stim_amps && ctx->n_clamps) {
+        // Staging buffer: [user-order amplitudes (f64) | sorted -> user map (i64)].
+        size_t half = ctx->clamp_amp_stage.bytes / 2;
+        const int64_t* s2u = (const int64_t*)((char*)ctx->clamp_amp_stage.ptr + half);
+        NW_CUDA(ctx, cudaMemcpyAsync(ctx->clamp_amp_stage.ptr, stim_amps, 8 * ctx->n_clamps,
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        int threads = 256;
+        int64_t blocks = (ctx->n_clamps + threads - 1) / threads;
+        if (ctx->precision == NW_F64)
+            stage_clamp_amps<double><<<blocks, threads, 0, ctx->stream>>>(
+                ctx->clamp_amp_stage.as<double>(), s2u, ctx->clamp_amp.as<double>(), ctx->n_clamps);
+        else
+            stage_clamp_amps<float><<<blocks, threads, 0, ctx->stream>>>(
+                ctx->clamp_amp_stage.as<double>(), s2u, ctx->clamp_amp.as<float>(), ctx->n_clamps);
+        NW_CUDA(ctx, cudaGetLastError());
+    }
+    if (k_steps) NW_CHECK(advance_batched(ctx, k_steps));
+    if (v_out) {
+        int rd = real_dtype(ctx);
+        if (v_dtype == rd) {
+            NW_CUDA(ctx, cudaMemcpyAsync(v_out, ctx->V.ptr, (size_t)ctx->precision * ctx->n_seg,
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+        } else {
+            NW_CHECK(download_convert(ctx, v_out, v_dtype, ctx->V.ptr, rd, ctx->n_seg));
+        }
+    }
+    return read_status(ctx);
+}
+
+int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks) {
+    if (!ctx) return NW_ERR_ARG;
+    if (steps) *steps = ctx->steps;
+    if (input_ticks) *input_ticks = ctx->input_ticks;
+    return NW_OK;
+}
+
+int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm) {
+    if (!ctx) return NW_ERR_ARG;
+    if (lanes_per_row != 0 && lanes_per_row != 4 && lanes_per_row != 8 && lanes_per_row != 16 && lanes_per_row != 32)
+        return fail(ctx, NW_ERR_ARG, "lanes_per_row must be 0, 4, 8, 16 or 32");
+    if (threads < 128 || threads > 1024 || threads % 32)
+        return fail(ctx, NW_ERR_ARG, "threads must be a multiple of 32 in [128, 1024]");
+    if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(ctx, NW_ERR_ARG, "ctas_per_sm out of range");
+    ctx->lanes_per_row = lanes_per_row;
+    ctx->threads = threads;
+    ctx->ctas_per_sm = ctas_per_sm;
+    return NW_OK;
+}
+
+int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm) {
+    if (!ctx) return NW_ERR_ARG;
+    if (lanes_per_row) *lanes_per_row = ctx->lanes_per_row ? ctx->lanes_per_row : choose_lanes_per_row(ctx);
+    if (threads) *threads = ctx->threads;
+    if (ctas_per_sm) *ctas_per_sm = ctx->ctas_per_sm;
+    return NW_OK;
+}
+
+}  // extern "C"

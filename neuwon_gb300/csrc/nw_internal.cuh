@@ -1,0 +1,137 @@
+// Internal declarations shared by the neuwon_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/neuwon_gb300.h"
+
+namespace nw {
+
+// One device allocation owned by a context.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Largest neuron the batched path keeps in shared memory, per precision,
+// and the most clamps one neuron may carry on that path.
+constexpr int kMaxClampsPerNeuron = 16;
+constexpr int kMaxProbesPerNeuron = 64;
+
+// Status bits written by kernels into the context's status word.
+constexpr int kStatusNonFinite = 1;
+
+struct HHState {
+    int64_t m = 0;              // instances
+    bool identity = false;      // instance i sits on segment i for every i
+    double ena = 0, ek = 0, el = 0, v_init = -70.0;
+    DevBuf seg;                 // u32 [m], segment-sorted order
+    DevBuf gm, gh, gn;          // real [m] gates
+    DevBuf cna, ck, cl;         // real [m] conductance coefficients (S)
+    DevBuf seg_ptr;             // u32 [n_seg+1] instance range of each segment
+    DevBuf neuron_ptr;          // i64 [n_neuron+1] instance range of each neuron
+    std::vector<int64_t> user_to_sorted;  // registration order -> device order
+};
+
+}  // namespace nw
+
+struct nw_ctx {
+    int device = 0;
+    int precision = NW_F32;     // bytes per real
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // Topology.
+    int64_t n_seg = 0, n_neuron = 0, max_neuron = 0;
+    double time_step = 0.1, celsius = 6.3;
+    std::vector<int64_t> h_neuron_start, h_parent;
+    nw::DevBuf neuron_start;    // i64 [n_neuron+1]
+    nw::DevBuf parent;          // i64 [n_seg]
+
+    // Electric state (context precision) and FP64 passive properties.
+    nw::DevBuf V, Vint, Inonspec, kI, kG;
+    nw::DevBuf cap64, res64;    // f64 [n_seg]
+    bool have_cap = false, have_res = false, nonspec_nonzero = false;
+
+    // Propagator: FP64 CSR with the diagonal (plain path, readback) and the
+    // batched difference form (off-diagonal entries, u16 neuron-relative
+    // columns, rows padded to 4 entries, per-row leak = 1 - row sum).
+    bool prop_valid = false;
+    int64_t nnz64 = 0, nnz_b = 0;
+    nw::DevBuf p_rowptr, p_col, p_val;          // i64, i32, f64
+    nw::DevBuf b_rowptr, b_col, b_val, b_leak;  // i64, u16, real, real
+
+    // Mechanisms.
+    nw::HHState hh;
+    bool g_valid = false;       // conductances computed by a mechanism step
+
+    // Clamps (sorted by neuron, stable).
+    int64_t n_clamps = 0;
+    std::vector<int64_t> clamp_user_to_sorted;
+    nw::DevBuf clamp_seg, clamp_amp, clamp_first, clamp_count, clamp_neuron_ptr;
+    nw::DevBuf clamp_amp_stage;  // f64 staging for nw_advance_host
+
+    // Detectors (one per neuron).
+    bool have_detectors = false;
+    nw::DevBuf det_seg, det_thr, ap_detected, ap_state, spike_count;
+
+    // Probes (sorted by neuron, stable).
+    int64_t n_probes = 0, probe_cap = 0, probe_len = 0;
+    std::vector<int64_t> probe_user_to_sorted;
+    nw::DevBuf probe_seg, probe_neuron_ptr, probe_slot, trace;
+
+    // Batched-path schedule and scratch.
+    nw::DevBuf neuron_order;    // i32 [n_neuron], descending work
+    nw::DevBuf work_counter;    // i32 [1]
+    nw::DevBuf status;          // i32 [1]
+    nw::DevBuf plain_x;         // real [n_seg] scratch of the plain path
+    int lanes_per_row = 0, threads = 512, ctas_per_sm = 0;
+
+    // Clock.
+    int64_t input_ticks = 0, steps = 0;
+};
+
+namespace nw {
+
+int fail(nw_ctx* ctx, int code, const std::string& msg);
+int cuda_fail(nw_ctx* ctx, cudaError_t e, const char* what);
+int dev_alloc(nw_ctx* ctx, DevBuf& b, size_t bytes);
+void dev_free(DevBuf& b);
+size_t dtype_size(int dtype);
+
+// Propagator (nw_propagator.cu).
+int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out);
+int propagator_from_host(nw_ctx* ctx, const int64_t* rowptr, const int64_t* col,
+                         const double* val, int64_t nnz);
+int propagator_to_batched(nw_ctx* ctx);
+
+// Stepping (nw_step.cu).
+int advance_batched(nw_ctx* ctx, int k_steps);
+int advance_plain(nw_ctx* ctx, int k_steps);
+int choose_lanes_per_row(nw_ctx* ctx);
+
+// Device conversions (nw_api.cu).
+int upload_convert(nw_ctx* ctx, void* dst, int dst_dtype, const void* host, int src_dtype,
+                   int64_t count);
+int download_convert(nw_ctx* ctx, void* host, int dst_dtype, const void* src, int src_dtype,
+                     int64_t count);
+
+}  // namespace nw
+
+#define NW_CUDA(ctx, call)                                              \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return nw::cuda_fail((ctx), e_, #call);  \
+    } while (0)
+
+#define NW_CHECK(expr)                  \
+    do {                                \
+        int rc_ = (expr);               \
+        if (rc_ != NW_OK) return rc_;   \
+    } while (0)

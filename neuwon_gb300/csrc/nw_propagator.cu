@@ -1,0 +1,415 @@
+// FP64 propagator construction on the GPU and conversion to the batched format.
+//
+// The reference (neuwon/rxd/neuron/electric.py:78-117) assembles the matrix A
+// of dV/dt coefficients (four entries per parent/child edge, already scaled
+// by the half step), takes P = expm(A) with scipy and drops |P_ij| < eps.
+//
+// Here expm(A) is evaluated by the contour integral
+//     expm(A) = 1/(2 pi i) \oint e^z (zI - A)^{-1} dz
+// on the parabolic contour z(t) = N (0.1309 - 0.1194 t^2 + 0.25 i t),
+// t in (-pi, pi), with the N-point midpoint rule (Weideman & Trefethen,
+// "Parabolic and hyperbolic contours for computing the Bromwich integral",
+// Math. Comp. 76 (2007)).  A is similar to a symmetric negative semidefinite
+// matrix, so its spectrum lies on the negative real axis, which the contour
+// encloses; with N = 32 the error is a few 1e-15 (absolute) for any step
+// size.  Conjugate symmetry halves the work to 16 poles:
+//     P = (2/N) sum_{t_k > 0} Im( e^{z_k} z'_k (z_k I - A)^{-1} ).
+//
+// Each resolvent (z I - A)^{-1} of a tree-structured matrix is evaluated with
+// the elimination that trees allow without fill-in: for every directed edge
+// the Schur pivot of the branch behind it (one leaves-to-root and one
+// root-to-leaves sweep per neuron and pole), after which row i of the
+// resolvent is a product of edge ratios along the path from i.  Row i of P
+// is then collected by a depth-first walk outward from i that keeps entries
+// with |P_ij| >= tol and stops exploring a branch once |P_ij| < tol * 1e-4.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "nw_internal.cuh"
+
+namespace nw {
+
+constexpr int kPoles = 16;            // N/2 for N = 32
+constexpr int kNodes = 2 * kPoles;
+constexpr int kStackDepth = 96;
+constexpr double kExploreFactor = 1e-4;
+constexpr int kStatusStackOverflow = 2;
+constexpr int kStatusRowMismatch = 4;
+
+__constant__ double2 c_z[kPoles];     // contour nodes z_k
+__constant__ double2 c_w[kPoles];     // weights e^{z_k} z'_k
+
+struct cplx {
+    double re, im;
+    __device__ cplx() : re(0), im(0) {}
+    __device__ cplx(double r, double i) : re(r), im(i) {}
+};
+__device__ __forceinline__ cplx operator*(cplx a, cplx b) { return cplx(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+__device__ __forceinline__ cplx operator-(cplx a, cplx b) { return cplx(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ cplx operator+(cplx a, cplx b) { return cplx(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ cplx scale(double s, cplx a) { return cplx(s * a.re, s * a.im); }
+__device__ __forceinline__ cplx inv(cplx a) {
+    // Smith's algorithm keeps the quotient accurate over a wide range of |a|.
+    if (fabs(a.re) >= fabs(a.im)) {
+        double r = a.im / a.re, d = a.re + a.im * r;
+        return cplx(1.0 / d, -r / d);
+    } else {
+        double r = a.re / a.im, d = a.re * r + a.im;
+        return cplx(r / d, -1.0 / d);
+    }
+}
+__device__ __forceinline__ cplx ld(const double2* p) { double2 v = *p; return cplx(v.x, v.y); }
+__device__ __forceinline__ void st(double2* p, cplx v) { *p = make_double2(v.re, v.im); }
+
+struct BuildArgs {
+    int64_t n_seg, n_neuron;
+    const int64_t* neuron_start;
+    const int64_t* parent;
+    const int64_t* child_ptr;   // [n_seg+1]
+    const int64_t* child_idx;
+    const double* cap;          // F
+    const double* res;          // ohm
+    const double* gsum;         // sum of 1/R over the edges at each node
+    double h_s;                 // half step in seconds
+    // per pole, per node (index pole * n_seg + node)
+    double2* down;              // pivot of the branch below node c, seen from its parent
+    double2* up;                // pivot of the rest of the tree, seen from c
+    double2* invT;              // 1 / total pivot: diagonal of the resolvent
+    double tol, explore;
+    int64_t* count;             // [n_seg] kept entries per row
+    const int64_t* rowptr;      // fill pass
+    int32_t* out_col;
+    double* out_val;
+    int* status;
+};
+
+// One thread per (neuron, pole): the two sweeps over the neuron's tree.
+__global__ void edge_pivots_kernel(const BuildArgs a) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= a.n_neuron * kPoles) return;
+    const int64_t j = t / kPoles;
+    const int k = (int)(t % kPoles);
+    const int64_t b = a.neuron_start[j], e = a.neuron_start[j + 1];
+    const cplx z = cplx(c_z[k].x, c_z[k].y);
+    double2* down = a.down + k * a.n_seg;
+    double2* up = a.up + k * a.n_seg;
+    double2* invT = a.invT + k * a.n_seg;
+    // M = zI - A^T: M_cc = z + h * gsum_c / C_c; M_pc * M_cp = a_pc * a_cp with
+    // a_pc = h/(R_c C_p), a_cp = h/(R_c C_c) for the edge of child c.
+    for (int64_t c = b; c < e; ++c) st(&down[c], z + cplx(a.h_s * a.gsum[c] / a.cap[c], 0.0));
+    for (int64_t c = e - 1; c >= b; --c) {
+        const int64_t p = a.parent[c];
+        if (p < 0) continue;
+        const double r = a.res[c];
+        const double prod = (a.h_s / (r * a.cap[p])) * (a.h_s / (r * a.cap[c]));
+        const cplx dc = ld(&down[c]);
+        st(&down[p], ld(&down[p]) - scale(prod, inv(dc)));
+    }
+    // Root-to-leaves: T_p (total pivot) is known before p's children.
+    for (int64_t c = b; c < e; ++c) {
+        const int64_t p = a.parent[c];
+        if (p < 0) {
+            st(&invT[c], inv(ld(&down[c])));
+            st(&up[c], cplx(0.0, 0.0));
+            continue;
+        }
+        const double r = a.res[c];
+        const double prod = (a.h_s / (r * a.cap[p])) * (a.h_s / (r * a.cap[c]));
+        const cplx dc = ld(&down[c]);
+        const cplx Tp = inv(ld(&invT[p]));
+        const cplx upc = Tp + scale(prod, inv(dc));
+        const cplx Tc = dc - scale(prod, inv(upc));
+        st(&up[c], upc);
+        st(&invT[c], inv(Tc));
+    }
+    // Store the step ratios in place of the pivots:
+    //   down[c] <- a_pc / down[c]  (parent -> child),  up[c] <- a_cp / up[c]  (child -> parent).
+    for (int64_t c = b; c < e; ++c) {
+        const int64_t p = a.parent[c];
+        if (p < 0) continue;
+        const double r = a.res[c];
+        st(&down[c], scale(a.h_s / (r * a.cap[p]), inv(ld(&down[c]))));
+        st(&up[c], scale(a.h_s / (r * a.cap[c]), inv(ld(&up[c]))));
+    }
+}
+
+// One warp per row; lanes 0..15 carry one pole each.  fill = 0 counts, 1 writes.
+// Both passes run this same code, so they take identical decisions; the fill
+// pass still checks that the row's entries land exactly in [rowptr[r], rowptr[r+1]).
+__global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a, const int fill) {
+    const int lane = threadIdx.x & 31;
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (row >= a.n_seg) return;
+    const bool act = lane < kPoles;
+    const int k = act ? lane : 0;
+    const int64_t ns = a.n_seg;
+    const cplx w = act ? cplx(c_w[k].x, c_w[k].y) : cplx(0.0, 0.0);
+    const double scale_out = 2.0 / kNodes;
+    int32_t st_node[kStackDepth], st_from[kStackDepth];
+    cplx st_y[kStackDepth];
+    int sp = 0;
+    int64_t cur = row, from = -1;
+    cplx y = ld(&a.invT[k * ns + row]);
+    int64_t kept = 0;
+    int64_t out = fill ? a.rowptr[row] : 0;
+    const int64_t out_end = fill ? a.rowptr[row + 1] : 0;
+    for (;;) {
+        cplx wy = w * y;
+        double v = act ? wy.im : 0.0;
+#pragma unroll
+        for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        v = __shfl_sync(0xffffffffu, v, 0) * scale_out;
+        if (fabs(v) >= a.tol) {
+            if (fill && lane == 0 && out < out_end) { a.out_col[out] = (int32_t)cur; a.out_val[out] = v; }
+            ++out;
+            ++kept;
+        }
+        int64_t next = -1;
+        cplx ynext;
+        if (fabs(v) >= a.explore) {
+            const int64_t p = a.parent[cur];
+            if (p >= 0 && p != from) {
+                next = p;
+                ynext = ld(&a.up[k * ns + cur]) * y;
+            }
+            for (int64_t q = a.child_ptr[cur]; q < a.child_ptr[cur + 1]; ++q) {
+                const int64_t c = a.child_idx[q];
+                if (c == from) continue;
+                const cplx yc = ld(&a.down[k * ns + c]) * y;
+                if (next < 0) { next = c; ynext = yc; continue; }
+                if (sp >= kStackDepth) {
+                    if (lane == 0) atomicOr(a.status, kStatusStackOverflow);
+                    goto done;
+                }
+                st_node[sp] = (int32_t)c; st_from[sp] = (int32_t)cur; st_y[sp] = yc; ++sp;
+            }
+        }
+        if (next >= 0) { from = cur; cur = next; y = ynext; continue; }
+        if (sp == 0) break;
+        --sp;
+        cur = st_node[sp]; from = st_from[sp]; y = st_y[sp];
+    }
+done:
+    if (!fill && lane == 0) a.count[row] = kept;
+    if (fill && lane == 0 && out != out_end) atomicOr(a.status, kStatusRowMismatch);
+}
+
+// ---------------------------------------------------------------- host
+
+static void contour_nodes(double2* z, double2* w) {
+    const double N = (double)kNodes;
+    int m = 0;
+    for (int k = 0; k < kNodes; ++k) {
+        const double th = -M_PI + (k + 0.5) * 2.0 * M_PI / N;
+        if (th <= 0) continue;
+        const double zr = N * (0.1309 - 0.1194 * th * th), zi = N * 0.25 * th;
+        const double dr = N * (-0.2388 * th), di = N * 0.25;
+        const double ez = std::exp(zr);
+        const double er = ez * std::cos(zi), ei = ez * std::sin(zi);
+        z[m] = make_double2(zr, zi);
+        w[m] = make_double2(er * dr - ei * di, er * di + ei * dr);
+        ++m;
+    }
+}
+
+int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
+    const int64_t n = ctx->n_seg, nn = ctx->n_neuron;
+    // Children lists and edge conductance sums (host, O(n)).
+    std::vector<int64_t> cptr(n + 1, 0), cidx;
+    for (int64_t i = 0; i < n; ++i) if (ctx->h_parent[i] >= 0) cptr[ctx->h_parent[i] + 1]++;
+    for (int64_t i = 0; i < n; ++i) cptr[i + 1] += cptr[i];
+    cidx.assign(std::max<int64_t>(cptr[n], 1), 0);
+    {
+        std::vector<int64_t> fillp(cptr.begin(), cptr.end() - 1);
+        for (int64_t i = 0; i < n; ++i) if (ctx->h_parent[i] >= 0) cidx[fillp[ctx->h_parent[i]]++] = i;
+    }
+    std::vector<double> res(n), gsum(n, 0.0);
+    NW_CUDA(ctx, cudaMemcpy(res.data(), ctx->res64.ptr, 8 * n, cudaMemcpyDeviceToHost));
+    for (int64_t c = 0; c < n; ++c) {
+        int64_t p = ctx->h_parent[c];
+        if (p < 0) continue;
+        gsum[c] += 1.0 / res[c];
+        gsum[p] += 1.0 / res[c];
+    }
+    double2 z[kPoles], w[kPoles];
+    contour_nodes(z, w);
+    NW_CUDA(ctx, cudaMemcpyToSymbol(c_z, z, sizeof(z)));
+    NW_CUDA(ctx, cudaMemcpyToSymbol(c_w, w, sizeof(w)));
+
+    DevBuf d_cptr, d_cidx, d_gsum, d_down, d_up, d_invT, d_count;
+    auto cleanup = [&]() {
+        dev_free(d_cptr); dev_free(d_cidx); dev_free(d_gsum); dev_free(d_down);
+        dev_free(d_up); dev_free(d_invT); dev_free(d_count);
+    };
+    int rc = NW_OK;
+    do {
+        if ((rc = dev_alloc(ctx, d_cptr, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_cidx, 8 * cidx.size())) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_gsum, 8 * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_down, sizeof(double2) * kPoles * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_up, sizeof(double2) * kPoles * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_invT, sizeof(double2) * kPoles * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_count, 8 * n)) != NW_OK) break;
+        cudaMemcpyAsync(d_cptr.ptr, cptr.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(d_cidx.ptr, cidx.data(), 8 * cidx.size(), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(d_gsum.ptr, gsum.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+        BuildArgs a{};
+        a.n_seg = n; a.n_neuron = nn;
+        a.neuron_start = ctx->neuron_start.as<int64_t>();
+        a.parent = ctx->parent.as<int64_t>();
+        a.child_ptr = d_cptr.as<int64_t>(); a.child_idx = d_cidx.as<int64_t>();
+        a.cap = ctx->cap64.as<double>(); a.res = ctx->res64.as<double>(); a.gsum = d_gsum.as<double>();
+        a.h_s = 0.5 * ctx->time_step * 1e-3;
+        a.down = d_down.as<double2>(); a.up = d_up.as<double2>(); a.invT = d_invT.as<double2>();
+        a.tol = tol; a.explore = tol * kExploreFactor;
+        a.count = d_count.as<int64_t>();
+        a.status = ctx->status.as<int>();
+        {
+            int64_t threads = 128, blocks = (nn * kPoles + threads - 1) / threads;
+            edge_pivots_kernel<<<(unsigned)blocks, (unsigned)threads, 0, ctx->stream>>>(a);
+        }
+        const int64_t rows_per_block = 8;
+        const int64_t rblocks = (n + rows_per_block - 1) / rows_per_block;
+        propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 0);
+        if (cudaGetLastError() != cudaSuccess) { rc = fail(ctx, NW_ERR_CUDA, "propagator build launch failed"); break; }
+        std::vector<int64_t> cnt(n);
+        int st = 0;
+        cudaMemcpyAsync(cnt.data(), d_count.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "propagator build (count pass)"); break; }
+        if (st & kStatusStackOverflow) {
+            cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+            rc = fail(ctx, NW_ERR_LIMIT, "propagator build: walk stack overflow (too many branch points within reach)");
+            break;
+        }
+        std::vector<int64_t> rowptr(n + 1, 0);
+        for (int64_t i = 0; i < n; ++i) rowptr[i + 1] = rowptr[i] + cnt[i];
+        const int64_t nnz = rowptr[n];
+        if ((rc = dev_alloc(ctx, ctx->p_rowptr, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->p_col, 4 * std::max<int64_t>(nnz, 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->p_val, 8 * std::max<int64_t>(nnz, 1))) != NW_OK) break;
+        cudaMemcpyAsync(ctx->p_rowptr.ptr, rowptr.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        a.rowptr = ctx->p_rowptr.as<int64_t>();
+        a.out_col = ctx->p_col.as<int32_t>();
+        a.out_val = ctx->p_val.as<double>();
+        propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 1);
+        cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "propagator build (fill pass)"); break; }
+        if (st & kStatusRowMismatch) {
+            cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+            rc = fail(ctx, NW_ERR_STATE, "propagator build: count and fill passes disagree");
+            break;
+        }
+        ctx->nnz64 = nnz;
+        if (nnz_out) *nnz_out = nnz;
+    } while (0);
+    cleanup();
+    return rc;
+}
+
+int propagator_from_host(nw_ctx* ctx, const int64_t* rowptr, const int64_t* col, const double* val,
+                         int64_t nnz) {
+    const int64_t n = ctx->n_seg;
+    NW_CHECK(dev_alloc(ctx, ctx->p_rowptr, 8 * (n + 1)));
+    NW_CHECK(dev_alloc(ctx, ctx->p_col, 4 * std::max<int64_t>(nnz, 1)));
+    NW_CHECK(dev_alloc(ctx, ctx->p_val, 8 * std::max<int64_t>(nnz, 1)));
+    std::vector<int32_t> c32(nnz);
+    for (int64_t e = 0; e < nnz; ++e) c32[e] = (int32_t)col[e];
+    NW_CUDA(ctx, cudaMemcpyAsync(ctx->p_rowptr.ptr, rowptr, 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+    if (nnz) {
+        NW_CUDA(ctx, cudaMemcpyAsync(ctx->p_col.ptr, c32.data(), 4 * nnz, cudaMemcpyHostToDevice, ctx->stream));
+        NW_CUDA(ctx, cudaMemcpyAsync(ctx->p_val.ptr, val, 8 * nnz, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->nnz64 = nnz;
+    return NW_OK;
+}
+
+// ------------------------------------------------- batched difference form
+
+__global__ void batched_count_kernel(int64_t n, const int64_t* prow, const int32_t* pcol, int64_t* cnt) {
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int64_t c = 0;
+    for (int64_t k = prow[r]; k < prow[r + 1]; ++k) c += (pcol[k] != (int32_t)r);
+    cnt[r] = (c + 3) & ~(int64_t)3;
+}
+
+template <typename real>
+__global__ void batched_fill_kernel(int64_t n, const int64_t* neuron_of_row_base, const int64_t* prow,
+                                    const int32_t* pcol, const double* pval, const int64_t* brow,
+                                    uint16_t* bcol, real* bval, real* leak) {
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (r >= n) return;
+    const int64_t base = neuron_of_row_base[r];
+    int64_t ob = brow[r];
+    double sum = 0.0;
+    for (int64_t k0 = prow[r]; k0 < prow[r + 1]; k0 += 32) {
+        const int64_t k = k0 + lane;
+        const bool valid = k < prow[r + 1];
+        const int32_t c = valid ? pcol[k] : -1;
+        const double v = valid ? pval[k] : 0.0;
+        sum += v;
+        const bool off = valid && c != (int32_t)r;
+        const unsigned mask = __ballot_sync(0xffffffffu, off);
+        const int pos = __popc(mask & ((1u << lane) - 1u));
+        if (off) { bcol[ob + pos] = (uint16_t)(c - base); bval[ob + pos] = (real)v; }
+        ob += __popc(mask);
+    }
+    for (int64_t k = ob + lane; k < brow[r + 1]; k += 32) { bcol[k] = 0; bval[k] = real(0); }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+    if (lane == 0) leak[r] = (real)(1.0 - sum);
+}
+
+int propagator_to_batched(nw_ctx* ctx) {
+    const int64_t n = ctx->n_seg;
+    DevBuf d_cnt, d_base;
+    NW_CHECK(dev_alloc(ctx, d_cnt, 8 * n));
+    int rc = dev_alloc(ctx, d_base, 8 * n);
+    if (rc != NW_OK) { dev_free(d_cnt); return rc; }
+    std::vector<int64_t> base(n);
+    for (int64_t j = 0; j < ctx->n_neuron; ++j)
+        for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) base[i] = ctx->h_neuron_start[j];
+    cudaMemcpyAsync(d_base.ptr, base.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+    batched_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+        n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), d_cnt.as<int64_t>());
+    std::vector<int64_t> cnt(n), brow(n + 1, 0);
+    cudaMemcpyAsync(cnt.data(), d_cnt.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { dev_free(d_cnt); dev_free(d_base); return cuda_fail(ctx, e, "batched count"); }
+    for (int64_t i = 0; i < n; ++i) brow[i + 1] = brow[i] + cnt[i];
+    const int64_t nb = brow[n];
+    size_t rs = (size_t)ctx->precision;
+    do {
+        if ((rc = dev_alloc(ctx, ctx->b_rowptr, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->b_col, 2 * std::max<int64_t>(nb, 4))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->b_val, rs * std::max<int64_t>(nb, 4))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->b_leak, rs * n)) != NW_OK) break;
+        cudaMemcpyAsync(ctx->b_rowptr.ptr, brow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        const unsigned blocks = (unsigned)((n * 32 + 255) / 256);
+        if (ctx->precision == NW_F64)
+            batched_fill_kernel<double><<<blocks, 256, 0, ctx->stream>>>(
+                n, d_base.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
+                ctx->p_val.as<double>(), ctx->b_rowptr.as<int64_t>(), ctx->b_col.as<uint16_t>(),
+                ctx->b_val.as<double>(), ctx->b_leak.as<double>());
+        else
+            batched_fill_kernel<float><<<blocks, 256, 0, ctx->stream>>>(
+                n, d_base.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
+                ctx->p_val.as<double>(), ctx->b_rowptr.as<int64_t>(), ctx->b_col.as<uint16_t>(),
+                ctx->b_val.as<float>(), ctx->b_leak.as<float>());
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "batched fill"); break; }
+        ctx->nnz_b = nb;
+    } while (0);
+    dev_free(d_cnt);
+    dev_free(d_base);
+    return rc;
+}
+
+}  // namespace nw

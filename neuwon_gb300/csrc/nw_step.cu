@@ -1,0 +1,508 @@
+// Time-step kernels of neuwon_gb300.
+//
+// One staggered step follows neuwon/rxd/rxd_model.py:63-80:
+//   species(dt/2) -> mechanisms(dt) -> species(dt/2) -> AP detector
+// where species(dt/2) (rxd_model.py:91-113) gathers every segment's
+// conductance / driving voltage / current, applies the exact exponential
+// membrane update of neuwon/rxd/neuron/electric.py:56-76 and multiplies by
+// the propagator.
+//
+// Batched path: a persistent kernel.  Each CTA takes whole neurons from a
+// work counter (largest first) and advances one neuron through all K steps
+// before taking the next, so the only synchronisation is __syncthreads():
+// the propagator is block-diagonal by neuron and nothing couples neurons.
+// The vector the propagator multiplies lives in shared memory; propagator
+// rows are streamed from HBM as (fp32 value, u16 neuron-relative column)
+// in 16-byte vectors, LPR lanes per row, with a compensated sum of
+//   V_i = x_i - leak_i * x_i + sum_{j != i} P_ij (x_j - x_i),
+// which equals sum_j P_ij x_j exactly when leak_i = 1 - sum_j P_ij.
+//
+// Plain path: the reference's GPU design (neuwon/database/compute.py:360-418):
+// per-neuron launches, one thread per row or per instance, 32 threads per
+// block, FP64 CSR with the diagonal.
+#include <algorithm>
+
+#include "nw_internal.cuh"
+
+namespace nw {
+
+template <typename real> __device__ __forceinline__ real d_exp(real x);
+template <> __device__ __forceinline__ float d_exp<float>(float x) { return expf(x); }
+template <> __device__ __forceinline__ double d_exp<double>(double x) { return exp(x); }
+template <typename real> __device__ __forceinline__ real d_expm1(real x);
+template <> __device__ __forceinline__ float d_expm1<float>(float x) { return expm1f(x); }
+template <> __device__ __forceinline__ double d_expm1<double>(double x) { return expm1(x); }
+
+// FUNCTION vtrap (nmodl_library/artificial/hh.mod:88-94).  x/(exp(x/y)-1) is
+// evaluated as x/expm1(x/y), the same quantity without cancellation.
+template <typename real>
+__device__ __forceinline__ real vtrap(real x, real y) {
+    real r = x / y;
+    if (fabs(r) < real(1e-6)) return y * (real(1) - r / real(2));
+    return x / d_expm1(r);
+}
+
+// rates(v) and the exact gate update x <- xinf + (x - xinf) exp(-dt/xtau)
+// (hh.mod:55-86, nmodl/solver.py:48-55); dtq10 = dt * q10, so
+// dt/xtau = dtq10 * (alpha + beta).
+template <typename real>
+__device__ __forceinline__ void hh_gates(real v, real dtq10, real& m, real& h, real& n) {
+    real a = real(0.1) * vtrap(-(v + real(40)), real(10));
+    real b = real(4) * d_exp(-(v + real(65)) / real(18));
+    real s = a + b, inf = a / s;
+    m = inf + (m - inf) * d_exp(-dtq10 * s);
+    a = real(0.07) * d_exp(-(v + real(65)) / real(20));
+    b = real(1) / (d_exp(-(v + real(35)) / real(10)) + real(1));
+    s = a + b; inf = a / s;
+    h = inf + (h - inf) * d_exp(-dtq10 * s);
+    a = real(0.01) * vtrap(-(v + real(55)), real(10));
+    b = real(0.125) * d_exp(-(v + real(65)) / real(80));
+    s = a + b; inf = a / s;
+    n = inf + (n - inf) * d_exp(-dtq10 * s);
+}
+
+template <typename real>
+struct StepArgs {
+    int64_t n_neuron;
+    const int64_t* neuron_start;
+    const int32_t* neuron_order;
+    int* work_counter;
+    int* status;
+    real* V; real* Vint;
+    const real* kI; const real* kG; const real* Inonspec; int has_nonspec;
+    // batched propagator
+    const int64_t* rowptr; const uint16_t* col; const real* val; const real* leak;
+    // plain propagator
+    const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
+    // hh
+    int hh_on, hh_identity;
+    const uint32_t* hh_seg_ptr; const int64_t* hh_neuron_ptr; const uint32_t* hh_seg;
+    real* gm; real* gh; real* gn; const real* cna; const real* ck; const real* cl;
+    real ena, ek, el, dtq10;
+    // clamps
+    const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
+    const int64_t* clamp_first; const int64_t* clamp_count;
+    // detectors
+    int has_det;
+    const uint32_t* det_seg; const real* det_thr;
+    uint8_t* ap_detected; uint8_t* ap_state; uint32_t* spike_count;
+    // probes
+    const int32_t* probe_neuron_ptr; const uint32_t* probe_seg; const uint32_t* probe_slot;
+    real* trace; int64_t n_probes; int64_t trace_row0;
+    // time
+    int64_t tick0; int k_steps; int g_valid; real h_s;
+};
+
+// Sum of a segment's mechanism conductances and conductance-weighted reversal
+// potentials (species.py:389-393 scatter, done here as a gather over the
+// segment's instances in registration order: deterministic, no atomics).
+template <typename real>
+__device__ __forceinline__ void segment_conductance(const StepArgs<real>& a, int64_t i, real& G, real& GE) {
+    G = real(0); GE = real(0);
+    if (!a.hh_on) return;
+    int64_t b, e;
+    if (a.hh_identity) { b = i; e = i + 1; }
+    else { b = a.hh_seg_ptr[i]; e = a.hh_seg_ptr[i + 1]; }
+    real gna = real(0), gk = real(0), gl = real(0);
+    for (int64_t k = b; k < e; ++k) {
+        real m = a.gm[k], h = a.gh[k], n = a.gn[k];
+        gna += a.cna[k] * m * m * m * h;
+        gk += a.ck[k] * n * n * n * n;
+        gl += a.cl[k];
+    }
+    G = (gna + gk) + gl;
+    GE = (gna * a.ena + gk * a.ek) + gl * a.el;
+}
+
+// Exact exponential membrane update of one segment (electric.py:60-76).
+template <typename real>
+__device__ __forceinline__ real membrane_x(const StepArgs<real>& a, int64_t i, real G, real GE, real I,
+                                           bool store_integral) {
+    real v = a.V[i];
+    real E = (G != real(0)) ? GE / G : real(0);          // nan_to_num(GE/G), rxd_model.py:106-109
+    real expo = -a.kG[i] * G;
+    real alpha = d_exp(expo);
+    real dv = a.kI[i] * I;
+    real diff = E - v;
+    real x = E - diff * alpha + dv;
+    if (store_integral) a.Vint[i] = a.h_s * E - expo * diff * alpha + real(0.5) * a.h_s * dv;
+    return x;
+}
+
+template <typename real> struct Vec4Loader;
+template <> struct Vec4Loader<float> {
+    static __device__ __forceinline__ void load(const float* p, float (&v)[4]) {
+        float4 q = __ldg(reinterpret_cast<const float4*>(p));
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+};
+template <> struct Vec4Loader<double> {
+    static __device__ __forceinline__ void load(const double* p, double (&v)[4]) {
+        double2 q0 = __ldg(reinterpret_cast<const double2*>(p));
+        double2 q1 = __ldg(reinterpret_cast<const double2*>(p) + 1);
+        v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+    }
+};
+
+template <typename real>
+__device__ __forceinline__ void kahan_add(real& s, real& c, real term) {
+    real y = term - c;
+    real t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// V_i <- propagator row i applied to xs, for every row of one neuron.
+template <typename real, int LPR>
+__device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_t base, int n,
+                                                 const real* __restrict__ xs) {
+    constexpr int GPW = 32 / LPR;                  // row groups per warp
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int q = lane / LPR, l = lane % LPR;
+    for (int rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int row = rb + q;
+        const bool valid = row < n;
+        real s = real(0), c = real(0), xi = real(0);
+        if (valid) {
+            const int64_t r = base + row;
+            const int64_t beg = a.rowptr[r], end = a.rowptr[r + 1];
+            xi = xs[row];
+            for (int64_t k = beg + 4 * l; k < end; k += 4 * LPR) {
+                real v[4];
+                Vec4Loader<real>::load(a.val + k, v);
+                const ushort4 cc = __ldg(reinterpret_cast<const ushort4*>(a.col + k));
+                kahan_add(s, c, v[0] * (xs[cc.x] - xi));
+                kahan_add(s, c, v[1] * (xs[cc.y] - xi));
+                kahan_add(s, c, v[2] * (xs[cc.z] - xi));
+                kahan_add(s, c, v[3] * (xs[cc.w] - xi));
+            }
+        }
+        real t = s - c;
+#pragma unroll
+        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        if (valid && l == 0) {
+            const int64_t r = base + row;
+            const real vnew = (xi - a.leak[r] * xi) + t;
+            if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
+            a.V[r] = vnew;
+        }
+    }
+}
+
+template <typename real, int LPR>
+__global__ void __launch_bounds__(1024)
+batched_advance_kernel(const StepArgs<real> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    real* xs = reinterpret_cast<real*>(smem_raw);
+    __shared__ int s_job;
+    __shared__ int s_nclamp;
+    __shared__ uint32_t s_cseg[kMaxClampsPerNeuron];
+    __shared__ real s_camp[kMaxClampsPerNeuron];
+    __shared__ int64_t s_cfirst[kMaxClampsPerNeuron], s_cend[kMaxClampsPerNeuron];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+
+    for (;;) {
+        if (tid == 0) s_job = atomicAdd(a.work_counter, 1);
+        __syncthreads();
+        const int job = s_job;
+        if (job >= a.n_neuron) break;
+        const int j = a.neuron_order[job];
+        const int64_t base = a.neuron_start[j];
+        const int n = (int)(a.neuron_start[j + 1] - base);
+        if (tid == 0) {
+            int c0 = a.clamp_neuron_ptr ? a.clamp_neuron_ptr[j] : 0;
+            int c1 = a.clamp_neuron_ptr ? a.clamp_neuron_ptr[j + 1] : 0;
+            s_nclamp = c1 - c0;
+            for (int c = 0; c < c1 - c0; ++c) {
+                s_cseg[c] = a.clamp_seg[c0 + c];
+                s_camp[c] = a.clamp_amp[c0 + c];
+                s_cfirst[c] = a.clamp_first[c0 + c];
+                s_cend[c] = a.clamp_first[c0 + c] + a.clamp_count[c0 + c];
+            }
+        }
+        __syncthreads();
+        const int nclamp = s_nclamp;
+        // Mechanism instance range of this neuron.
+        int64_t ib = 0, ie = 0;
+        if (a.hh_on) {
+            if (a.hh_identity) { ib = base; ie = base + n; }
+            else { ib = a.hh_neuron_ptr[j]; ie = a.hh_neuron_ptr[j + 1]; }
+        }
+        // AP detector state lives in thread 0's registers across the K steps.
+        bool ap_state = false, ap_det = false;
+        uint32_t spikes = 0;
+        if (tid == 0 && a.has_det) {
+            ap_state = a.ap_state[j] != 0;
+            ap_det = a.ap_detected[j] != 0;
+            spikes = a.spike_count[j];
+        }
+        int pb = 0, pe = 0;
+        if (a.n_probes) { pb = a.probe_neuron_ptr[j]; pe = a.probe_neuron_ptr[j + 1]; }
+
+        for (int s = 0; s < a.k_steps; ++s) {
+#pragma unroll 1
+            for (int half = 0; half < 2; ++half) {
+                const int64_t tick = a.tick0 + 2 * s + half + 1;
+                const bool gv = (s > 0) || (half > 0) || a.g_valid;
+                const bool last = (s == a.k_steps - 1) && (half == 1);
+                for (int li = tid; li < n; li += nthr) {
+                    const int64_t i = base + li;
+                    real G, GE;
+                    if (gv) segment_conductance(a, i, G, GE);
+                    else { G = real(0); GE = real(0); }
+                    real I = a.has_nonspec ? a.Inonspec[i] : real(0);
+                    for (int c = 0; c < nclamp; ++c)
+                        if (s_cseg[c] == (uint32_t)i && tick >= s_cfirst[c] && tick < s_cend[c]) I += s_camp[c];
+                    xs[li] = membrane_x(a, i, G, GE, I, last);
+                }
+                __syncthreads();
+                propagate_neuron<real, LPR>(a, base, n, xs);
+                __syncthreads();
+                if (half == 0) {
+                    // Mechanisms (rxd_model.py:115-123) at the mid-step voltage.
+                    if (a.hh_on) {
+                        for (int64_t k = ib + tid; k < ie; k += nthr) {
+                            const real v = a.V[a.hh_identity ? k : (int64_t)a.hh_seg[k]];
+                            real m = a.gm[k], h = a.gh[k], nn = a.gn[k];
+                            hh_gates(v, a.dtq10, m, h, nn);
+                            a.gm[k] = m; a.gh[k] = h; a.gn[k] = nn;
+                        }
+                    }
+                    if (!a.hh_identity) __syncthreads();
+                }
+            }
+            // AP detector (neuron.py:184-188) and probes after the full step.
+            if (tid == 0 && a.has_det) {
+                const bool over = a.V[a.det_seg[j]] >= a.det_thr[j];
+                ap_det = over && !ap_state;
+                ap_state = over;
+                spikes += ap_det ? 1u : 0u;
+            }
+            for (int p = pb + tid; p < pe; p += nthr)
+                a.trace[(a.trace_row0 + s) * a.n_probes + a.probe_slot[p]] = a.V[a.probe_seg[p]];
+        }
+        if (tid == 0 && a.has_det) {
+            a.ap_state[j] = ap_state;
+            a.ap_detected[j] = ap_det;
+            a.spike_count[j] = spikes;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ plain path
+
+template <typename real>
+__global__ void plain_prepare_kernel(const StepArgs<real> a, int j, int64_t base, int n, int64_t tick,
+                                     int gv, int last) {
+    int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n) return;
+    int64_t i = base + li;
+    real G, GE;
+    if (gv) segment_conductance(a, i, G, GE);
+    else { G = real(0); GE = real(0); }
+    real I = a.has_nonspec ? a.Inonspec[i] : real(0);
+    if (a.clamp_neuron_ptr) {
+        for (int c = a.clamp_neuron_ptr[j]; c < a.clamp_neuron_ptr[j + 1]; ++c)
+            if (a.clamp_seg[c] == (uint32_t)i && tick >= a.clamp_first[c] && tick < a.clamp_first[c] + a.clamp_count[c])
+                I += a.clamp_amp[c];
+    }
+    a.px[i] = membrane_x(a, i, G, GE, I, last != 0);
+}
+
+template <typename real>
+__global__ void plain_spmv_kernel(const StepArgs<real> a, int64_t base, int n) {
+    int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n) return;
+    int64_t r = base + li;
+    double acc = 0.0;
+    for (int64_t k = a.prow[r]; k < a.prow[r + 1]; ++k) acc += a.pval[k] * (double)a.px[a.pcol[k]];
+    if (!isfinite(acc)) atomicOr(a.status, kStatusNonFinite);
+    a.V[r] = (real)acc;
+}
+
+template <typename real>
+__global__ void plain_hh_kernel(const StepArgs<real> a, int64_t ib, int64_t ie) {
+    int64_t k = ib + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= ie) return;
+    const real v = a.V[a.hh_identity ? k : (int64_t)a.hh_seg[k]];
+    real m = a.gm[k], h = a.gh[k], nn = a.gn[k];
+    hh_gates(v, a.dtq10, m, h, nn);
+    a.gm[k] = m; a.gh[k] = h; a.gn[k] = nn;
+}
+
+template <typename real>
+__global__ void plain_detect_kernel(const StepArgs<real> a, int64_t row) {
+    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j < a.n_neuron && a.has_det) {
+        const bool over = a.V[a.det_seg[j]] >= a.det_thr[j];
+        const bool det = over && !a.ap_state[j];
+        a.ap_detected[j] = det;
+        a.ap_state[j] = over;
+        a.spike_count[j] += det ? 1u : 0u;
+    }
+    if (j < a.n_probes && a.n_probes) {
+        // probe_seg/probe_slot are neuron-sorted; every probe is written once.
+        a.trace[row * a.n_probes + a.probe_slot[j]] = a.V[a.probe_seg[j]];
+    }
+}
+
+// ------------------------------------------------------------ host side
+
+template <typename real>
+static StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
+    StepArgs<real> a{};
+    a.n_neuron = ctx->n_neuron;
+    a.neuron_start = ctx->neuron_start.as<int64_t>();
+    a.neuron_order = ctx->neuron_order.as<int32_t>();
+    a.work_counter = ctx->work_counter.as<int>();
+    a.status = ctx->status.as<int>();
+    a.V = ctx->V.as<real>(); a.Vint = ctx->Vint.as<real>();
+    a.kI = ctx->kI.as<real>(); a.kG = ctx->kG.as<real>();
+    a.Inonspec = ctx->Inonspec.as<real>(); a.has_nonspec = ctx->nonspec_nonzero ? 1 : 0;
+    a.rowptr = ctx->b_rowptr.as<int64_t>(); a.col = ctx->b_col.as<uint16_t>();
+    a.val = ctx->b_val.as<real>(); a.leak = ctx->b_leak.as<real>();
+    a.prow = ctx->p_rowptr.as<int64_t>(); a.pcol = ctx->p_col.as<int32_t>(); a.pval = ctx->p_val.as<double>();
+    a.px = ctx->plain_x.as<real>();
+    const HHState& hh = ctx->hh;
+    a.hh_on = hh.m > 0 ? 1 : 0;
+    a.hh_identity = hh.identity ? 1 : 0;
+    a.hh_seg_ptr = hh.seg_ptr.as<uint32_t>(); a.hh_neuron_ptr = hh.neuron_ptr.as<int64_t>();
+    a.hh_seg = hh.seg.as<uint32_t>();
+    a.gm = hh.gm.as<real>(); a.gh = hh.gh.as<real>(); a.gn = hh.gn.as<real>();
+    a.cna = hh.cna.as<real>(); a.ck = hh.ck.as<real>(); a.cl = hh.cl.as<real>();
+    a.ena = (real)hh.ena; a.ek = (real)hh.ek; a.el = (real)hh.el;
+    const double q10 = pow(3.0, (ctx->celsius - 6.3) / 10.0);      // hh.mod:67
+    a.dtq10 = (real)(ctx->time_step * q10);
+    if (ctx->n_clamps) {
+        a.clamp_neuron_ptr = ctx->clamp_neuron_ptr.as<int32_t>();
+        a.clamp_seg = ctx->clamp_seg.as<uint32_t>(); a.clamp_amp = ctx->clamp_amp.as<real>();
+        a.clamp_first = ctx->clamp_first.as<int64_t>(); a.clamp_count = ctx->clamp_count.as<int64_t>();
+    }
+    a.has_det = ctx->have_detectors ? 1 : 0;
+    a.det_seg = ctx->det_seg.as<uint32_t>(); a.det_thr = ctx->det_thr.as<real>();
+    a.ap_detected = ctx->ap_detected.as<uint8_t>(); a.ap_state = ctx->ap_state.as<uint8_t>();
+    a.spike_count = ctx->spike_count.as<uint32_t>();
+    a.n_probes = ctx->n_probes;
+    if (ctx->n_probes) {
+        a.probe_neuron_ptr = ctx->probe_neuron_ptr.as<int32_t>();
+        a.probe_seg = ctx->probe_seg.as<uint32_t>(); a.probe_slot = ctx->probe_slot.as<uint32_t>();
+        a.trace = ctx->trace.as<real>(); a.trace_row0 = ctx->probe_len;
+    }
+    a.tick0 = ctx->input_ticks;
+    a.k_steps = k_steps;
+    a.g_valid = ctx->g_valid ? 1 : 0;
+    a.h_s = (real)(0.5 * ctx->time_step * 1e-3);
+    return a;
+}
+
+int choose_lanes_per_row(nw_ctx* ctx) {
+    if (ctx->lanes_per_row) return ctx->lanes_per_row;
+    double avg = ctx->n_seg ? (double)ctx->nnz_b / (double)ctx->n_seg : 0.0;
+    if (avg >= 96) return 32;
+    if (avg >= 48) return 16;
+    if (avg >= 20) return 8;
+    return 4;
+}
+
+template <typename real, int LPR>
+static int launch_batched_lpr(nw_ctx* ctx, const StepArgs<real>& a) {
+    auto kern = batched_advance_kernel<real, LPR>;
+    size_t smem = (size_t)ctx->max_neuron * sizeof(real);
+    smem = (smem + 15) & ~(size_t)15;
+    size_t static_smem = 4096;
+    if (smem + static_smem > ctx->smem_optin)
+        return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron of " + std::to_string(ctx->max_neuron) +
+                                       " segments does not fit in shared memory at this precision");
+    NW_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int threads = ctx->threads;
+    int occ = 0;
+    NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem));
+    if (occ < 1) return fail(ctx, NW_ERR_LIMIT, "batched path: kernel does not fit on an SM");
+    int per_sm = ctx->ctas_per_sm ? std::min(ctx->ctas_per_sm, occ) : occ;
+    int64_t grid = std::min<int64_t>(ctx->n_neuron, (int64_t)per_sm * ctx->num_sms);
+    NW_CUDA(ctx, cudaMemsetAsync(ctx->work_counter.ptr, 0, sizeof(int), ctx->stream));
+    kern<<<(unsigned)grid, threads, smem, ctx->stream>>>(a);
+    NW_CUDA(ctx, cudaGetLastError());
+    return NW_OK;
+}
+
+template <typename real>
+static int launch_batched(nw_ctx* ctx, int k_steps) {
+    StepArgs<real> a = make_args<real>(ctx, k_steps);
+    switch (choose_lanes_per_row(ctx)) {
+        case 4: return launch_batched_lpr<real, 4>(ctx, a);
+        case 8: return launch_batched_lpr<real, 8>(ctx, a);
+        case 16: return launch_batched_lpr<real, 16>(ctx, a);
+        default: return launch_batched_lpr<real, 32>(ctx, a);
+    }
+}
+
+static void finish_steps(nw_ctx* ctx, int k_steps) {
+    ctx->input_ticks += 2 * (int64_t)k_steps;
+    ctx->steps += k_steps;
+    if (ctx->n_probes) ctx->probe_len += k_steps;
+    if (ctx->hh.m > 0) ctx->g_valid = true;
+}
+
+int advance_batched(nw_ctx* ctx, int k_steps) {
+    int rc = ctx->precision == NW_F64 ? launch_batched<double>(ctx, k_steps)
+                                      : launch_batched<float>(ctx, k_steps);
+    if (rc != NW_OK) return rc;
+    finish_steps(ctx, k_steps);
+    return NW_OK;
+}
+
+template <typename real>
+static int plain_steps(nw_ctx* ctx, int k_steps) {
+    constexpr int T = 32;   // compute.py:368: 32 threads per block
+    for (int s = 0; s < k_steps; ++s) {
+        StepArgs<real> a = make_args<real>(ctx, 1);
+        for (int half = 0; half < 2; ++half) {
+            const int64_t tick = ctx->input_ticks + half + 1;
+            const int gv = (half > 0 || ctx->g_valid) ? 1 : 0;
+            const int last = half == 1;
+            for (int64_t j = 0; j < ctx->n_neuron; ++j) {
+                int64_t base = ctx->h_neuron_start[j];
+                int n = (int)(ctx->h_neuron_start[j + 1] - base);
+                int blocks = (n + T - 1) / T;
+                plain_prepare_kernel<real><<<blocks, T, 0, ctx->stream>>>(a, (int)j, base, n, tick, gv, last);
+                plain_spmv_kernel<real><<<blocks, T, 0, ctx->stream>>>(a, base, n);
+            }
+            if (half == 0 && ctx->hh.m > 0) {
+                std::vector<int64_t> nptr(ctx->n_neuron + 1);
+                // Instance ranges per neuron (identity: the neuron's segments).
+                for (int64_t j = 0; j < ctx->n_neuron; ++j) {
+                    int64_t ib, ie;
+                    if (ctx->hh.identity) { ib = ctx->h_neuron_start[j]; ie = ctx->h_neuron_start[j + 1]; }
+                    else {
+                        // Whole range in one launch when instances are not segment-aligned.
+                        if (j > 0) break;
+                        ib = 0; ie = ctx->hh.m;
+                    }
+                    if (ie > ib) {
+                        int64_t blocks = (ie - ib + T - 1) / T;
+                        plain_hh_kernel<real><<<(unsigned)blocks, T, 0, ctx->stream>>>(a, ib, ie);
+                    }
+                }
+            }
+            ctx->g_valid = ctx->g_valid || ctx->hh.m > 0;
+        }
+        int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
+        StepArgs<real> d = make_args<real>(ctx, 1);
+        plain_detect_kernel<real><<<(unsigned)((cover + 127) / 128), 128, 0, ctx->stream>>>(d, ctx->probe_len);
+        NW_CUDA(ctx, cudaGetLastError());
+        ctx->input_ticks += 2;
+        ctx->steps += 1;
+        if (ctx->n_probes) ctx->probe_len += 1;
+    }
+    return NW_OK;
+}
+
+int advance_plain(nw_ctx* ctx, int k_steps) {
+    return ctx->precision == NW_F64 ? plain_steps<double>(ctx, k_steps) : plain_steps<float>(ctx, k_steps);
+}
+
+}  // namespace nw

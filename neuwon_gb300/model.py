@@ -1,0 +1,666 @@
+"""Host-side mirror of the reference's model API around the GPU step.
+
+``RxD_Model`` keeps the reference's public surface for the hot path
+(neuwon/rxd/rxd_model.py:9-80): the constructor arguments, ``Neuron`` and
+``Segment`` factories (neuwon/rxd/neuron/neuron.py:148-156,
+segment.py:27-104), mechanism insertion (segment.py:124-160,
+mechanisms.py:56-99), ``Segment.inject_current`` (electric.py:119-125),
+AP detectors (neuron.py:178-188), the clocks (database/time.py:54-121) and
+``TimeSeries.record`` of voltages (time.py:189-231).
+
+The segment table is a structure of arrays in creation order.  Before the
+first ``advance()`` (and again after any structural change) it is sorted by
+neuron the way ``Database.sort()`` does (stable, database.py:589-646), its
+geometry and passive properties are computed (morphology.geometry), and
+everything is mirrored on the device; the propagator is then built on the
+GPU.  After that ``advance()`` is a single C-ABI call.
+"""
+import math
+
+import numpy as np
+
+from . import _lib
+from .morphology import EPSILON, Tree, geometry, passive_electric
+from .mechanisms import HH, Mechanism
+
+
+class Clock:
+    """Tick counter; neuwon/database/time.py:54-121."""
+
+    def __init__(self, tick_period, units=""):
+        self.dt = self.time_step = self.tick_period = float(tick_period)
+        self.ticks = 0
+        self.units = str(units)
+        self._callbacks = []
+
+    def get_time(self):
+        return self.ticks * self.dt
+
+    def __call__(self):
+        return self.get_time()
+
+    def get_ticks(self):
+        return self.ticks
+
+    def get_time_step(self):
+        return self.dt
+
+    def get_units(self):
+        return self.units
+
+    def is_now(self, time):
+        return round(float(time) / self.dt) == self.ticks
+
+    def register_callback(self, function):
+        self._callbacks.append(function)
+
+    def _tick(self, n=1):
+        self.ticks += n
+        if self._callbacks:
+            self._callbacks = [f for f in self._callbacks if not f()]
+
+
+class Segment:
+    """Handle of one segment (a row of the segment table)."""
+    __slots__ = ("_model", "_idx")
+
+    def __init__(self, model, idx):
+        self._model = model
+        self._idx = int(idx)
+
+    def __eq__(self, other):
+        return isinstance(other, Segment) and other._model is self._model and other._idx == self._idx
+
+    def __hash__(self):
+        return hash((id(self._model), self._idx))
+
+    def __repr__(self):
+        return f"<Segment {self._idx}>"
+
+    def get_unstable_index(self):
+        return self._idx
+
+    @property
+    def parent(self):
+        p = self._model._parent_of(self._idx)
+        return None if p < 0 else Segment(self._model, p)
+
+    @property
+    def children(self):
+        return [Segment(self._model, c) for c in self._model._children_of(self._idx)]
+
+    @property
+    def neuron(self):
+        return self._model._neuron_handle(self._model._seg_neuron[self._idx])
+
+    @property
+    def coordinates(self):
+        return self._model._coords[self._idx].copy()
+
+    @property
+    def diameter(self):
+        return float(self._model._diam[self._idx])
+
+    def is_root(self):
+        return self._model._parent_of(self._idx) < 0
+
+    is_sphere = is_root
+
+    def is_cylinder(self):
+        return not self.is_root()
+
+    def _geom(self, name):
+        return float(self._model._geometry()[name][self._idx])
+
+    length = property(lambda self: self._geom("length"))
+    surface_area = property(lambda self: self._geom("surface_area"))
+    cross_sectional_area = property(lambda self: self._geom("cross_sectional_area"))
+    volume = property(lambda self: self._geom("volume"))
+    axial_resistance = property(lambda self: self._geom("axial_resistance"))
+    capacitance = property(lambda self: self._geom("capacitance"))
+
+    @property
+    def voltage(self):
+        return float(self._model._get_segment_values("Segment.voltage")[self._idx])
+
+    @voltage.setter
+    def voltage(self, value):
+        self._model._set_segment_value("Segment.voltage", self._idx, float(value))
+
+    def add_segment(self, coordinates, diameter, segment_type=None):
+        return self._model.Segment(self, coordinates, diameter)
+
+    def add_section(self, coordinates, diameter, maximum_segment_length=np.inf, segment_type=None):
+        """segment.py:75-104: a straight section split into equal segments."""
+        maximum_segment_length = float(maximum_segment_length)
+        assert maximum_segment_length > 0
+        coordinates = [float(x) for x in coordinates]
+        diameter = float(diameter)
+        displace = np.subtract(self.coordinates, coordinates)
+        length = np.linalg.norm(displace)
+        p_coords = np.array(self.coordinates)
+        if self.is_sphere() or len(self.children) > 0:
+            self_r = 0.5 * self.diameter
+            if self_r < length - EPSILON:
+                p_coords -= displace * (self_r / length)
+                length -= self_r
+        divisions = max(1, int(np.ceil(length / maximum_segment_length)))
+        x = np.linspace(p_coords[0], coordinates[0], divisions + 1)
+        y = np.linspace(p_coords[1], coordinates[1], divisions + 1)
+        z = np.linspace(p_coords[2], coordinates[2], divisions + 1)
+        d = np.linspace(self.diameter, diameter, divisions + 1)
+        section, cur = [], self
+        for (xx, yy, zz, dd) in list(zip(x, y, z, d))[1:]:
+            cur = cur.add_segment((xx, yy, zz), dd)
+            section.append(cur)
+        return section
+
+    def insert(self, mechanisms, outside=None):
+        """segment.py:124-160."""
+        if isinstance(mechanisms, dict):
+            pass
+        elif isinstance(mechanisms, str):
+            mechanisms = {mechanisms: 1.0}
+        else:
+            mechanisms = {name: 1.0 for name in mechanisms}
+        out = {}
+        for name, magnitude in mechanisms.items():
+            out[name] = self._model.mechanisms[name](self, outside, float(magnitude))
+        return out
+
+    def inject_current(self, current=1.0, duration=1.0):
+        """electric.py:119-125: constant current (nA) for duration (ms), on the
+        half-step input clock, starting with the next input tick."""
+        current = float(current) * 1e-9
+        duration = float(duration)
+        assert duration >= 0
+        count = math.ceil(duration / self._model.input_hook.dt)
+        self._model._add_clamp(self._idx, current, self._model.input_hook.ticks + 1, count)
+
+    def get_time_constant(self):
+        raise NotImplementedError("sum_conductance is not kept on the device between steps")
+
+
+class Neuron:
+    """Handle of one neuron."""
+    __slots__ = ("_model", "_nid")
+
+    def __init__(self, model, nid):
+        self._model = model
+        self._nid = int(nid)
+
+    def __eq__(self, other):
+        return isinstance(other, Neuron) and other._model is self._model and other._nid == self._nid
+
+    def __hash__(self):
+        return hash((id(self._model), self._nid, "neuron"))
+
+    @property
+    def root(self):
+        return Segment(self._model, self._model._neuron_root[self._nid])
+
+    def set_AP_detector(self, segment=None, threshold=None):
+        m = self._model
+        if segment is not None:
+            m._det_seg[self._nid] = segment._idx
+        if threshold is not None:
+            m._det_thr[self._nid] = float(threshold)
+        m._dirty_detectors = True
+
+    @property
+    def AP_detected(self):
+        return bool(self._model._get_neuron_values("Neuron.AP_detected")[self._nid])
+
+    @property
+    def spike_count(self):
+        return int(self._model._get_neuron_values("Neuron.spike_count")[self._nid])
+
+
+class TimeSeries:
+    """Voltage recorder; the record half of neuwon/database/time.py:123-231."""
+
+    def __init__(self):
+        self._model = None
+        self.data = []
+        self.timestamps = []
+
+    def record(self, segment, component="voltage", immediate=True):
+        if component != "voltage":
+            raise NotImplementedError("device probes record Segment.voltage only")
+        self._model = segment._model
+        self._model._add_probe(self, segment._idx, immediate)
+        return self
+
+    def stop(self):
+        if self._model is not None:
+            self._model._remove_probe(self)
+        return self
+
+    def get_data(self):
+        if self._model is not None:
+            self._model._flush_probes()
+        return self.data
+
+    def get_timestamps(self):
+        if self._model is not None:
+            self._model._flush_probes()
+        return self.timestamps
+
+    def __len__(self):
+        return len(self.get_data())
+
+
+class RxD_Model:
+    """GPU-backed model with the reference's RxD_Model interface (rxd_model.py:9-80).
+
+    Extra keyword arguments (not in the reference):
+      precision             'f32' (default) or 'f64' state and step arithmetic
+      device                CUDA device ordinal
+      propagator_tolerance  prune |P_ij| below this (reference: machine epsilon)
+      path                  'batched' (fused persistent kernel) or 'plain'
+    """
+
+    def __init__(self, time_step=0.1, *, temperature=37, initial_voltage=-70,
+                 cytoplasmic_resistance=100, membrane_capacitance=1,
+                 extracellular_tortuosity=1.55, extracellular_max_distance=20e-6,
+                 species=(), mechanisms=(), precision="f32", device=0,
+                 propagator_tolerance=EPSILON, path="batched"):
+        if species:
+            raise NotImplementedError("species beyond the mechanisms' nonspecific conductances "
+                                      "are not on the GPU path")
+        self.time_step = float(time_step)
+        self.temperature = float(temperature)
+        self.initial_voltage = float(initial_voltage)
+        self.cytoplasmic_resistance = float(cytoplasmic_resistance)
+        self.membrane_capacitance = float(membrane_capacitance)
+        self.precision = precision
+        self.device = int(device)
+        self.propagator_tolerance = float(propagator_tolerance)
+        self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN}[path]
+        self.input_hook = Clock(0.5 * self.time_step, units="ms")
+        self.advance_hook = self.clock = Clock(self.time_step, units="ms")
+        # Segment table (creation order).
+        self._n = 0
+        self._parent = np.empty(0, np.int64)
+        self._coords = np.empty((0, 3))
+        self._diam = np.empty(0)
+        self._seg_neuron = np.empty(0, np.int64)
+        self._neuron_root = []
+        self._det_seg, self._det_thr = [], []
+        # Mechanisms.
+        self.mechanisms = {}
+        self._mech_instances = {}
+        for m in mechanisms:
+            self._load_mechanism(m)
+        self._clamps = []
+        self._probes = []
+        self._ctx = None
+        self._order = None
+        self._geom_cache = None
+        self._dirty_structure = True
+        self._dirty_clamps = True
+        self._dirty_detectors = True
+        self._dirty_probes = True
+        self._pending = {}
+
+    # ------------------------------------------------------ reference API
+    def get_time_step(self):
+        return self.time_step
+
+    def get_temperature(self):
+        return self.temperature
+
+    def get_clock(self):
+        return self.clock
+
+    def get_mechanisms(self):
+        return dict(self.mechanisms)
+
+    def register_advance_callback(self, function):
+        self.advance_hook.register_callback(function)
+
+    def Neuron(self, coordinates, diameter, *, neuron_type=None, segment_type=None):
+        nid = len(self._neuron_root)
+        root = self._append(-1, coordinates, diameter, nid)
+        self._neuron_root.append(root)
+        self._det_seg.append(root)
+        self._det_thr.append(20.0)
+        return Neuron(self, nid)
+
+    def Segment(self, parent, coordinates, diameter, *, segment_type=None):
+        if parent is None:
+            return self.Neuron(coordinates, diameter).root
+        nid = int(self._seg_neuron[parent._idx])
+        return Segment(self, self._append(parent._idx, coordinates, diameter, nid))
+
+    def add_tree(self, tree):
+        """Bulk-create one neuron from a ``morphology.Tree``; returns the Neuron."""
+        nid = len(self._neuron_root)
+        base = self._n
+        par = np.where(tree.parent < 0, -1, tree.parent + base)
+        self._grow(len(tree))
+        sl = slice(base, base + len(tree))
+        self._parent[sl] = par
+        self._coords[sl] = tree.coordinates
+        self._diam[sl] = tree.diameter
+        self._seg_neuron[sl] = nid
+        self._n += len(tree)
+        self._neuron_root.append(base)
+        self._det_seg.append(base)
+        self._det_thr.append(20.0)
+        self._dirty_structure = True
+        return Neuron(self, nid)
+
+    def insert_everywhere(self, name, magnitude=1.0, **per_instance):
+        """Insert mechanism ``name`` on every segment (one vectorised call)."""
+        cls = self.mechanisms[name]
+        segs = np.arange(self._n, dtype=np.int64)
+        self._add_instances_bulk(cls, segs, np.full(self._n, float(magnitude)), per_instance)
+
+    def advance(self, k_steps=1):
+        """rxd_model.py:63-80, k_steps times, as one device launch."""
+        self._sync()
+        k = int(k_steps)
+        if self._probes:
+            self._ensure_probe_room(k)
+        self._ctx.advance(k, self.path)
+        self.input_hook.ticks += 2 * k
+        self.advance_hook._tick(k)
+
+    def check(self):
+        v = self.get_data("Segment.voltage")
+        assert np.all(np.isfinite(v)), "non-finite voltage"
+
+    def get_data(self, name):
+        """Whole-attribute read in creation order ('Segment.voltage', 'hh.m', ...)."""
+        if name.startswith("Segment."):
+            return self._get_segment_values(name).copy()
+        if name.startswith("Neuron."):
+            return self._get_neuron_values(name).copy()
+        mech, attr = name.split(".")
+        self._sync()
+        cls = self.mechanisms[mech]
+        n = self._instance_count(cls.get_name())
+        return self._ctx.get_data(f"hh.{attr}", n)
+
+    def close(self):
+        if self._ctx is not None:
+            self._ctx.close()
+            self._ctx = None
+
+    # ------------------------------------------------------ internals
+    def _load_mechanism(self, mechanism):
+        if isinstance(mechanism, str):
+            from .mechanisms import NMODL
+            mechanism = NMODL(mechanism)
+        if not (isinstance(mechanism, type) and issubclass(mechanism, Mechanism)):
+            raise TypeError(f"not a Mechanism subclass: {mechanism!r}")
+        bound = mechanism.initialize(self) or mechanism
+        if not issubclass(bound, HH):
+            raise NotImplementedError(f"mechanism {bound.get_name()} has no GPU kernel")
+        name = bound.get_name()
+        if name in self.mechanisms:
+            raise ValueError(f"duplicate mechanism {name}")
+        if any(issubclass(c, HH) for c in self.mechanisms.values()):
+            raise NotImplementedError("one HH mechanism per model")
+        self.mechanisms[name] = bound
+        self._mech_instances[name] = {"seg": [], "mag": [], "n_at": [], "gnabar": [], "gkbar": [], "glbar": []}
+
+    def _grow(self, extra):
+        need = self._n + extra
+        cap = len(self._parent)
+        if need <= cap:
+            return
+        cap = max(need, 2 * cap, 64)
+        def grow(a, shape_tail=()):
+            b = np.zeros((cap,) + shape_tail, dtype=a.dtype)
+            b[:self._n] = a[:self._n]
+            return b
+        self._parent = grow(self._parent)
+        self._coords = grow(self._coords, (3,))
+        self._diam = grow(self._diam)
+        self._seg_neuron = grow(self._seg_neuron)
+
+    def _append(self, parent, coordinates, diameter, nid):
+        self._grow(1)
+        i = self._n
+        self._parent[i] = parent
+        self._coords[i] = np.asarray(coordinates, dtype=np.float64)
+        self._diam[i] = float(diameter)
+        self._seg_neuron[i] = nid
+        self._n += 1
+        self._dirty_structure = True
+        self._geom_cache = None
+        return i
+
+    def _parent_of(self, i):
+        return int(self._parent[i])
+
+    def _children_of(self, i):
+        return [int(c) for c in np.nonzero(self._parent[:self._n] == int(i))[0]]
+
+    def _neuron_handle(self, nid):
+        return Neuron(self, nid)
+
+    def _geometry(self):
+        if self._geom_cache is None or self._geom_cache["_n"] != self._n:
+            tree = Tree(self._parent[:self._n], self._coords[:self._n], self._diam[:self._n])
+            g = geometry(tree)
+            R, C = passive_electric(g, self.cytoplasmic_resistance, self.membrane_capacitance)
+            g["axial_resistance"] = R
+            g["capacitance"] = C
+            g["_n"] = self._n
+            self._geom_cache = g
+        return self._geom_cache
+
+    def _area_at(self, n_at):
+        """Surface areas of the first n_at segments with only their children then."""
+        if n_at == self._n:
+            return self._geometry()["surface_area"]
+        t = Tree(self._parent[:n_at], self._coords[:n_at], self._diam[:n_at])
+        return geometry(t)["surface_area"]
+
+    def _add_mechanism_instance(self, cls, segment, magnitude, overrides):
+        self._add_instances_bulk(cls, np.array([segment._idx]), np.array([magnitude]),
+                                 {k: v for k, v in overrides.items() if v is not None})
+        return self._instance_count(cls.get_name()) - 1
+
+    def _instance_count(self, name):
+        return sum(len(c) for c in self._mech_instances[name]["seg"])
+
+    def _add_instances_bulk(self, cls, segs, mags, per_instance):
+        """Append instances; per_instance maps gbar names to scalars or arrays."""
+        rec = self._mech_instances[cls.get_name()]
+        segs = np.asarray(segs, dtype=np.int64)
+        m = len(segs)
+        rec["seg"].append(segs)
+        rec["mag"].append(np.broadcast_to(np.asarray(mags, dtype=np.float64), (m,)).copy())
+        rec["n_at"].append(np.full(m, self._n, dtype=np.int64))
+        for key in ("gnabar", "gkbar", "glbar"):
+            v = per_instance.get(key)
+            arr = np.full(m, np.nan) if v is None else np.broadcast_to(np.asarray(v, np.float64), (m,)).copy()
+            rec[key].append(arr)
+        self._dirty_structure = True
+
+    def _add_clamp(self, seg, amps, first_tick, count):
+        self._clamps.append((int(seg), float(amps), int(first_tick), int(count)))
+        self._dirty_clamps = True
+
+    def _add_probe(self, ts, seg, immediate):
+        rec = {"ts": ts, "seg": seg, "start_step": self.clock.ticks}
+        self._flush_probes()
+        self._probes.append(rec)
+        if immediate:
+            ts.data.append(self._get_segment_values("Segment.voltage")[seg])
+            ts.timestamps.append(self.clock())
+        self._dirty_probes = True
+
+    def _remove_probe(self, ts):
+        self._flush_probes()
+        self._probes = [p for p in self._probes if p["ts"] is not ts]
+        self._dirty_probes = True
+
+    # --- device mirror ---------------------------------------------------
+    def _sync(self):
+        if self._ctx is None:
+            self._ctx = _lib.Context(self.device, self.precision)
+        if self._dirty_structure:
+            self._sync_structure()
+        if self._dirty_clamps:
+            self._sync_clamps()
+        if self._dirty_detectors:
+            self._sync_detectors()
+        if self._dirty_probes:
+            self._sync_probes()
+
+    def _sync_structure(self):
+        ctx = self._ctx
+        n = self._n
+        if n == 0:
+            raise RuntimeError("model has no segments")
+        saved = None
+        if self._order is not None:
+            saved = self._save_state()
+        order = np.argsort(self._seg_neuron[:n], kind="stable")     # Database.sort()
+        inv = np.empty(n, np.int64)
+        inv[order] = np.arange(n)
+        self._order, self._inv = order, inv
+        nids = self._seg_neuron[:n][order]
+        counts = np.bincount(nids, minlength=len(self._neuron_root))
+        neuron_start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        par = self._parent[:n][order]
+        parent_dev = np.where(par < 0, -1, inv[np.maximum(par, 0)]).astype(np.int64)
+        g = self._geometry()
+        ctx.call("nw_model_init", n, len(self._neuron_root), _lib.ptr(neuron_start),
+                 _lib.ptr(parent_dev), self.time_step, self.temperature)
+        ctx.set_data("Segment.capacitance", g["capacitance"][order])
+        ctx.set_data("Segment.axial_resistance", np.where(par < 0, 1.0, g["axial_resistance"][order]))
+        ctx.set_data("Segment.voltage", np.full(n, self.initial_voltage))
+        nnz = _lib.ctypes.c_int64()
+        ctx.call("nw_propagator_build", self.propagator_tolerance, _lib.ctypes.byref(nnz))
+        self.propagator_nnz = nnz.value
+        for name, cls in self.mechanisms.items():
+            self._sync_hh(cls)
+        self._dirty_structure = False
+        self._dirty_clamps = self._dirty_detectors = self._dirty_probes = True
+        if saved is not None:
+            self._restore_state(saved)
+        for key, (name, values) in list(self._pending.items()):
+            self._ctx.set_data(name, values[self._order])
+        self._pending.clear()
+
+    def _sync_hh(self, cls):
+        rec = self._mech_instances[cls.get_name()]
+        cat = lambda key, dt: (np.concatenate(rec[key]) if rec[key] else np.empty(0, dt))
+        seg = cat("seg", np.int64)
+        mag = cat("mag", np.float64)
+        n_at = cat("n_at", np.int64)
+        area = np.empty(len(seg))
+        for k in np.unique(n_at):
+            sel = n_at == k
+            area[sel] = self._area_at(int(k))[seg[sel]]
+        magnitude = mag * area                                 # nmodl/__init__.py:496-500
+
+        def coef(key, default):
+            v = cat(key, np.float64)
+            v = np.where(np.isnan(v), default, v)
+            return np.ascontiguousarray(v * 1e-8 * magnitude)  # nmodl/__init__.py:103-107, 404-406
+        gna = coef("gnabar", cls.gnabar)
+        gk = coef("gkbar", cls.gkbar)
+        gl = coef("glbar", cls.glbar)
+        seg_dev = np.ascontiguousarray(self._inv[seg]) if len(seg) else seg
+        self._ctx.call("nw_hh_register", len(seg), _lib.ptr(seg_dev),
+                       _lib.ptr(gna), _lib.ptr(gk), _lib.ptr(gl),
+                       float(cls.ena), float(cls.ek), float(cls.el), self.initial_voltage)
+
+    def _sync_clamps(self):
+        c = self._clamps
+        seg = np.array([self._inv[x[0]] for x in c], dtype=np.int64)
+        amp = np.array([x[1] for x in c], dtype=np.float64)
+        first = np.array([x[2] for x in c], dtype=np.int64)
+        cnt = np.array([x[3] for x in c], dtype=np.int64)
+        self._ctx.call("nw_clamps_set", len(c), _lib.ptr(seg), _lib.ptr(amp), _lib.ptr(first), _lib.ptr(cnt))
+        self._dirty_clamps = False
+
+    def _sync_detectors(self):
+        seg = self._inv[np.asarray(self._det_seg, dtype=np.int64)]
+        thr = np.asarray(self._det_thr, dtype=np.float64)
+        self._ctx.call("nw_detectors_set", _lib.ptr(np.ascontiguousarray(seg)), _lib.ptr(thr))
+        self._dirty_detectors = False
+
+    def _sync_probes(self, capacity=None):
+        self._flush_probes()
+        segs = np.array([self._inv[p["seg"]] for p in self._probes], dtype=np.int64)
+        self._probe_cap = capacity or 4096
+        self._ctx.call("nw_probes_set", len(segs), _lib.ptr(segs), self._probe_cap)
+        self._probe_base_step = self.clock.ticks
+        self._dirty_probes = False
+
+    def _ensure_probe_room(self, k):
+        steps = self._probe_steps()
+        if steps + k > self._probe_cap:
+            self._sync_probes(capacity=max(4096, k))
+
+    def _probe_steps(self):
+        if self._ctx is None or not self._probes or self._dirty_probes:
+            return 0
+        s = _lib.ctypes.c_int64()
+        self._ctx.call("nw_probes_read", None, 2, 0, _lib.ctypes.byref(s))
+        return s.value
+
+    def _flush_probes(self):
+        """Move device-recorded samples into the TimeSeries objects."""
+        if self._ctx is None or not self._probes or self._dirty_probes:
+            return
+        steps = self._probe_steps()
+        if steps == 0:
+            return
+        buf = np.empty((steps, len(self._probes)), dtype=np.float64)
+        s = _lib.ctypes.c_int64()
+        self._ctx.call("nw_probes_read", _lib.ptr(buf), 1, steps, _lib.ctypes.byref(s))
+        for k, p in enumerate(self._probes):
+            p["ts"].data.extend(buf[:, k].tolist())
+            p["ts"].timestamps.extend(((self._probe_base_step + 1 + np.arange(steps)) * self.time_step).tolist())
+        segs = np.array([self._inv[p["seg"]] for p in self._probes], dtype=np.int64)
+        self._ctx.call("nw_probes_set", len(segs), _lib.ptr(segs), self._probe_cap)
+        self._probe_base_step = self.clock.ticks
+
+    def _save_state(self):
+        st = {"V": self._ctx.get_data("Segment.voltage", len(self._order))[self._inv_prev()]}
+        return st
+
+    def _inv_prev(self):
+        inv = np.empty(len(self._order), np.int64)
+        inv[self._order] = np.arange(len(self._order))
+        return inv
+
+    def _restore_state(self, st):
+        V = np.full(self._n, self.initial_voltage)
+        V[:len(st["V"])] = st["V"]
+        self._ctx.set_data("Segment.voltage", V[self._order])
+
+    def _get_segment_values(self, name):
+        if self._ctx is None or self._dirty_structure:
+            if name == "Segment.voltage":
+                v = np.full(self._n, self.initial_voltage)
+                if "V" in self._pending:
+                    v = self._pending["V"][1].copy()
+                return v
+            raise RuntimeError(f"{name} is available after the first advance()")
+        dev = self._ctx.get_data(name, self._n)
+        return dev[self._inv]
+
+    def _set_segment_value(self, name, idx, value):
+        vals = self._get_segment_values(name).copy()
+        vals[idx] = value
+        if self._ctx is None or self._dirty_structure:
+            self._pending["V"] = (name, vals)
+        else:
+            self._ctx.set_data(name, vals[self._order])
+
+    def _get_neuron_values(self, name):
+        self._sync()
+        return self._ctx.get_data(name, len(self._neuron_root))
+
+
+Model = RxD_Model

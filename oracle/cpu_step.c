@@ -1,0 +1,131 @@
+/*
+ * CPU restatement of NEUWON's staggered Model.advance() -- TEST ORACLE and
+ * CPU baseline only (never linked into the product library).
+ *
+ * FP64, OpenMP over segments / instances.  Follows:
+ *   neuwon/rxd/rxd_model.py:63-80     advance: species(dt/2), mechanisms, species(dt/2), AP
+ *   neuwon/rxd/rxd_model.py:91-113    accumulators, input clock tick, driving voltage
+ *   neuwon/rxd/species.py:389-393     nonspecific conductance scatter (summed here)
+ *   neuwon/rxd/neuron/electric.py:56-76  exact membrane update and V <- P x
+ *   nmodl_library/artificial/hh.mod + neuwon/rxd/nmodl/solver.py:48-55  HH gates
+ *   neuwon/rxd/neuron/neuron.py:184-188  AP detector
+ *   neuwon/database/time.py:287-302   current clamps on the half-step clock
+ *
+ * Build: see oracle/Makefile (gcc -O3 -fopenmp -shared).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct {
+    int64_t n_seg;
+    /* propagator, CSR with the diagonal, global column indices */
+    const int64_t* rowptr; const int32_t* col; const double* val;
+    /* electric state */
+    double* V; double* Vint; const double* C; const double* Inonspec;
+    double time_step;              /* ms */
+    /* hh instances sorted by segment; inst range of segment i: [seg_ptr[i], seg_ptr[i+1]) */
+    int64_t m; const int64_t* hh_seg_ptr; const int64_t* hh_seg;
+    double* gm; double* gh; double* gn; const double* cna; const double* ck; const double* cl;
+    double ena, ek, el, celsius;
+    /* clamps grouped by segment: [clamp_ptr[i], clamp_ptr[i+1]) */
+    const int64_t* clamp_ptr; const double* clamp_amp; const int64_t* clamp_first; const int64_t* clamp_count;
+    /* detectors */
+    int64_t n_neuron; const int64_t* det_seg; const double* det_thr;
+    uint8_t* ap_state; uint8_t* ap_detected; int64_t* spike_count;
+    /* scratch [n_seg] and clock */
+    double* x;
+    int64_t input_ticks;
+    int g_valid;
+} oracle_model;
+
+static double vtrap(double x, double y) {
+    if (fabs(x / y) < 1e-6) return y * (1 - x / y / 2);
+    return x / (exp(x / y) - 1);
+}
+
+static void half_step(oracle_model* m) {
+    const double h = 0.5 * m->time_step, h_s = h * 1e-3;
+    const int64_t tick = ++m->input_ticks;
+    const int gv = m->g_valid;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < m->n_seg; ++i) {
+        double gna = 0, gk = 0, gl = 0;
+        if (gv && m->m) {
+            for (int64_t k = m->hh_seg_ptr[i]; k < m->hh_seg_ptr[i + 1]; ++k) {
+                double mm = m->gm[k], hh = m->gh[k], nn = m->gn[k];
+                gna += m->cna[k] * mm * mm * mm * hh;
+                gk += m->ck[k] * nn * nn * nn * nn;
+                gl += m->cl[k];
+            }
+        }
+        double G = (gna + gk) + gl;
+        double GE = (gna * m->ena + gk * m->ek) + gl * m->el;
+        double I = m->Inonspec ? m->Inonspec[i] : 0.0;
+        if (m->clamp_ptr)
+            for (int64_t c = m->clamp_ptr[i]; c < m->clamp_ptr[i + 1]; ++c)
+                if (tick >= m->clamp_first[c] && tick < m->clamp_first[c] + m->clamp_count[c]) I += m->clamp_amp[c];
+        double E = GE / G;
+        if (isnan(E)) E = 0.0;
+        double dv = h * I / m->C[i];
+        double expo = -h_s * G / m->C[i];
+        double alpha = exp(expo);
+        double diff = E - m->V[i];
+        m->x[i] = E - diff * alpha + dv;
+        m->Vint[i] = h_s * E - expo * diff * alpha + (.5 * h_s * dv);
+    }
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < m->n_seg; ++i) {
+        double acc = 0.0;
+        for (int64_t k = m->rowptr[i]; k < m->rowptr[i + 1]; ++k) acc += m->val[k] * m->x[m->col[k]];
+        m->V[i] = acc;
+    }
+}
+
+static void mechanisms(oracle_model* m) {
+    const double q10 = pow(3.0, (m->celsius - 6.3) / 10.0);
+    const double dt = m->time_step;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < m->n_seg; ++i) {
+        for (int64_t k = m->hh_seg_ptr[i]; k < m->hh_seg_ptr[i + 1]; ++k) {
+            double v = m->V[m->hh_seg[k]];
+            double a = .1 * vtrap(-(v + 40), 10), b = 4 * exp(-(v + 65) / 18);
+            double mtau = 1 / (q10 * (a + b)), minf = a / (a + b);
+            a = .07 * exp(-(v + 65) / 20); b = 1 / (exp(-(v + 35) / 10) + 1);
+            double htau = 1 / (q10 * (a + b)), hinf = a / (a + b);
+            a = .01 * vtrap(-(v + 55), 10); b = .125 * exp(-(v + 65) / 80);
+            double ntau = 1 / (q10 * (a + b)), ninf = a / (a + b);
+            m->gm[k] = minf + (m->gm[k] - minf) * exp(-dt / mtau);
+            m->gh[k] = hinf + (m->gh[k] - hinf) * exp(-dt / htau);
+            m->gn[k] = ninf + (m->gn[k] - ninf) * exp(-dt / ntau);
+        }
+    }
+}
+
+int oracle_advance(oracle_model* m, int k_steps) {
+    for (int s = 0; s < k_steps; ++s) {
+        half_step(m);
+        if (m->m) { mechanisms(m); m->g_valid = 1; }
+        half_step(m);
+        for (int64_t j = 0; j < m->n_neuron; ++j) {
+            int over = m->V[m->det_seg[j]] >= m->det_thr[j];
+            int det = over && !m->ap_state[j];
+            m->ap_detected[j] = (uint8_t)det;
+            m->ap_state[j] = (uint8_t)over;
+            m->spike_count[j] += det;
+        }
+    }
+    return 0;
+}
+
+int oracle_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,264 @@
+"""FP64 numpy restatement of the reference's staggered time step (test oracle).
+
+Each function names the reference lines it follows (paths relative to the
+reference project).  Units follow the reference: voltages mV, currents A,
+conductances S, capacitances F, time ms.
+"""
+import math
+import numpy as np
+import scipy.linalg
+import scipy.sparse
+import scipy.sparse.linalg
+
+EPSILON = float(np.finfo(np.float64).eps)   # neuwon/database/dtypes.py:4
+
+
+def coefficient_coo(parent, R, C, time_step_ms):
+    """COO of dV/dt coefficients; neuwon/rxd/neuron/electric.py:85-109.
+
+    Four entries per (child, parent) edge, in the reference's append order.
+    Returns (dst, src, coef) so that ``matrix[dst, src] = coef`` (duplicates sum).
+    """
+    dt = time_step_ms * 1e-3
+    src, dst, coef = [], [], []
+    for child, p in enumerate(parent):
+        if p < 0:
+            continue
+        r = R[child]; c_parent = C[p]; c_child = C[child]
+        src.append(child); dst.append(p);     coef.append(+dt / (r * c_parent))
+        src.append(child); dst.append(child); coef.append(-dt / (r * c_child))
+        src.append(p);     dst.append(child); coef.append(+dt / (r * c_child))
+        src.append(p);     dst.append(p);     coef.append(-dt / (r * c_parent))
+    return (np.asarray(dst, dtype=np.int64), np.asarray(src, dtype=np.int64),
+            np.asarray(coef, dtype=np.float64))
+
+
+def propagator(parent, R, C, time_step_ms, prune=EPSILON, dense_above=400):
+    """expm of the coefficient matrix, pruned below ``prune``; electric.py:78-117.
+
+    The reference calls ``scipy.sparse.linalg.expm`` on a CSC matrix; above
+    ``dense_above`` segments the same exponential is taken with the dense
+    ``scipy.linalg.expm`` (same mathematics, far faster).  Independent trees
+    (separate neurons) are exponentiated block by block, which is exact for a
+    block-diagonal matrix.  Returns a scipy CSR matrix.
+    """
+    parent = np.asarray(parent, dtype=np.int64)
+    n = len(parent)
+    dst, src, coef = coefficient_coo(parent, R, C, time_step_ms)
+    # Block boundaries: trees are contiguous ranges starting at each root.
+    roots = np.nonzero(parent < 0)[0]
+    bounds = list(roots) + [n]
+    blocks = []
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        sel = (dst >= a) & (dst < b)
+        m = b - a
+        if m <= dense_above:
+            A = scipy.sparse.csc_matrix((coef[sel], (dst[sel] - a, src[sel] - a)),
+                                        shape=(m, m), dtype=np.float64)
+            P = scipy.sparse.linalg.expm(A)
+            P = scipy.sparse.csr_matrix(P) if scipy.sparse.issparse(P) else scipy.sparse.csr_matrix(np.atleast_2d(P))
+            P = P.toarray()
+        else:
+            A = np.zeros((m, m))
+            np.add.at(A, (dst[sel] - a, src[sel] - a), coef[sel])
+            P = scipy.linalg.expm(A)
+        P[np.abs(P) < prune] = 0.0
+        blocks.append(scipy.sparse.csr_matrix(P))
+    P = scipy.sparse.block_diag(blocks, format="csr") if len(blocks) > 1 else blocks[0]
+    P.eliminate_zeros()
+    P.sort_indices()
+    return P
+
+
+# ---------------------------------------------------------------- HH (hh.mod)
+
+def _vtrap(x, y):
+    """nmodl_library/artificial/hh.mod:88-94."""
+    x = np.asarray(x, dtype=np.float64)
+    small = np.abs(x / y) < 1e-6
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        big = x / (np.exp(x / y) - 1.0)
+    return np.where(small, y * (1.0 - x / y / 2.0), big)
+
+
+def hh_rates(v, celsius):
+    """PROCEDURE rates(v); nmodl_library/artificial/hh.mod:62-86.
+
+    Returns (minf, mtau, hinf, htau, ninf, ntau)."""
+    q10 = 3.0 ** ((celsius - 6.3) / 10.0)
+    alpha = 0.1 * _vtrap(-(v + 40.0), 10.0)
+    beta = 4.0 * np.exp(-(v + 65.0) / 18.0)
+    s = alpha + beta
+    mtau = 1.0 / (q10 * s); minf = alpha / s
+    alpha = 0.07 * np.exp(-(v + 65.0) / 20.0)
+    beta = 1.0 / (np.exp(-(v + 35.0) / 10.0) + 1.0)
+    s = alpha + beta
+    htau = 1.0 / (q10 * s); hinf = alpha / s
+    alpha = 0.01 * _vtrap(-(v + 55.0), 10.0)
+    beta = 0.125 * np.exp(-(v + 65.0) / 80.0)
+    s = alpha + beta
+    ntau = 1.0 / (q10 * s); ninf = alpha / s
+    return minf, mtau, hinf, htau, ninf, ntau
+
+
+class HHInstances:
+    """``hh`` mechanism instances as the NMODL front end would lay them out.
+
+    * gbar parameters in S/cm2 are converted to S/um2 (x1e-8) and multiplied
+      by the instance magnitude (um2); neuwon/rxd/nmodl/__init__.py:99-107, 404-406;
+    * ``USEION na WRITE gna, ena`` writes the equilibrium, so each conductance
+      is a *nonspecific* conductance stored on the instance and scattered to
+      its segment; nmodl/__init__.py:179-208, species.py:359-396;
+    * ``SOLVE states`` without METHOD uses the exact solution of the linear
+      gate ODEs, x <- xinf + (x - xinf)*exp(-dt/xtau); nmodl/solver.py:48-55,105-106.
+    """
+
+    def __init__(self, segment, magnitude, *, gnabar=0.12, gkbar=0.036, glbar=0.0003,
+                 ena=60.0, ek=-88.0, el=-54.3, v_init=-70.0, celsius=6.3):
+        self.segment = np.asarray(segment, dtype=np.int64)
+        m = len(self.segment)
+        mag = np.broadcast_to(np.asarray(magnitude, dtype=np.float64), (m,)).copy()
+        self.gna_coef = np.broadcast_to(np.asarray(gnabar, np.float64) * 1e-8, (m,)) * mag
+        self.gk_coef = np.broadcast_to(np.asarray(gkbar, np.float64) * 1e-8, (m,)) * mag
+        self.gl_coef = np.broadcast_to(np.asarray(glbar, np.float64) * 1e-8, (m,)) * mag
+        self.E = {"na": float(ena), "k": float(ek), "l": float(el)}
+        minf, _, hinf, _, ninf, _ = hh_rates(np.full(m, float(v_init)), celsius)
+        self.m, self.h, self.n = minf.copy(), hinf.copy(), ninf.copy()
+        self.g = {"na": np.zeros(m), "k": np.zeros(m), "l": np.zeros(m)}
+
+    def zero_accumulators(self):
+        """species.py:385-387 (nonspecific conductances reset before mechanisms run)."""
+        for g in self.g.values():
+            g.fill(0.0)
+
+    def advance(self, voltage, dt, celsius):
+        """BREAKPOINT block of hh.mod:41-46 after NMODL's solve and IO fixups."""
+        v = voltage[self.segment]
+        minf, mtau, hinf, htau, ninf, ntau = hh_rates(v, celsius)
+        m = minf + (self.m - minf) * np.exp(-dt / mtau)
+        h = hinf + (self.h - hinf) * np.exp(-dt / htau)
+        n = ninf + (self.n - ninf) * np.exp(-dt / ntau)
+        self.m, self.h, self.n = m, h, n
+        self.g["na"] += self.gna_coef * m * m * m * h
+        self.g["k"] += self.gk_coef * n * n * n * n
+        self.g["l"] += self.gl_coef
+
+
+class OracleModel:
+    """FP64 restatement of ``RxD_Model.advance()`` (neuwon/rxd/rxd_model.py:63-80).
+
+    Inputs are plain arrays for the segments (creation order, neurons
+    contiguous as after ``Database.sort()``).  ``clamps`` is a list of
+    (segment, amperes, first_tick, num_ticks) in input-hook ticks (half steps);
+    ``detectors`` is a list of (segment, threshold_mV) per neuron.
+
+    ``duplicates='sum'`` adds every mechanism instance's conductance into its
+    segment.  ``duplicates='numpy'`` reproduces the reference's fancy-index
+    ``a[idx] += b`` (species.py:392-393), under which only one of several
+    instances on the same segment is counted.
+    """
+
+    def __init__(self, parent, R, C, *, time_step=0.1, celsius=6.3, v_init=-70.0,
+                 prune=EPSILON, propagator_matrix=None, hh=None, clamps=(),
+                 detectors=(), duplicates="sum"):
+        self.parent = np.asarray(parent, dtype=np.int64)
+        self.n = len(self.parent)
+        self.R = np.asarray(R, dtype=np.float64)
+        self.C = np.asarray(C, dtype=np.float64)
+        self.time_step = float(time_step)
+        self.half_step = 0.5 * self.time_step     # rxd_model.py:21, species.py:406
+        self.celsius = float(celsius)
+        self.voltage = np.full(self.n, float(v_init))
+        self.integral_voltage = np.zeros(self.n)
+        self.nonspecific_current = np.zeros(self.n)
+        self.sum_current = np.zeros(self.n)
+        self.sum_conductance = np.zeros(self.n)
+        self.driving_voltage = np.zeros(self.n)
+        self.P = propagator_matrix if propagator_matrix is not None else \
+            propagator(self.parent, self.R, self.C, self.half_step, prune)
+        self.hh = hh
+        self.clamps = [(int(s), float(a), int(f), int(k)) for (s, a, f, k) in clamps]
+        self.detectors = [(int(s), float(t)) for (s, t) in detectors]
+        self.AP_detected = np.zeros(len(self.detectors), dtype=bool)
+        self._AP_true_state = np.zeros(len(self.detectors), dtype=bool)
+        self.spike_count = np.zeros(len(self.detectors), dtype=np.int64)
+        self.input_ticks = 0
+        self.steps = 0
+        self.duplicates = duplicates
+
+    # rxd_model.py:91-113
+    def _advance_species(self):
+        self.sum_current[:] = self.nonspecific_current
+        self.sum_conductance.fill(0.0)
+        self.driving_voltage.fill(0.0)
+        if self.hh is not None:
+            seg = self.hh.segment
+            for ion in ("na", "k", "l"):
+                g = self.hh.g[ion]
+                if self.duplicates == "numpy":
+                    self.sum_conductance[seg] += g
+                    self.driving_voltage[seg] += g * self.hh.E[ion]
+                else:
+                    np.add.at(self.sum_conductance, seg, g)
+                    np.add.at(self.driving_voltage, seg, g * self.hh.E[ion])
+        # input_hook.tick(): Clock.tick then TimeSeries._play_implementation
+        # (database/time.py:114-117, 287-302), current clamps in "+=" mode.
+        self.input_ticks += 1
+        t = self.input_ticks
+        for seg, amps, first, count in self.clamps:
+            if first <= t < first + count:
+                self.sum_current[seg] += amps
+        with np.errstate(divide="ignore", invalid="ignore"):
+            self.driving_voltage /= self.sum_conductance
+        self.driving_voltage[:] = np.nan_to_num(self.driving_voltage)
+        self._advance_electric(self.half_step)
+
+    # neuwon/rxd/neuron/electric.py:56-76
+    def _advance_electric(self, time_step):
+        dt = time_step * 1e-3
+        dv_currents = time_step * self.sum_current / self.C
+        exponent = -dt * self.sum_conductance / self.C
+        alpha = np.exp(exponent)
+        diff_v = self.driving_voltage - self.voltage
+        self.voltage[:] = self.P.dot(self.driving_voltage - diff_v * alpha + dv_currents)
+        self.integral_voltage[:] = (dt * self.driving_voltage - exponent * diff_v * alpha
+                                    + (.5 * dt * dv_currents))
+
+    # rxd_model.py:115-123
+    def _advance_mechanisms(self):
+        self.nonspecific_current.fill(0.0)
+        if self.hh is not None:
+            self.hh.zero_accumulators()
+            self.hh.advance(self.voltage, self.time_step, self.celsius)
+
+    # neuwon/rxd/neuron/neuron.py:184-188
+    def _advance_AP_detector(self):
+        for k, (seg, thr) in enumerate(self.detectors):
+            over = self.voltage[seg] >= thr
+            self.AP_detected[k] = over and not self._AP_true_state[k]
+            self._AP_true_state[k] = over
+            self.spike_count[k] += int(self.AP_detected[k])
+
+    def advance(self):
+        """rxd_model.py:63-80: species(dt/2) -> mechanisms(dt) -> species(dt/2) -> AP."""
+        self._advance_species()
+        self._advance_mechanisms()
+        self._advance_species()
+        self._advance_AP_detector()
+        self.steps += 1
+
+
+def clamp_ticks(start_ms, duration_ms, time_step):
+    """Ticks on which ``Segment.inject_current`` adds its current.
+
+    ``inject_current`` (electric.py:119-125) plays a two-point constant wave on
+    the half-step input clock with ``immediate=False`` (time.py:245-285): it
+    fires on the ``ceil(duration/half_step)`` ticks after the call.  A call made
+    when the model clock reads ``start_ms`` (i.e. before the advance that starts
+    at ``start_ms``) therefore covers ticks [2k+1, 2k+1+count) with
+    k = round(start_ms / time_step).
+    """
+    half = 0.5 * time_step
+    count = math.ceil(float(duration_ms) / half)
+    k = round(float(start_ms) / time_step)
+    return 2 * k + 1, count
