@@ -1,0 +1,366 @@
+"""Benchmark: batched FP32 Model.advance() on one GB300 (segment-steps/s).
+
+Workload (neuwon_gb300.workloads.batched): 1,024 seeded neurons, log-uniform
+500-20,000 segments (5.59 M segments), HH on every segment, one soma current
+per neuron, dt = 0.1 ms, propagator pruned at --tol.  A "step" is one
+Model.advance() of the whole batch.  The propagator (about 10+ GB) is far
+larger than L2, so no L2 flush is needed between timed steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  Under torchrun each rank advances its own 1,024-neuron
+batch (seeds offset by rank; weak scaling) and rank 0 prints; the reference
+arm runs on rank 0 only.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoint ms/step"
+
+
+def algorithmic_bytes_per_segment_step(r, s_total=3, p_seg=4):
+    """B = 2(8r + 4) + 4(2 + 2 S_total + P_seg + 1): two propagator passes (4 B value +
+    4 B column per entry, 4 B row pointer), V read+write, every state read+write,
+    per-segment parameters (C and three HH gbar), one stimulus read."""
+    return 2 * (8 * r + 4) + 4 * (2 + 2 * s_total + p_seg + 1)
+
+
+def format_bytes_per_segment_step(r_stored, prec=4, s_total=3):
+    """Compulsory HBM bytes of this implementation's layout per segment-step:
+    two passes over (value + u16 column) per stored entry and an 8 B row pointer and
+    leak, V read+write (x2), gates read twice + written once, kI/kG/coefficients."""
+    per_half = r_stored * (prec + 2) + 8 + prec + 2 * prec + 2 * prec + 3 * prec + 3 * prec
+    mech = 2 * s_total * prec + prec
+    return 2 * per_half + mech
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, device=0):
+    """Time the C oracle (FP64, OpenMP, all host threads) on the first few neurons."""
+    from neuwon_gb300 import _lib
+    from neuwon_gb300.workloads import build_model
+    from oracle.cpu_oracle import CpuOracle
+    sample, segs = [], 0
+    for t in trees:
+        sample.append(t)
+        segs += len(t)
+        if segs >= 25000:
+            break
+    m, neurons = build_model(sample, currents[:len(sample)], precision="f64", tolerance=tol, device=device)
+    m._sync()
+    ctx = m._ctx
+    n = m._n
+    nnz = ctypes.c_int64()
+    ctx.call("nw_propagator_get_csr", None, None, None, ctypes.byref(nnz))
+    rowptr = np.empty(n + 1, np.int64); col = np.empty(nnz.value, np.int64); val = np.empty(nnz.value)
+    ctx.call("nw_propagator_get_csr", _lib.ptr(rowptr), _lib.ptr(col), _lib.ptr(val), ctypes.byref(nnz))
+    # Device order equals creation order here (neurons were added one after another).
+    g = m._geometry()
+    rec = m._mech_instances["hh"]
+    seg = np.concatenate(rec["seg"])
+    area = g["surface_area"][seg]
+    from neuwon_gb300.workloads import HH_PARAMS
+    hh = dict(segment=seg, gna=HH_PARAMS["gnabar"] * 1e-8 * area, gk=HH_PARAMS["gkbar"] * 1e-8 * area,
+              gl=HH_PARAMS["glbar"] * 1e-8 * area, ena=HH_PARAMS["ena"], ek=HH_PARAMS["ek"], el=HH_PARAMS["el"])
+    clamps = [(c[0], c[1], c[2], c[3]) for c in m._clamps]
+    roots = [int(nr.root.get_unstable_index()) for nr in neurons]
+    m.close()
+    co = CpuOracle(rowptr, col.astype(np.int32), val, g["capacitance"], time_step=0.1, celsius=6.3,
+                   hh=hh, clamps=clamps, detectors=[(r, 20.0) for r in roots])
+    co.advance(2)
+    done, t0 = 0, time.perf_counter()
+    while done < steps and time.perf_counter() - t0 < time_budget_s:
+        co.advance(1)
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": n * done / dt, "unit": "segment-steps/s", "cores": co.threads(), "kind": "port",
+            "sample": f"first {len(sample)} neurons of the batch ({n} segments, "
+                      f"{nnz.value / n:.0f} propagator entries/row), {done} steps, FP64 C restatement "
+                      f"(oracle/cpu_step.c) with OpenMP"}
+
+
+def run_reference(args, rank):
+    from neuwon_gb300.workloads import batched_currents, batched_trees
+    trees = batched_trees(args.neurons, first=0, count=16, processes=8)
+    currents = batched_currents(args.neurons)
+    res = cpu_sample(trees, currents, args.tol, steps=args.steps + args.warmup, time_budget_s=120.0)
+    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "segment-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "batched: 1024 HH neurons, 500-20000 segments, dt 0.1 ms",
+                                            "sample": res["sample"], "propagator_tolerance": args.tol},
+            "cpu_baseline": res,
+            "e2e": {"value": res["value"], "unit": "segment-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def accuracy_and_plain(trees, currents, tol, device, steps=2000, plain_steps=10):
+    """FP32 batched vs FP64 batched on a subset; FP64 plain path timing on the same subset."""
+    import torch
+    from neuwon_gb300 import _lib
+    from neuwon_gb300.workloads import build_model
+    m64, n64 = build_model(trees, currents, precision="f64", tolerance=tol, device=device)
+    m32, n32 = build_model(trees, currents, precision="f32", tolerance=tol, device=device)
+    m64._sync(); m32._sync()
+    worst = 0.0
+    chunk = 50
+    for k in range(steps // chunk):
+        m64.advance(chunk); m32.advance(chunk)
+        worst = max(worst, float(np.abs(m64.get_data("Segment.voltage") - m32.get_data("Segment.voltage")).max()))
+    sp64 = m64.get_data("Neuron.spike_count"); sp32 = m32.get_data("Neuron.spike_count")
+    m32.close()
+    # Plain per-neuron FP64 path on the same neurons.
+    m64.path = _lib.PATH_PLAIN
+    torch.cuda.synchronize()
+    m64.advance(1)
+    m64._ctx.call("nw_synchronize")
+    t0 = time.perf_counter()
+    m64.advance(plain_steps)
+    m64._ctx.call("nw_synchronize")
+    dt = time.perf_counter() - t0
+    n = m64._n
+    m64.close()
+    return {"max_err_mV": worst, "spikes_equal": bool(np.array_equal(sp64, sp32)),
+            "spikes_total": int(sp64.sum()), "steps": steps,
+            "sample": f"first {len(trees)} neurons ({n} segments)"}, \
+           {"value": n * plain_steps / dt, "unit": "segment-steps/s", "ms_per_step": 1e3 * dt / plain_steps,
+            "sample": f"first {len(trees)} neurons ({n} segments), {plain_steps} steps, "
+                      "per-neuron launches, 32 threads/block, FP64 CSR"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--neurons", type=int, default=1024)
+    ap.add_argument("--tol", type=float, default=1e-9)
+    ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch")
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=512)
+    ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu legs")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, rank)
+        return
+
+    from neuwon_gb300.workloads import batched_currents, batched_trees, build_model
+    # Trees are generated in a spawned pool before any CUDA work.
+    t_setup = time.perf_counter()
+    trees = batched_trees(args.neurons, seed=rank, processes=min(16, os.cpu_count() or 1))
+    currents = batched_currents(args.neurons, seed=rank)
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    extra = {}
+    if not args.quick and rank == 0:
+        sub = trees[:64]
+        extra["accuracy"], extra["plain_fp64"] = accuracy_and_plain(sub, currents[:64], args.tol, local)
+
+    from neuwon_gb300 import _lib
+    model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, device=local)
+    t_build = time.perf_counter()
+    model._sync()
+    ctx = model._ctx
+    ctx.call("nw_set_tuning", args.lanes, args.threads, 0)
+    ctx.call("nw_synchronize")
+    build_s = time.perf_counter() - t_build
+    rows, nnz, stored, pbytes = (ctypes.c_int64() for _ in range(4))
+    ctx.call("nw_propagator_stats", ctypes.byref(rows), ctypes.byref(nnz), ctypes.byref(stored), ctypes.byref(pbytes))
+    n = model._n
+    r_kept = nnz.value / n
+    r_stored = stored.value / n
+    lanes = ctypes.c_int(); thr = ctypes.c_int(); cps = ctypes.c_int()
+    ctx.call("nw_get_tuning", ctypes.byref(lanes), ctypes.byref(thr), ctypes.byref(cps))
+    sptr = ctypes.c_void_p()
+    ctx.call("nw_get_stream", ctypes.byref(sptr))
+    stream = torch.cuda.ExternalStream(sptr.value, device=torch.device("cuda", local))
+
+    F = max(1, min(args.fusion, args.steps))
+    # Warm-up.
+    w = args.warmup
+    while w > 0:
+        k = min(F, w)
+        model.advance(k)
+        w -= k
+    ctx.call("nw_synchronize")
+
+    # Timed device-resident region: K steps as launches of F fused steps.
+    launches = []
+    K = args.steps
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ctx.call("nw_synchronize")
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            done = 0
+            while done < K:
+                k = min(F, K - done)
+                e_a = torch.cuda.Event(enable_timing=True); e_b = torch.cuda.Event(enable_timing=True)
+                e_a.record(stream)
+                ctx.advance(k, _lib.PATH_BATCHED)
+                e_b.record(stream)
+                launches.append((e_a, e_b, k))
+                done += k
+            ev1.record(stream)
+        ev1.synchronize()
+    model.input_hook.ticks += 2 * K
+    model.advance_hook.ticks += K
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * world * K / (ms * 1e-3)
+    launch_ms = [a.elapsed_time(b) / k for (a, b, k) in launches]   # per fused step
+    per_step_launch_ms = float(np.mean(launch_ms))
+
+    # End to end through the C ABI with host buffers: per step, the clamp currents
+    # go host->device and every segment voltage comes back device->host.
+    stim = torch.empty(len(neurons), dtype=torch.float64, pin_memory=True)
+    stim.copy_(torch.from_numpy(np.asarray(currents, dtype=np.float64) * 1e-9))
+    vout = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    E = max(10, min(K, 200))
+    ctx.call("nw_advance_host", 1, ctypes.c_void_p(stim.data_ptr()), ctypes.c_void_p(vout.data_ptr()), 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(E):
+        ctx.call("nw_advance_host", 1, ctypes.c_void_p(stim.data_ptr()), ctypes.c_void_p(vout.data_ptr()), 2)
+    e2e_s = time.perf_counter() - t0
+    model.input_hook.ticks += 2 * (E + 1)
+    model.advance_hook.ticks += E + 1
+    e2e_value = n * world * E / e2e_s
+    vcheck = vout.numpy()
+    finite = bool(np.all(np.isfinite(vcheck)))
+
+    from neuwon_gb300.morphology import EPSILON  # noqa: F401
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    B_alg = algorithmic_bytes_per_segment_step(r_kept)
+    B_fmt = format_bytes_per_segment_step(r_stored)
+    achieved = B_alg * n / (per_step_launch_ms * 1e-3) / 1e9
+    achieved_fmt = B_fmt * n / (per_step_launch_ms * 1e-3) / 1e9
+
+    cpu = None
+    if not args.quick and rank == 0:
+        cpu = cpu_sample(trees[:16], currents, args.tol, steps=100000, time_budget_s=15.0, device=local)
+    spikes = model.get_data("Neuron.spike_count")
+    model.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "segment-steps/s", "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded trees; no dataset involved)",
+        "config": {"workload": "batched: 1024 neurons, log-uniform 500-20000 segments, HH on every "
+                               "segment, soma current U(0.05,0.5) nA, dt 0.1 ms, FP32 state, FP64-built "
+                               "propagator",
+                   "segments": n, "neurons": len(neurons), "propagator_tolerance": args.tol,
+                   "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
+                   "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
+                   "threads": thr.value, "l2": "inputs larger than L2 (propagator "
+                   f"{pbytes.value / 1e9:.1f} GB), no flush", "mechanisms": ["hh"],
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_src,
+                     "bytes_per_segment_step": B_alg,
+                     "format_bytes_per_segment_step": B_fmt,
+                     "format_achieved": achieved_fmt, "format_frac": achieved_fmt / peak,
+                     "kernel": "batched_advance_kernel", "launch_ms_per_step": per_step_launch_ms},
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e_value, "unit": "segment-steps/s", "steps": E,
+                "h2d_bytes_per_step": int(stim.numel() * 8), "d2h_bytes_per_step": int(vout.numel() * 4),
+                "api": "nw_advance_host (C ABI), one step per call", "finite": finite},
+        "gpu_launches": len(launches),
+        "cpu_baseline": cpu,
+        "spikes_total": int(spikes.sum()),
+        "setup_s": time.perf_counter() - t_setup,
+    }
+    line.update(extra)
+    if "plain_fp64" in extra:
+        line["batched_over_plain"] = value / world / extra["plain_fp64"]["value"]
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -21,7 +21,7 @@
 // root-to-leaves sweep per neuron and pole), after which row i of the
 // resolvent is a product of edge ratios along the path from i.  Row i of P
 // is then collected by a depth-first walk outward from i that keeps entries
-// with |P_ij| >= tol and stops exploring a branch once |P_ij| < tol * 1e-4.
+// with |P_ij| >= tol and stops exploring a branch once |P_ij| < tol * 1e-3.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -33,7 +33,7 @@ namespace nw {
 constexpr int kPoles = 16;            // N/2 for N = 32
 constexpr int kNodes = 2 * kPoles;
 constexpr int kStackDepth = 96;
-constexpr double kExploreFactor = 1e-4;
+constexpr double kExploreFactor = 1e-3;
 constexpr int kStatusStackOverflow = 2;
 constexpr int kStatusRowMismatch = 4;
 
