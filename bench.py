@@ -104,7 +104,8 @@ def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, device=0):
         segs += len(t)
         if segs >= 25000:
             break
-    m, neurons = build_model(sample, currents[:len(sample)], precision="f64", tolerance=tol, device=device)
+    m, neurons = build_model(sample, currents[:len(sample)], precision="f64", tolerance=tol, conserve=True,
+                             device=device)
     m._sync()
     ctx = m._ctx
     n = m._n
@@ -141,7 +142,7 @@ def run_reference(args, rank):
     from neuwon_gb300.workloads import batched_currents, batched_trees
     trees = batched_trees(args.neurons, first=0, count=16, processes=8)
     currents = batched_currents(args.neurons)
-    res = cpu_sample(trees, currents, args.tol, steps=args.steps + args.warmup, time_budget_s=120.0)
+    res = cpu_sample(trees, currents, args.tol, steps=args.steps + args.warmup, time_budget_s=60.0)
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "segment-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -153,38 +154,58 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def accuracy_and_plain(trees, currents, tol, device, steps=2000, plain_steps=10):
-    """FP32 batched vs FP64 batched on a subset; FP64 plain path timing on the same subset."""
-    import torch
-    from neuwon_gb300 import _lib
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def accuracy(trees, currents, tol, device, steps):
+    """FP32 batched at the bench tolerance (charge-conserving pruning) against the FP64
+    batched path with the reference's own propagator (machine-epsilon pruning)."""
+    from neuwon_gb300 import Segment, TimeSeries
+    from neuwon_gb300.morphology import EPSILON
     from neuwon_gb300.workloads import build_model
-    m64, n64 = build_model(trees, currents, precision="f64", tolerance=tol, device=device)
-    m32, n32 = build_model(trees, currents, precision="f32", tolerance=tol, device=device)
-    m64._sync(); m32._sync()
-    worst = 0.0
-    chunk = 50
-    for k in range(steps // chunk):
-        m64.advance(chunk); m32.advance(chunk)
-        worst = max(worst, float(np.abs(m64.get_data("Segment.voltage") - m32.get_data("Segment.voltage")).max()))
-    sp64 = m64.get_data("Neuron.spike_count"); sp32 = m32.get_data("Neuron.spike_count")
-    m32.close()
-    # Plain per-neuron FP64 path on the same neurons.
-    m64.path = _lib.PATH_PLAIN
-    torch.cuda.synchronize()
-    m64.advance(1)
-    m64._ctx.call("nw_synchronize")
+    ref, nref = build_model(trees, currents, precision="f64", tolerance=EPSILON, conserve=False, device=device)
+    test, ntest = build_model(trees, currents, precision="f32", tolerance=tol, conserve=True, device=device)
+    probes = []
+    for m, ns in ((ref, nref), (test, ntest)):
+        probes.append([TimeSeries().record(nr.root, "voltage") for nr in ns])
+    ref._sync(); test._sync()
+    worst_all, chunk = 0.0, 50
+    for _ in range(steps // chunk):
+        ref.advance(chunk); test.advance(chunk)
+        worst_all = max(worst_all, float(np.abs(ref.get_data("Segment.voltage") -
+                                                test.get_data("Segment.voltage")).max()))
+    soma_ref = np.array([p.get_data() for p in probes[0]])
+    soma_test = np.array([p.get_data() for p in probes[1]])
+    sp_ref = ref.get_data("Neuron.spike_count"); sp_test = test.get_data("Neuron.spike_count")
+    n = ref._n
+    ref.close(); test.close()
+    return {"max_err_mV": max(worst_all, float(np.abs(soma_ref - soma_test).max())),
+            "max_err_soma_every_step_mV": float(np.abs(soma_ref - soma_test).max()),
+            "max_err_all_segments_every_50_steps_mV": worst_all,
+            "spikes_equal": bool(np.array_equal(sp_ref, sp_test)), "spikes_total": int(sp_ref.sum()),
+            "steps": steps,
+            "against": "FP64 batched GPU path with machine-epsilon pruning (the reference's propagator)",
+            "sample": f"first {len(trees)} neurons of the batch ({n} segments)"}
+
+
+def plain_timing(trees, currents, tol, device, steps=10):
+    """The plain per-neuron FP64 path (reference GPU design) on a subset of the batch."""
+    from neuwon_gb300.workloads import build_model
+    m, _ = build_model(trees, currents, precision="f64", tolerance=tol, conserve=True, path="plain",
+                       device=device)
+    m._sync()
+    m.advance(1)
+    m._ctx.call("nw_synchronize")
     t0 = time.perf_counter()
-    m64.advance(plain_steps)
-    m64._ctx.call("nw_synchronize")
+    m.advance(steps)
+    m._ctx.call("nw_synchronize")
     dt = time.perf_counter() - t0
-    n = m64._n
-    m64.close()
-    return {"max_err_mV": worst, "spikes_equal": bool(np.array_equal(sp64, sp32)),
-            "spikes_total": int(sp64.sum()), "steps": steps,
-            "sample": f"first {len(trees)} neurons ({n} segments)"}, \
-           {"value": n * plain_steps / dt, "unit": "segment-steps/s", "ms_per_step": 1e3 * dt / plain_steps,
-            "sample": f"first {len(trees)} neurons ({n} segments), {plain_steps} steps, "
-                      "per-neuron launches, 32 threads/block, FP64 CSR"}
+    n = m._n
+    m.close()
+    return {"value": n * steps / dt, "unit": "segment-steps/s", "ms_per_step": 1e3 * dt / steps,
+            "sample": f"first {len(trees)} neurons ({n} segments), {steps} steps, per-neuron launches, "
+                      "32 threads/block, FP64 CSR, same propagator tolerance"}
 
 
 def main():
@@ -194,7 +215,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--neurons", type=int, default=1024)
-    ap.add_argument("--tol", type=float, default=1e-9)
+    ap.add_argument("--tol", type=float, default=1e-7)
+    ap.add_argument("--acc-neurons", type=int, default=16)
+    ap.add_argument("--acc-steps", type=int, default=2000)
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--threads", type=int, default=512)
@@ -221,19 +244,26 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
+    log(f"trees ready ({sum(len(t) for t in trees)} segments) in {time.perf_counter() - t_setup:.1f} s")
     extra = {}
     if not args.quick and rank == 0:
-        sub = trees[:64]
-        extra["accuracy"], extra["plain_fp64"] = accuracy_and_plain(sub, currents[:64], args.tol, local)
+        k = args.acc_neurons
+        extra["accuracy"] = accuracy(trees[:k], currents[:k], args.tol, local, args.acc_steps)
+        log(f"accuracy: {extra['accuracy']}")
+        extra["plain_fp64"] = plain_timing(trees[:64], currents[:64], args.tol, local)
+        log(f"plain: {extra['plain_fp64']}")
 
     from neuwon_gb300 import _lib
-    model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, device=local)
     t_build = time.perf_counter()
+    model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, conserve=True,
+                                 device=local)
+    log(f"host model built in {time.perf_counter() - t_build:.1f} s")
     model._sync()
     ctx = model._ctx
     ctx.call("nw_set_tuning", args.lanes, args.threads, 0)
     ctx.call("nw_synchronize")
     build_s = time.perf_counter() - t_build
+    log(f"device model + propagator in {build_s:.1f} s")
     rows, nnz, stored, pbytes = (ctypes.c_int64() for _ in range(4))
     ctx.call("nw_propagator_stats", ctypes.byref(rows), ctypes.byref(nnz), ctypes.byref(stored), ctypes.byref(pbytes))
     n = model._n
@@ -320,6 +350,7 @@ def main():
     achieved = B_alg * n / (per_step_launch_ms * 1e-3) / 1e9
     achieved_fmt = B_fmt * n / (per_step_launch_ms * 1e-3) / 1e9
 
+    log(f"timed: {ms / K:.3f} ms/step; e2e {e2e_s / E * 1e3:.3f} ms/step")
     cpu = None
     if not args.quick and rank == 0:
         cpu = cpu_sample(trees[:16], currents, args.tol, steps=100000, time_budget_s=15.0, device=local)
@@ -335,6 +366,7 @@ def main():
                                "segment, soma current U(0.05,0.5) nA, dt 0.1 ms, FP32 state, FP64-built "
                                "propagator",
                    "segments": n, "neurons": len(neurons), "propagator_tolerance": args.tol,
+                   "propagator_pruning": "charge-conserving (pruned mass returned to the diagonal)",
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
                    "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
                    "threads": thr.value, "l2": "inputs larger than L2 (propagator "

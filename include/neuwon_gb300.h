@@ -98,6 +98,14 @@ int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out);
 int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr,
                           const int64_t* col, const double* val, int64_t nnz);
 
+/* Charge-conserving pruning: returns the pruned mass of every row of the installed
+ * propagator to its diagonal, so each row sums to 1 again.  The unpruned matrix has
+ * unit row sums (the reference tests this charge conservation,
+ * neuwon/rxd/tests/test_electric.py:216-217); pruning without this correction
+ * (the reference's own behaviour, electric.py:114-115) leaks voltage toward 0 mV
+ * at coarse tolerances.  Requires a stored diagonal entry in every row. */
+int nw_propagator_conserve(nw_ctx* ctx);
+
 /* Reads the FP64 propagator back as CSR (rowptr[n+1], col[nnz], val[nnz]);
  * pass NULL arrays to query *nnz_out only. */
 int nw_propagator_get_csr(nw_ctx* ctx, int64_t* rowptr, int64_t* col, double* val,

@@ -23,7 +23,7 @@ EXPORTS = [
     "nw_synchronize", "nw_model_init", "nw_set_data", "nw_get_data", "nw_propagator_build",
     "nw_propagator_set_csr", "nw_propagator_get_csr", "nw_hh_register", "nw_clamps_set",
     "nw_detectors_set", "nw_probes_set", "nw_probes_read", "nw_advance", "nw_advance_host",
-    "nw_get_clock", "nw_set_tuning", "nw_get_tuning", "nw_propagator_stats",
+    "nw_get_clock", "nw_set_tuning", "nw_get_tuning", "nw_propagator_stats", "nw_propagator_conserve",
 ]
 
 _lib = None
@@ -58,6 +58,7 @@ def load(build_if_missing=True):
         "nw_propagator_build": ([c_void_p, c_double, P(c_i64)], c_int),
         "nw_propagator_set_csr": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64], c_int),
         "nw_propagator_get_csr": ([c_void_p, c_void_p, c_void_p, c_void_p, P(c_i64)], c_int),
+        "nw_propagator_conserve": ([c_void_p], c_int),
         "nw_hh_register": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p,
                             c_double, c_double, c_double, c_double], c_int),
         "nw_clamps_set": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p], c_int),

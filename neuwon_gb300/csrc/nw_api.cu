@@ -456,6 +456,14 @@ int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr, const i
     return NW_OK;
 }
 
+int nw_propagator_conserve(nw_ctx* ctx) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "nw_propagator_conserve: no propagator installed");
+    NW_CHECK(propagator_conserve(ctx));
+    return propagator_to_batched(ctx);
+}
+
 int nw_propagator_get_csr(nw_ctx* ctx, int64_t* rowptr, int64_t* col, double* val, int64_t* nnz_out) {
     if (!ctx) return NW_ERR_ARG;
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");

@@ -110,6 +110,7 @@ int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out);
 int propagator_from_host(nw_ctx* ctx, const int64_t* rowptr, const int64_t* col,
                          const double* val, int64_t nnz);
 int propagator_to_batched(nw_ctx* ctx);
+int propagator_conserve(nw_ctx* ctx);
 
 // Stepping (nw_step.cu).
 int advance_batched(nw_ctx* ctx, int k_steps);

@@ -329,6 +329,45 @@ int propagator_from_host(nw_ctx* ctx, const int64_t* rowptr, const int64_t* col,
     return NW_OK;
 }
 
+// ------------------------------------------------- charge-conserving pruning
+
+// One warp per row: diag += 1 - sum(row), summed in FP64 in a fixed order.
+__global__ void conserve_rows_kernel(int64_t n, const int64_t* prow, const int32_t* pcol, double* pval,
+                                     int* status) {
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (r >= n) return;
+    double sum = 0.0;
+    int64_t diag = -1;
+    for (int64_t k = prow[r] + lane; k < prow[r + 1]; k += 32) {
+        sum += pval[k];
+        if (pcol[k] == (int32_t)r) diag = k;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+    const unsigned has = __ballot_sync(0xffffffffu, diag >= 0);
+    if (!has) {
+        if (lane == 0) atomicOr(status, 8);
+        return;
+    }
+    if (lane == __ffs(has) - 1) pval[diag] += 1.0 - sum;
+}
+
+int propagator_conserve(nw_ctx* ctx) {
+    const int64_t n = ctx->n_seg;
+    cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+    conserve_rows_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(
+        n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(), ctx->status.as<int>());
+    int st = 0;
+    NW_CUDA(ctx, cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (st & 8) {
+        cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+        return fail(ctx, NW_ERR_STATE, "nw_propagator_conserve: a row has no diagonal entry");
+    }
+    return NW_OK;
+}
+
 // ------------------------------------------------- batched difference form
 
 __global__ void batched_count_kernel(int64_t n, const int64_t* prow, const int32_t* pcol, int64_t* cnt) {

@@ -129,17 +129,19 @@ __device__ __forceinline__ real membrane_x(const StepArgs<real>& a, int64_t i, r
     return x;
 }
 
+// Propagator entries are streamed once per half step and do not fit in L2, so
+// they are loaded with the evict-first (streaming) cache hint.
 template <typename real> struct Vec4Loader;
 template <> struct Vec4Loader<float> {
     static __device__ __forceinline__ void load(const float* p, float (&v)[4]) {
-        float4 q = __ldg(reinterpret_cast<const float4*>(p));
+        float4 q = __ldcs(reinterpret_cast<const float4*>(p));
         v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
     }
 };
 template <> struct Vec4Loader<double> {
     static __device__ __forceinline__ void load(const double* p, double (&v)[4]) {
-        double2 q0 = __ldg(reinterpret_cast<const double2*>(p));
-        double2 q1 = __ldg(reinterpret_cast<const double2*>(p) + 1);
+        double2 q0 = __ldcs(reinterpret_cast<const double2*>(p));
+        double2 q1 = __ldcs(reinterpret_cast<const double2*>(p) + 1);
         v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
     }
 };
@@ -153,7 +155,7 @@ __device__ __forceinline__ void kahan_add(real& s, real& c, real term) {
 }
 
 // V_i <- propagator row i applied to xs, for every row of one neuron.
-template <typename real, int LPR>
+template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2)>
 __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_t base, int n,
                                                  const real* __restrict__ xs) {
     constexpr int GPW = 32 / LPR;                  // row groups per warp
@@ -169,14 +171,29 @@ __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_
             const int64_t r = base + row;
             const int64_t beg = a.rowptr[r], end = a.rowptr[r + 1];
             xi = xs[row];
-            for (int64_t k = beg + 4 * l; k < end; k += 4 * LPR) {
-                real v[4];
-                Vec4Loader<real>::load(a.val + k, v);
-                const ushort4 cc = __ldg(reinterpret_cast<const ushort4*>(a.col + k));
-                kahan_add(s, c, v[0] * (xs[cc.x] - xi));
-                kahan_add(s, c, v[1] * (xs[cc.y] - xi));
-                kahan_add(s, c, v[2] * (xs[cc.z] - xi));
-                kahan_add(s, c, v[3] * (xs[cc.w] - xi));
+            // UNROLL chunks of 4 entries per lane are loaded before any is consumed,
+            // to keep enough bytes in flight per SM for HBM latency.
+            for (int64_t k0 = beg + 4 * l; k0 < end; k0 += 4 * LPR * UNROLL) {
+                real v[UNROLL][4];
+                ushort4 cc[UNROLL];
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const int64_t k = k0 + 4 * LPR * u;
+                    if (k < end) {
+                        Vec4Loader<real>::load(a.val + k, v[u]);
+                        cc[u] = __ldcs(reinterpret_cast<const ushort4*>(a.col + k));
+                    } else {
+                        v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                        cc[u] = make_ushort4(0, 0, 0, 0);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    kahan_add(s, c, v[u][0] * (xs[cc[u].x] - xi));
+                    kahan_add(s, c, v[u][1] * (xs[cc[u].y] - xi));
+                    kahan_add(s, c, v[u][2] * (xs[cc[u].z] - xi));
+                    kahan_add(s, c, v[u][3] * (xs[cc[u].w] - xi));
+                }
             }
         }
         real t = s - c;

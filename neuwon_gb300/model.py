@@ -257,6 +257,8 @@ class RxD_Model:
       precision             'f32' (default) or 'f64' state and step arithmetic
       device                CUDA device ordinal
       propagator_tolerance  prune |P_ij| below this (reference: machine epsilon)
+      propagator_conserve   return the pruned mass of each row to its diagonal
+                            (charge-conserving pruning; the reference does not)
       path                  'batched' (fused persistent kernel) or 'plain'
     """
 
@@ -264,7 +266,7 @@ class RxD_Model:
                  cytoplasmic_resistance=100, membrane_capacitance=1,
                  extracellular_tortuosity=1.55, extracellular_max_distance=20e-6,
                  species=(), mechanisms=(), precision="f32", device=0,
-                 propagator_tolerance=EPSILON, path="batched"):
+                 propagator_tolerance=EPSILON, propagator_conserve=False, path="batched"):
         if species:
             raise NotImplementedError("species beyond the mechanisms' nonspecific conductances "
                                       "are not on the GPU path")
@@ -276,6 +278,7 @@ class RxD_Model:
         self.precision = precision
         self.device = int(device)
         self.propagator_tolerance = float(propagator_tolerance)
+        self.propagator_conserve = bool(propagator_conserve)
         self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN}[path]
         self.input_hook = Clock(0.5 * self.time_step, units="ms")
         self.advance_hook = self.clock = Clock(self.time_step, units="ms")
@@ -538,6 +541,8 @@ class RxD_Model:
         ctx.set_data("Segment.voltage", np.full(n, self.initial_voltage))
         nnz = _lib.ctypes.c_int64()
         ctx.call("nw_propagator_build", self.propagator_tolerance, _lib.ctypes.byref(nnz))
+        if self.propagator_conserve:
+            ctx.call("nw_propagator_conserve")
         self.propagator_nnz = nnz.value
         for name, cls in self.mechanisms.items():
             self._sync_hh(cls)

@@ -47,12 +47,12 @@ def batched_currents(num_neurons=1024, seed=0):
     return np.random.default_rng(seed).uniform(0.05, 0.5, num_neurons)
 
 
-def build_model(trees, currents_nA, *, precision="f32", tolerance=1e-7, duration_ms=1e9,
-                path="batched", device=0):
+def build_model(trees, currents_nA, *, precision="f32", tolerance=1e-7, conserve=True,
+                duration_ms=1e9, path="batched", device=0):
     """RxD_Model with HH on every segment and a constant soma clamp per neuron."""
     from .model import RxD_Model
     m = RxD_Model(time_step=TIME_STEP, temperature=CELSIUS, precision=precision, device=device,
-                  propagator_tolerance=tolerance, path=path,
+                  propagator_tolerance=tolerance, propagator_conserve=conserve, path=path,
                   mechanisms=[HH.configure(**HH_PARAMS)])
     neurons = [m.add_tree(t) for t in trees]
     m.insert_everywhere("hh")
