@@ -29,19 +29,21 @@ sys.path.insert(0, ROOT)
 METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoint ms/step"
 
 
-def algorithmic_bytes_per_segment_step(r, s_total=3, p_seg=4):
+def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
     """B = 2(8r + 4) + 4(2 + 2 S_total + P_seg + 1): two propagator passes (4 B value +
-    4 B column per entry, 4 B row pointer), V read+write, every state read+write,
-    per-segment parameters (C and three HH gbar), one stimulus read."""
+    4 B column per entry, 4 B row pointer), V read+write, every state read+write
+    (HH 3 + na8 8), per-segment parameters (C, three HH gbar, na8 gbar), one stimulus read."""
     return 2 * (8 * r + 4) + 4 * (2 + 2 * s_total + p_seg + 1)
 
 
-def format_bytes_per_segment_step(r_stored, prec=4, s_total=3):
+def format_bytes_per_segment_step(r_stored, prec=4):
     """Compulsory HBM bytes of this implementation's layout per segment-step:
-    two passes over (value + u16 column) per stored entry and an 8 B row pointer and
-    leak, V read+write (x2), gates read twice + written once, kI/kG/coefficients."""
-    per_half = r_stored * (prec + 2) + 8 + prec + 2 * prec + 2 * prec + 3 * prec + 3 * prec
-    mech = 2 * s_total * prec + prec
+    per half step, (value + u16 column) per stored entry, an 8 B row pointer, the
+    leak, V read + write, kI and kG, HH gates (3) and coefficients (3), the na8 open
+    state and coefficient; per step the mechanism update reads V and reads + writes
+    3 HH gates and 8 na8 states."""
+    per_half = r_stored * (prec + 2) + 8 + prec + 2 * prec + 2 * prec + 6 * prec + 2 * prec
+    mech = prec + 2 * (3 + 8) * prec
     return 2 * per_half + mech
 
 
@@ -140,7 +142,8 @@ def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, device=0):
 
 def run_reference(args, rank):
     from neuwon_gb300.workloads import batched_currents, batched_trees
-    trees = batched_trees(args.neurons, first=0, count=16, processes=8)
+    lo, hi = (int(x) for x in args.size_range.split(","))
+    trees = batched_trees(args.neurons, first=0, count=16, processes=8, lo=lo, hi=hi)
     currents = batched_currents(args.neurons)
     res = cpu_sample(trees, currents, args.tol, steps=args.steps + args.warmup, time_budget_s=60.0)
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "segment-steps/s",
@@ -158,13 +161,12 @@ def log(msg):
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
-def accuracy(trees, currents, tol, device, steps):
-    """FP32 batched at the bench tolerance (charge-conserving pruning) against the FP64
-    batched path with the reference's own propagator (machine-epsilon pruning)."""
+def accuracy(trees, currents, tol, device, steps, ref_tol):
+    """FP32 batched at the bench tolerance against the FP64 batched path with a propagator
+    pruned at ref_tol (both charge-conserving)."""
     from neuwon_gb300 import Segment, TimeSeries
-    from neuwon_gb300.morphology import EPSILON
     from neuwon_gb300.workloads import build_model
-    ref, nref = build_model(trees, currents, precision="f64", tolerance=EPSILON, conserve=False, device=device)
+    ref, nref = build_model(trees, currents, precision="f64", tolerance=ref_tol, conserve=True, device=device)
     test, ntest = build_model(trees, currents, precision="f32", tolerance=tol, conserve=True, device=device)
     probes = []
     for m, ns in ((ref, nref), (test, ntest)):
@@ -185,7 +187,7 @@ def accuracy(trees, currents, tol, device, steps):
             "max_err_all_segments_every_50_steps_mV": worst_all,
             "spikes_equal": bool(np.array_equal(sp_ref, sp_test)), "spikes_total": int(sp_ref.sum()),
             "steps": steps,
-            "against": "FP64 batched GPU path with machine-epsilon pruning (the reference's propagator)",
+            "against": f"FP64 batched GPU path, propagator pruned at {ref_tol:g} (charge-conserving)",
             "sample": f"first {len(trees)} neurons of the batch ({n} segments)"}
 
 
@@ -215,7 +217,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--neurons", type=int, default=1024)
-    ap.add_argument("--tol", type=float, default=1e-7)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--ref-tol", type=float, default=1e-11,
+                    help="pruning of the FP64 accuracy reference (machine epsilon makes rows dense)")
+    ap.add_argument("--size-range", default="500,20000", help="neuron size range (segments)")
     ap.add_argument("--acc-neurons", type=int, default=16)
     ap.add_argument("--acc-steps", type=int, default=2000)
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch")
@@ -235,7 +240,8 @@ def main():
     from neuwon_gb300.workloads import batched_currents, batched_trees, build_model
     # Trees are generated in a spawned pool before any CUDA work.
     t_setup = time.perf_counter()
-    trees = batched_trees(args.neurons, seed=rank, processes=min(16, os.cpu_count() or 1))
+    lo, hi = (int(x) for x in args.size_range.split(","))
+    trees = batched_trees(args.neurons, seed=rank, processes=min(16, os.cpu_count() or 1), lo=lo, hi=hi)
     currents = batched_currents(args.neurons, seed=rank)
     import torch
     torch.cuda.set_device(local)
@@ -248,7 +254,7 @@ def main():
     extra = {}
     if not args.quick and rank == 0:
         k = args.acc_neurons
-        extra["accuracy"] = accuracy(trees[:k], currents[:k], args.tol, local, args.acc_steps)
+        extra["accuracy"] = accuracy(trees[:k], currents[:k], args.tol, local, args.acc_steps, args.ref_tol)
         log(f"accuracy: {extra['accuracy']}")
         extra["plain_fp64"] = plain_timing(trees[:64], currents[:64], args.tol, local)
         log(f"plain: {extra['plain_fp64']}")
@@ -362,15 +368,15 @@ def main():
         "metric": METRIC, "value": value, "unit": "segment-steps/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded trees; no dataset involved)",
-        "config": {"workload": "batched: 1024 neurons, log-uniform 500-20000 segments, HH on every "
-                               "segment, soma current U(0.05,0.5) nA, dt 0.1 ms, FP32 state, FP64-built "
-                               "propagator",
+        "config": {"workload": f"batched: {len(neurons)} neurons, log-uniform {lo}-{hi} segments, HH + "
+                               "8-state Markov Na on every segment, soma current U(0.05,0.5) nA, dt 0.1 ms, "
+                               "FP32 state, FP64-built propagator",
                    "segments": n, "neurons": len(neurons), "propagator_tolerance": args.tol,
                    "propagator_pruning": "charge-conserving (pruned mass returned to the diagonal)",
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
                    "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
                    "threads": thr.value, "l2": "inputs larger than L2 (propagator "
-                   f"{pbytes.value / 1e9:.1f} GB), no flush", "mechanisms": ["hh"],
+                   f"{pbytes.value / 1e9:.1f} GB), no flush", "mechanisms": ["hh", "na8 (8-state Markov Na, LTI voltage table 1600 x 0.1 mV, linear)"],
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,

@@ -79,6 +79,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
  *   Segment.voltage, Segment.integral_voltage, Segment.capacitance,
  *   Segment.axial_resistance, Segment.nonspecific_current,
  *   hh.m, hh.h, hh.n (instance order as registered),
+ *   kinetic.state (num_instances * S values, [instance][state], registration order),
  *   Neuron.AP_detected, Neuron.spike_count.
  * Values are converted between dtype and the context precision. */
 int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int64_t count);
@@ -123,6 +124,22 @@ int nw_propagator_get_csr(nw_ctx* ctx, int64_t* rowptr, int64_t* col, double* va
 int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
                    const double* gna_coef, const double* gk_coef, const double* gl_coef,
                    double ena, double ek, double el, double v_init);
+
+/* Registers the instances of one linear kinetic scheme solved by exact integration
+ * with a voltage table (lti_sim: neuwon/rxd/lti_sim/lti_model.py:5-65, approx.py:159-174,
+ * codegen.py:29-106; NMODL "SOLVE ... METHOD sparse", nmodl/__init__.py:298-306).
+ *   num_states S (1..16), open_states: indices whose sum is the open probability;
+ *   g_coef[i]: instance i's maximal conductance in siemens (gbar * 1e-8 * magnitude);
+ *   erev: reversal potential of its nonspecific conductance (mV);
+ *   table: [num_buckets][S (col)][S (row)][num_terms] polynomial coefficients, the
+ *   layout of codegen.py:35-37; the voltage v falls in bucket trunc((v - vmin) * bucket_frq)
+ *   clamped as in codegen.py:43-59;
+ *   conserve_sum: states are rescaled to this sum after each step (<= 0: no CONSERVE);
+ *   init_state: S initial occupancies for every instance. */
+int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
+                        const double* g_coef, int num_states, int num_open, const int32_t* open_states,
+                        double erev, const double* table, int num_buckets, int num_terms,
+                        double vmin, double bucket_frq, double conserve_sum, const double* init_state);
 
 /* ---- stimulus, detection, recording --------------------------------- */
 

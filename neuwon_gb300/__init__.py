@@ -4,11 +4,12 @@ The host API mirrors the reference's RxD_Model / Neuron / Segment / Mechanism
 interface; every time step runs in hand-written CUDA kernels behind the C ABI
 declared in include/neuwon_gb300.h (loaded with ctypes, no CPU fallback).
 """
+from .kinetic import Kinetic, KineticScheme, LTITable, na8
 from .mechanisms import HH, Mechanism, NMODL
 from .model import Clock, Model, Neuron, RxD_Model, Segment, TimeSeries
 from .morphology import EPSILON, Tree, geometry, neuron_sizes, passive_electric, random_tree
 
-__all__ = ["HH", "Mechanism", "NMODL", "Clock", "Model", "Neuron", "RxD_Model", "Segment",
+__all__ = ["Kinetic", "KineticScheme", "LTITable", "na8", "HH", "Mechanism", "NMODL", "Clock", "Model", "Neuron", "RxD_Model", "Segment",
            "TimeSeries", "EPSILON", "Tree", "geometry", "neuron_sizes", "passive_electric",
            "random_tree"]
 __version__ = "0.1.0"

@@ -24,6 +24,7 @@ EXPORTS = [
     "nw_propagator_set_csr", "nw_propagator_get_csr", "nw_hh_register", "nw_clamps_set",
     "nw_detectors_set", "nw_probes_set", "nw_probes_read", "nw_advance", "nw_advance_host",
     "nw_get_clock", "nw_set_tuning", "nw_get_tuning", "nw_propagator_stats", "nw_propagator_conserve",
+    "nw_kinetic_register",
 ]
 
 _lib = None
@@ -61,6 +62,8 @@ def load(build_if_missing=True):
         "nw_propagator_conserve": ([c_void_p], c_int),
         "nw_hh_register": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p,
                             c_double, c_double, c_double, c_double], c_int),
+        "nw_kinetic_register": ([c_void_p, c_i64, c_void_p, c_void_p, c_int, c_int, c_void_p, c_double,
+                                 c_void_p, c_int, c_int, c_double, c_double, c_double, c_void_p], c_int),
         "nw_clamps_set": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
         "nw_detectors_set": ([c_void_p, c_void_p, c_void_p], c_int),
         "nw_probes_set": ([c_void_p, c_i64, c_void_p, c_i64], c_int),

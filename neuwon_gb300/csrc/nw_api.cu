@@ -160,6 +160,17 @@ static int64_t neuron_of(const nw_ctx* ctx, int64_t seg) {
     return (int64_t)(std::upper_bound(s.begin(), s.end(), seg) - s.begin()) - 1;
 }
 
+static void free_hh(HHState& hh) {
+    for (DevBuf* b : {&hh.seg, &hh.gm, &hh.gh, &hh.gn, &hh.cna, &hh.ck, &hh.cl, &hh.seg_ptr, &hh.neuron_ptr})
+        dev_free(*b);
+    hh = HHState();
+}
+
+static void free_kin(KineticState& k) {
+    for (DevBuf* b : {&k.seg, &k.state, &k.gcoef, &k.table, &k.seg_ptr, &k.neuron_ptr}) dev_free(*b);
+    k = KineticState();
+}
+
 // HH steady state at v (nmodl_library/artificial/hh.mod:48-53, 62-94).
 static void hh_steady(double v, double* m, double* h, double* n) {
     auto vtrap = [](double x, double y) {
@@ -219,11 +230,11 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     if (!ctx) return NW_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    free_hh(ctx->hh);
+    free_kin(ctx->kin);
     DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec,
                       &ctx->kI, &ctx->kG, &ctx->cap64, &ctx->res64, &ctx->p_rowptr, &ctx->p_col,
                       &ctx->p_val, &ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak,
-                      &ctx->hh.seg, &ctx->hh.gm, &ctx->hh.gh, &ctx->hh.gn, &ctx->hh.cna,
-                      &ctx->hh.ck, &ctx->hh.cl, &ctx->hh.seg_ptr, &ctx->hh.neuron_ptr,
                       &ctx->clamp_seg, &ctx->clamp_amp, &ctx->clamp_first, &ctx->clamp_count,
                       &ctx->clamp_neuron_ptr, &ctx->clamp_amp_stage, &ctx->det_seg, &ctx->det_thr,
                       &ctx->ap_detected, &ctx->ap_state, &ctx->spike_count, &ctx->probe_seg,
@@ -294,7 +305,8 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     ctx->have_detectors = false;
     ctx->n_clamps = 0;
     ctx->n_probes = 0;
-    ctx->hh = HHState();
+    free_hh(ctx->hh);
+    free_kin(ctx->kin);
     size_t rs = (size_t)ctx->precision;
     NW_CHECK(dev_alloc(ctx, ctx->neuron_start, 8 * (num_neurons + 1)));
     NW_CHECK(dev_alloc(ctx, ctx->parent, 8 * num_segments));
@@ -380,6 +392,15 @@ int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int6
         DevBuf& b = nm == "hh.m" ? ctx->hh.gm : (nm == "hh.h" ? ctx->hh.gh : ctx->hh.gn);
         return upload_convert(ctx, b.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
     }
+    if (nm == "kinetic.state") {
+        const KineticState& K = ctx->kin;
+        NW_CHECK(need(K.m * K.S));
+        std::vector<double> sorted((size_t)K.S * K.m);
+        for (int64_t u = 0; u < K.m; ++u)
+            for (int c = 0; c < K.S; ++c)
+                sorted[(size_t)c * K.m + K.user_to_sorted[u]] = read_as_double(host, dtype, u * K.S + c);
+        return upload_convert(ctx, K.state.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
+    }
     if (nm == "Neuron.AP_detected") {
         NW_CHECK(need(ctx->n_neuron));
         return upload_convert(ctx, ctx->ap_detected.ptr, NW_DTYPE_U8, host, dtype, count);
@@ -412,6 +433,16 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
         std::vector<double> sorted(count);
         NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, b.ptr, rd, count));
         for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[ctx->hh.user_to_sorted[i]]);
+        return NW_OK;
+    }
+    if (nm == "kinetic.state") {
+        const KineticState& K = ctx->kin;
+        NW_CHECK(need(K.m * K.S));
+        std::vector<double> sorted((size_t)K.S * K.m);
+        NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, K.state.ptr, rd, count));
+        for (int64_t u = 0; u < K.m; ++u)
+            for (int c = 0; c < K.S; ++c)
+                write_from_double(host, dtype, u * K.S + c, sorted[(size_t)c * K.m + K.user_to_sorted[u]]);
         return NW_OK;
     }
     if (nm == "Neuron.AP_detected") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->ap_detected.ptr, NW_DTYPE_U8, count); }
@@ -490,6 +521,54 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
     return NW_OK;
 }
 
+// Segment-sorted (stable) layout of mechanism instances, so every segment's
+// instances are contiguous and every neuron's instances form one range.
+struct InstanceLayout {
+    std::vector<int64_t> order;          // sorted position -> user index
+    std::vector<int64_t> user_to_sorted;
+    std::vector<uint32_t> seg, seg_ptr;  // [m], [n_seg+1]
+    std::vector<int64_t> nptr;           // [n_neuron+1]
+    bool identity = false;
+};
+
+static int layout_instances(nw_ctx* ctx, int64_t m, const int64_t* segment, const char* who,
+                            InstanceLayout& L) {
+    const int64_t n = ctx->n_seg;
+    for (int64_t i = 0; i < m; ++i)
+        if (segment[i] < 0 || segment[i] >= n)
+            return fail(ctx, NW_ERR_ARG, std::string(who) + ": segment index out of range");
+    L.order.resize(m);
+    std::iota(L.order.begin(), L.order.end(), 0);
+    std::stable_sort(L.order.begin(), L.order.end(), [&](int64_t a, int64_t b) { return segment[a] < segment[b]; });
+    L.user_to_sorted.assign(m, 0);
+    for (int64_t s = 0; s < m; ++s) L.user_to_sorted[L.order[s]] = s;
+    L.identity = (m == n);
+    for (int64_t s = 0; s < m && L.identity; ++s) L.identity = segment[L.order[s]] == s;
+    L.seg.assign(m, 0);
+    L.seg_ptr.assign(n + 1, 0);
+    L.nptr.assign(ctx->n_neuron + 1, 0);
+    for (int64_t s = 0; s < m; ++s) {
+        int64_t u = L.order[s];
+        L.seg[s] = (uint32_t)segment[u];
+        L.seg_ptr[segment[u] + 1]++;
+        L.nptr[neuron_of(ctx, segment[u]) + 1]++;
+    }
+    for (int64_t i = 0; i < n; ++i) L.seg_ptr[i + 1] += L.seg_ptr[i];
+    for (int64_t k = 0; k < ctx->n_neuron; ++k) L.nptr[k + 1] += L.nptr[k];
+    return NW_OK;
+}
+
+static int upload_layout(nw_ctx* ctx, const InstanceLayout& L, DevBuf& seg, DevBuf& seg_ptr, DevBuf& nptr) {
+    const int64_t m = (int64_t)L.seg.size();
+    NW_CHECK(dev_alloc(ctx, seg, 4 * std::max<int64_t>(m, 1)));
+    NW_CHECK(dev_alloc(ctx, seg_ptr, 4 * (ctx->n_seg + 1)));
+    NW_CHECK(dev_alloc(ctx, nptr, 8 * (ctx->n_neuron + 1)));
+    NW_CHECK(upload_convert(ctx, seg.ptr, NW_DTYPE_U32, L.seg.data(), NW_DTYPE_U32, m));
+    NW_CHECK(upload_convert(ctx, seg_ptr.ptr, NW_DTYPE_U32, L.seg_ptr.data(), NW_DTYPE_U32, ctx->n_seg + 1));
+    NW_CHECK(upload_convert(ctx, nptr.ptr, NW_DTYPE_I64, L.nptr.data(), NW_DTYPE_I64, ctx->n_neuron + 1));
+    return NW_OK;
+}
+
 int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
                    const double* gna_coef, const double* gk_coef, const double* gl_coef,
                    double ena, double ek, double el, double v_init) {
@@ -498,47 +577,28 @@ int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_hh_register before nw_model_init");
     if (num_instances < 0 || (num_instances && (!segment || !gna_coef || !gk_coef || !gl_coef)))
         return fail(ctx, NW_ERR_ARG, "nw_hh_register: null arrays");
-    const int64_t m = num_instances, n = ctx->n_seg;
-    for (int64_t i = 0; i < m; ++i)
-        if (segment[i] < 0 || segment[i] >= n)
-            return fail(ctx, NW_ERR_ARG, "nw_hh_register: segment index out of range");
-    // Segment-sorted order (stable), so every segment's instances are contiguous
-    // and every neuron's instances form one range.
-    std::vector<int64_t> order(m);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return segment[a] < segment[b]; });
+    const int64_t m = num_instances;
+    InstanceLayout L;
+    NW_CHECK(layout_instances(ctx, m, segment, "nw_hh_register", L));
     HHState& hh = ctx->hh;
-    hh = HHState();
+    free_hh(hh);
     hh.m = m;
     hh.ena = ena; hh.ek = ek; hh.el = el; hh.v_init = v_init;
-    hh.user_to_sorted.assign(m, 0);
-    for (int64_t s = 0; s < m; ++s) hh.user_to_sorted[order[s]] = s;
-    hh.identity = (m == n);
-    for (int64_t s = 0; s < m && hh.identity; ++s) hh.identity = segment[order[s]] == s;
-    std::vector<uint32_t> seg(m), seg_ptr(n + 1, 0);
+    hh.user_to_sorted = L.user_to_sorted;
+    hh.identity = L.identity;
+    hh.h_neuron_ptr = L.nptr;
     std::vector<double> cna(m), ck(m), cl(m), g0(m);
-    std::vector<int64_t> nptr(ctx->n_neuron + 1, 0);
     for (int64_t s = 0; s < m; ++s) {
-        int64_t u = order[s];
-        seg[s] = (uint32_t)segment[u];
+        int64_t u = L.order[s];
         cna[s] = gna_coef[u]; ck[s] = gk_coef[u]; cl[s] = gl_coef[u];
-        seg_ptr[segment[u] + 1]++;
-        nptr[neuron_of(ctx, segment[u]) + 1]++;
     }
-    for (int64_t i = 0; i < n; ++i) seg_ptr[i + 1] += seg_ptr[i];
-    for (int64_t k = 0; k < ctx->n_neuron; ++k) nptr[k + 1] += nptr[k];
     double m0, h0, n0;
     hh_steady(v_init, &m0, &h0, &n0);
     size_t rs = (size_t)ctx->precision;
     int rd = real_dtype(ctx);
-    NW_CHECK(dev_alloc(ctx, hh.seg, 4 * std::max<int64_t>(m, 1)));
-    NW_CHECK(dev_alloc(ctx, hh.seg_ptr, 4 * (n + 1)));
-    NW_CHECK(dev_alloc(ctx, hh.neuron_ptr, 8 * (ctx->n_neuron + 1)));
+    NW_CHECK(upload_layout(ctx, L, hh.seg, hh.seg_ptr, hh.neuron_ptr));
     for (DevBuf* b : {&hh.gm, &hh.gh, &hh.gn, &hh.cna, &hh.ck, &hh.cl})
         NW_CHECK(dev_alloc(ctx, *b, rs * std::max<int64_t>(m, 1)));
-    NW_CHECK(upload_convert(ctx, hh.seg.ptr, NW_DTYPE_U32, seg.data(), NW_DTYPE_U32, m));
-    NW_CHECK(upload_convert(ctx, hh.seg_ptr.ptr, NW_DTYPE_U32, seg_ptr.data(), NW_DTYPE_U32, n + 1));
-    NW_CHECK(upload_convert(ctx, hh.neuron_ptr.ptr, NW_DTYPE_I64, nptr.data(), NW_DTYPE_I64, ctx->n_neuron + 1));
     NW_CHECK(upload_convert(ctx, hh.cna.ptr, rd, cna.data(), NW_DTYPE_F64, m));
     NW_CHECK(upload_convert(ctx, hh.ck.ptr, rd, ck.data(), NW_DTYPE_F64, m));
     NW_CHECK(upload_convert(ctx, hh.cl.ptr, rd, cl.data(), NW_DTYPE_F64, m));
@@ -548,6 +608,51 @@ int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
     NW_CHECK(upload_convert(ctx, hh.gh.ptr, rd, g0.data(), NW_DTYPE_F64, m));
     std::fill(g0.begin(), g0.end(), n0);
     NW_CHECK(upload_convert(ctx, hh.gn.ptr, rd, g0.data(), NW_DTYPE_F64, m));
+    ctx->g_valid = false;
+    return NW_OK;
+}
+
+int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
+                        const double* g_coef, int num_states, int num_open, const int32_t* open_states,
+                        double erev, const double* table, int num_buckets, int num_terms,
+                        double vmin, double bucket_frq, double conserve_sum, const double* init_state) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_kinetic_register before nw_model_init");
+    const int S = num_states, T = num_terms;
+    if (S < 1 || S > 16 || T < 1 || T > 4 || num_buckets < 1 || num_open < 1 || num_open > 4 ||
+        !open_states || !table || !init_state || !(bucket_frq > 0))
+        return fail(ctx, NW_ERR_ARG, "nw_kinetic_register: need 1<=S<=16, 1<=terms<=4, 1..4 open states, "
+                                     "a table and an initial state");
+    for (int k = 0; k < num_open; ++k)
+        if (open_states[k] < 0 || open_states[k] >= S)
+            return fail(ctx, NW_ERR_ARG, "nw_kinetic_register: open state index out of range");
+    const int64_t m = num_instances;
+    if (m < 0 || (m && (!segment || !g_coef))) return fail(ctx, NW_ERR_ARG, "nw_kinetic_register: null arrays");
+    InstanceLayout L;
+    NW_CHECK(layout_instances(ctx, m, segment, "nw_kinetic_register", L));
+    KineticState& K = ctx->kin;
+    free_kin(K);
+    K.m = m; K.S = S; K.T = T; K.nb = num_buckets; K.n_open = num_open;
+    for (int k = 0; k < num_open; ++k) K.open[k] = open_states[k];
+    K.identity = L.identity;
+    K.erev = erev; K.vmin = vmin; K.frq = bucket_frq; K.conserve = conserve_sum;
+    K.user_to_sorted = L.user_to_sorted;
+    K.h_neuron_ptr = L.nptr;
+    size_t rs = (size_t)ctx->precision;
+    int rd = real_dtype(ctx);
+    NW_CHECK(upload_layout(ctx, L, K.seg, K.seg_ptr, K.neuron_ptr));
+    NW_CHECK(dev_alloc(ctx, K.state, rs * S * std::max<int64_t>(m, 1)));
+    NW_CHECK(dev_alloc(ctx, K.gcoef, rs * std::max<int64_t>(m, 1)));
+    const int64_t tsize = (int64_t)num_buckets * S * S * T;
+    NW_CHECK(dev_alloc(ctx, K.table, rs * tsize));
+    std::vector<double> g(m), st((size_t)S * m);
+    for (int64_t s = 0; s < m; ++s) g[s] = g_coef[L.order[s]];
+    for (int c = 0; c < S; ++c)
+        for (int64_t s = 0; s < m; ++s) st[(size_t)c * m + s] = init_state[c];
+    NW_CHECK(upload_convert(ctx, K.gcoef.ptr, rd, g.data(), NW_DTYPE_F64, m));
+    NW_CHECK(upload_convert(ctx, K.state.ptr, rd, st.data(), NW_DTYPE_F64, (int64_t)S * m));
+    NW_CHECK(upload_convert(ctx, K.table.ptr, rd, table, NW_DTYPE_F64, tsize));
     ctx->g_valid = false;
     return NW_OK;
 }

@@ -35,6 +35,23 @@ struct HHState {
     DevBuf seg_ptr;             // u32 [n_seg+1] instance range of each segment
     DevBuf neuron_ptr;          // i64 [n_neuron+1] instance range of each neuron
     std::vector<int64_t> user_to_sorted;  // registration order -> device order
+    std::vector<int64_t> h_neuron_ptr;    // host copy of neuron_ptr
+};
+
+struct KineticState {
+    int64_t m = 0;
+    int S = 0, T = 0, nb = 0, n_open = 0;
+    int open[4] = {0, 0, 0, 0};
+    bool identity = false;
+    double erev = 0, vmin = 0, frq = 0, conserve = 0;
+    DevBuf seg;                 // u32 [m] segment-sorted
+    DevBuf state;               // real [S][m]
+    DevBuf gcoef;               // real [m]
+    DevBuf table;               // real [nb][S][S][T]
+    DevBuf seg_ptr;             // u32 [n_seg+1]
+    DevBuf neuron_ptr;          // i64 [n_neuron+1]
+    std::vector<int64_t> user_to_sorted;
+    std::vector<int64_t> h_neuron_ptr;
 };
 
 }  // namespace nw
@@ -69,6 +86,7 @@ struct nw_ctx {
 
     // Mechanisms.
     nw::HHState hh;
+    nw::KineticState kin;
     bool g_valid = false;       // conductances computed by a mechanism step
 
     // Clamps (sorted by neuron, stable).

@@ -79,6 +79,13 @@ struct StepArgs {
     const uint32_t* hh_seg_ptr; const int64_t* hh_neuron_ptr; const uint32_t* hh_seg;
     real* gm; real* gh; real* gn; const real* cna; const real* ck; const real* cl;
     real ena, ek, el, dtq10;
+    // kinetic scheme (lti_sim)
+    int kin_on, kin_identity, kin_S, kin_T, kin_nb, kin_nopen;
+    int kin_open[4];
+    int64_t kin_m;
+    const uint32_t* kin_seg_ptr; const int64_t* kin_neuron_ptr; const uint32_t* kin_seg;
+    real* kin_state; const real* kin_gcoef; const real* kin_table;
+    real kin_vmin, kin_frq, kin_cs, kin_erev;
     // clamps
     const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
     const int64_t* clamp_first; const int64_t* clamp_count;
@@ -99,19 +106,118 @@ struct StepArgs {
 template <typename real>
 __device__ __forceinline__ void segment_conductance(const StepArgs<real>& a, int64_t i, real& G, real& GE) {
     G = real(0); GE = real(0);
-    if (!a.hh_on) return;
-    int64_t b, e;
-    if (a.hh_identity) { b = i; e = i + 1; }
-    else { b = a.hh_seg_ptr[i]; e = a.hh_seg_ptr[i + 1]; }
-    real gna = real(0), gk = real(0), gl = real(0);
-    for (int64_t k = b; k < e; ++k) {
-        real m = a.gm[k], h = a.gh[k], n = a.gn[k];
-        gna += a.cna[k] * m * m * m * h;
-        gk += a.ck[k] * n * n * n * n;
-        gl += a.cl[k];
+    if (a.hh_on) {
+        int64_t b, e;
+        if (a.hh_identity) { b = i; e = i + 1; }
+        else { b = a.hh_seg_ptr[i]; e = a.hh_seg_ptr[i + 1]; }
+        real gna = real(0), gk = real(0), gl = real(0);
+        for (int64_t k = b; k < e; ++k) {
+            real m = a.gm[k], h = a.gh[k], n = a.gn[k];
+            gna += a.cna[k] * m * m * m * h;
+            gk += a.ck[k] * n * n * n * n;
+            gl += a.cl[k];
+        }
+        G = (gna + gk) + gl;
+        GE = (gna * a.ena + gk * a.ek) + gl * a.el;
     }
-    G = (gna + gk) + gl;
-    GE = (gna * a.ena + gk * a.ek) + gl * a.el;
+    if (a.kin_on) {
+        int64_t b, e;
+        if (a.kin_identity) { b = i; e = i + 1; }
+        else { b = a.kin_seg_ptr[i]; e = a.kin_seg_ptr[i + 1]; }
+        real gkin = real(0);
+        for (int64_t k = b; k < e; ++k) {
+            real open = real(0);
+            for (int o = 0; o < a.kin_nopen; ++o) open += a.kin_state[(int64_t)a.kin_open[o] * a.kin_m + k];
+            gkin += a.kin_gcoef[k] * open;
+        }
+        G += gkin;
+        GE += gkin * a.kin_erev;
+    }
+}
+
+// Voltage -> (bucket, location within it) as the generated lti_sim kernel
+// computes them (codegen.py:43-59): bucket = trunc((v - vmin) * frq), clamped to
+// the table, location 1 above it and 0 below it.  Non-finite voltages land in bucket 0.
+template <typename real>
+__device__ __forceinline__ int kinetic_locate(const StepArgs<real>& a, real v, real& loc) {
+    real x = (v - a.kin_vmin) * a.kin_frq;
+    if (!(x > real(-2))) x = real(-2);
+    if (x > real(a.kin_nb + 1)) x = real(a.kin_nb + 1);
+    int b = (int)x;
+    if (b > a.kin_nb - 1) { b = a.kin_nb - 1; loc = real(1); }
+    else if (b < 0) { b = 0; loc = real(0); }
+    else loc = x - real(b);
+    return b;
+}
+
+// One exact-integration step of a kinetic instance (codegen.py:60-106): the
+// polynomial approximation of the column-normalised propagator, evaluated per
+// (col, row) as table[bucket][col][row][term], times the state, then CONSERVE.
+template <typename real, int S, int T>
+__device__ __forceinline__ void kinetic_step_fixed(const StepArgs<real>& a, int64_t k, real v) {
+    real loc;
+    const int b = kinetic_locate(a, v, loc);
+    real basis[T];
+    basis[0] = real(1);
+#pragma unroll
+    for (int t = 1; t < T; ++t) basis[t] = basis[t - 1] * loc;
+    const real* __restrict__ tb = a.kin_table + (int64_t)b * (S * S * T);
+    real st[S], out[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) { st[c] = a.kin_state[(int64_t)c * a.kin_m + k]; out[c] = real(0); }
+#pragma unroll
+    for (int col = 0; col < S; ++col) {
+#pragma unroll
+        for (int row = 0; row < S; ++row) {
+            const real* p = tb + (col * S + row) * T;
+            real poly = real(0) + __ldg(p);
+#pragma unroll
+            for (int t = 1; t < T; ++t) poly += basis[t] * __ldg(p + t);
+            out[row] += poly * st[col];
+        }
+    }
+    if (a.kin_cs > real(0)) {
+        real sum = out[0];
+#pragma unroll
+        for (int c = 1; c < S; ++c) sum += out[c];
+        const real f = a.kin_cs / sum;
+#pragma unroll
+        for (int c = 0; c < S; ++c) out[c] *= f;
+    }
+#pragma unroll
+    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = out[c];
+}
+
+// Same step for any S <= 16 and T <= 4.
+template <typename real>
+__device__ __noinline__ void kinetic_step_generic(const StepArgs<real>& a, int64_t k, real v) {
+    const int S = a.kin_S, T = a.kin_T;
+    real loc;
+    const int b = kinetic_locate(a, v, loc);
+    real basis[4] = {real(1), loc, loc * loc, loc * loc * loc};
+    const real* tb = a.kin_table + (int64_t)b * (S * S * T);
+    real st[16], out[16];
+    for (int c = 0; c < S; ++c) { st[c] = a.kin_state[(int64_t)c * a.kin_m + k]; out[c] = real(0); }
+    for (int col = 0; col < S; ++col)
+        for (int row = 0; row < S; ++row) {
+            const real* p = tb + (col * S + row) * T;
+            real poly = real(0) + p[0];
+            for (int t = 1; t < T; ++t) poly += basis[t] * p[t];
+            out[row] += poly * st[col];
+        }
+    if (a.kin_cs > real(0)) {
+        real sum = out[0];
+        for (int c = 1; c < S; ++c) sum += out[c];
+        const real f = a.kin_cs / sum;
+        for (int c = 0; c < S; ++c) out[c] *= f;
+    }
+    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = out[c];
+}
+
+template <typename real>
+__device__ __forceinline__ void kinetic_step(const StepArgs<real>& a, int64_t k, real v) {
+    if (a.kin_S == 8 && a.kin_T == 2) kinetic_step_fixed<real, 8, 2>(a, k, v);
+    else kinetic_step_generic(a, k, v);
 }
 
 // Exact exponential membrane update of one segment (electric.py:60-76).
@@ -241,12 +347,19 @@ batched_advance_kernel(const StepArgs<real> a) {
         }
         __syncthreads();
         const int nclamp = s_nclamp;
-        // Mechanism instance range of this neuron.
-        int64_t ib = 0, ie = 0;
+        // Mechanism instance ranges of this neuron.
+        int64_t ib = 0, ie = 0, kb = 0, ke = 0;
         if (a.hh_on) {
             if (a.hh_identity) { ib = base; ie = base + n; }
             else { ib = a.hh_neuron_ptr[j]; ie = a.hh_neuron_ptr[j + 1]; }
         }
+        if (a.kin_on) {
+            if (a.kin_identity) { kb = base; ke = base + n; }
+            else { kb = a.kin_neuron_ptr[j]; ke = a.kin_neuron_ptr[j + 1]; }
+        }
+        // With one instance per segment the thread that updates a segment's
+        // instances is the one that gathers them next; otherwise synchronise.
+        const bool mech_sync = (a.hh_on && !a.hh_identity) || (a.kin_on && !a.kin_identity);
         // AP detector state lives in thread 0's registers across the K steps.
         bool ap_state = false, ap_det = false;
         uint32_t spikes = 0;
@@ -287,7 +400,11 @@ batched_advance_kernel(const StepArgs<real> a) {
                             a.gm[k] = m; a.gh[k] = h; a.gn[k] = nn;
                         }
                     }
-                    if (!a.hh_identity) __syncthreads();
+                    if (a.kin_on) {
+                        for (int64_t k = kb + tid; k < ke; k += nthr)
+                            kinetic_step(a, k, a.V[a.kin_identity ? k : (int64_t)a.kin_seg[k]]);
+                    }
+                    if (mech_sync) __syncthreads();
                 }
             }
             // AP detector (neuron.py:184-188) and probes after the full step.
@@ -351,6 +468,13 @@ __global__ void plain_hh_kernel(const StepArgs<real> a, int64_t ib, int64_t ie) 
 }
 
 template <typename real>
+__global__ void plain_kinetic_kernel(const StepArgs<real> a, int64_t kb, int64_t ke) {
+    int64_t k = kb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= ke) return;
+    kinetic_step_generic(a, k, a.V[a.kin_identity ? k : (int64_t)a.kin_seg[k]]);
+}
+
+template <typename real>
 __global__ void plain_detect_kernel(const StepArgs<real> a, int64_t row) {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j < a.n_neuron && a.has_det) {
@@ -391,6 +515,16 @@ static StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.gm = hh.gm.as<real>(); a.gh = hh.gh.as<real>(); a.gn = hh.gn.as<real>();
     a.cna = hh.cna.as<real>(); a.ck = hh.ck.as<real>(); a.cl = hh.cl.as<real>();
     a.ena = (real)hh.ena; a.ek = (real)hh.ek; a.el = (real)hh.el;
+    const KineticState& K = ctx->kin;
+    a.kin_on = K.m > 0 ? 1 : 0;
+    a.kin_identity = K.identity ? 1 : 0;
+    a.kin_S = K.S; a.kin_T = K.T; a.kin_nb = K.nb; a.kin_nopen = K.n_open;
+    for (int o = 0; o < 4; ++o) a.kin_open[o] = K.open[o];
+    a.kin_m = K.m;
+    a.kin_seg_ptr = K.seg_ptr.as<uint32_t>(); a.kin_neuron_ptr = K.neuron_ptr.as<int64_t>();
+    a.kin_seg = K.seg.as<uint32_t>();
+    a.kin_state = K.state.as<real>(); a.kin_gcoef = K.gcoef.as<real>(); a.kin_table = K.table.as<real>();
+    a.kin_vmin = (real)K.vmin; a.kin_frq = (real)K.frq; a.kin_cs = (real)K.conserve; a.kin_erev = (real)K.erev;
     const double q10 = pow(3.0, (ctx->celsius - 6.3) / 10.0);      // hh.mod:67
     a.dtq10 = (real)(ctx->time_step * q10);
     if (ctx->n_clamps) {
@@ -461,7 +595,7 @@ static void finish_steps(nw_ctx* ctx, int k_steps) {
     ctx->input_ticks += 2 * (int64_t)k_steps;
     ctx->steps += k_steps;
     if (ctx->n_probes) ctx->probe_len += k_steps;
-    if (ctx->hh.m > 0) ctx->g_valid = true;
+    if (ctx->hh.m > 0 || ctx->kin.m > 0) ctx->g_valid = true;
 }
 
 int advance_batched(nw_ctx* ctx, int k_steps) {
@@ -488,24 +622,21 @@ static int plain_steps(nw_ctx* ctx, int k_steps) {
                 plain_prepare_kernel<real><<<blocks, T, 0, ctx->stream>>>(a, (int)j, base, n, tick, gv, last);
                 plain_spmv_kernel<real><<<blocks, T, 0, ctx->stream>>>(a, base, n);
             }
-            if (half == 0 && ctx->hh.m > 0) {
-                std::vector<int64_t> nptr(ctx->n_neuron + 1);
-                // Instance ranges per neuron (identity: the neuron's segments).
+            if (half == 0) {
                 for (int64_t j = 0; j < ctx->n_neuron; ++j) {
-                    int64_t ib, ie;
-                    if (ctx->hh.identity) { ib = ctx->h_neuron_start[j]; ie = ctx->h_neuron_start[j + 1]; }
-                    else {
-                        // Whole range in one launch when instances are not segment-aligned.
-                        if (j > 0) break;
-                        ib = 0; ie = ctx->hh.m;
+                    if (ctx->hh.m > 0) {
+                        const int64_t ib = ctx->hh.h_neuron_ptr[j], ie = ctx->hh.h_neuron_ptr[j + 1];
+                        if (ie > ib)
+                            plain_hh_kernel<real><<<(unsigned)((ie - ib + T - 1) / T), T, 0, ctx->stream>>>(a, ib, ie);
                     }
-                    if (ie > ib) {
-                        int64_t blocks = (ie - ib + T - 1) / T;
-                        plain_hh_kernel<real><<<(unsigned)blocks, T, 0, ctx->stream>>>(a, ib, ie);
+                    if (ctx->kin.m > 0) {
+                        const int64_t kb = ctx->kin.h_neuron_ptr[j], ke = ctx->kin.h_neuron_ptr[j + 1];
+                        if (ke > kb)
+                            plain_kinetic_kernel<real><<<(unsigned)((ke - kb + T - 1) / T), T, 0, ctx->stream>>>(a, kb, ke);
                     }
                 }
             }
-            ctx->g_valid = ctx->g_valid || ctx->hh.m > 0;
+            ctx->g_valid = ctx->g_valid || ctx->hh.m > 0 || ctx->kin.m > 0;
         }
         int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
         StepArgs<real> d = make_args<real>(ctx, 1);

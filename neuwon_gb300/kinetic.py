@@ -1,0 +1,228 @@
+"""Linear kinetic schemes solved by exact integration with voltage tables.
+
+Restates the reference's lti_sim pipeline (neuwon/rxd/lti_sim/):
+
+* the propagator of one step is expm(A(v) dt) with every column renormalised
+  to sum to 1 (lti_model.py:51-65);
+* the input range is cut into equal buckets (inputs.py:150-161) and, in every
+  bucket, each matrix entry is fitted by least squares with a polynomial in
+  the location within the bucket (approx.py:159-174, polynomial.py:3-20);
+* at run time an instance locates its voltage, evaluates the polynomials and
+  multiplies its state vector, then rescales the states to the CONSERVE sum
+  (codegen.py:39-106).  The table is stored as [bucket][col][row][term]
+  (codegen.py:29-37).
+
+The exact matrices are sampled at deterministic points (the midpoints of
+``samples_per_bucket`` equal sub-buckets) instead of the reference's one
+random point per sub-bucket; ``build_table(sample_inputs=...)`` accepts the
+reference's own sample points to reproduce its table.
+
+The 8-state sodium scheme ``na8`` is the Markov form of the Hodgkin-Huxley
+sodium channel: states (k, h) with k = 0..3 open m-gates and h = 1 (available)
+or 0 (inactivated); k -> k+1 at (3-k) alpha_m, k+1 -> k at (k+1) beta_m,
+available -> inactivated at beta_h, back at alpha_h, rates of
+nmodl_library/artificial/hh.mod scaled by q10.  Started from the binomial
+distribution of (m, h), its open state (3, 1) equals m^3 h exactly.
+"""
+import math
+
+import numpy as np
+import scipy.linalg
+
+from .mechanisms import Mechanism
+
+
+class KineticScheme:
+    """A linear kinetic scheme dS/dt = A(v) S."""
+
+    def __init__(self, name, states, transitions, open_states, conserve_sum=1.0):
+        """transitions(v, celsius) -> list of (src, dst, rate) with numpy rates."""
+        self.name = str(name)
+        self.states = list(states)
+        self.num_states = len(self.states)
+        self.transitions = transitions
+        self.open_states = [self.states.index(s) for s in open_states]
+        self.conserve_sum = conserve_sum
+
+    def matrix(self, v, celsius):
+        """A(v) for an array of voltages: shape (len(v), S, S)."""
+        v = np.atleast_1d(np.asarray(v, dtype=np.float64))
+        S = self.num_states
+        A = np.zeros((len(v), S, S))
+        for src, dst, rate in self.transitions(v, celsius):
+            A[:, dst, src] += rate
+            A[:, src, src] -= rate
+        return A
+
+    def exact_propagator(self, v, dt, celsius):
+        """expm(A(v) dt) with columns renormalised to sum 1 (lti_model.py:51-65)."""
+        M = scipy.linalg.expm(self.matrix(v, celsius) * dt)
+        M /= M.sum(axis=1, keepdims=True)
+        return M
+
+    def steady_state(self, v, celsius):
+        """State after a very long time at voltage v, scaled to the conserve sum."""
+        M = scipy.linalg.expm(self.matrix([v], celsius)[0] * 3600e3)
+        s = M @ np.full(self.num_states, (self.conserve_sum or 1.0) / self.num_states)
+        return s
+
+
+def _vtrap(x, y):
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        big = x / (np.exp(x / y) - 1.0)
+    return np.where(np.abs(x / y) < 1e-6, y * (1.0 - x / y / 2.0), big)
+
+
+def hh_sodium_rates(v, celsius):
+    """alpha/beta of the m and h gates (hh.mod:62-86), times q10."""
+    q10 = 3.0 ** ((celsius - 6.3) / 10.0)
+    am = 0.1 * _vtrap(-(v + 40.0), 10.0)
+    bm = 4.0 * np.exp(-(v + 65.0) / 18.0)
+    ah = 0.07 * np.exp(-(v + 65.0) / 20.0)
+    bh = 1.0 / (np.exp(-(v + 35.0) / 10.0) + 1.0)
+    return q10 * am, q10 * bm, q10 * ah, q10 * bh
+
+
+def na8():
+    states = ["C3", "C2", "C1", "O", "I3", "I2", "I1", "I"]   # (k, h): k = index % 4, h = index < 4
+
+    def transitions(v, celsius):
+        am, bm, ah, bh = hh_sodium_rates(v, celsius)
+        out = []
+        for row in (0, 4):
+            for k in range(3):
+                out.append((row + k, row + k + 1, (3 - k) * am))
+                out.append((row + k + 1, row + k, (k + 1) * bm))
+        for k in range(4):
+            out.append((k, 4 + k, bh))
+            out.append((4 + k, k, ah))
+        return out
+    return KineticScheme("na8", states, transitions, open_states=["O"], conserve_sum=1.0)
+
+
+def binomial_state(m, h):
+    """Na8 occupancy equivalent to HH gates (m, h)."""
+    s = np.zeros(8)
+    for k in range(4):
+        p = math.comb(3, k) * m ** k * (1 - m) ** (3 - k)
+        s[k] = p * h
+        s[4 + k] = p * (1 - h)
+    return s
+
+
+class LTITable:
+    """Voltage-bucketed polynomial approximation of the per-step propagator."""
+
+    def __init__(self, scheme, dt, celsius, vmin=-100.0, vmax=60.0, num_buckets=1600, degree=1,
+                 samples_per_bucket=20, sample_inputs=None):
+        self.scheme = scheme
+        self.dt, self.celsius = float(dt), float(celsius)
+        self.vmin, self.vmax = float(vmin), float(vmax)
+        self.num_buckets = int(num_buckets)
+        self.num_terms = int(degree) + 1
+        self.bucket_frq = self.num_buckets / (self.vmax - self.vmin)       # inputs.py:152-155
+        self.bucket_width = (self.vmax - self.vmin) / self.num_buckets
+        S, T, nb = scheme.num_states, self.num_terms, self.num_buckets
+        if sample_inputs is None:
+            sub = (np.arange(samples_per_bucket) + 0.5) / samples_per_bucket
+            loc = (np.arange(nb)[:, None] + sub[None, :]).ravel()
+            sample_inputs = self.vmin + loc * self.bucket_width
+        v = np.asarray(sample_inputs, dtype=np.float64)
+        exact = scheme.exact_propagator(v, self.dt, self.celsius)             # (n, S, S)
+        pos = (v - self.vmin) * self.bucket_frq
+        bucket = pos.astype(np.int32)                                         # approx.py:16-18
+        order = np.argsort(bucket, kind="stable")
+        bucket, pos, exact = bucket[order], pos[order], exact[order]
+        table = np.empty((nb, S, S, T))
+        bounds = np.searchsorted(bucket, np.arange(nb + 1))
+        for b in range(nb):
+            lo, hi = bounds[b], bounds[b + 1]
+            loc = pos[lo:hi] - b
+            A = loc[:, None] ** np.arange(T)[None, :]
+            B = exact[lo:hi].reshape(-1, S * S)
+            coef = np.linalg.lstsq(A, B, rcond=None)[0]
+            table[b] = coef.reshape(T, S, S).transpose(1, 2, 0)
+        self.table = table                                   # [bucket][row][col][term]
+        self.layout = np.ascontiguousarray(table.transpose(0, 2, 1, 3))   # [bucket][col][row][term]
+
+    def locate(self, v):
+        """Bucket index and location, as the generated kernel computes them (codegen.py:43-59)."""
+        x = (np.asarray(v, dtype=np.float64) - self.vmin) * self.bucket_frq
+        b = np.trunc(x).astype(np.int64)
+        loc = x - b
+        hi = b > self.num_buckets - 1
+        lo = b < 0
+        b = np.where(hi, self.num_buckets - 1, np.where(lo, 0, b))
+        loc = np.where(hi, 1.0, np.where(lo, 0.0, loc))
+        return b, loc
+
+    def advance(self, v, states):
+        """One step for arrays of instances: states (n, S) -> new states (codegen.py:74-106)."""
+        b, loc = self.locate(v)
+        basis = loc[:, None] ** np.arange(self.num_terms)[None, :]           # (n, T)
+        M = np.einsum("ncrt,nt->nrc", self.layout[b], basis)                  # (n, row, col)
+        new = np.einsum("nrc,nc->nr", M, states)
+        cs = self.scheme.conserve_sum
+        if cs is not None:
+            new *= (cs / new.sum(axis=1))[:, None]
+        return new
+
+    def max_error(self, samples=64):
+        """Max |table - exact| over points spread through every bucket."""
+        sub = (np.arange(samples) + 0.37) / samples
+        v = (self.vmin + (np.arange(self.num_buckets)[:, None] + sub[None, :]) * self.bucket_width).ravel()
+        exact = self.scheme.exact_propagator(v, self.dt, self.celsius)
+        b, loc = self.locate(v)
+        basis = loc[:, None] ** np.arange(self.num_terms)[None, :]
+        approx = np.einsum("nrct,nt->nrc", self.table[b], basis)
+        return float(np.abs(approx - exact).max())
+
+
+class Kinetic(Mechanism):
+    """A kinetic-scheme channel with one nonspecific conductance.
+
+    conductance = gbar[S/cm2] * 1e-8 * magnitude[um2] * sum(open states), reversal
+    potential ``erev``; the step uses an ``LTITable`` built for the model's dt and
+    temperature when the model is first advanced.
+    """
+    name = "na8"
+    scheme_factory = staticmethod(na8)
+    gbar = 0.012
+    erev = 50.0
+    vmin, vmax, num_buckets, degree = -100.0, 60.0, 1600, 1
+    _model = None
+
+    @classmethod
+    def configure(cls, **params):
+        ok = {"name", "scheme_factory", "gbar", "erev", "vmin", "vmax", "num_buckets", "degree"}
+        bad = set(params) - ok
+        if bad:
+            raise ValueError(f"unknown kinetic parameters {sorted(bad)}")
+        if "scheme_factory" in params:
+            params["scheme_factory"] = staticmethod(params["scheme_factory"])
+        return type(cls.__name__, (cls,), dict(params))
+
+    @classmethod
+    def initialize(cls, model):
+        return type(cls.__name__, (cls,), {"_model": model})
+
+    @classmethod
+    def get_name(cls):
+        return cls.name
+
+    def __init__(self, segment, outside=None, magnitude=1.0, *other_mechanisms, gbar=None):
+        model = type(self)._model
+        if model is None:
+            raise TypeError("mechanism class is not bound to a model; use model.mechanisms[name]")
+        self.segment = segment
+        self.magnitude = float(magnitude)
+        self.index = model._add_kinetic_instances(type(self), np.array([segment._idx]),
+                                                  np.array([self.magnitude]), gbar)
+
+    @classmethod
+    def get_database_class(cls):
+        return cls
+
+    @classmethod
+    def build_table(cls, dt, celsius):
+        return LTITable(cls.scheme_factory(), dt, celsius, cls.vmin, cls.vmax, cls.num_buckets, cls.degree)

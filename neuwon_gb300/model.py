@@ -21,6 +21,7 @@ import numpy as np
 
 from . import _lib
 from .morphology import EPSILON, Tree, geometry, passive_electric
+from .kinetic import Kinetic
 from .mechanisms import HH, Mechanism
 
 
@@ -358,7 +359,10 @@ class RxD_Model:
         """Insert mechanism ``name`` on every segment (one vectorised call)."""
         cls = self.mechanisms[name]
         segs = np.arange(self._n, dtype=np.int64)
-        self._add_instances_bulk(cls, segs, np.full(self._n, float(magnitude)), per_instance)
+        if issubclass(cls, Kinetic):
+            self._add_kinetic_instances(cls, segs, np.full(self._n, float(magnitude)), per_instance.get("gbar"))
+        else:
+            self._add_instances_bulk(cls, segs, np.full(self._n, float(magnitude)), per_instance)
 
     def advance(self, k_steps=1):
         """rxd_model.py:63-80, k_steps times, as one device launch."""
@@ -384,6 +388,9 @@ class RxD_Model:
         self._sync()
         cls = self.mechanisms[mech]
         n = self._instance_count(cls.get_name())
+        if issubclass(cls, Kinetic):
+            S = len(cls.scheme_factory().states)
+            return self._ctx.get_data("kinetic.state", n * S).reshape(n, S)
         return self._ctx.get_data(f"hh.{attr}", n)
 
     def close(self):
@@ -399,15 +406,17 @@ class RxD_Model:
         if not (isinstance(mechanism, type) and issubclass(mechanism, Mechanism)):
             raise TypeError(f"not a Mechanism subclass: {mechanism!r}")
         bound = mechanism.initialize(self) or mechanism
-        if not issubclass(bound, HH):
+        if not issubclass(bound, (HH, Kinetic)):
             raise NotImplementedError(f"mechanism {bound.get_name()} has no GPU kernel")
         name = bound.get_name()
         if name in self.mechanisms:
             raise ValueError(f"duplicate mechanism {name}")
-        if any(issubclass(c, HH) for c in self.mechanisms.values()):
-            raise NotImplementedError("one HH mechanism per model")
+        for kind in (HH, Kinetic):
+            if issubclass(bound, kind) and any(issubclass(c, kind) for c in self.mechanisms.values()):
+                raise NotImplementedError(f"one {kind.__name__} mechanism per model")
         self.mechanisms[name] = bound
-        self._mech_instances[name] = {"seg": [], "mag": [], "n_at": [], "gnabar": [], "gkbar": [], "glbar": []}
+        self._mech_instances[name] = {"seg": [], "mag": [], "n_at": [], "gnabar": [], "gkbar": [],
+                                      "glbar": [], "gbar": []}
 
     def _grow(self, extra):
         need = self._n + extra
@@ -485,6 +494,18 @@ class RxD_Model:
             rec[key].append(arr)
         self._dirty_structure = True
 
+    def _add_kinetic_instances(self, cls, segs, mags, gbar):
+        rec = self._mech_instances[cls.get_name()]
+        segs = np.asarray(segs, dtype=np.int64)
+        m = len(segs)
+        rec["seg"].append(segs)
+        rec["mag"].append(np.broadcast_to(np.asarray(mags, dtype=np.float64), (m,)).copy())
+        rec["n_at"].append(np.full(m, self._n, dtype=np.int64))
+        rec["gbar"].append(np.full(m, np.nan) if gbar is None
+                           else np.broadcast_to(np.asarray(gbar, np.float64), (m,)).copy())
+        self._dirty_structure = True
+        return self._instance_count(cls.get_name()) - 1
+
     def _add_clamp(self, seg, amps, first_tick, count):
         self._clamps.append((int(seg), float(amps), int(first_tick), int(count)))
         self._dirty_clamps = True
@@ -545,7 +566,10 @@ class RxD_Model:
             ctx.call("nw_propagator_conserve")
         self.propagator_nnz = nnz.value
         for name, cls in self.mechanisms.items():
-            self._sync_hh(cls)
+            if issubclass(cls, Kinetic):
+                self._sync_kinetic(cls)
+            else:
+                self._sync_hh(cls)
         self._dirty_structure = False
         self._dirty_clamps = self._dirty_detectors = self._dirty_probes = True
         if saved is not None:
@@ -577,6 +601,39 @@ class RxD_Model:
         self._ctx.call("nw_hh_register", len(seg), _lib.ptr(seg_dev),
                        _lib.ptr(gna), _lib.ptr(gk), _lib.ptr(gl),
                        float(cls.ena), float(cls.ek), float(cls.el), self.initial_voltage)
+
+    def _insertion_magnitude(self, rec):
+        cat = lambda key, dt: (np.concatenate(rec[key]) if rec[key] else np.empty(0, dt))
+        seg = cat("seg", np.int64)
+        mag = cat("mag", np.float64)
+        n_at = cat("n_at", np.int64)
+        area = np.empty(len(seg))
+        for k in np.unique(n_at):
+            sel = n_at == k
+            area[sel] = self._area_at(int(k))[seg[sel]]
+        return seg, mag * area                                 # nmodl/__init__.py:496-500
+
+    def _sync_kinetic(self, cls):
+        rec = self._mech_instances[cls.get_name()]
+        seg, magnitude = self._insertion_magnitude(rec)
+        gbar = np.concatenate(rec["gbar"]) if rec["gbar"] else np.empty(0)
+        gbar = np.where(np.isnan(gbar), cls.gbar, gbar)
+        g = np.ascontiguousarray(gbar * 1e-8 * magnitude)
+        key = (cls, self.time_step, self.temperature)
+        cache = getattr(self, "_tables", {})
+        if key not in cache:
+            cache[key] = cls.build_table(self.time_step, self.temperature)
+        self._tables = cache
+        tbl = cache[key]
+        sch = tbl.scheme
+        init = np.ascontiguousarray(sch.steady_state(self.initial_voltage, self.temperature))
+        open_idx = np.asarray(sch.open_states, dtype=np.int32)
+        layout = np.ascontiguousarray(tbl.layout.ravel())
+        seg_dev = np.ascontiguousarray(self._inv[seg]) if len(seg) else seg
+        cs = float(sch.conserve_sum) if sch.conserve_sum is not None else 0.0
+        self._ctx.call("nw_kinetic_register", len(seg), _lib.ptr(seg_dev), _lib.ptr(g), sch.num_states,
+                       len(open_idx), _lib.ptr(open_idx), float(cls.erev), _lib.ptr(layout),
+                       tbl.num_buckets, tbl.num_terms, tbl.vmin, tbl.bucket_frq, cs, _lib.ptr(init))
 
     def _sync_clamps(self):
         c = self._clamps

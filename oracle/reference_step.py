@@ -144,6 +144,60 @@ class HHInstances:
         self.g["l"] += self.gl_coef
 
 
+class KineticInstances:
+    """Instances of one lti_sim kinetic mechanism, stepped as the kernel that
+    neuwon/rxd/lti_sim/codegen.py:39-106 generates, with its conductance
+    gbar*magnitude*(open states) written by the BREAKPOINT block after the
+    LTI call (nmodl/__init__.py:415-429) as a nonspecific conductance.
+
+    ``layout`` is the flattened table [bucket][col][row][term] (codegen.py:29-37)."""
+
+    def __init__(self, segment, g_coef, layout, vmin, bucket_frq, open_states, erev,
+                 conserve_sum, init_state):
+        self.segment = np.asarray(segment, dtype=np.int64)
+        m = len(self.segment)
+        self.g_coef = np.broadcast_to(np.asarray(g_coef, np.float64), (m,)).copy()
+        self.layout = np.asarray(layout, dtype=np.float64)
+        self.nb, S, S2, self.T = self.layout.shape
+        assert S == S2
+        self.S = S
+        self.vmin, self.frq = float(vmin), float(bucket_frq)
+        self.open_states = list(open_states)
+        self.erev = float(erev)
+        self.conserve_sum = conserve_sum
+        self.state = np.tile(np.asarray(init_state, dtype=np.float64), (m, 1))   # [inst][state]
+        self.g = np.zeros(m)
+
+    def zero_accumulators(self):
+        self.g.fill(0.0)
+
+    def advance(self, voltage):
+        v = voltage[self.segment]
+        inp = (v - self.vmin) * self.frq                         # codegen.py:45
+        bucket = np.trunc(inp).astype(np.int64)                  # int(input0)
+        hi = bucket > self.nb - 1
+        lo = (~hi) & (bucket < 0)
+        loc = np.where(hi, 1.0, np.where(lo, 0.0, inp - bucket))
+        bucket = np.where(hi, self.nb - 1, np.where(lo, 0, bucket))
+        tbl = self.layout[bucket]                                # [inst][col][row][term]
+        terms = [None] + [loc ** p for p in range(1, self.T)]
+        scratch = np.zeros((len(v), self.S))
+        for col in range(self.S):
+            s = self.state[:, col]
+            for row in range(self.S):
+                poly = 0.0 + tbl[:, col, row, 0]
+                for t in range(1, self.T):
+                    poly = poly + terms[t] * tbl[:, col, row, t]
+                scratch[:, row] += poly * s
+        if self.conserve_sum is not None:
+            total = scratch[:, 0].copy()
+            for x in range(1, self.S):
+                total += scratch[:, x]
+            scratch *= (self.conserve_sum / total)[:, None]
+        self.state = scratch
+        self.g += self.g_coef * self.state[:, self.open_states].sum(axis=1)
+
+
 class OracleModel:
     """FP64 restatement of ``RxD_Model.advance()`` (neuwon/rxd/rxd_model.py:63-80).
 
@@ -160,7 +214,7 @@ class OracleModel:
 
     def __init__(self, parent, R, C, *, time_step=0.1, celsius=6.3, v_init=-70.0,
                  prune=EPSILON, propagator_matrix=None, hh=None, clamps=(),
-                 detectors=(), duplicates="sum"):
+                 detectors=(), duplicates="sum", kinetic=None):
         self.parent = np.asarray(parent, dtype=np.int64)
         self.n = len(self.parent)
         self.R = np.asarray(R, dtype=np.float64)
@@ -177,6 +231,7 @@ class OracleModel:
         self.P = propagator_matrix if propagator_matrix is not None else \
             propagator(self.parent, self.R, self.C, self.half_step, prune)
         self.hh = hh
+        self.kinetic = kinetic
         self.clamps = [(int(s), float(a), int(f), int(k)) for (s, a, f, k) in clamps]
         self.detectors = [(int(s), float(t)) for (s, t) in detectors]
         self.AP_detected = np.zeros(len(self.detectors), dtype=bool)
@@ -201,6 +256,10 @@ class OracleModel:
                 else:
                     np.add.at(self.sum_conductance, seg, g)
                     np.add.at(self.driving_voltage, seg, g * self.hh.E[ion])
+        if self.kinetic is not None:
+            k = self.kinetic
+            np.add.at(self.sum_conductance, k.segment, k.g)
+            np.add.at(self.driving_voltage, k.segment, k.g * k.erev)
         # input_hook.tick(): Clock.tick then TimeSeries._play_implementation
         # (database/time.py:114-117, 287-302), current clamps in "+=" mode.
         self.input_ticks += 1
@@ -230,6 +289,9 @@ class OracleModel:
         if self.hh is not None:
             self.hh.zero_accumulators()
             self.hh.advance(self.voltage, self.time_step, self.celsius)
+        if self.kinetic is not None:
+            self.kinetic.zero_accumulators()
+            self.kinetic.advance(self.voltage)
 
     # neuwon/rxd/neuron/neuron.py:184-188
     def _advance_AP_detector(self):

@@ -256,6 +256,35 @@ def run_hh_tree(out, prefix, trees, *, time_step, celsius, t_stop, clamps, hh_kw
     out[prefix + "_meta"] = np.array([time_step, celsius, t_stop])
 
 
+def run_lti(out):
+    """The reference's lti_sim table builder (approx.py) on the 8-state sodium scheme."""
+    np.random.seed(1234)
+    if not hasattr(np, "product"):
+        np.product = np.prod            # removed in numpy 2; used by approx.py:81
+    from neuwon.rxd.lti_sim import LTI_Model, LinearInput
+    from neuwon.rxd.lti_sim.approx import Approx1D, MatrixSamples
+    from neuwon_gb300.kinetic import na8
+    sch = na8()
+
+    def derivative(v, *state):
+        return list(sch.matrix([v], 6.3)[0] @ np.array(state))
+    inp = LinearInput('v', 'self.segment.voltage', -100, 60)
+    model = LTI_Model('na8', [inp], sch.states, derivative, 1.0, 0.1)
+    inp.set_num_buckets(1600)
+    samples = MatrixSamples(model)
+    approx = Approx1D(samples, 1)
+    out["lti_table"] = approx.table
+    out["lti_samples"] = samples.inputs[0]
+    rng = np.random.default_rng(5)
+    v = np.concatenate([rng.uniform(-110, 70, 300), [-100.0, -100.05, -100.2, 60.0, 75.0, -99.95]])
+    st = rng.dirichlet(np.ones(8), len(v))
+    new = []
+    for vi, si in zip(v, st):
+        x = approx.approximate_matrix(vi) @ si
+        new.append(x * (1.0 / x.sum()))          # CONSERVE, codegen.py:95-102
+    out["lti_v"], out["lti_state"], out["lti_new"] = v, st, np.array(new)
+
+
 def main():
     install_stubs()
     from neuwon_gb300.morphology import random_tree, Tree
@@ -284,6 +313,8 @@ def main():
                 hh_kwargs=dict(ena=50.0, ek=-77.0),
                 probes=[0, 10, 40, 45, 65, 95, 124], snapshots={150},
                 duplicate_segments=[(0, 3), (2, 30)])
+
+    run_lti(out)
 
     path = os.path.join(HERE, "reference_fixtures.npz")
     np.savez_compressed(path, **out)

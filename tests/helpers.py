@@ -27,8 +27,19 @@ def concat(trees):
     return np.concatenate(parents), R, C, area, offs
 
 
+def kinetic_oracle(seg, area, time_step, celsius, gbar=0.012, erev=50.0, v_init=-70.0):
+    """Na8 instances for the oracle, with the table and initial state the model uses."""
+    from neuwon_gb300.kinetic import LTITable, na8
+    from oracle.reference_step import KineticInstances
+    sch = na8()
+    tbl = LTITable(sch, time_step, celsius)
+    init = sch.steady_state(v_init, celsius)
+    return KineticInstances(seg, gbar * 1e-8 * area[seg], tbl.layout, tbl.vmin, tbl.bucket_frq,
+                            sch.open_states, erev, sch.conserve_sum, init)
+
+
 def oracle_case(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(),
-                duplicates="sum", prune=None, insert_as_created=False):
+                duplicates="sum", prune=None, insert_as_created=False, kinetic=False):
     """clamps: [(tree, seg, nA, start_ms, dur_ms)]; dups: [(tree, seg)] extra hh instances.
 
     insert_as_created: instance magnitudes use each segment's area as a leaf
@@ -46,19 +57,22 @@ def oracle_case(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(
         cl.append((offs[ti] + s, nA * 1e-9, f, c))
     det = [(o, 20.0) for o in offs]
     kw = {} if prune is None else {"prune": prune}
+    if kinetic:
+        kw["kinetic"] = kinetic_oracle(np.arange(n), area, time_step, celsius)
     om = OracleModel(parent, R, C, time_step=time_step, celsius=celsius, hh=hh, clamps=cl,
                      detectors=det, duplicates=duplicates, **kw)
     return om, dict(parent=parent, R=R, C=C, area=area, offs=offs, seg=seg, clamps=cl)
 
 
 def gpu_model(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(), precision="f32",
-              path="batched", tolerance=None, probes=(), insert_as_created=False):
+              path="batched", tolerance=None, probes=(), insert_as_created=False, kinetic=False):
     """The same case through the public RxD_Model API."""
     import neuwon_gb300 as nw
     hh_kw = dict(hh_kw or {})
     kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
+    mechs = [nw.HH.configure(**hh_kw)] + ([nw.Kinetic] if kinetic else [])
     m = nw.RxD_Model(time_step=time_step, temperature=celsius, precision=precision, path=path,
-                     mechanisms=[nw.HH.configure(**hh_kw)], **kw)
+                     mechanisms=mechs, **kw)
     hh = m.mechanisms["hh"]
     if insert_as_created:
         neurons = []
@@ -75,6 +89,8 @@ def gpu_model(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(),
     else:
         neurons = [m.add_tree(t) for t in trees]
         m.insert_everywhere("hh")
+        if kinetic:
+            m.insert_everywhere("na8")
     offs = np.cumsum([0] + [len(t) for t in trees])[:-1]
     for (ti, s) in dups:
         hh(nw.Segment(m, offs[ti] + s))

@@ -222,3 +222,46 @@ def test_bad_propagator_rejected():
     val = np.ones(n)
     with pytest.raises(_lib.NeuwonError, match="couples two neurons"):
         ctx.call("nw_propagator_set_csr", n, _lib.ptr(rowptr), _lib.ptr(col), _lib.ptr(val), n)
+
+
+@pytest.mark.parametrize("path", ["batched", "plain"])
+def test_f64_hh_plus_na8_kinetic_matches_oracle(path):
+    """HH + the 8-state Markov sodium scheme (voltage-table LTI step) vs the oracle."""
+    trees = [random_tree(150, seed=31), random_tree(90, seed=32)]
+    clamps = [(0, 0, 0.3, 1.0, 8.0), (1, 4, 0.2, 0.5, 5.0)]
+    hh_kw = dict(ena=50., ek=-77.)
+    om, _ = oracle_case(trees, clamps, hh_kw=hh_kw, kinetic=True)
+    m, neurons, offs, _ = gpu_model(trees, clamps, hh_kw=hh_kw, precision="f64", path=path, kinetic=True)
+    worst = 0.0
+    for k in range(120):
+        for (ti, s, nA, start, dur) in clamps:
+            if m.clock.is_now(start):
+                nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance()
+        om.advance()
+        if k % 20 == 19:
+            worst = max(worst, np.abs(m.get_data("Segment.voltage") - om.voltage).max())
+    assert worst < 1e-7
+    st = m.get_data("na8.state")
+    assert np.abs(st - om.kinetic.state).max() < 1e-9
+    np.testing.assert_array_equal(m.get_data("Neuron.spike_count"), om.spike_count)
+    m.close()
+
+
+def test_f32_hh_plus_na8_within_bound():
+    trees = [random_tree(400, seed=41)]
+    clamps = [(0, 0, 0.4, 0.0, 30.0)]
+    om, _ = oracle_case(trees, clamps, hh_kw=dict(ena=50., ek=-77.), kinetic=True)
+    m, neurons, offs, _ = gpu_model(trees, clamps, hh_kw=dict(ena=50., ek=-77.), precision="f32", kinetic=True)
+    worst = 0.0
+    for k in range(300):
+        for (ti, s, nA, start, dur) in clamps:
+            if m.clock.is_now(start):
+                nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance()
+        om.advance()
+        if k % 10 == 9:
+            worst = max(worst, np.abs(m.get_data("Segment.voltage") - om.voltage).max())
+    assert worst < 0.1, worst
+    np.testing.assert_array_equal(m.get_data("Neuron.spike_count"), om.spike_count)
+    m.close()

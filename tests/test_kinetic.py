@@ -1,0 +1,72 @@
+"""Kinetic schemes (lti_sim): the table builder and run-time step against the
+reference's own lti_sim output, and the 8-state sodium scheme against HH."""
+import numpy as np
+import pytest
+import scipy.linalg
+
+from neuwon_gb300.kinetic import LTITable, binomial_state, hh_sodium_rates, na8
+from oracle.reference_step import KineticInstances, hh_rates
+from tests.helpers import FIXTURES
+
+F = np.load(FIXTURES)
+
+
+def test_table_matches_reference_lti_sim():
+    """Same sample points as the reference's MatrixSamples -> same least-squares table."""
+    t = LTITable(na8(), 0.1, 6.3, sample_inputs=F["lti_samples"])
+    assert np.abs(t.table - F["lti_table"]).max() < 1e-13
+
+
+def test_runtime_step_matches_reference_approximation():
+    t = LTITable(na8(), 0.1, 6.3, sample_inputs=F["lti_samples"])
+    new = t.advance(F["lti_v"], F["lti_state"])
+    assert np.abs(new - F["lti_new"]).max() < 1e-14
+
+
+def test_oracle_kinetic_step_matches_reference():
+    """The oracle's codegen restatement on the reference's own table."""
+    sch = na8()
+    layout = F["lti_table"].transpose(0, 2, 1, 3)
+    v = F["lti_v"]
+    ki = KineticInstances(np.arange(len(v)), 1.0, layout, -100.0, 1600 / 160.0, sch.open_states, 50.0,
+                          1.0, np.zeros(8))
+    ki.state = F["lti_state"].copy()
+    ki.advance(v)
+    assert np.abs(ki.state - F["lti_new"]).max() < 1e-14
+
+
+def test_deterministic_table_error_within_reference_target():
+    """The reference optimises tables to 1e-4 max error (nmodl/__init__.py:305)."""
+    t = LTITable(na8(), 0.1, 6.3)
+    assert t.max_error(16) < 1e-5
+
+
+def test_na8_is_the_markov_form_of_hh_sodium():
+    """With exact propagators, the open state of Na8 equals m^3 h along any voltage path."""
+    sch = na8()
+    rng = np.random.default_rng(0)
+    v_path = np.concatenate([np.full(20, -65.0), rng.uniform(-90, 40, 200)])
+    m0, _, h0, _, _, _ = hh_rates(np.array([-65.0]), 6.3)
+    m, h = m0[0], h0[0]
+    s = binomial_state(m, h)
+    dt = 0.1
+    for v in v_path:
+        P = scipy.linalg.expm(sch.matrix([v], 6.3)[0] * dt)
+        s = P @ s
+        am, bm, ah, bh = hh_sodium_rates(np.array([v]), 6.3)
+        minf, mt = am[0] / (am[0] + bm[0]), 1 / (am[0] + bm[0])
+        hinf, ht = ah[0] / (ah[0] + bh[0]), 1 / (ah[0] + bh[0])
+        m = minf + (m - minf) * np.exp(-dt / mt)
+        h = hinf + (h - hinf) * np.exp(-dt / ht)
+        assert abs(s[3] - m ** 3 * h) < 1e-12
+    assert abs(s.sum() - 1.0) < 1e-12
+
+
+def test_locate_matches_generated_kernel_rules():
+    """Truncation toward zero and clamping (codegen.py:43-59)."""
+    t = LTITable(na8(), 0.1, 6.3)
+    b, loc = t.locate(np.array([-100.0, -100.05, -100.2, 59.99, 60.0, 70.0, -50.0]))
+    assert list(b[:3]) == [0, 0, 0]
+    assert loc[0] == 0.0 and loc[1] == pytest.approx(-0.5) and loc[2] == 0.0
+    assert b[3] == 1599 and b[4] == 1599 and loc[4] == 1.0 and loc[5] == 1.0
+    assert b[6] == 500 and loc[6] == pytest.approx(0.0, abs=1e-9)
