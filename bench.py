@@ -275,6 +275,8 @@ def main():
     n = model._n
     r_kept = nnz.value / n
     r_stored = stored.value / n
+    bulk_active = ctypes.c_int64()
+    ctx.call("nw_get_option", b"bulk_pipeline_active", ctypes.byref(bulk_active))
     lanes = ctypes.c_int(); thr = ctypes.c_int(); cps = ctypes.c_int()
     ctx.call("nw_get_tuning", ctypes.byref(lanes), ctypes.byref(thr), ctypes.byref(cps))
     sptr = ctypes.c_void_p()
@@ -375,6 +377,8 @@ def main():
                    "propagator_pruning": "charge-conserving (pruned mass returned to the diagonal)",
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
                    "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
+                   "propagator_stream": "cp.async.bulk ring (4 x 256 entries per warp)" if bulk_active.value
+                   else "register loads",
                    "threads": thr.value, "l2": "inputs larger than L2 (propagator "
                    f"{pbytes.value / 1e9:.1f} GB), no flush", "mechanisms": ["hh", "na8 (8-state Markov Na, LTI voltage table 1600 x 0.1 mV, linear)"],
                    "parallelism": f"replicas x{world}"},

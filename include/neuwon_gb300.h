@@ -180,6 +180,13 @@ int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks);
 int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm);
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm);
 
+/* Named options.  "bulk_pipeline" (default 1): stream the propagator of the FP32
+ * batched path through shared memory with cp.async.bulk copies (needs lanes_per_row
+ * 0 in nw_set_tuning); nw_get_option("bulk_pipeline_active") tells whether the next
+ * batched launch will use it. */
+int nw_set_option(nw_ctx* ctx, const char* name, int64_t value);
+int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value);
+
 /* Statistics of the installed propagator: rows, kept entries (with diagonal),
  * stored off-diagonal entries including padding, bytes of the batched format. */
 int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* stored,

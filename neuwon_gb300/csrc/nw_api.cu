@@ -790,6 +790,10 @@ static int read_status(nw_ctx* ctx) {
     int st = 0;
     NW_CUDA(ctx, cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
     NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (st & kStatusWaitTimeout) {
+        cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+        return fail(ctx, NW_ERR_CUDA, "batched step: a bulk copy did not complete within the wait limit");
+    }
     if (st & kStatusNonFinite) {
         cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
         return fail(ctx, NW_ERR_NUMERIC, "a segment voltage became non-finite");
@@ -859,6 +863,21 @@ int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm) 
     ctx->threads = threads;
     ctx->ctas_per_sm = ctas_per_sm;
     return NW_OK;
+}
+
+int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
+    if (!ctx || !name) return NW_ERR_ARG;
+    std::string nm(name);
+    if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
+    return fail(ctx, NW_ERR_ARG, "nw_set_option: unknown option " + nm);
+}
+
+int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
+    if (!ctx || !name || !value) return NW_ERR_ARG;
+    std::string nm(name);
+    if (nm == "bulk_pipeline") { *value = ctx->use_bulk ? 1 : 0; return NW_OK; }
+    if (nm == "bulk_pipeline_active") { *value = uses_bulk_pipeline(ctx) ? 1 : 0; return NW_OK; }
+    return fail(ctx, NW_ERR_ARG, "nw_get_option: unknown option " + nm);
 }
 
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm) {

@@ -24,6 +24,7 @@ constexpr int kMaxProbesPerNeuron = 64;
 
 // Status bits written by kernels into the context's status word.
 constexpr int kStatusNonFinite = 1;
+constexpr int kStatusWaitTimeout = 16;   // a bounded wait on an mbarrier gave up
 
 struct HHState {
     int64_t m = 0;              // instances
@@ -110,6 +111,7 @@ struct nw_ctx {
     nw::DevBuf status;          // i32 [1]
     nw::DevBuf plain_x;         // real [n_seg] scratch of the plain path
     int lanes_per_row = 0, threads = 512, ctas_per_sm = 0;
+    bool use_bulk = true;       // asynchronous bulk-copy pipeline (FP32 batched path)
 
     // Clock.
     int64_t input_ticks = 0, steps = 0;
@@ -134,6 +136,7 @@ int propagator_conserve(nw_ctx* ctx);
 int advance_batched(nw_ctx* ctx, int k_steps);
 int advance_plain(nw_ctx* ctx, int k_steps);
 int choose_lanes_per_row(nw_ctx* ctx);
+bool uses_bulk_pipeline(nw_ctx* ctx);
 
 // Device conversions (nw_api.cu).
 int upload_convert(nw_ctx* ctx, void* dst, int dst_dtype, const void* host, int src_dtype,

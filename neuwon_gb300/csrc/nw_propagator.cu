@@ -375,7 +375,7 @@ __global__ void batched_count_kernel(int64_t n, const int64_t* prow, const int32
     if (r >= n) return;
     int64_t c = 0;
     for (int64_t k = prow[r]; k < prow[r + 1]; ++k) c += (pcol[k] != (int32_t)r);
-    cnt[r] = (c + 3) & ~(int64_t)3;
+    cnt[r] = (c + 7) & ~(int64_t)7;   // 8-entry rows: 16-byte aligned bulk copies
 }
 
 template <typename real>

@@ -21,6 +21,7 @@
 // per-neuron launches, one thread per row or per instance, 32 threads per
 // block, FP64 CSR with the diagonal.
 #include <algorithm>
+#include <type_traits>
 
 #include "nw_internal.cuh"
 
@@ -314,12 +315,191 @@ __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_
     }
 }
 
-template <typename real, int LPR>
+
+// ----------------------------------------------------------------------------
+// Asynchronous bulk-copy pipeline for the propagator stream (FP32 path).
+//
+// Each warp owns a ring of kBulkStages shared-memory stages.  Lane 0 copies
+// row chunks of up to kBulkChunk entries (values, then u16 columns) with
+// cp.async.bulk, completing on the stage's mbarrier; all lanes wait on the
+// barrier, consume the chunk from shared memory and lane 0 refills the stage
+// with the chunk kBulkStages ahead.  Rows are padded to multiples of 8 entries,
+// so every copy starts on a 16-byte boundary and moves a multiple of 16 bytes.
+// Waits are bounded: on timeout the kernel records kStatusWaitTimeout and stops.
+constexpr int kBulkChunk = 256;
+constexpr int kBulkStages = 4;
+constexpr uint32_t kWaitLimit = 1u << 20;
+
+template <typename real>
+struct BulkGeom {
+    static constexpr int kValBytes = kBulkChunk * (int)sizeof(real);
+    static constexpr int kStageBytes = kValBytes + kBulkChunk * 2;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+struct BulkRing {
+    unsigned char* stages;   // this warp's kBulkStages stages
+    uint64_t* bar;           // this warp's kBulkStages mbarriers
+    uint32_t seq;            // chunks consumed by this warp since the kernel started
+};
+
+// Producer state, meaningful in lane 0 only.
+struct BulkProducer {
+    int row;                 // next row (neuron-relative) with chunks left
+    int64_t off, end;        // next chunk starts at off; the row ends at end
+    uint32_t next_seq;       // sequence number of the next chunk to issue
+};
+
+template <typename real>
+__device__ __forceinline__ void bulk_issue(const StepArgs<real>& a, BulkRing& R, uint32_t seq,
+                                           int64_t off, int64_t end) {
+    const int stage = (int)(seq % kBulkStages);
+    const int len = (int)((end - off) < (int64_t)kBulkChunk ? (end - off) : (int64_t)kBulkChunk);
+    unsigned char* dst = R.stages + stage * BulkGeom<real>::kStageBytes;
+    const uint32_t bv = (uint32_t)len * (uint32_t)sizeof(real), bc = (uint32_t)len * 2u;
+    const uint32_t bar = smem_u32(R.bar + stage);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(bar), "r"(bv + bc) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_u32(dst)), "l"(a.val + off), "r"(bv), "r"(bar) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_u32(dst + BulkGeom<real>::kValBytes)), "l"(a.col + off), "r"(bc), "r"(bar)
+                 : "memory");
+}
+
+// Advance the producer to the next row that has entries.
+template <typename real>
+__device__ __forceinline__ void bulk_next_row(const StepArgs<real>& a, BulkProducer& P, int64_t base, int n,
+                                              int nw) {
+    for (P.row += nw; P.row < n; P.row += nw) {
+        P.off = a.rowptr[base + P.row];
+        P.end = a.rowptr[base + P.row + 1];
+        if (P.end > P.off) return;
+    }
+}
+
+template <typename real>
+__device__ __forceinline__ void bulk_issue_next(const StepArgs<real>& a, BulkRing& R, BulkProducer& P,
+                                                int64_t base, int n, int nw) {
+    if (P.row >= n) return;
+    bulk_issue(a, R, P.next_seq, P.off, P.end);
+    ++P.next_seq;
+    P.off += kBulkChunk;
+    if (P.off >= P.end) bulk_next_row(a, P, base, n, nw);
+}
+
+// Lane 0 of every warp starts the copies of its first kBulkStages chunks.
+template <typename real>
+__device__ __forceinline__ void bulk_prologue(const StepArgs<real>& a, BulkRing& R, BulkProducer& P,
+                                              int64_t base, int n) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane != 0) return;
+    P.next_seq = R.seq;
+    P.row = warp - nw;
+    bulk_next_row(a, P, base, n, nw);
+    for (int k = 0; k < kBulkStages; ++k) bulk_issue_next(a, R, P, base, n, nw);
+}
+
+__device__ __forceinline__ bool bulk_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          int* status) {
+    const uint32_t b = smem_u32(bar);
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(ok) : "r"(b), "r"(parity) : "memory");
+        if (ok) return true;
+        if (*abort_flag) return false;
+    }
+    atomicOr(status, kStatusWaitTimeout);
+    *abort_flag = 1;
+    return false;
+}
+
+// V_i <- propagator row i applied to xs, rows streamed through the warp's ring.
+template <typename real>
+__device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, int64_t base, int n,
+                                                      const real* __restrict__ xs, BulkRing& R,
+                                                      BulkProducer& P, volatile int* abort_flag) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t seq = R.seq;
+    for (int row = warp; row < n; row += nw) {
+        const int64_t r = base + row;
+        const int64_t beg = a.rowptr[r], end = a.rowptr[r + 1];
+        const real xi = xs[row];
+        real s = real(0), c = real(0);
+        for (int64_t off = beg; off < end; off += kBulkChunk) {
+            const int stage = (int)(seq % kBulkStages);
+            // Every lane waits (the barrier's acquire covers its own reads); the vote
+            // keeps the warp uniform if a bounded wait gave up in some lanes only.
+            const bool ok = __all_sync(0xffffffffu, bulk_wait(R.bar + stage, (seq / kBulkStages) & 1u,
+                                                              abort_flag, a.status));
+            if (!ok) {
+                *abort_flag = 1;
+                R.seq = seq;
+                return;
+            }
+            const int len = (int)((end - off) < (int64_t)kBulkChunk ? (end - off) : (int64_t)kBulkChunk);
+            const real* vals = reinterpret_cast<const real*>(R.stages + stage * BulkGeom<real>::kStageBytes);
+            const uint16_t* cols = reinterpret_cast<const uint16_t*>(
+                R.stages + stage * BulkGeom<real>::kStageBytes + BulkGeom<real>::kValBytes);
+            for (int q = 4 * lane; q < len; q += 128) {
+                real v[4];
+                if (sizeof(real) == 4) {
+                    const float4 f = *reinterpret_cast<const float4*>(vals + q);
+                    v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+                } else {
+                    v[0] = vals[q]; v[1] = vals[q + 1]; v[2] = vals[q + 2]; v[3] = vals[q + 3];
+                }
+                const ushort4 cc = *reinterpret_cast<const ushort4*>(cols + q);
+                kahan_add(s, c, v[0] * (xs[cc.x] - xi));
+                kahan_add(s, c, v[1] * (xs[cc.y] - xi));
+                kahan_add(s, c, v[2] * (xs[cc.z] - xi));
+                kahan_add(s, c, v[3] * (xs[cc.w] - xi));
+            }
+            __syncwarp();
+            if (lane == 0) bulk_issue_next(a, R, P, base, n, nw);
+            ++seq;
+        }
+        real t = s - c;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) {
+            const real vnew = (xi - a.leak[r] * xi) + t;
+            if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
+            a.V[r] = vnew;
+        }
+    }
+    R.seq = seq;
+}
+
+template <typename real, int LPR, bool BULK>
 __global__ void __launch_bounds__(1024)
-batched_advance_kernel(const StepArgs<real> a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     real* xs = reinterpret_cast<real*>(smem_raw);
     __shared__ int s_job;
+    __shared__ int s_abort;
+    BulkRing ring;
+    BulkProducer prod;
+    if (BULK) {
+        const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
+        unsigned char* rings = smem_raw + xs_bytes;
+        uint64_t* bars = reinterpret_cast<uint64_t*>(rings + nw * kBulkStages * BulkGeom<real>::kStageBytes);
+        ring.stages = rings + warp * kBulkStages * BulkGeom<real>::kStageBytes;
+        ring.bar = bars + warp * kBulkStages;
+        ring.seq = 0;
+        prod.row = 0; prod.off = prod.end = 0; prod.next_seq = 0;
+        if (threadIdx.x < nw * kBulkStages)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(bars + threadIdx.x)) : "memory");
+        if (threadIdx.x == 0) s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        __syncthreads();
+    }
     __shared__ int s_nclamp;
     __shared__ uint32_t s_cseg[kMaxClampsPerNeuron];
     __shared__ real s_camp[kMaxClampsPerNeuron];
@@ -330,7 +510,7 @@ batched_advance_kernel(const StepArgs<real> a) {
         if (tid == 0) s_job = atomicAdd(a.work_counter, 1);
         __syncthreads();
         const int job = s_job;
-        if (job >= a.n_neuron) break;
+        if (job >= a.n_neuron || (BULK && s_abort)) break;
         const int j = a.neuron_order[job];
         const int64_t base = a.neuron_start[j];
         const int n = (int)(a.neuron_start[j + 1] - base);
@@ -377,6 +557,8 @@ batched_advance_kernel(const StepArgs<real> a) {
                 const int64_t tick = a.tick0 + 2 * s + half + 1;
                 const bool gv = (s > 0) || (half > 0) || a.g_valid;
                 const bool last = (s == a.k_steps - 1) && (half == 1);
+                // The propagator does not depend on x: start streaming it now.
+                if (BULK) bulk_prologue(a, ring, prod, base, n);
                 for (int li = tid; li < n; li += nthr) {
                     const int64_t i = base + li;
                     real G, GE;
@@ -388,8 +570,10 @@ batched_advance_kernel(const StepArgs<real> a) {
                     xs[li] = membrane_x(a, i, G, GE, I, last);
                 }
                 __syncthreads();
-                propagate_neuron<real, LPR>(a, base, n, xs);
+                if (BULK) propagate_neuron_bulk(a, base, n, xs, ring, prod, &s_abort);
+                else propagate_neuron<real, LPR>(a, base, n, xs);
                 __syncthreads();
+                if (BULK && s_abort) break;
                 if (half == 0) {
                     // Mechanisms (rxd_model.py:115-123) at the mid-step voltage.
                     if (a.hh_on) {
@@ -407,6 +591,7 @@ batched_advance_kernel(const StepArgs<real> a) {
                     if (mech_sync) __syncthreads();
                 }
             }
+            if (BULK && s_abort) break;
             // AP detector (neuron.py:184-188) and probes after the full step.
             if (tid == 0 && a.has_det) {
                 const bool over = a.V[a.det_seg[j]] >= a.det_thr[j];
@@ -558,36 +743,52 @@ int choose_lanes_per_row(nw_ctx* ctx) {
     return 4;
 }
 
-template <typename real, int LPR>
-static int launch_batched_lpr(nw_ctx* ctx, const StepArgs<real>& a) {
-    auto kern = batched_advance_kernel<real, LPR>;
-    size_t smem = (size_t)ctx->max_neuron * sizeof(real);
-    smem = (smem + 15) & ~(size_t)15;
-    size_t static_smem = 4096;
+template <typename real, int LPR, bool BULK>
+static int launch_batched_cfg(nw_ctx* ctx, const StepArgs<real>& a) {
+    auto kern = batched_advance_kernel<real, LPR, BULK>;
+    const size_t xs_bytes = ((size_t)ctx->max_neuron * sizeof(real) + 127) & ~(size_t)127;
+    const int threads = ctx->threads;
+    size_t smem = xs_bytes;
+    if (BULK) smem += (size_t)(threads / 32) * kBulkStages * (BulkGeom<real>::kStageBytes + 8);
+    const size_t static_smem = 4096;
     if (smem + static_smem > ctx->smem_optin)
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron of " + std::to_string(ctx->max_neuron) +
                                        " segments does not fit in shared memory at this precision");
     NW_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int threads = ctx->threads;
     int occ = 0;
     NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem));
     if (occ < 1) return fail(ctx, NW_ERR_LIMIT, "batched path: kernel does not fit on an SM");
     int per_sm = ctx->ctas_per_sm ? std::min(ctx->ctas_per_sm, occ) : occ;
     int64_t grid = std::min<int64_t>(ctx->n_neuron, (int64_t)per_sm * ctx->num_sms);
     NW_CUDA(ctx, cudaMemsetAsync(ctx->work_counter.ptr, 0, sizeof(int), ctx->stream));
-    kern<<<(unsigned)grid, threads, smem, ctx->stream>>>(a);
+    kern<<<(unsigned)grid, threads, smem, ctx->stream>>>(a, (int)xs_bytes);
     NW_CUDA(ctx, cudaGetLastError());
     return NW_OK;
+}
+
+// The asynchronous bulk pipeline is used for FP32 state when it fits in shared
+// memory next to the neuron's x vector; otherwise the register path.
+static bool bulk_fits(nw_ctx* ctx) {
+    const size_t xs_bytes = ((size_t)ctx->max_neuron * sizeof(float) + 127) & ~(size_t)127;
+    const size_t ring = (size_t)(ctx->threads / 32) * kBulkStages * (BulkGeom<float>::kStageBytes + 8);
+    return xs_bytes + ring + 4096 <= ctx->smem_optin;
+}
+
+bool uses_bulk_pipeline(nw_ctx* ctx) {
+    return ctx->precision == NW_F32 && ctx->use_bulk && ctx->lanes_per_row == 0 && bulk_fits(ctx);
 }
 
 template <typename real>
 static int launch_batched(nw_ctx* ctx, int k_steps) {
     StepArgs<real> a = make_args<real>(ctx, k_steps);
+    if constexpr (std::is_same<real, float>::value) {
+        if (uses_bulk_pipeline(ctx)) return launch_batched_cfg<float, 32, true>(ctx, a);
+    }
     switch (choose_lanes_per_row(ctx)) {
-        case 4: return launch_batched_lpr<real, 4>(ctx, a);
-        case 8: return launch_batched_lpr<real, 8>(ctx, a);
-        case 16: return launch_batched_lpr<real, 16>(ctx, a);
-        default: return launch_batched_lpr<real, 32>(ctx, a);
+        case 4: return launch_batched_cfg<real, 4, false>(ctx, a);
+        case 8: return launch_batched_cfg<real, 8, false>(ctx, a);
+        case 16: return launch_batched_cfg<real, 16, false>(ctx, a);
+        default: return launch_batched_cfg<real, 32, false>(ctx, a);
     }
 }
 

@@ -265,3 +265,26 @@ def test_f32_hh_plus_na8_within_bound():
     assert worst < 0.1, worst
     np.testing.assert_array_equal(m.get_data("Neuron.spike_count"), om.spike_count)
     m.close()
+
+
+def test_bulk_pipeline_matches_register_path_bitwise():
+    """The cp.async.bulk stream and the register stream sum each row in the same order."""
+    trees = [random_tree(1500, seed=51), random_tree(700, seed=52), random_tree(1, seed=0),
+             random_tree(2600, seed=53)]
+    clamps = [(0, 0, 0.4, 0.0, 20.0), (1, 0, 0.3, 1.0, 10.0), (3, 100, 0.5, 0.5, 15.0)]
+    outs = []
+    for bulk in (1, 0):
+        m, neurons, offs, _ = gpu_model(trees, clamps, precision="f32", kinetic=True, tolerance=1e-9)
+        m._sync()
+        m._ctx.call("nw_set_option", b"bulk_pipeline", bulk)
+        m._ctx.call("nw_set_tuning", 0 if bulk else 32, 512, 0)
+        active = ctypes.c_int64()
+        m._ctx.call("nw_get_option", b"bulk_pipeline_active", ctypes.byref(active))
+        assert active.value == bulk
+        run_with_clamps(m, clamps, offs, 150)
+        m.advance(50)
+        outs.append((m.get_data("Segment.voltage"), m.get_data("na8.state"), m.get_data("Neuron.spike_count")))
+        m.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert np.array_equal(outs[0][2], outs[1][2])
