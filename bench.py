@@ -225,7 +225,8 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=2000)
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch")
     ap.add_argument("--lanes", type=int, default=0)
-    ap.add_argument("--threads", type=int, default=512)
+    ap.add_argument("--threads", type=int, default=1024)
+    ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
     ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu legs")
     args = ap.parse_args()
 
@@ -267,6 +268,7 @@ def main():
     model._sync()
     ctx = model._ctx
     ctx.call("nw_set_tuning", args.lanes, args.threads, 0)
+    ctx.call("nw_set_option", b"bulk_pipeline", args.bulk)
     ctx.call("nw_synchronize")
     build_s = time.perf_counter() - t_build
     log(f"device model + propagator in {build_s:.1f} s")

@@ -176,11 +176,11 @@ int nw_advance_host(nw_ctx* ctx, int32_t k_steps, const double* stim_amps,
 int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks);
 
 /* Tuning of the batched path: lanes per propagator row (4, 8, 16 or 32, 0 = auto),
- * threads per CTA (128..1024), CTAs per SM (0 = occupancy maximum). */
+ * threads per CTA (128..1024, default 1024), CTAs per SM (0 = occupancy maximum). */
 int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm);
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm);
 
-/* Named options.  "bulk_pipeline" (default 1): stream the propagator of the FP32
+/* Named options.  "bulk_pipeline" (default 0): stream the propagator of the FP32
  * batched path through shared memory with cp.async.bulk copies (needs lanes_per_row
  * 0 in nw_set_tuning); nw_get_option("bulk_pipeline_active") tells whether the next
  * batched launch will use it. */

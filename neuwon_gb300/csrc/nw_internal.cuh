@@ -110,8 +110,8 @@ struct nw_ctx {
     nw::DevBuf work_counter;    // i32 [1]
     nw::DevBuf status;          // i32 [1]
     nw::DevBuf plain_x;         // real [n_seg] scratch of the plain path
-    int lanes_per_row = 0, threads = 512, ctas_per_sm = 0;
-    bool use_bulk = true;       // asynchronous bulk-copy pipeline (FP32 batched path)
+    int lanes_per_row = 0, threads = 1024, ctas_per_sm = 0;
+    bool use_bulk = false;      // asynchronous bulk-copy pipeline (FP32 batched path)
 
     // Clock.
     int64_t input_ticks = 0, steps = 0;

@@ -734,10 +734,11 @@ static StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     return a;
 }
 
+// Lanes per propagator row (measured on GB300 with ~490 entries/row: 16 lanes and
+// 1,024 threads beat 32 lanes; 8 lanes is too few for such rows).
 int choose_lanes_per_row(nw_ctx* ctx) {
     if (ctx->lanes_per_row) return ctx->lanes_per_row;
     double avg = ctx->n_seg ? (double)ctx->nnz_b / (double)ctx->n_seg : 0.0;
-    if (avg >= 96) return 32;
     if (avg >= 48) return 16;
     if (avg >= 20) return 8;
     return 4;

@@ -277,7 +277,7 @@ def test_bulk_pipeline_matches_register_path_bitwise():
         m, neurons, offs, _ = gpu_model(trees, clamps, precision="f32", kinetic=True, tolerance=1e-9)
         m._sync()
         m._ctx.call("nw_set_option", b"bulk_pipeline", bulk)
-        m._ctx.call("nw_set_tuning", 0 if bulk else 32, 512, 0)
+        m._ctx.call("nw_set_tuning", 0 if bulk else 32, 512, 0)   # the ring needs 512 threads
         active = ctypes.c_int64()
         m._ctx.call("nw_get_option", b"bulk_pipeline_active", ctypes.byref(active))
         assert active.value == bulk
