@@ -192,6 +192,37 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value);
 int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* stored,
                         int64_t* bytes);
 
+/* ---- allocation-free half step --------------------------------------- */
+
+/* Largest num_segments accepted by nw_electric_half_step_noalloc. */
+#define NW_NOALLOC_MAX_SEGMENTS (1 << 20)
+
+/* No counterpart in the reference: one electric half step (membrane update and
+ * propagator multiply, the arithmetic of Segment._advance_electric) on arrays the
+ * caller allocated, for callers that cannot call cudaMalloc -- e.g. a host whose
+ * device memory must all come from its own pool allocator, or a loop that must
+ * not allocate between steps.  Nothing is allocated by the call: the scratch
+ * vector the propagator multiplies is a static device array of
+ * NW_NOALLOC_MAX_SEGMENTS doubles (8 MiB, held on every GPU that loads this
+ * library until the process exits).
+ *   rowptr/col/val: the propagator in CSR, FP64, diagonal included (n x n);
+ *   voltage (mV): read, then overwritten with the result;
+ *   capacitance (F), sum_conductance (S), driving_voltage (mV), sum_current (A): inputs;
+ *   half_step_ms: the time step of this half step (dt/2);
+ *   stream: cudaStream_t to launch on (NULL = default stream); the call returns
+ *   after enqueueing, without synchronising.
+ * All device pointers must be on the current device.  Returns NW_ERR_LIMIT when
+ * num_segments > NW_NOALLOC_MAX_SEGMENTS, NW_ERR_ARG for null pointers or a
+ * non-positive step.  The first call on each device looks up the scratch
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  Every call shares the one scratch array, so calls that
+ * overlap on the GPU (different streams, or different threads) race; each call
+ * overwrites the part it uses before reading it, so nothing needs clearing. */
+int nw_electric_half_step_noalloc(int64_t num_segments, const int64_t* rowptr, const int32_t* col,
+                                  const double* val, double* voltage, const double* capacitance,
+                                  const double* sum_conductance, const double* driving_voltage,
+                                  const double* sum_current, double half_step_ms, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
