@@ -319,14 +319,18 @@ __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_
 // ----------------------------------------------------------------------------
 // Asynchronous bulk-copy pipeline for the propagator stream (FP32 path).
 //
-// Each warp owns a ring of kBulkStages shared-memory stages.  Lane 0 copies
-// row chunks of up to kBulkChunk entries (values, then u16 columns) with
-// cp.async.bulk, completing on the stage's mbarrier; all lanes wait on the
-// barrier, consume the chunk from shared memory and lane 0 refills the stage
-// with the chunk kBulkStages ahead.  Rows are padded to multiples of 8 entries,
-// so every copy starts on a 16-byte boundary and moves a multiple of 16 bytes.
-// Waits are bounded: on timeout the kernel records kStatusWaitTimeout and stops.
-constexpr int kBulkChunk = 256;
+// The rows of a neuron are split among the warps of the CTA into contiguous
+// ranges holding about equal numbers of entries, so each warp's part of the
+// propagator is one contiguous stream.  Each warp owns a ring of kBulkStages
+// shared-memory stages; lane 0 copies the stream in chunks of kBulkChunk
+// entries (values, then u16 columns) with cp.async.bulk, completing on the
+// stage's mbarrier, kBulkStages chunks ahead of the consumer.  All lanes wait
+// on the barrier and consume a chunk row segment by row segment; row ends come
+// from a 32-row window of row pointers held one per lane.  Rows are padded to
+// multiples of 8 entries, so every copy starts on a 16-byte boundary and moves
+// a multiple of 16 bytes, and no 4-entry vector straddles two rows.  Waits are
+// bounded: on timeout the kernel records kStatusWaitTimeout and stops.
+constexpr int kBulkChunk = 128;
 constexpr int kBulkStages = 4;
 constexpr uint32_t kWaitLimit = 1u << 20;
 
@@ -346,12 +350,35 @@ struct BulkRing {
     uint32_t seq;            // chunks consumed by this warp since the kernel started
 };
 
-// Producer state, meaningful in lane 0 only.
-struct BulkProducer {
-    int row;                 // next row (neuron-relative) with chunks left
-    int64_t off, end;        // next chunk starts at off; the row ends at end
-    uint32_t next_seq;       // sequence number of the next chunk to issue
+// This warp's rows [row_lo, row_hi) and their entries [e0, e1) in one neuron.
+struct WarpSlice {
+    int row_lo, row_hi;
+    int64_t e0, e1;
 };
+
+// Entry-balanced split of the neuron's rows among the warps (once per neuron).
+template <typename real>
+__device__ __forceinline__ WarpSlice warp_slice(const StepArgs<real>& a, int64_t base, int n) {
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int64_t E0 = a.rowptr[base], total = a.rowptr[base + n] - E0;
+    auto split = [&](int w) -> int {
+        if (w <= 0) return 0;
+        if (w >= nw) return n;
+        const int64_t target = E0 + (total * w) / nw;
+        int lo = 0, hi = n;                     // first row whose start is >= target
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (a.rowptr[base + mid] < target) lo = mid + 1; else hi = mid;
+        }
+        return lo;
+    };
+    WarpSlice ws;
+    ws.row_lo = split(warp);
+    ws.row_hi = split(warp + 1);
+    ws.e0 = a.rowptr[base + ws.row_lo];
+    ws.e1 = a.rowptr[base + ws.row_hi];
+    return ws;
+}
 
 template <typename real>
 __device__ __forceinline__ void bulk_issue(const StepArgs<real>& a, BulkRing& R, uint32_t seq,
@@ -371,37 +398,16 @@ __device__ __forceinline__ void bulk_issue(const StepArgs<real>& a, BulkRing& R,
                  : "memory");
 }
 
-// Advance the producer to the next row that has entries.
+// Lane 0 starts the copies of the first kBulkStages chunks of the warp's stream.
 template <typename real>
-__device__ __forceinline__ void bulk_next_row(const StepArgs<real>& a, BulkProducer& P, int64_t base, int n,
-                                              int nw) {
-    for (P.row += nw; P.row < n; P.row += nw) {
-        P.off = a.rowptr[base + P.row];
-        P.end = a.rowptr[base + P.row + 1];
-        if (P.end > P.off) return;
+__device__ __forceinline__ void bulk_prologue(const StepArgs<real>& a, BulkRing& R, const WarpSlice& ws) {
+    if ((threadIdx.x & 31) != 0) return;
+    uint32_t seq = R.seq;
+    for (int k = 0; k < kBulkStages; ++k) {
+        const int64_t off = ws.e0 + (int64_t)k * kBulkChunk;
+        if (off >= ws.e1) break;
+        bulk_issue(a, R, seq++, off, ws.e1);
     }
-}
-
-template <typename real>
-__device__ __forceinline__ void bulk_issue_next(const StepArgs<real>& a, BulkRing& R, BulkProducer& P,
-                                                int64_t base, int n, int nw) {
-    if (P.row >= n) return;
-    bulk_issue(a, R, P.next_seq, P.off, P.end);
-    ++P.next_seq;
-    P.off += kBulkChunk;
-    if (P.off >= P.end) bulk_next_row(a, P, base, n, nw);
-}
-
-// Lane 0 of every warp starts the copies of its first kBulkStages chunks.
-template <typename real>
-__device__ __forceinline__ void bulk_prologue(const StepArgs<real>& a, BulkRing& R, BulkProducer& P,
-                                              int64_t base, int n) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (lane != 0) return;
-    P.next_seq = R.seq;
-    P.row = warp - nw;
-    bulk_next_row(a, P, base, n, nw);
-    for (int k = 0; k < kBulkStages; ++k) bulk_issue_next(a, R, P, base, n, nw);
 }
 
 __device__ __forceinline__ bool bulk_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
@@ -420,34 +426,63 @@ __device__ __forceinline__ bool bulk_wait(uint64_t* bar, uint32_t parity, volati
     return false;
 }
 
-// V_i <- propagator row i applied to xs, rows streamed through the warp's ring.
+// V_i <- propagator row i applied to xs for the rows of this warp's slice.
 template <typename real>
-__device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, int64_t base, int n,
+__device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, int64_t base,
                                                       const real* __restrict__ xs, BulkRing& R,
-                                                      BulkProducer& P, volatile int* abort_flag) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t seq = R.seq;
-    for (int row = warp; row < n; row += nw) {
-        const int64_t r = base + row;
-        const int64_t beg = a.rowptr[r], end = a.rowptr[r + 1];
-        const real xi = xs[row];
-        real s = real(0), c = real(0);
-        for (int64_t off = beg; off < end; off += kBulkChunk) {
-            const int stage = (int)(seq % kBulkStages);
-            // Every lane waits (the barrier's acquire covers its own reads); the vote
-            // keeps the warp uniform if a bounded wait gave up in some lanes only.
-            const bool ok = __all_sync(0xffffffffu, bulk_wait(R.bar + stage, (seq / kBulkStages) & 1u,
-                                                              abort_flag, a.status));
-            if (!ok) {
-                *abort_flag = 1;
-                R.seq = seq;
-                return;
+                                                      const WarpSlice& ws, volatile int* abort_flag) {
+    const int lane = threadIdx.x & 31;
+    // Row-end window: lane k holds the end of row win + k.
+    int win = ws.row_lo;
+    int64_t wend = (win + lane < ws.row_hi) ? a.rowptr[base + win + lane + 1] : ws.e1;
+    int row = ws.row_lo;
+    int64_t row_end = __shfl_sync(0xffffffffu, wend, 0);
+    real s = real(0), c = real(0);
+    // Finishes `row` (all of its entries have been summed) and moves to the next one.
+    auto finish_row = [&]() {
+        real t = s - c;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) {
+            const int64_t r = base + row;
+            const real xi = xs[row];
+            const real vnew = (xi - a.leak[r] * xi) + t;
+            if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
+            a.V[r] = vnew;
+        }
+        s = real(0); c = real(0);
+        ++row;
+        if (row < ws.row_hi) {
+            if (row - win == 32) {
+                win = row;
+                wend = (win + lane < ws.row_hi) ? a.rowptr[base + win + lane + 1] : ws.e1;
             }
-            const int len = (int)((end - off) < (int64_t)kBulkChunk ? (end - off) : (int64_t)kBulkChunk);
-            const real* vals = reinterpret_cast<const real*>(R.stages + stage * BulkGeom<real>::kStageBytes);
-            const uint16_t* cols = reinterpret_cast<const uint16_t*>(
-                R.stages + stage * BulkGeom<real>::kStageBytes + BulkGeom<real>::kValBytes);
-            for (int q = 4 * lane; q < len; q += 128) {
+            row_end = __shfl_sync(0xffffffffu, wend, row - win);
+        }
+    };
+    uint32_t seq = R.seq;
+    // Rows without off-diagonal entries before the first chunk.
+    while (row < ws.row_hi && row_end == ws.e0) finish_row();
+    for (int64_t c0 = ws.e0; c0 < ws.e1; c0 += kBulkChunk) {
+        const int64_t c1 = (ws.e1 - c0) < (int64_t)kBulkChunk ? ws.e1 : c0 + kBulkChunk;
+        const int stage = (int)(seq % kBulkStages);
+        // Every lane waits (the barrier's acquire covers its own reads); the vote
+        // keeps the warp uniform if a bounded wait gave up in some lanes only.
+        const bool ok = __all_sync(0xffffffffu, bulk_wait(R.bar + stage, (seq / kBulkStages) & 1u,
+                                                          abort_flag, a.status));
+        if (!ok) {
+            *abort_flag = 1;
+            R.seq = seq;
+            return;
+        }
+        const real* vals = reinterpret_cast<const real*>(R.stages + stage * BulkGeom<real>::kStageBytes);
+        const uint16_t* cols = reinterpret_cast<const uint16_t*>(
+            R.stages + stage * BulkGeom<real>::kStageBytes + BulkGeom<real>::kValBytes);
+        int64_t pos = c0;
+        while (pos < c1) {
+            const int64_t seg_end = row_end < c1 ? row_end : c1;
+            const real xi = xs[row];
+            for (int q = (int)(pos - c0) + 4 * lane; q < (int)(seg_end - c0); q += 128) {
                 real v[4];
                 if (sizeof(real) == 4) {
                     const float4 f = *reinterpret_cast<const float4*>(vals + q);
@@ -461,18 +496,18 @@ __device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, i
                 kahan_add(s, c, v[2] * (xs[cc.z] - xi));
                 kahan_add(s, c, v[3] * (xs[cc.w] - xi));
             }
-            __syncwarp();
-            if (lane == 0) bulk_issue_next(a, R, P, base, n, nw);
-            ++seq;
+            pos = seg_end;
+            if (pos == row_end) {
+                finish_row();
+                while (row < ws.row_hi && row_end == pos) finish_row();   // empty rows
+            }
         }
-        real t = s - c;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        __syncwarp();
         if (lane == 0) {
-            const real vnew = (xi - a.leak[r] * xi) + t;
-            if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
-            a.V[r] = vnew;
+            const int64_t nxt = c0 + (int64_t)kBulkStages * kBulkChunk;
+            if (nxt < ws.e1) bulk_issue(a, R, seq + kBulkStages, nxt, ws.e1);
         }
+        ++seq;
     }
     R.seq = seq;
 }
@@ -485,7 +520,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
     __shared__ int s_job;
     __shared__ int s_abort;
     BulkRing ring;
-    BulkProducer prod;
+    WarpSlice slice;
     if (BULK) {
         const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
         unsigned char* rings = smem_raw + xs_bytes;
@@ -493,7 +528,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
         ring.stages = rings + warp * kBulkStages * BulkGeom<real>::kStageBytes;
         ring.bar = bars + warp * kBulkStages;
         ring.seq = 0;
-        prod.row = 0; prod.off = prod.end = 0; prod.next_seq = 0;
+        slice.row_lo = slice.row_hi = 0; slice.e0 = slice.e1 = 0;
         if (threadIdx.x < nw * kBulkStages)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(bars + threadIdx.x)) : "memory");
         if (threadIdx.x == 0) s_abort = 0;
@@ -527,6 +562,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
         }
         __syncthreads();
         const int nclamp = s_nclamp;
+        if (BULK) slice = warp_slice(a, base, n);
         // Mechanism instance ranges of this neuron.
         int64_t ib = 0, ie = 0, kb = 0, ke = 0;
         if (a.hh_on) {
@@ -558,7 +594,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
                 const bool gv = (s > 0) || (half > 0) || a.g_valid;
                 const bool last = (s == a.k_steps - 1) && (half == 1);
                 // The propagator does not depend on x: start streaming it now.
-                if (BULK) bulk_prologue(a, ring, prod, base, n);
+                if (BULK) bulk_prologue(a, ring, slice);
                 for (int li = tid; li < n; li += nthr) {
                     const int64_t i = base + li;
                     real G, GE;
@@ -570,7 +606,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
                     xs[li] = membrane_x(a, i, G, GE, I, last);
                 }
                 __syncthreads();
-                if (BULK) propagate_neuron_bulk(a, base, n, xs, ring, prod, &s_abort);
+                if (BULK) propagate_neuron_bulk(a, base, xs, ring, slice, &s_abort);
                 else propagate_neuron<real, LPR>(a, base, n, xs);
                 __syncthreads();
                 if (BULK && s_abort) break;

@@ -161,12 +161,15 @@ def test_lanes_per_row_variants_agree(lanes):
     assert np.abs(res[0] - res[1]).max() < 1e-9
 
 
-def test_batched_is_deterministic():
+@pytest.mark.parametrize("bulk", [0, 1])
+def test_batched_is_deterministic(bulk):
     trees = [random_tree(300, seed=s) for s in range(5)]
     clamps = [(k, 0, 0.3, 0.0, 20.0) for k in range(5)]
     outs = []
     for _ in range(2):
         m, neurons, offs, _ = gpu_model(trees, clamps, precision="f32")
+        m._sync()
+        m._ctx.call("nw_set_option", b"bulk_pipeline", bulk)
         run_with_clamps(m, clamps, offs, 100)
         outs.append(m.get_data("Segment.voltage"))
         m.close()
@@ -267,8 +270,9 @@ def test_f32_hh_plus_na8_within_bound():
     m.close()
 
 
-def test_bulk_pipeline_matches_register_path_bitwise():
-    """The cp.async.bulk stream and the register stream sum each row in the same order."""
+def test_bulk_pipeline_matches_register_path():
+    """The cp.async.bulk stream and the register stream compute the same step (FP32;
+    only the assignment of entries to lanes, hence the rounding, differs)."""
     trees = [random_tree(1500, seed=51), random_tree(700, seed=52), random_tree(1, seed=0),
              random_tree(2600, seed=53)]
     clamps = [(0, 0, 0.4, 0.0, 20.0), (1, 0, 0.3, 1.0, 10.0), (3, 100, 0.5, 0.5, 15.0)]
@@ -277,7 +281,7 @@ def test_bulk_pipeline_matches_register_path_bitwise():
         m, neurons, offs, _ = gpu_model(trees, clamps, precision="f32", kinetic=True, tolerance=1e-9)
         m._sync()
         m._ctx.call("nw_set_option", b"bulk_pipeline", bulk)
-        m._ctx.call("nw_set_tuning", 0 if bulk else 32, 512, 0)   # the ring needs 512 threads
+        m._ctx.call("nw_set_tuning", 0 if bulk else 32, 1024, 0)
         active = ctypes.c_int64()
         m._ctx.call("nw_get_option", b"bulk_pipeline_active", ctypes.byref(active))
         assert active.value == bulk
@@ -285,6 +289,6 @@ def test_bulk_pipeline_matches_register_path_bitwise():
         m.advance(50)
         outs.append((m.get_data("Segment.voltage"), m.get_data("na8.state"), m.get_data("Neuron.spike_count")))
         m.close()
-    assert np.array_equal(outs[0][0], outs[1][0])
-    assert np.array_equal(outs[0][1], outs[1][1])
+    assert np.abs(outs[0][0] - outs[1][0]).max() < 1e-3
+    assert np.abs(outs[0][1] - outs[1][1]).max() < 1e-5
     assert np.array_equal(outs[0][2], outs[1][2])
