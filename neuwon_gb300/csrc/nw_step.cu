@@ -261,6 +261,17 @@ __device__ __forceinline__ void kahan_add(real& s, real& c, real term) {
     s = t;
 }
 
+// Four entries of a row: sum of P_ij (x_j - x_i), added pairwise; the running
+// row sum around it is compensated (kahan_add), so the dependent chain per lane
+// is one compensated add per 4 entries.
+template <typename real>
+__device__ __forceinline__ real quad_sum(const real (&v)[4], const ushort4 cc, const real* __restrict__ xs,
+                                         real xi) {
+    const real a = v[0] * (xs[cc.x] - xi) + v[1] * (xs[cc.y] - xi);
+    const real b = v[2] * (xs[cc.z] - xi) + v[3] * (xs[cc.w] - xi);
+    return a + b;
+}
+
 // V_i <- propagator row i applied to xs, for every row of one neuron.
 template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2)>
 __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_t base, int n,
@@ -295,12 +306,8 @@ __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < UNROLL; ++u) {
-                    kahan_add(s, c, v[u][0] * (xs[cc[u].x] - xi));
-                    kahan_add(s, c, v[u][1] * (xs[cc[u].y] - xi));
-                    kahan_add(s, c, v[u][2] * (xs[cc[u].z] - xi));
-                    kahan_add(s, c, v[u][3] * (xs[cc[u].w] - xi));
-                }
+                for (int u = 0; u < UNROLL; ++u)
+                    kahan_add(s, c, quad_sum(v[u], cc[u], xs, xi));
             }
         }
         real t = s - c;
@@ -491,10 +498,7 @@ __device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, i
                     v[0] = vals[q]; v[1] = vals[q + 1]; v[2] = vals[q + 2]; v[3] = vals[q + 3];
                 }
                 const ushort4 cc = *reinterpret_cast<const ushort4*>(cols + q);
-                kahan_add(s, c, v[0] * (xs[cc.x] - xi));
-                kahan_add(s, c, v[1] * (xs[cc.y] - xi));
-                kahan_add(s, c, v[2] * (xs[cc.z] - xi));
-                kahan_add(s, c, v[3] * (xs[cc.w] - xi));
+                kahan_add(s, c, quad_sum(v, cc, xs, xi));
             }
             pos = seg_end;
             if (pos == row_end) {
