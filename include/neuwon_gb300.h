@@ -78,7 +78,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
  * for the device-resident attributes.  name is "Class.attribute":
  *   Segment.voltage, Segment.integral_voltage, Segment.capacitance,
  *   Segment.axial_resistance, Segment.nonspecific_current,
- *   hh.m, hh.h, hh.n (instance order as registered),
+ *   hh.m, hh.h, hh.n, hh.gna_coef, hh.gk_coef, hh.gl_coef (instance order as registered),
  *   kinetic.state (num_instances * S values, [instance][state], registration order),
  *   Neuron.AP_detected, Neuron.spike_count.
  * Values are converted between dtype and the context precision. */
@@ -180,7 +180,27 @@ int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks);
 int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm);
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm);
 
-/* Named options.  "bulk_pipeline" (default 0): stream the propagator of the FP32
+/* ---- differentiation ----------------------------------------------- */
+
+/* No counterpart in the reference (it has no autodiff): the forward half of a
+ * gradient computation.  Advances num_steps steps like nw_advance (HH models with
+ * one instance per segment), keeping the state every checkpoint_every steps, and
+ * returns loss = mean over steps s and neurons j of (V_det(j) after step s -
+ * target[s * num_neurons + j])^2, V_det the neuron's AP-detector segment. */
+int nw_adjoint_forward(nw_ctx* ctx, int64_t num_steps, int32_t checkpoint_every, const double* target,
+                       double* loss_out);
+
+/* The reverse half: d loss / d (every HH instance's gna/gk/gl coefficient, S) in
+ * registration order, and d loss / d Ra (cytoplasmic resistivity, ohm cm; pass its
+ * current value).  Recomputes each checkpoint interval, taping V and the gates, and
+ * sweeps it backwards (transposed propagator, gate Jacobians); leaves the model in
+ * the state nw_adjoint_forward ended in.  Any output pointer may be NULL. */
+int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad_gna, double* grad_gk,
+                        double* grad_gl, double* grad_ra);
+
+/* Named options.  "reset_clock" (any value): back to time 0 (clock, detector state,
+ * probes; conductances count as not yet computed) without touching V or gates.
+ * "bulk_pipeline" (default 0): stream the propagator of the FP32
  * batched path through shared memory with cp.async.bulk copies (needs lanes_per_row
  * 0 in nw_set_tuning); nw_get_option("bulk_pipeline_active") tells whether the next
  * batched launch will use it. */

@@ -166,6 +166,13 @@ static void free_hh(HHState& hh) {
     hh = HHState();
 }
 
+static void free_adj(AdjointState& a) {
+    for (DevBuf* b : {&a.ckpt, &a.target, &a.loss_part, &a.tape, &a.lamV, &a.lamV2, &a.lamM, &a.lamH, &a.lamN,
+                      &a.gGna, &a.gGk, &a.gGl, &a.ra_part})
+        dev_free(*b);
+    a = AdjointState();
+}
+
 static void free_kin(KineticState& k) {
     for (DevBuf* b : {&k.seg, &k.state, &k.gcoef, &k.table, &k.seg_ptr, &k.neuron_ptr}) dev_free(*b);
     k = KineticState();
@@ -232,6 +239,7 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     free_hh(ctx->hh);
     free_kin(ctx->kin);
+    free_adj(ctx->adj);
     DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec,
                       &ctx->kI, &ctx->kG, &ctx->cap64, &ctx->res64, &ctx->p_rowptr, &ctx->p_col,
                       &ctx->p_val, &ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak,
@@ -307,6 +315,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     ctx->n_probes = 0;
     free_hh(ctx->hh);
     free_kin(ctx->kin);
+    free_adj(ctx->adj);
     size_t rs = (size_t)ctx->precision;
     NW_CHECK(dev_alloc(ctx, ctx->neuron_start, 8 * (num_neurons + 1)));
     NW_CHECK(dev_alloc(ctx, ctx->parent, 8 * num_segments));
@@ -385,11 +394,14 @@ int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int6
         NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         return NW_OK;
     }
-    if (nm == "hh.m" || nm == "hh.h" || nm == "hh.n") {
+    if (nm == "hh.m" || nm == "hh.h" || nm == "hh.n" ||
+        nm == "hh.gna_coef" || nm == "hh.gk_coef" || nm == "hh.gl_coef") {
         NW_CHECK(need(ctx->hh.m));
         std::vector<double> sorted(count);
         for (int64_t i = 0; i < count; ++i) sorted[ctx->hh.user_to_sorted[i]] = read_as_double(host, dtype, i);
-        DevBuf& b = nm == "hh.m" ? ctx->hh.gm : (nm == "hh.h" ? ctx->hh.gh : ctx->hh.gn);
+        HHState& hh = ctx->hh;
+        DevBuf& b = nm == "hh.m" ? hh.gm : nm == "hh.h" ? hh.gh : nm == "hh.n" ? hh.gn :
+                    nm == "hh.gna_coef" ? hh.cna : nm == "hh.gk_coef" ? hh.ck : hh.cl;
         return upload_convert(ctx, b.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
     }
     if (nm == "kinetic.state") {
@@ -427,9 +439,12 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
     if (nm == "Segment.nonspecific_current") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->Inonspec.ptr, rd, count); }
     if (nm == "Segment.capacitance") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->cap64.ptr, NW_DTYPE_F64, count); }
     if (nm == "Segment.axial_resistance") { NW_CHECK(need(ctx->n_seg)); return download_convert(ctx, host, dtype, ctx->res64.ptr, NW_DTYPE_F64, count); }
-    if (nm == "hh.m" || nm == "hh.h" || nm == "hh.n") {
+    if (nm == "hh.m" || nm == "hh.h" || nm == "hh.n" ||
+        nm == "hh.gna_coef" || nm == "hh.gk_coef" || nm == "hh.gl_coef") {
         NW_CHECK(need(ctx->hh.m));
-        const DevBuf& b = nm == "hh.m" ? ctx->hh.gm : (nm == "hh.h" ? ctx->hh.gh : ctx->hh.gn);
+        const HHState& hh = ctx->hh;
+        const DevBuf& b = nm == "hh.m" ? hh.gm : nm == "hh.h" ? hh.gh : nm == "hh.n" ? hh.gn :
+                          nm == "hh.gna_coef" ? hh.cna : nm == "hh.gk_coef" ? hh.ck : hh.cl;
         std::vector<double> sorted(count);
         NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, b.ptr, rd, count));
         for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[ctx->hh.user_to_sorted[i]]);
@@ -869,6 +884,19 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     if (!ctx || !name) return NW_ERR_ARG;
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
+    if (nm == "reset_clock") {
+        // Back to time 0: clock, conductance validity, detector state and probes.
+        ctx->input_ticks = ctx->steps = 0;
+        ctx->g_valid = false;
+        ctx->probe_len = 0;
+        if (ctx->have_detectors) {
+            NW_CUDA(ctx, cudaMemsetAsync(ctx->ap_detected.ptr, 0, ctx->n_neuron, ctx->stream));
+            NW_CUDA(ctx, cudaMemsetAsync(ctx->ap_state.ptr, 0, ctx->n_neuron, ctx->stream));
+            NW_CUDA(ctx, cudaMemsetAsync(ctx->spike_count.ptr, 0, 4 * ctx->n_neuron, ctx->stream));
+            NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        }
+        return NW_OK;
+    }
     return fail(ctx, NW_ERR_ARG, "nw_set_option: unknown option " + nm);
 }
 
@@ -878,6 +906,20 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "bulk_pipeline") { *value = ctx->use_bulk ? 1 : 0; return NW_OK; }
     if (nm == "bulk_pipeline_active") { *value = uses_bulk_pipeline(ctx) ? 1 : 0; return NW_OK; }
     return fail(ctx, NW_ERR_ARG, "nw_get_option: unknown option " + nm);
+}
+
+int nw_adjoint_forward(nw_ctx* ctx, int64_t num_steps, int32_t checkpoint_every, const double* target,
+                       double* loss_out) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    return adjoint_forward(ctx, num_steps, checkpoint_every, target, loss_out);
+}
+
+int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad_gna, double* grad_gk,
+                        double* grad_gl, double* grad_ra) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    return adjoint_backward(ctx, cytoplasmic_resistance, grad_gna, grad_gk, grad_gl, grad_ra);
 }
 
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm) {

@@ -55,6 +55,16 @@ struct KineticState {
     std::vector<int64_t> h_neuron_ptr;
 };
 
+struct AdjointState {
+    bool ready = false, g_valid0 = false;
+    int K = 0;
+    int64_t total_steps = 0, tick0 = 0;
+    double loss = 0.0;
+    DevBuf ckpt, target, loss_part, tape;
+    DevBuf lamV, lamV2, lamM, lamH, lamN;
+    DevBuf gGna, gGk, gGl, ra_part;
+};
+
 }  // namespace nw
 
 struct nw_ctx {
@@ -88,6 +98,7 @@ struct nw_ctx {
     // Mechanisms.
     nw::HHState hh;
     nw::KineticState kin;
+    nw::AdjointState adj;
     bool g_valid = false;       // conductances computed by a mechanism step
 
     // Clamps (sorted by neuron, stable).
@@ -137,6 +148,10 @@ int advance_batched(nw_ctx* ctx, int k_steps);
 int advance_plain(nw_ctx* ctx, int k_steps);
 int choose_lanes_per_row(nw_ctx* ctx);
 bool uses_bulk_pipeline(nw_ctx* ctx);
+
+// Adjoint (nw_adjoint.cu).
+int adjoint_forward(nw_ctx* ctx, int64_t T, int K, const double* target, double* loss_out);
+int adjoint_backward(nw_ctx* ctx, double Ra, double* g_gna, double* g_gk, double* g_gl, double* g_ra);
 
 // Device conversions (nw_api.cu).
 int upload_convert(nw_ctx* ctx, void* dst, int dst_dtype, const void* host, int src_dtype,

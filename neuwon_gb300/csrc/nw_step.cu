@@ -23,306 +23,9 @@
 #include <algorithm>
 #include <type_traits>
 
-#include "nw_internal.cuh"
+#include "nw_step_common.cuh"
 
 namespace nw {
-
-template <typename real> __device__ __forceinline__ real d_exp(real x);
-template <> __device__ __forceinline__ float d_exp<float>(float x) { return expf(x); }
-template <> __device__ __forceinline__ double d_exp<double>(double x) { return exp(x); }
-template <typename real> __device__ __forceinline__ real d_expm1(real x);
-template <> __device__ __forceinline__ float d_expm1<float>(float x) { return expm1f(x); }
-template <> __device__ __forceinline__ double d_expm1<double>(double x) { return expm1(x); }
-
-// FUNCTION vtrap (nmodl_library/artificial/hh.mod:88-94).  x/(exp(x/y)-1) is
-// evaluated as x/expm1(x/y), the same quantity without cancellation.
-template <typename real>
-__device__ __forceinline__ real vtrap(real x, real y) {
-    real r = x / y;
-    if (fabs(r) < real(1e-6)) return y * (real(1) - r / real(2));
-    return x / d_expm1(r);
-}
-
-// rates(v) and the exact gate update x <- xinf + (x - xinf) exp(-dt/xtau)
-// (hh.mod:55-86, nmodl/solver.py:48-55); dtq10 = dt * q10, so
-// dt/xtau = dtq10 * (alpha + beta).
-template <typename real>
-__device__ __forceinline__ void hh_gates(real v, real dtq10, real& m, real& h, real& n) {
-    real a = real(0.1) * vtrap(-(v + real(40)), real(10));
-    real b = real(4) * d_exp(-(v + real(65)) / real(18));
-    real s = a + b, inf = a / s;
-    m = inf + (m - inf) * d_exp(-dtq10 * s);
-    a = real(0.07) * d_exp(-(v + real(65)) / real(20));
-    b = real(1) / (d_exp(-(v + real(35)) / real(10)) + real(1));
-    s = a + b; inf = a / s;
-    h = inf + (h - inf) * d_exp(-dtq10 * s);
-    a = real(0.01) * vtrap(-(v + real(55)), real(10));
-    b = real(0.125) * d_exp(-(v + real(65)) / real(80));
-    s = a + b; inf = a / s;
-    n = inf + (n - inf) * d_exp(-dtq10 * s);
-}
-
-template <typename real>
-struct StepArgs {
-    int64_t n_neuron;
-    const int64_t* neuron_start;
-    const int32_t* neuron_order;
-    int* work_counter;
-    int* status;
-    real* V; real* Vint;
-    const real* kI; const real* kG; const real* Inonspec; int has_nonspec;
-    // batched propagator
-    const int64_t* rowptr; const uint16_t* col; const real* val; const real* leak;
-    // plain propagator
-    const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
-    // hh
-    int hh_on, hh_identity;
-    const uint32_t* hh_seg_ptr; const int64_t* hh_neuron_ptr; const uint32_t* hh_seg;
-    real* gm; real* gh; real* gn; const real* cna; const real* ck; const real* cl;
-    real ena, ek, el, dtq10;
-    // kinetic scheme (lti_sim)
-    int kin_on, kin_identity, kin_S, kin_T, kin_nb, kin_nopen;
-    int kin_open[4];
-    int64_t kin_m;
-    const uint32_t* kin_seg_ptr; const int64_t* kin_neuron_ptr; const uint32_t* kin_seg;
-    real* kin_state; const real* kin_gcoef; const real* kin_table;
-    real kin_vmin, kin_frq, kin_cs, kin_erev;
-    // clamps
-    const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
-    const int64_t* clamp_first; const int64_t* clamp_count;
-    // detectors
-    int has_det;
-    const uint32_t* det_seg; const real* det_thr;
-    uint8_t* ap_detected; uint8_t* ap_state; uint32_t* spike_count;
-    // probes
-    const int32_t* probe_neuron_ptr; const uint32_t* probe_seg; const uint32_t* probe_slot;
-    real* trace; int64_t n_probes; int64_t trace_row0;
-    // time
-    int64_t tick0; int k_steps; int g_valid; real h_s;
-};
-
-// Sum of a segment's mechanism conductances and conductance-weighted reversal
-// potentials (species.py:389-393 scatter, done here as a gather over the
-// segment's instances in registration order: deterministic, no atomics).
-template <typename real>
-__device__ __forceinline__ void segment_conductance(const StepArgs<real>& a, int64_t i, real& G, real& GE) {
-    G = real(0); GE = real(0);
-    if (a.hh_on) {
-        int64_t b, e;
-        if (a.hh_identity) { b = i; e = i + 1; }
-        else { b = a.hh_seg_ptr[i]; e = a.hh_seg_ptr[i + 1]; }
-        real gna = real(0), gk = real(0), gl = real(0);
-        for (int64_t k = b; k < e; ++k) {
-            real m = a.gm[k], h = a.gh[k], n = a.gn[k];
-            gna += a.cna[k] * m * m * m * h;
-            gk += a.ck[k] * n * n * n * n;
-            gl += a.cl[k];
-        }
-        G = (gna + gk) + gl;
-        GE = (gna * a.ena + gk * a.ek) + gl * a.el;
-    }
-    if (a.kin_on) {
-        int64_t b, e;
-        if (a.kin_identity) { b = i; e = i + 1; }
-        else { b = a.kin_seg_ptr[i]; e = a.kin_seg_ptr[i + 1]; }
-        real gkin = real(0);
-        for (int64_t k = b; k < e; ++k) {
-            real open = real(0);
-            for (int o = 0; o < a.kin_nopen; ++o) open += a.kin_state[(int64_t)a.kin_open[o] * a.kin_m + k];
-            gkin += a.kin_gcoef[k] * open;
-        }
-        G += gkin;
-        GE += gkin * a.kin_erev;
-    }
-}
-
-// Voltage -> (bucket, location within it) as the generated lti_sim kernel
-// computes them (codegen.py:43-59): bucket = trunc((v - vmin) * frq), clamped to
-// the table, location 1 above it and 0 below it.  Non-finite voltages land in bucket 0.
-template <typename real>
-__device__ __forceinline__ int kinetic_locate(const StepArgs<real>& a, real v, real& loc) {
-    real x = (v - a.kin_vmin) * a.kin_frq;
-    if (!(x > real(-2))) x = real(-2);
-    if (x > real(a.kin_nb + 1)) x = real(a.kin_nb + 1);
-    int b = (int)x;
-    if (b > a.kin_nb - 1) { b = a.kin_nb - 1; loc = real(1); }
-    else if (b < 0) { b = 0; loc = real(0); }
-    else loc = x - real(b);
-    return b;
-}
-
-// One exact-integration step of a kinetic instance (codegen.py:60-106): the
-// polynomial approximation of the column-normalised propagator, evaluated per
-// (col, row) as table[bucket][col][row][term], times the state, then CONSERVE.
-template <typename real, int S, int T>
-__device__ __forceinline__ void kinetic_step_fixed(const StepArgs<real>& a, int64_t k, real v) {
-    real loc;
-    const int b = kinetic_locate(a, v, loc);
-    real basis[T];
-    basis[0] = real(1);
-#pragma unroll
-    for (int t = 1; t < T; ++t) basis[t] = basis[t - 1] * loc;
-    const real* __restrict__ tb = a.kin_table + (int64_t)b * (S * S * T);
-    real st[S], out[S];
-#pragma unroll
-    for (int c = 0; c < S; ++c) { st[c] = a.kin_state[(int64_t)c * a.kin_m + k]; out[c] = real(0); }
-#pragma unroll
-    for (int col = 0; col < S; ++col) {
-#pragma unroll
-        for (int row = 0; row < S; ++row) {
-            const real* p = tb + (col * S + row) * T;
-            real poly = real(0) + __ldg(p);
-#pragma unroll
-            for (int t = 1; t < T; ++t) poly += basis[t] * __ldg(p + t);
-            out[row] += poly * st[col];
-        }
-    }
-    if (a.kin_cs > real(0)) {
-        real sum = out[0];
-#pragma unroll
-        for (int c = 1; c < S; ++c) sum += out[c];
-        const real f = a.kin_cs / sum;
-#pragma unroll
-        for (int c = 0; c < S; ++c) out[c] *= f;
-    }
-#pragma unroll
-    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = out[c];
-}
-
-// Same step for any S <= 16 and T <= 4.
-template <typename real>
-__device__ __noinline__ void kinetic_step_generic(const StepArgs<real>& a, int64_t k, real v) {
-    const int S = a.kin_S, T = a.kin_T;
-    real loc;
-    const int b = kinetic_locate(a, v, loc);
-    real basis[4] = {real(1), loc, loc * loc, loc * loc * loc};
-    const real* tb = a.kin_table + (int64_t)b * (S * S * T);
-    real st[16], out[16];
-    for (int c = 0; c < S; ++c) { st[c] = a.kin_state[(int64_t)c * a.kin_m + k]; out[c] = real(0); }
-    for (int col = 0; col < S; ++col)
-        for (int row = 0; row < S; ++row) {
-            const real* p = tb + (col * S + row) * T;
-            real poly = real(0) + p[0];
-            for (int t = 1; t < T; ++t) poly += basis[t] * p[t];
-            out[row] += poly * st[col];
-        }
-    if (a.kin_cs > real(0)) {
-        real sum = out[0];
-        for (int c = 1; c < S; ++c) sum += out[c];
-        const real f = a.kin_cs / sum;
-        for (int c = 0; c < S; ++c) out[c] *= f;
-    }
-    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = out[c];
-}
-
-template <typename real>
-__device__ __forceinline__ void kinetic_step(const StepArgs<real>& a, int64_t k, real v) {
-    if (a.kin_S == 8 && a.kin_T == 2) kinetic_step_fixed<real, 8, 2>(a, k, v);
-    else kinetic_step_generic(a, k, v);
-}
-
-// Exact exponential membrane update of one segment (electric.py:60-76).
-template <typename real>
-__device__ __forceinline__ real membrane_x(const StepArgs<real>& a, int64_t i, real G, real GE, real I,
-                                           bool store_integral) {
-    real v = a.V[i];
-    real E = (G != real(0)) ? GE / G : real(0);          // nan_to_num(GE/G), rxd_model.py:106-109
-    real expo = -a.kG[i] * G;
-    real alpha = d_exp(expo);
-    real dv = a.kI[i] * I;
-    real diff = E - v;
-    real x = E - diff * alpha + dv;
-    if (store_integral) a.Vint[i] = a.h_s * E - expo * diff * alpha + real(0.5) * a.h_s * dv;
-    return x;
-}
-
-// Propagator entries are streamed once per half step and do not fit in L2, so
-// they are loaded with the evict-first (streaming) cache hint.
-template <typename real> struct Vec4Loader;
-template <> struct Vec4Loader<float> {
-    static __device__ __forceinline__ void load(const float* p, float (&v)[4]) {
-        float4 q = __ldcs(reinterpret_cast<const float4*>(p));
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-    }
-};
-template <> struct Vec4Loader<double> {
-    static __device__ __forceinline__ void load(const double* p, double (&v)[4]) {
-        double2 q0 = __ldcs(reinterpret_cast<const double2*>(p));
-        double2 q1 = __ldcs(reinterpret_cast<const double2*>(p) + 1);
-        v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
-    }
-};
-
-template <typename real>
-__device__ __forceinline__ void kahan_add(real& s, real& c, real term) {
-    real y = term - c;
-    real t = s + y;
-    c = (t - s) - y;
-    s = t;
-}
-
-// Four entries of a row: sum of P_ij (x_j - x_i), added pairwise; the running
-// row sum around it is compensated (kahan_add), so the dependent chain per lane
-// is one compensated add per 4 entries.
-template <typename real>
-__device__ __forceinline__ real quad_sum(const real (&v)[4], const ushort4 cc, const real* __restrict__ xs,
-                                         real xi) {
-    const real a = v[0] * (xs[cc.x] - xi) + v[1] * (xs[cc.y] - xi);
-    const real b = v[2] * (xs[cc.z] - xi) + v[3] * (xs[cc.w] - xi);
-    return a + b;
-}
-
-// V_i <- propagator row i applied to xs, for every row of one neuron.
-template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2)>
-__device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_t base, int n,
-                                                 const real* __restrict__ xs) {
-    constexpr int GPW = 32 / LPR;                  // row groups per warp
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int nwarps = blockDim.x >> 5;
-    const int q = lane / LPR, l = lane % LPR;
-    for (int rb = warp * GPW; rb < n; rb += nwarps * GPW) {
-        const int row = rb + q;
-        const bool valid = row < n;
-        real s = real(0), c = real(0), xi = real(0);
-        if (valid) {
-            const int64_t r = base + row;
-            const int64_t beg = a.rowptr[r], end = a.rowptr[r + 1];
-            xi = xs[row];
-            // UNROLL chunks of 4 entries per lane are loaded before any is consumed,
-            // to keep enough bytes in flight per SM for HBM latency.
-            for (int64_t k0 = beg + 4 * l; k0 < end; k0 += 4 * LPR * UNROLL) {
-                real v[UNROLL][4];
-                ushort4 cc[UNROLL];
-#pragma unroll
-                for (int u = 0; u < UNROLL; ++u) {
-                    const int64_t k = k0 + 4 * LPR * u;
-                    if (k < end) {
-                        Vec4Loader<real>::load(a.val + k, v[u]);
-                        cc[u] = __ldcs(reinterpret_cast<const ushort4*>(a.col + k));
-                    } else {
-                        v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
-                        cc[u] = make_ushort4(0, 0, 0, 0);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < UNROLL; ++u)
-                    kahan_add(s, c, quad_sum(v[u], cc[u], xs, xi));
-            }
-        }
-        real t = s - c;
-#pragma unroll
-        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-        if (valid && l == 0) {
-            const int64_t r = base + row;
-            const real vnew = (xi - a.leak[r] * xi) + t;
-            if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
-            a.V[r] = vnew;
-        }
-    }
-}
-
-
 // ----------------------------------------------------------------------------
 // Asynchronous bulk-copy pipeline for the propagator stream (FP32 path).
 //
@@ -717,65 +420,6 @@ __global__ void plain_detect_kernel(const StepArgs<real> a, int64_t row) {
 
 // ------------------------------------------------------------ host side
 
-template <typename real>
-static StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
-    StepArgs<real> a{};
-    a.n_neuron = ctx->n_neuron;
-    a.neuron_start = ctx->neuron_start.as<int64_t>();
-    a.neuron_order = ctx->neuron_order.as<int32_t>();
-    a.work_counter = ctx->work_counter.as<int>();
-    a.status = ctx->status.as<int>();
-    a.V = ctx->V.as<real>(); a.Vint = ctx->Vint.as<real>();
-    a.kI = ctx->kI.as<real>(); a.kG = ctx->kG.as<real>();
-    a.Inonspec = ctx->Inonspec.as<real>(); a.has_nonspec = ctx->nonspec_nonzero ? 1 : 0;
-    a.rowptr = ctx->b_rowptr.as<int64_t>(); a.col = ctx->b_col.as<uint16_t>();
-    a.val = ctx->b_val.as<real>(); a.leak = ctx->b_leak.as<real>();
-    a.prow = ctx->p_rowptr.as<int64_t>(); a.pcol = ctx->p_col.as<int32_t>(); a.pval = ctx->p_val.as<double>();
-    a.px = ctx->plain_x.as<real>();
-    const HHState& hh = ctx->hh;
-    a.hh_on = hh.m > 0 ? 1 : 0;
-    a.hh_identity = hh.identity ? 1 : 0;
-    a.hh_seg_ptr = hh.seg_ptr.as<uint32_t>(); a.hh_neuron_ptr = hh.neuron_ptr.as<int64_t>();
-    a.hh_seg = hh.seg.as<uint32_t>();
-    a.gm = hh.gm.as<real>(); a.gh = hh.gh.as<real>(); a.gn = hh.gn.as<real>();
-    a.cna = hh.cna.as<real>(); a.ck = hh.ck.as<real>(); a.cl = hh.cl.as<real>();
-    a.ena = (real)hh.ena; a.ek = (real)hh.ek; a.el = (real)hh.el;
-    const KineticState& K = ctx->kin;
-    a.kin_on = K.m > 0 ? 1 : 0;
-    a.kin_identity = K.identity ? 1 : 0;
-    a.kin_S = K.S; a.kin_T = K.T; a.kin_nb = K.nb; a.kin_nopen = K.n_open;
-    for (int o = 0; o < 4; ++o) a.kin_open[o] = K.open[o];
-    a.kin_m = K.m;
-    a.kin_seg_ptr = K.seg_ptr.as<uint32_t>(); a.kin_neuron_ptr = K.neuron_ptr.as<int64_t>();
-    a.kin_seg = K.seg.as<uint32_t>();
-    a.kin_state = K.state.as<real>(); a.kin_gcoef = K.gcoef.as<real>(); a.kin_table = K.table.as<real>();
-    a.kin_vmin = (real)K.vmin; a.kin_frq = (real)K.frq; a.kin_cs = (real)K.conserve; a.kin_erev = (real)K.erev;
-    const double q10 = pow(3.0, (ctx->celsius - 6.3) / 10.0);      // hh.mod:67
-    a.dtq10 = (real)(ctx->time_step * q10);
-    if (ctx->n_clamps) {
-        a.clamp_neuron_ptr = ctx->clamp_neuron_ptr.as<int32_t>();
-        a.clamp_seg = ctx->clamp_seg.as<uint32_t>(); a.clamp_amp = ctx->clamp_amp.as<real>();
-        a.clamp_first = ctx->clamp_first.as<int64_t>(); a.clamp_count = ctx->clamp_count.as<int64_t>();
-    }
-    a.has_det = ctx->have_detectors ? 1 : 0;
-    a.det_seg = ctx->det_seg.as<uint32_t>(); a.det_thr = ctx->det_thr.as<real>();
-    a.ap_detected = ctx->ap_detected.as<uint8_t>(); a.ap_state = ctx->ap_state.as<uint8_t>();
-    a.spike_count = ctx->spike_count.as<uint32_t>();
-    a.n_probes = ctx->n_probes;
-    if (ctx->n_probes) {
-        a.probe_neuron_ptr = ctx->probe_neuron_ptr.as<int32_t>();
-        a.probe_seg = ctx->probe_seg.as<uint32_t>(); a.probe_slot = ctx->probe_slot.as<uint32_t>();
-        a.trace = ctx->trace.as<real>(); a.trace_row0 = ctx->probe_len;
-    }
-    a.tick0 = ctx->input_ticks;
-    a.k_steps = k_steps;
-    a.g_valid = ctx->g_valid ? 1 : 0;
-    a.h_s = (real)(0.5 * ctx->time_step * 1e-3);
-    return a;
-}
-
-// Lanes per propagator row (measured on GB300 with ~490 entries/row: 16 lanes and
-// 1,024 threads beat 32 lanes; 8 lanes is too few for such rows).
 int choose_lanes_per_row(nw_ctx* ctx) {
     if (ctx->lanes_per_row) return ctx->lanes_per_row;
     double avg = ctx->n_seg ? (double)ctx->nnz_b / (double)ctx->n_seg : 0.0;

@@ -91,6 +91,20 @@ class HH(Mechanism):
         return cls
 
 
+def hh_steady_state(v, celsius=6.3):
+    """Steady-state (m, h, n) of hh.mod at voltage v (INITIAL block, hh.mod:48-53)."""
+    v = np.asarray(v, dtype=np.float64)
+
+    def vtrap(x, y):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            big = x / np.expm1(x / y)
+        return np.where(np.abs(x / y) < 1e-6, y * (1 - x / y / 2), big)
+    a = .1 * vtrap(-(v + 40), 10); b = 4 * np.exp(-(v + 65) / 18); m = a / (a + b)
+    a = .07 * np.exp(-(v + 65) / 20); b = 1 / (np.exp(-(v + 35) / 10) + 1); h = a / (a + b)
+    a = .01 * vtrap(-(v + 55), 10); b = .125 * np.exp(-(v + 65) / 80); n = a / (a + b)
+    return m, h, n
+
+
 def NMODL(filename, use_cache=True):
     """Minimal NMODL front end: maps a .mod file onto a GPU mechanism.
 

@@ -22,7 +22,7 @@ import numpy as np
 from . import _lib
 from .morphology import EPSILON, Tree, geometry, passive_electric
 from .kinetic import Kinetic
-from .mechanisms import HH, Mechanism
+from .mechanisms import HH, Mechanism, hh_steady_state
 
 
 class Clock:
@@ -374,6 +374,49 @@ class RxD_Model:
         self.input_hook.ticks += 2 * k
         self.advance_hook._tick(k)
 
+    # --------------------------------------------------- differentiation helpers
+    def set_hh_densities(self, gnabar, gkbar, glbar):
+        """Per-instance HH densities (S/cm2, registration order) without a rebuild."""
+        self._sync()
+        scale = 1e-8 * self._hh_magnitude                     # nmodl/__init__.py:103-107, 404-406
+        for name, dens in (("hh.gna_coef", gnabar), ("hh.gk_coef", gkbar), ("hh.gl_coef", glbar)):
+            d = np.broadcast_to(np.asarray(dens, dtype=np.float64), scale.shape)
+            self._ctx.set_data(name, np.ascontiguousarray(d * scale))
+
+    def hh_density_scale(self):
+        """d coefficient (S) / d density (S/cm2) for every HH instance."""
+        self._sync()
+        return 1e-8 * self._hh_magnitude
+
+    def set_cytoplasmic_resistance(self, ra):
+        """Change Ra (ohm cm); the propagator is rebuilt before the next step."""
+        ra = float(ra)
+        if ra != self.cytoplasmic_resistance:
+            self.cytoplasmic_resistance = ra
+            self._geom_cache = None
+            self._dirty_structure = True
+
+    def reset_state(self):
+        """Back to t = 0: initial voltage, steady-state gates, clock and detectors reset."""
+        self._sync()
+        n = self._n
+        self._ctx.set_data("Segment.voltage", np.full(n, self.initial_voltage))
+        for name, cls in self.mechanisms.items():
+            if issubclass(cls, HH):
+                m = self._instance_count(name)
+                g = hh_steady_state(self.initial_voltage, self.temperature)
+                for attr, val in zip(("hh.m", "hh.h", "hh.n"), g):
+                    self._ctx.set_data(attr, np.full(m, float(val)))
+            elif issubclass(cls, Kinetic):
+                m = self._instance_count(name)
+                sch = cls.scheme_factory()
+                init = sch.steady_state(self.initial_voltage, self.temperature)
+                self._ctx.set_data("kinetic.state", np.tile(init, m))
+        self._ctx.call("nw_set_option", b"reset_clock", 1)
+        self.input_hook.ticks = 0
+        self.advance_hook.ticks = 0
+        self._flush_probes()
+
     def check(self):
         v = self.get_data("Segment.voltage")
         assert np.all(np.isfinite(v)), "non-finite voltage"
@@ -597,6 +640,7 @@ class RxD_Model:
         gna = coef("gnabar", cls.gnabar)
         gk = coef("gkbar", cls.gkbar)
         gl = coef("glbar", cls.glbar)
+        self._hh_magnitude = magnitude.copy()
         seg_dev = np.ascontiguousarray(self._inv[seg]) if len(seg) else seg
         self._ctx.call("nw_hh_register", len(seg), _lib.ptr(seg_dev),
                        _lib.ptr(gna), _lib.ptr(gk), _lib.ptr(gl),
