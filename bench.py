@@ -210,6 +210,61 @@ def plain_timing(trees, currents, tol, device, steps=10):
                       "32 threads/block, FP64 CSR, same propagator tolerance"}
 
 
+def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
+    """Config 4 shape: 256 HH neurons of 2,000 segments, dt 0.025 ms, FP32, targets = FP64
+    soma traces of the same neurons with densities drawn +-30 % around the defaults;
+    gradients of the soma MSE w.r.t. per-segment gNa/gK/gL and Ra (checkpoint every 100)."""
+    import torch
+    from neuwon_gb300 import HH, RxD_Model
+    from neuwon_gb300.adjoint import _backward, _forward
+    from neuwon_gb300.morphology import random_tree
+    from neuwon_gb300.workloads import HH_PARAMS
+    trees = [random_tree(size, seed=5000 + k) for k in range(neurons)]
+    rng = np.random.default_rng(4)
+
+    def build(precision):
+        m = RxD_Model(time_step=0.025, temperature=6.3, precision=precision, device=device,
+                      propagator_tolerance=1e-8, propagator_conserve=True,
+                      mechanisms=[HH.configure(**HH_PARAMS)])
+        ns = [m.add_tree(t) for t in trees]
+        m.insert_everywhere("hh")
+        for nr in ns:
+            nr.root.inject_current(0.3, 1e9)
+        m._sync()
+        return m
+    k = neurons * size
+    m64 = build("f64")
+    m64.set_hh_densities(*(rng.uniform(0.7, 1.3, k) * HH_PARAMS[g] for g in ("gnabar", "gkbar", "glbar")))
+    m64.reset_state()
+    m64._ctx.call("nw_probes_set", len(trees), _lib_ptr(np.array(m64._neuron_root, dtype=np.int64)), steps)
+    m64._ctx.advance(steps)
+    target = np.empty((steps, len(trees)))
+    s_out = ctypes.c_int64()
+    m64._ctx.call("nw_probes_read", _lib_ptr(target), 1, steps, ctypes.byref(s_out))
+    m64.close()
+    m = build("f32")
+    m.reset_state()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = _forward(m, steps, target, checkpoint_every)
+    t1 = time.perf_counter()
+    gna, gk, gl, gra = _backward(m)
+    t2 = time.perf_counter()
+    m.close()
+    return {"ms_per_step": 1e3 * (t2 - t0) / steps, "forward_ms_per_step": 1e3 * (t1 - t0) / steps,
+            "backward_ms_per_step": 1e3 * (t2 - t1) / steps, "steps": steps,
+            "checkpoint_every": checkpoint_every, "loss_mV2": loss,
+            "grad_norm": float(np.sqrt((gna ** 2).sum() + (gk ** 2).sum() + (gl ** 2).sum())),
+            "grad_ra": gra, "parameters": 3 * k + 1,
+            "config": f"{neurons} HH neurons x {size} segments, dt 0.025 ms, FP32, propagator 1e-8 "
+                      "(charge-conserving), targets from FP64 runs with densities +-30 %"}
+
+
+def _lib_ptr(a):
+    from neuwon_gb300 import _lib
+    return _lib.ptr(a)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -227,7 +282,8 @@ def main():
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
-    ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu legs")
+    ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu/adjoint legs")
+    ap.add_argument("--adjoint-steps", type=int, default=800)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -261,6 +317,9 @@ def main():
         log(f"plain: {extra['plain_fp64']}")
 
     from neuwon_gb300 import _lib
+    if not args.quick and rank == 0 and args.adjoint_steps > 0:
+        extra["adjoint"] = adjoint_leg(local, args.adjoint_steps)
+        log(f"adjoint: {extra['adjoint']}")
     t_build = time.perf_counter()
     model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, conserve=True,
                                  device=local)
