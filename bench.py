@@ -236,7 +236,8 @@ def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
     m64 = build("f64")
     m64.set_hh_densities(*(rng.uniform(0.7, 1.3, k) * HH_PARAMS[g] for g in ("gnabar", "gkbar", "glbar")))
     m64.reset_state()
-    m64._ctx.call("nw_probes_set", len(trees), _lib_ptr(np.array(m64._neuron_root, dtype=np.int64)), steps)
+    roots = np.array(m64._neuron_root, dtype=np.int64)
+    m64._ctx.call("nw_probes_set", len(trees), _lib_ptr(roots), steps)
     m64._ctx.advance(steps)
     target = np.empty((steps, len(trees)))
     s_out = ctypes.c_int64()

@@ -91,11 +91,13 @@ def load(build_if_missing=True):
 
 
 def ptr(a):
-    """Data pointer of a C-contiguous numpy array (or None)."""
+    """Data pointer of a C-contiguous numpy array (or None).  The returned ctypes
+    object keeps a reference to the array, so a temporary passed inline stays
+    alive for the duration of the call."""
     if a is None:
         return None
     assert a.flags["C_CONTIGUOUS"]
-    return ctypes.c_void_p(a.ctypes.data)
+    return a.ctypes.data_as(ctypes.c_void_p)
 
 
 class Context:
