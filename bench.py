@@ -28,6 +28,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoint ms/step"
 
+# DRAM bytes (read + write) per segment-step of batched_advance_kernel, from one ncu
+# capture of one 50-step launch of the default configuration (tolerance 1e-8, 1,024
+# neurons, 5,593,190 segments): 1,741.6 GB per launch.  Command and figures:
+# profiles/batched_advance_kernel.md.
+NCU_TRAFFIC_PER_SEGMENT_STEP = 6227.5
+NCU_TRAFFIC_CONFIG = (1e-8, 5593190)
+
 
 def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
     """B = 2(8r + 4) + 4(2 + 2 S_total + P_seg + 1): two propagator passes (4 B value +
@@ -166,17 +173,22 @@ def accuracy(trees, currents, tol, device, steps, ref_tol):
     pruned at ref_tol (both charge-conserving)."""
     from neuwon_gb300 import Segment, TimeSeries
     from neuwon_gb300.workloads import build_model
+    t0 = time.perf_counter()
     ref, nref = build_model(trees, currents, precision="f64", tolerance=ref_tol, conserve=True, device=device)
     test, ntest = build_model(trees, currents, precision="f32", tolerance=tol, conserve=True, device=device)
     probes = []
     for m, ns in ((ref, nref), (test, ntest)):
         probes.append([TimeSeries().record(nr.root, "voltage") for nr in ns])
     ref._sync(); test._sync()
+    log(f"accuracy models built in {time.perf_counter() - t0:.1f} s "
+        f"(reference {ref.propagator_nnz / ref._n:.0f} entries/row)")
+    t0 = time.perf_counter()
     worst_all, chunk = 0.0, 50
     for _ in range(steps // chunk):
         ref.advance(chunk); test.advance(chunk)
         worst_all = max(worst_all, float(np.abs(ref.get_data("Segment.voltage") -
                                                 test.get_data("Segment.voltage")).max()))
+    log(f"accuracy run of {steps} steps in {time.perf_counter() - t0:.1f} s")
     soma_ref = np.array([p.get_data() for p in probes[0]])
     soma_test = np.array([p.get_data() for p in probes[1]])
     sp_ref = ref.get_data("Neuron.spike_count"); sp_test = test.get_data("Neuron.spike_count")
@@ -274,7 +286,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--neurons", type=int, default=1024)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--ref-tol", type=float, default=1e-11,
+    ap.add_argument("--ref-tol", type=float, default=1e-10,
                     help="pruning of the FP64 accuracy reference (machine epsilon makes rows dense)")
     ap.add_argument("--size-range", default="500,20000", help="neuron size range (segments)")
     ap.add_argument("--acc-neurons", type=int, default=16)
@@ -445,7 +457,11 @@ def main():
                    f"{pbytes.value / 1e9:.1f} GB), no flush", "mechanisms": ["hh", "na8 (8-state Markov Na, LTI voltage table 1600 x 0.1 mV, linear)"],
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": (NCU_TRAFFIC_PER_SEGMENT_STEP * n * F
+                                 if (args.tol, n) == NCU_TRAFFIC_CONFIG else None),
+                     "traffic_unit": f"bytes per launch of {F} steps (ncu dram__bytes_read+write)",
+                     "algorithmic_bytes_per_launch": B_alg * n * F,
                      "peak_source": peak_src,
                      "bytes_per_segment_step": B_alg,
                      "format_bytes_per_segment_step": B_fmt,

@@ -21,7 +21,7 @@
 // root-to-leaves sweep per neuron and pole), after which row i of the
 // resolvent is a product of edge ratios along the path from i.  Row i of P
 // is then collected by a depth-first walk outward from i that keeps entries
-// with |P_ij| >= tol and stops exploring a branch once |P_ij| < tol * 1e-3.
+// with |P_ij| >= tol and stops exploring a branch once |P_ij| < tol * 1e-2.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -32,8 +32,8 @@ namespace nw {
 
 constexpr int kPoles = 16;            // N/2 for N = 32
 constexpr int kNodes = 2 * kPoles;
-constexpr int kStackDepth = 96;
-constexpr double kExploreFactor = 1e-3;
+constexpr int kStackDepth = 64;
+constexpr double kExploreFactor = 1e-2;
 constexpr int kStatusStackOverflow = 2;
 constexpr int kStatusRowMismatch = 4;
 
@@ -72,7 +72,8 @@ struct BuildArgs {
     const double* res;          // ohm
     const double* gsum;         // sum of 1/R over the edges at each node
     double h_s;                 // half step in seconds
-    // per pole, per node (index pole * n_seg + node)
+    // per node, per pole (index node * kPoles + pole): the 16 lanes of a warp read
+    // one node's values as one contiguous 256-byte line
     double2* down;              // pivot of the branch below node c, seen from its parent
     double2* up;                // pivot of the rest of the tree, seen from c
     double2* invT;              // 1 / total pivot: diagonal of the resolvent
@@ -92,36 +93,37 @@ __global__ void edge_pivots_kernel(const BuildArgs a) {
     const int k = (int)(t % kPoles);
     const int64_t b = a.neuron_start[j], e = a.neuron_start[j + 1];
     const cplx z = cplx(c_z[k].x, c_z[k].y);
-    double2* down = a.down + k * a.n_seg;
-    double2* up = a.up + k * a.n_seg;
-    double2* invT = a.invT + k * a.n_seg;
+    // Node-major layout: element c of pole k lives at c * kPoles + k.
+    auto D = [&](int64_t c) -> double2* { return a.down + c * kPoles + k; };
+    auto U = [&](int64_t c) -> double2* { return a.up + c * kPoles + k; };
+    auto IT = [&](int64_t c) -> double2* { return a.invT + c * kPoles + k; };
     // M = zI - A^T: M_cc = z + h * gsum_c / C_c; M_pc * M_cp = a_pc * a_cp with
     // a_pc = h/(R_c C_p), a_cp = h/(R_c C_c) for the edge of child c.
-    for (int64_t c = b; c < e; ++c) st(&down[c], z + cplx(a.h_s * a.gsum[c] / a.cap[c], 0.0));
+    for (int64_t c = b; c < e; ++c) st(D(c), z + cplx(a.h_s * a.gsum[c] / a.cap[c], 0.0));
     for (int64_t c = e - 1; c >= b; --c) {
         const int64_t p = a.parent[c];
         if (p < 0) continue;
         const double r = a.res[c];
         const double prod = (a.h_s / (r * a.cap[p])) * (a.h_s / (r * a.cap[c]));
-        const cplx dc = ld(&down[c]);
-        st(&down[p], ld(&down[p]) - scale(prod, inv(dc)));
+        const cplx dc = ld(D(c));
+        st(D(p), ld(D(p)) - scale(prod, inv(dc)));
     }
     // Root-to-leaves: T_p (total pivot) is known before p's children.
     for (int64_t c = b; c < e; ++c) {
         const int64_t p = a.parent[c];
         if (p < 0) {
-            st(&invT[c], inv(ld(&down[c])));
-            st(&up[c], cplx(0.0, 0.0));
+            st(IT(c), inv(ld(D(c))));
+            st(U(c), cplx(0.0, 0.0));
             continue;
         }
         const double r = a.res[c];
         const double prod = (a.h_s / (r * a.cap[p])) * (a.h_s / (r * a.cap[c]));
-        const cplx dc = ld(&down[c]);
-        const cplx Tp = inv(ld(&invT[p]));
+        const cplx dc = ld(D(c));
+        const cplx Tp = inv(ld(IT(p)));
         const cplx upc = Tp + scale(prod, inv(dc));
         const cplx Tc = dc - scale(prod, inv(upc));
-        st(&up[c], upc);
-        st(&invT[c], inv(Tc));
+        st(U(c), upc);
+        st(IT(c), inv(Tc));
     }
     // Store the step ratios in place of the pivots:
     //   down[c] <- a_pc / down[c]  (parent -> child),  up[c] <- a_cp / up[c]  (child -> parent).
@@ -129,8 +131,8 @@ __global__ void edge_pivots_kernel(const BuildArgs a) {
         const int64_t p = a.parent[c];
         if (p < 0) continue;
         const double r = a.res[c];
-        st(&down[c], scale(a.h_s / (r * a.cap[p]), inv(ld(&down[c]))));
-        st(&up[c], scale(a.h_s / (r * a.cap[c]), inv(ld(&up[c]))));
+        st(D(c), scale(a.h_s / (r * a.cap[p]), inv(ld(D(c)))));
+        st(U(c), scale(a.h_s / (r * a.cap[c]), inv(ld(U(c)))));
     }
 }
 
@@ -143,14 +145,13 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
     if (row >= a.n_seg) return;
     const bool act = lane < kPoles;
     const int k = act ? lane : 0;
-    const int64_t ns = a.n_seg;
     const cplx w = act ? cplx(c_w[k].x, c_w[k].y) : cplx(0.0, 0.0);
     const double scale_out = 2.0 / kNodes;
     int32_t st_node[kStackDepth], st_from[kStackDepth];
     cplx st_y[kStackDepth];
     int sp = 0;
     int64_t cur = row, from = -1;
-    cplx y = ld(&a.invT[k * ns + row]);
+    cplx y = ld(&a.invT[row * kPoles + k]);
     int64_t kept = 0;
     int64_t out = fill ? a.rowptr[row] : 0;
     const int64_t out_end = fill ? a.rowptr[row + 1] : 0;
@@ -171,12 +172,12 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
             const int64_t p = a.parent[cur];
             if (p >= 0 && p != from) {
                 next = p;
-                ynext = ld(&a.up[k * ns + cur]) * y;
+                ynext = ld(&a.up[cur * kPoles + k]) * y;
             }
             for (int64_t q = a.child_ptr[cur]; q < a.child_ptr[cur + 1]; ++q) {
                 const int64_t c = a.child_idx[q];
                 if (c == from) continue;
-                const cplx yc = ld(&a.down[k * ns + c]) * y;
+                const cplx yc = ld(&a.down[c * kPoles + k]) * y;
                 if (next < 0) { next = c; ynext = yc; continue; }
                 if (sp >= kStackDepth) {
                     if (lane == 0) atomicOr(a.status, kStatusStackOverflow);
