@@ -291,7 +291,9 @@ def main():
     ap.add_argument("--size-range", default="500,20000", help="neuron size range (segments)")
     ap.add_argument("--acc-neurons", type=int, default=16)
     ap.add_argument("--acc-steps", type=int, default=2000)
-    ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch")
+    ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
+    ap.add_argument("--autotune", type=int, default=10,
+                    help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
@@ -341,9 +343,16 @@ def main():
     ctx = model._ctx
     ctx.call("nw_set_tuning", args.lanes, args.threads, 0)
     ctx.call("nw_set_option", b"bulk_pipeline", args.bulk)
+    ctx.set_option("fusion_depth", max(1, min(args.fusion, args.steps)))
     ctx.call("nw_synchronize")
     build_s = time.perf_counter() - t_build
     log(f"device model + propagator in {build_s:.1f} s")
+    tuned = None
+    if args.autotune > 0:
+        t0 = time.perf_counter()
+        tuned = ctx.autotune(args.autotune)
+        tuned["seconds"] = time.perf_counter() - t0
+        log(f"autotune: {tuned}")
     rows, nnz, stored, pbytes = (ctypes.c_int64() for _ in range(4))
     ctx.call("nw_propagator_stats", ctypes.byref(rows), ctypes.byref(nnz), ctypes.byref(stored), ctypes.byref(pbytes))
     n = model._n
@@ -357,7 +366,7 @@ def main():
     ctx.call("nw_get_stream", ctypes.byref(sptr))
     stream = torch.cuda.ExternalStream(sptr.value, device=torch.device("cuda", local))
 
-    F = max(1, min(args.fusion, args.steps))
+    F = ctx.get_option("fusion_depth") or args.steps
     # Warm-up.
     w = args.warmup
     while w > 0:
@@ -366,9 +375,13 @@ def main():
         w -= k
     ctx.call("nw_synchronize")
 
-    # Timed device-resident region: K steps as launches of F fused steps.
-    launches = []
+    # Timed device-resident region: the K steps are one nw_advance call, which
+    # replays one CUDA graph of ceil(K / F) launches of F fused steps.  The graph
+    # is captured (not run) beforehand.
     K = args.steps
+    ctx.set_option("prepare_graph", K)
+    n_launch = -(-K // F)
+    replays0 = ctx.get_option("graph_replays")
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -378,17 +391,10 @@ def main():
             ev0 = torch.cuda.Event(enable_timing=True)
             ev1 = torch.cuda.Event(enable_timing=True)
             ev0.record(stream)
-            done = 0
-            while done < K:
-                k = min(F, K - done)
-                e_a = torch.cuda.Event(enable_timing=True); e_b = torch.cuda.Event(enable_timing=True)
-                e_a.record(stream)
-                ctx.advance(k, _lib.PATH_BATCHED)
-                e_b.record(stream)
-                launches.append((e_a, e_b, k))
-                done += k
+            ctx.advance(K, _lib.PATH_BATCHED)
             ev1.record(stream)
         ev1.synchronize()
+    graph_replayed = ctx.get_option("graph_replays") - replays0 == 1
     model.input_hook.ticks += 2 * K
     model.advance_hook.ticks += K
     torch.cuda.synchronize()
@@ -400,8 +406,9 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = n * world * K / (ms * 1e-3)
-    launch_ms = [a.elapsed_time(b) / k for (a, b, k) in launches]   # per fused step
-    per_step_launch_ms = float(np.mean(launch_ms))
+    # Average launch of the batched kernel, per fused step (the region holds the
+    # n_launch kernels plus one clock write and n_launch 4-byte memsets).
+    per_step_launch_ms = ms / K
 
     # End to end through the C ABI with host buffers: per step, the clamp currents
     # go host->device and every segment voltage comes back device->host.
@@ -451,6 +458,7 @@ def main():
                    "propagator_pruning": "charge-conserving (pruned mass returned to the diagonal)",
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
                    "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
+                   "autotune": tuned, "cuda_graph": {"replayed": graph_replayed, "launches_in_graph": n_launch},
                    "propagator_stream": "cp.async.bulk ring (4 x 256 entries per warp)" if bulk_active.value
                    else "register loads",
                    "threads": thr.value, "l2": "inputs larger than L2 (propagator "
@@ -471,7 +479,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "segment-steps/s", "steps": E,
                 "h2d_bytes_per_step": int(stim.numel() * 8), "d2h_bytes_per_step": int(vout.numel() * 4),
                 "api": "nw_advance_host (C ABI), one step per call", "finite": finite},
-        "gpu_launches": len(launches),
+        "gpu_launches": n_launch + 1,
         "cpu_baseline": cpu,
         "spikes_total": int(spikes.sum()),
         "setup_s": time.perf_counter() - t_setup,

@@ -163,7 +163,9 @@ int nw_probes_read(nw_ctx* ctx, void* host, int dtype, int64_t max_rows, int64_t
 
 /* Replaces RxD_Model.advance (neuwon/rxd/rxd_model.py:63-80) called k_steps times:
  * species(dt/2) -> mechanisms(dt) -> species(dt/2) -> AP detector, per step.
- * path selects NW_PATH_BATCHED (fused persistent kernel) or NW_PATH_PLAIN. */
+ * path selects NW_PATH_BATCHED (fused persistent kernel) or NW_PATH_PLAIN.  The
+ * batched path runs the k_steps as launches of "fusion_depth" fused steps, captured
+ * once per distinct call shape in a CUDA graph and replayed (option "cuda_graph"). */
 int nw_advance(nw_ctx* ctx, int32_t k_steps, int path);
 
 /* End-to-end step with host buffers: copies stim_amps (one value per clamp, A, or
@@ -179,6 +181,16 @@ int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks);
  * threads per CTA (128..1024, default 1024), CTAs per SM (0 = occupancy maximum). */
 int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm);
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm);
+
+/* Autotuner of the batched path (replaces the fixed 32-threads-per-block launch of
+ * the reference's GPU kernels, neuwon/database/compute.py:360-418): times short runs
+ * of this model over lanes per row {4, 8, 16, 32} x threads {512, 768, 1024} (plus the
+ * bulk-copy pipeline for FP32), then the fusion depth over {1, 2, 5, ..., 500} steps
+ * up to 4 x trial_steps, and keeps the fastest (ties within 1 % go to deeper fusion).
+ * The model's state, clock and probes are restored afterwards.  Outputs may be NULL;
+ * lanes_per_row 0 means the bulk pipeline was chosen. */
+int nw_autotune(nw_ctx* ctx, int32_t trial_steps, int32_t* lanes_per_row, int32_t* threads,
+                int32_t* fusion_depth, double* ms_per_step);
 
 /* ---- differentiation ----------------------------------------------- */
 
@@ -200,6 +212,11 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
 
 /* Named options.  "reset_clock" (any value): back to time 0 (clock, detector state,
  * probes; conductances count as not yet computed) without touching V or gates.
+ * "fusion_depth" (default 50, 0 = the whole call in one launch): steps per launch of
+ * the batched kernel.  "cuda_graph" (default 1): replay batched launch sequences as
+ * CUDA graphs; "prepare_graph" (k) captures, without running, the graph that a later
+ * nw_advance(k) replays; "clear_graphs" drops the cached graphs; nw_get_option also reports
+ * "graphs_cached", "graph_captures" and "graph_replays". 
  * "bulk_pipeline" (default 0): stream the propagator of the FP32
  * batched path through shared memory with cp.async.bulk copies (needs lanes_per_row
  * 0 in nw_set_tuning); nw_get_option("bulk_pipeline_active") tells whether the next

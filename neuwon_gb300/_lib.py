@@ -25,7 +25,7 @@ EXPORTS = [
     "nw_detectors_set", "nw_probes_set", "nw_probes_read", "nw_advance", "nw_advance_host",
     "nw_get_clock", "nw_set_tuning", "nw_get_tuning", "nw_propagator_stats", "nw_propagator_conserve",
     "nw_kinetic_register", "nw_set_option", "nw_get_option", "nw_electric_half_step_noalloc",
-    "nw_adjoint_forward", "nw_adjoint_backward",
+    "nw_adjoint_forward", "nw_adjoint_backward", "nw_autotune",
 ]
 
 _lib = None
@@ -80,6 +80,8 @@ def load(build_if_missing=True):
         "nw_adjoint_forward": ([c_void_p, c_i64, ctypes.c_int32, c_void_p, P(c_double)], c_int),
         "nw_adjoint_backward": ([c_void_p, c_double, c_void_p, c_void_p, c_void_p, P(c_double)], c_int),
         "nw_get_tuning": ([c_void_p, P(c_int), P(c_int), P(c_int)], c_int),
+        "nw_autotune": ([c_void_p, ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32),
+                         P(c_double)], c_int),
         "nw_propagator_stats": ([c_void_p, P(c_i64), P(c_i64), P(c_i64), P(c_i64)], c_int),
     }
     for name, (args, res) in sig.items():
@@ -153,6 +155,24 @@ class Context:
         s, t = ctypes.c_int64(), ctypes.c_int64()
         self.call("nw_get_clock", ctypes.byref(s), ctypes.byref(t))
         return s.value, t.value
+
+    def set_option(self, name, value):
+        self.call("nw_set_option", name.encode(), int(value))
+
+    def get_option(self, name):
+        v = ctypes.c_int64()
+        self.call("nw_get_option", name.encode(), ctypes.byref(v))
+        return v.value
+
+    def autotune(self, trial_steps=10):
+        """Times the batched path's launch shapes on this model and keeps the fastest;
+        returns dict(lanes_per_row, threads, fusion_depth, ms_per_step)."""
+        l, t, f = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        ms = ctypes.c_double()
+        self.call("nw_autotune", int(trial_steps), ctypes.byref(l), ctypes.byref(t), ctypes.byref(f),
+                  ctypes.byref(ms))
+        return {"lanes_per_row": l.value, "threads": t.value, "fusion_depth": f.value,
+                "ms_per_step": ms.value}
 
     def propagator_csr(self):
         nnz = ctypes.c_int64()

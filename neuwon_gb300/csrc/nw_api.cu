@@ -227,7 +227,8 @@ int nw_ctx_create(int device, int precision, nw_ctx** out) {
     ctx->num_sms = sms;
     ctx->smem_optin = (size_t)optin;
     if (dev_alloc(ctx, ctx->work_counter, 64) != NW_OK ||
-        dev_alloc(ctx, ctx->status, 64) != NW_OK) { delete ctx; return NW_ERR_NOMEM; }
+        dev_alloc(ctx, ctx->status, 64) != NW_OK ||
+        dev_alloc(ctx, ctx->dclock, 64) != NW_OK) { delete ctx; return NW_ERR_NOMEM; }
     cudaMemsetAsync(ctx->status.ptr, 0, 64, ctx->stream);
     *out = ctx;
     return NW_OK;
@@ -237,6 +238,7 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     if (!ctx) return NW_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    graphs_clear(ctx);
     free_hh(ctx->hh);
     free_kin(ctx->kin);
     free_adj(ctx->adj);
@@ -247,7 +249,7 @@ int nw_ctx_destroy(nw_ctx* ctx) {
                       &ctx->clamp_neuron_ptr, &ctx->clamp_amp_stage, &ctx->det_seg, &ctx->det_thr,
                       &ctx->ap_detected, &ctx->ap_state, &ctx->spike_count, &ctx->probe_seg,
                       &ctx->probe_neuron_ptr, &ctx->probe_slot, &ctx->trace, &ctx->neuron_order,
-                      &ctx->work_counter, &ctx->status, &ctx->plain_x};
+                      &ctx->work_counter, &ctx->status, &ctx->plain_x, &ctx->dclock};
     for (DevBuf* b : bufs) dev_free(*b);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -313,6 +315,9 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     ctx->have_detectors = false;
     ctx->n_clamps = 0;
     ctx->n_probes = 0;
+    ctx->probe_len = 0;
+    cudaStreamSynchronize(ctx->stream);
+    graphs_clear(ctx);
     free_hh(ctx->hh);
     free_kin(ctx->kin);
     free_adj(ctx->adj);
@@ -884,6 +889,24 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     if (!ctx || !name) return NW_ERR_ARG;
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
+    if (nm == "cuda_graph") { ctx->use_graph = value != 0; return NW_OK; }
+    if (nm == "fusion_depth") {
+        if (value < 0 || value > (1 << 20)) return fail(ctx, NW_ERR_ARG, "fusion_depth must be in [0, 2^20]");
+        ctx->fusion = (int)value;
+        return NW_OK;
+    }
+    if (nm == "prepare_graph") {
+        // Capture (without running) the graph a later nw_advance(value) will replay.
+        if (value < 1 || value > INT32_MAX) return fail(ctx, NW_ERR_ARG, "prepare_graph: step count out of range");
+        NW_CHECK(check_ready(ctx, (int32_t)value));
+        if (!ctx->use_graph) return NW_OK;
+        return prepare_graph(ctx, (int)value);
+    }
+    if (nm == "clear_graphs") {
+        NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        graphs_clear(ctx);
+        return NW_OK;
+    }
     if (nm == "reset_clock") {
         // Back to time 0: clock, conductance validity, detector state and probes.
         ctx->input_ticks = ctx->steps = 0;
@@ -905,6 +928,11 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     std::string nm(name);
     if (nm == "bulk_pipeline") { *value = ctx->use_bulk ? 1 : 0; return NW_OK; }
     if (nm == "bulk_pipeline_active") { *value = uses_bulk_pipeline(ctx) ? 1 : 0; return NW_OK; }
+    if (nm == "cuda_graph") { *value = ctx->use_graph ? 1 : 0; return NW_OK; }
+    if (nm == "fusion_depth") { *value = ctx->fusion; return NW_OK; }
+    if (nm == "graphs_cached") { *value = (int64_t)ctx->graphs.size(); return NW_OK; }
+    if (nm == "graph_captures") { *value = ctx->graph_captures; return NW_OK; }
+    if (nm == "graph_replays") { *value = ctx->graph_replays; return NW_OK; }
     return fail(ctx, NW_ERR_ARG, "nw_get_option: unknown option " + nm);
 }
 
@@ -920,6 +948,14 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     return adjoint_backward(ctx, cytoplasmic_resistance, grad_gna, grad_gk, grad_gl, grad_ra);
+}
+
+int nw_autotune(nw_ctx* ctx, int32_t trial_steps, int32_t* lanes_per_row, int32_t* threads,
+                int32_t* fusion_depth, double* ms_per_step) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    NW_CHECK(check_ready(ctx, 0));
+    return autotune(ctx, trial_steps, lanes_per_row, threads, fusion_depth, ms_per_step);
 }
 
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm) {

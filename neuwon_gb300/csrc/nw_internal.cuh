@@ -26,6 +26,25 @@ constexpr int kMaxProbesPerNeuron = 64;
 constexpr int kStatusNonFinite = 1;
 constexpr int kStatusWaitTimeout = 16;   // a bounded wait on an mbarrier gave up
 
+// Simulation clock as the step kernels see it.  The host keeps the
+// authoritative copy and writes this one (by value, in stream order) before
+// every batched launch sequence, so a captured CUDA graph replays unchanged.
+struct DevClock {
+    int64_t input_ticks;        // half-step input clock before the sequence
+    int64_t probe_len;          // probe rows already recorded
+    int32_t g_valid;            // mechanism conductances valid at the first half step
+    int32_t pad;
+};
+
+// One instantiated CUDA graph of a batched launch sequence, keyed by every
+// byte that enters its launches (arguments, launch shape, step count, fusion).
+struct GraphEntry {
+    std::vector<unsigned char> key;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t last_use = 0;
+};
+
 struct HHState {
     int64_t m = 0;              // instances
     bool identity = false;      // instance i sits on segment i for every i
@@ -122,7 +141,13 @@ struct nw_ctx {
     nw::DevBuf status;          // i32 [1]
     nw::DevBuf plain_x;         // real [n_seg] scratch of the plain path
     int lanes_per_row = 0, threads = 1024, ctas_per_sm = 0;
+    int fusion = 50;            // steps fused per launch (0: one launch per call)
     bool use_bulk = false;      // asynchronous bulk-copy pipeline (FP32 batched path)
+    bool use_graph = true;      // replay batched launch sequences as CUDA graphs
+    nw::DevBuf dclock;          // nw::DevClock
+    std::vector<nw::GraphEntry> graphs;
+    uint64_t graph_uses = 0;
+    int64_t graph_captures = 0, graph_replays = 0;
 
     // Clock.
     int64_t input_ticks = 0, steps = 0;
@@ -148,6 +173,10 @@ int advance_batched(nw_ctx* ctx, int k_steps);
 int advance_plain(nw_ctx* ctx, int k_steps);
 int choose_lanes_per_row(nw_ctx* ctx);
 bool uses_bulk_pipeline(nw_ctx* ctx);
+void graphs_clear(nw_ctx* ctx);
+int prepare_graph(nw_ctx* ctx, int k_steps);
+int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes, int32_t* threads, int32_t* fusion,
+             double* ms_per_step);
 
 // Adjoint (nw_adjoint.cu).
 int adjoint_forward(nw_ctx* ctx, int64_t T, int K, const double* target, double* loss_out);

@@ -221,9 +221,13 @@ __device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, i
 
 template <typename real, int LPR, bool BULK>
 __global__ void __launch_bounds__(1024)
-batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
+batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_off) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     real* xs = reinterpret_cast<real*>(smem_raw);
+    // Steps s_off .. s_off + k_steps - 1 of the sequence that starts at the clock.
+    const int64_t tick_base = a.clk->input_ticks + 2 * (int64_t)s_off;
+    const int64_t row_base = a.clk->probe_len + s_off;
+    const bool g_valid0 = s_off > 0 || a.clk->g_valid != 0;
     __shared__ int s_job;
     __shared__ int s_abort;
     BulkRing ring;
@@ -297,8 +301,8 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
         for (int s = 0; s < a.k_steps; ++s) {
 #pragma unroll 1
             for (int half = 0; half < 2; ++half) {
-                const int64_t tick = a.tick0 + 2 * s + half + 1;
-                const bool gv = (s > 0) || (half > 0) || a.g_valid;
+                const int64_t tick = tick_base + 2 * s + half + 1;
+                const bool gv = (s > 0) || (half > 0) || g_valid0;
                 const bool last = (s == a.k_steps - 1) && (half == 1);
                 // The propagator does not depend on x: start streaming it now.
                 if (BULK) bulk_prologue(a, ring, slice);
@@ -343,7 +347,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes) {
                 spikes += ap_det ? 1u : 0u;
             }
             for (int p = pb + tid; p < pe; p += nthr)
-                a.trace[(a.trace_row0 + s) * a.n_probes + a.probe_slot[p]] = a.V[a.probe_seg[p]];
+                a.trace[(row_base + s) * a.n_probes + a.probe_slot[p]] = a.V[a.probe_seg[p]];
         }
         if (tid == 0 && a.has_det) {
             a.ap_state[j] = ap_state;
@@ -428,8 +432,18 @@ int choose_lanes_per_row(nw_ctx* ctx) {
     return 4;
 }
 
+// Launch shape of the batched kernel for the context's current tuning.
+template <typename real>
+struct BatchedCfg {
+    void (*kern)(const StepArgs<real>, int, int);
+    unsigned grid;
+    int threads;
+    size_t smem;
+    int xs_bytes;
+};
+
 template <typename real, int LPR, bool BULK>
-static int launch_batched_cfg(nw_ctx* ctx, const StepArgs<real>& a) {
+static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
     auto kern = batched_advance_kernel<real, LPR, BULK>;
     const size_t xs_bytes = ((size_t)ctx->max_neuron * sizeof(real) + 127) & ~(size_t)127;
     const int threads = ctx->threads;
@@ -444,10 +458,11 @@ static int launch_batched_cfg(nw_ctx* ctx, const StepArgs<real>& a) {
     NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem));
     if (occ < 1) return fail(ctx, NW_ERR_LIMIT, "batched path: kernel does not fit on an SM");
     int per_sm = ctx->ctas_per_sm ? std::min(ctx->ctas_per_sm, occ) : occ;
-    int64_t grid = std::min<int64_t>(ctx->n_neuron, (int64_t)per_sm * ctx->num_sms);
-    NW_CUDA(ctx, cudaMemsetAsync(ctx->work_counter.ptr, 0, sizeof(int), ctx->stream));
-    kern<<<(unsigned)grid, threads, smem, ctx->stream>>>(a, (int)xs_bytes);
-    NW_CUDA(ctx, cudaGetLastError());
+    c.kern = kern;
+    c.grid = (unsigned)std::min<int64_t>(ctx->n_neuron, (int64_t)per_sm * ctx->num_sms);
+    c.threads = threads;
+    c.smem = smem;
+    c.xs_bytes = (int)xs_bytes;
     return NW_OK;
 }
 
@@ -464,17 +479,138 @@ bool uses_bulk_pipeline(nw_ctx* ctx) {
 }
 
 template <typename real>
-static int launch_batched(nw_ctx* ctx, int k_steps) {
-    StepArgs<real> a = make_args<real>(ctx, k_steps);
+static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
     if constexpr (std::is_same<real, float>::value) {
-        if (uses_bulk_pipeline(ctx)) return launch_batched_cfg<float, 32, true>(ctx, a);
+        if (uses_bulk_pipeline(ctx)) return config_batched_lpr<float, 32, true>(ctx, c);
     }
     switch (choose_lanes_per_row(ctx)) {
-        case 4: return launch_batched_cfg<real, 4, false>(ctx, a);
-        case 8: return launch_batched_cfg<real, 8, false>(ctx, a);
-        case 16: return launch_batched_cfg<real, 16, false>(ctx, a);
-        default: return launch_batched_cfg<real, 32, false>(ctx, a);
+        case 4: return config_batched_lpr<real, 4, false>(ctx, c);
+        case 8: return config_batched_lpr<real, 8, false>(ctx, c);
+        case 16: return config_batched_lpr<real, 16, false>(ctx, c);
+        default: return config_batched_lpr<real, 32, false>(ctx, c);
     }
+}
+
+// k_steps steps as launches of ctx->fusion fused steps each, on the context's
+// stream (also the body of a captured graph: no host synchronisation here).
+template <typename real>
+static int enqueue_batched(nw_ctx* ctx, const BatchedCfg<real>& c, const StepArgs<real>& a0, int k_steps) {
+    const int F = ctx->fusion > 0 ? ctx->fusion : k_steps;
+    for (int s_off = 0; s_off < k_steps; s_off += F) {
+        StepArgs<real> a = a0;
+        a.k_steps = std::min(F, k_steps - s_off);
+        NW_CUDA(ctx, cudaMemsetAsync(ctx->work_counter.ptr, 0, sizeof(int), ctx->stream));
+        c.kern<<<c.grid, c.threads, c.smem, ctx->stream>>>(a, c.xs_bytes, s_off);
+        NW_CUDA(ctx, cudaGetLastError());
+    }
+    return NW_OK;
+}
+
+__global__ void set_clock_kernel(DevClock* d, DevClock v) { *d = v; }
+
+static int push_clock(nw_ctx* ctx) {
+    DevClock v;
+    memset(&v, 0, sizeof(v));
+    v.input_ticks = ctx->input_ticks;
+    v.probe_len = ctx->probe_len;
+    v.g_valid = ctx->g_valid ? 1 : 0;
+    set_clock_kernel<<<1, 1, 0, ctx->stream>>>(ctx->dclock.as<DevClock>(), v);
+    NW_CUDA(ctx, cudaGetLastError());
+    return NW_OK;
+}
+
+void graphs_clear(nw_ctx* ctx) {
+    for (auto& g : ctx->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+    }
+    ctx->graphs.clear();
+}
+
+static void key_append(std::vector<unsigned char>& key, const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    key.insert(key.end(), b, b + n);
+}
+
+constexpr size_t kMaxGraphs = 8;
+
+// Replays (capturing first if needed) the graph of k_steps batched steps.
+// The key holds every byte that enters the captured launches, so an entry is
+// reused exactly when the launches it recorded are the ones asked for.
+template <typename real>
+static int launch_graph(nw_ctx* ctx, const BatchedCfg<real>& c, const StepArgs<real>& a0, int k_steps,
+                        bool launch = true) {
+    std::vector<unsigned char> key;
+    StepArgs<real> ka = a0;
+    ka.tick0 = 0; ka.g_valid = 0; ka.trace_row0 = 0; ka.k_steps = 0;   // not read by the kernel
+    key_append(key, &ka, sizeof(ka));
+    key_append(key, &c, sizeof(c));
+    key_append(key, &k_steps, sizeof(k_steps));
+    key_append(key, &ctx->fusion, sizeof(ctx->fusion));
+    key_append(key, &ctx->work_counter.ptr, sizeof(void*));
+    for (auto& g : ctx->graphs) {
+        if (g.key == key) {
+            g.last_use = ++ctx->graph_uses;
+            if (!launch) return NW_OK;
+            NW_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+            ctx->graph_replays++;
+            return NW_OK;
+        }
+    }
+    if (ctx->graphs.size() >= kMaxGraphs) {
+        size_t lru = 0;
+        for (size_t i = 1; i < ctx->graphs.size(); ++i)
+            if (ctx->graphs[i].last_use < ctx->graphs[lru].last_use) lru = i;
+        cudaGraphExecDestroy(ctx->graphs[lru].exec);
+        cudaGraphDestroy(ctx->graphs[lru].graph);
+        ctx->graphs.erase(ctx->graphs.begin() + lru);
+    }
+    GraphEntry e;
+    e.key = std::move(key);
+    NW_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_batched(ctx, c, a0, k_steps);
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &e.graph);
+    if (rc != NW_OK) {
+        if (e.graph) cudaGraphDestroy(e.graph);
+        return rc;
+    }
+    NW_CUDA(ctx, ce);
+    const cudaError_t ie = cudaGraphInstantiate(&e.exec, e.graph, 0);
+    if (ie != cudaSuccess) {
+        cudaGraphDestroy(e.graph);
+        return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+    }
+    e.last_use = ++ctx->graph_uses;
+    ctx->graph_captures++;
+    ctx->graphs.push_back(std::move(e));
+    if (!launch) return NW_OK;
+    NW_CUDA(ctx, cudaGraphLaunch(ctx->graphs.back().exec, ctx->stream));
+    ctx->graph_replays++;
+    return NW_OK;
+}
+
+template <typename real>
+static int launch_batched(nw_ctx* ctx, int k_steps) {
+    BatchedCfg<real> c;
+    memset(&c, 0, sizeof(c));
+    NW_CHECK(config_batched<real>(ctx, c));
+    const StepArgs<real> a = make_args<real>(ctx, k_steps);
+    NW_CHECK(push_clock(ctx));
+    if (ctx->use_graph) return launch_graph<real>(ctx, c, a, k_steps);
+    return enqueue_batched<real>(ctx, c, a, k_steps);
+}
+
+template <typename real>
+static int prepare_graph_t(nw_ctx* ctx, int k_steps) {
+    BatchedCfg<real> c;
+    memset(&c, 0, sizeof(c));
+    NW_CHECK(config_batched<real>(ctx, c));
+    const StepArgs<real> a = make_args<real>(ctx, k_steps);
+    return launch_graph<real>(ctx, c, a, k_steps, false);
+}
+
+int prepare_graph(nw_ctx* ctx, int k_steps) {
+    return ctx->precision == NW_F64 ? prepare_graph_t<double>(ctx, k_steps) : prepare_graph_t<float>(ctx, k_steps);
 }
 
 static void finish_steps(nw_ctx* ctx, int k_steps) {

@@ -2,6 +2,7 @@
 // (nw_step.cu) and the adjoint kernels (nw_adjoint.cu).
 #pragma once
 
+#include <cstring>
 #include <type_traits>
 
 #include "nw_internal.cuh"
@@ -108,7 +109,9 @@ struct StepArgs {
     // probes
     const int32_t* probe_neuron_ptr; const uint32_t* probe_seg; const uint32_t* probe_slot;
     real* trace; int64_t n_probes; int64_t trace_row0;
-    // time
+    // time: the batched kernel reads the clock from clk (device), the
+    // plain and adjoint kernels from tick0 / g_valid / trace_row0
+    const DevClock* clk;
     int64_t tick0; int k_steps; int g_valid; real h_s;
 };
 
@@ -345,7 +348,8 @@ __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_
 
 template <typename real>
 inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
-    StepArgs<real> a{};
+    StepArgs<real> a;
+    memset(&a, 0, sizeof(a));      // padding bytes too: the struct is a graph-cache key
     a.n_neuron = ctx->n_neuron;
     a.neuron_start = ctx->neuron_start.as<int64_t>();
     a.neuron_order = ctx->neuron_order.as<int32_t>();
@@ -393,6 +397,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
         a.probe_seg = ctx->probe_seg.as<uint32_t>(); a.probe_slot = ctx->probe_slot.as<uint32_t>();
         a.trace = ctx->trace.as<real>(); a.trace_row0 = ctx->probe_len;
     }
+    a.clk = ctx->dclock.as<DevClock>();
     a.tick0 = ctx->input_ticks;
     a.k_steps = k_steps;
     a.g_valid = ctx->g_valid ? 1 : 0;

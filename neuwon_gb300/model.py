@@ -374,6 +374,12 @@ class RxD_Model:
         self.input_hook.ticks += 2 * k
         self.advance_hook._tick(k)
 
+    def autotune(self, trial_steps=10):
+        """Choose the batched path's lanes per row, threads per CTA and step-fusion
+        depth by timing short runs of this model (state restored afterwards)."""
+        self._sync()
+        return self._ctx.autotune(trial_steps)
+
     # --------------------------------------------------- differentiation helpers
     def set_hh_densities(self, gnabar, gkbar, glbar):
         """Per-instance HH densities (S/cm2, registration order) without a rebuild."""

@@ -314,6 +314,17 @@ def main():
                 probes=[0, 10, 40, 45, 65, 95, 124], snapshots={150},
                 duplicate_segments=[(0, 3), (2, 30)])
 
+    # (4) The single-neuron configuration at full size: 2,000 segments (seed 0),
+    #     HH everywhere, 0.2 nA soma clamp 5-80 ms, dt 0.1 ms for 100 ms, the
+    #     reference's own epsilon-pruned propagator.  All segment voltages every
+    #     100 steps.
+    t2000 = random_tree(2000, seed=0)
+    run_hh_tree(out, "c1", [t2000], time_step=0.1, celsius=6.3, t_stop=100.0,
+                clamps=[(0, 0, 0.2, 5.0, 75.0)],
+                hh_kwargs=dict(ena=50.0, ek=-77.0, el=-54.3),
+                probes=[0, 1, 500, 1000, 1500, 1999],
+                snapshots={100 * i for i in range(1, 11)})
+
     run_lti(out)
 
     path = os.path.join(HERE, "reference_fixtures.npz")

@@ -146,6 +146,38 @@ def test_f32_batched_single_neuron_config_short():
     assert worst < 0.1, worst
 
 
+@pytest.mark.parametrize("precision,tol,conserve,bound", [
+    ("f64", EPSILON, False, 1e-6),
+    ("f32", EPSILON, False, 0.1),
+    ("f32", 1e-8, True, 0.1),
+])
+def test_single_neuron_config_matches_reference(precision, tol, conserve, bound):
+    """The single-neuron configuration at full size and length (2,000 segments, HH,
+    0.2 nA soma clamp 5-80 ms, dt 0.1 ms for 100 ms): every segment's voltage every
+    10 ms and the probed traces every step against the reference's own run; equal
+    spike counts."""
+    clamps = [(0, 0, 0.2, 5.0, 75.0)]
+    probes = list(F["c1_probes"])
+    m, neurons, offs, recs = gpu_model([random_tree(2000, seed=0)], clamps,
+                                       hh_kw=dict(ena=50.0, ek=-77.0, el=-54.3), precision=precision,
+                                       tolerance=tol, conserve=conserve, probes=probes)
+    worst = 0.0
+    for k in range(1000):
+        for (ti, s, nA, start, dur) in clamps:
+            if m.clock.is_now(start):
+                nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance()
+        if (k + 1) % 100 == 0:
+            worst = max(worst, np.abs(m.get_data("Segment.voltage") - F[f"c1_snap{k + 1}"]).max())
+    got = np.array([r.get_data() for r in recs]).T
+    ref = F["c1_trace"]
+    assert got.shape == ref.shape
+    assert worst < bound, worst
+    assert np.abs(got - ref).max() < bound
+    assert int(m.get_data("Neuron.spike_count")[0]) == int(F["c1_ap"].sum())
+    m.close()
+
+
 @pytest.mark.parametrize("lanes", [4, 8, 16, 32])
 def test_lanes_per_row_variants_agree(lanes):
     tree = random_tree(500, seed=2)

@@ -87,6 +87,26 @@ def test_oracle_traces_match_reference(prefix, trees, clamps, hh_kw, dups, as_cr
     np.testing.assert_array_equal(om.AP_detected, F[prefix + "_ap"][-1])
 
 
+def test_oracle_single_neuron_config_matches_reference():
+    """The single-neuron configuration at full size: 2,000 segments, HH, 0.2 nA soma
+    clamp 5-80 ms, dt 0.1 ms for 100 ms; every segment's voltage every 10 ms against
+    the reference's own run (epsilon-pruned propagator on both sides)."""
+    clamps = [(0, 0, 0.2, 5.0, 75.0)]
+    om, _ = oracle_case([random_tree(2000, seed=0)], clamps, hh_kw=dict(ena=50., ek=-77., el=-54.3),
+                        duplicates="numpy")
+    probes = F["c1_probes"]
+    trace = [om.voltage[probes].copy()]
+    worst = 0.0
+    for k in range(1000):
+        om.advance()
+        trace.append(om.voltage[probes].copy())
+        if (k + 1) % 100 == 0:
+            worst = max(worst, np.abs(om.voltage - F[f"c1_snap{k + 1}"]).max())
+    assert worst < 1e-8, worst
+    assert np.abs(np.array(trace) - F["c1_trace"]).max() < 1e-8
+    assert int(om.spike_count[0]) == int(F["c1_ap"].sum())
+
+
 def test_duplicate_instances_reference_drops_one():
     """species.py:392-393 drops duplicate segment indices; the sum differs."""
     trees = [random_tree(40, seed=21), random_tree(25, seed=22), random_tree(60, seed=23)]
