@@ -23,7 +23,7 @@ def _case(precision="f32", probes=(0, 5, 400)):
 
 
 def _state(m):
-    return (m.get_data("Segment.voltage"), m.get_data("hh.m"), m.get_data("kinetic.state"),
+    return (m.get_data("Segment.voltage"), m.get_data("hh.m"), m.get_data("na8.state"),
             m.get_data("Neuron.spike_count"))
 
 
