@@ -141,6 +141,28 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
                         double erev, const double* table, int num_buckets, int num_terms,
                         double vmin, double bucket_frq, double conserve_sum, const double* init_state);
 
+/* ---- synapses and spike events ------------------------------------ */
+
+/* No counterpart in the reference: its neuwon/rxd/synapses.py grows synapse
+ * geometry only, and no mechanism has a NET_RECEIVE block.  Spikes are the AP
+ * detector's output (neuwon/rxd/neuron/neuron.py:184-188, one detector per neuron,
+ * nw_detectors_set).  A spike of neuron pre_neuron[k] at step t arrives at synapse k
+ * at step t + delay_steps[k] (>= 1), and keeps transmitter present for the
+ * mechanism updates of pulse_steps steps.  Each synapse holds a 2-state AMPA scheme
+ * (C, O) and a 3-state NMDA scheme (C, O, D) advanced exactly per step by the given
+ * transition matrices (row-major, new state from old; *_on with transmitter, *_off
+ * without; 2x2 and 3x3).  Conductance into post_segment[k]:
+ * w_ampa O_ampa + w_nmda O_nmda B(V), B(V) = 1 / (1 + exp(-0.062 V) mg / 3.57) (S, mV,
+ * mM), reversal e_syn (mV).  The batched path fuses at most min(delay) steps per
+ * launch.  Replaces any previous synapse set; states start closed. Readable:
+ * "Synapse.ampa_open", "Synapse.nmda_open", "Synapse.nmda_desensitized" (settable),
+ * "Synapse.events" (deliveries), "Synapse.last_event", "Synapse.pulse_end" (steps). */
+int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron,
+                    const int64_t* post_segment, const double* w_ampa, const double* w_nmda,
+                    const int32_t* delay_steps, const double* ampa_on, const double* ampa_off,
+                    const double* nmda_on, const double* nmda_off, int32_t pulse_steps,
+                    double e_syn, double mg);
+
 /* ---- stimulus, detection, recording --------------------------------- */
 
 /* Current clamps: replaces Segment.inject_current + TimeSeries.play on the

@@ -25,7 +25,7 @@ EXPORTS = [
     "nw_detectors_set", "nw_probes_set", "nw_probes_read", "nw_advance", "nw_advance_host",
     "nw_get_clock", "nw_set_tuning", "nw_get_tuning", "nw_propagator_stats", "nw_propagator_conserve",
     "nw_kinetic_register", "nw_set_option", "nw_get_option", "nw_electric_half_step_noalloc",
-    "nw_adjoint_forward", "nw_adjoint_backward", "nw_autotune",
+    "nw_adjoint_forward", "nw_adjoint_backward", "nw_autotune", "nw_synapses_set",
 ]
 
 _lib = None
@@ -80,6 +80,8 @@ def load(build_if_missing=True):
         "nw_adjoint_forward": ([c_void_p, c_i64, ctypes.c_int32, c_void_p, P(c_double)], c_int),
         "nw_adjoint_backward": ([c_void_p, c_double, c_void_p, c_void_p, c_void_p, P(c_double)], c_int),
         "nw_get_tuning": ([c_void_p, P(c_int), P(c_int), P(c_int)], c_int),
+        "nw_synapses_set": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                             c_void_p, c_void_p, c_void_p, ctypes.c_int32, c_double, c_double], c_int),
         "nw_autotune": ([c_void_p, ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32),
                          P(c_double)], c_int),
         "nw_propagator_stats": ([c_void_p, P(c_i64), P(c_i64), P(c_i64), P(c_i64)], c_int),

@@ -478,6 +478,7 @@ static int adjoint_check(nw_ctx* ctx) {
     if (ctx->hh.m == 0 || !ctx->hh.identity)
         return fail(ctx, NW_ERR_STATE, "adjoint: needs exactly one HH instance on every segment");
     if (ctx->kin.m != 0) return fail(ctx, NW_ERR_STATE, "adjoint: kinetic mechanisms are not differentiated");
+    if (ctx->syn.n != 0) return fail(ctx, NW_ERR_STATE, "adjoint: synapses are not differentiated");
     if (ctx->nonspec_nonzero) return fail(ctx, NW_ERR_STATE, "adjoint: nonspecific currents are not supported");
     return NW_OK;
 }

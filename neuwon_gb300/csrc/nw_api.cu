@@ -178,6 +178,19 @@ static void free_kin(KineticState& k) {
     k = KineticState();
 }
 
+void free_syn(SynState& y) {
+    for (DevBuf* b : {&y.seg, &y.pre, &y.delay, &y.wa, &y.wn, &y.oa, &y.on, &y.od, &y.pulse_end, &y.events,
+                      &y.last_event, &y.mats, &y.seg_ptr, &y.neuron_ptr, &y.ring})
+        dev_free(*b);
+    y = SynState();
+}
+
+int synapse_ring_clear(nw_ctx* ctx) {
+    if (ctx->syn.n == 0) return NW_OK;
+    NW_CUDA(ctx, cudaMemsetAsync(ctx->syn.ring.ptr, 0, ctx->syn.ring.bytes, ctx->stream));
+    return NW_OK;
+}
+
 // HH steady state at v (nmodl_library/artificial/hh.mod:48-53, 62-94).
 static void hh_steady(double v, double* m, double* h, double* n) {
     auto vtrap = [](double x, double y) {
@@ -241,6 +254,7 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     graphs_clear(ctx);
     free_hh(ctx->hh);
     free_kin(ctx->kin);
+    free_syn(ctx->syn);
     free_adj(ctx->adj);
     DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec,
                       &ctx->kI, &ctx->kG, &ctx->cap64, &ctx->res64, &ctx->p_rowptr, &ctx->p_col,
@@ -320,6 +334,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     graphs_clear(ctx);
     free_hh(ctx->hh);
     free_kin(ctx->kin);
+    free_syn(ctx->syn);
     free_adj(ctx->adj);
     size_t rs = (size_t)ctx->precision;
     NW_CHECK(dev_alloc(ctx, ctx->neuron_start, 8 * (num_neurons + 1)));
@@ -418,6 +433,14 @@ int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int6
                 sorted[(size_t)c * K.m + K.user_to_sorted[u]] = read_as_double(host, dtype, u * K.S + c);
         return upload_convert(ctx, K.state.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
     }
+    if (nm == "Synapse.ampa_open" || nm == "Synapse.nmda_open" || nm == "Synapse.nmda_desensitized") {
+        SynState& Y = ctx->syn;
+        NW_CHECK(need(Y.n));
+        std::vector<double> sorted(count);
+        for (int64_t i = 0; i < count; ++i) sorted[Y.user_to_sorted[i]] = read_as_double(host, dtype, i);
+        DevBuf& b = nm == "Synapse.ampa_open" ? Y.oa : nm == "Synapse.nmda_open" ? Y.on : Y.od;
+        return upload_convert(ctx, b.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
+    }
     if (nm == "Neuron.AP_detected") {
         NW_CHECK(need(ctx->n_neuron));
         return upload_convert(ctx, ctx->ap_detected.ptr, NW_DTYPE_U8, host, dtype, count);
@@ -463,6 +486,23 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
         for (int64_t u = 0; u < K.m; ++u)
             for (int c = 0; c < K.S; ++c)
                 write_from_double(host, dtype, u * K.S + c, sorted[(size_t)c * K.m + K.user_to_sorted[u]]);
+        return NW_OK;
+    }
+    if (nm.rfind("Synapse.", 0) == 0) {
+        const SynState& Y = ctx->syn;
+        const DevBuf* b = nullptr;
+        int sd = rd;
+        if (nm == "Synapse.ampa_open") b = &Y.oa;
+        else if (nm == "Synapse.nmda_open") b = &Y.on;
+        else if (nm == "Synapse.nmda_desensitized") b = &Y.od;
+        else if (nm == "Synapse.events") { b = &Y.events; sd = NW_DTYPE_U32; }
+        else if (nm == "Synapse.last_event") { b = &Y.last_event; sd = NW_DTYPE_I32; }
+        else if (nm == "Synapse.pulse_end") { b = &Y.pulse_end; sd = NW_DTYPE_I32; }
+        else return fail(ctx, NW_ERR_ARG, "nw_get_data: unknown attribute " + nm);
+        NW_CHECK(need(Y.n));
+        std::vector<double> sorted(count);
+        NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, b->ptr, sd, count));
+        for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[Y.user_to_sorted[i]]);
         return NW_OK;
     }
     if (nm == "Neuron.AP_detected") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->ap_detected.ptr, NW_DTYPE_U8, count); }
@@ -674,6 +714,80 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
     NW_CHECK(upload_convert(ctx, K.state.ptr, rd, st.data(), NW_DTYPE_F64, (int64_t)S * m));
     NW_CHECK(upload_convert(ctx, K.table.ptr, rd, table, NW_DTYPE_F64, tsize));
     ctx->g_valid = false;
+    return NW_OK;
+}
+
+int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron, const int64_t* post_segment,
+                    const double* w_ampa, const double* w_nmda, const int32_t* delay_steps,
+                    const double* ampa_on, const double* ampa_off, const double* nmda_on, const double* nmda_off,
+                    int32_t pulse_steps, double e_syn, double mg) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_synapses_set before nw_model_init");
+    const int64_t m = num_synapses;
+    if (m < 0 || (m && (!pre_neuron || !post_segment || !w_ampa || !w_nmda || !delay_steps ||
+                        !ampa_on || !ampa_off || !nmda_on || !nmda_off)))
+        return fail(ctx, NW_ERR_ARG, "nw_synapses_set: null arrays");
+    if (m > 0 && (pulse_steps < 1 || !(mg >= 0.0) || !std::isfinite(e_syn)))
+        return fail(ctx, NW_ERR_ARG, "nw_synapses_set: pulse_steps >= 1, mg >= 0, finite e_syn");
+    int dmin = INT32_MAX, dmax = 0;
+    for (int64_t k = 0; k < m; ++k) {
+        if (pre_neuron[k] < 0 || pre_neuron[k] >= ctx->n_neuron)
+            return fail(ctx, NW_ERR_ARG, "nw_synapses_set: presynaptic neuron out of range");
+        if (delay_steps[k] < 1 || delay_steps[k] > (1 << 20))
+            return fail(ctx, NW_ERR_ARG, "nw_synapses_set: delay must be in [1, 2^20] steps");
+        if (!(w_ampa[k] >= 0.0) || !(w_nmda[k] >= 0.0))
+            return fail(ctx, NW_ERR_ARG, "nw_synapses_set: weights must be >= 0");
+        dmin = std::min(dmin, (int)delay_steps[k]);
+        dmax = std::max(dmax, (int)delay_steps[k]);
+    }
+    InstanceLayout L;
+    NW_CHECK(layout_instances(ctx, m, post_segment, "nw_synapses_set", L));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SynState& Y = ctx->syn;
+    free_syn(Y);
+    if (m == 0) return NW_OK;
+    Y.n = m;
+    Y.min_delay = dmin; Y.max_delay = dmax; Y.pulse_steps = pulse_steps;
+    Y.e_syn = e_syn; Y.mg = mg;
+    // A spike of step t is read up to max_delay steps later while its owner may
+    // already have written min_delay (the most steps one launch fuses) newer ones.
+    int R = 32;
+    while (R < dmax + dmin + 1) R *= 2;
+    Y.ring_steps = R;
+    Y.ring_words = R / 32;
+    Y.user_to_sorted = L.user_to_sorted;
+    Y.h_neuron_ptr = L.nptr;
+    NW_CHECK(upload_layout(ctx, L, Y.seg, Y.seg_ptr, Y.neuron_ptr));
+    const size_t rs = (size_t)ctx->precision;
+    std::vector<int32_t> pre(m), dl(m), pe(m, 0), last(m, -1);
+    std::vector<double> wa(m), wn(m), zero(m, 0.0);
+    for (int64_t s = 0; s < m; ++s) {
+        const int64_t u = L.order[s];
+        pre[s] = (int32_t)pre_neuron[u]; dl[s] = delay_steps[u];
+        wa[s] = w_ampa[u]; wn[s] = w_nmda[u];
+    }
+    for (DevBuf* b : {&Y.pre, &Y.delay, &Y.pulse_end, &Y.last_event, &Y.events}) NW_CHECK(dev_alloc(ctx, *b, 4 * m));
+    for (DevBuf* b : {&Y.wa, &Y.wn, &Y.oa, &Y.on, &Y.od}) NW_CHECK(dev_alloc(ctx, *b, rs * m));
+    NW_CHECK(dev_alloc(ctx, Y.mats, rs * 26));
+    NW_CHECK(dev_alloc(ctx, Y.ring, 4 * (size_t)Y.ring_words * ctx->n_neuron));
+    NW_CHECK(upload_convert(ctx, Y.pre.ptr, NW_DTYPE_I32, pre.data(), NW_DTYPE_I32, m));
+    NW_CHECK(upload_convert(ctx, Y.delay.ptr, NW_DTYPE_I32, dl.data(), NW_DTYPE_I32, m));
+    NW_CHECK(upload_convert(ctx, Y.pulse_end.ptr, NW_DTYPE_I32, pe.data(), NW_DTYPE_I32, m));
+    NW_CHECK(upload_convert(ctx, Y.last_event.ptr, NW_DTYPE_I32, last.data(), NW_DTYPE_I32, m));
+    NW_CUDA(ctx, cudaMemsetAsync(Y.events.ptr, 0, 4 * m, ctx->stream));
+    const int rd = real_dtype(ctx);
+    NW_CHECK(upload_convert(ctx, Y.wa.ptr, rd, wa.data(), NW_DTYPE_F64, m));
+    NW_CHECK(upload_convert(ctx, Y.wn.ptr, rd, wn.data(), NW_DTYPE_F64, m));
+    for (DevBuf* b : {&Y.oa, &Y.on, &Y.od}) NW_CHECK(upload_convert(ctx, b->ptr, rd, zero.data(), NW_DTYPE_F64, m));
+    std::vector<double> mats(26);
+    std::copy(ampa_on, ampa_on + 4, mats.begin());
+    std::copy(ampa_off, ampa_off + 4, mats.begin() + 4);
+    std::copy(nmda_on, nmda_on + 9, mats.begin() + 8);
+    std::copy(nmda_off, nmda_off + 9, mats.begin() + 17);
+    NW_CHECK(upload_convert(ctx, Y.mats.ptr, rd, mats.data(), NW_DTYPE_F64, 26));
+    NW_CHECK(synapse_ring_clear(ctx));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return NW_OK;
 }
 
@@ -918,6 +1032,7 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
             NW_CUDA(ctx, cudaMemsetAsync(ctx->spike_count.ptr, 0, 4 * ctx->n_neuron, ctx->stream));
             NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
+        NW_CHECK(synapse_ring_clear(ctx));
         return NW_OK;
     }
     return fail(ctx, NW_ERR_ARG, "nw_set_option: unknown option " + nm);

@@ -31,6 +31,7 @@ constexpr int kStatusWaitTimeout = 16;   // a bounded wait on an mbarrier gave u
 // every batched launch sequence, so a captured CUDA graph replays unchanged.
 struct DevClock {
     int64_t input_ticks;        // half-step input clock before the sequence
+    int64_t steps;              // completed steps before the sequence
     int64_t probe_len;          // probe rows already recorded
     int32_t g_valid;            // mechanism conductances valid at the first half step
     int32_t pad;
@@ -70,6 +71,30 @@ struct KineticState {
     DevBuf table;               // real [nb][S][S][T]
     DevBuf seg_ptr;             // u32 [n_seg+1]
     DevBuf neuron_ptr;          // i64 [n_neuron+1]
+    std::vector<int64_t> user_to_sorted;
+    std::vector<int64_t> h_neuron_ptr;
+};
+
+// Synapses with AMPA (C, O) and NMDA (C, O, D) kinetics, driven by spikes of
+// their presynaptic neuron after an axonal delay of whole steps.  Spikes are
+// kept per neuron in a bit ring of the last ring_steps steps; a synapse pulls
+// its arrival from the ring (step - delay), so delivery order cannot vary.
+struct SynState {
+    int64_t n = 0;
+    int min_delay = 0, max_delay = 0, pulse_steps = 0, ring_steps = 0, ring_words = 0;
+    double e_syn = 0, mg = 1.0;
+    DevBuf seg;                 // u32 [n] post segment, segment-sorted order
+    DevBuf pre;                 // i32 [n] presynaptic neuron
+    DevBuf delay;               // i32 [n] steps, >= 1
+    DevBuf wa, wn;              // real [n] AMPA / NMDA weights (S)
+    DevBuf oa, on, od;          // real [n] AMPA open, NMDA open, NMDA desensitised
+    DevBuf pulse_end;           // i32 [n] first step without transmitter
+    DevBuf events;              // u32 [n] deliveries so far
+    DevBuf last_event;          // i32 [n] step of the last delivery (-1: none)
+    DevBuf mats;                // real [26]: AMPA on, off (2x2), NMDA on, off (3x3), row-major
+    DevBuf seg_ptr;             // u32 [n_seg+1]
+    DevBuf neuron_ptr;          // i64 [n_neuron+1] synapse range of each post neuron
+    DevBuf ring;                // u32 [n_neuron][ring_words] spike bits by step mod ring_steps
     std::vector<int64_t> user_to_sorted;
     std::vector<int64_t> h_neuron_ptr;
 };
@@ -117,6 +142,7 @@ struct nw_ctx {
     // Mechanisms.
     nw::HHState hh;
     nw::KineticState kin;
+    nw::SynState syn;
     nw::AdjointState adj;
     bool g_valid = false;       // conductances computed by a mechanism step
 
@@ -174,6 +200,8 @@ int advance_plain(nw_ctx* ctx, int k_steps);
 int choose_lanes_per_row(nw_ctx* ctx);
 bool uses_bulk_pipeline(nw_ctx* ctx);
 void graphs_clear(nw_ctx* ctx);
+void free_syn(SynState& s);
+int synapse_ring_clear(nw_ctx* ctx);
 int prepare_graph(nw_ctx* ctx, int k_steps);
 int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes, int32_t* threads, int32_t* fusion,
              double* ms_per_step);

@@ -227,6 +227,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
     // Steps s_off .. s_off + k_steps - 1 of the sequence that starts at the clock.
     const int64_t tick_base = a.clk->input_ticks + 2 * (int64_t)s_off;
     const int64_t row_base = a.clk->probe_len + s_off;
+    const int64_t step_base = a.clk->steps + s_off;
     const bool g_valid0 = s_off > 0 || a.clk->g_valid != 0;
     __shared__ int s_job;
     __shared__ int s_abort;
@@ -275,7 +276,8 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         const int nclamp = s_nclamp;
         if (BULK) slice = warp_slice(a, base, n);
         // Mechanism instance ranges of this neuron.
-        int64_t ib = 0, ie = 0, kb = 0, ke = 0;
+        int64_t ib = 0, ie = 0, kb = 0, ke = 0, yb = 0, ye = 0;
+        if (a.syn_on) { yb = a.syn_neuron_ptr[j]; ye = a.syn_neuron_ptr[j + 1]; }
         if (a.hh_on) {
             if (a.hh_identity) { ib = base; ie = base + n; }
             else { ib = a.hh_neuron_ptr[j]; ie = a.hh_neuron_ptr[j + 1]; }
@@ -286,7 +288,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         }
         // With one instance per segment the thread that updates a segment's
         // instances is the one that gathers them next; otherwise synchronise.
-        const bool mech_sync = (a.hh_on && !a.hh_identity) || (a.kin_on && !a.kin_identity);
+        const bool mech_sync = (a.hh_on && !a.hh_identity) || (a.kin_on && !a.kin_identity) || ye > yb;
         // AP detector state lives in thread 0's registers across the K steps.
         bool ap_state = false, ap_det = false;
         uint32_t spikes = 0;
@@ -335,6 +337,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                         for (int64_t k = kb + tid; k < ke; k += nthr)
                             kinetic_step(a, k, a.V[a.kin_identity ? k : (int64_t)a.kin_seg[k]]);
                     }
+                    for (int64_t k = yb + tid; k < ye; k += nthr) synapse_step(a, k, step_base + s);
                     if (mech_sync) __syncthreads();
                 }
             }
@@ -345,6 +348,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                 ap_det = over && !ap_state;
                 ap_state = over;
                 spikes += ap_det ? 1u : 0u;
+                if (a.syn_on) spike_ring_write(a, j, step_base + s, ap_det);
             }
             for (int p = pb + tid; p < pe; p += nthr)
                 a.trace[(row_base + s) * a.n_probes + a.probe_slot[p]] = a.V[a.probe_seg[p]];
@@ -493,9 +497,17 @@ static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
 
 // k_steps steps as launches of ctx->fusion fused steps each, on the context's
 // stream (also the body of a captured graph: no host synchronisation here).
+// Steps per launch: the fusion depth, capped by the shortest axonal delay so that
+// every spike a synapse reads was written by an earlier launch.
+static int fusion_steps(nw_ctx* ctx, int k_steps) {
+    int F = ctx->fusion > 0 ? ctx->fusion : k_steps;
+    if (ctx->syn.n > 0) F = std::min(F, ctx->syn.min_delay);
+    return std::max(F, 1);
+}
+
 template <typename real>
 static int enqueue_batched(nw_ctx* ctx, const BatchedCfg<real>& c, const StepArgs<real>& a0, int k_steps) {
-    const int F = ctx->fusion > 0 ? ctx->fusion : k_steps;
+    const int F = fusion_steps(ctx, k_steps);
     for (int s_off = 0; s_off < k_steps; s_off += F) {
         StepArgs<real> a = a0;
         a.k_steps = std::min(F, k_steps - s_off);
@@ -512,6 +524,7 @@ static int push_clock(nw_ctx* ctx) {
     DevClock v;
     memset(&v, 0, sizeof(v));
     v.input_ticks = ctx->input_ticks;
+    v.steps = ctx->steps;
     v.probe_len = ctx->probe_len;
     v.g_valid = ctx->g_valid ? 1 : 0;
     set_clock_kernel<<<1, 1, 0, ctx->stream>>>(ctx->dclock.as<DevClock>(), v);
@@ -546,7 +559,8 @@ static int launch_graph(nw_ctx* ctx, const BatchedCfg<real>& c, const StepArgs<r
     key_append(key, &ka, sizeof(ka));
     key_append(key, &c, sizeof(c));
     key_append(key, &k_steps, sizeof(k_steps));
-    key_append(key, &ctx->fusion, sizeof(ctx->fusion));
+    const int F = fusion_steps(ctx, k_steps);
+    key_append(key, &F, sizeof(F));
     key_append(key, &ctx->work_counter.ptr, sizeof(void*));
     for (auto& g : ctx->graphs) {
         if (g.key == key) {
@@ -672,6 +686,7 @@ static int plain_steps(nw_ctx* ctx, int k_steps) {
 }
 
 int advance_plain(nw_ctx* ctx, int k_steps) {
+    if (ctx->syn.n) return fail(ctx, NW_ERR_STATE, "the plain path has no synapses; use the batched path");
     return ctx->precision == NW_F64 ? plain_steps<double>(ctx, k_steps) : plain_steps<float>(ctx, k_steps);
 }
 

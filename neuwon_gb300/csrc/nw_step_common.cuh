@@ -99,6 +99,14 @@ struct StepArgs {
     const uint32_t* kin_seg_ptr; const int64_t* kin_neuron_ptr; const uint32_t* kin_seg;
     real* kin_state; const real* kin_gcoef; const real* kin_table;
     real kin_vmin, kin_frq, kin_cs, kin_erev;
+    // synapses
+    int syn_on, syn_ring_words, syn_ring_mask, syn_pulse;
+    const uint32_t* syn_seg_ptr; const int64_t* syn_neuron_ptr;
+    const int32_t* syn_pre; const int32_t* syn_delay;
+    const real* syn_wa; const real* syn_wn; real* syn_oa; real* syn_on_; real* syn_od;
+    int32_t* syn_pulse_end; uint32_t* syn_events; int32_t* syn_last; const real* syn_mats;
+    uint32_t* syn_ring;
+    real syn_e, syn_mg357;
     // clamps
     const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
     const int64_t* clamp_first; const int64_t* clamp_count;
@@ -148,6 +156,59 @@ __device__ __forceinline__ void segment_conductance(const StepArgs<real>& a, int
         G += gkin;
         GE += gkin * a.kin_erev;
     }
+    if (a.syn_on) {
+        const uint32_t b = a.syn_seg_ptr[i], e = a.syn_seg_ptr[i + 1];
+        if (b < e) {
+            // NMDA magnesium block at the segment's present voltage (Jahr & Stevens 1990).
+            const real block = real(1) / (real(1) + d_exp(real(-0.062) * a.V[i]) * a.syn_mg357);
+            real gs = real(0);
+            for (uint32_t k = b; k < e; ++k) gs += a.syn_wa[k] * a.syn_oa[k] + a.syn_wn[k] * a.syn_on_[k] * block;
+            G += gs;
+            GE += gs * a.syn_e;
+        }
+    }
+}
+
+// One synapse through step s_abs: a spike of its presynaptic neuron at step
+// s_abs - delay (read from that neuron's spike ring) arrives now and keeps
+// transmitter present for syn_pulse steps; then the exact per-step update of the
+// AMPA (C, O) and NMDA (C, O, D) schemes with the transmitter present or absent.
+template <typename real>
+__device__ __forceinline__ void synapse_step(const StepArgs<real>& a, int64_t k, int64_t s_abs) {
+    const int64_t src = s_abs - a.syn_delay[k];
+    bool arrive = false;
+    if (src >= 0) {
+        const uint32_t slot = (uint32_t)(src & a.syn_ring_mask);
+        const uint32_t w = __ldcg(a.syn_ring + (int64_t)a.syn_pre[k] * a.syn_ring_words + (slot >> 5));
+        arrive = ((w >> (slot & 31u)) & 1u) != 0u;
+    }
+    int32_t pe = a.syn_pulse_end[k];
+    if (arrive) {
+        pe = (int32_t)(s_abs + a.syn_pulse);
+        a.syn_pulse_end[k] = pe;
+        a.syn_events[k] += 1u;
+        a.syn_last[k] = (int32_t)s_abs;
+    }
+    const bool on = s_abs < (int64_t)pe;
+    const real* Ma = a.syn_mats + (on ? 0 : 4);
+    const real oa = a.syn_oa[k];
+    a.syn_oa[k] = Ma[2] * (real(1) - oa) + Ma[3] * oa;
+    const real* Mn = a.syn_mats + 8 + (on ? 0 : 9);
+    const real o = a.syn_on_[k], d = a.syn_od[k];
+    const real c = (real(1) - o) - d;
+    a.syn_on_[k] = Mn[3] * c + Mn[4] * o + Mn[5] * d;
+    a.syn_od[k] = Mn[6] * c + Mn[7] * o + Mn[8] * d;
+}
+
+// The AP detector's output for step s_abs into the neuron's spike ring (the
+// neuron's own CTA is the only writer of its words).
+template <typename real>
+__device__ __forceinline__ void spike_ring_write(const StepArgs<real>& a, int64_t j, int64_t s_abs, bool spike) {
+    const uint32_t slot = (uint32_t)(s_abs & a.syn_ring_mask);
+    uint32_t* wp = a.syn_ring + j * a.syn_ring_words + (slot >> 5);
+    const uint32_t bit = 1u << (slot & 31u);
+    const uint32_t w = __ldcg(wp);
+    *wp = spike ? (w | bit) : (w & ~bit);
 }
 
 // Voltage -> (bucket, location within it) as the generated lti_sim kernel
@@ -380,6 +441,19 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.kin_seg = K.seg.as<uint32_t>();
     a.kin_state = K.state.as<real>(); a.kin_gcoef = K.gcoef.as<real>(); a.kin_table = K.table.as<real>();
     a.kin_vmin = (real)K.vmin; a.kin_frq = (real)K.frq; a.kin_cs = (real)K.conserve; a.kin_erev = (real)K.erev;
+    const SynState& Y = ctx->syn;
+    a.syn_on = Y.n > 0 ? 1 : 0;
+    if (Y.n > 0) {
+        a.syn_ring_words = Y.ring_words; a.syn_ring_mask = Y.ring_steps - 1; a.syn_pulse = Y.pulse_steps;
+        a.syn_seg_ptr = Y.seg_ptr.as<uint32_t>(); a.syn_neuron_ptr = Y.neuron_ptr.as<int64_t>();
+        a.syn_pre = Y.pre.as<int32_t>(); a.syn_delay = Y.delay.as<int32_t>();
+        a.syn_wa = Y.wa.as<real>(); a.syn_wn = Y.wn.as<real>();
+        a.syn_oa = Y.oa.as<real>(); a.syn_on_ = Y.on.as<real>(); a.syn_od = Y.od.as<real>();
+        a.syn_pulse_end = Y.pulse_end.as<int32_t>(); a.syn_events = Y.events.as<uint32_t>();
+        a.syn_last = Y.last_event.as<int32_t>(); a.syn_mats = Y.mats.as<real>();
+        a.syn_ring = Y.ring.as<uint32_t>();
+        a.syn_e = (real)Y.e_syn; a.syn_mg357 = (real)(Y.mg / 3.57);
+    }
     const double q10 = pow(3.0, (ctx->celsius - 6.3) / 10.0);      // hh.mod:67
     a.dtq10 = (real)(ctx->time_step * q10);
     if (ctx->n_clamps) {

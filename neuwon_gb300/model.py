@@ -298,6 +298,8 @@ class RxD_Model:
             self._load_mechanism(m)
         self._clamps = []
         self._probes = []
+        self._syn = None
+        self._dirty_synapses = False
         self._ctx = None
         self._order = None
         self._geom_cache = None
@@ -374,6 +376,50 @@ class RxD_Model:
         self.input_hook.ticks += 2 * k
         self.advance_hook._tick(k)
 
+    def add_synapses(self, pre_neurons, post_segments, w_ampa, w_nmda=None, delay=1.0, kinetics=None):
+        """Synapses from neurons (handles or ids) onto segments (handles or creation
+        indices) with AMPA / NMDA weights in nS and axonal delays in ms (rounded to
+        whole steps, at least one).  Returns the new synapses' indices."""
+        from .synapses import SynapseKinetics, delay_steps
+        pre = np.array([getattr(p, "_nid", p) for p in np.atleast_1d(np.asarray(pre_neurons, dtype=object))],
+                       dtype=np.int64)
+        post = np.array([getattr(s, "_idx", s) for s in np.atleast_1d(np.asarray(post_segments, dtype=object))],
+                        dtype=np.int64)
+        m = len(pre)
+        if len(post) != m:
+            raise ValueError("pre_neurons and post_segments differ in length")
+        if np.any(pre < 0) or np.any(pre >= len(self._neuron_root)):
+            raise ValueError("presynaptic neuron out of range")
+        if np.any(post < 0) or np.any(post >= self._n):
+            raise ValueError("post segment out of range")
+        wa = np.broadcast_to(np.asarray(w_ampa, dtype=np.float64), (m,))
+        wn = wa if w_nmda is None else np.broadcast_to(np.asarray(w_nmda, dtype=np.float64), (m,))
+        d = np.broadcast_to(delay_steps(delay, self.time_step), (m,))
+        old = self._syn or {"pre": np.empty(0, np.int64), "post": np.empty(0, np.int64),
+                            "wa": np.empty(0), "wn": np.empty(0), "delay": np.empty(0, np.int64),
+                            "kinetics": SynapseKinetics()}
+        if kinetics is not None:
+            old["kinetics"] = kinetics
+        first = len(old["pre"])
+        self._syn = {"pre": np.concatenate([old["pre"], pre]), "post": np.concatenate([old["post"], post]),
+                     "wa": np.concatenate([old["wa"], wa]), "wn": np.concatenate([old["wn"], wn]),
+                     "delay": np.concatenate([old["delay"], d]), "kinetics": old["kinetics"]}
+        self._dirty_synapses = True
+        return np.arange(first, first + m)
+
+    def _sync_synapses(self):
+        sy = self._syn
+        kin = sy["kinetics"]
+        ao, af, no, nf = (np.ascontiguousarray(x, dtype=np.float64) for x in kin.matrices(self.time_step))
+        post_dev = np.ascontiguousarray(self._inv[sy["post"]])
+        self._ctx.call("nw_synapses_set", len(sy["pre"]), _lib.ptr(np.ascontiguousarray(sy["pre"])),
+                       _lib.ptr(post_dev), _lib.ptr(np.ascontiguousarray(sy["wa"] * 1e-9)),
+                       _lib.ptr(np.ascontiguousarray(sy["wn"] * 1e-9)),
+                       _lib.ptr(np.ascontiguousarray(sy["delay"], dtype=np.int32)),
+                       _lib.ptr(ao), _lib.ptr(af), _lib.ptr(no), _lib.ptr(nf),
+                       kin.pulse_steps(self.time_step), kin.e_syn, kin.mg)
+        self._dirty_synapses = False
+
     def autotune(self, trial_steps=10):
         """Choose the batched path's lanes per row, threads per CTA and step-fusion
         depth by timing short runs of this model (state restored afterwards)."""
@@ -433,6 +479,11 @@ class RxD_Model:
             return self._get_segment_values(name).copy()
         if name.startswith("Neuron."):
             return self._get_neuron_values(name).copy()
+        if name.startswith("Synapse."):
+            self._sync()
+            n = 0 if self._syn is None else len(self._syn["pre"])
+            dt = np.int64 if name in ("Synapse.events", "Synapse.last_event", "Synapse.pulse_end") else np.float64
+            return self._ctx.get_data(name, n, dt)
         mech, attr = name.split(".")
         self._sync()
         cls = self.mechanisms[mech]
@@ -585,6 +636,8 @@ class RxD_Model:
             self._sync_detectors()
         if self._dirty_probes:
             self._sync_probes()
+        if self._dirty_synapses:
+            self._sync_synapses()
 
     def _sync_structure(self):
         ctx = self._ctx
@@ -621,6 +674,7 @@ class RxD_Model:
                 self._sync_hh(cls)
         self._dirty_structure = False
         self._dirty_clamps = self._dirty_detectors = self._dirty_probes = True
+        self._dirty_synapses = self._syn is not None
         if saved is not None:
             self._restore_state(saved)
         for key, (name, values) in list(self._pending.items()):

@@ -198,6 +198,105 @@ class KineticInstances:
         self.g += self.g_coef * self.state[:, self.open_states].sum(axis=1)
 
 
+# --------------------------------------------------------------------- synapses
+# The reference has no synaptic kinetics and no event delivery (its
+# neuwon/rxd/synapses.py only grows synapse geometry; there is no NET_RECEIVE).
+# What follows is this project's definition, restated here as the oracle for the
+# GPU kernels: spikes are the AP detector's output (neuron.py:184-188), routed
+# through a priority queue to synapses after an axonal delay of whole steps.
+
+def synapse_matrices(time_step, alpha, beta, delta=None, rho=None, t_max=1.0):
+    """Exact per-step transition matrices (row-major, new state from old) of the
+    2-state AMPA scheme C <-> O or the 3-state NMDA scheme C -> O -> D -> C
+    (C -> O at alpha*T, O -> C at beta, O -> D at delta, D -> C at rho), with the
+    transmitter present (T = t_max) and absent (T = 0)."""
+    import scipy.linalg
+    out = []
+    for T in (t_max, 0.0):
+        if delta is None:
+            Q = np.array([[-alpha * T, beta], [alpha * T, -beta]])
+        else:
+            Q = np.array([[-alpha * T, beta, rho],
+                          [alpha * T, -beta - delta, 0.0],
+                          [0.0, delta, -rho]])
+        out.append(scipy.linalg.expm(Q * time_step))
+    return out
+
+
+class EventQueue:
+    """Spike (neuron, step) -> deliveries (step + delay, synapse), kept in a heap."""
+
+    def __init__(self, pre, delay):
+        import heapq
+        self._heapq = heapq
+        self.pre = np.asarray(pre, dtype=np.int64)
+        self.delay = np.asarray(delay, dtype=np.int64)
+        order = np.argsort(self.pre, kind="stable")
+        self._out = {}
+        for k in order:
+            self._out.setdefault(int(self.pre[k]), []).append(int(k))
+        self._heap = []
+
+    def push(self, step, neurons):
+        for j in neurons:
+            for k in self._out.get(int(j), ()):
+                self._heapq.heappush(self._heap, (step + int(self.delay[k]), k))
+
+    def pop(self, step):
+        got = []
+        while self._heap and self._heap[0][0] <= step:
+            when, k = self._heapq.heappop(self._heap)
+            assert when == step, "event in the past"
+            got.append(k)
+        return sorted(got)
+
+
+class SynapseInstances:
+    """AMPA (C, O) + NMDA (C, O, D) per synapse, on post segments.
+
+    g = w_ampa * O_ampa + w_nmda * O_nmda * B(V),  B(V) = 1 / (1 + exp(-0.062 V) mg / 3.57)
+    (Jahr & Stevens 1990), reversal e_syn.  A delivery at step s keeps transmitter
+    present for the mechanism updates of steps s .. s + pulse_steps - 1."""
+
+    def __init__(self, segment, pre, delay_steps, w_ampa, w_nmda, ampa_on, ampa_off, nmda_on, nmda_off,
+                 pulse_steps, e_syn=0.0, mg=1.0):
+        self.segment = np.asarray(segment, dtype=np.int64)
+        self.pre = np.asarray(pre, dtype=np.int64)
+        self.delay = np.asarray(delay_steps, dtype=np.int64)
+        self.w_ampa = np.asarray(w_ampa, dtype=np.float64)
+        self.w_nmda = np.asarray(w_nmda, dtype=np.float64)
+        self.Ma = (np.asarray(ampa_on), np.asarray(ampa_off))
+        self.Mn = (np.asarray(nmda_on), np.asarray(nmda_off))
+        self.pulse_steps = int(pulse_steps)
+        self.e_syn = float(e_syn)
+        self.mg = float(mg)
+        m = len(self.segment)
+        self.ampa = np.zeros((m, 2)); self.ampa[:, 0] = 1.0
+        self.nmda = np.zeros((m, 3)); self.nmda[:, 0] = 1.0
+        self.pulse_end = np.zeros(m, dtype=np.int64)
+        self.events = np.zeros(m, dtype=np.int64)
+        self.last_event = np.full(m, -1, dtype=np.int64)
+        self.queue = EventQueue(self.pre, self.delay)
+        self.delivered = []                      # (step, synapse) log
+
+    def conductance(self, voltage):
+        v = voltage[self.segment]
+        block = 1.0 / (1.0 + np.exp(-0.062 * v) * (self.mg / 3.57))
+        return self.w_ampa * self.ampa[:, 1] + self.w_nmda * self.nmda[:, 1] * block
+
+    def advance(self, step):
+        for k in self.queue.pop(step):
+            self.pulse_end[k] = step + self.pulse_steps
+            self.events[k] += 1
+            self.last_event[k] = step
+            self.delivered.append((step, k))
+        on = step < self.pulse_end
+        for Mx, st in ((self.Ma, self.ampa), (self.Mn, self.nmda)):
+            new_on = st @ Mx[0].T
+            new_off = st @ Mx[1].T
+            st[:] = np.where(on[:, None], new_on, new_off)
+
+
 class OracleModel:
     """FP64 restatement of ``RxD_Model.advance()`` (neuwon/rxd/rxd_model.py:63-80).
 
@@ -214,7 +313,7 @@ class OracleModel:
 
     def __init__(self, parent, R, C, *, time_step=0.1, celsius=6.3, v_init=-70.0,
                  prune=EPSILON, propagator_matrix=None, hh=None, clamps=(),
-                 detectors=(), duplicates="sum", kinetic=None):
+                 detectors=(), duplicates="sum", kinetic=None, synapses=None):
         self.parent = np.asarray(parent, dtype=np.int64)
         self.n = len(self.parent)
         self.R = np.asarray(R, dtype=np.float64)
@@ -232,6 +331,7 @@ class OracleModel:
             propagator(self.parent, self.R, self.C, self.half_step, prune)
         self.hh = hh
         self.kinetic = kinetic
+        self.synapses = synapses
         self.clamps = [(int(s), float(a), int(f), int(k)) for (s, a, f, k) in clamps]
         self.detectors = [(int(s), float(t)) for (s, t) in detectors]
         self.AP_detected = np.zeros(len(self.detectors), dtype=bool)
@@ -260,6 +360,11 @@ class OracleModel:
             k = self.kinetic
             np.add.at(self.sum_conductance, k.segment, k.g)
             np.add.at(self.driving_voltage, k.segment, k.g * k.erev)
+        if self.synapses is not None:
+            sy = self.synapses
+            g = sy.conductance(self.voltage)
+            np.add.at(self.sum_conductance, sy.segment, g)
+            np.add.at(self.driving_voltage, sy.segment, g * sy.e_syn)
         # input_hook.tick(): Clock.tick then TimeSeries._play_implementation
         # (database/time.py:114-117, 287-302), current clamps in "+=" mode.
         self.input_ticks += 1
@@ -292,6 +397,8 @@ class OracleModel:
         if self.kinetic is not None:
             self.kinetic.zero_accumulators()
             self.kinetic.advance(self.voltage)
+        if self.synapses is not None:
+            self.synapses.advance(self.steps)
 
     # neuwon/rxd/neuron/neuron.py:184-188
     def _advance_AP_detector(self):
@@ -300,6 +407,8 @@ class OracleModel:
             self.AP_detected[k] = over and not self._AP_true_state[k]
             self._AP_true_state[k] = over
             self.spike_count[k] += int(self.AP_detected[k])
+        if self.synapses is not None:
+            self.synapses.queue.push(self.steps, np.flatnonzero(self.AP_detected))
 
     def advance(self):
         """rxd_model.py:63-80: species(dt/2) -> mechanisms(dt) -> species(dt/2) -> AP."""

@@ -111,3 +111,42 @@ def run_with_clamps(model, clamps, offs, steps):
                 nw.Segment(model, offs[ti] + s).inject_current(nA, dur)
         model.advance()
     return out
+
+
+def network_case(sizes, num_synapses, *, seed=0, time_step=0.1, precision="f64", currents=None,
+                 delay_lo=1.0, delay_hi=5.0, oracle=True, tolerance=None):
+    """Random trees wired by random_network; HH everywhere, a soma current per neuron.
+
+    Returns (gpu model, oracle model or None, net dict, offsets)."""
+    import neuwon_gb300 as nw
+    from neuwon_gb300.synapses import SynapseKinetics, random_network
+    from oracle.reference_step import SynapseInstances, synapse_matrices
+    trees = [random_tree(int(n), seed=seed * 1000 + k) for k, n in enumerate(sizes)]
+    net = random_network([len(t) for t in trees], num_synapses, seed, time_step=time_step,
+                         delay_lo=delay_lo, delay_hi=delay_hi)
+    rng = np.random.default_rng(seed + 7)
+    amps = rng.uniform(0.05, 0.5, len(trees)) if currents is None else np.asarray(currents)
+    clamps = [(k, 0, float(amps[k]), 0.0, 1e9) for k in range(len(trees))]
+    hh_kw = dict(ena=50.0, ek=-77.0, el=-54.3)
+    kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
+    m = nw.RxD_Model(time_step=time_step, precision=precision, mechanisms=[nw.HH.configure(**hh_kw)], **kw)
+    neurons = [m.add_tree(t) for t in trees]
+    m.insert_everywhere("hh")
+    offs = np.cumsum([0] + [len(t) for t in trees])[:-1]
+    post = offs[net["post_neuron"]] + net["post_local"]
+    kin = SynapseKinetics()
+    m.add_synapses(net["pre"], post, net["weight_nS"], net["weight_nS"], net["delay_steps"] * time_step,
+                   kinetics=kin)
+    for (ti, s, nA, start, dur) in clamps:
+        nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+    om = None
+    if oracle:
+        om, info = oracle_case(trees, clamps, time_step=time_step, hh_kw=hh_kw,
+                               prune=tolerance if tolerance is not None else None)
+        ao, af = synapse_matrices(time_step, kin.ampa_alpha, kin.ampa_beta, t_max=kin.t_max)
+        no, nf = synapse_matrices(time_step, kin.nmda_alpha, kin.nmda_beta, kin.nmda_delta, kin.nmda_rho,
+                                  t_max=kin.t_max)
+        om.synapses = SynapseInstances(post, net["pre"], net["delay_steps"], net["weight_nS"] * 1e-9,
+                                       net["weight_nS"] * 1e-9, ao, af, no, nf,
+                                       kin.pulse_steps(time_step), kin.e_syn, kin.mg)
+    return m, om, dict(net, post=post), offs

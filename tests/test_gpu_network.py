@@ -1,0 +1,98 @@
+"""Spike events and synapses on the GPU against the oracle's priority queue.
+
+Routing is integer work and must be bit-exact: given the spike list the GPU
+produced, the oracle queue delivers the same events to the same synapses at
+the same steps (per-synapse event counts and last delivery step).  Dynamics
+(HH + AMPA/NMDA) in FP64 match the oracle's voltages."""
+import numpy as np
+import pytest
+
+from oracle.reference_step import EventQueue
+from tests.helpers import network_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _replay_queue(net, spikes, steps):
+    """Per-synapse (events, last_event) from the oracle queue fed with a spike list."""
+    q = EventQueue(net["pre"], net["delay_steps"])
+    by_step = {}
+    for j, t in spikes:
+        by_step.setdefault(t, []).append(j)
+    M = len(net["pre"])
+    events = np.zeros(M, np.int64)
+    last = np.full(M, -1, np.int64)
+    for step in range(steps):
+        for k in q.pop(step):
+            events[k] += 1
+            last[k] = step
+        q.push(step, by_step.get(step, []))
+    return events, last
+
+
+def _run_recording(m, steps):
+    spikes = []
+    for step in range(steps):
+        m.advance(1)
+        ap = m.get_data("Neuron.AP_detected")
+        spikes += [(int(j), step) for j in np.flatnonzero(ap)]
+    return spikes
+
+
+def test_f64_network_matches_oracle():
+    m, om, net, offs = network_case([150, 90, 200, 60], 300, seed=2, delay_lo=1.0, delay_hi=4.0)
+    steps = 400
+    spikes = []
+    worst = 0.0
+    for step in range(steps):
+        m.advance(1)
+        om.advance()
+        spikes += [(int(j), step) for j in np.flatnonzero(m.get_data("Neuron.AP_detected"))]
+        if step % 20 == 19:
+            worst = max(worst, np.abs(m.get_data("Segment.voltage") - om.voltage).max())
+    assert worst < 1e-6, worst
+    np.testing.assert_array_equal(m.get_data("Neuron.spike_count"), om.spike_count)
+    assert len(spikes) > 4
+    ev, last = _replay_queue(net, spikes, steps)
+    np.testing.assert_array_equal(m.get_data("Synapse.events"), om.synapses.events)
+    np.testing.assert_array_equal(m.get_data("Synapse.events"), ev)
+    np.testing.assert_array_equal(m.get_data("Synapse.last_event"), last)
+    assert ev.sum() > 0
+    for name, ref in (("Synapse.ampa_open", om.synapses.ampa[:, 1]), ("Synapse.nmda_open", om.synapses.nmda[:, 1]),
+                      ("Synapse.nmda_desensitized", om.synapses.nmda[:, 2])):
+        assert np.abs(m.get_data(name) - ref).max() < 1e-9
+    m.close()
+
+
+def test_fusion_is_capped_by_the_shortest_delay():
+    """Fusing more steps than the shortest delay would read spikes not yet written;
+    the library caps it, so any requested depth gives the single-step result."""
+    res = []
+    for fusion in (1, 50):
+        m, _, net, _ = network_case([300, 200, 250, 100, 400], 2000, seed=3, precision="f32", oracle=False,
+                                    delay_lo=1.0, delay_hi=3.0)
+        m._sync()
+        m._ctx.set_option("fusion_depth", fusion)
+        m.advance(300)
+        res.append((m.get_data("Segment.voltage"), m.get_data("Synapse.events"), m.get_data("Neuron.spike_count")))
+        m.close()
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
+    assert res[0][1].sum() > 0
+
+
+def test_f32_routing_is_bit_exact_given_the_spike_list():
+    """A larger FP32 network (64 neurons, 20,000 synapses, delays 1-20 ms, 300 ms):
+    every synapse's delivery count and last delivery step equal the oracle queue's
+    for the spikes the GPU produced."""
+    rng = np.random.default_rng(11)
+    sizes = np.exp(rng.uniform(np.log(200), np.log(1500), 64)).astype(int)
+    m, _, net, _ = network_case(sizes, 20000, seed=4, precision="f32", oracle=False, delay_lo=1.0, delay_hi=20.0,
+                                tolerance=1e-8)
+    steps = 3000
+    spikes = _run_recording(m, steps)
+    ev, last = _replay_queue(net, spikes, steps)
+    assert len(spikes) > 50 and ev.sum() > 1000
+    np.testing.assert_array_equal(m.get_data("Synapse.events"), ev)
+    np.testing.assert_array_equal(m.get_data("Synapse.last_event"), last)
+    m.close()
