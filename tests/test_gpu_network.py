@@ -96,3 +96,21 @@ def test_f32_routing_is_bit_exact_given_the_spike_list():
     np.testing.assert_array_equal(m.get_data("Synapse.events"), ev)
     np.testing.assert_array_equal(m.get_data("Synapse.last_event"), last)
     m.close()
+
+
+def test_autotune_restores_synapse_state():
+    m, _, net, _ = network_case([300, 200, 250], 800, seed=5, precision="f32", oracle=False, delay_lo=1.0,
+                                delay_hi=3.0)
+    m.advance(200)
+    names = ("Synapse.events", "Synapse.last_event", "Synapse.pulse_end", "Synapse.ampa_open", "Synapse.nmda_open")
+    before = [m.get_data(n) for n in names]
+    ref, _, _, _ = network_case([300, 200, 250], 800, seed=5, precision="f32", oracle=False, delay_lo=1.0,
+                                delay_hi=3.0)
+    ref.advance(200)
+    m.autotune(trial_steps=4)
+    for n, b in zip(names, before):
+        assert np.array_equal(m.get_data(n), b)
+    m.advance(200)
+    ref.advance(200)
+    np.testing.assert_array_equal(m.get_data("Synapse.events"), ref.get_data("Synapse.events"))
+    m.close(); ref.close()
