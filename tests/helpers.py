@@ -129,7 +129,8 @@ def network_case(sizes, num_synapses, *, seed=0, time_step=0.1, precision="f64",
     clamps = [(k, 0, float(amps[k]), 0.0, 1e9) for k in range(len(trees))]
     hh_kw = dict(ena=50.0, ek=-77.0, el=-54.3)
     kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
-    m = nw.RxD_Model(time_step=time_step, precision=precision, mechanisms=[nw.HH.configure(**hh_kw)], **kw)
+    m = nw.RxD_Model(time_step=time_step, temperature=6.3, precision=precision,
+                     mechanisms=[nw.HH.configure(**hh_kw)], **kw)
     neurons = [m.add_tree(t) for t in trees]
     m.insert_everywhere("hh")
     offs = np.cumsum([0] + [len(t) for t in trees])[:-1]
