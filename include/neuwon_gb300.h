@@ -48,6 +48,8 @@ typedef struct nw_ctx nw_ctx;
 /* Step implementations for nw_advance. */
 #define NW_PATH_BATCHED 0   /* persistent fused K-step kernel, one CTA per neuron */
 #define NW_PATH_PLAIN   1   /* per-neuron launches, one thread per row/instance  */
+#define NW_PATH_WIDE    2   /* whole-model launches per half step, rows spread over all
+                               SMs: neurons of any size (no shared-memory or 65,535 limit) */
 
 /* ---- context -------------------------------------------------------- */
 
@@ -185,7 +187,9 @@ int nw_probes_read(nw_ctx* ctx, void* host, int dtype, int64_t max_rows, int64_t
 
 /* Replaces RxD_Model.advance (neuwon/rxd/rxd_model.py:63-80) called k_steps times:
  * species(dt/2) -> mechanisms(dt) -> species(dt/2) -> AP detector, per step.
- * path selects NW_PATH_BATCHED (fused persistent kernel) or NW_PATH_PLAIN.  The
+ * path selects NW_PATH_BATCHED (fused persistent kernel), NW_PATH_WIDE (neurons of any
+ * size; one launch per phase, replayed as CUDA graphs of up to 32 steps) or
+ * NW_PATH_PLAIN.  The
  * batched path runs the k_steps as launches of "fusion_depth" fused steps, captured
  * once per distinct call shape in a CUDA graph and replayed (option "cuda_graph"). */
 int nw_advance(nw_ctx* ctx, int32_t k_steps, int path);

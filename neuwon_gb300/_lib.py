@@ -16,7 +16,7 @@ NW_F32, NW_F64 = 4, 8
 DTYPES = {np.dtype(np.float64): 1, np.dtype(np.float32): 2, np.dtype(np.int64): 3,
           np.dtype(np.int32): 4, np.dtype(np.uint32): 5, np.dtype(np.uint8): 6,
           np.dtype(np.bool_): 6}
-PATH_BATCHED, PATH_PLAIN = 0, 1
+PATH_BATCHED, PATH_PLAIN, PATH_WIDE = 0, 1, 2
 
 EXPORTS = [
     "nw_version", "nw_ctx_create", "nw_ctx_destroy", "nw_last_error", "nw_get_stream",

@@ -263,7 +263,8 @@ int nw_ctx_destroy(nw_ctx* ctx) {
                       &ctx->clamp_neuron_ptr, &ctx->clamp_amp_stage, &ctx->det_seg, &ctx->det_thr,
                       &ctx->ap_detected, &ctx->ap_state, &ctx->spike_count, &ctx->probe_seg,
                       &ctx->probe_neuron_ptr, &ctx->probe_slot, &ctx->trace, &ctx->neuron_order,
-                      &ctx->work_counter, &ctx->status, &ctx->plain_x, &ctx->dclock};
+                      &ctx->work_counter, &ctx->status, &ctx->plain_x, &ctx->dclock,
+                      &ctx->clamp_seg_ptr, &ctx->w_rowptr, &ctx->w_col, &ctx->w_val, &ctx->w_leak};
     for (DevBuf* b : bufs) dev_free(*b);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -576,8 +577,9 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");
     if (rows) *rows = ctx->n_seg;
     if (nnz) *nnz = ctx->nnz64;
-    if (stored) *stored = ctx->nnz_b;
-    if (bytes) *bytes = ctx->nnz_b * (2 + ctx->precision) + ctx->n_seg * (8 + ctx->precision);
+    if (stored) *stored = ctx->b_ok ? ctx->nnz_b : ctx->nnz_w;
+    if (bytes) *bytes = ctx->b_ok ? ctx->nnz_b * (2 + ctx->precision) + ctx->n_seg * (8 + ctx->precision)
+                                  : ctx->nnz_w * (4 + ctx->precision) + ctx->n_seg * (8 + ctx->precision);
     return NW_OK;
 }
 
@@ -811,8 +813,11 @@ int nw_clamps_set(nw_ctx* ctx, int64_t count, const int64_t* segment, const doub
     for (int64_t k = 0; k < ctx->n_neuron; ++k) per[k + 1] += per[k];
     std::vector<int64_t> order(count);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return nb[a] < nb[b]; });
-    std::vector<uint32_t> seg(count);
+    // By segment (segments are neuron-contiguous, so also by neuron).
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return segment[a] < segment[b]; });
+    std::vector<uint32_t> seg(count), seg_ptr(ctx->n_seg + 1, 0);
+    for (int64_t c = 0; c < count; ++c) seg_ptr[segment[c] + 1]++;
+    for (int64_t i = 0; i < ctx->n_seg; ++i) seg_ptr[i + 1] += seg_ptr[i];
     std::vector<double> amp(count);
     std::vector<int64_t> first(count), cnt(count);
     ctx->clamp_user_to_sorted.assign(count, 0);
@@ -828,6 +833,8 @@ int nw_clamps_set(nw_ctx* ctx, int64_t count, const int64_t* segment, const doub
     NW_CHECK(dev_alloc(ctx, ctx->clamp_first, 8 * n1));
     NW_CHECK(dev_alloc(ctx, ctx->clamp_count, 8 * n1));
     NW_CHECK(dev_alloc(ctx, ctx->clamp_neuron_ptr, 4 * (ctx->n_neuron + 1)));
+    NW_CHECK(dev_alloc(ctx, ctx->clamp_seg_ptr, 4 * (ctx->n_seg + 1)));
+    NW_CHECK(upload_convert(ctx, ctx->clamp_seg_ptr.ptr, NW_DTYPE_U32, seg_ptr.data(), NW_DTYPE_U32, ctx->n_seg + 1));
     NW_CHECK(upload_convert(ctx, ctx->clamp_seg.ptr, NW_DTYPE_U32, seg.data(), NW_DTYPE_U32, count));
     NW_CHECK(upload_convert(ctx, ctx->clamp_amp.ptr, real_dtype(ctx), amp.data(), NW_DTYPE_F64, count));
     NW_CHECK(upload_convert(ctx, ctx->clamp_first.ptr, NW_DTYPE_I64, first.data(), NW_DTYPE_I64, count));
@@ -942,6 +949,7 @@ int nw_advance(nw_ctx* ctx, int32_t k_steps, int path) {
     if (k_steps == 0) return NW_OK;
     if (path == NW_PATH_BATCHED) NW_CHECK(advance_batched(ctx, k_steps));
     else if (path == NW_PATH_PLAIN) NW_CHECK(advance_plain(ctx, k_steps));
+    else if (path == NW_PATH_WIDE) NW_CHECK(advance_wide(ctx, k_steps));
     else return fail(ctx, NW_ERR_ARG, "nw_advance: unknown path");
     return read_status(ctx);
 }

@@ -135,9 +135,12 @@ struct nw_ctx {
     // batched difference form (off-diagonal entries, u16 neuron-relative
     // columns, rows padded to 4 entries, per-row leak = 1 - row sum).
     bool prop_valid = false;
-    int64_t nnz64 = 0, nnz_b = 0;
+    bool b_ok = false;          // batched format present (every neuron <= 65,535 segments)
+    bool w_ok = false;          // wide format present (built on first use of the wide path)
+    int64_t nnz64 = 0, nnz_b = 0, nnz_w = 0;
     nw::DevBuf p_rowptr, p_col, p_val;          // i64, i32, f64
     nw::DevBuf b_rowptr, b_col, b_val, b_leak;  // i64, u16, real, real
+    nw::DevBuf w_rowptr, w_col, w_val, w_leak;  // i64, i32 (global columns), real, real
 
     // Mechanisms.
     nw::HHState hh;
@@ -150,6 +153,7 @@ struct nw_ctx {
     int64_t n_clamps = 0;
     std::vector<int64_t> clamp_user_to_sorted;
     nw::DevBuf clamp_seg, clamp_amp, clamp_first, clamp_count, clamp_neuron_ptr;
+    nw::DevBuf clamp_seg_ptr;    // u32 [n_seg+1]: clamps are sorted by segment
     nw::DevBuf clamp_amp_stage;  // f64 staging for nw_advance_host
 
     // Detectors (one per neuron).
@@ -197,6 +201,9 @@ int propagator_conserve(nw_ctx* ctx);
 // Stepping (nw_step.cu).
 int advance_batched(nw_ctx* ctx, int k_steps);
 int advance_plain(nw_ctx* ctx, int k_steps);
+int advance_wide(nw_ctx* ctx, int k_steps);
+int ensure_wide(nw_ctx* ctx);
+void free_wide(nw_ctx* ctx);
 int choose_lanes_per_row(nw_ctx* ctx);
 bool uses_bulk_pipeline(nw_ctx* ctx);
 void graphs_clear(nw_ctx* ctx);

@@ -371,22 +371,25 @@ int propagator_conserve(nw_ctx* ctx) {
 
 // ------------------------------------------------- batched difference form
 
-__global__ void batched_count_kernel(int64_t n, const int64_t* prow, const int32_t* pcol, int64_t* cnt) {
+__global__ void rows_count_kernel(int64_t n, const int64_t* prow, const int32_t* pcol, int64_t* cnt) {
     int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= n) return;
     int64_t c = 0;
     for (int64_t k = prow[r]; k < prow[r + 1]; ++k) c += (pcol[k] != (int32_t)r);
-    cnt[r] = (c + 7) & ~(int64_t)7;   // 8-entry rows: 16-byte aligned bulk copies
+    cnt[r] = (c + 7) & ~(int64_t)7;   // 8-entry rows: 16-byte aligned vectors and bulk copies
 }
 
-template <typename real>
-__global__ void batched_fill_kernel(int64_t n, const int64_t* neuron_of_row_base, const int64_t* prow,
-                                    const int32_t* pcol, const double* pval, const int64_t* brow,
-                                    uint16_t* bcol, real* bval, real* leak) {
+// Off-diagonal entries of each row (warp per row, order kept) with columns
+// relative to the row's neuron (u16, batched format) or global (i32, wide
+// format), zero padding, and leak = 1 - row sum accumulated in FP64.
+template <typename real, typename CT>
+__global__ void rows_fill_kernel(int64_t n, const int64_t* neuron_of_row_base, const int64_t* prow,
+                                 const int32_t* pcol, const double* pval, const int64_t* brow,
+                                 CT* bcol, real* bval, real* leak) {
     const int lane = threadIdx.x & 31;
     const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (r >= n) return;
-    const int64_t base = neuron_of_row_base[r];
+    const int64_t base = neuron_of_row_base ? neuron_of_row_base[r] : 0;
     int64_t ob = brow[r];
     double sum = 0.0;
     for (int64_t k0 = prow[r]; k0 < prow[r + 1]; k0 += 32) {
@@ -398,58 +401,92 @@ __global__ void batched_fill_kernel(int64_t n, const int64_t* neuron_of_row_base
         const bool off = valid && c != (int32_t)r;
         const unsigned mask = __ballot_sync(0xffffffffu, off);
         const int pos = __popc(mask & ((1u << lane) - 1u));
-        if (off) { bcol[ob + pos] = (uint16_t)(c - base); bval[ob + pos] = (real)v; }
+        if (off) { bcol[ob + pos] = (CT)(c - base); bval[ob + pos] = (real)v; }
         ob += __popc(mask);
     }
-    for (int64_t k = ob + lane; k < brow[r + 1]; k += 32) { bcol[k] = 0; bval[k] = real(0); }
+    // Padding points at the row itself (x_i - x_i = 0 in the difference form).
+    for (int64_t k = ob + lane; k < brow[r + 1]; k += 32) { bcol[k] = (CT)(r - base); bval[k] = real(0); }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
     if (lane == 0) leak[r] = (real)(1.0 - sum);
 }
 
-int propagator_to_batched(nw_ctx* ctx) {
+void free_wide(nw_ctx* ctx) {
+    for (DevBuf* b : {&ctx->w_rowptr, &ctx->w_col, &ctx->w_val, &ctx->w_leak}) dev_free(*b);
+    ctx->w_ok = false;
+    ctx->nnz_w = 0;
+}
+
+// Builds one row format from the FP64 CSR: relative u16 columns into the b_*
+// buffers (wide = false) or global i32 columns into the w_* buffers.
+template <typename CT>
+static int propagator_to_rows(nw_ctx* ctx, bool wide) {
     const int64_t n = ctx->n_seg;
     DevBuf d_cnt, d_base;
     NW_CHECK(dev_alloc(ctx, d_cnt, 8 * n));
-    int rc = dev_alloc(ctx, d_base, 8 * n);
-    if (rc != NW_OK) { dev_free(d_cnt); return rc; }
-    std::vector<int64_t> base(n);
-    for (int64_t j = 0; j < ctx->n_neuron; ++j)
-        for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) base[i] = ctx->h_neuron_start[j];
-    cudaMemcpyAsync(d_base.ptr, base.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
-    batched_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+    int rc = NW_OK;
+    if (!wide) {
+        rc = dev_alloc(ctx, d_base, 8 * n);
+        if (rc != NW_OK) { dev_free(d_cnt); return rc; }
+        std::vector<int64_t> base(n);
+        for (int64_t j = 0; j < ctx->n_neuron; ++j)
+            for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) base[i] = ctx->h_neuron_start[j];
+        cudaMemcpyAsync(d_base.ptr, base.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    rows_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
         n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), d_cnt.as<int64_t>());
     std::vector<int64_t> cnt(n), brow(n + 1, 0);
     cudaMemcpyAsync(cnt.data(), d_cnt.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) { dev_free(d_cnt); dev_free(d_base); return cuda_fail(ctx, e, "batched count"); }
+    if (e != cudaSuccess) { dev_free(d_cnt); dev_free(d_base); return cuda_fail(ctx, e, "row format count"); }
     for (int64_t i = 0; i < n; ++i) brow[i + 1] = brow[i] + cnt[i];
     const int64_t nb = brow[n];
-    size_t rs = (size_t)ctx->precision;
+    const size_t rs = (size_t)ctx->precision;
+    DevBuf& R = wide ? ctx->w_rowptr : ctx->b_rowptr;
+    DevBuf& C = wide ? ctx->w_col : ctx->b_col;
+    DevBuf& V = wide ? ctx->w_val : ctx->b_val;
+    DevBuf& L = wide ? ctx->w_leak : ctx->b_leak;
     do {
-        if ((rc = dev_alloc(ctx, ctx->b_rowptr, 8 * (n + 1))) != NW_OK) break;
-        if ((rc = dev_alloc(ctx, ctx->b_col, 2 * std::max<int64_t>(nb, 4))) != NW_OK) break;
-        if ((rc = dev_alloc(ctx, ctx->b_val, rs * std::max<int64_t>(nb, 4))) != NW_OK) break;
-        if ((rc = dev_alloc(ctx, ctx->b_leak, rs * n)) != NW_OK) break;
-        cudaMemcpyAsync(ctx->b_rowptr.ptr, brow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        if ((rc = dev_alloc(ctx, R, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, C, sizeof(CT) * std::max<int64_t>(nb, 8))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, V, rs * std::max<int64_t>(nb, 8))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, L, rs * n)) != NW_OK) break;
+        cudaMemcpyAsync(R.ptr, brow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
         const unsigned blocks = (unsigned)((n * 32 + 255) / 256);
+        const int64_t* base = wide ? nullptr : d_base.as<int64_t>();
         if (ctx->precision == NW_F64)
-            batched_fill_kernel<double><<<blocks, 256, 0, ctx->stream>>>(
-                n, d_base.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
-                ctx->p_val.as<double>(), ctx->b_rowptr.as<int64_t>(), ctx->b_col.as<uint16_t>(),
-                ctx->b_val.as<double>(), ctx->b_leak.as<double>());
+            rows_fill_kernel<double, CT><<<blocks, 256, 0, ctx->stream>>>(
+                n, base, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
+                R.as<int64_t>(), C.as<CT>(), V.as<double>(), L.as<double>());
         else
-            batched_fill_kernel<float><<<blocks, 256, 0, ctx->stream>>>(
-                n, d_base.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
-                ctx->p_val.as<double>(), ctx->b_rowptr.as<int64_t>(), ctx->b_col.as<uint16_t>(),
-                ctx->b_val.as<float>(), ctx->b_leak.as<float>());
+            rows_fill_kernel<float, CT><<<blocks, 256, 0, ctx->stream>>>(
+                n, base, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
+                R.as<int64_t>(), C.as<CT>(), V.as<float>(), L.as<float>());
         e = cudaStreamSynchronize(ctx->stream);
-        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "batched fill"); break; }
-        ctx->nnz_b = nb;
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "row format fill"); break; }
+        if (wide) { ctx->nnz_w = nb; ctx->w_ok = true; }
+        else { ctx->nnz_b = nb; ctx->b_ok = true; }
     } while (0);
     dev_free(d_cnt);
     dev_free(d_base);
     return rc;
+}
+
+// Called whenever the FP64 propagator changes: rebuilds the batched format (if
+// every neuron fits its 16-bit columns) and drops the wide one until next used.
+int propagator_to_batched(nw_ctx* ctx) {
+    free_wide(ctx);
+    for (DevBuf* b : {&ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak}) dev_free(*b);
+    ctx->b_ok = false;
+    ctx->nnz_b = 0;
+    if (ctx->max_neuron > 65535) return NW_OK;
+    return propagator_to_rows<uint16_t>(ctx, false);
+}
+
+int ensure_wide(nw_ctx* ctx) {
+    if (ctx->w_ok) return NW_OK;
+    return propagator_to_rows<int32_t>(ctx, true);
 }
 
 }  // namespace nw

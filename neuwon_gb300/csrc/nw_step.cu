@@ -484,6 +484,8 @@ bool uses_bulk_pipeline(nw_ctx* ctx) {
 
 template <typename real>
 static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
+    if (!ctx->b_ok)
+        return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron has more than 65,535 segments (use the wide path)");
     if constexpr (std::is_same<real, float>::value) {
         if (uses_bulk_pipeline(ctx)) return config_batched_lpr<float, 32, true>(ctx, c);
     }

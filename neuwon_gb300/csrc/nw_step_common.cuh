@@ -87,6 +87,8 @@ struct StepArgs {
     const int64_t* rowptr; const uint16_t* col; const real* val; const real* leak;
     // plain propagator
     const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
+    // wide propagator (global int32 columns)
+    const int64_t* wrow; const int32_t* wcol; const real* wval; const real* wleak;
     // hh
     int hh_on, hh_identity;
     const uint32_t* hh_seg_ptr; const int64_t* hh_neuron_ptr; const uint32_t* hh_seg;
@@ -107,7 +109,8 @@ struct StepArgs {
     int32_t* syn_pulse_end; uint32_t* syn_events; int32_t* syn_last; const real* syn_mats;
     uint32_t* syn_ring;
     real syn_e, syn_mg357;
-    // clamps
+    // clamps (sorted by segment)
+    const uint32_t* clamp_seg_ptr;
     const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
     const int64_t* clamp_first; const int64_t* clamp_count;
     // detectors
@@ -423,6 +426,8 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.val = ctx->b_val.as<real>(); a.leak = ctx->b_leak.as<real>();
     a.prow = ctx->p_rowptr.as<int64_t>(); a.pcol = ctx->p_col.as<int32_t>(); a.pval = ctx->p_val.as<double>();
     a.px = ctx->plain_x.as<real>();
+    a.wrow = ctx->w_rowptr.as<int64_t>(); a.wcol = ctx->w_col.as<int32_t>();
+    a.wval = ctx->w_val.as<real>(); a.wleak = ctx->w_leak.as<real>();
     const HHState& hh = ctx->hh;
     a.hh_on = hh.m > 0 ? 1 : 0;
     a.hh_identity = hh.identity ? 1 : 0;
@@ -458,6 +463,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.dtq10 = (real)(ctx->time_step * q10);
     if (ctx->n_clamps) {
         a.clamp_neuron_ptr = ctx->clamp_neuron_ptr.as<int32_t>();
+        a.clamp_seg_ptr = ctx->clamp_seg_ptr.as<uint32_t>();
         a.clamp_seg = ctx->clamp_seg.as<uint32_t>(); a.clamp_amp = ctx->clamp_amp.as<real>();
         a.clamp_first = ctx->clamp_first.as<int64_t>(); a.clamp_count = ctx->clamp_count.as<int64_t>();
     }

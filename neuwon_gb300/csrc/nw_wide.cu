@@ -1,0 +1,262 @@
+// Wide path: the staggered step (neuwon/rxd/rxd_model.py:63-80) as whole-model
+// launches, one per phase, so a neuron of any size spreads over every SM.
+//
+//   membrane x (all segments) -> propagator rows (all rows, x from L2) ->
+//   mechanisms (HH, kinetic, synapses; first half only) -> ... -> AP detector
+//
+// The propagator is the same difference form as the batched path with global
+// int32 columns.  Launch sequences of up to kWideGraphSteps steps are captured
+// as CUDA graphs; the step offset within the sequence is a launch argument and
+// the clock is the device word written before each replay.
+#include <algorithm>
+#include <cstring>
+
+#include "nw_step_common.cuh"
+
+namespace nw {
+
+constexpr int kWideGraphSteps = 32;
+constexpr int kWideThreads = 256;
+
+template <typename real>
+__global__ void __launch_bounds__(kWideThreads)
+wide_membrane_kernel(const StepArgs<real> a, const int s_off, const int half, const int last) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= a.neuron_start[a.n_neuron]) return;
+    const int64_t tick = a.clk->input_ticks + 2 * (int64_t)s_off + half + 1;
+    const bool gv = s_off > 0 || half > 0 || a.clk->g_valid != 0;
+    real G = real(0), GE = real(0);
+    if (gv) segment_conductance(a, i, G, GE);
+    real I = a.has_nonspec ? a.Inonspec[i] : real(0);
+    if (a.clamp_seg_ptr) {
+        for (uint32_t c = a.clamp_seg_ptr[i]; c < a.clamp_seg_ptr[i + 1]; ++c)
+            if (tick >= a.clamp_first[c] && tick < a.clamp_first[c] + a.clamp_count[c]) I += a.clamp_amp[c];
+    }
+    a.px[i] = membrane_x(a, i, G, GE, I, last != 0);
+}
+
+// V_i = x_i - leak_i x_i + sum_j P_ij (x_j - x_i), LPR lanes per row, 4-entry
+// vectors with the evict-first hint, Kahan-compensated lane sums.
+template <typename real, int LPR>
+__global__ void __launch_bounds__(kWideThreads)
+wide_rows_kernel(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                 const real* __restrict__ val, const real* __restrict__ leak, const real* __restrict__ x,
+                 real* __restrict__ y, const int64_t n, int* status) {
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPR;
+    const int l = threadIdx.x % LPR;
+    const bool valid = g < n;
+    real s = real(0), c = real(0), xi = real(0);
+    if (valid) {
+        xi = __ldg(x + g);
+        const int64_t beg = rowptr[g], end = rowptr[g + 1];
+        for (int64_t k = beg + 4 * l; k < end; k += 4 * LPR) {
+            real v[4];
+            Vec4Loader<real>::load(val + k, v);
+            const int4 cc = __ldcs(reinterpret_cast<const int4*>(col + k));
+            const real p = v[0] * (__ldg(x + cc.x) - xi) + v[1] * (__ldg(x + cc.y) - xi);
+            const real q = v[2] * (__ldg(x + cc.z) - xi) + v[3] * (__ldg(x + cc.w) - xi);
+            kahan_add(s, c, p + q);
+        }
+    }
+    real t = s - c;
+#pragma unroll
+    for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off, LPR);
+    if (valid && l == 0) {
+        const real vnew = (xi - leak[g] * xi) + t;
+        if (!isfinite(vnew)) atomicOr(status, kStatusNonFinite);
+        y[g] = vnew;
+    }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(kWideThreads)
+wide_mechanism_kernel(const StepArgs<real> a, const int s_off, const int64_t n_hh, const int64_t n_kin,
+                      const int64_t n_syn) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < n_hh) {
+        const real v = a.V[a.hh_identity ? k : (int64_t)a.hh_seg[k]];
+        real m = a.gm[k], h = a.gh[k], nn = a.gn[k];
+        hh_gates(v, a.dtq10, m, h, nn);
+        a.gm[k] = m; a.gh[k] = h; a.gn[k] = nn;
+        return;
+    }
+    k -= n_hh;
+    if (k < n_kin) {
+        kinetic_step(a, k, a.V[a.kin_identity ? k : (int64_t)a.kin_seg[k]]);
+        return;
+    }
+    k -= n_kin;
+    if (k < n_syn) synapse_step(a, k, a.clk->steps + s_off);
+}
+
+template <typename real>
+__global__ void wide_detect_kernel(const StepArgs<real> a, const int s_off) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t s_abs = a.clk->steps + s_off;
+    if (j < a.n_neuron && a.has_det) {
+        const bool over = a.V[a.det_seg[j]] >= a.det_thr[j];
+        const bool det = over && !a.ap_state[j];
+        a.ap_detected[j] = det;
+        a.ap_state[j] = over;
+        a.spike_count[j] += det ? 1u : 0u;
+        if (a.syn_on) spike_ring_write(a, j, s_abs, det);
+    }
+    if (j < a.n_probes)
+        a.trace[(a.clk->probe_len + s_off) * a.n_probes + a.probe_slot[j]] = a.V[a.probe_seg[j]];
+}
+
+// ------------------------------------------------------------ host side
+
+static int wide_lanes(nw_ctx* ctx) {
+    if (ctx->lanes_per_row) return ctx->lanes_per_row;
+    const double avg = ctx->n_seg ? (double)ctx->nnz_w / (double)ctx->n_seg : 0.0;
+    if (avg >= 48) return 16;
+    if (avg >= 20) return 8;
+    return 4;
+}
+
+template <typename real>
+static int launch_rows(nw_ctx* ctx, int lanes, const StepArgs<real>& a) {
+    const int64_t n = ctx->n_seg;
+    const unsigned blocks = (unsigned)((n * lanes + kWideThreads - 1) / kWideThreads);
+    const int64_t* R = ctx->w_rowptr.as<int64_t>();
+    const int32_t* C = ctx->w_col.as<int32_t>();
+    const real* V = ctx->w_val.as<real>();
+    const real* L = ctx->w_leak.as<real>();
+    switch (lanes) {
+        case 4: wide_rows_kernel<real, 4><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
+        case 8: wide_rows_kernel<real, 8><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
+        case 16: wide_rows_kernel<real, 16><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
+        default: wide_rows_kernel<real, 32><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
+    }
+    NW_CUDA(ctx, cudaGetLastError());
+    return NW_OK;
+}
+
+// The launches of `steps` steps (no host synchronisation: also a graph body).
+template <typename real>
+static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lanes) {
+    const int64_t n = ctx->n_seg;
+    const unsigned seg_blocks = (unsigned)((n + kWideThreads - 1) / kWideThreads);
+    const int64_t n_hh = ctx->hh.m, n_kin = ctx->kin.m, n_syn = ctx->syn.n;
+    const int64_t n_mech = n_hh + n_kin + n_syn;
+    const int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
+    for (int s = 0; s < steps; ++s) {
+        for (int half = 0; half < 2; ++half) {
+            const int last = (s == steps - 1 && half == 1) ? 1 : 0;
+            wide_membrane_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a, s, half, last);
+            NW_CUDA(ctx, cudaGetLastError());
+            NW_CHECK(launch_rows<real>(ctx, lanes, a));
+            if (half == 0 && n_mech > 0) {
+                wide_mechanism_kernel<real><<<(unsigned)((n_mech + kWideThreads - 1) / kWideThreads), kWideThreads, 0,
+                                              ctx->stream>>>(a, s, n_hh, n_kin, n_syn);
+                NW_CUDA(ctx, cudaGetLastError());
+            }
+        }
+        wide_detect_kernel<real><<<(unsigned)((cover + 127) / 128), 128, 0, ctx->stream>>>(a, s);
+        NW_CUDA(ctx, cudaGetLastError());
+    }
+    return NW_OK;
+}
+
+__global__ void wide_set_clock_kernel(DevClock* d, DevClock v) { *d = v; }
+
+static int push_clock_wide(nw_ctx* ctx) {
+    DevClock v;
+    memset(&v, 0, sizeof(v));
+    v.input_ticks = ctx->input_ticks;
+    v.steps = ctx->steps;
+    v.probe_len = ctx->probe_len;
+    v.g_valid = ctx->g_valid ? 1 : 0;
+    wide_set_clock_kernel<<<1, 1, 0, ctx->stream>>>(ctx->dclock.as<DevClock>(), v);
+    NW_CUDA(ctx, cudaGetLastError());
+    return NW_OK;
+}
+
+static void key_bytes(std::vector<unsigned char>& key, const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    key.insert(key.end(), b, b + n);
+}
+
+// Replays (capturing on first use) the graph of `steps` wide steps.
+template <typename real>
+static int wide_graph(nw_ctx* ctx, const StepArgs<real>& a0, int steps, int lanes) {
+    std::vector<unsigned char> key;
+    StepArgs<real> ka = a0;
+    ka.tick0 = 0; ka.g_valid = 0; ka.trace_row0 = 0; ka.k_steps = 0;
+    const int tag = 0x57494445;   // distinguishes wide-path entries in the shared cache
+    key_bytes(key, &tag, sizeof(tag));
+    key_bytes(key, &ka, sizeof(ka));
+    key_bytes(key, &steps, sizeof(steps));
+    key_bytes(key, &lanes, sizeof(lanes));
+    key_bytes(key, &ctx->n_seg, sizeof(ctx->n_seg));
+    key_bytes(key, &ctx->hh.m, sizeof(ctx->hh.m));
+    key_bytes(key, &ctx->kin.m, sizeof(ctx->kin.m));
+    key_bytes(key, &ctx->syn.n, sizeof(ctx->syn.n));
+    for (auto& g : ctx->graphs) {
+        if (g.key == key) {
+            g.last_use = ++ctx->graph_uses;
+            NW_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+            ctx->graph_replays++;
+            return NW_OK;
+        }
+    }
+    if (ctx->graphs.size() >= 8) {
+        size_t lru = 0;
+        for (size_t i = 1; i < ctx->graphs.size(); ++i)
+            if (ctx->graphs[i].last_use < ctx->graphs[lru].last_use) lru = i;
+        cudaGraphExecDestroy(ctx->graphs[lru].exec);
+        cudaGraphDestroy(ctx->graphs[lru].graph);
+        ctx->graphs.erase(ctx->graphs.begin() + lru);
+    }
+    GraphEntry e;
+    e.key = std::move(key);
+    NW_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_wide<real>(ctx, a0, steps, lanes);
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &e.graph);
+    if (rc != NW_OK) {
+        if (e.graph) cudaGraphDestroy(e.graph);
+        return rc;
+    }
+    NW_CUDA(ctx, ce);
+    const cudaError_t ie = cudaGraphInstantiate(&e.exec, e.graph, 0);
+    if (ie != cudaSuccess) {
+        cudaGraphDestroy(e.graph);
+        return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+    }
+    e.last_use = ++ctx->graph_uses;
+    ctx->graph_captures++;
+    ctx->graphs.push_back(std::move(e));
+    NW_CUDA(ctx, cudaGraphLaunch(ctx->graphs.back().exec, ctx->stream));
+    ctx->graph_replays++;
+    return NW_OK;
+}
+
+template <typename real>
+static int wide_steps(nw_ctx* ctx, int k_steps) {
+    NW_CHECK(ensure_wide(ctx));
+    const int lanes = wide_lanes(ctx);
+    // Every phase is its own launch, so a spike written by one step's detector
+    // launch is visible to every later mechanism launch: no cap by the delays.
+    const int G = kWideGraphSteps;
+    int done = 0;
+    while (done < k_steps) {
+        const int steps = std::min(G, k_steps - done);
+        const StepArgs<real> a = make_args<real>(ctx, steps);
+        NW_CHECK(push_clock_wide(ctx));
+        if (ctx->use_graph) NW_CHECK(wide_graph<real>(ctx, a, steps, lanes));
+        else NW_CHECK(enqueue_wide<real>(ctx, a, steps, lanes));
+        ctx->input_ticks += 2 * (int64_t)steps;
+        ctx->steps += steps;
+        if (ctx->n_probes) ctx->probe_len += steps;
+        if (ctx->hh.m > 0 || ctx->kin.m > 0) ctx->g_valid = true;
+        done += steps;
+    }
+    return NW_OK;
+}
+
+int advance_wide(nw_ctx* ctx, int k_steps) {
+    return ctx->precision == NW_F64 ? wide_steps<double>(ctx, k_steps) : wide_steps<float>(ctx, k_steps);
+}
+
+}  // namespace nw

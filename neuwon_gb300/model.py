@@ -260,7 +260,9 @@ class RxD_Model:
       propagator_tolerance  prune |P_ij| below this (reference: machine epsilon)
       propagator_conserve   return the pruned mass of each row to its diagonal
                             (charge-conserving pruning; the reference does not)
-      path                  'batched' (fused persistent kernel) or 'plain'
+      path                  'batched' (fused persistent kernel, one CTA per neuron),
+                            'wide' (whole-model launches per phase: neurons of any
+                            size) or 'plain' (per-neuron launches)
     """
 
     def __init__(self, time_step=0.1, *, temperature=37, initial_voltage=-70,
@@ -280,7 +282,7 @@ class RxD_Model:
         self.device = int(device)
         self.propagator_tolerance = float(propagator_tolerance)
         self.propagator_conserve = bool(propagator_conserve)
-        self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN}[path]
+        self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN, "wide": _lib.PATH_WIDE}[path]
         self.input_hook = Clock(0.5 * self.time_step, units="ms")
         self.advance_hook = self.clock = Clock(self.time_step, units="ms")
         # Segment table (creation order).

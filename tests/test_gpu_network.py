@@ -39,8 +39,9 @@ def _run_recording(m, steps):
     return spikes
 
 
-def test_f64_network_matches_oracle():
-    m, om, net, offs = network_case([150, 90, 200, 60], 300, seed=2, delay_lo=1.0, delay_hi=4.0)
+@pytest.mark.parametrize("path", ["batched", "wide"])
+def test_f64_network_matches_oracle(path):
+    m, om, net, offs = network_case([150, 90, 200, 60], 300, seed=2, delay_lo=1.0, delay_hi=4.0, path=path)
     steps = 400
     spikes = []
     worst = 0.0

@@ -84,7 +84,7 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-@pytest.mark.parametrize("path", ["batched", "plain"])
+@pytest.mark.parametrize("path", ["batched", "plain", "wide"])
 def test_f64_paths_match_reference_fixture(name, path):
     """The reference's own recorded voltages, reproduced by the FP64 GPU paths."""
     trees, clamps, hh_kw, as_created = CASES[name]
@@ -146,12 +146,14 @@ def test_f32_batched_single_neuron_config_short():
     assert worst < 0.1, worst
 
 
-@pytest.mark.parametrize("precision,tol,conserve,bound", [
-    ("f64", EPSILON, False, 1e-6),
-    ("f32", EPSILON, False, 0.1),
-    ("f32", 1e-8, True, 0.1),
+@pytest.mark.parametrize("precision,tol,conserve,bound,path", [
+    ("f64", EPSILON, False, 1e-6, "batched"),
+    ("f32", EPSILON, False, 0.1, "batched"),
+    ("f32", 1e-8, True, 0.1, "batched"),
+    ("f64", EPSILON, False, 1e-6, "wide"),
+    ("f32", 1e-8, True, 0.1, "wide"),
 ])
-def test_single_neuron_config_matches_reference(precision, tol, conserve, bound):
+def test_single_neuron_config_matches_reference(precision, tol, conserve, bound, path):
     """The single-neuron configuration at full size and length (2,000 segments, HH,
     0.2 nA soma clamp 5-80 ms, dt 0.1 ms for 100 ms): every segment's voltage every
     10 ms and the probed traces every step against the reference's own run; equal
@@ -160,7 +162,7 @@ def test_single_neuron_config_matches_reference(precision, tol, conserve, bound)
     probes = list(F["c1_probes"])
     m, neurons, offs, recs = gpu_model([random_tree(2000, seed=0)], clamps,
                                        hh_kw=dict(ena=50.0, ek=-77.0, el=-54.3), precision=precision,
-                                       tolerance=tol, conserve=conserve, probes=probes)
+                                       tolerance=tol, conserve=conserve, probes=probes, path=path)
     worst = 0.0
     for k in range(1000):
         for (ti, s, nA, start, dur) in clamps:
@@ -259,7 +261,7 @@ def test_bad_propagator_rejected():
         ctx.call("nw_propagator_set_csr", n, _lib.ptr(rowptr), _lib.ptr(col), _lib.ptr(val), n)
 
 
-@pytest.mark.parametrize("path", ["batched", "plain"])
+@pytest.mark.parametrize("path", ["batched", "plain", "wide"])
 def test_f64_hh_plus_na8_kinetic_matches_oracle(path):
     """HH + the 8-state Markov sodium scheme (voltage-table LTI step) vs the oracle."""
     trees = [random_tree(150, seed=31), random_tree(90, seed=32)]
