@@ -313,8 +313,10 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
                                              " must be an earlier segment of the same neuron");
         }
     }
-    if (maxn > 65535)
-        return fail(ctx, NW_ERR_LIMIT, "nw_model_init: neurons larger than 65535 segments are not supported");
+    // Propagator columns are 32-bit segment indices (the batched path's are
+    // 16-bit within a neuron: larger neurons run on the wide path).
+    if (num_segments >= INT32_MAX)
+        return fail(ctx, NW_ERR_LIMIT, "nw_model_init: at most 2^31 - 2 segments");
     ctx->n_seg = num_segments;
     ctx->n_neuron = num_neurons;
     ctx->max_neuron = maxn;
