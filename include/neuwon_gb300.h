@@ -143,6 +143,37 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
                         double erev, const double* table, int num_buckets, int num_terms,
                         double vmin, double bucket_frq, double conserve_sum, const double* init_state);
 
+/* ---- intracellular calcium ----------------------------------------- */
+
+/* One diffusing intracellular species (calcium), as neuwon/rxd/species.py advances
+ * one (_SpeciesInstance._advance, species.py:56-70): after each electric half step,
+ * c <- max(0, c + dc/dt * dt/2), then c <- M c with M = expm of the diffusion operator
+ * over dt/2.  The reference's builder of M (_compute_matrix, species.py:74-83) is
+ * unfinished; here M comes from the same tree builder as the electric propagator:
+ * d c_i / dt = D A_i / (L_i vol_i) (c_parent - c_i) through segment i's own cross
+ * section A_i and length L_i (D in um^2/ms, um, um^3), pruned at prune_tolerance
+ * (conserve != 0: pruned mass returned to the diagonal).  Starts at initial_mM
+ * everywhere with dc/dt = 0.  "Species.ca" (mM) and "Species.ca_derivative" read and
+ * write through nw_calcium_data. */
+int nw_calcium_set(nw_ctx* ctx, double diffusivity, const double* cross_area_um2,
+                   const double* length_um, const double* volume_um3, double initial_mM,
+                   double prune_tolerance, int conserve, int64_t* nnz_out);
+
+/* Calcium mechanisms, run in the mechanism phase after the others (no counterpart in
+ * the reference library): dc_i/dt = -influx_coef_i * I_Na,i - efflux_coef_i * E1Ca_i,
+ * I_Na the segment's HH sodium current (A) and E1Ca the bound state of a 3-state pump
+ * (E1, E1Ca, E2) on every segment.  The pump advances one step at the present c by a
+ * table in lti_sim's layout [bucket][col][row][term] over a logarithmic input
+ * (neuwon/rxd/lti_sim/inputs.py:85-109: location = (log2(c + scale) - log2_min) *
+ * bucket_frq), then is renormalised to sum 1.  table may be NULL: influx only. */
+int nw_calcium_pump_set(nw_ctx* ctx, const double* influx_coef, const double* efflux_coef,
+                        const double* table, int32_t num_buckets, int32_t num_terms, double log2_min,
+                        double bucket_frq, double scale, const double* initial_state);
+
+/* Read (write = 0) or write "Species.ca", "Species.ca_derivative" (n_seg values) or
+ * "CaPump.state" (3 * n_seg, state-major) in device order and the given dtype. */
+int nw_calcium_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t count, int write);
+
 /* ---- synapses and spike events ------------------------------------ */
 
 /* No counterpart in the reference: its neuwon/rxd/synapses.py grows synapse

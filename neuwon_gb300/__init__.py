@@ -8,8 +8,10 @@ from .kinetic import Kinetic, KineticScheme, LTITable, na8
 from .mechanisms import HH, Mechanism, NMODL
 from .model import Clock, Model, Neuron, RxD_Model, Segment, TimeSeries
 from .morphology import EPSILON, Tree, geometry, neuron_sizes, passive_electric, random_tree
+from .species import Calcium
+from .synapses import SynapseKinetics
 
 __all__ = ["Kinetic", "KineticScheme", "LTITable", "na8", "HH", "Mechanism", "NMODL", "Clock", "Model", "Neuron", "RxD_Model", "Segment",
            "TimeSeries", "EPSILON", "Tree", "geometry", "neuron_sizes", "passive_electric",
-           "random_tree"]
+           "random_tree", "Calcium", "SynapseKinetics"]
 __version__ = "0.1.0"

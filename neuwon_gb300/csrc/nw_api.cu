@@ -255,6 +255,7 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     free_hh(ctx->hh);
     free_kin(ctx->kin);
     free_syn(ctx->syn);
+    free_calcium(ctx->ca);
     free_adj(ctx->adj);
     DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec,
                       &ctx->kI, &ctx->kG, &ctx->cap64, &ctx->res64, &ctx->p_rowptr, &ctx->p_col,
@@ -338,6 +339,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     free_hh(ctx->hh);
     free_kin(ctx->kin);
     free_syn(ctx->syn);
+    free_calcium(ctx->ca);
     free_adj(ctx->adj);
     size_t rs = (size_t)ctx->precision;
     NW_CHECK(dev_alloc(ctx, ctx->neuron_start, 8 * (num_neurons + 1)));

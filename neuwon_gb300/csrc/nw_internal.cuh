@@ -99,6 +99,28 @@ struct SynState {
     std::vector<int64_t> h_neuron_ptr;
 };
 
+// Intracellular calcium (one diffusing species): concentration per segment,
+// its diffusion propagator (same tree builder, same row formats as the
+// electric one), a 3-state pump on every segment advanced through a table over
+// log2(c + scale), and an influx that is a fraction of the segment's HH sodium
+// current.
+struct CalciumState {
+    bool on = false, pump = false;
+    double D = 0, c0 = 0;
+    int64_t nnz64 = 0, nnz_b = 0, nnz_w = 0;
+    bool b_ok = false, w_ok = false;
+    DevBuf res, vol;                            // f64 [n_seg]: 1e-3 L / (D A) and volume (um3)
+    DevBuf p_rowptr, p_col, p_val;              // FP64 CSR
+    DevBuf b_rowptr, b_col, b_val, b_leak;      // batched format
+    DevBuf w_rowptr, w_col, w_val, w_leak;      // wide format
+    DevBuf c, dcdt, scratch;                    // real [n_seg]: mM, mM/ms, wide-path scratch
+    DevBuf influx, efflux;                      // real [n_seg]: mM/ms per A of Na current, per bound pump fraction
+    DevBuf state;                               // real [3][n_seg] pump states (E1, E1Ca, E2)
+    DevBuf table;                               // real [nb][3][3][T] ([bucket][col][row][term])
+    int nb = 0, T = 0;
+    double log2_min = 0, frq = 0, scale = 0;
+};
+
 struct AdjointState {
     bool ready = false, g_valid0 = false;
     int K = 0;
@@ -146,6 +168,7 @@ struct nw_ctx {
     nw::HHState hh;
     nw::KineticState kin;
     nw::SynState syn;
+    nw::CalciumState ca;
     nw::AdjointState adj;
     bool g_valid = false;       // conductances computed by a mechanism step
 
@@ -197,6 +220,12 @@ int propagator_from_host(nw_ctx* ctx, const int64_t* rowptr, const int64_t* col,
                          const double* val, int64_t nnz);
 int propagator_to_batched(nw_ctx* ctx);
 int propagator_conserve(nw_ctx* ctx);
+int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap, double h_s, double tol,
+                          DevBuf& out_rowptr, DevBuf& out_col, DevBuf& out_val, int64_t* nnz_out);
+int csr_conserve(nw_ctx* ctx, DevBuf& rowptr, DevBuf& col, DevBuf& val);
+template <typename CT>
+int csr_to_rows(nw_ctx* ctx, const DevBuf& src_row, const DevBuf& src_col, const DevBuf& src_val, bool relative,
+                DevBuf& R, DevBuf& C, DevBuf& V, DevBuf& L, int64_t* nnz_out);
 
 // Stepping (nw_step.cu).
 int advance_batched(nw_ctx* ctx, int k_steps);
@@ -208,6 +237,8 @@ int choose_lanes_per_row(nw_ctx* ctx);
 bool uses_bulk_pipeline(nw_ctx* ctx);
 void graphs_clear(nw_ctx* ctx);
 void free_syn(SynState& s);
+void free_calcium(CalciumState& c);
+int calcium_ensure_wide(nw_ctx* ctx);
 int synapse_ring_clear(nw_ctx* ctx);
 int prepare_graph(nw_ctx* ctx, int k_steps);
 int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes, int32_t* threads, int32_t* fusion,

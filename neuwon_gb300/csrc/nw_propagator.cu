@@ -214,7 +214,11 @@ static void contour_nodes(double2* z, double2* w) {
     }
 }
 
-int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
+// expm(A h) of the tree operator with edge "resistances" d_res (child edge) and
+// node "capacities" d_cap (coefficients h_s / (R C), electric.py:85-109 form),
+// pruned at tol, into an FP64 CSR with global int32 columns.
+int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap, double h_s, double tol,
+                          DevBuf& out_rowptr, DevBuf& out_col, DevBuf& out_val, int64_t* nnz_out) {
     const int64_t n = ctx->n_seg, nn = ctx->n_neuron;
     // Children lists and edge conductance sums (host, O(n)).
     std::vector<int64_t> cptr(n + 1, 0), cidx;
@@ -226,7 +230,7 @@ int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
         for (int64_t i = 0; i < n; ++i) if (ctx->h_parent[i] >= 0) cidx[fillp[ctx->h_parent[i]]++] = i;
     }
     std::vector<double> res(n), gsum(n, 0.0);
-    NW_CUDA(ctx, cudaMemcpy(res.data(), ctx->res64.ptr, 8 * n, cudaMemcpyDeviceToHost));
+    NW_CUDA(ctx, cudaMemcpy(res.data(), d_res, 8 * n, cudaMemcpyDeviceToHost));
     for (int64_t c = 0; c < n; ++c) {
         int64_t p = ctx->h_parent[c];
         if (p < 0) continue;
@@ -261,8 +265,8 @@ int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
         a.neuron_start = ctx->neuron_start.as<int64_t>();
         a.parent = ctx->parent.as<int64_t>();
         a.child_ptr = d_cptr.as<int64_t>(); a.child_idx = d_cidx.as<int64_t>();
-        a.cap = ctx->cap64.as<double>(); a.res = ctx->res64.as<double>(); a.gsum = d_gsum.as<double>();
-        a.h_s = 0.5 * ctx->time_step * 1e-3;
+        a.cap = d_cap; a.res = d_res; a.gsum = d_gsum.as<double>();
+        a.h_s = h_s;
         a.down = d_down.as<double2>(); a.up = d_up.as<double2>(); a.invT = d_invT.as<double2>();
         a.tol = tol; a.explore = tol * kExploreFactor;
         a.count = d_count.as<int64_t>();
@@ -289,13 +293,13 @@ int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
         std::vector<int64_t> rowptr(n + 1, 0);
         for (int64_t i = 0; i < n; ++i) rowptr[i + 1] = rowptr[i] + cnt[i];
         const int64_t nnz = rowptr[n];
-        if ((rc = dev_alloc(ctx, ctx->p_rowptr, 8 * (n + 1))) != NW_OK) break;
-        if ((rc = dev_alloc(ctx, ctx->p_col, 4 * std::max<int64_t>(nnz, 1))) != NW_OK) break;
-        if ((rc = dev_alloc(ctx, ctx->p_val, 8 * std::max<int64_t>(nnz, 1))) != NW_OK) break;
-        cudaMemcpyAsync(ctx->p_rowptr.ptr, rowptr.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
-        a.rowptr = ctx->p_rowptr.as<int64_t>();
-        a.out_col = ctx->p_col.as<int32_t>();
-        a.out_val = ctx->p_val.as<double>();
+        if ((rc = dev_alloc(ctx, out_rowptr, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, out_col, 4 * std::max<int64_t>(nnz, 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, out_val, 8 * std::max<int64_t>(nnz, 1))) != NW_OK) break;
+        cudaMemcpyAsync(out_rowptr.ptr, rowptr.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        a.rowptr = out_rowptr.as<int64_t>();
+        a.out_col = out_col.as<int32_t>();
+        a.out_val = out_val.as<double>();
         propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 1);
         cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream);
         e = cudaStreamSynchronize(ctx->stream);
@@ -305,11 +309,19 @@ int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
             rc = fail(ctx, NW_ERR_STATE, "propagator build: count and fill passes disagree");
             break;
         }
-        ctx->nnz64 = nnz;
         if (nnz_out) *nnz_out = nnz;
     } while (0);
     cleanup();
     return rc;
+}
+
+int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
+    int64_t nnz = 0;
+    NW_CHECK(tree_propagator_build(ctx, ctx->res64.as<double>(), ctx->cap64.as<double>(),
+                                   0.5 * ctx->time_step * 1e-3, tol, ctx->p_rowptr, ctx->p_col, ctx->p_val, &nnz));
+    ctx->nnz64 = nnz;
+    if (nnz_out) *nnz_out = nnz;
+    return NW_OK;
 }
 
 int propagator_from_host(nw_ctx* ctx, const int64_t* rowptr, const int64_t* col, const double* val,
@@ -354,11 +366,11 @@ __global__ void conserve_rows_kernel(int64_t n, const int64_t* prow, const int32
     if (lane == __ffs(has) - 1) pval[diag] += 1.0 - sum;
 }
 
-int propagator_conserve(nw_ctx* ctx) {
+int csr_conserve(nw_ctx* ctx, DevBuf& rowptr, DevBuf& col, DevBuf& val) {
     const int64_t n = ctx->n_seg;
     cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
     conserve_rows_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(
-        n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(), ctx->status.as<int>());
+        n, rowptr.as<int64_t>(), col.as<int32_t>(), val.as<double>(), ctx->status.as<int>());
     int st = 0;
     NW_CUDA(ctx, cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
     NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -368,6 +380,8 @@ int propagator_conserve(nw_ctx* ctx) {
     }
     return NW_OK;
 }
+
+int propagator_conserve(nw_ctx* ctx) { return csr_conserve(ctx, ctx->p_rowptr, ctx->p_col, ctx->p_val); }
 
 // ------------------------------------------------- batched difference form
 
@@ -417,15 +431,16 @@ void free_wide(nw_ctx* ctx) {
     ctx->nnz_w = 0;
 }
 
-// Builds one row format from the FP64 CSR: relative u16 columns into the b_*
-// buffers (wide = false) or global i32 columns into the w_* buffers.
+// One row format from an FP64 CSR (src_*): columns relative to the row's
+// neuron (u16, batched format) or global (i32, wide format).
 template <typename CT>
-static int propagator_to_rows(nw_ctx* ctx, bool wide) {
+int csr_to_rows(nw_ctx* ctx, const DevBuf& src_row, const DevBuf& src_col, const DevBuf& src_val, bool relative,
+                DevBuf& R, DevBuf& C, DevBuf& V, DevBuf& L, int64_t* nnz_out) {
     const int64_t n = ctx->n_seg;
     DevBuf d_cnt, d_base;
     NW_CHECK(dev_alloc(ctx, d_cnt, 8 * n));
     int rc = NW_OK;
-    if (!wide) {
+    if (relative) {
         rc = dev_alloc(ctx, d_base, 8 * n);
         if (rc != NW_OK) { dev_free(d_cnt); return rc; }
         std::vector<int64_t> base(n);
@@ -435,7 +450,7 @@ static int propagator_to_rows(nw_ctx* ctx, bool wide) {
         cudaStreamSynchronize(ctx->stream);
     }
     rows_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
-        n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), d_cnt.as<int64_t>());
+        n, src_row.as<int64_t>(), src_col.as<int32_t>(), d_cnt.as<int64_t>());
     std::vector<int64_t> cnt(n), brow(n + 1, 0);
     cudaMemcpyAsync(cnt.data(), d_cnt.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -443,10 +458,6 @@ static int propagator_to_rows(nw_ctx* ctx, bool wide) {
     for (int64_t i = 0; i < n; ++i) brow[i + 1] = brow[i] + cnt[i];
     const int64_t nb = brow[n];
     const size_t rs = (size_t)ctx->precision;
-    DevBuf& R = wide ? ctx->w_rowptr : ctx->b_rowptr;
-    DevBuf& C = wide ? ctx->w_col : ctx->b_col;
-    DevBuf& V = wide ? ctx->w_val : ctx->b_val;
-    DevBuf& L = wide ? ctx->w_leak : ctx->b_leak;
     do {
         if ((rc = dev_alloc(ctx, R, 8 * (n + 1))) != NW_OK) break;
         if ((rc = dev_alloc(ctx, C, sizeof(CT) * std::max<int64_t>(nb, 8))) != NW_OK) break;
@@ -454,24 +465,27 @@ static int propagator_to_rows(nw_ctx* ctx, bool wide) {
         if ((rc = dev_alloc(ctx, L, rs * n)) != NW_OK) break;
         cudaMemcpyAsync(R.ptr, brow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
         const unsigned blocks = (unsigned)((n * 32 + 255) / 256);
-        const int64_t* base = wide ? nullptr : d_base.as<int64_t>();
+        const int64_t* base = relative ? d_base.as<int64_t>() : nullptr;
         if (ctx->precision == NW_F64)
             rows_fill_kernel<double, CT><<<blocks, 256, 0, ctx->stream>>>(
-                n, base, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
+                n, base, src_row.as<int64_t>(), src_col.as<int32_t>(), src_val.as<double>(),
                 R.as<int64_t>(), C.as<CT>(), V.as<double>(), L.as<double>());
         else
             rows_fill_kernel<float, CT><<<blocks, 256, 0, ctx->stream>>>(
-                n, base, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
+                n, base, src_row.as<int64_t>(), src_col.as<int32_t>(), src_val.as<double>(),
                 R.as<int64_t>(), C.as<CT>(), V.as<float>(), L.as<float>());
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "row format fill"); break; }
-        if (wide) { ctx->nnz_w = nb; ctx->w_ok = true; }
-        else { ctx->nnz_b = nb; ctx->b_ok = true; }
+        if (nnz_out) *nnz_out = nb;
     } while (0);
     dev_free(d_cnt);
     dev_free(d_base);
     return rc;
 }
+template int csr_to_rows<uint16_t>(nw_ctx*, const DevBuf&, const DevBuf&, const DevBuf&, bool, DevBuf&, DevBuf&,
+                                   DevBuf&, DevBuf&, int64_t*);
+template int csr_to_rows<int32_t>(nw_ctx*, const DevBuf&, const DevBuf&, const DevBuf&, bool, DevBuf&, DevBuf&,
+                                  DevBuf&, DevBuf&, int64_t*);
 
 // Called whenever the FP64 propagator changes: rebuilds the batched format (if
 // every neuron fits its 16-bit columns) and drops the wide one until next used.
@@ -481,12 +495,18 @@ int propagator_to_batched(nw_ctx* ctx) {
     ctx->b_ok = false;
     ctx->nnz_b = 0;
     if (ctx->max_neuron > 65535) return NW_OK;
-    return propagator_to_rows<uint16_t>(ctx, false);
+    NW_CHECK(csr_to_rows<uint16_t>(ctx, ctx->p_rowptr, ctx->p_col, ctx->p_val, true, ctx->b_rowptr, ctx->b_col,
+                                   ctx->b_val, ctx->b_leak, &ctx->nnz_b));
+    ctx->b_ok = true;
+    return NW_OK;
 }
 
 int ensure_wide(nw_ctx* ctx) {
     if (ctx->w_ok) return NW_OK;
-    return propagator_to_rows<int32_t>(ctx, true);
+    NW_CHECK(csr_to_rows<int32_t>(ctx, ctx->p_rowptr, ctx->p_col, ctx->p_val, false, ctx->w_rowptr, ctx->w_col,
+                                  ctx->w_val, ctx->w_leak, &ctx->nnz_w));
+    ctx->w_ok = true;
+    return NW_OK;
 }
 
 }  // namespace nw

@@ -323,6 +323,17 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                 else propagate_neuron<real, LPR>(a, base, n, xs);
                 __syncthreads();
                 if (BULK && s_abort) break;
+                if (a.ca_on) {
+                    // species._advance (species.py:56-70): c <- max(0, c + dcdt h), then diffusion.
+                    for (int li = tid; li < n; li += nthr) {
+                        const int64_t i = base + li;
+                        xs[li] = fmax(real(0), a.ca_c[i] + a.ca_dcdt[i] * a.h_ms);
+                    }
+                    __syncthreads();
+                    propagate_rows_of<real, 4>(a.ca_brow, a.ca_bcol, a.ca_bval, a.ca_bleak, base, n, xs,
+                                               [&](int64_t r, int, real, real cnew) { a.ca_c[r] = cnew; });
+                    __syncthreads();
+                }
                 if (half == 0) {
                     // Mechanisms (rxd_model.py:115-123) at the mid-step voltage.
                     if (a.hh_on) {
@@ -339,6 +350,10 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     }
                     for (int64_t k = yb + tid; k < ye; k += nthr) synapse_step(a, k, step_base + s);
                     if (mech_sync) __syncthreads();
+                    if (a.ca_on) {
+                        for (int li = tid; li < n; li += nthr) calcium_mechanisms(a, base + li);
+                        __syncthreads();
+                    }
                 }
             }
             if (BULK && s_abort) break;
@@ -484,7 +499,7 @@ bool uses_bulk_pipeline(nw_ctx* ctx) {
 
 template <typename real>
 static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
-    if (!ctx->b_ok)
+    if (!ctx->b_ok || (ctx->ca.on && !ctx->ca.b_ok))
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron has more than 65,535 segments (use the wide path)");
     if constexpr (std::is_same<real, float>::value) {
         if (uses_bulk_pipeline(ctx)) return config_batched_lpr<float, 32, true>(ctx, c);
@@ -689,6 +704,7 @@ static int plain_steps(nw_ctx* ctx, int k_steps) {
 
 int advance_plain(nw_ctx* ctx, int k_steps) {
     if (ctx->syn.n) return fail(ctx, NW_ERR_STATE, "the plain path has no synapses; use the batched path");
+    if (ctx->ca.on) return fail(ctx, NW_ERR_STATE, "the plain path has no calcium; use the batched or wide path");
     return ctx->precision == NW_F64 ? plain_steps<double>(ctx, k_steps) : plain_steps<float>(ctx, k_steps);
 }
 

@@ -109,6 +109,14 @@ struct StepArgs {
     int32_t* syn_pulse_end; uint32_t* syn_events; int32_t* syn_last; const real* syn_mats;
     uint32_t* syn_ring;
     real syn_e, syn_mg357;
+    // calcium
+    int ca_on, ca_pump, ca_nb, ca_T;
+    real* ca_c; real* ca_dcdt; real* ca_scratch; const real* ca_influx; const real* ca_efflux;
+    real* ca_state; const real* ca_table;
+    const int64_t* ca_brow; const uint16_t* ca_bcol; const real* ca_bval; const real* ca_bleak;
+    const int64_t* ca_wrow; const int32_t* ca_wcol; const real* ca_wval; const real* ca_wleak;
+    int64_t ca_n;
+    real ca_log2min, ca_frq, ca_scale, h_ms;
     // clamps (sorted by segment)
     const uint32_t* clamp_seg_ptr;
     const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
@@ -201,6 +209,60 @@ __device__ __forceinline__ void synapse_step(const StepArgs<real>& a, int64_t k,
     const real c = (real(1) - o) - d;
     a.syn_on_[k] = Mn[3] * c + Mn[4] * o + Mn[5] * d;
     a.syn_od[k] = Mn[6] * c + Mn[7] * o + Mn[8] * d;
+}
+
+template <typename real> __device__ __forceinline__ real d_log2(real x);
+template <> __device__ __forceinline__ float d_log2<float>(float x) { return log2f(x); }
+template <> __device__ __forceinline__ double d_log2<double>(double x) { return log2(x); }
+
+// Calcium of segment i through the mechanism phase: the pump's 3 states advance
+// one step at the present concentration (table over log2(c + scale), bucket and
+// in-bucket location as lti_sim's LogarithmicInput and codegen compute them,
+// neuwon/rxd/lti_sim/inputs.py:85-109, codegen.py:43-106, then renormalised),
+// and the concentration's rate of change for this step: influx = a fraction of
+// the segment's HH sodium current, efflux = transport from the bound state.
+template <typename real>
+__device__ __forceinline__ void calcium_mechanisms(const StepArgs<real>& a, int64_t i) {
+    const real v = a.V[i];
+    real d = real(0);
+    if (a.hh_on) {
+        int64_t b, e;
+        if (a.hh_identity) { b = i; e = i + 1; }
+        else { b = a.hh_seg_ptr[i]; e = a.hh_seg_ptr[i + 1]; }
+        real ina = real(0);
+        for (int64_t k = b; k < e; ++k) {
+            const real m = a.gm[k], h = a.gh[k];
+            ina += a.cna[k] * m * m * m * h * (v - a.ena);
+        }
+        d = -a.ca_influx[i] * ina;
+    }
+    if (a.ca_pump) {
+        const real c = a.ca_c[i];
+        real x = (d_log2(c + a.ca_scale) - a.ca_log2min) * a.ca_frq;
+        int b = (int)x;
+        real loc = x - (real)b;
+        if (b > a.ca_nb - 1) { b = a.ca_nb - 1; loc = real(1); }
+        if (b < 0 || !(x == x)) { b = 0; loc = real(0); }
+        const int T = a.ca_T;
+        const real* tb = a.ca_table + (int64_t)b * 9 * T;
+        const int64_t n = a.ca_n;
+        real st[3] = {a.ca_state[i], a.ca_state[n + i], a.ca_state[2 * n + i]};
+        real out[3] = {real(0), real(0), real(0)};
+        for (int col = 0; col < 3; ++col) {
+            for (int row = 0; row < 3; ++row) {
+                const real* t = tb + (col * 3 + row) * T;
+                real poly = t[T - 1];
+                for (int k = T - 2; k >= 0; --k) poly = poly * loc + t[k];
+                out[row] += poly * st[col];
+            }
+        }
+        const real inv = real(1) / ((out[0] + out[1]) + out[2]);
+        a.ca_state[i] = out[0] * inv;
+        a.ca_state[n + i] = out[1] * inv;
+        a.ca_state[2 * n + i] = out[2] * inv;
+        d -= a.ca_efflux[i] * (out[1] * inv);
+    }
+    a.ca_dcdt[i] = d;
 }
 
 // The AP detector's output for step s_abs into the neuron's spike ring (the
@@ -353,8 +415,9 @@ __device__ __forceinline__ real quad_sum(const real (&v)[4], const ushort4 cc, c
 // Row i of the propagator applied to xs for every row of one neuron; fin(r, row, xi, y)
 // receives y = sum_j P_ij xs_j for the global row r.
 template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
-__device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t base, int n,
-                                               const real* __restrict__ xs, Fin fin) {
+__device__ __forceinline__ void propagate_rows_of(const int64_t* __restrict__ rowptr, const uint16_t* __restrict__ col,
+                                                  const real* __restrict__ val, const real* __restrict__ leak,
+                                                  int64_t base, int n, const real* __restrict__ xs, Fin fin) {
     constexpr int GPW = 32 / LPR;                  // row groups per warp
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -366,7 +429,7 @@ __device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t 
         real s = real(0), c = real(0), xi = real(0);
         if (valid) {
             const int64_t r = base + row;
-            const int64_t beg = a.rowptr[r], end = a.rowptr[r + 1];
+            const int64_t beg = rowptr[r], end = rowptr[r + 1];
             xi = xs[row];
             // UNROLL chunks of 4 entries per lane are loaded before any is consumed,
             // to keep enough bytes in flight per SM for HBM latency.
@@ -377,8 +440,8 @@ __device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t 
                 for (int u = 0; u < UNROLL; ++u) {
                     const int64_t k = k0 + 4 * LPR * u;
                     if (k < end) {
-                        Vec4Loader<real>::load(a.val + k, v[u]);
-                        cc[u] = __ldcs(reinterpret_cast<const ushort4*>(a.col + k));
+                        Vec4Loader<real>::load(val + k, v[u]);
+                        cc[u] = __ldcs(reinterpret_cast<const ushort4*>(col + k));
                     } else {
                         v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
                         cc[u] = make_ushort4(0, 0, 0, 0);
@@ -394,9 +457,15 @@ __device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t 
         for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
         if (valid && l == 0) {
             const int64_t r = base + row;
-            fin(r, row, xi, (xi - a.leak[r] * xi) + t);
+            fin(r, row, xi, (xi - leak[r] * xi) + t);
         }
     }
+}
+
+template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
+__device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t base, int n,
+                                               const real* __restrict__ xs, Fin fin) {
+    propagate_rows_of<real, LPR, UNROLL>(a.rowptr, a.col, a.val, a.leak, base, n, xs, fin);
 }
 
 // V_i <- propagator row i applied to xs, for every row of one neuron.
@@ -446,6 +515,21 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.kin_seg = K.seg.as<uint32_t>();
     a.kin_state = K.state.as<real>(); a.kin_gcoef = K.gcoef.as<real>(); a.kin_table = K.table.as<real>();
     a.kin_vmin = (real)K.vmin; a.kin_frq = (real)K.frq; a.kin_cs = (real)K.conserve; a.kin_erev = (real)K.erev;
+    const CalciumState& Ca = ctx->ca;
+    a.ca_on = Ca.on ? 1 : 0;
+    a.h_ms = (real)(0.5 * ctx->time_step);
+    if (Ca.on) {
+        a.ca_pump = Ca.pump ? 1 : 0; a.ca_nb = Ca.nb; a.ca_T = Ca.T;
+        a.ca_c = Ca.c.as<real>(); a.ca_dcdt = Ca.dcdt.as<real>(); a.ca_scratch = Ca.scratch.as<real>();
+        a.ca_influx = Ca.influx.as<real>(); a.ca_efflux = Ca.efflux.as<real>();
+        a.ca_state = Ca.state.as<real>(); a.ca_table = Ca.table.as<real>();
+        a.ca_brow = Ca.b_rowptr.as<int64_t>(); a.ca_bcol = Ca.b_col.as<uint16_t>();
+        a.ca_bval = Ca.b_val.as<real>(); a.ca_bleak = Ca.b_leak.as<real>();
+        a.ca_wrow = Ca.w_rowptr.as<int64_t>(); a.ca_wcol = Ca.w_col.as<int32_t>();
+        a.ca_wval = Ca.w_val.as<real>(); a.ca_wleak = Ca.w_leak.as<real>();
+        a.ca_log2min = (real)Ca.log2_min; a.ca_frq = (real)Ca.frq; a.ca_scale = (real)Ca.scale;
+        a.ca_n = ctx->n_seg;
+    }
     const SynState& Y = ctx->syn;
     a.syn_on = Y.n > 0 ? 1 : 0;
     if (Y.n > 0) {

@@ -28,7 +28,8 @@ std::vector<DevBuf*> stepped_buffers(nw_ctx* ctx) {
                               &ctx->kin.state, &ctx->ap_detected, &ctx->ap_state,
                               &ctx->spike_count, &ctx->status, &ctx->syn.oa, &ctx->syn.on,
                               &ctx->syn.od, &ctx->syn.pulse_end, &ctx->syn.events,
-                              &ctx->syn.last_event, &ctx->syn.ring};
+                              &ctx->syn.last_event, &ctx->syn.ring, &ctx->ca.c, &ctx->ca.dcdt,
+                              &ctx->ca.state};
     std::vector<DevBuf*> out;
     for (DevBuf* b : v)
         if (b->ptr && b->bytes) out.push_back(b);

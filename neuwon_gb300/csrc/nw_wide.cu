@@ -90,6 +90,22 @@ wide_mechanism_kernel(const StepArgs<real> a, const int s_off, const int64_t n_h
 }
 
 template <typename real>
+__global__ void __launch_bounds__(kWideThreads)
+wide_calcium_prepare_kernel(const StepArgs<real> a) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= a.ca_n) return;
+    a.ca_scratch[i] = fmax(real(0), a.ca_c[i] + a.ca_dcdt[i] * a.h_ms);
+}
+
+template <typename real>
+__global__ void __launch_bounds__(kWideThreads)
+wide_calcium_mechanism_kernel(const StepArgs<real> a) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= a.ca_n) return;
+    calcium_mechanisms(a, i);
+}
+
+template <typename real>
 __global__ void wide_detect_kernel(const StepArgs<real> a, const int s_off) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t s_abs = a.clk->steps + s_off;
@@ -116,18 +132,15 @@ static int wide_lanes(nw_ctx* ctx) {
 }
 
 template <typename real>
-static int launch_rows(nw_ctx* ctx, int lanes, const StepArgs<real>& a) {
+static int launch_rows(nw_ctx* ctx, int lanes, const int64_t* R, const int32_t* C, const real* V, const real* L,
+                       const real* x, real* y, int* status) {
     const int64_t n = ctx->n_seg;
     const unsigned blocks = (unsigned)((n * lanes + kWideThreads - 1) / kWideThreads);
-    const int64_t* R = ctx->w_rowptr.as<int64_t>();
-    const int32_t* C = ctx->w_col.as<int32_t>();
-    const real* V = ctx->w_val.as<real>();
-    const real* L = ctx->w_leak.as<real>();
     switch (lanes) {
-        case 4: wide_rows_kernel<real, 4><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
-        case 8: wide_rows_kernel<real, 8><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
-        case 16: wide_rows_kernel<real, 16><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
-        default: wide_rows_kernel<real, 32><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, a.px, a.V, n, a.status); break;
+        case 4: wide_rows_kernel<real, 4><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, x, y, n, status); break;
+        case 8: wide_rows_kernel<real, 8><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, x, y, n, status); break;
+        case 16: wide_rows_kernel<real, 16><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, x, y, n, status); break;
+        default: wide_rows_kernel<real, 32><<<blocks, kWideThreads, 0, ctx->stream>>>(R, C, V, L, x, y, n, status); break;
     }
     NW_CUDA(ctx, cudaGetLastError());
     return NW_OK;
@@ -146,10 +159,20 @@ static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lan
             const int last = (s == steps - 1 && half == 1) ? 1 : 0;
             wide_membrane_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a, s, half, last);
             NW_CUDA(ctx, cudaGetLastError());
-            NW_CHECK(launch_rows<real>(ctx, lanes, a));
+            NW_CHECK(launch_rows<real>(ctx, lanes, a.wrow, a.wcol, a.wval, a.wleak, a.px, a.V, a.status));
+            if (a.ca_on) {
+                wide_calcium_prepare_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
+                NW_CUDA(ctx, cudaGetLastError());
+                NW_CHECK(launch_rows<real>(ctx, 4, a.ca_wrow, a.ca_wcol, a.ca_wval, a.ca_wleak, a.ca_scratch, a.ca_c,
+                                           a.status));
+            }
             if (half == 0 && n_mech > 0) {
                 wide_mechanism_kernel<real><<<(unsigned)((n_mech + kWideThreads - 1) / kWideThreads), kWideThreads, 0,
                                               ctx->stream>>>(a, s, n_hh, n_kin, n_syn);
+                NW_CUDA(ctx, cudaGetLastError());
+            }
+            if (half == 0 && a.ca_on) {
+                wide_calcium_mechanism_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
                 NW_CUDA(ctx, cudaGetLastError());
             }
         }
@@ -193,6 +216,7 @@ static int wide_graph(nw_ctx* ctx, const StepArgs<real>& a0, int steps, int lane
     key_bytes(key, &ctx->hh.m, sizeof(ctx->hh.m));
     key_bytes(key, &ctx->kin.m, sizeof(ctx->kin.m));
     key_bytes(key, &ctx->syn.n, sizeof(ctx->syn.n));
+    key_bytes(key, &ctx->ca.on, sizeof(ctx->ca.on));
     for (auto& g : ctx->graphs) {
         if (g.key == key) {
             g.last_use = ++ctx->graph_uses;
@@ -235,6 +259,7 @@ static int wide_graph(nw_ctx* ctx, const StepArgs<real>& a0, int steps, int lane
 template <typename real>
 static int wide_steps(nw_ctx* ctx, int k_steps) {
     NW_CHECK(ensure_wide(ctx));
+    if (ctx->ca.on) NW_CHECK(calcium_ensure_wide(ctx));
     const int lanes = wide_lanes(ctx);
     // Every phase is its own launch, so a spike written by one step's detector
     // launch is visible to every later mechanism launch: no cap by the delays.

@@ -270,9 +270,13 @@ class RxD_Model:
                  extracellular_tortuosity=1.55, extracellular_max_distance=20e-6,
                  species=(), mechanisms=(), precision="f32", device=0,
                  propagator_tolerance=EPSILON, propagator_conserve=False, path="batched"):
-        if species:
-            raise NotImplementedError("species beyond the mechanisms' nonspecific conductances "
-                                      "are not on the GPU path")
+        from .species import Calcium
+        self._calcium = None
+        for sp in species:
+            ca = sp if isinstance(sp, Calcium) else Calcium.from_reference_kwargs(sp)
+            if self._calcium is not None:
+                raise NotImplementedError("one diffusing species (calcium) per model")
+            self._calcium = ca
         self.time_step = float(time_step)
         self.temperature = float(temperature)
         self.initial_voltage = float(initial_voltage)
@@ -378,6 +382,40 @@ class RxD_Model:
         self.input_hook.ticks += 2 * k
         self.advance_hook._tick(k)
 
+    def _sync_calcium(self, g, order, par):
+        ca = self._calcium
+        nnz = _lib.ctypes.c_int64()
+        A = np.ascontiguousarray(g["cross_sectional_area"][order], dtype=np.float64)
+        L = np.ascontiguousarray(g["length"][order], dtype=np.float64)
+        vol = np.ascontiguousarray(g["volume"][order], dtype=np.float64)
+        self._ctx.call("nw_calcium_set", ca.diffusivity, _lib.ptr(A), _lib.ptr(L), _lib.ptr(vol), ca.initial,
+                       self.propagator_tolerance, int(self.propagator_conserve), _lib.ctypes.byref(nnz))
+        self.calcium_nnz = nnz.value
+        geom_sorted = {k: np.asarray(v)[order] for k, v in g.items() if k in ("volume", "surface_area")}
+        influx, efflux = (np.ascontiguousarray(x) for x in ca.coefficients(geom_sorted))
+        if ca.pump:
+            table = ca.table(self.time_step)
+            st0 = np.ascontiguousarray(ca.steady_state(ca.initial))
+            self._ctx.call("nw_calcium_pump_set", _lib.ptr(influx), _lib.ptr(efflux),
+                           _lib.ptr(np.ascontiguousarray(table)), ca.num_buckets, ca.degree + 1, ca.log2_min(),
+                           ca.bucket_frq(), ca.scale, _lib.ptr(st0))
+        else:
+            self._ctx.call("nw_calcium_pump_set", _lib.ptr(influx), _lib.ptr(efflux), None, 0, 0, 0.0, 0.0, 0.0,
+                           None)
+
+    def _calcium_values(self, name, count_per_segment=1):
+        self._sync()
+        n = self._n
+        buf = np.empty(n * count_per_segment, dtype=np.float64)
+        self._ctx.call("nw_calcium_data", name.encode(), _lib.ptr(buf), 1, len(buf), 0)
+        if count_per_segment == 1:
+            out = np.empty(n)
+            out[self._order] = buf
+            return out
+        out = np.empty((n, count_per_segment))
+        out[self._order] = buf.reshape(count_per_segment, n).T
+        return out
+
     def add_synapses(self, pre_neurons, post_segments, w_ampa, w_nmda=None, delay=1.0, kinetics=None):
         """Synapses from neurons (handles or ids) onto segments (handles or creation
         indices) with AMPA / NMDA weights in nS and axonal delays in ms (rounded to
@@ -481,6 +519,10 @@ class RxD_Model:
             return self._get_segment_values(name).copy()
         if name.startswith("Neuron."):
             return self._get_neuron_values(name).copy()
+        if name in ("Species.ca", "Species.ca_derivative"):
+            return self._calcium_values(name)
+        if name == "CaPump.state":
+            return self._calcium_values(name, 3)
         if name.startswith("Synapse."):
             self._sync()
             n = 0 if self._syn is None else len(self._syn["pre"])
@@ -674,6 +716,8 @@ class RxD_Model:
                 self._sync_kinetic(cls)
             else:
                 self._sync_hh(cls)
+        if self._calcium is not None:
+            self._sync_calcium(g, order, par)
         self._dirty_structure = False
         self._dirty_clamps = self._dirty_detectors = self._dirty_probes = True
         self._dirty_synapses = self._syn is not None

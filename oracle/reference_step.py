@@ -297,6 +297,44 @@ class SynapseInstances:
             st[:] = np.where(on[:, None], new_on, new_off)
 
 
+# --------------------------------------------------------------------- calcium
+class CalciumOracle:
+    """Intracellular calcium for the oracle: species.py:56-70's update after every
+    electric half step (c <- max(0, c + dcdt h), then c <- M c) with M = expm of the
+    diffusion operator built like electric.py:85-109 (resistance 1e-3 L / (D A),
+    capacity = volume), and the pump / sodium-fraction influx writing dc/dt in the
+    mechanism phase (the pump steps through the same tabled propagator as the
+    device, given as ``table_step(c, states)``)."""
+
+    def __init__(self, parent, cross_area, length, volume, diffusivity, time_step, initial, influx, efflux,
+                 table_step=None, pump_state=None, prune=EPSILON):
+        parent = np.asarray(parent, dtype=np.int64)
+        n = len(parent)
+        res = np.where(parent < 0, 1.0, 1e-3 * np.asarray(length) / (diffusivity * np.asarray(cross_area)))
+        self.M = propagator(parent, res, np.asarray(volume, dtype=np.float64), 0.5 * time_step, prune)
+        self.volume = np.asarray(volume, dtype=np.float64)
+        self.c = np.full(n, float(initial))
+        self.dcdt = np.zeros(n)
+        self.influx = np.asarray(influx, dtype=np.float64)
+        self.efflux = np.asarray(efflux, dtype=np.float64)
+        self.table_step = table_step
+        self.state = None if pump_state is None else np.tile(np.asarray(pump_state, dtype=np.float64), (n, 1))
+        self.half_step = 0.5 * time_step
+
+    def advance_half(self):
+        self.c = self.M.dot(np.maximum(0.0, self.c + self.dcdt * self.half_step))
+
+    def mechanisms(self, voltage, hh):
+        ina = np.zeros(len(self.c))
+        if hh is not None:
+            np.add.at(ina, hh.segment, hh.g["na"] * (voltage[hh.segment] - hh.E["na"]))
+        d = -self.influx * ina
+        if self.table_step is not None:
+            self.state = self.table_step(self.c, self.state)
+            d = d - self.efflux * self.state[:, 1]
+        self.dcdt = d
+
+
 class OracleModel:
     """FP64 restatement of ``RxD_Model.advance()`` (neuwon/rxd/rxd_model.py:63-80).
 
@@ -313,7 +351,7 @@ class OracleModel:
 
     def __init__(self, parent, R, C, *, time_step=0.1, celsius=6.3, v_init=-70.0,
                  prune=EPSILON, propagator_matrix=None, hh=None, clamps=(),
-                 detectors=(), duplicates="sum", kinetic=None, synapses=None):
+                 detectors=(), duplicates="sum", kinetic=None, synapses=None, calcium=None):
         self.parent = np.asarray(parent, dtype=np.int64)
         self.n = len(self.parent)
         self.R = np.asarray(R, dtype=np.float64)
@@ -332,6 +370,7 @@ class OracleModel:
         self.hh = hh
         self.kinetic = kinetic
         self.synapses = synapses
+        self.calcium = calcium
         self.clamps = [(int(s), float(a), int(f), int(k)) for (s, a, f, k) in clamps]
         self.detectors = [(int(s), float(t)) for (s, t) in detectors]
         self.AP_detected = np.zeros(len(self.detectors), dtype=bool)
@@ -376,6 +415,8 @@ class OracleModel:
             self.driving_voltage /= self.sum_conductance
         self.driving_voltage[:] = np.nan_to_num(self.driving_voltage)
         self._advance_electric(self.half_step)
+        if self.calcium is not None:
+            self.calcium.advance_half()
 
     # neuwon/rxd/neuron/electric.py:56-76
     def _advance_electric(self, time_step):
@@ -399,6 +440,8 @@ class OracleModel:
             self.kinetic.advance(self.voltage)
         if self.synapses is not None:
             self.synapses.advance(self.steps)
+        if self.calcium is not None:
+            self.calcium.mechanisms(self.voltage, self.hh)
 
     # neuwon/rxd/neuron/neuron.py:184-188
     def _advance_AP_detector(self):

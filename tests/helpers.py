@@ -151,3 +151,36 @@ def network_case(sizes, num_synapses, *, seed=0, time_step=0.1, precision="f64",
                                        net["weight_nS"] * 1e-9, ao, af, no, nf,
                                        kin.pulse_steps(time_step), kin.e_syn, kin.mg)
     return m, om, dict(net, post=post), offs
+
+
+def calcium_case(trees, clamps, *, time_step=0.025, precision="f64", path="batched", tolerance=None,
+                 conserve=False, oracle=True, calcium=None):
+    """HH everywhere plus intracellular calcium (diffusion, pump, Na-fraction influx):
+    the GPU model and the oracle with the same parameters."""
+    import neuwon_gb300 as nw
+    from oracle.reference_step import CalciumOracle
+    ca = calcium or nw.Calcium()
+    hh_kw = dict(ena=50.0, ek=-77.0, el=-54.3)
+    kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
+    m = nw.RxD_Model(time_step=time_step, temperature=6.3, precision=precision, path=path, species=[ca],
+                     propagator_conserve=conserve, mechanisms=[nw.HH.configure(**hh_kw)], **kw)
+    neurons = [m.add_tree(t) for t in trees]
+    m.insert_everywhere("hh")
+    offs = np.cumsum([0] + [len(t) for t in trees])[:-1]
+    for (ti, s, nA, start, dur) in clamps:
+        nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+    om = None
+    if oracle:
+        om, info = oracle_case(trees, [(ti, s, nA, start, dur) for (ti, s, nA, start, dur) in clamps],
+                               time_step=time_step, hh_kw=hh_kw, prune=tolerance)
+        geoms = [geometry(t) for t in trees]
+        cat = {k: np.concatenate([g[k] for g in geoms]) for k in ("cross_sectional_area", "length", "volume",
+                                                                   "surface_area")}
+        influx, efflux = ca.coefficients(cat)
+        table = ca.table(time_step) if ca.pump else None
+        om.calcium = CalciumOracle(info["parent"], cat["cross_sectional_area"], cat["length"], cat["volume"],
+                                   ca.diffusivity, time_step, ca.initial, influx, efflux,
+                                   table_step=(lambda c, st: ca.table_step(table, c, st)) if ca.pump else None,
+                                   pump_state=ca.steady_state(ca.initial) if ca.pump else None,
+                                   prune=tolerance if tolerance is not None else 2.220446049250313e-16)
+    return m, om, offs
