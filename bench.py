@@ -278,6 +278,65 @@ def _lib_ptr(a):
     return _lib.ptr(a)
 
 
+def precision_study(args, device):
+    """The 1 M-segment precision configuration: one seeded tree (same length and
+    diameter laws), HH + intracellular calcium (D 0.6 um2/ms, pump, Na-fraction
+    influx), dt 0.025 ms for 500 ms on the wide path; FP32 + compensated sums vs
+    FP64 (both on the GPU, run in lockstep), propagators pruned at 1e-6 and 1e-9
+    (charge- and mass-conserving).  Reports max |dV| and max relative d[Ca]."""
+    import neuwon_gb300 as nw
+    from neuwon_gb300.morphology import random_tree
+    steps, chunk = args.study_steps, 500
+    t0 = time.perf_counter()
+    tree = random_tree(args.study_segments, seed=3)
+    log(f"precision study: tree of {len(tree)} segments in {time.perf_counter() - t0:.1f} s")
+    out = {"metric": "precision study: FP32 vs FP64, max |dV| (mV) and max relative d[Ca]",
+           "config": {"workload": f"one tree of {len(tree)} segments, HH + calcium (diffusion 0.6 um2/ms, 3-state "
+                                  "pump, 0.5 % of the Na current as Ca), 1 nA soma clamp, dt 0.025 ms",
+                      "steps": steps, "path": "wide", "pruning": "charge/mass-conserving"},
+           "results": []}
+    for tol in (1e-6, 1e-9):
+        models = {}
+        for precision in ("f64", "f32"):
+            t0 = time.perf_counter()
+            m = nw.RxD_Model(time_step=0.025, temperature=6.3, precision=precision, path="wide", species=[nw.Calcium()],
+                             propagator_tolerance=tol, propagator_conserve=True, device=device,
+                             mechanisms=[nw.HH.configure(ena=50.0, ek=-77.0, el=-54.3)])
+            nr = m.add_tree(tree)
+            m.insert_everywhere("hh")
+            nr.root.inject_current(1.0, 1e9)
+            m._sync()
+            m._ctx.call("nw_synchronize")
+            models[precision] = (m, time.perf_counter() - t0)
+        dv = dca = 0.0
+        times = {"f64": 0.0, "f32": 0.0}
+        done = 0
+        while done < steps:
+            k = min(chunk, steps - done)
+            for precision, (m, _) in models.items():
+                m._ctx.call("nw_synchronize")
+                t0 = time.perf_counter()
+                m.advance(k)
+                m._ctx.call("nw_synchronize")
+                times[precision] += time.perf_counter() - t0
+            done += k
+            v64, v32 = (models[p][0].get_data("Segment.voltage") for p in ("f64", "f32"))
+            c64, c32 = (models[p][0].get_data("Species.ca") for p in ("f64", "f32"))
+            dv = max(dv, float(np.abs(v64 - v32).max()))
+            dca = max(dca, float((np.abs(c64 - c32) / c64).max()))
+        spikes = {p: int(models[p][0].get_data("Neuron.spike_count")[0]) for p in models}
+        nnz = models["f32"][0].propagator_nnz / len(tree)
+        res = {"tolerance": tol, "max_abs_dV_mV": dv, "max_rel_dCa": dca, "spikes": spikes,
+               "entries_per_row": nnz, "calcium_entries_per_row": models["f32"][0].calcium_nnz / len(tree),
+               "ms_per_step": {p: 1e3 * times[p] / steps for p in times},
+               "build_s": {p: models[p][1] for p in models}}
+        log(f"precision study {res}")
+        out["results"].append(res)
+        for m, _ in models.values():
+            m.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -299,6 +358,10 @@ def main():
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
     ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu/adjoint legs")
     ap.add_argument("--adjoint-steps", type=int, default=800)
+    ap.add_argument("--precision-study", action="store_true",
+                    help="run only the 1 M-segment FP32-vs-FP64 calcium precision study")
+    ap.add_argument("--study-segments", type=int, default=1_000_000)
+    ap.add_argument("--study-steps", type=int, default=20000)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -307,6 +370,12 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             run_reference(args, rank)
+        return
+    if args.precision_study:
+        import torch
+        torch.cuda.set_device(local)
+        if rank == 0:
+            precision_study(args, local)
         return
 
     from neuwon_gb300.workloads import batched_currents, batched_trees, build_model
