@@ -143,6 +143,24 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
                         double erev, const double* table, int num_buckets, int num_terms,
                         double vmin, double bucket_frq, double conserve_sum, const double* init_state);
 
+/* ---- kinetic-scheme tables (GPU, FP64) ------------------------------ */
+
+/* lti_sim's table generation (neuwon/rxd/lti_sim/approx.py:159-174, lti_model.py:51-65)
+ * on the GPU: the exact one-step propagators expm(Q dt) of the num_buckets *
+ * samples_per_bucket rate matrices `rates` (row-major S x S each, bucket-major,
+ * S <= 16; FP64 scaling and squaring), then per bucket the polynomial fit
+ * table[b][col][row][t] = sum_s fit[t][s] * P[b, s][row][col] (fit = the
+ * least-squares pseudo-inverse of the in-bucket sample locations, the same for
+ * every bucket).  target 1 installs the table as the kinetic mechanism's, 2 as the
+ * calcium pump's (shapes must match what is registered), 0 only returns it;
+ * table_out (may be NULL) receives it in FP64. */
+int nw_lti_table_build(nw_ctx* ctx, int32_t S, int32_t num_buckets, int32_t samples_per_bucket,
+                       int32_t num_terms, const double* rates, const double* fit, double dt,
+                       int32_t target, double* table_out);
+
+/* expm(Q dt) of `count` row-major S x S matrices (the same FP64 routine). */
+int nw_lti_expm(nw_ctx* ctx, int32_t S, int64_t count, const double* rates, double dt, double* out);
+
 /* ---- intracellular calcium ----------------------------------------- */
 
 /* One diffusing intracellular species (calcium), as neuwon/rxd/species.py advances

@@ -26,7 +26,7 @@ EXPORTS = [
     "nw_get_clock", "nw_set_tuning", "nw_get_tuning", "nw_propagator_stats", "nw_propagator_conserve",
     "nw_kinetic_register", "nw_set_option", "nw_get_option", "nw_electric_half_step_noalloc",
     "nw_adjoint_forward", "nw_adjoint_backward", "nw_autotune", "nw_synapses_set",
-    "nw_calcium_set", "nw_calcium_pump_set", "nw_calcium_data",
+    "nw_calcium_set", "nw_calcium_pump_set", "nw_calcium_data", "nw_lti_table_build", "nw_lti_expm",
 ]
 
 _lib = None
@@ -88,6 +88,9 @@ def load(build_if_missing=True):
         "nw_calcium_pump_set": ([c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_int32, ctypes.c_int32,
                                  c_double, c_double, c_double, c_void_p], c_int),
         "nw_calcium_data": ([c_void_p, ctypes.c_char_p, c_void_p, c_int, c_i64, c_int], c_int),
+        "nw_lti_table_build": ([c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, c_void_p,
+                                c_void_p, c_double, ctypes.c_int32, c_void_p], c_int),
+        "nw_lti_expm": ([c_void_p, ctypes.c_int32, c_i64, c_void_p, c_double, c_void_p], c_int),
         "nw_autotune": ([c_void_p, ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32),
                          P(c_double)], c_int),
         "nw_propagator_stats": ([c_void_p, P(c_i64), P(c_i64), P(c_i64), P(c_i64)], c_int),

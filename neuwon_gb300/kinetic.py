@@ -178,6 +178,101 @@ class LTITable:
         return float(np.abs(approx - exact).max())
 
 
+def table_inputs(rate_fn, to_input, num_buckets, degree, samples_per_bucket):
+    """Sample rate matrices and the per-bucket least-squares fit weights of a table:
+    sample k of bucket b sits at location (k + 1/2) / samples_per_bucket in the
+    bucket (input value to_input(b + location)); the fit of approx.py:159-174 is
+    then the same pseudo-inverse for every bucket.  Returns (rates, fit)."""
+    nb, spb, T = int(num_buckets), int(samples_per_bucket), int(degree) + 1
+    sub = (np.arange(spb) + 0.5) / spb
+    pos = (np.arange(nb)[:, None] + sub[None, :]).ravel()
+    rates = np.ascontiguousarray(rate_fn(to_input(pos)), dtype=np.float64)
+    fit = np.ascontiguousarray(np.linalg.pinv(sub[:, None] ** np.arange(T)[None, :]))
+    return rates, fit
+
+
+def gpu_table(ctx, rates, fit, num_buckets, dt, target=0):
+    """lti_sim table generated on the GPU in FP64 (nw_lti_table_build); layout
+    [bucket][col][row][term]."""
+    from . import _lib
+    S = rates.shape[-1]
+    T, spb = fit.shape
+    table = np.empty((num_buckets, S, S, T))
+    ctx.call("nw_lti_table_build", S, int(num_buckets), int(spb), int(T), _lib.ptr(rates), _lib.ptr(fit),
+             float(dt), int(target), _lib.ptr(table))
+    return table
+
+
+def scheme_table_gpu(ctx, scheme, dt, celsius, vmin, vmax, num_buckets, degree, samples_per_bucket=20, target=0):
+    """The voltage table of a kinetic scheme (LinearInput over [vmin, vmax]) built on the GPU."""
+    width = (vmax - vmin) / num_buckets
+    rates, fit = table_inputs(lambda v: scheme.matrix(v, celsius), lambda pos: vmin + pos * width,
+                              num_buckets, degree, samples_per_bucket)
+    return gpu_table(ctx, rates, fit, num_buckets, dt, target)
+
+
+def optimize_table(ctx, scheme, dt, celsius, accuracy, vmin=-100.0, vmax=60.0, degrees=(1, 2, 3),
+                   start_buckets=10, samples_per_bucket=20, test_points=16, max_table_bytes=8 << 20):
+    """Smallest table meeting ``accuracy`` (max |table - exact| entry error), as
+    lti_sim's optimizer searches it (optimizer.py:184-213): per polynomial degree
+    grow the bucket count by max(1.5, 1.7^orders of magnitude of the excess) until
+    the error is met, then shrink by 0.9 while it still is.  Tables and the exact
+    reference propagators come from the GPU (FP64).  Among the degrees, the one
+    with fewest terms per entry whose FP32 table fits ``max_table_bytes`` wins
+    (fewer bytes on ties).  Returns dict(num_buckets, degree, max_error, table)."""
+    from . import _lib
+    S = scheme.num_states
+
+    def error_of(nb, degree):
+        table = scheme_table_gpu(ctx, scheme, dt, celsius, vmin, vmax, nb, degree, samples_per_bucket)
+        width = (vmax - vmin) / nb
+        sub = (np.arange(test_points) + 0.37) / test_points
+        pos = (np.arange(nb)[:, None] + sub[None, :]).ravel()
+        Q = np.ascontiguousarray(scheme.matrix(vmin + pos * width, celsius))
+        exact = np.empty_like(Q)
+        ctx.call("nw_lti_expm", S, len(Q), _lib.ptr(Q), float(dt), _lib.ptr(exact))
+        exact /= exact.sum(axis=1, keepdims=True)
+        b = pos.astype(np.int64)
+        loc = pos - b
+        basis = loc[:, None] ** np.arange(degree + 1)[None, :]
+        approx = np.einsum("ncrt,nt->nrc", table[b], basis)
+        return float(np.abs(approx - exact).max()), table
+
+    best = None
+    for degree in degrees:
+        nb = float(start_buckets)
+        err, table = error_of(int(round(nb)), degree)
+        lo = 1
+        while err > accuracy:
+            lo = int(round(nb))
+            nb *= max(1.5, 1.7 ** np.log10(err / accuracy))
+            if nb > 1e6:
+                break
+            new_err, new_table = error_of(int(round(nb)), degree)
+            if not new_err < err:
+                break
+            err, table = new_err, new_table
+        if err > accuracy:
+            continue
+        cur = (int(round(nb)), err, table)
+        while True:
+            nb *= 0.9
+            if int(round(nb)) <= lo or int(round(nb)) == cur[0]:
+                break
+            e2, t2 = error_of(int(round(nb)), degree)
+            if e2 > accuracy:
+                break
+            cur = (int(round(nb)), e2, t2)
+        nbytes = cur[0] * S * S * (degree + 1) * 4
+        cand = {"num_buckets": cur[0], "degree": degree, "max_error": cur[1], "table": cur[2], "bytes": nbytes}
+        key = (nbytes > max_table_bytes, degree + 1, nbytes)
+        if best is None or key < best[0]:
+            best = (key, cand)
+    if best is None:
+        raise RuntimeError("no table meets the accuracy")
+    return best[1]
+
+
 class Kinetic(Mechanism):
     """A kinetic-scheme channel with one nonspecific conductance.
 

@@ -394,11 +394,15 @@ class RxD_Model:
         geom_sorted = {k: np.asarray(v)[order] for k, v in g.items() if k in ("volume", "surface_area")}
         influx, efflux = (np.ascontiguousarray(x) for x in ca.coefficients(geom_sorted))
         if ca.pump:
-            table = ca.table(self.time_step)
+            # Pump table generated on the GPU in FP64 (nw_lti_table_build).
+            T = ca.degree + 1
             st0 = np.ascontiguousarray(ca.steady_state(ca.initial))
             self._ctx.call("nw_calcium_pump_set", _lib.ptr(influx), _lib.ptr(efflux),
-                           _lib.ptr(np.ascontiguousarray(table)), ca.num_buckets, ca.degree + 1, ca.log2_min(),
+                           _lib.ptr(np.zeros(ca.num_buckets * 9 * T)), ca.num_buckets, T, ca.log2_min(),
                            ca.bucket_frq(), ca.scale, _lib.ptr(st0))
+            from .kinetic import gpu_table
+            rates, fit = ca.table_inputs()
+            gpu_table(self._ctx, rates, fit, ca.num_buckets, self.time_step, target=2)
         else:
             self._ctx.call("nw_calcium_pump_set", _lib.ptr(influx), _lib.ptr(efflux), None, 0, 0, 0.0, 0.0, 0.0,
                            None)
@@ -769,21 +773,29 @@ class RxD_Model:
         gbar = np.concatenate(rec["gbar"]) if rec["gbar"] else np.empty(0)
         gbar = np.where(np.isnan(gbar), cls.gbar, gbar)
         g = np.ascontiguousarray(gbar * 1e-8 * magnitude)
+        # The table is generated on the GPU in FP64 (nw_lti_table_build) the first
+        # time this mechanism, step and temperature are seen, then reused.
+        sch = cls.scheme_factory()
+        nb, T = cls.num_buckets, cls.degree + 1
         key = (cls, self.time_step, self.temperature)
         cache = getattr(self, "_tables", {})
-        if key not in cache:
-            cache[key] = cls.build_table(self.time_step, self.temperature)
         self._tables = cache
-        tbl = cache[key]
-        sch = tbl.scheme
+        layout = cache.get(key)
+        placeholder = layout is None
+        if placeholder:
+            layout = np.zeros((nb, sch.num_states, sch.num_states, T))
         init = np.ascontiguousarray(sch.steady_state(self.initial_voltage, self.temperature))
         open_idx = np.asarray(sch.open_states, dtype=np.int32)
-        layout = np.ascontiguousarray(tbl.layout.ravel())
         seg_dev = np.ascontiguousarray(self._inv[seg]) if len(seg) else seg
         cs = float(sch.conserve_sum) if sch.conserve_sum is not None else 0.0
+        frq = nb / (cls.vmax - cls.vmin)
         self._ctx.call("nw_kinetic_register", len(seg), _lib.ptr(seg_dev), _lib.ptr(g), sch.num_states,
-                       len(open_idx), _lib.ptr(open_idx), float(cls.erev), _lib.ptr(layout),
-                       tbl.num_buckets, tbl.num_terms, tbl.vmin, tbl.bucket_frq, cs, _lib.ptr(init))
+                       len(open_idx), _lib.ptr(open_idx), float(cls.erev), _lib.ptr(np.ascontiguousarray(layout.ravel())),
+                       nb, T, float(cls.vmin), frq, cs, _lib.ptr(init))
+        if placeholder and len(seg):
+            from .kinetic import scheme_table_gpu
+            cache[key] = scheme_table_gpu(self._ctx, sch, self.time_step, self.temperature, cls.vmin, cls.vmax, nb,
+                                          cls.degree, target=1)
 
     def _sync_clamps(self):
         c = self._clamps

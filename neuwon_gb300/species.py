@@ -113,6 +113,14 @@ class Calcium:
             table[b] = coef.reshape(T, 3, 3).transpose(1, 2, 0)   # [row][col][term]
         return np.ascontiguousarray(table.transpose(0, 2, 1, 3))  # [bucket][col][row][term]
 
+    def table_inputs(self):
+        """Sample rate matrices and fit weights for the GPU table builder (same
+        sample points and fit as ``table``)."""
+        from .kinetic import table_inputs
+        frq, lo = self.bucket_frq(), self.log2_min()
+        return table_inputs(self.generator, lambda pos: 2.0 ** (lo + pos / frq) - self.scale,
+                            self.num_buckets, self.degree, self.samples_per_bucket)
+
     def table_step(self, table, c, states):
         """One step of the tabled pump for arrays of instances (the device's arithmetic)."""
         b, loc = self.locate(c)

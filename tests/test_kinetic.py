@@ -70,3 +70,18 @@ def test_locate_matches_generated_kernel_rules():
     assert loc[0] == 0.0 and loc[1] == pytest.approx(-0.5) and loc[2] == 0.0
     assert b[3] == 1599 and b[4] == 1599 and loc[4] == 1.0 and loc[5] == 1.0
     assert b[6] == 500 and loc[6] == pytest.approx(0.0, abs=1e-9)
+
+
+def test_table_inputs_fit_equals_host_least_squares():
+    """The GPU builder's inputs (sample rate matrices, one pseudo-inverse for every
+    bucket) reproduce the host table when the exponentials are taken on the host."""
+    import scipy.linalg
+    from neuwon_gb300.kinetic import LTITable, na8, table_inputs
+    sch = na8()
+    nb, deg, spb = 200, 1, 20
+    rates, fit = table_inputs(lambda v: sch.matrix(v, 6.3), lambda pos: -100.0 + pos * 160.0 / nb, nb, deg, spb)
+    P = np.array([scipy.linalg.expm(q * 0.1) for q in rates])
+    P /= P.sum(axis=1, keepdims=True)
+    table = np.einsum("ts,bsrc->bcrt", fit, P.reshape(nb, spb, 8, 8))
+    host = LTITable(sch, 0.1, 6.3, num_buckets=nb, degree=deg, samples_per_bucket=spb)
+    assert np.abs(table - host.layout).max() < 1e-12
