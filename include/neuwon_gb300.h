@@ -287,11 +287,14 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
 
 /* Named options.  "reset_clock" (any value): back to time 0 (clock, detector state,
  * probes; conductances count as not yet computed) without touching V or gates.
+ * "set_steps" (k): resume at step k (clock, input ticks 2k, conductances valid when
+ * k > 0 and mechanisms exist; probes start empty), for restoring a checkpoint.
  * "fusion_depth" (default 50, 0 = the whole call in one launch): steps per launch of
  * the batched kernel.  "cuda_graph" (default 1): replay batched launch sequences as
  * CUDA graphs; "prepare_graph" (k) captures, without running, the graph that a later
  * nw_advance(k) replays; "clear_graphs" drops the cached graphs; nw_get_option also reports
- * "graphs_cached", "graph_captures" and "graph_replays". 
+ * "graphs_cached", "graph_captures", "graph_replays" and "synapse_ring_words" (u32 words
+ * per neuron of the spike ring read and written as "Synapse.spike_ring"). 
  * "bulk_pipeline" (default 0): stream the propagator of the FP32
  * batched path through shared memory with cp.async.bulk copies (needs lanes_per_row
  * 0 in nw_set_tuning); nw_get_option("bulk_pipeline_active") tells whether the next

@@ -446,6 +446,25 @@ int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int6
         DevBuf& b = nm == "Synapse.ampa_open" ? Y.oa : nm == "Synapse.nmda_open" ? Y.on : Y.od;
         return upload_convert(ctx, b.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
     }
+    if (nm == "Synapse.events" || nm == "Synapse.last_event" || nm == "Synapse.pulse_end") {
+        SynState& Y = ctx->syn;
+        NW_CHECK(need(Y.n));
+        std::vector<double> sorted(count);
+        for (int64_t i = 0; i < count; ++i) sorted[Y.user_to_sorted[i]] = read_as_double(host, dtype, i);
+        DevBuf& b = nm == "Synapse.events" ? Y.events : nm == "Synapse.last_event" ? Y.last_event : Y.pulse_end;
+        return upload_convert(ctx, b.ptr, nm == "Synapse.events" ? NW_DTYPE_U32 : NW_DTYPE_I32, sorted.data(),
+                              NW_DTYPE_F64, count);
+    }
+    if (nm == "Synapse.spike_ring") {
+        // Raw spike bits: n_neuron x ring_words u32 words (steps modulo the ring length).
+        NW_CHECK(need(ctx->syn.n ? ctx->n_neuron * ctx->syn.ring_words : 0));
+        if (!count) return NW_OK;
+        return upload_convert(ctx, ctx->syn.ring.ptr, NW_DTYPE_U32, host, dtype, count);
+    }
+    if (nm == "Neuron.AP_state") {
+        NW_CHECK(need(ctx->n_neuron));
+        return upload_convert(ctx, ctx->ap_state.ptr, NW_DTYPE_U8, host, dtype, count);
+    }
     if (nm == "Neuron.AP_detected") {
         NW_CHECK(need(ctx->n_neuron));
         return upload_convert(ctx, ctx->ap_detected.ptr, NW_DTYPE_U8, host, dtype, count);
@@ -510,6 +529,12 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
         for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[Y.user_to_sorted[i]]);
         return NW_OK;
     }
+    if (nm == "Synapse.spike_ring") {
+        NW_CHECK(need(ctx->syn.n ? ctx->n_neuron * ctx->syn.ring_words : 0));
+        if (!count) return NW_OK;
+        return download_convert(ctx, host, dtype, ctx->syn.ring.ptr, NW_DTYPE_U32, count);
+    }
+    if (nm == "Neuron.AP_state") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->ap_state.ptr, NW_DTYPE_U8, count); }
     if (nm == "Neuron.AP_detected") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->ap_detected.ptr, NW_DTYPE_U8, count); }
     if (nm == "Neuron.spike_count") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->spike_count.ptr, NW_DTYPE_U32, count); }
     return fail(ctx, NW_ERR_ARG, "nw_get_data: unknown attribute " + nm);
@@ -1033,6 +1058,16 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         graphs_clear(ctx);
         return NW_OK;
     }
+    if (nm == "set_steps") {
+        // Resume at a saved step: clock, input ticks (two per step) and
+        // conductance validity; probes start empty.
+        if (value < 0) return fail(ctx, NW_ERR_ARG, "set_steps: negative step");
+        ctx->steps = value;
+        ctx->input_ticks = 2 * value;
+        ctx->g_valid = value > 0 && (ctx->hh.m > 0 || ctx->kin.m > 0);
+        ctx->probe_len = 0;
+        return NW_OK;
+    }
     if (nm == "reset_clock") {
         // Back to time 0: clock, conductance validity, detector state and probes.
         ctx->input_ticks = ctx->steps = 0;
@@ -1060,6 +1095,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "graphs_cached") { *value = (int64_t)ctx->graphs.size(); return NW_OK; }
     if (nm == "graph_captures") { *value = ctx->graph_captures; return NW_OK; }
     if (nm == "graph_replays") { *value = ctx->graph_replays; return NW_OK; }
+    if (nm == "synapse_ring_words") { *value = ctx->syn.ring_words; return NW_OK; }
     return fail(ctx, NW_ERR_ARG, "nw_get_option: unknown option " + nm);
 }
 

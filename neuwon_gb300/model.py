@@ -464,6 +464,16 @@ class RxD_Model:
                        kin.pulse_steps(self.time_step), kin.e_syn, kin.mg)
         self._dirty_synapses = False
 
+    def save_sqlite(self, filename):
+        """Checkpoint the device state (neuwon/database/sql.py:78-101 layout)."""
+        from .checkpoint import save_sqlite
+        save_sqlite(self, filename)
+
+    def load_sqlite(self, filename):
+        """Restore a checkpoint written by ``save_sqlite`` (sql.py:103-129)."""
+        from .checkpoint import load_sqlite
+        load_sqlite(self, filename)
+
     def autotune(self, trial_steps=10):
         """Choose the batched path's lanes per row, threads per CTA and step-fusion
         depth by timing short runs of this model (state restored afterwards)."""
