@@ -512,6 +512,11 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
                 write_from_double(host, dtype, u * K.S + c, sorted[(size_t)c * K.m + K.user_to_sorted[u]]);
         return NW_OK;
     }
+    if (nm == "Synapse.spike_ring") {
+        NW_CHECK(need(ctx->syn.n ? ctx->n_neuron * ctx->syn.ring_words : 0));
+        if (!count) return NW_OK;
+        return download_convert(ctx, host, dtype, ctx->syn.ring.ptr, NW_DTYPE_U32, count);
+    }
     if (nm.rfind("Synapse.", 0) == 0) {
         const SynState& Y = ctx->syn;
         const DevBuf* b = nullptr;
@@ -528,11 +533,6 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
         NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, b->ptr, sd, count));
         for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[Y.user_to_sorted[i]]);
         return NW_OK;
-    }
-    if (nm == "Synapse.spike_ring") {
-        NW_CHECK(need(ctx->syn.n ? ctx->n_neuron * ctx->syn.ring_words : 0));
-        if (!count) return NW_OK;
-        return download_convert(ctx, host, dtype, ctx->syn.ring.ptr, NW_DTYPE_U32, count);
     }
     if (nm == "Neuron.AP_state") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->ap_state.ptr, NW_DTYPE_U8, count); }
     if (nm == "Neuron.AP_detected") { NW_CHECK(need(ctx->n_neuron)); return download_convert(ctx, host, dtype, ctx->ap_detected.ptr, NW_DTYPE_U8, count); }
