@@ -550,6 +550,7 @@ int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out) {
     NW_CHECK(propagator_build(ctx, prune_tolerance, nnz_out));
     NW_CHECK(propagator_to_batched(ctx));
     ctx->prop_valid = true;
+    ctx->prop_built = true;
     return NW_OK;
 }
 
@@ -574,6 +575,8 @@ int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr, const i
     NW_CHECK(propagator_from_host(ctx, rowptr, col, val, nnz));
     NW_CHECK(propagator_to_batched(ctx));
     ctx->prop_valid = true;
+    ctx->prop_built = false;
+    ctx->prop_format = 0;
     return NW_OK;
 }
 
@@ -1041,6 +1044,15 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
     if (nm == "cuda_graph") { ctx->use_graph = value != 0; return NW_OK; }
+    if (nm == "propagator_format") {
+        // 0: rows (every P_ij stored in its row); 1: pairs (each coupling once,
+        // applied to both rows through detailed balance; built propagators only).
+        if (value != 0 && value != 1) return fail(ctx, NW_ERR_ARG, "propagator_format must be 0 or 1");
+        if (value == 1 && !ctx->prop_built)
+            return fail(ctx, NW_ERR_STATE, "pair format needs a propagator built by nw_propagator_build");
+        ctx->prop_format = (int)value;
+        return NW_OK;
+    }
     if (nm == "fusion_depth") {
         if (value < 0 || value > (1 << 20)) return fail(ctx, NW_ERR_ARG, "fusion_depth must be in [0, 2^20]");
         ctx->fusion = (int)value;
@@ -1091,6 +1103,8 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "bulk_pipeline") { *value = ctx->use_bulk ? 1 : 0; return NW_OK; }
     if (nm == "bulk_pipeline_active") { *value = uses_bulk_pipeline(ctx) ? 1 : 0; return NW_OK; }
     if (nm == "cuda_graph") { *value = ctx->use_graph ? 1 : 0; return NW_OK; }
+    if (nm == "propagator_format") { *value = ctx->prop_format; return NW_OK; }
+    if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "fusion_depth") { *value = ctx->fusion; return NW_OK; }
     if (nm == "graphs_cached") { *value = (int64_t)ctx->graphs.size(); return NW_OK; }
     if (nm == "graph_captures") { *value = ctx->graph_captures; return NW_OK; }

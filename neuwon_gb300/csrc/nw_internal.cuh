@@ -157,12 +157,21 @@ struct nw_ctx {
     // batched difference form (off-diagonal entries, u16 neuron-relative
     // columns, rows padded to 4 entries, per-row leak = 1 - row sum).
     bool prop_valid = false;
+    bool prop_built = false;    // built here (detailed balance holds): the pair format may be used
     bool b_ok = false;          // batched format present (every neuron <= 65,535 segments)
     bool w_ok = false;          // wide format present (built on first use of the wide path)
     int64_t nnz64 = 0, nnz_b = 0, nnz_w = 0;
     nw::DevBuf p_rowptr, p_col, p_val;          // i64, i32, f64
     nw::DevBuf b_rowptr, b_col, b_val, b_leak;  // i64, u16, real, real
     nw::DevBuf w_rowptr, w_col, w_val, w_leak;  // i64, i32 (global columns), real, real
+    // Pair ("flux") format of the batched path: each coupled pair (i, j) stored
+    // once, in the row of the member with the smaller capacitance (the larger
+    // P), as w = c_i P_ij / c_max(neuron); both rows receive w (x_j - x_i).
+    bool f_ok = false;
+    int64_t nnz_f = 0;
+    nw::DevBuf f_rowptr, f_col, f_val, f_leak, f_rc;   // i64, u16, real, real, real (c_max / c_i)
+    nw::DevBuf f_acc;                                  // i64 [n_seg] accumulators of neurons too large for shared memory
+    int prop_format = 0;                               // 0: rows, 1: pairs
 
     // Mechanisms.
     nw::HHState hh;
@@ -232,6 +241,8 @@ int advance_batched(nw_ctx* ctx, int k_steps);
 int advance_plain(nw_ctx* ctx, int k_steps);
 int advance_wide(nw_ctx* ctx, int k_steps);
 int ensure_wide(nw_ctx* ctx);
+int ensure_flux(nw_ctx* ctx);
+void free_flux(nw_ctx* ctx);
 void free_wide(nw_ctx* ctx);
 int choose_lanes_per_row(nw_ctx* ctx);
 bool uses_bulk_pipeline(nw_ctx* ctx);

@@ -487,10 +487,127 @@ template int csr_to_rows<uint16_t>(nw_ctx*, const DevBuf&, const DevBuf&, const 
 template int csr_to_rows<int32_t>(nw_ctx*, const DevBuf&, const DevBuf&, const DevBuf&, bool, DevBuf&, DevBuf&,
                                   DevBuf&, DevBuf&, int64_t*);
 
+// ------------------------------------------------- pair (flux) format
+
+// Entry (i, c) of row i belongs to row i when c_i < c_c (ties: i < c).
+__device__ __forceinline__ bool pair_owner(const double* cap, int64_t i, int64_t c) {
+    const double ci = cap[i], cc = cap[c];
+    return ci < cc || (ci == cc && i < c);
+}
+
+__global__ void flux_count_kernel(int64_t n, const int64_t* prow, const int32_t* pcol, const double* cap,
+                                  int64_t* cnt) {
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int64_t c = 0;
+    for (int64_t k = prow[r]; k < prow[r + 1]; ++k) {
+        const int64_t col = pcol[k];
+        c += (col != r && pair_owner(cap, r, col)) ? 1 : 0;
+    }
+    cnt[r] = (c + 3) & ~(int64_t)3;   // 4-entry vectors
+}
+
+template <typename real>
+__global__ void flux_fill_kernel(int64_t n, const int64_t* row_base, const double* row_cmax, const int64_t* prow,
+                                 const int32_t* pcol, const double* pval, const double* cap, const int64_t* frow,
+                                 uint16_t* fcol, real* fval, real* leak, real* rc) {
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (r >= n) return;
+    const int64_t base = row_base[r];
+    const double cmax = row_cmax[r];
+    const double scale = cap[r] / cmax;
+    int64_t ob = frow[r];
+    double sum = 0.0;
+    for (int64_t k0 = prow[r]; k0 < prow[r + 1]; k0 += 32) {
+        const int64_t k = k0 + lane;
+        const bool valid = k < prow[r + 1];
+        const int32_t c = valid ? pcol[k] : -1;
+        const double v = valid ? pval[k] : 0.0;
+        sum += v;
+        const bool own = valid && c != (int32_t)r && pair_owner(cap, r, c);
+        const unsigned mask = __ballot_sync(0xffffffffu, own);
+        const int pos = __popc(mask & ((1u << lane) - 1u));
+        if (own) { fcol[ob + pos] = (uint16_t)(c - base); fval[ob + pos] = (real)(v * scale); }
+        ob += __popc(mask);
+    }
+    for (int64_t k = ob + lane; k < frow[r + 1]; k += 32) { fcol[k] = (uint16_t)(r - base); fval[k] = real(0); }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+    if (lane == 0) { leak[r] = (real)(1.0 - sum); rc[r] = (real)(cmax / cap[r]); }
+}
+
+void free_flux(nw_ctx* ctx) {
+    for (DevBuf* b : {&ctx->f_rowptr, &ctx->f_col, &ctx->f_val, &ctx->f_leak, &ctx->f_rc, &ctx->f_acc}) dev_free(*b);
+    ctx->f_ok = false;
+    ctx->nnz_f = 0;
+}
+
+int ensure_flux(nw_ctx* ctx) {
+    if (ctx->f_ok) return NW_OK;
+    if (ctx->max_neuron > 65535) return fail(ctx, NW_ERR_LIMIT, "pair format: a neuron has more than 65,535 segments");
+    const int64_t n = ctx->n_seg;
+    std::vector<double> cap(n);
+    NW_CUDA(ctx, cudaMemcpy(cap.data(), ctx->cap64.ptr, 8 * n, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> base(n);
+    std::vector<double> cmax(n);
+    for (int64_t j = 0; j < ctx->n_neuron; ++j) {
+        double m = 0.0;
+        for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) m = std::max(m, cap[i]);
+        for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) { base[i] = ctx->h_neuron_start[j]; cmax[i] = m; }
+    }
+    DevBuf d_cnt, d_base, d_cmax;
+    auto cleanup = [&]() { dev_free(d_cnt); dev_free(d_base); dev_free(d_cmax); };
+    int rc = NW_OK;
+    do {
+        if ((rc = dev_alloc(ctx, d_cnt, 8 * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_base, 8 * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_cmax, 8 * n)) != NW_OK) break;
+        cudaMemcpyAsync(d_base.ptr, base.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(d_cmax.ptr, cmax.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+        flux_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+            n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->cap64.as<double>(), d_cnt.as<int64_t>());
+        std::vector<int64_t> cnt(n), frow(n + 1, 0);
+        cudaMemcpyAsync(cnt.data(), d_cnt.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "pair format count"); break; }
+        for (int64_t i = 0; i < n; ++i) frow[i + 1] = frow[i] + cnt[i];
+        const int64_t nf = frow[n];
+        const size_t rs = (size_t)ctx->precision;
+        if ((rc = dev_alloc(ctx, ctx->f_rowptr, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->f_col, 2 * std::max<int64_t>(nf, 8))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->f_val, rs * std::max<int64_t>(nf, 8))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->f_leak, rs * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->f_rc, rs * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->f_acc, 8 * n)) != NW_OK) break;
+        cudaMemcpyAsync(ctx->f_rowptr.ptr, frow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemsetAsync(ctx->f_acc.ptr, 0, 8 * n, ctx->stream);
+        const unsigned blocks = (unsigned)((n * 32 + 255) / 256);
+        if (ctx->precision == NW_F64)
+            flux_fill_kernel<double><<<blocks, 256, 0, ctx->stream>>>(
+                n, d_base.as<int64_t>(), d_cmax.as<double>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
+                ctx->p_val.as<double>(), ctx->cap64.as<double>(), ctx->f_rowptr.as<int64_t>(),
+                ctx->f_col.as<uint16_t>(), ctx->f_val.as<double>(), ctx->f_leak.as<double>(), ctx->f_rc.as<double>());
+        else
+            flux_fill_kernel<float><<<blocks, 256, 0, ctx->stream>>>(
+                n, d_base.as<int64_t>(), d_cmax.as<double>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
+                ctx->p_val.as<double>(), ctx->cap64.as<double>(), ctx->f_rowptr.as<int64_t>(),
+                ctx->f_col.as<uint16_t>(), ctx->f_val.as<float>(), ctx->f_leak.as<float>(), ctx->f_rc.as<float>());
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "pair format fill"); break; }
+        ctx->nnz_f = nf;
+        ctx->f_ok = true;
+    } while (0);
+    cleanup();
+    return rc;
+}
+
 // Called whenever the FP64 propagator changes: rebuilds the batched format (if
-// every neuron fits its 16-bit columns) and drops the wide one until next used.
+// every neuron fits its 16-bit columns) and drops the wide and pair formats
+// until next used.
 int propagator_to_batched(nw_ctx* ctx) {
     free_wide(ctx);
+    free_flux(ctx);
     for (DevBuf* b : {&ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak}) dev_free(*b);
     ctx->b_ok = false;
     ctx->nnz_b = 0;

@@ -219,7 +219,86 @@ __device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, i
     R.seq = seq;
 }
 
-template <typename real, int LPR, bool BULK>
+// ------------------------------------------------------------ pair format
+
+// Every stored pair (i, j) of a neuron adds t = w (x_j - x_i) to row i's sum and
+// subtracts it from row j's (w = c_i P_ij / c_max, detailed balance c_i P_ij =
+// c_j P_ji), so each coupling is read from HBM once instead of twice.  The sums
+// are 2^-40 fixed point, so integer atomic adds give the same bits in any order.
+constexpr double kFluxScale = 1099511627776.0;   // 2^40
+__device__ __forceinline__ long long flux_fix(float t) { return __float2ll_rn(t * (float)kFluxScale); }
+__device__ __forceinline__ long long flux_fix(double t) { return __double2ll_rn(t * kFluxScale); }
+__device__ __forceinline__ float flux_unfix(long long q, float scale) { return __ll2float_rn(q) * scale; }
+__device__ __forceinline__ double flux_unfix(long long q, double scale) { return __ll2double_rn(q) * scale; }
+
+template <typename real, int LPR>
+__device__ __forceinline__ void propagate_flux(const StepArgs<real>& a, int64_t base, int n,
+                                               const real* __restrict__ xs, unsigned long long* acc) {
+    constexpr int UNROLL = 2;
+    constexpr int GPW = 32 / LPR;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int q = lane / LPR, l = lane % LPR;
+    for (int rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int row = rb + q;
+        const bool valid = row < n;
+        real s = real(0), c = real(0), xi = real(0);
+        if (valid) {
+            const int64_t r = base + row;
+            const int64_t beg = a.frow[r], end = a.frow[r + 1];
+            xi = xs[row];
+            for (int64_t k0 = beg + 4 * l; k0 < end; k0 += 4 * LPR * UNROLL) {
+                real v[UNROLL][4];
+                ushort4 cc[UNROLL];
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const int64_t k = k0 + 4 * LPR * u;
+                    if (k < end) {
+                        Vec4Loader<real>::load(a.fval + k, v[u]);
+                        cc[u] = __ldcs(reinterpret_cast<const ushort4*>(a.fcol + k));
+                    } else {
+                        v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                        cc[u] = make_ushort4((unsigned short)row, (unsigned short)row, (unsigned short)row,
+                                             (unsigned short)row);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const real t0 = v[u][0] * (xs[cc[u].x] - xi), t1 = v[u][1] * (xs[cc[u].y] - xi);
+                    const real t2 = v[u][2] * (xs[cc[u].z] - xi), t3 = v[u][3] * (xs[cc[u].w] - xi);
+                    kahan_add(s, c, (t0 + t1) + (t2 + t3));
+                    if (t0 != real(0)) atomicAdd(acc + cc[u].x, (unsigned long long)(-flux_fix(t0)));
+                    if (t1 != real(0)) atomicAdd(acc + cc[u].y, (unsigned long long)(-flux_fix(t1)));
+                    if (t2 != real(0)) atomicAdd(acc + cc[u].z, (unsigned long long)(-flux_fix(t2)));
+                    if (t3 != real(0)) atomicAdd(acc + cc[u].w, (unsigned long long)(-flux_fix(t3)));
+                }
+            }
+        }
+        real t = s - c;
+#pragma unroll
+        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        if (valid && l == 0) atomicAdd(acc + row, (unsigned long long)flux_fix(t));
+    }
+}
+
+// V_i = x_i - leak_i x_i + (sum of row i's pair terms) * c_max / c_i; resets the sums.
+template <typename real>
+__device__ __forceinline__ void flux_finalize(const StepArgs<real>& a, int64_t base, int n, const real* xs,
+                                              unsigned long long* acc) {
+    const real unit = (real)(1.0 / kFluxScale);
+    for (int li = threadIdx.x; li < n; li += blockDim.x) {
+        const int64_t i = base + li;
+        const real xi = xs[li];
+        const long long q = (long long)acc[li];
+        acc[li] = 0ull;
+        const real vnew = (xi - a.fleak[i] * xi) + flux_unfix(q, a.frc[i] * unit);
+        if (!isfinite(vnew) || !isfinite(xi)) atomicOr(a.status, kStatusNonFinite);
+        a.V[i] = vnew;
+    }
+}
+
+template <typename real, int LPR, bool BULK, bool FLUX>
 __global__ void __launch_bounds__(1024)
 batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_off) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -261,6 +340,15 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         const int j = a.neuron_order[job];
         const int64_t base = a.neuron_start[j];
         const int n = (int)(a.neuron_start[j + 1] - base);
+        if (FLUX) {
+            // The finalize pass leaves the accumulators at zero for the next half step.
+            if (n <= a.facc_cap) {
+                unsigned long long* z = reinterpret_cast<unsigned long long*>(smem_raw + xs_bytes);
+                for (int li = threadIdx.x; li < n; li += blockDim.x) z[li] = 0ull;
+            } else {
+                for (int li = threadIdx.x; li < n; li += blockDim.x) a.facc[base + li] = 0ull;
+            }
+        }
         if (tid == 0) {
             int c0 = a.clamp_neuron_ptr ? a.clamp_neuron_ptr[j] : 0;
             int c1 = a.clamp_neuron_ptr ? a.clamp_neuron_ptr[j + 1] : 0;
@@ -275,6 +363,12 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         __syncthreads();
         const int nclamp = s_nclamp;
         if (BULK) slice = warp_slice(a, base, n);
+        // Pair-format accumulators: in shared memory behind x when the neuron fits,
+        // else the neuron's slice of a global array (each branch keeps its address
+        // space known to the compiler).
+        const bool acc_in_smem = n <= a.facc_cap;
+        unsigned long long* const sacc = reinterpret_cast<unsigned long long*>(smem_raw + xs_bytes);
+        unsigned long long* const gacc = a.facc + base;
         // Mechanism instance ranges of this neuron.
         int64_t ib = 0, ie = 0, kb = 0, ke = 0, yb = 0, ye = 0;
         if (a.syn_on) { yb = a.syn_neuron_ptr[j]; ye = a.syn_neuron_ptr[j + 1]; }
@@ -319,7 +413,17 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     xs[li] = membrane_x(a, i, G, GE, I, last);
                 }
                 __syncthreads();
-                if (BULK) propagate_neuron_bulk(a, base, xs, ring, slice, &s_abort);
+                if (FLUX) {
+                    if (acc_in_smem) {
+                        propagate_flux<real, LPR>(a, base, n, xs, sacc);
+                        __syncthreads();
+                        flux_finalize(a, base, n, xs, sacc);
+                    } else {
+                        propagate_flux<real, LPR>(a, base, n, xs, gacc);
+                        __syncthreads();
+                        flux_finalize(a, base, n, xs, gacc);
+                    }
+                } else if (BULK) propagate_neuron_bulk(a, base, xs, ring, slice, &s_abort);
                 else propagate_neuron<real, LPR>(a, base, n, xs);
                 __syncthreads();
                 if (BULK && s_abort) break;
@@ -445,7 +549,8 @@ __global__ void plain_detect_kernel(const StepArgs<real> a, int64_t row) {
 
 int choose_lanes_per_row(nw_ctx* ctx) {
     if (ctx->lanes_per_row) return ctx->lanes_per_row;
-    double avg = ctx->n_seg ? (double)ctx->nnz_b / (double)ctx->n_seg : 0.0;
+    const int64_t nnz = (ctx->prop_format == 1 && ctx->f_ok) ? ctx->nnz_f : ctx->nnz_b;
+    double avg = ctx->n_seg ? (double)nnz / (double)ctx->n_seg : 0.0;
     if (avg >= 48) return 16;
     if (avg >= 20) return 8;
     return 4;
@@ -459,16 +564,22 @@ struct BatchedCfg {
     int threads;
     size_t smem;
     int xs_bytes;
+    int acc_cap;      // pair format: largest neuron whose accumulators fit in shared memory
 };
 
-template <typename real, int LPR, bool BULK>
+template <typename real, int LPR, bool BULK, bool FLUX>
 static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
-    auto kern = batched_advance_kernel<real, LPR, BULK>;
+    auto kern = batched_advance_kernel<real, LPR, BULK, FLUX>;
     const size_t xs_bytes = ((size_t)ctx->max_neuron * sizeof(real) + 127) & ~(size_t)127;
     const int threads = ctx->threads;
     size_t smem = xs_bytes;
     if (BULK) smem += (size_t)(threads / 32) * kBulkStages * (BulkGeom<real>::kStageBytes + 8);
     const size_t static_smem = 4096;
+    int acc_cap = 0;
+    if (FLUX && xs_bytes + static_smem < ctx->smem_optin) {
+        acc_cap = (int)std::min<int64_t>(ctx->max_neuron, (int64_t)((ctx->smem_optin - static_smem - xs_bytes) / 8));
+        smem += (size_t)acc_cap * 8;
+    }
     if (smem + static_smem > ctx->smem_optin)
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron of " + std::to_string(ctx->max_neuron) +
                                        " segments does not fit in shared memory at this precision");
@@ -482,6 +593,7 @@ static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
     c.threads = threads;
     c.smem = smem;
     c.xs_bytes = (int)xs_bytes;
+    c.acc_cap = acc_cap;
     return NW_OK;
 }
 
@@ -501,14 +613,23 @@ template <typename real>
 static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
     if (!ctx->b_ok || (ctx->ca.on && !ctx->ca.b_ok))
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron has more than 65,535 segments (use the wide path)");
+    if (ctx->prop_format == 1) {
+        NW_CHECK(ensure_flux(ctx));
+        switch (choose_lanes_per_row(ctx)) {
+            case 4: return config_batched_lpr<real, 4, false, true>(ctx, c);
+            case 8: return config_batched_lpr<real, 8, false, true>(ctx, c);
+            case 16: return config_batched_lpr<real, 16, false, true>(ctx, c);
+            default: return config_batched_lpr<real, 32, false, true>(ctx, c);
+        }
+    }
     if constexpr (std::is_same<real, float>::value) {
-        if (uses_bulk_pipeline(ctx)) return config_batched_lpr<float, 32, true>(ctx, c);
+        if (uses_bulk_pipeline(ctx)) return config_batched_lpr<float, 32, true, false>(ctx, c);
     }
     switch (choose_lanes_per_row(ctx)) {
-        case 4: return config_batched_lpr<real, 4, false>(ctx, c);
-        case 8: return config_batched_lpr<real, 8, false>(ctx, c);
-        case 16: return config_batched_lpr<real, 16, false>(ctx, c);
-        default: return config_batched_lpr<real, 32, false>(ctx, c);
+        case 4: return config_batched_lpr<real, 4, false, false>(ctx, c);
+        case 8: return config_batched_lpr<real, 8, false, false>(ctx, c);
+        case 16: return config_batched_lpr<real, 16, false, false>(ctx, c);
+        default: return config_batched_lpr<real, 32, false, false>(ctx, c);
     }
 }
 
@@ -625,7 +746,8 @@ static int launch_batched(nw_ctx* ctx, int k_steps) {
     BatchedCfg<real> c;
     memset(&c, 0, sizeof(c));
     NW_CHECK(config_batched<real>(ctx, c));
-    const StepArgs<real> a = make_args<real>(ctx, k_steps);
+    StepArgs<real> a = make_args<real>(ctx, k_steps);
+    a.facc_cap = c.acc_cap;
     NW_CHECK(push_clock(ctx));
     if (ctx->use_graph) return launch_graph<real>(ctx, c, a, k_steps);
     return enqueue_batched<real>(ctx, c, a, k_steps);
@@ -636,7 +758,8 @@ static int prepare_graph_t(nw_ctx* ctx, int k_steps) {
     BatchedCfg<real> c;
     memset(&c, 0, sizeof(c));
     NW_CHECK(config_batched<real>(ctx, c));
-    const StepArgs<real> a = make_args<real>(ctx, k_steps);
+    StepArgs<real> a = make_args<real>(ctx, k_steps);
+    a.facc_cap = c.acc_cap;
     return launch_graph<real>(ctx, c, a, k_steps, false);
 }
 

@@ -87,6 +87,9 @@ struct StepArgs {
     const int64_t* rowptr; const uint16_t* col; const real* val; const real* leak;
     // plain propagator
     const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
+    // pair ("flux") propagator: rows of owned pairs, leak, c_max / c_i, global accumulators
+    const int64_t* frow; const uint16_t* fcol; const real* fval; const real* fleak; const real* frc;
+    unsigned long long* facc; int facc_cap;
     // wide propagator (global int32 columns)
     const int64_t* wrow; const int32_t* wcol; const real* wval; const real* wleak;
     // hh
@@ -495,6 +498,9 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.val = ctx->b_val.as<real>(); a.leak = ctx->b_leak.as<real>();
     a.prow = ctx->p_rowptr.as<int64_t>(); a.pcol = ctx->p_col.as<int32_t>(); a.pval = ctx->p_val.as<double>();
     a.px = ctx->plain_x.as<real>();
+    a.frow = ctx->f_rowptr.as<int64_t>(); a.fcol = ctx->f_col.as<uint16_t>();
+    a.fval = ctx->f_val.as<real>(); a.fleak = ctx->f_leak.as<real>(); a.frc = ctx->f_rc.as<real>();
+    a.facc = ctx->f_acc.as<unsigned long long>();
     a.wrow = ctx->w_rowptr.as<int64_t>(); a.wcol = ctx->w_col.as<int32_t>();
     a.wval = ctx->w_val.as<real>(); a.wleak = ctx->w_leak.as<real>();
     const HHState& hh = ctx->hh;

@@ -260,6 +260,9 @@ class RxD_Model:
       propagator_tolerance  prune |P_ij| below this (reference: machine epsilon)
       propagator_conserve   return the pruned mass of each row to its diagonal
                             (charge-conserving pruning; the reference does not)
+      propagator_format     'rows' (every P_ij in its row) or 'pairs' (each coupling
+                            stored once and applied to both segments through
+                            detailed balance: half the propagator bytes per step)
       path                  'batched' (fused persistent kernel, one CTA per neuron),
                             'wide' (whole-model launches per phase: neurons of any
                             size) or 'plain' (per-neuron launches)
@@ -269,7 +272,8 @@ class RxD_Model:
                  cytoplasmic_resistance=100, membrane_capacitance=1,
                  extracellular_tortuosity=1.55, extracellular_max_distance=20e-6,
                  species=(), mechanisms=(), precision="f32", device=0,
-                 propagator_tolerance=EPSILON, propagator_conserve=False, path="batched"):
+                 propagator_tolerance=EPSILON, propagator_conserve=False, path="batched",
+                 propagator_format="rows"):
         from .species import Calcium
         self._calcium = None
         for sp in species:
@@ -287,6 +291,7 @@ class RxD_Model:
         self.propagator_tolerance = float(propagator_tolerance)
         self.propagator_conserve = bool(propagator_conserve)
         self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN, "wide": _lib.PATH_WIDE}[path]
+        self.propagator_format = {"rows": 0, "pairs": 1}[propagator_format]
         self.input_hook = Clock(0.5 * self.time_step, units="ms")
         self.advance_hook = self.clock = Clock(self.time_step, units="ms")
         # Segment table (creation order).
@@ -724,6 +729,7 @@ class RxD_Model:
         ctx.call("nw_propagator_build", self.propagator_tolerance, _lib.ctypes.byref(nnz))
         if self.propagator_conserve:
             ctx.call("nw_propagator_conserve")
+        ctx.set_option("propagator_format", self.propagator_format)
         self.propagator_nnz = nnz.value
         for name, cls in self.mechanisms.items():
             if issubclass(cls, Kinetic):

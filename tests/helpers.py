@@ -66,13 +66,14 @@ def oracle_case(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(
 
 def gpu_model(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(), precision="f32",
               path="batched", tolerance=None, probes=(), insert_as_created=False, kinetic=False,
-              conserve=False):
+              conserve=False, fmt="rows"):
     """The same case through the public RxD_Model API."""
     import neuwon_gb300 as nw
     hh_kw = dict(hh_kw or {})
     kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
     if conserve:
         kw["propagator_conserve"] = True
+    kw["propagator_format"] = fmt
     mechs = [nw.HH.configure(**hh_kw)] + ([nw.Kinetic] if kinetic else [])
     m = nw.RxD_Model(time_step=time_step, temperature=celsius, precision=precision, path=path,
                      mechanisms=mechs, **kw)

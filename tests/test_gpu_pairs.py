@@ -1,0 +1,97 @@
+"""The pair format of the batched path: each coupling (i, j) stored once and
+applied to both segments through detailed balance (c_i P_ij = c_j P_ji), with
+fixed-point accumulation so the result does not depend on the order of the
+atomic adds."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import neuwon_gb300 as nw
+from neuwon_gb300.morphology import EPSILON, random_tree
+from tests.helpers import FIXTURES, gpu_model, run_with_clamps, tree11
+
+F = np.load(FIXTURES)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", ["hh11", "hh200"])
+def test_f64_pairs_match_reference_fixture(name):
+    cases = {"hh11": ([tree11()], [(0, 0, .1, 5., 1.), (0, 0, .1, 15., 1.)], {}, True),
+             "hh200": ([random_tree(200, seed=11)], [(0, 0, 0.2, 5., 20.)], dict(ena=50., ek=-77., el=-54.3), False)}
+    trees, clamps, hh_kw, as_created = cases[name]
+    ref = F[name + "_trace"]
+    m, neurons, offs, recs = gpu_model(trees, clamps, hh_kw=hh_kw, precision="f64", probes=list(F[name + "_probes"]),
+                                       insert_as_created=as_created, fmt="pairs")
+    run_with_clamps(m, clamps, offs, len(ref) - 1)
+    got = np.array([r.get_data() for r in recs]).T
+    assert np.abs(got - ref).max() < 1e-7
+    assert m._ctx.get_option("propagator_format") == 1
+    m.close()
+
+
+def test_f32_pairs_single_neuron_config_matches_reference():
+    clamps = [(0, 0, 0.2, 5.0, 75.0)]
+    m, _, offs, recs = gpu_model([random_tree(2000, seed=0)], clamps, hh_kw=dict(ena=50.0, ek=-77.0, el=-54.3),
+                                 precision="f32", tolerance=1e-8, conserve=True, probes=list(F["c1_probes"]),
+                                 fmt="pairs")
+    worst = 0.0
+    for k in range(1000):
+        for (ti, s, nA, start, dur) in clamps:
+            if m.clock.is_now(start):
+                nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance()
+        if (k + 1) % 100 == 0:
+            worst = max(worst, np.abs(m.get_data("Segment.voltage") - F[f"c1_snap{k + 1}"]).max())
+    assert worst < 0.1, worst
+    assert int(m.get_data("Neuron.spike_count")[0]) == int(F["c1_ap"].sum())
+    m.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_pairs_equal_rows_with_global_accumulators(precision):
+    """A 19,500-segment neuron keeps its sums in global memory (shared memory holds
+    fewer), the small ones in shared memory; both agree with the row format."""
+    trees = [random_tree(19500, seed=2), random_tree(3000, seed=3), random_tree(700, seed=4)]
+    clamps = [(0, 0, 3.0, 0.0, 50.0), (1, 0, 0.5, 0.0, 50.0), (2, 0, 0.3, 0.0, 50.0)]
+    out = []
+    for fmt in ("rows", "pairs"):
+        m, _, offs, _ = gpu_model(trees, clamps, precision=precision, tolerance=1e-8, conserve=True, fmt=fmt,
+                                  kinetic=True)
+        for (ti, s, nA, start, dur) in clamps:
+            nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance(300)
+        out.append((m.get_data("Segment.voltage"), m.get_data("Neuron.spike_count")))
+        m.close()
+    tol = 1e-9 if precision == "f64" else 2e-3
+    assert np.abs(out[0][0] - out[1][0]).max() < tol
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_pairs_are_deterministic():
+    trees = [random_tree(800, seed=s) for s in range(6)]
+    clamps = [(k, 0, 0.4, 0.0, 30.0) for k in range(6)]
+    outs = []
+    for _ in range(2):
+        m, _, offs, _ = gpu_model(trees, clamps, precision="f32", tolerance=1e-8, conserve=True, fmt="pairs")
+        for (ti, s, nA, start, dur) in clamps:
+            nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance(200)
+        outs.append(m.get_data("Segment.voltage"))
+        m.close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_pairs_need_a_built_propagator():
+    m, _, _, _ = gpu_model([random_tree(50, seed=1)], [], precision="f64")
+    m._sync()
+    n = m._n
+    rowptr = np.arange(n + 1, dtype=np.int64)
+    col = np.arange(n, dtype=np.int64)
+    val = np.ones(n)
+    m._ctx.call("nw_propagator_set_csr", n, rowptr.ctypes.data_as(ctypes.c_void_p),
+                col.ctypes.data_as(ctypes.c_void_p), val.ctypes.data_as(ctypes.c_void_p), n)
+    rc = m._ctx.lib.nw_set_option(m._ctx.handle, b"propagator_format", 1)
+    assert rc == -3                                                    # NW_ERR_STATE
+    m.close()
