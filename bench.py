@@ -33,7 +33,7 @@ METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoi
 # neurons, 5,593,190 segments): 1,741.6 GB per launch.  Command and figures:
 # profiles/batched_advance_kernel.md.
 NCU_TRAFFIC_PER_SEGMENT_STEP = 6227.5
-NCU_TRAFFIC_CONFIG = (1e-8, 5593190)
+NCU_TRAFFIC_CONFIG = ("rows", 1e-8, 5593190)
 
 
 def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
@@ -43,13 +43,16 @@ def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
     return 2 * (8 * r + 4) + 4 * (2 + 2 * s_total + p_seg + 1)
 
 
-def format_bytes_per_segment_step(r_stored, prec=4):
+def format_bytes_per_segment_step(r_stored, prec=4, pairs=False):
     """Compulsory HBM bytes of this implementation's layout per segment-step:
-    per half step, (value + u16 column) per stored entry, an 8 B row pointer, the
-    leak, V read + write, kI and kG, HH gates (3) and coefficients (3), the na8 open
-    state and coefficient; per step the mechanism update reads V and reads + writes
-    3 HH gates and 8 na8 states."""
+    per half step, (value + u16 column) per stored entry (pair format: per stored
+    pair), an 8 B row pointer, the leak (pairs: and c_max / c_i), V read + write,
+    kI and kG, HH gates (3) and coefficients (3), the na8 open state and
+    coefficient; per step the mechanism update reads V and reads + writes 3 HH
+    gates and 8 na8 states."""
     per_half = r_stored * (prec + 2) + 8 + prec + 2 * prec + 2 * prec + 6 * prec + 2 * prec
+    if pairs:
+        per_half += prec
     mech = prec + 2 * (3 + 8) * prec
     return 2 * per_half + mech
 
@@ -168,14 +171,14 @@ def log(msg):
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
-def accuracy(trees, currents, tol, device, steps, ref_tol):
+def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows"):
     """FP32 batched at the bench tolerance against the FP64 batched path with a propagator
     pruned at ref_tol (both charge-conserving)."""
     from neuwon_gb300 import Segment, TimeSeries
     from neuwon_gb300.workloads import build_model
     t0 = time.perf_counter()
     ref, nref = build_model(trees, currents, precision="f64", tolerance=ref_tol, conserve=True, device=device)
-    test, ntest = build_model(trees, currents, precision="f32", tolerance=tol, conserve=True, device=device)
+    test, ntest = build_model(trees, currents, precision="f32", tolerance=tol, conserve=True, device=device, fmt=fmt)
     probes = []
     for m, ns in ((ref, nref), (test, ntest)):
         probes.append([TimeSeries().record(nr.root, "voltage") for nr in ns])
@@ -353,6 +356,8 @@ def main():
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
     ap.add_argument("--autotune", type=int, default=10,
                     help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
+    ap.add_argument("--format", default="pairs", choices=["rows", "pairs"],
+                    help="propagator storage: every P_ij in its row, or each coupling once (detailed balance)")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
@@ -395,7 +400,8 @@ def main():
     extra = {}
     if not args.quick and rank == 0:
         k = args.acc_neurons
-        extra["accuracy"] = accuracy(trees[:k], currents[:k], args.tol, local, args.acc_steps, args.ref_tol)
+        extra["accuracy"] = accuracy(trees[:k], currents[:k], args.tol, local, args.acc_steps, args.ref_tol,
+                                     args.format)
         log(f"accuracy: {extra['accuracy']}")
         extra["plain_fp64"] = plain_timing(trees[:64], currents[:64], args.tol, local)
         log(f"plain: {extra['plain_fp64']}")
@@ -406,7 +412,7 @@ def main():
         log(f"adjoint: {extra['adjoint']}")
     t_build = time.perf_counter()
     model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, conserve=True,
-                                 device=local)
+                                 device=local, fmt=args.format)
     log(f"host model built in {time.perf_counter() - t_build:.1f} s")
     model._sync()
     ctx = model._ctx
@@ -504,7 +510,7 @@ def main():
         peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     B_alg = algorithmic_bytes_per_segment_step(r_kept)
-    B_fmt = format_bytes_per_segment_step(r_stored)
+    B_fmt = format_bytes_per_segment_step(r_stored, pairs=args.format == "pairs")
     achieved = B_alg * n / (per_step_launch_ms * 1e-3) / 1e9
     achieved_fmt = B_fmt * n / (per_step_launch_ms * 1e-3) / 1e9
 
@@ -525,6 +531,7 @@ def main():
                                "FP32 state, FP64-built propagator",
                    "segments": n, "neurons": len(neurons), "propagator_tolerance": args.tol,
                    "propagator_pruning": "charge-conserving (pruned mass returned to the diagonal)",
+                   "propagator_format": args.format,
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
                    "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
                    "autotune": tuned, "cuda_graph": {"replayed": graph_replayed, "launches_in_graph": n_launch},
@@ -536,7 +543,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": (NCU_TRAFFIC_PER_SEGMENT_STEP * n * F
-                                 if (args.tol, n) == NCU_TRAFFIC_CONFIG else None),
+                                 if (args.format, args.tol, n) == NCU_TRAFFIC_CONFIG else None),
                      "traffic_unit": f"bytes per launch of {F} steps (ncu dram__bytes_read+write)",
                      "algorithmic_bytes_per_launch": B_alg * n * F,
                      "peak_source": peak_src,

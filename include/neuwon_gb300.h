@@ -287,6 +287,11 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
 
 /* Named options.  "reset_clock" (any value): back to time 0 (clock, detector state,
  * probes; conductances count as not yet computed) without touching V or gates.
+ * "propagator_format" (default 0): 0 = every P_ij in its row; 1 = pairs: each
+ * coupling (i, j) stored once, in the row of the segment with the smaller
+ * capacitance, and applied to both rows through detailed balance c_i P_ij = c_j P_ji
+ * (propagators from nw_propagator_build only; kept when the other row pruned it, so
+ * a pair survives if either P_ij or P_ji reaches the tolerance).
  * "set_steps" (k): resume at step k (clock, input ticks 2k, conductances valid when
  * k > 0 and mechanisms exist; probes start empty), for restoring a checkpoint.
  * "fusion_depth" (default 50, 0 = the whole call in one launch): steps per launch of
@@ -303,7 +308,9 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value);
 int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value);
 
 /* Statistics of the installed propagator: rows, kept entries (with diagonal),
- * stored off-diagonal entries including padding, bytes of the batched format. */
+ * stored off-diagonal entries including padding, bytes of the batched format (of
+ * the pair format when "propagator_format" is 1: stored pairs, bytes with the
+ * per-row c_max / c_i). */
 int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* stored,
                         int64_t* bytes);
 

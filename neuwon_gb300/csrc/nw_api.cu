@@ -609,6 +609,13 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");
     if (rows) *rows = ctx->n_seg;
     if (nnz) *nnz = ctx->nnz64;
+    if (ctx->prop_format == 1) {
+        // Pair format: stored pairs, with c_max / c_i per row besides the leak.
+        NW_CHECK(ensure_flux(ctx));
+        if (stored) *stored = ctx->nnz_f;
+        if (bytes) *bytes = ctx->nnz_f * (2 + ctx->precision) + ctx->n_seg * (8 + 2 * ctx->precision);
+        return NW_OK;
+    }
     if (stored) *stored = ctx->b_ok ? ctx->nnz_b : ctx->nnz_w;
     if (bytes) *bytes = ctx->b_ok ? ctx->nnz_b * (2 + ctx->precision) + ctx->n_seg * (8 + ctx->precision)
                                   : ctx->nnz_w * (4 + ctx->precision) + ctx->n_seg * (8 + ctx->precision);
