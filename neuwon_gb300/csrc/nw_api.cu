@@ -1051,6 +1051,13 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
     if (nm == "cuda_graph") { ctx->use_graph = value != 0; return NW_OK; }
+    if (nm == "pair_shared_limit") {
+        // Largest neuron whose pair sums stay in shared memory (-1: as many as fit);
+        // larger ones use global memory.  The integer sums are the same either way.
+        if (value < -1 || value > INT32_MAX) return fail(ctx, NW_ERR_ARG, "pair_shared_limit out of range");
+        ctx->pair_shared_limit = (int)value;
+        return NW_OK;
+    }
     if (nm == "propagator_format") {
         // 0: rows (every P_ij stored in its row); 1: pairs (each coupling once,
         // applied to both rows through detailed balance; built propagators only).

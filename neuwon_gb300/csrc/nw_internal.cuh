@@ -172,6 +172,7 @@ struct nw_ctx {
     nw::DevBuf f_rowptr, f_col, f_val, f_leak, f_rc;   // i64, u16, real, real, real (c_max / c_i)
     nw::DevBuf f_acc;                                  // i64 [n_seg] accumulators of neurons too large for shared memory
     int prop_format = 0;                               // 0: rows, 1: pairs
+    int pair_shared_limit = -1;                        // cap on neurons with shared-memory sums (-1: none)
 
     // Mechanisms.
     nw::HHState hh;

@@ -578,6 +578,7 @@ static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
     int acc_cap = 0;
     if (FLUX && xs_bytes + static_smem < ctx->smem_optin) {
         acc_cap = (int)std::min<int64_t>(ctx->max_neuron, (int64_t)((ctx->smem_optin - static_smem - xs_bytes) / 8));
+        if (ctx->pair_shared_limit >= 0) acc_cap = std::min(acc_cap, ctx->pair_shared_limit);
         smem += (size_t)acc_cap * 8;
     }
     if (smem + static_smem > ctx->smem_optin)
