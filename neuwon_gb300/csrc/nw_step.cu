@@ -221,19 +221,34 @@ __device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, i
 
 // ------------------------------------------------------------ pair format
 
-// Every stored pair (i, j) of a neuron adds t = w (x_j - x_i) to row i's sum and
-// subtracts it from row j's (w = c_i P_ij / c_max, detailed balance c_i P_ij =
-// c_j P_ji), so each coupling is read from HBM once instead of twice.  The sums
-// are 2^-40 fixed point, so integer atomic adds give the same bits in any order.
-constexpr double kFluxScale = 1099511627776.0;   // 2^40
-__device__ __forceinline__ long long flux_fix(float t) { return __float2ll_rn(t * (float)kFluxScale); }
-__device__ __forceinline__ long long flux_fix(double t) { return __double2ll_rn(t * kFluxScale); }
-__device__ __forceinline__ float flux_unfix(long long q, float scale) { return __ll2float_rn(q) * scale; }
-__device__ __forceinline__ double flux_unfix(long long q, double scale) { return __ll2double_rn(q) * scale; }
+// Every stored pair (i, j) of a neuron adds t = w (x_j - x_i) to row i and
+// subtracts it from row j (w = c_i P_ij / c_max; detailed balance c_i P_ij =
+// c_j P_ji), so each coupling is read from HBM once instead of twice.  The
+// contributions are summed per segment in fixed point, in mV (scaled by
+// c_max / c of the receiving segment), so integer atomic adds give the same
+// bits in any order.  FP32 state: 32-bit sums with 2^-22 mV resolution (range
+// +-512 mV, checked); FP64 state: 64-bit sums with 2^-40 mV resolution.
+template <typename real> struct PairSum;
+template <> struct PairSum<float> {
+    using acc_t = unsigned int;
+    static constexpr float kScale = 4194304.0f;              // 2^22
+    static constexpr float kLimit = 400.0f;                   // |x| beyond this could overflow a sum
+    static __device__ __forceinline__ acc_t fix(float t) { return (acc_t)__float2int_rn(t * kScale); }
+    static __device__ __forceinline__ float unfix(acc_t q) { return (float)(int)q * (1.0f / kScale); }
+};
+template <> struct PairSum<double> {
+    using acc_t = unsigned long long;
+    static constexpr double kScale = 1099511627776.0;         // 2^40
+    static constexpr double kLimit = 1e6;
+    static __device__ __forceinline__ acc_t fix(double t) { return (acc_t)__double2ll_rn(t * kScale); }
+    static __device__ __forceinline__ double unfix(acc_t q) { return (double)(long long)q * (1.0 / kScale); }
+};
 
 template <typename real, int LPR>
 __device__ __forceinline__ void propagate_flux(const StepArgs<real>& a, int64_t base, int n,
-                                               const real* __restrict__ xs, unsigned long long* acc) {
+                                               const real* __restrict__ xs, const real* __restrict__ rcs,
+                                               typename PairSum<real>::acc_t* acc) {
+    using PS = PairSum<real>;
     constexpr int UNROLL = 2;
     constexpr int GPW = 32 / LPR;
     const int lane = threadIdx.x & 31;
@@ -268,32 +283,31 @@ __device__ __forceinline__ void propagate_flux(const StepArgs<real>& a, int64_t 
                     const real t0 = v[u][0] * (xs[cc[u].x] - xi), t1 = v[u][1] * (xs[cc[u].y] - xi);
                     const real t2 = v[u][2] * (xs[cc[u].z] - xi), t3 = v[u][3] * (xs[cc[u].w] - xi);
                     kahan_add(s, c, (t0 + t1) + (t2 + t3));
-                    if (t0 != real(0)) atomicAdd(acc + cc[u].x, (unsigned long long)(-flux_fix(t0)));
-                    if (t1 != real(0)) atomicAdd(acc + cc[u].y, (unsigned long long)(-flux_fix(t1)));
-                    if (t2 != real(0)) atomicAdd(acc + cc[u].z, (unsigned long long)(-flux_fix(t2)));
-                    if (t3 != real(0)) atomicAdd(acc + cc[u].w, (unsigned long long)(-flux_fix(t3)));
+                    if (t0 != real(0)) atomicAdd(acc + cc[u].x, PS::fix(-t0 * rcs[cc[u].x]));
+                    if (t1 != real(0)) atomicAdd(acc + cc[u].y, PS::fix(-t1 * rcs[cc[u].y]));
+                    if (t2 != real(0)) atomicAdd(acc + cc[u].z, PS::fix(-t2 * rcs[cc[u].z]));
+                    if (t3 != real(0)) atomicAdd(acc + cc[u].w, PS::fix(-t3 * rcs[cc[u].w]));
                 }
             }
         }
         real t = s - c;
 #pragma unroll
         for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-        if (valid && l == 0) atomicAdd(acc + row, (unsigned long long)flux_fix(t));
+        if (valid && l == 0) atomicAdd(acc + row, PS::fix(t * rcs[row]));
     }
 }
 
-// V_i = x_i - leak_i x_i + (sum of row i's pair terms) * c_max / c_i; resets the sums.
+// V_i = x_i - leak_i x_i + (sum of the pair terms reaching i); resets the sums.
 template <typename real>
 __device__ __forceinline__ void flux_finalize(const StepArgs<real>& a, int64_t base, int n, const real* xs,
-                                              unsigned long long* acc) {
-    const real unit = (real)(1.0 / kFluxScale);
+                                              typename PairSum<real>::acc_t* acc) {
     for (int li = threadIdx.x; li < n; li += blockDim.x) {
         const int64_t i = base + li;
         const real xi = xs[li];
-        const long long q = (long long)acc[li];
-        acc[li] = 0ull;
-        const real vnew = (xi - a.fleak[i] * xi) + flux_unfix(q, a.frc[i] * unit);
-        if (!isfinite(vnew) || !isfinite(xi)) atomicOr(a.status, kStatusNonFinite);
+        const typename PairSum<real>::acc_t q = acc[li];
+        acc[li] = 0;
+        const real vnew = (xi - a.fleak[i] * xi) + PairSum<real>::unfix(q);
+        if (!isfinite(vnew) || !(fabs(xi) < PairSum<real>::kLimit)) atomicOr(a.status, kStatusNonFinite);
         a.V[i] = vnew;
     }
 }
@@ -341,12 +355,17 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         const int64_t base = a.neuron_start[j];
         const int n = (int)(a.neuron_start[j + 1] - base);
         if (FLUX) {
-            // The finalize pass leaves the accumulators at zero for the next half step.
+            // c_max / c of the neuron's segments next to x; sums start at zero (the
+            // finalize pass leaves them at zero for the next half step).
+            using acc_t = typename PairSum<real>::acc_t;
+            real* rc = reinterpret_cast<real*>(smem_raw + xs_bytes);
+            for (int li = threadIdx.x; li < n; li += blockDim.x) rc[li] = a.frc[base + li];
             if (n <= a.facc_cap) {
-                unsigned long long* z = reinterpret_cast<unsigned long long*>(smem_raw + xs_bytes);
-                for (int li = threadIdx.x; li < n; li += blockDim.x) z[li] = 0ull;
+                acc_t* z = reinterpret_cast<acc_t*>(smem_raw + 2 * xs_bytes);
+                for (int li = threadIdx.x; li < n; li += blockDim.x) z[li] = 0;
             } else {
-                for (int li = threadIdx.x; li < n; li += blockDim.x) a.facc[base + li] = 0ull;
+                acc_t* z = reinterpret_cast<acc_t*>(a.facc) + base;
+                for (int li = threadIdx.x; li < n; li += blockDim.x) z[li] = 0;
             }
         }
         if (tid == 0) {
@@ -366,9 +385,11 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         // Pair-format accumulators: in shared memory behind x when the neuron fits,
         // else the neuron's slice of a global array (each branch keeps its address
         // space known to the compiler).
+        using acc_t = typename PairSum<real>::acc_t;
         const bool acc_in_smem = n <= a.facc_cap;
-        unsigned long long* const sacc = reinterpret_cast<unsigned long long*>(smem_raw + xs_bytes);
-        unsigned long long* const gacc = a.facc + base;
+        real* const rcs = reinterpret_cast<real*>(smem_raw + xs_bytes);
+        acc_t* const sacc = reinterpret_cast<acc_t*>(smem_raw + 2 * xs_bytes);
+        acc_t* const gacc = reinterpret_cast<acc_t*>(a.facc) + base;
         // Mechanism instance ranges of this neuron.
         int64_t ib = 0, ie = 0, kb = 0, ke = 0, yb = 0, ye = 0;
         if (a.syn_on) { yb = a.syn_neuron_ptr[j]; ye = a.syn_neuron_ptr[j + 1]; }
@@ -415,11 +436,11 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                 __syncthreads();
                 if (FLUX) {
                     if (acc_in_smem) {
-                        propagate_flux<real, LPR>(a, base, n, xs, sacc);
+                        propagate_flux<real, LPR>(a, base, n, xs, rcs, sacc);
                         __syncthreads();
                         flux_finalize(a, base, n, xs, sacc);
                     } else {
-                        propagate_flux<real, LPR>(a, base, n, xs, gacc);
+                        propagate_flux<real, LPR>(a, base, n, xs, rcs, gacc);
                         __syncthreads();
                         flux_finalize(a, base, n, xs, gacc);
                     }
@@ -576,10 +597,14 @@ static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
     if (BULK) smem += (size_t)(threads / 32) * kBulkStages * (BulkGeom<real>::kStageBytes + 8);
     const size_t static_smem = 4096;
     int acc_cap = 0;
-    if (FLUX && xs_bytes + static_smem < ctx->smem_optin) {
-        acc_cap = (int)std::min<int64_t>(ctx->max_neuron, (int64_t)((ctx->smem_optin - static_smem - xs_bytes) / 8));
+    if (FLUX) {
+        // x | c_max / c | pair sums (as many neurons' sums as fit; larger ones use global memory)
+        smem += xs_bytes;
+        const size_t acc_bytes = sizeof(typename PairSum<real>::acc_t);
+        if (smem + static_smem < ctx->smem_optin)
+            acc_cap = (int)std::min<int64_t>(ctx->max_neuron, (int64_t)((ctx->smem_optin - static_smem - smem) / acc_bytes));
         if (ctx->pair_shared_limit >= 0) acc_cap = std::min(acc_cap, ctx->pair_shared_limit);
-        smem += (size_t)acc_cap * 8;
+        smem += (size_t)acc_cap * acc_bytes;
     }
     if (smem + static_smem > ctx->smem_optin)
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron of " + std::to_string(ctx->max_neuron) +
