@@ -358,10 +358,12 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
             // c_max / c of the neuron's segments next to x; sums start at zero (the
             // finalize pass leaves them at zero for the next half step).
             using acc_t = typename PairSum<real>::acc_t;
-            real* rc = reinterpret_cast<real*>(smem_raw + xs_bytes);
-            for (int li = threadIdx.x; li < n; li += blockDim.x) rc[li] = a.frc[base + li];
+            if (a.frc_smem) {
+                real* rc = reinterpret_cast<real*>(smem_raw + xs_bytes);
+                for (int li = threadIdx.x; li < n; li += blockDim.x) rc[li] = a.frc[base + li];
+            }
             if (n <= a.facc_cap) {
-                acc_t* z = reinterpret_cast<acc_t*>(smem_raw + 2 * xs_bytes);
+                acc_t* z = reinterpret_cast<acc_t*>(smem_raw + (a.frc_smem ? 2 : 1) * xs_bytes);
                 for (int li = threadIdx.x; li < n; li += blockDim.x) z[li] = 0;
             } else {
                 acc_t* z = reinterpret_cast<acc_t*>(a.facc) + base;
@@ -387,8 +389,8 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         // space known to the compiler).
         using acc_t = typename PairSum<real>::acc_t;
         const bool acc_in_smem = n <= a.facc_cap;
-        real* const rcs = reinterpret_cast<real*>(smem_raw + xs_bytes);
-        acc_t* const sacc = reinterpret_cast<acc_t*>(smem_raw + 2 * xs_bytes);
+        const real* const rcs = a.frc_smem ? reinterpret_cast<const real*>(smem_raw + xs_bytes) : a.frc + base;
+        acc_t* const sacc = reinterpret_cast<acc_t*>(smem_raw + (a.frc_smem ? 2 : 1) * xs_bytes);
         acc_t* const gacc = reinterpret_cast<acc_t*>(a.facc) + base;
         // Mechanism instance ranges of this neuron.
         int64_t ib = 0, ie = 0, kb = 0, ke = 0, yb = 0, ye = 0;
@@ -586,6 +588,7 @@ struct BatchedCfg {
     size_t smem;
     int xs_bytes;
     int acc_cap;      // pair format: largest neuron whose accumulators fit in shared memory
+    int rc_smem;      // pair format: c_max / c staged in shared memory
 };
 
 template <typename real, int LPR, bool BULK, bool FLUX>
@@ -597,9 +600,11 @@ static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
     if (BULK) smem += (size_t)(threads / 32) * kBulkStages * (BulkGeom<real>::kStageBytes + 8);
     const size_t static_smem = 4096;
     int acc_cap = 0;
+    int rc_smem = 0;
     if (FLUX) {
-        // x | c_max / c | pair sums (as many neurons' sums as fit; larger ones use global memory)
-        smem += xs_bytes;
+        // x | c_max / c (when it fits) | pair sums (as many neurons' sums as fit;
+        // larger ones use global memory)
+        if (2 * xs_bytes + static_smem <= ctx->smem_optin) { smem += xs_bytes; rc_smem = 1; }
         const size_t acc_bytes = sizeof(typename PairSum<real>::acc_t);
         if (smem + static_smem < ctx->smem_optin)
             acc_cap = (int)std::min<int64_t>(ctx->max_neuron, (int64_t)((ctx->smem_optin - static_smem - smem) / acc_bytes));
@@ -620,6 +625,7 @@ static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
     c.smem = smem;
     c.xs_bytes = (int)xs_bytes;
     c.acc_cap = acc_cap;
+    c.rc_smem = rc_smem;
     return NW_OK;
 }
 
@@ -774,6 +780,7 @@ static int launch_batched(nw_ctx* ctx, int k_steps) {
     NW_CHECK(config_batched<real>(ctx, c));
     StepArgs<real> a = make_args<real>(ctx, k_steps);
     a.facc_cap = c.acc_cap;
+    a.frc_smem = c.rc_smem;
     NW_CHECK(push_clock(ctx));
     if (ctx->use_graph) return launch_graph<real>(ctx, c, a, k_steps);
     return enqueue_batched<real>(ctx, c, a, k_steps);
@@ -786,6 +793,7 @@ static int prepare_graph_t(nw_ctx* ctx, int k_steps) {
     NW_CHECK(config_batched<real>(ctx, c));
     StepArgs<real> a = make_args<real>(ctx, k_steps);
     a.facc_cap = c.acc_cap;
+    a.frc_smem = c.rc_smem;
     return launch_graph<real>(ctx, c, a, k_steps, false);
 }
 

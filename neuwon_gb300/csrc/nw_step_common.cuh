@@ -89,7 +89,7 @@ struct StepArgs {
     const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
     // pair ("flux") propagator: rows of owned pairs, leak, c_max / c_i, global accumulators
     const int64_t* frow; const uint16_t* fcol; const real* fval; const real* fleak; const real* frc;
-    unsigned long long* facc; int facc_cap;
+    unsigned long long* facc; int facc_cap; int frc_smem;
     // wide propagator (global int32 columns)
     const int64_t* wrow; const int32_t* wcol; const real* wval; const real* wleak;
     // hh
