@@ -22,6 +22,11 @@ struct DevBuf {
 constexpr int kMaxClampsPerNeuron = 16;
 constexpr int kMaxProbesPerNeuron = 64;
 
+// Fixed-point scales of the pair format's per-segment sums (mV): 2^22 with FP32
+// state (32-bit sums), 2^40 with FP64 state (64-bit sums).
+constexpr double kPairScaleF32 = 4194304.0;
+constexpr double kPairScaleF64 = 1099511627776.0;
+
 // Status bits written by kernels into the context's status word.
 constexpr int kStatusNonFinite = 1;
 constexpr int kStatusWaitTimeout = 16;   // a bounded wait on an mbarrier gave up

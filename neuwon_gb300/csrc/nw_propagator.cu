@@ -534,7 +534,9 @@ __global__ void flux_fill_kernel(int64_t n, const int64_t* row_base, const doubl
     for (int64_t k = ob + lane; k < frow[r + 1]; k += 32) { fcol[k] = (uint16_t)(r - base); fval[k] = real(0); }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
-    if (lane == 0) { leak[r] = (real)(1.0 - sum); rc[r] = (real)(cmax / cap[r]); }
+    // c_max / c_r times the fixed-point scale of the pair sums.
+    const double fixed = sizeof(real) == 4 ? kPairScaleF32 : kPairScaleF64;
+    if (lane == 0) { leak[r] = (real)(1.0 - sum); rc[r] = (real)(cmax / cap[r] * fixed); }
 }
 
 void free_flux(nw_ctx* ctx) {

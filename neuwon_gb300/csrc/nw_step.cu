@@ -231,16 +231,16 @@ __device__ __forceinline__ void propagate_neuron_bulk(const StepArgs<real>& a, i
 template <typename real> struct PairSum;
 template <> struct PairSum<float> {
     using acc_t = unsigned int;
-    static constexpr float kScale = 4194304.0f;              // 2^22
+    static constexpr float kScale = (float)kPairScaleF32;
     static constexpr float kLimit = 400.0f;                   // |x| beyond this could overflow a sum
-    static __device__ __forceinline__ acc_t fix(float t) { return (acc_t)__float2int_rn(t * kScale); }
+    static __device__ __forceinline__ acc_t fix_scaled(float t) { return (acc_t)__float2int_rn(t); }
     static __device__ __forceinline__ float unfix(acc_t q) { return (float)(int)q * (1.0f / kScale); }
 };
 template <> struct PairSum<double> {
     using acc_t = unsigned long long;
-    static constexpr double kScale = 1099511627776.0;         // 2^40
+    static constexpr double kScale = kPairScaleF64;
     static constexpr double kLimit = 1e6;
-    static __device__ __forceinline__ acc_t fix(double t) { return (acc_t)__double2ll_rn(t * kScale); }
+    static __device__ __forceinline__ acc_t fix_scaled(double t) { return (acc_t)__double2ll_rn(t); }
     static __device__ __forceinline__ double unfix(acc_t q) { return (double)(long long)q * (1.0 / kScale); }
 };
 
@@ -283,17 +283,18 @@ __device__ __forceinline__ void propagate_flux(const StepArgs<real>& a, int64_t 
                     const real t0 = v[u][0] * (xs[cc[u].x] - xi), t1 = v[u][1] * (xs[cc[u].y] - xi);
                     const real t2 = v[u][2] * (xs[cc[u].z] - xi), t3 = v[u][3] * (xs[cc[u].w] - xi);
                     kahan_add(s, c, (t0 + t1) + (t2 + t3));
-                    if (t0 != real(0)) atomicAdd(acc + cc[u].x, PS::fix(-t0 * rcs[cc[u].x]));
-                    if (t1 != real(0)) atomicAdd(acc + cc[u].y, PS::fix(-t1 * rcs[cc[u].y]));
-                    if (t2 != real(0)) atomicAdd(acc + cc[u].z, PS::fix(-t2 * rcs[cc[u].z]));
-                    if (t3 != real(0)) atomicAdd(acc + cc[u].w, PS::fix(-t3 * rcs[cc[u].w]));
+                    // Padding (w = 0, column = the row) adds zero to the row's own sum.
+                    atomicAdd(acc + cc[u].x, PS::fix_scaled(-t0 * rcs[cc[u].x]));
+                    atomicAdd(acc + cc[u].y, PS::fix_scaled(-t1 * rcs[cc[u].y]));
+                    atomicAdd(acc + cc[u].z, PS::fix_scaled(-t2 * rcs[cc[u].z]));
+                    atomicAdd(acc + cc[u].w, PS::fix_scaled(-t3 * rcs[cc[u].w]));
                 }
             }
         }
         real t = s - c;
 #pragma unroll
         for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-        if (valid && l == 0) atomicAdd(acc + row, PS::fix(t * rcs[row]));
+        if (valid && l == 0) atomicAdd(acc + row, PS::fix_scaled(t * rcs[row]));
     }
 }
 
@@ -359,6 +360,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
             // finalize pass leaves them at zero for the next half step).
             using acc_t = typename PairSum<real>::acc_t;
             if (a.frc_smem) {
+                // c_max / c times the fixed-point scale: one multiply per pair term.
                 real* rc = reinterpret_cast<real*>(smem_raw + xs_bytes);
                 for (int li = threadIdx.x; li < n; li += blockDim.x) rc[li] = a.frc[base + li];
             }
