@@ -276,6 +276,45 @@ def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
                       "(charge-conserving), targets from FP64 runs with densities +-30 %"}
 
 
+def network_leg(device, steps, neurons=4096, synapses=2_000_000):
+    """Config 5 shape: 4,096 seeded neurons of 200-5,000 segments (log-uniform), HH on every
+    segment, 2 M synapses (AMPA + NMDA with Mg block), lognormal weights (mu -1, sigma 0.5,
+    nS), delays U(1, 20) ms, FP32, dt 0.1 ms, autotuned fusion depth (capped at the shortest
+    delay), a bounded sample of the 2 s run."""
+    from neuwon_gb300.synapses import random_network
+    from neuwon_gb300.workloads import batched_currents, batched_trees, build_model
+    t0 = time.perf_counter()
+    trees = batched_trees(neurons, seed=7, processes=min(16, os.cpu_count() or 1), lo=200, hi=5000)
+    currents = batched_currents(neurons, seed=7)
+    m, _ = build_model(trees, currents, precision="f32", tolerance=1e-8, conserve=True, device=device,
+                       kinetic=False)
+    net = random_network([len(t) for t in trees], synapses, 7)
+    offs = np.cumsum([0] + [len(t) for t in trees])[:-1]
+    m.add_synapses(net["pre"], offs[net["post_neuron"]] + net["post_local"], net["weight_nS"], net["weight_nS"],
+                   net["delay_steps"] * 0.1)
+    m._sync()
+    build_s = time.perf_counter() - t0
+    tuned = m.autotune(5)
+    m.advance(20)
+    m._ctx.call("nw_synchronize")
+    ev0 = int(m.get_data("Synapse.events").sum())
+    sp0 = int(m.get_data("Neuron.spike_count").sum())
+    t0 = time.perf_counter()
+    m.advance(steps)
+    m._ctx.call("nw_synchronize")
+    dt = time.perf_counter() - t0
+    n = m._n
+    out = {"ms_per_step": 1e3 * dt / steps, "segment_steps_per_s": n * steps / dt, "segments": n,
+           "synapses": synapses, "steps": steps, "build_s": build_s,
+           "events_delivered": int(m.get_data("Synapse.events").sum()) - ev0,
+           "spikes": int(m.get_data("Neuron.spike_count").sum()) - sp0,
+           "fusion_depth": min(tuned["fusion_depth"], int(net["delay_steps"].min())), "autotune": tuned,
+           "config": f"{neurons} HH neurons, log-uniform 200-5000 segments, {synapses} AMPA+NMDA synapses, "
+                     "delays U(1, 20) ms, FP32, dt 0.1 ms, propagator 1e-8 (charge-conserving)"}
+    m.close()
+    return out
+
+
 def _lib_ptr(a):
     from neuwon_gb300 import _lib
     return _lib.ptr(a)
@@ -363,6 +402,8 @@ def main():
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
     ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu/adjoint legs")
     ap.add_argument("--adjoint-steps", type=int, default=800)
+    ap.add_argument("--network-steps", type=int, default=200,
+                    help="steps of the 4,096-neuron, 2 M-synapse network leg (0 = skip)")
     ap.add_argument("--precision-study", action="store_true",
                     help="run only the 1 M-segment FP32-vs-FP64 calcium precision study")
     ap.add_argument("--study-segments", type=int, default=1_000_000)
@@ -410,6 +451,9 @@ def main():
     if not args.quick and rank == 0 and args.adjoint_steps > 0:
         extra["adjoint"] = adjoint_leg(local, args.adjoint_steps)
         log(f"adjoint: {extra['adjoint']}")
+    if not args.quick and rank == 0 and args.network_steps > 0:
+        extra["network"] = network_leg(local, args.network_steps)
+        log(f"network: {extra['network']}")
     t_build = time.perf_counter()
     model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, conserve=True,
                                  device=local, fmt=args.format)
