@@ -428,7 +428,8 @@ def main():
     # Trees are generated in a spawned pool before any CUDA work.
     t_setup = time.perf_counter()
     lo, hi = (int(x) for x in args.size_range.split(","))
-    trees = batched_trees(args.neurons, seed=rank, processes=min(16, os.cpu_count() or 1), lo=lo, hi=hi)
+    from neuwon_gb300.replicas import replica_seed
+    trees = batched_trees(args.neurons, seed=replica_seed(rank), processes=min(16, os.cpu_count() or 1), lo=lo, hi=hi)
     currents = batched_currents(args.neurons, seed=rank)
     import torch
     torch.cuda.set_device(local)
@@ -519,12 +520,9 @@ def main():
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * world * K / (ms * 1e-3)
+    from neuwon_gb300.replicas import aggregate
+    agg = aggregate(ev0.elapsed_time(ev1), n, K, dist, device=f"cuda:{local}")
+    ms, n_total, value = agg["ms"], agg["segments"], agg["value"]
     # Average launch of the batched kernel, per fused step (the region holds the
     # n_launch kernels plus one clock write and n_launch 4-byte memsets).
     per_step_launch_ms = ms / K
@@ -543,7 +541,7 @@ def main():
     e2e_s = time.perf_counter() - t0
     model.input_hook.ticks += 2 * (E + 1)
     model.advance_hook.ticks += E + 1
-    e2e_value = n * world * E / e2e_s
+    e2e_value = aggregate(e2e_s * 1e3, n, E, dist, device=f"cuda:{local}")["value"]
     vcheck = vout.numpy()
     finite = bool(np.all(np.isfinite(vcheck)))
 
@@ -573,7 +571,8 @@ def main():
         "config": {"workload": f"batched: {len(neurons)} neurons, log-uniform {lo}-{hi} segments, HH + "
                                "8-state Markov Na on every segment, soma current U(0.05,0.5) nA, dt 0.1 ms, "
                                "FP32 state, FP64-built propagator",
-                   "segments": n, "neurons": len(neurons), "propagator_tolerance": args.tol,
+                   "segments": n_total, "segments_rank0": n, "neurons": len(neurons) * world,
+                   "propagator_tolerance": args.tol,
                    "propagator_pruning": "charge-conserving (pruned mass returned to the diagonal)",
                    "propagator_format": args.format,
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
