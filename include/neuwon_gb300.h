@@ -292,6 +292,11 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * capacitance, and applied to both rows through detailed balance c_i P_ij = c_j P_ji
  * (propagators from nw_propagator_build only; kept when the other row pruned it, so
  * a pair survives if either P_ij or P_ji reaches the tolerance).
+ * "spike_neurons" (N), "spike_neuron_offset" (o), "spike_ring_steps" (R): for a network
+ * split across ranks, taken by the next nw_synapses_set: presynaptic ids are global
+ * (< N), the spike ring covers all N neurons with this model's neuron j at o + j, and
+ * its length is at least R steps (a common value for all ranks); the ranks sum their
+ * rings (own neurons only) after every epoch of at most the shortest delay.
  * "set_steps" (k): resume at step k (clock, input ticks 2k, conductances valid when
  * k > 0 and mechanisms exist; probes start empty), for restoring a checkpoint.
  * "fusion_depth" (default 50, 0 = the whole call in one launch): steps per launch of

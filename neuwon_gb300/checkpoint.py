@@ -69,7 +69,7 @@ def save_sqlite(model, filename):
         rows = [np.asarray(v).tolist() for v in cols.values()]
         _table(cur, table, columns, rows)
     if m._syn is not None:
-        nn = len(m._neuron_root)
+        nn = m._ctx.get_option("spike_neurons")
         words = m._ctx.get_option("synapse_ring_words")
         ring = m._ctx.get_data("Synapse.spike_ring", nn * words, np.uint32).reshape(nn, -1)
         cur.execute("CREATE TABLE SpikeRing (_idx BIGINT NOT NULL, bits BLOB NOT NULL, PRIMARY KEY (_idx))")

@@ -456,8 +456,8 @@ int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int6
                               NW_DTYPE_F64, count);
     }
     if (nm == "Synapse.spike_ring") {
-        // Raw spike bits: n_neuron x ring_words u32 words (steps modulo the ring length).
-        NW_CHECK(need(ctx->syn.n ? ctx->n_neuron * ctx->syn.ring_words : 0));
+        // Raw spike bits: ring_neurons x ring_words u32 words (steps modulo the ring length).
+        NW_CHECK(need(ctx->syn.n ? ctx->syn.ring_neurons * ctx->syn.ring_words : 0));
         if (!count) return NW_OK;
         return upload_convert(ctx, ctx->syn.ring.ptr, NW_DTYPE_U32, host, dtype, count);
     }
@@ -513,7 +513,7 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
         return NW_OK;
     }
     if (nm == "Synapse.spike_ring") {
-        NW_CHECK(need(ctx->syn.n ? ctx->n_neuron * ctx->syn.ring_words : 0));
+        NW_CHECK(need(ctx->syn.n ? ctx->syn.ring_neurons * ctx->syn.ring_words : 0));
         if (!count) return NW_OK;
         return download_convert(ctx, host, dtype, ctx->syn.ring.ptr, NW_DTYPE_U32, count);
     }
@@ -771,9 +771,14 @@ int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron
         return fail(ctx, NW_ERR_ARG, "nw_synapses_set: null arrays");
     if (m > 0 && (pulse_steps < 1 || !(mg >= 0.0) || !std::isfinite(e_syn)))
         return fail(ctx, NW_ERR_ARG, "nw_synapses_set: pulse_steps >= 1, mg >= 0, finite e_syn");
+    // Presynaptic neurons index the spike ring: this model's neurons, or all
+    // ranks' neurons when the network is partitioned ("spike_neurons").
+    const int64_t ring_neurons = ctx->spike_neurons > 0 ? ctx->spike_neurons : ctx->n_neuron;
+    if (ctx->spike_offset < 0 || ctx->spike_offset + ctx->n_neuron > ring_neurons)
+        return fail(ctx, NW_ERR_ARG, "nw_synapses_set: spike_neuron_offset + neurons exceeds spike_neurons");
     int dmin = INT32_MAX, dmax = 0;
     for (int64_t k = 0; k < m; ++k) {
-        if (pre_neuron[k] < 0 || pre_neuron[k] >= ctx->n_neuron)
+        if (pre_neuron[k] < 0 || pre_neuron[k] >= ring_neurons)
             return fail(ctx, NW_ERR_ARG, "nw_synapses_set: presynaptic neuron out of range");
         if (delay_steps[k] < 1 || delay_steps[k] > (1 << 20))
             return fail(ctx, NW_ERR_ARG, "nw_synapses_set: delay must be in [1, 2^20] steps");
@@ -794,9 +799,11 @@ int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron
     // A spike of step t is read up to max_delay steps later while its owner may
     // already have written min_delay (the most steps one launch fuses) newer ones.
     int R = 32;
-    while (R < dmax + dmin + 1) R *= 2;
+    while (R < dmax + dmin + 1 || R < ctx->spike_ring_min) R *= 2;
     Y.ring_steps = R;
     Y.ring_words = R / 32;
+    Y.ring_neurons = ring_neurons;
+    Y.neuron_offset = ctx->spike_offset;
     Y.user_to_sorted = L.user_to_sorted;
     Y.h_neuron_ptr = L.nptr;
     NW_CHECK(upload_layout(ctx, L, Y.seg, Y.seg_ptr, Y.neuron_ptr));
@@ -811,7 +818,7 @@ int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron
     for (DevBuf* b : {&Y.pre, &Y.delay, &Y.pulse_end, &Y.last_event, &Y.events}) NW_CHECK(dev_alloc(ctx, *b, 4 * m));
     for (DevBuf* b : {&Y.wa, &Y.wn, &Y.oa, &Y.on, &Y.od}) NW_CHECK(dev_alloc(ctx, *b, rs * m));
     NW_CHECK(dev_alloc(ctx, Y.mats, rs * 26));
-    NW_CHECK(dev_alloc(ctx, Y.ring, 4 * (size_t)Y.ring_words * ctx->n_neuron));
+    NW_CHECK(dev_alloc(ctx, Y.ring, 4 * (size_t)Y.ring_words * ring_neurons));
     NW_CHECK(upload_convert(ctx, Y.pre.ptr, NW_DTYPE_I32, pre.data(), NW_DTYPE_I32, m));
     NW_CHECK(upload_convert(ctx, Y.delay.ptr, NW_DTYPE_I32, dl.data(), NW_DTYPE_I32, m));
     NW_CHECK(upload_convert(ctx, Y.pulse_end.ptr, NW_DTYPE_I32, pe.data(), NW_DTYPE_I32, m));
@@ -1051,6 +1058,14 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
     if (nm == "cuda_graph") { ctx->use_graph = value != 0; return NW_OK; }
+    if (nm == "spike_neurons" || nm == "spike_neuron_offset" || nm == "spike_ring_steps") {
+        // Partitioned networks: taken by the next nw_synapses_set.
+        if (value < 0 || value > INT32_MAX) return fail(ctx, NW_ERR_ARG, nm + " out of range");
+        if (nm == "spike_neurons") ctx->spike_neurons = value;
+        else if (nm == "spike_neuron_offset") ctx->spike_offset = value;
+        else ctx->spike_ring_min = (int)value;
+        return NW_OK;
+    }
     if (nm == "pair_shared_limit") {
         // Largest neuron whose pair sums stay in shared memory (-1: as many as fit);
         // larger ones use global memory.  The integer sums are the same either way.
@@ -1124,6 +1139,8 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "graph_captures") { *value = ctx->graph_captures; return NW_OK; }
     if (nm == "graph_replays") { *value = ctx->graph_replays; return NW_OK; }
     if (nm == "synapse_ring_words") { *value = ctx->syn.ring_words; return NW_OK; }
+    if (nm == "spike_neurons") { *value = ctx->syn.n ? ctx->syn.ring_neurons : ctx->n_neuron; return NW_OK; }
+    if (nm == "spike_neuron_offset") { *value = ctx->spike_offset; return NW_OK; }
     return fail(ctx, NW_ERR_ARG, "nw_get_option: unknown option " + nm);
 }
 

@@ -86,6 +86,11 @@ struct KineticState {
 // its arrival from the ring (step - delay), so delivery order cannot vary.
 struct SynState {
     int64_t n = 0;
+    // Spike-ring partition: the ring covers `ring_neurons` neurons (all ranks' when
+    // neurons are split across GPUs) and this model's neuron j is ring entry
+    // j + `neuron_offset`; `ring_steps_min` forces a common ring length.
+    int64_t ring_neurons = 0, neuron_offset = 0;
+    int ring_steps_min = 0;
     int min_delay = 0, max_delay = 0, pulse_steps = 0, ring_steps = 0, ring_words = 0;
     double e_syn = 0, mg = 1.0;
     DevBuf seg;                 // u32 [n] post segment, segment-sorted order
@@ -183,6 +188,8 @@ struct nw_ctx {
     nw::HHState hh;
     nw::KineticState kin;
     nw::SynState syn;
+    int64_t spike_neurons = 0, spike_offset = 0;   // partition settings applied by nw_synapses_set
+    int spike_ring_min = 0;
     nw::CalciumState ca;
     nw::AdjointState adj;
     bool g_valid = false;       // conductances computed by a mechanism step

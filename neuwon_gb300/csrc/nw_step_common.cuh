@@ -110,7 +110,7 @@ struct StepArgs {
     const int32_t* syn_pre; const int32_t* syn_delay;
     const real* syn_wa; const real* syn_wn; real* syn_oa; real* syn_on_; real* syn_od;
     int32_t* syn_pulse_end; uint32_t* syn_events; int32_t* syn_last; const real* syn_mats;
-    uint32_t* syn_ring;
+    uint32_t* syn_ring; int64_t syn_ring_offset;
     real syn_e, syn_mg357;
     // calcium
     int ca_on, ca_pump, ca_nb, ca_T;
@@ -273,7 +273,7 @@ __device__ __forceinline__ void calcium_mechanisms(const StepArgs<real>& a, int6
 template <typename real>
 __device__ __forceinline__ void spike_ring_write(const StepArgs<real>& a, int64_t j, int64_t s_abs, bool spike) {
     const uint32_t slot = (uint32_t)(s_abs & a.syn_ring_mask);
-    uint32_t* wp = a.syn_ring + j * a.syn_ring_words + (slot >> 5);
+    uint32_t* wp = a.syn_ring + (j + a.syn_ring_offset) * a.syn_ring_words + (slot >> 5);
     const uint32_t bit = 1u << (slot & 31u);
     const uint32_t w = __ldcg(wp);
     *wp = spike ? (w | bit) : (w & ~bit);
@@ -546,7 +546,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
         a.syn_oa = Y.oa.as<real>(); a.syn_on_ = Y.on.as<real>(); a.syn_od = Y.od.as<real>();
         a.syn_pulse_end = Y.pulse_end.as<int32_t>(); a.syn_events = Y.events.as<uint32_t>();
         a.syn_last = Y.last_event.as<int32_t>(); a.syn_mats = Y.mats.as<real>();
-        a.syn_ring = Y.ring.as<uint32_t>();
+        a.syn_ring = Y.ring.as<uint32_t>(); a.syn_ring_offset = Y.neuron_offset;
         a.syn_e = (real)Y.e_syn; a.syn_mg357 = (real)(Y.mg / 3.57);
     }
     const double q10 = pow(3.0, (ctx->celsius - 6.3) / 10.0);      // hh.mod:67

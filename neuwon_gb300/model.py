@@ -310,6 +310,7 @@ class RxD_Model:
         self._clamps = []
         self._probes = []
         self._syn = None
+        self._spike_partition = None
         self._dirty_synapses = False
         self._ctx = None
         self._order = None
@@ -425,6 +426,15 @@ class RxD_Model:
         out[self._order] = buf.reshape(count_per_segment, n).T
         return out
 
+    def set_spike_partition(self, total_neurons, neuron_offset, ring_steps=0):
+        """This model holds neurons [neuron_offset, neuron_offset + its neurons) of a
+        network of total_neurons split across ranks: presynaptic ids of
+        add_synapses are global, and the spike ring covers every neuron (the
+        ranks exchange it with replicas.SpikeExchange).  ring_steps forces a
+        common ring length (a power of two above max + min delay of all ranks)."""
+        self._spike_partition = (int(total_neurons), int(neuron_offset), int(ring_steps))
+        self._dirty_synapses = self._syn is not None
+
     def add_synapses(self, pre_neurons, post_segments, w_ampa, w_nmda=None, delay=1.0, kinetics=None):
         """Synapses from neurons (handles or ids) onto segments (handles or creation
         indices) with AMPA / NMDA weights in nS and axonal delays in ms (rounded to
@@ -437,7 +447,8 @@ class RxD_Model:
         m = len(pre)
         if len(post) != m:
             raise ValueError("pre_neurons and post_segments differ in length")
-        if np.any(pre < 0) or np.any(pre >= len(self._neuron_root)):
+        n_pre = self._spike_partition[0] if self._spike_partition else len(self._neuron_root)
+        if np.any(pre < 0) or np.any(pre >= n_pre):
             raise ValueError("presynaptic neuron out of range")
         if np.any(post < 0) or np.any(post >= self._n):
             raise ValueError("post segment out of range")
@@ -461,6 +472,11 @@ class RxD_Model:
         kin = sy["kinetics"]
         ao, af, no, nf = (np.ascontiguousarray(x, dtype=np.float64) for x in kin.matrices(self.time_step))
         post_dev = np.ascontiguousarray(self._inv[sy["post"]])
+        if self._spike_partition is not None:
+            total, offset, ring_steps = self._spike_partition
+            self._ctx.set_option("spike_neurons", total)
+            self._ctx.set_option("spike_neuron_offset", offset)
+            self._ctx.set_option("spike_ring_steps", ring_steps)
         self._ctx.call("nw_synapses_set", len(sy["pre"]), _lib.ptr(np.ascontiguousarray(sy["pre"])),
                        _lib.ptr(post_dev), _lib.ptr(np.ascontiguousarray(sy["wa"] * 1e-9)),
                        _lib.ptr(np.ascontiguousarray(sy["wn"] * 1e-9)),

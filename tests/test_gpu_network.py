@@ -115,3 +115,65 @@ def test_autotune_restores_synapse_state():
     ref.advance(200)
     np.testing.assert_array_equal(m.get_data("Synapse.events"), ref.get_data("Synapse.events"))
     m.close(); ref.close()
+
+
+def test_partitioned_network_equals_one_model():
+    """A network split into two models (emulated ranks on one GPU, each advancing an
+    epoch of the shortest delay, then summing spike rings on the host) gives the
+    single model's voltages, spikes and deliveries bit for bit."""
+    import neuwon_gb300 as nw
+    from neuwon_gb300.morphology import random_tree
+    from neuwon_gb300.replicas import SpikeExchange
+    from neuwon_gb300.synapses import random_network
+    sizes = [300, 250, 400, 150, 350, 200]
+    trees = [random_tree(n, seed=60 + k) for k, n in enumerate(sizes)]
+    amps = [0.5, 0.4, 0.6, 0.3, 0.45, 0.55]
+    net = random_network(sizes, 1200, 9, delay_lo=1.0, delay_hi=4.0)
+    E = int(net["delay_steps"].min())
+
+    def build(neuron_ids, syn_ids, partition=None):
+        m = nw.RxD_Model(time_step=0.1, temperature=6.3, precision="f64", mechanisms=[nw.HH.configure(ena=50.0, ek=-77.0)])
+        offs, o = {}, 0
+        for j in neuron_ids:
+            nr = m.add_tree(trees[j])
+            offs[j] = o
+            o += sizes[j]
+            nr.root.inject_current(amps[j], 1e9)
+        m.insert_everywhere("hh")
+        if partition is not None:
+            m.set_spike_partition(*partition)
+        post = np.array([offs[net["post_neuron"][k]] + net["post_local"][k] for k in syn_ids])
+        m.add_synapses(net["pre"][syn_ids], post, net["weight_nS"][syn_ids], net["weight_nS"][syn_ids],
+                       net["delay_steps"][syn_ids] * 0.1)
+        m._sync()
+        return m
+
+    all_syn = np.arange(1200)
+    full = build(range(6), all_syn)
+    R = 32 * full._ctx.get_option("synapse_ring_words")
+    a_syn = all_syn[net["post_neuron"] < 3]
+    b_syn = all_syn[net["post_neuron"] >= 3]
+    A = build(range(3), a_syn, (6, 0, R))
+    B = build(range(3, 6), b_syn, (6, 3, R))
+    ranks = [SpikeExchange(A), SpikeExchange(B)]
+    total = lambda _: sum(r.own() for r in ranks)
+    for r in ranks:
+        r.reduce = total
+    for epoch in range(40):
+        A.advance(E)
+        B.advance(E)
+        summed = total(None)
+        for r in ranks:
+            r.install(summed)
+        full.advance(E)
+    v_full = full.get_data("Segment.voltage")
+    v_parts = np.concatenate([A.get_data("Segment.voltage"), B.get_data("Segment.voltage")])
+    assert np.array_equal(v_full, v_parts)
+    ev = full.get_data("Synapse.events")
+    assert np.array_equal(ev[a_syn], A.get_data("Synapse.events"))
+    assert np.array_equal(ev[b_syn], B.get_data("Synapse.events"))
+    assert ev.sum() > 0 and (ev[a_syn] > 0).any() and (ev[b_syn] > 0).any()
+    np.testing.assert_array_equal(full.get_data("Neuron.spike_count"),
+                                  np.concatenate([A.get_data("Neuron.spike_count"), B.get_data("Neuron.spike_count")]))
+    for m in (full, A, B):
+        m.close()

@@ -53,3 +53,28 @@ def test_single_process_aggregate_is_local():
     a = batched_trees(4, seed=replica_seed(3), processes=1, lo=50, hi=100)
     b = batched_trees(4, seed=replica_seed(3), processes=1, lo=50, hi=100)
     assert all(np.array_equal(x.parent, y.parent) for x, y in zip(a, b))
+
+
+def _exchange_rank(rank, world, port, out_dir):
+    from neuwon_gb300.replicas import exchange_rings
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    rng = np.random.default_rng(rank)
+    ring = rng.integers(0, 2 ** 32, (10, 4), dtype=np.uint64).astype(np.uint32)   # stale words everywhere
+    offset, count = (0, 6) if rank == 0 else (6, 4)
+    total = exchange_rings(ring, offset, count, dist)
+    np.save(os.path.join(out_dir, f"ring{rank}.npy"), ring)
+    np.save(os.path.join(out_dir, f"total{rank}.npy"), total)
+    dist.destroy_process_group()
+
+
+def test_spike_ring_exchange_over_gloo():
+    """Two ranks own neurons 0-5 and 6-9; after the exchange both hold every
+    neuron's words from its owner."""
+    with tempfile.TemporaryDirectory() as d:
+        mp.start_processes(_exchange_rank, args=(2, _free_port(), d), nprocs=2, start_method="spawn", join=True)
+        r0, r1 = (np.load(os.path.join(d, f"ring{k}.npy")) for k in range(2))
+        t0, t1 = (np.load(os.path.join(d, f"total{k}.npy")) for k in range(2))
+    expect = np.concatenate([r0[:6], r1[6:]])
+    assert np.array_equal(t0, expect) and np.array_equal(t1, expect)
+    assert t0.dtype == np.uint32
