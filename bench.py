@@ -392,7 +392,7 @@ def main():
     ap.add_argument("--ref-tol", type=float, default=1e-10,
                     help="pruning of the FP64 accuracy reference (machine epsilon makes rows dense)")
     ap.add_argument("--size-range", default="500,20000", help="neuron size range (segments)")
-    ap.add_argument("--acc-neurons", type=int, default=16)
+    ap.add_argument("--acc-neurons", type=int, default=64)
     ap.add_argument("--acc-steps", type=int, default=2000)
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
     ap.add_argument("--autotune", type=int, default=10,
