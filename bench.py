@@ -105,39 +105,51 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, device=0):
-    """Time the C oracle (FP64, OpenMP, all host threads) on the first few neurons."""
-    from neuwon_gb300 import _lib
-    from neuwon_gb300.workloads import build_model
+def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, max_neuron=3000, target_segments=20000):
+    """Time the C oracle (FP64, OpenMP, all host threads) on a sample of the batch: its
+    first neurons of at most max_neuron segments, up to target_segments segments, with
+    the same mechanisms (HH + na8), soma clamps and detectors.  Everything is built on
+    the CPU (scipy expm per neuron, pruned, charge-conserving; host lti_sim table): no
+    GPU and none of this package's kernels are involved."""
+    from neuwon_gb300.kinetic import Kinetic, LTITable, na8
+    from neuwon_gb300.morphology import geometry, passive_electric
+    from neuwon_gb300.workloads import CELSIUS, HH_PARAMS, TIME_STEP
     from oracle.cpu_oracle import CpuOracle
-    sample, segs = [], 0
-    for t in trees:
-        sample.append(t)
-        segs += len(t)
-        if segs >= 25000:
-            break
-    m, neurons = build_model(sample, currents[:len(sample)], precision="f64", tolerance=tol, conserve=True,
-                             device=device)
-    m._sync()
-    ctx = m._ctx
-    n = m._n
-    nnz = ctypes.c_int64()
-    ctx.call("nw_propagator_get_csr", None, None, None, ctypes.byref(nnz))
-    rowptr = np.empty(n + 1, np.int64); col = np.empty(nnz.value, np.int64); val = np.empty(nnz.value)
-    ctx.call("nw_propagator_get_csr", _lib.ptr(rowptr), _lib.ptr(col), _lib.ptr(val), ctypes.byref(nnz))
-    # Device order equals creation order here (neurons were added one after another).
-    g = m._geometry()
-    rec = m._mech_instances["hh"]
-    seg = np.concatenate(rec["seg"])
-    area = g["surface_area"][seg]
-    from neuwon_gb300.workloads import HH_PARAMS
+    from oracle.reference_step import propagator
+    sample, idx, segs = [], [], 0
+    for k, t in enumerate(trees):
+        if len(t) <= max_neuron:
+            sample.append(t)
+            idx.append(k)
+            segs += len(t)
+            if segs >= target_segments:
+                break
+    parents, R, C, area, roots, off = [], [], [], [], [], 0
+    for t in sample:
+        g = geometry(t)
+        r, c = passive_electric(g)
+        parents.append(np.where(t.parent < 0, -1, t.parent + off))
+        R.append(r); C.append(c); area.append(g["surface_area"]); roots.append(off)
+        off += len(t)
+    parent, R, C, area = (np.concatenate(x) for x in (parents, R, C, area))
+    n = len(parent)
+    t_build = time.perf_counter()
+    P = propagator(parent, R, C, 0.5 * TIME_STEP, prune=tol).tocsr()
+    rows = np.repeat(np.arange(n), np.diff(P.indptr))
+    diag = np.flatnonzero(P.indices == rows)
+    P.data[diag] += 1.0 - np.asarray(P.sum(axis=1)).ravel()[rows[diag]]   # charge-conserving
+    seg = np.arange(n)
     hh = dict(segment=seg, gna=HH_PARAMS["gnabar"] * 1e-8 * area, gk=HH_PARAMS["gkbar"] * 1e-8 * area,
               gl=HH_PARAMS["glbar"] * 1e-8 * area, ena=HH_PARAMS["ena"], ek=HH_PARAMS["ek"], el=HH_PARAMS["el"])
-    clamps = [(c[0], c[1], c[2], c[3]) for c in m._clamps]
-    roots = [int(nr.root.get_unstable_index()) for nr in neurons]
-    m.close()
-    co = CpuOracle(rowptr, col.astype(np.int32), val, g["capacitance"], time_step=0.1, celsius=6.3,
-                   hh=hh, clamps=clamps, detectors=[(r, 20.0) for r in roots])
+    sch = na8()
+    tbl = LTITable(sch, TIME_STEP, CELSIUS)
+    kin = dict(segment=seg, gcoef=Kinetic.gbar * 1e-8 * area, table=tbl.layout, vmin=tbl.vmin,
+               bucket_frq=tbl.bucket_frq, open=sch.open_states, erev=Kinetic.erev, conserve=sch.conserve_sum,
+               init=sch.steady_state(-70.0, CELSIUS))
+    clamps = [(r, float(currents[k]) * 1e-9, 1, 1 << 40) for r, k in zip(roots, idx)]
+    co = CpuOracle(P.indptr, P.indices.astype(np.int32), P.data, C, time_step=TIME_STEP, celsius=CELSIUS,
+                   hh=hh, clamps=clamps, detectors=[(r, 20.0) for r in roots], kinetic=kin)
+    build_s = time.perf_counter() - t_build
     co.advance(2)
     done, t0 = 0, time.perf_counter()
     while done < steps and time.perf_counter() - t0 < time_budget_s:
@@ -145,21 +157,22 @@ def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, device=0):
         done += 1
     dt = time.perf_counter() - t0
     return {"value": n * done / dt, "unit": "segment-steps/s", "cores": co.threads(), "kind": "port",
-            "sample": f"first {len(sample)} neurons of the batch ({n} segments, "
-                      f"{nnz.value / n:.0f} propagator entries/row), {done} steps, FP64 C restatement "
-                      f"(oracle/cpu_step.c) with OpenMP"}
+            "sample": f"{len(sample)} neurons of the batch of <= {max_neuron} segments ({n} segments, "
+                      f"{P.nnz / n:.0f} propagator entries/row), HH + na8, {done} steps, FP64 C restatement "
+                      f"(oracle/cpu_step.c) with OpenMP, built on the CPU in {build_s:.0f} s"}
 
 
 def run_reference(args, rank):
     from neuwon_gb300.workloads import batched_currents, batched_trees
     lo, hi = (int(x) for x in args.size_range.split(","))
-    trees = batched_trees(args.neurons, first=0, count=16, processes=8, lo=lo, hi=hi)
+    trees = batched_trees(args.neurons, first=0, count=64, processes=8, lo=lo, hi=hi)
     currents = batched_currents(args.neurons)
     res = cpu_sample(trees, currents, args.tol, steps=args.steps + args.warmup, time_budget_s=60.0)
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "segment-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "batched: 1024 HH neurons, 500-20000 segments, dt 0.1 ms",
+            "data": "synthetic", "config": {"workload": "batched: 1024 neurons, log-uniform 500-20000 segments, HH + "
+                                                        "8-state Markov Na on every segment, dt 0.1 ms",
                                             "sample": res["sample"], "propagator_tolerance": args.tol},
             "cpu_baseline": res,
             "e2e": {"value": res["value"], "unit": "segment-steps/s", "h2d_bytes_per_step": 0,
@@ -561,7 +574,7 @@ def main():
     log(f"timed: {ms / K:.3f} ms/step; e2e {e2e_s / E * 1e3:.3f} ms/step")
     cpu = None
     if not args.quick and rank == 0:
-        cpu = cpu_sample(trees[:16], currents, args.tol, steps=100000, time_budget_s=15.0, device=local)
+        cpu = cpu_sample(trees, currents, args.tol, steps=100000, time_budget_s=15.0)
     spikes = model.get_data("Neuron.spike_count")
     model.close()
     if rank != 0:

@@ -20,7 +20,7 @@ import math
 import numpy as np
 
 from . import _lib
-from .morphology import EPSILON, Tree, geometry, passive_electric
+from .morphology import EPSILON, Tree, device_order, geometry, passive_electric
 from .kinetic import Kinetic
 from .mechanisms import HH, Mechanism, hh_steady_state
 
@@ -726,7 +726,8 @@ class RxD_Model:
         saved = None
         if self._order is not None:
             saved = self._save_state()
-        order = np.argsort(self._seg_neuron[:n], kind="stable")     # Database.sort()
+        # Database.sort() (stable by neuron), depth-first within each neuron.
+        order = device_order(self._parent[:n], self._seg_neuron[:n], len(self._neuron_root))
         inv = np.empty(n, np.int64)
         inv[order] = np.arange(n)
         self._order, self._inv = order, inv

@@ -174,3 +174,58 @@ def passive_electric(geom, cytoplasmic_resistance=100.0, membrane_capacitance=1.
     R = Ra * geom["length"] / geom["cross_sectional_area"]
     C = Cm * geom["creation_area"]
     return R, C
+
+
+def device_order(parent, seg_neuron, num_neurons):
+    """Order of the segments on the device: neurons contiguous in neuron order (the
+    stable sort by neuron of ``Database.sort``, database.py:189-222) and, within a
+    neuron, depth-first preorder with children in creation order.  Preorder puts
+    every subtree on consecutive indices, so a propagator row's columns form a few
+    runs of neighbours (shared-memory and cache locality).  Vectorised: depths and
+    path sums by pointer doubling, subtree sizes level by level.  Returns order
+    (device position -> creation index)."""
+    parent = np.asarray(parent, dtype=np.int64)
+    seg_neuron = np.asarray(seg_neuron, dtype=np.int64)
+    n = len(parent)
+    if n == 0:
+        return np.empty(0, np.int64)
+    has_p = parent >= 0
+
+    def path_sum(val):
+        """sum of val over the node and its ancestors (roots included)."""
+        acc = val.astype(np.int64).copy()
+        anc = np.where(has_p, parent, -1)
+        while True:
+            m = anc >= 0
+            if not m.any():
+                return acc
+            idx = np.nonzero(m)[0]
+            a = anc[idx]
+            acc[idx] += acc[a]
+            anc[idx] = anc[a]
+
+    depth = path_sum(has_p.astype(np.int64))
+    size = np.ones(n, np.int64)
+    by_depth = np.argsort(-depth, kind="stable")
+    d_sorted = depth[by_depth]
+    bounds = np.flatnonzero(np.diff(d_sorted)) + 1
+    for grp in np.split(by_depth, bounds):
+        grp = grp[has_p[grp]]
+        if len(grp):
+            np.add.at(size, parent[grp], size[grp])
+    # Exclusive prefix of earlier siblings' subtree sizes (children in creation order).
+    kids = np.flatnonzero(has_p)
+    kids = kids[np.lexsort((kids, parent[kids]))]
+    csum = np.cumsum(size[kids])
+    first = np.r_[True, parent[kids][1:] != parent[kids][:-1]]
+    group_start = np.maximum.accumulate(np.where(first, np.arange(len(kids)), 0))
+    before = np.where(first, 0, csum - size[kids] - (csum[group_start] - size[kids[group_start]]))
+    val = np.zeros(n, np.int64)
+    val[kids] = 1 + before
+    local = path_sum(val)
+    counts = np.bincount(seg_neuron, minlength=num_neurons)
+    start = np.concatenate([[0], np.cumsum(counts)])[:-1]
+    pos = start[seg_neuron] + local
+    order = np.empty(n, np.int64)
+    order[pos] = np.arange(n)
+    return order

@@ -32,6 +32,11 @@ class _Model(ctypes.Structure):
         ("n_neuron", ctypes.c_int64), ("det_seg", ctypes.c_void_p), ("det_thr", ctypes.c_void_p),
         ("ap_state", ctypes.c_void_p), ("ap_detected", ctypes.c_void_p), ("spike_count", ctypes.c_void_p),
         ("x", ctypes.c_void_p), ("input_ticks", ctypes.c_int64), ("g_valid", ctypes.c_int),
+        ("km", ctypes.c_int64), ("kin_seg_ptr", ctypes.c_void_p), ("kin_seg", ctypes.c_void_p),
+        ("kstate", ctypes.c_void_p), ("kgcoef", ctypes.c_void_p), ("ktable", ctypes.c_void_p),
+        ("kS", ctypes.c_int64), ("kT", ctypes.c_int64), ("knb", ctypes.c_int64), ("knopen", ctypes.c_int64),
+        ("kopen", ctypes.c_void_p),
+        ("kvmin", ctypes.c_double), ("kfrq", ctypes.c_double), ("kcs", ctypes.c_double), ("kerev", ctypes.c_double),
     ]]
 
 
@@ -43,11 +48,13 @@ class CpuOracle:
     """FP64 OpenMP step over a CSR propagator (with diagonal) and HH instances.
 
     hh: dict(segment, gna, gk, gl (S), ena, ek, el); clamps: list of
-    (segment, amps, first_tick, num_ticks); detectors: list of (segment, thr).
+    (segment, amps, first_tick, num_ticks); detectors: list of (segment, thr);
+    kinetic: dict(segment, gcoef (S), table [bucket][col][row][term], vmin,
+    bucket_frq, open (state indices), erev, conserve (0: none), init (S,)).
     """
 
     def __init__(self, csr_indptr, csr_indices, csr_data, C, *, time_step, celsius, v_init=-70.0,
-                 hh=None, clamps=(), detectors=(), m0=None):
+                 hh=None, clamps=(), detectors=(), m0=None, kinetic=None):
         self.lib = ctypes.CDLL(build())
         self.lib.oracle_advance.argtypes = [ctypes.POINTER(_Model), ctypes.c_int]
         self.lib.oracle_threads.restype = ctypes.c_int
@@ -109,6 +116,27 @@ class CpuOracle:
         M.det_seg, M.det_thr = _p(self.det_seg), _p(self.det_thr)
         M.ap_state, M.ap_detected, M.spike_count = _p(self.ap_state), _p(self.ap_detected), _p(self.spike_count)
         M.x = _p(self.x)
+        if kinetic is not None:
+            seg = np.asarray(kinetic["segment"], dtype=np.int64)
+            order = np.argsort(seg, kind="stable")
+            self.kin_seg = np.ascontiguousarray(seg[order])
+            self.kin_seg_ptr = np.zeros(n + 1, np.int64)
+            np.add.at(self.kin_seg_ptr, self.kin_seg + 1, 1)
+            self.kin_seg_ptr = np.cumsum(self.kin_seg_ptr)
+            table = np.ascontiguousarray(kinetic["table"], dtype=np.float64)
+            nb, S, _, T = table.shape
+            km = len(seg)
+            self.kstate = np.ascontiguousarray(np.repeat(np.asarray(kinetic["init"], np.float64)[:, None], km, 1))
+            self.kgcoef = np.ascontiguousarray(np.asarray(kinetic["gcoef"], np.float64)[order])
+            self.ktable = table
+            self.kopen = np.ascontiguousarray(kinetic["open"], dtype=np.int64)
+            M.km = km
+            M.kin_seg_ptr, M.kin_seg = _p(self.kin_seg_ptr), _p(self.kin_seg)
+            M.kstate, M.kgcoef, M.ktable = _p(self.kstate), _p(self.kgcoef), _p(self.ktable)
+            M.kS, M.kT, M.knb, M.knopen = S, T, nb, len(self.kopen)
+            M.kopen = _p(self.kopen)
+            M.kvmin, M.kfrq = float(kinetic["vmin"]), float(kinetic["bucket_frq"])
+            M.kcs, M.kerev = float(kinetic.get("conserve") or 0.0), float(kinetic["erev"])
         self.M = M
 
     def advance(self, k=1):

@@ -10,6 +10,8 @@
  *   nmodl_library/artificial/hh.mod + neuwon/rxd/nmodl/solver.py:48-55  HH gates
  *   neuwon/rxd/neuron/neuron.py:184-188  AP detector
  *   neuwon/database/time.py:287-302   current clamps on the half-step clock
+ *   neuwon/rxd/lti_sim/codegen.py:39-106  kinetic scheme: voltage bucket, polynomial
+ *                                     table [bucket][col][row][term], CONSERVE renormalisation
  *
  * Build: see oracle/Makefile (gcc -O3 -fopenmp -shared).
  */
@@ -41,6 +43,11 @@ typedef struct {
     double* x;
     int64_t input_ticks;
     int g_valid;
+    /* kinetic instances sorted by segment; states state-major [S][km] */
+    int64_t km; const int64_t* kin_seg_ptr; const int64_t* kin_seg;
+    double* kstate; const double* kgcoef; const double* ktable;
+    int64_t kS, kT, knb, knopen; const int64_t* kopen;
+    double kvmin, kfrq, kcs, kerev;
 } oracle_model;
 
 static double vtrap(double x, double y) {
@@ -65,6 +72,16 @@ static void half_step(oracle_model* m) {
         }
         double G = (gna + gk) + gl;
         double GE = (gna * m->ena + gk * m->ek) + gl * m->el;
+        if (gv && m->km) {
+            double gkin = 0.0;
+            for (int64_t k = m->kin_seg_ptr[i]; k < m->kin_seg_ptr[i + 1]; ++k) {
+                double open = 0.0;
+                for (int64_t o = 0; o < m->knopen; ++o) open += m->kstate[m->kopen[o] * m->km + k];
+                gkin += m->kgcoef[k] * open;
+            }
+            G += gkin;
+            GE += gkin * m->kerev;
+        }
         double I = m->Inonspec ? m->Inonspec[i] : 0.0;
         if (m->clamp_ptr)
             for (int64_t c = m->clamp_ptr[i]; c < m->clamp_ptr[i + 1]; ++c)
@@ -106,10 +123,38 @@ static void mechanisms(oracle_model* m) {
     }
 }
 
+static void kinetic(oracle_model* m) {
+    const int64_t S = m->kS, T = m->kT;
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < m->km; ++k) {
+        double x = (m->V[m->kin_seg[k]] - m->kvmin) * m->kfrq;
+        int64_t b = (int64_t)trunc(x);
+        double loc = x - (double)b;
+        if (b > m->knb - 1) { b = m->knb - 1; loc = 1.0; }
+        if (b < 0) { b = 0; loc = 0.0; }
+        double s_old[16], s_new[16];
+        for (int64_t c = 0; c < S; ++c) { s_old[c] = m->kstate[c * m->km + k]; s_new[c] = 0.0; }
+        const double* tb = m->ktable + b * S * S * T;
+        for (int64_t c = 0; c < S; ++c)
+            for (int64_t r = 0; r < S; ++r) {
+                const double* t = tb + (c * S + r) * T;
+                double poly = 0.0, p = 1.0;
+                for (int64_t u = 0; u < T; ++u) { poly += t[u] * p; p *= loc; }
+                s_new[r] += poly * s_old[c];
+            }
+        double sum = 0.0;
+        for (int64_t r = 0; r < S; ++r) sum += s_new[r];
+        const double f = m->kcs > 0 ? m->kcs / sum : 1.0;
+        for (int64_t r = 0; r < S; ++r) m->kstate[r * m->km + k] = s_new[r] * f;
+    }
+}
+
 int oracle_advance(oracle_model* m, int k_steps) {
     for (int s = 0; s < k_steps; ++s) {
         half_step(m);
-        if (m->m) { mechanisms(m); m->g_valid = 1; }
+        if (m->m) mechanisms(m);
+        if (m->km) kinetic(m);
+        if (m->m || m->km) m->g_valid = 1;
         half_step(m);
         for (int64_t j = 0; j < m->n_neuron; ++j) {
             int over = m->V[m->det_seg[j]] >= m->det_thr[j];

@@ -84,9 +84,41 @@ def test_model_sorts_segments_by_neuron_stably():
     s1 = a.root.add_segment([12, 0, 0], 1)
     s2 = b.root.add_segment([62, 0, 0], 1)
     s3 = s1.add_segment([20, 0, 0], 1)
-    order = np.argsort(m._seg_neuron[:m._n], kind="stable")
+    order = np.argsort(m._seg_neuron[:m._n], kind="stable")        # Database.sort
     assert list(order) == [0, 2, 4, 1, 3]
     assert s3.parent == s1 and s1.children == [s3]
+    dev = nw.morphology.device_order(m._parent[:m._n], m._seg_neuron[:m._n], 2)
+    assert list(dev) == [0, 2, 4, 1, 3]                             # a chain: the same
+
+
+def test_device_order_is_neuron_sort_refined_by_preorder():
+    """Neurons stay contiguous in Database.sort's order; within a neuron every
+    subtree occupies consecutive positions (depth-first, children in creation order)."""
+    rng = np.random.default_rng(0)
+    for trial in range(30):
+        N = int(rng.integers(1, 5))
+        parent, nid = [-1] * N, list(range(N))
+        for k in range(int(rng.integers(1, 150))):
+            j = int(rng.integers(0, N))
+            cand = [i for i in range(len(parent)) if nid[i] == j]
+            parent.append(int(rng.choice(cand)))
+            nid.append(j)
+        parent, nid = np.array(parent), np.array(nid)
+        order = nw.morphology.device_order(parent, nid, N)
+        stable = np.argsort(nid, kind="stable")
+        assert np.array_equal(nid[order], nid[stable])              # same neuron blocks
+        children = [[] for _ in parent]
+        for i, p in enumerate(parent):
+            if p >= 0:
+                children[p].append(i)
+        expect = []
+        for j in range(N):
+            st = [j]
+            while st:
+                u = st.pop()
+                expect.append(u)
+                st.extend(reversed(children[u]))
+        assert np.array_equal(order, expect)
 
 
 def test_inject_current_schedules_half_step_ticks():

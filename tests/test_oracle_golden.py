@@ -215,6 +215,29 @@ def test_c_oracle_matches_numpy_oracle():
     np.testing.assert_array_equal(om.spike_count, co.spike_count)
 
 
+def test_c_oracle_with_kinetic_matches_numpy_oracle():
+    """The C oracle's kinetic step (table lookup, CONSERVE) equals the numpy oracle's."""
+    from oracle.cpu_oracle import CpuOracle
+    om, d = oracle_case([random_tree(150, seed=5), random_tree(90, seed=6)],
+                        [(0, 0, 0.3, 1., 10.), (1, 10, 0.25, 2., 5.)], hh_kw=dict(ena=50., ek=-77.),
+                        kinetic=True)
+    P = om.P
+    k = om.kinetic
+    co = CpuOracle(P.indptr, P.indices, P.data, d["C"], time_step=0.1, celsius=6.3,
+                   hh=dict(segment=d["seg"], gna=om.hh.gna_coef, gk=om.hh.gk_coef, gl=om.hh.gl_coef,
+                           ena=50., ek=-77., el=-54.3),
+                   clamps=d["clamps"], detectors=[(o, 20.0) for o in d["offs"]],
+                   kinetic=dict(segment=k.segment, gcoef=k.g_coef, table=k.layout, vmin=k.vmin,
+                                bucket_frq=k.frq, open=k.open_states, erev=k.erev, conserve=k.conserve_sum,
+                                init=k.state[0].copy()))
+    for _ in range(200):
+        om.advance()
+        co.advance()
+    assert np.abs(om.voltage - co.V).max() < 1e-9
+    assert np.abs(om.kinetic.state - co.kstate.T).max() < 1e-12
+    np.testing.assert_array_equal(om.spike_count, co.spike_count)
+
+
 def test_clamp_ticks_match_reference_timeseries():
     """time.py:276-279: ceil(duration / half_step) plays, first on the next tick."""
     assert clamp_ticks(5.0, 1.0, 0.1) == (101, 20)
