@@ -45,7 +45,7 @@ def test_noalloc_half_step_matches_advance_on_two_calls():
     nw.Segment(m, 0).inject_current(0.3, 10.0)            # active on ticks 1..200
     m._sync()
     rowptr, col, val = _propagator(m)
-    C = m._geometry()["capacitance"]                      # one neuron: device order = creation order
+    C = m._geometry()["capacitance"][m._order]            # device order (depth-first within the neuron)
     n = m._n
     lib = _lib.load()
 
@@ -71,8 +71,8 @@ def test_noalloc_half_step_matches_advance_on_two_calls():
         half_step()
         half_step()
         m.advance(1)
-        want = m.get_data("Segment.voltage")
-        got = d["V"].cpu().numpy()
+        want = m.get_data("Segment.voltage")              # creation order
+        got = d["V"].cpu().numpy()[m._inv]
         assert np.abs(got - want).max() < TOL_MV
         assert np.abs(got + 70.0).max() > 1e-6        # the clamp moved the voltage
     m.close()
