@@ -33,6 +33,7 @@ namespace nw {
 constexpr int kPoles = 16;            // N/2 for N = 32
 constexpr int kNodes = 2 * kPoles;
 constexpr int kStackDepth = 64;
+constexpr int kChainDepth = 384;
 constexpr double kExploreFactor = 1e-2;
 constexpr int kStatusStackOverflow = 2;
 constexpr int kStatusRowMismatch = 4;
@@ -139,6 +140,16 @@ __global__ void edge_pivots_kernel(const BuildArgs a) {
 // One warp per row; lanes 0..15 carry one pole each.  fill = 0 counts, 1 writes.
 // Both passes run this same code, so they take identical decisions; the fill
 // pass still checks that the row's entries land exactly in [rowptr[r], rowptr[r+1]).
+//
+// The walk emits a row's columns in increasing order when segments are numbered
+// depth-first (children after their parent, subtrees contiguous): it first
+// climbs from the row's segment i towards the root while the values stay above
+// the exploration threshold (keeping each ancestor's value, which comes from
+// below), then walks the reached region in preorder from the top ancestor,
+// children in index order.  A chain node's value is the kept one; any other
+// node's is its parent's times the edge ratio.  A node is expanded when its
+// value reaches the exploration threshold (the top one, if it does not, still
+// leads down the chain), so the visited set is the same as a plain walk's.
 __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a, const int fill) {
     const int lane = threadIdx.x & 31;
     const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -147,49 +158,82 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
     const int k = act ? lane : 0;
     const cplx w = act ? cplx(c_w[k].x, c_w[k].y) : cplx(0.0, 0.0);
     const double scale_out = 2.0 / kNodes;
-    int32_t st_node[kStackDepth], st_from[kStackDepth];
-    cplx st_y[kStackDepth];
-    int sp = 0;
-    int64_t cur = row, from = -1;
-    cplx y = ld(&a.invT[row * kPoles + k]);
-    int64_t kept = 0;
-    int64_t out = fill ? a.rowptr[row] : 0;
-    const int64_t out_end = fill ? a.rowptr[row + 1] : 0;
-    for (;;) {
-        cplx wy = w * y;
+    auto value = [&](cplx yy) -> double {
+        const cplx wy = w * yy;
         double v = act ? wy.im : 0.0;
 #pragma unroll
         for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        v = __shfl_sync(0xffffffffu, v, 0) * scale_out;
-        if (fabs(v) >= a.tol) {
-            if (fill && lane == 0 && out < out_end) { a.out_col[out] = (int32_t)cur; a.out_val[out] = v; }
-            ++out;
-            ++kept;
+        return __shfl_sync(0xffffffffu, v, 0) * scale_out;
+    };
+    int32_t chain[kChainDepth];
+    cplx chain_y[kChainDepth];
+    int32_t st_node[kStackDepth], st_cp[kStackDepth];
+    cplx st_y[kStackDepth];
+    int64_t kept = 0;
+    int64_t out = fill ? a.rowptr[row] : 0;
+    const int64_t out_end = fill ? a.rowptr[row + 1] : 0;
+    // Climb.
+    int depth = 0;
+    int64_t cur = row;
+    cplx y = ld(&a.invT[row * kPoles + k]);
+    chain[0] = (int32_t)row;
+    chain_y[0] = y;
+    double v = value(y);
+    while (fabs(v) >= a.explore) {
+        const int64_t p = a.parent[cur];
+        if (p < 0) break;
+        if (depth + 1 >= kChainDepth) {
+            if (lane == 0) atomicOr(a.status, kStatusStackOverflow);
+            goto done;
         }
-        int64_t next = -1;
-        cplx ynext;
-        if (fabs(v) >= a.explore) {
-            const int64_t p = a.parent[cur];
-            if (p >= 0 && p != from) {
-                next = p;
-                ynext = ld(&a.up[cur * kPoles + k]) * y;
+        y = ld(&a.up[cur * kPoles + k]) * y;
+        cur = p;
+        ++depth;
+        chain[depth] = (int32_t)cur;
+        chain_y[depth] = y;
+        v = value(y);
+    }
+    {
+        // Preorder from the top; st_cp = position on the chain, -1 off it.
+        int sp = 0;
+        st_node[0] = chain[depth]; st_cp[0] = depth; st_y[0] = chain_y[depth]; sp = 1;
+        while (sp > 0) {
+            --sp;
+            const int64_t u = st_node[sp];
+            const int cp = st_cp[sp];
+            const cplx yu = st_y[sp];
+            const double vu = value(yu);
+            if (fabs(vu) >= a.tol) {
+                if (fill && lane == 0 && out < out_end) { a.out_col[out] = (int32_t)u; a.out_val[out] = vu; }
+                ++out;
+                ++kept;
             }
-            for (int64_t q = a.child_ptr[cur]; q < a.child_ptr[cur + 1]; ++q) {
-                const int64_t c = a.child_idx[q];
-                if (c == from) continue;
-                const cplx yc = ld(&a.down[c * kPoles + k]) * y;
-                if (next < 0) { next = c; ynext = yc; continue; }
+            const bool expand = fabs(vu) >= a.explore;
+            const int64_t chain_child = cp > 0 ? chain[cp - 1] : -1;
+            if (!expand) {
+                if (chain_child < 0) continue;
                 if (sp >= kStackDepth) {
                     if (lane == 0) atomicOr(a.status, kStatusStackOverflow);
                     goto done;
                 }
-                st_node[sp] = (int32_t)c; st_from[sp] = (int32_t)cur; st_y[sp] = yc; ++sp;
+                st_node[sp] = (int32_t)chain_child; st_cp[sp] = cp - 1; st_y[sp] = chain_y[cp - 1]; ++sp;
+                continue;
+            }
+            // Children pushed last-first so that they come off the stack in index order.
+            for (int64_t q = a.child_ptr[u + 1] - 1; q >= a.child_ptr[u]; --q) {
+                const int64_t c = a.child_idx[q];
+                if (sp >= kStackDepth) {
+                    if (lane == 0) atomicOr(a.status, kStatusStackOverflow);
+                    goto done;
+                }
+                if (c == chain_child) {
+                    st_node[sp] = (int32_t)c; st_cp[sp] = cp - 1; st_y[sp] = chain_y[cp - 1];
+                } else {
+                    st_node[sp] = (int32_t)c; st_cp[sp] = -1; st_y[sp] = ld(&a.down[c * kPoles + k]) * yu;
+                }
+                ++sp;
             }
         }
-        if (next >= 0) { from = cur; cur = next; y = ynext; continue; }
-        if (sp == 0) break;
-        --sp;
-        cur = st_node[sp]; from = st_from[sp]; y = st_y[sp];
     }
 done:
     if (!fill && lane == 0) a.count[row] = kept;
@@ -287,7 +331,8 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "propagator build (count pass)"); break; }
         if (st & kStatusStackOverflow) {
             cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
-            rc = fail(ctx, NW_ERR_LIMIT, "propagator build: walk stack overflow (too many branch points within reach)");
+            rc = fail(ctx, NW_ERR_LIMIT, "propagator build: walk stack or ancestor chain overflow (reach too large "
+                                         "for this tolerance)");
             break;
         }
         std::vector<int64_t> rowptr(n + 1, 0);
