@@ -43,7 +43,7 @@ def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
     return 2 * (8 * r + 4) + 4 * (2 + 2 * s_total + p_seg + 1)
 
 
-def format_bytes_per_segment_step(r_stored, prec=4, pairs=False):
+def format_bytes_per_segment_step(r_stored, prec=4, pairs=False, quads=False):
     """Compulsory HBM bytes of this implementation's layout per segment-step:
     per half step, (value + u16 column) per stored entry (pair format: per stored
     pair), an 8 B row pointer, the leak (pairs: and c_max / c_i), V read + write,
@@ -53,6 +53,8 @@ def format_bytes_per_segment_step(r_stored, prec=4, pairs=False):
     per_half = r_stored * (prec + 2) + 8 + prec + 2 * prec + 2 * prec + 6 * prec + 2 * prec
     if pairs:
         per_half += prec
+    if quads:                                   # r_stored = value slots: 4 per quad, one u16 base
+        per_half -= r_stored * (prec + 2) - (r_stored / 4) * (4 * prec + 2)
     mech = prec + 2 * (3 + 8) * prec
     return 2 * per_half + mech
 
@@ -410,8 +412,9 @@ def main():
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
     ap.add_argument("--autotune", type=int, default=10,
                     help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
-    ap.add_argument("--format", default="rows", choices=["rows", "pairs"],
-                    help="propagator storage: every P_ij in its row, or each coupling once (detailed balance)")
+    ap.add_argument("--format", default="rows", choices=["rows", "pairs", "quads"],
+                    help="propagator storage: every P_ij in its row; windows of 4 consecutive columns; "
+                         "or each coupling once (detailed balance)")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
@@ -567,7 +570,7 @@ def main():
         peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     B_alg = algorithmic_bytes_per_segment_step(r_kept)
-    B_fmt = format_bytes_per_segment_step(r_stored, pairs=args.format == "pairs")
+    B_fmt = format_bytes_per_segment_step(r_stored, pairs=args.format == "pairs", quads=args.format == "quads")
     achieved = B_alg * n / (per_step_launch_ms * 1e-3) / 1e9
     achieved_fmt = B_fmt * n / (per_step_launch_ms * 1e-3) / 1e9
 

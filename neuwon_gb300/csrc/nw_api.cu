@@ -257,6 +257,8 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     free_syn(ctx->syn);
     free_calcium(ctx->ca);
     free_adj(ctx->adj);
+    free_flux(ctx);
+    free_quads(ctx);
     DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec,
                       &ctx->kI, &ctx->kG, &ctx->cap64, &ctx->res64, &ctx->p_rowptr, &ctx->p_col,
                       &ctx->p_val, &ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak,
@@ -341,6 +343,8 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     free_syn(ctx->syn);
     free_calcium(ctx->ca);
     free_adj(ctx->adj);
+    free_flux(ctx);
+    free_quads(ctx);
     size_t rs = (size_t)ctx->precision;
     NW_CHECK(dev_alloc(ctx, ctx->neuron_start, 8 * (num_neurons + 1)));
     NW_CHECK(dev_alloc(ctx, ctx->parent, 8 * num_segments));
@@ -609,6 +613,13 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");
     if (rows) *rows = ctx->n_seg;
     if (nnz) *nnz = ctx->nnz64;
+    if (ctx->prop_format == 2) {
+        // Quad format: 4 value slots + a 16-bit base per quad.
+        NW_CHECK(ensure_quads(ctx));
+        if (stored) *stored = 4 * ctx->nq;
+        if (bytes) *bytes = ctx->nq * (4 * ctx->precision + 2) + ctx->n_seg * (8 + ctx->precision);
+        return NW_OK;
+    }
     if (ctx->prop_format == 1) {
         // Pair format: stored pairs, with c_max / c_i per row besides the leak.
         NW_CHECK(ensure_flux(ctx));
@@ -1076,9 +1087,11 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     if (nm == "propagator_format") {
         // 0: rows (every P_ij stored in its row); 1: pairs (each coupling once,
         // applied to both rows through detailed balance; built propagators only).
-        if (value != 0 && value != 1) return fail(ctx, NW_ERR_ARG, "propagator_format must be 0 or 1");
+        if (value < 0 || value > 2) return fail(ctx, NW_ERR_ARG, "propagator_format must be 0, 1 or 2");
         if (value == 1 && !ctx->prop_built)
             return fail(ctx, NW_ERR_STATE, "pair format needs a propagator built by nw_propagator_build");
+        if (value == 2 && ctx->max_neuron > 65535)
+            return fail(ctx, NW_ERR_LIMIT, "quad format: a neuron has more than 65,535 segments");
         ctx->prop_format = (int)value;
         return NW_OK;
     }
@@ -1134,6 +1147,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "cuda_graph") { *value = ctx->use_graph ? 1 : 0; return NW_OK; }
     if (nm == "propagator_format") { *value = ctx->prop_format; return NW_OK; }
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
+    if (nm == "quads") { *value = ctx->nq; return NW_OK; }
     if (nm == "fusion_depth") { *value = ctx->fusion; return NW_OK; }
     if (nm == "graphs_cached") { *value = (int64_t)ctx->graphs.size(); return NW_OK; }
     if (nm == "graph_captures") { *value = ctx->graph_captures; return NW_OK; }

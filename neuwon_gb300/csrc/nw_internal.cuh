@@ -181,7 +181,13 @@ struct nw_ctx {
     int64_t nnz_f = 0;
     nw::DevBuf f_rowptr, f_col, f_val, f_leak, f_rc;   // i64, u16, real, real, real (c_max / c_i)
     nw::DevBuf f_acc;                                  // i64 [n_seg] accumulators of neurons too large for shared memory
-    int prop_format = 0;                               // 0: rows, 1: pairs
+    // Quad format of the batched path: each row's off-diagonal entries covered by
+    // windows of 4 consecutive columns (base column + 4 values, zero where a
+    // column is not kept); rows with depth-first numbering form long runs.
+    bool q_ok = false;
+    int64_t nq = 0;
+    nw::DevBuf q_rowptr, q_base, q_val;                // i64 (in quads), u16 (neuron-relative), real x 4
+    int prop_format = 0;                               // 0: rows, 1: pairs, 2: quads
     int pair_shared_limit = -1;                        // cap on neurons with shared-memory sums (-1: none)
 
     // Mechanisms.
@@ -255,6 +261,8 @@ int advance_plain(nw_ctx* ctx, int k_steps);
 int advance_wide(nw_ctx* ctx, int k_steps);
 int ensure_wide(nw_ctx* ctx);
 int ensure_flux(nw_ctx* ctx);
+int ensure_quads(nw_ctx* ctx);
+void free_quads(nw_ctx* ctx);
 void free_flux(nw_ctx* ctx);
 void free_wide(nw_ctx* ctx);
 int choose_lanes_per_row(nw_ctx* ctx);

@@ -649,12 +649,122 @@ int ensure_flux(nw_ctx* ctx) {
     return rc;
 }
 
+// ------------------------------------------------- quad format
+
+// Quads of row r: windows [b, b+3] (b <= neuron end - 4) opened at an entry that
+// does not fit the current window, in the row's entry order.  With columns in
+// increasing order every window is as full as the runs allow.
+__device__ __forceinline__ int64_t quad_window(int64_t c, int64_t lo, int64_t hi) {
+    int64_t b = c;
+    if (b > hi - 4) b = hi - 4;
+    if (b < lo) b = lo;
+    return b;
+}
+
+__global__ void quad_count_kernel(int64_t n, const int64_t* nstart_of_row, const int64_t* nend_of_row,
+                                  const int64_t* prow, const int32_t* pcol, int64_t* cnt) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int64_t lo = nstart_of_row[r], hi = nend_of_row[r];
+    int64_t q = 0, b = -1, last = -1;
+    for (int64_t k = prow[r]; k < prow[r + 1]; ++k) {
+        const int64_t c = pcol[k];
+        if (c == r) continue;
+        if (b < 0 || c < b || c > b + 3 || c <= last) { b = quad_window(c, lo, hi); ++q; }
+        last = c;
+    }
+    cnt[r] = q;
+}
+
+template <typename real>
+__global__ void quad_fill_kernel(int64_t n, const int64_t* nstart_of_row, const int64_t* nend_of_row,
+                                 const int64_t* prow, const int32_t* pcol, const double* pval,
+                                 const int64_t* qrow, uint16_t* qbase, real* qval) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int64_t lo = nstart_of_row[r], hi = nend_of_row[r];
+    int64_t q = qrow[r] - 1, b = -1, last = -1;
+    for (int64_t k = prow[r]; k < prow[r + 1]; ++k) {
+        const int64_t c = pcol[k];
+        if (c == r) continue;
+        if (b < 0 || c < b || c > b + 3 || c <= last) {
+            b = quad_window(c, lo, hi);
+            ++q;
+            qbase[q] = (uint16_t)(b - lo);
+            for (int j = 0; j < 4; ++j) qval[4 * q + j] = real(0);
+        }
+        qval[4 * q + (c - b)] = (real)pval[k];
+        last = c;
+    }
+}
+
+void free_quads(nw_ctx* ctx) {
+    for (DevBuf* b : {&ctx->q_rowptr, &ctx->q_base, &ctx->q_val}) dev_free(*b);
+    ctx->q_ok = false;
+    ctx->nq = 0;
+}
+
+int ensure_quads(nw_ctx* ctx) {
+    if (ctx->q_ok) return NW_OK;
+    if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "quad format: needs the batched format (neurons <= 65,535)");
+    for (int64_t j = 0; j < ctx->n_neuron; ++j)
+        if (ctx->h_neuron_start[j + 1] - ctx->h_neuron_start[j] < 4)
+            return fail(ctx, NW_ERR_LIMIT, "quad format: every neuron needs at least 4 segments");
+    const int64_t n = ctx->n_seg;
+    std::vector<int64_t> lo(n), hi(n);
+    for (int64_t j = 0; j < ctx->n_neuron; ++j)
+        for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) {
+            lo[i] = ctx->h_neuron_start[j];
+            hi[i] = ctx->h_neuron_start[j + 1];
+        }
+    DevBuf d_lo, d_hi, d_cnt;
+    auto cleanup = [&]() { dev_free(d_lo); dev_free(d_hi); dev_free(d_cnt); };
+    int rc = NW_OK;
+    do {
+        if ((rc = dev_alloc(ctx, d_lo, 8 * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_hi, 8 * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_cnt, 8 * n)) != NW_OK) break;
+        cudaMemcpyAsync(d_lo.ptr, lo.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(d_hi.ptr, hi.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+        quad_count_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
+            n, d_lo.as<int64_t>(), d_hi.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
+            d_cnt.as<int64_t>());
+        std::vector<int64_t> cnt(n), qrow(n + 1, 0);
+        cudaMemcpyAsync(cnt.data(), d_cnt.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "quad format count"); break; }
+        for (int64_t i = 0; i < n; ++i) qrow[i + 1] = qrow[i] + cnt[i];
+        const int64_t nq = qrow[n];
+        if ((rc = dev_alloc(ctx, ctx->q_rowptr, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->q_base, 2 * std::max<int64_t>(nq, 8))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->q_val, (size_t)ctx->precision * 4 * std::max<int64_t>(nq, 1))) != NW_OK) break;
+        cudaMemcpyAsync(ctx->q_rowptr.ptr, qrow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        if (ctx->precision == NW_F64)
+            quad_fill_kernel<double><<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
+                n, d_lo.as<int64_t>(), d_hi.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
+                ctx->p_val.as<double>(), ctx->q_rowptr.as<int64_t>(), ctx->q_base.as<uint16_t>(),
+                ctx->q_val.as<double>());
+        else
+            quad_fill_kernel<float><<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
+                n, d_lo.as<int64_t>(), d_hi.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
+                ctx->p_val.as<double>(), ctx->q_rowptr.as<int64_t>(), ctx->q_base.as<uint16_t>(),
+                ctx->q_val.as<float>());
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "quad format fill"); break; }
+        ctx->nq = nq;
+        ctx->q_ok = true;
+    } while (0);
+    cleanup();
+    return rc;
+}
+
 // Called whenever the FP64 propagator changes: rebuilds the batched format (if
-// every neuron fits its 16-bit columns) and drops the wide and pair formats
-// until next used.
+// every neuron fits its 16-bit columns) and drops the wide, pair and quad
+// formats until next used.
 int propagator_to_batched(nw_ctx* ctx) {
     free_wide(ctx);
     free_flux(ctx);
+    free_quads(ctx);
     for (DevBuf* b : {&ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak}) dev_free(*b);
     ctx->b_ok = false;
     ctx->nnz_b = 0;

@@ -313,7 +313,7 @@ __device__ __forceinline__ void flux_finalize(const StepArgs<real>& a, int64_t b
     }
 }
 
-template <typename real, int LPR, bool BULK, bool FLUX>
+template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false>
 __global__ void __launch_bounds__(1024)
 batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_off) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -448,6 +448,11 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                         __syncthreads();
                         flux_finalize(a, base, n, xs, gacc);
                     }
+                } else if (QUAD) {
+                    propagate_quads<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real vnew) {
+                        if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
+                        a.V[r] = vnew;
+                    });
                 } else if (BULK) propagate_neuron_bulk(a, base, xs, ring, slice, &s_abort);
                 else propagate_neuron<real, LPR>(a, base, n, xs);
                 __syncthreads();
@@ -574,7 +579,8 @@ __global__ void plain_detect_kernel(const StepArgs<real> a, int64_t row) {
 
 int choose_lanes_per_row(nw_ctx* ctx) {
     if (ctx->lanes_per_row) return ctx->lanes_per_row;
-    const int64_t nnz = (ctx->prop_format == 1 && ctx->f_ok) ? ctx->nnz_f : ctx->nnz_b;
+    int64_t nnz = (ctx->prop_format == 1 && ctx->f_ok) ? ctx->nnz_f : ctx->nnz_b;
+    if (ctx->prop_format == 2 && ctx->q_ok) nnz = ctx->nq;   // quads per row: one per lane and load
     double avg = ctx->n_seg ? (double)nnz / (double)ctx->n_seg : 0.0;
     if (avg >= 48) return 16;
     if (avg >= 20) return 8;
@@ -593,9 +599,9 @@ struct BatchedCfg {
     int rc_smem;      // pair format: c_max / c staged in shared memory
 };
 
-template <typename real, int LPR, bool BULK, bool FLUX>
+template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false>
 static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
-    auto kern = batched_advance_kernel<real, LPR, BULK, FLUX>;
+    auto kern = batched_advance_kernel<real, LPR, BULK, FLUX, QUAD>;
     const size_t xs_bytes = ((size_t)ctx->max_neuron * sizeof(real) + 127) & ~(size_t)127;
     const int threads = ctx->threads;
     size_t smem = xs_bytes;
@@ -647,6 +653,15 @@ template <typename real>
 static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
     if (!ctx->b_ok || (ctx->ca.on && !ctx->ca.b_ok))
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron has more than 65,535 segments (use the wide path)");
+    if (ctx->prop_format == 2) {
+        NW_CHECK(ensure_quads(ctx));
+        switch (choose_lanes_per_row(ctx)) {
+            case 4: return config_batched_lpr<real, 4, false, false, true>(ctx, c);
+            case 8: return config_batched_lpr<real, 8, false, false, true>(ctx, c);
+            case 16: return config_batched_lpr<real, 16, false, false, true>(ctx, c);
+            default: return config_batched_lpr<real, 32, false, false, true>(ctx, c);
+        }
+    }
     if (ctx->prop_format == 1) {
         NW_CHECK(ensure_flux(ctx));
         switch (choose_lanes_per_row(ctx)) {

@@ -87,6 +87,8 @@ struct StepArgs {
     const int64_t* rowptr; const uint16_t* col; const real* val; const real* leak;
     // plain propagator
     const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
+    // quad propagator: windows of 4 consecutive columns
+    const int64_t* qrow; const uint16_t* qbase; const real* qval;
     // pair ("flux") propagator: rows of owned pairs, leak, c_max / c_i, global accumulators
     const int64_t* frow; const uint16_t* fcol; const real* fval; const real* fleak; const real* frc;
     unsigned long long* facc; int facc_cap; int frc_smem;
@@ -471,6 +473,57 @@ __device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t 
     propagate_rows_of<real, LPR, UNROLL>(a.rowptr, a.col, a.val, a.leak, base, n, xs, fin);
 }
 
+// Quad format: row i is a list of windows (base b, values v0..v3 for columns
+// b..b+3); the window's four x are consecutive in shared memory.
+template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
+__device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t base, int n,
+                                                const real* __restrict__ xs, Fin fin) {
+    constexpr int GPW = 32 / LPR;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int q = lane / LPR, l = lane % LPR;
+    for (int rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int row = rb + q;
+        const bool valid = row < n;
+        real s = real(0), c = real(0), xi = real(0);
+        if (valid) {
+            const int64_t r = base + row;
+            const int64_t beg = a.qrow[r], end = a.qrow[r + 1];
+            xi = xs[row];
+            for (int64_t k0 = beg + l; k0 < end; k0 += LPR * UNROLL) {
+                real v[UNROLL][4];
+                int b[UNROLL];
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const int64_t k = k0 + LPR * u;
+                    if (k < end) {
+                        Vec4Loader<real>::load(a.qval + 4 * k, v[u]);
+                        b[u] = __ldcs(a.qbase + k);
+                    } else {
+                        v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                        b[u] = 0;                         // zero weights on x[0..3] (n >= 4)
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const real* x = xs + b[u];
+                    const real p = v[u][0] * (x[0] - xi) + v[u][1] * (x[1] - xi);
+                    const real t = v[u][2] * (x[2] - xi) + v[u][3] * (x[3] - xi);
+                    kahan_add(s, c, p + t);
+                }
+            }
+        }
+        real t = s - c;
+#pragma unroll
+        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        if (valid && l == 0) {
+            const int64_t r = base + row;
+            fin(r, row, xi, (xi - a.leak[r] * xi) + t);
+        }
+    }
+}
+
 // V_i <- propagator row i applied to xs, for every row of one neuron.
 template <typename real, int LPR>
 __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_t base, int n,
@@ -498,6 +551,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.val = ctx->b_val.as<real>(); a.leak = ctx->b_leak.as<real>();
     a.prow = ctx->p_rowptr.as<int64_t>(); a.pcol = ctx->p_col.as<int32_t>(); a.pval = ctx->p_val.as<double>();
     a.px = ctx->plain_x.as<real>();
+    a.qrow = ctx->q_rowptr.as<int64_t>(); a.qbase = ctx->q_base.as<uint16_t>(); a.qval = ctx->q_val.as<real>();
     a.frow = ctx->f_rowptr.as<int64_t>(); a.fcol = ctx->f_col.as<uint16_t>();
     a.fval = ctx->f_val.as<real>(); a.fleak = ctx->f_leak.as<real>(); a.frc = ctx->f_rc.as<real>();
     a.facc = ctx->f_acc.as<unsigned long long>();

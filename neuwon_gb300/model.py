@@ -260,9 +260,12 @@ class RxD_Model:
       propagator_tolerance  prune |P_ij| below this (reference: machine epsilon)
       propagator_conserve   return the pruned mass of each row to its diagonal
                             (charge-conserving pruning; the reference does not)
-      propagator_format     'rows' (every P_ij in its row) or 'pairs' (each coupling
+      propagator_format     'rows' (every P_ij in its row, 16-bit column each),
+                            'quads' (windows of 4 consecutive columns with one
+                            16-bit base: ~16 % fewer bytes with the model's
+                            depth-first numbering) or 'pairs' (each coupling
                             stored once and applied to both segments through
-                            detailed balance: half the propagator bytes per step)
+                            detailed balance)
       path                  'batched' (fused persistent kernel, one CTA per neuron),
                             'wide' (whole-model launches per phase: neurons of any
                             size) or 'plain' (per-neuron launches)
@@ -291,7 +294,7 @@ class RxD_Model:
         self.propagator_tolerance = float(propagator_tolerance)
         self.propagator_conserve = bool(propagator_conserve)
         self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN, "wide": _lib.PATH_WIDE}[path]
-        self.propagator_format = {"rows": 0, "pairs": 1}[propagator_format]
+        self.propagator_format = {"rows": 0, "pairs": 1, "quads": 2}[propagator_format]
         self.input_hook = Clock(0.5 * self.time_step, units="ms")
         self.advance_hook = self.clock = Clock(self.time_step, units="ms")
         # Segment table (creation order).

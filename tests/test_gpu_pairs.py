@@ -16,26 +16,28 @@ F = np.load(FIXTURES)
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("fmt", ["pairs", "quads"])
 @pytest.mark.parametrize("name", ["hh11", "hh200"])
-def test_f64_pairs_match_reference_fixture(name):
+def test_f64_pairs_match_reference_fixture(name, fmt):
     cases = {"hh11": ([tree11()], [(0, 0, .1, 5., 1.), (0, 0, .1, 15., 1.)], {}, True),
              "hh200": ([random_tree(200, seed=11)], [(0, 0, 0.2, 5., 20.)], dict(ena=50., ek=-77., el=-54.3), False)}
     trees, clamps, hh_kw, as_created = cases[name]
     ref = F[name + "_trace"]
     m, neurons, offs, recs = gpu_model(trees, clamps, hh_kw=hh_kw, precision="f64", probes=list(F[name + "_probes"]),
-                                       insert_as_created=as_created, fmt="pairs")
+                                       insert_as_created=as_created, fmt=fmt)
     run_with_clamps(m, clamps, offs, len(ref) - 1)
     got = np.array([r.get_data() for r in recs]).T
     assert np.abs(got - ref).max() < 1e-7
-    assert m._ctx.get_option("propagator_format") == 1
+    assert m._ctx.get_option("propagator_format") == {"pairs": 1, "quads": 2}[fmt]
     m.close()
 
 
-def test_f32_pairs_single_neuron_config_matches_reference():
+@pytest.mark.parametrize("fmt", ["pairs", "quads"])
+def test_f32_pairs_single_neuron_config_matches_reference(fmt):
     clamps = [(0, 0, 0.2, 5.0, 75.0)]
     m, _, offs, recs = gpu_model([random_tree(2000, seed=0)], clamps, hh_kw=dict(ena=50.0, ek=-77.0, el=-54.3),
                                  precision="f32", tolerance=1e-8, conserve=True, probes=list(F["c1_probes"]),
-                                 fmt="pairs")
+                                 fmt=fmt)
     worst = 0.0
     for k in range(1000):
         for (ti, s, nA, start, dur) in clamps:
@@ -74,12 +76,13 @@ def test_pair_sums_in_global_memory_are_bit_identical(precision):
     assert np.array_equal(out[0][1], out[2][1])
 
 
-def test_pairs_are_deterministic():
+@pytest.mark.parametrize("fmt", ["pairs", "quads"])
+def test_pairs_are_deterministic(fmt):
     trees = [random_tree(800, seed=s) for s in range(6)]
     clamps = [(k, 0, 0.4, 0.0, 30.0) for k in range(6)]
     outs = []
     for _ in range(2):
-        m, _, offs, _ = gpu_model(trees, clamps, precision="f32", tolerance=1e-8, conserve=True, fmt="pairs")
+        m, _, offs, _ = gpu_model(trees, clamps, precision="f32", tolerance=1e-8, conserve=True, fmt=fmt)
         for (ti, s, nA, start, dur) in clamps:
             nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
         m.advance(200)
@@ -100,3 +103,27 @@ def test_pairs_need_a_built_propagator():
     rc = m._ctx.lib.nw_set_option(m._ctx.handle, b"propagator_format", 1)
     assert rc == -3                                                    # NW_ERR_STATE
     m.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_quads_equal_rows(precision):
+    """The quad format holds exactly the row format's entries (zeros fill the
+    windows), so results agree to rounding; with depth-first numbering a window
+    holds about 3.5 of its 4 slots."""
+    trees = [random_tree(n, seed=90 + n) for n in (2500, 600, 40, 4)]
+    clamps = [(0, 0, 0.5, 0.0, 50.0), (1, 0, 0.3, 0.0, 50.0), (2, 0, 0.2, 0.0, 50.0)]
+    out = []
+    for fmt in ("rows", "quads"):
+        m, _, offs, _ = gpu_model(trees, clamps, precision=precision, tolerance=1e-8, conserve=True, fmt=fmt,
+                                  kinetic=True)
+        for (ti, s, nA, start, dur) in clamps:
+            nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance(300)
+        out.append((m.get_data("Segment.voltage"), m.get_data("Neuron.spike_count")))
+        if fmt == "quads":
+            nq = m._ctx.get_option("quads")
+            assert m.propagator_nnz - m._n <= 4 * nq < 1.25 * (m.propagator_nnz - m._n)
+        m.close()
+    tol = 1e-9 if precision == "f64" else 2e-3
+    assert np.abs(out[0][0] - out[1][0]).max() < tol
+    assert np.array_equal(out[0][1], out[1][1])
