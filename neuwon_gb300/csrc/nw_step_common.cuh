@@ -475,7 +475,7 @@ __device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t 
 
 // Quad format: row i is a list of windows (base b, values v0..v3 for columns
 // b..b+3); the window's four x are consecutive in shared memory.
-template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
+template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 8 : 2), typename Fin>
 __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t base, int n,
                                                 const real* __restrict__ xs, Fin fin) {
     constexpr int GPW = 32 / LPR;
