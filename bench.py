@@ -412,7 +412,7 @@ def main():
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
     ap.add_argument("--autotune", type=int, default=10,
                     help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
-    ap.add_argument("--format", default="rows", choices=["rows", "pairs", "quads"],
+    ap.add_argument("--format", default="quads", choices=["rows", "pairs", "quads"],
                     help="propagator storage: every P_ij in its row; windows of 4 consecutive columns; "
                          "or each coupling once (detailed balance)")
     ap.add_argument("--lanes", type=int, default=0)

@@ -290,7 +290,7 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * "propagator_format" (default 0): 0 = every P_ij in its row; 2 = quads: each row as
  * windows of 4 consecutive columns (a 16-bit base and 4 values, zeros where a column
  * is not kept; fewer bytes when segments are numbered depth-first, so a row's
- * columns form runs; every neuron needs 4 segments); 1 = pairs: each
+ * columns form runs); 1 = pairs: each
  * coupling (i, j) stored once, in the row of the segment with the smaller
  * capacitance, and applied to both rows through detailed balance c_i P_ij = c_j P_ji
  * (propagators from nw_propagator_build only; kept when the other row pruned it, so

@@ -651,8 +651,9 @@ int ensure_flux(nw_ctx* ctx) {
 
 // ------------------------------------------------- quad format
 
-// Quads of row r: windows [b, b+3] (b <= neuron end - 4) opened at an entry that
-// does not fit the current window, in the row's entry order.  With columns in
+// Quads of row r: windows [b, b+3] (b <= neuron end - 4, and b = the neuron's first
+// segment for neurons of fewer than 4) opened at an entry that does not fit the
+// current window, in the row's entry order.  With columns in
 // increasing order every window is as full as the runs allow.
 __device__ __forceinline__ int64_t quad_window(int64_t c, int64_t lo, int64_t hi) {
     int64_t b = c;
@@ -707,9 +708,6 @@ void free_quads(nw_ctx* ctx) {
 int ensure_quads(nw_ctx* ctx) {
     if (ctx->q_ok) return NW_OK;
     if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "quad format: needs the batched format (neurons <= 65,535)");
-    for (int64_t j = 0; j < ctx->n_neuron; ++j)
-        if (ctx->h_neuron_start[j + 1] - ctx->h_neuron_start[j] < 4)
-            return fail(ctx, NW_ERR_LIMIT, "quad format: every neuron needs at least 4 segments");
     const int64_t n = ctx->n_seg;
     std::vector<int64_t> lo(n), hi(n);
     for (int64_t j = 0; j < ctx->n_neuron; ++j)

@@ -355,6 +355,10 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         const int j = a.neuron_order[job];
         const int64_t base = a.neuron_start[j];
         const int n = (int)(a.neuron_start[j + 1] - base);
+        if (QUAD && n < 4) {
+            // Quad windows of a neuron of fewer than 4 segments reach past it: zeros there.
+            for (int li = n + threadIdx.x; li < 4; li += blockDim.x) xs[li] = real(0);
+        }
         if (FLUX) {
             // c_max / c of the neuron's segments next to x; sums start at zero (the
             // finalize pass leaves them at zero for the next half step).

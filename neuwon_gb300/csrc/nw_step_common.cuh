@@ -474,8 +474,9 @@ __device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t 
 }
 
 // Quad format: row i is a list of windows (base b, values v0..v3 for columns
-// b..b+3); the window's four x are consecutive in shared memory.
-template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 8 : 2), typename Fin>
+// b..b+3); the window's four x are consecutive in shared memory (neurons of
+// fewer than 4 segments keep zeros in x[n..3]).
+template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
 __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t base, int n,
                                                 const real* __restrict__ xs, Fin fin) {
     constexpr int GPW = 32 / LPR;
@@ -502,7 +503,7 @@ __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t
                         b[u] = __ldcs(a.qbase + k);
                     } else {
                         v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
-                        b[u] = 0;                         // zero weights on x[0..3] (n >= 4)
+                        b[u] = 0;                         // zero weights on x[0..3]
                     }
                 }
 #pragma unroll

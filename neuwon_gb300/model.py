@@ -276,7 +276,7 @@ class RxD_Model:
                  extracellular_tortuosity=1.55, extracellular_max_distance=20e-6,
                  species=(), mechanisms=(), precision="f32", device=0,
                  propagator_tolerance=EPSILON, propagator_conserve=False, path="batched",
-                 propagator_format="rows"):
+                 propagator_format="quads"):
         from .species import Calcium
         self._calcium = None
         for sp in species:
