@@ -613,14 +613,14 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");
     if (rows) *rows = ctx->n_seg;
     if (nnz) *nnz = ctx->nnz64;
-    if (ctx->prop_format == 2) {
+    if (ctx->prop_format == 2 && ctx->b_ok) {
         // Quad format: 4 value slots + a 16-bit base per quad.
         NW_CHECK(ensure_quads(ctx));
         if (stored) *stored = 4 * ctx->nq;
         if (bytes) *bytes = ctx->nq * (4 * ctx->precision + 2) + ctx->n_seg * (8 + ctx->precision);
         return NW_OK;
     }
-    if (ctx->prop_format == 1) {
+    if (ctx->prop_format == 1 && ctx->b_ok) {
         // Pair format: stored pairs, with c_max / c_i per row besides the leak.
         NW_CHECK(ensure_flux(ctx));
         if (stored) *stored = ctx->nnz_f;
@@ -1090,8 +1090,6 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         if (value < 0 || value > 2) return fail(ctx, NW_ERR_ARG, "propagator_format must be 0, 1 or 2");
         if (value == 1 && !ctx->prop_built)
             return fail(ctx, NW_ERR_STATE, "pair format needs a propagator built by nw_propagator_build");
-        if (value == 2 && ctx->max_neuron > 65535)
-            return fail(ctx, NW_ERR_LIMIT, "quad format: a neuron has more than 65,535 segments");
         ctx->prop_format = (int)value;
         return NW_OK;
     }
