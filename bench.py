@@ -29,11 +29,11 @@ sys.path.insert(0, ROOT)
 METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoint ms/step"
 
 # DRAM bytes (read + write) per segment-step of batched_advance_kernel, from one ncu
-# capture of one 50-step launch of the default configuration (tolerance 1e-8, 1,024
-# neurons, 5,593,190 segments): 1,741.6 GB per launch.  Command and figures:
-# profiles/batched_advance_kernel.md.
-NCU_TRAFFIC_PER_SEGMENT_STEP = 6227.5
-NCU_TRAFFIC_CONFIG = ("rows", 1e-8, 5593190)
+# capture of one full-size launch per propagator format (tolerance 1e-8, 1,024
+# neurons, 5,593,190 segments): quads 742.6 GB per 25-step launch, rows 1,741.6 GB per
+# 50-step launch.  Commands and figures: profiles/batched_advance_kernel.md.
+NCU_TRAFFIC_PER_SEGMENT_STEP = {"quads": 5310.6, "rows": 6227.5}
+NCU_TRAFFIC_CONFIG = (1e-8, 5593190)
 
 
 def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
@@ -603,8 +603,9 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "traffic": (NCU_TRAFFIC_PER_SEGMENT_STEP * n * F
-                                 if (args.format, args.tol, n) == NCU_TRAFFIC_CONFIG else None),
+                     "traffic": (NCU_TRAFFIC_PER_SEGMENT_STEP[args.format] * n * F
+                                 if (args.tol, n) == NCU_TRAFFIC_CONFIG and args.format in NCU_TRAFFIC_PER_SEGMENT_STEP
+                                 else None),
                      "traffic_unit": f"bytes per launch of {F} steps (ncu dram__bytes_read+write)",
                      "algorithmic_bytes_per_launch": B_alg * n * F,
                      "peak_source": peak_src,
