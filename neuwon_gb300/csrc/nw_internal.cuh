@@ -187,6 +187,9 @@ struct nw_ctx {
     bool q_ok = false;
     int64_t nq = 0;
     nw::DevBuf q_rowptr, q_base, q_val;                // i64 (in quads), u16 (neuron-relative), real x 4
+    bool wq_ok = false;                                // wide path: global 32-bit bases
+    int64_t nwq = 0;
+    nw::DevBuf wq_rowptr, wq_base, wq_val;
     int prop_format = 0;                               // 0: rows, 1: pairs, 2: quads
     int pair_shared_limit = -1;                        // cap on neurons with shared-memory sums (-1: none)
 
@@ -262,6 +265,7 @@ int advance_wide(nw_ctx* ctx, int k_steps);
 int ensure_wide(nw_ctx* ctx);
 int ensure_flux(nw_ctx* ctx);
 int ensure_quads(nw_ctx* ctx);
+int ensure_wide_quads(nw_ctx* ctx);
 void free_quads(nw_ctx* ctx);
 void free_flux(nw_ctx* ctx);
 void free_wide(nw_ctx* ctx);

@@ -677,10 +677,10 @@ __global__ void quad_count_kernel(int64_t n, const int64_t* nstart_of_row, const
     cnt[r] = q;
 }
 
-template <typename real>
+template <typename real, typename BT>
 __global__ void quad_fill_kernel(int64_t n, const int64_t* nstart_of_row, const int64_t* nend_of_row,
                                  const int64_t* prow, const int32_t* pcol, const double* pval,
-                                 const int64_t* qrow, uint16_t* qbase, real* qval) {
+                                 const int64_t* qrow, BT* qbase, real* qval, int relative) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= n) return;
     const int64_t lo = nstart_of_row[r], hi = nend_of_row[r];
@@ -691,7 +691,7 @@ __global__ void quad_fill_kernel(int64_t n, const int64_t* nstart_of_row, const 
         if (b < 0 || c < b || c > b + 3 || c <= last) {
             b = quad_window(c, lo, hi);
             ++q;
-            qbase[q] = (uint16_t)(b - lo);
+            qbase[q] = (BT)(relative ? b - lo : b);
             for (int j = 0; j < 4; ++j) qval[4 * q + j] = real(0);
         }
         qval[4 * q + (c - b)] = (real)pval[k];
@@ -700,21 +700,27 @@ __global__ void quad_fill_kernel(int64_t n, const int64_t* nstart_of_row, const 
 }
 
 void free_quads(nw_ctx* ctx) {
-    for (DevBuf* b : {&ctx->q_rowptr, &ctx->q_base, &ctx->q_val}) dev_free(*b);
-    ctx->q_ok = false;
-    ctx->nq = 0;
+    for (DevBuf* b : {&ctx->q_rowptr, &ctx->q_base, &ctx->q_val, &ctx->wq_rowptr, &ctx->wq_base, &ctx->wq_val})
+        dev_free(*b);
+    ctx->q_ok = ctx->wq_ok = false;
+    ctx->nq = ctx->nwq = 0;
 }
 
-int ensure_quads(nw_ctx* ctx) {
-    if (ctx->q_ok) return NW_OK;
-    if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "quad format: needs the batched format (neurons <= 65,535)");
+// Quads of the FP64 CSR: neuron-relative 16-bit bases (batched path) or global
+// 32-bit bases (wide path; windows of neurons of fewer than 4 segments may
+// reach into the neighbouring segments, whose weights are zero).
+template <typename BT>
+static int build_quads(nw_ctx* ctx, bool relative, DevBuf& R, DevBuf& B, DevBuf& V, int64_t* nq_out) {
     const int64_t n = ctx->n_seg;
     std::vector<int64_t> lo(n), hi(n);
-    for (int64_t j = 0; j < ctx->n_neuron; ++j)
-        for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) {
-            lo[i] = ctx->h_neuron_start[j];
-            hi[i] = ctx->h_neuron_start[j + 1];
+    for (int64_t j = 0; j < ctx->n_neuron; ++j) {
+        int64_t l = ctx->h_neuron_start[j], h = ctx->h_neuron_start[j + 1];
+        if (!relative) {
+            h = std::min<int64_t>(std::max<int64_t>(h, l + 4), n);
+            l = std::min<int64_t>(l, h - 4);
         }
+        for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) { lo[i] = l; hi[i] = h; }
+    }
     DevBuf d_lo, d_hi, d_cnt;
     auto cleanup = [&]() { dev_free(d_lo); dev_free(d_hi); dev_free(d_cnt); };
     int rc = NW_OK;
@@ -733,27 +739,41 @@ int ensure_quads(nw_ctx* ctx) {
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "quad format count"); break; }
         for (int64_t i = 0; i < n; ++i) qrow[i + 1] = qrow[i] + cnt[i];
         const int64_t nq = qrow[n];
-        if ((rc = dev_alloc(ctx, ctx->q_rowptr, 8 * (n + 1))) != NW_OK) break;
-        if ((rc = dev_alloc(ctx, ctx->q_base, 2 * std::max<int64_t>(nq, 8))) != NW_OK) break;
-        if ((rc = dev_alloc(ctx, ctx->q_val, (size_t)ctx->precision * 4 * std::max<int64_t>(nq, 1))) != NW_OK) break;
-        cudaMemcpyAsync(ctx->q_rowptr.ptr, qrow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        if ((rc = dev_alloc(ctx, R, 8 * (n + 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, B, sizeof(BT) * std::max<int64_t>(nq, 8))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, V, (size_t)ctx->precision * 4 * std::max<int64_t>(nq, 1))) != NW_OK) break;
+        cudaMemcpyAsync(R.ptr, qrow.data(), 8 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
         if (ctx->precision == NW_F64)
-            quad_fill_kernel<double><<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
+            quad_fill_kernel<double, BT><<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
                 n, d_lo.as<int64_t>(), d_hi.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
-                ctx->p_val.as<double>(), ctx->q_rowptr.as<int64_t>(), ctx->q_base.as<uint16_t>(),
-                ctx->q_val.as<double>());
+                ctx->p_val.as<double>(), R.as<int64_t>(), B.as<BT>(), V.as<double>(), relative ? 1 : 0);
         else
-            quad_fill_kernel<float><<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
+            quad_fill_kernel<float, BT><<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
                 n, d_lo.as<int64_t>(), d_hi.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(),
-                ctx->p_val.as<double>(), ctx->q_rowptr.as<int64_t>(), ctx->q_base.as<uint16_t>(),
-                ctx->q_val.as<float>());
+                ctx->p_val.as<double>(), R.as<int64_t>(), B.as<BT>(), V.as<float>(), relative ? 1 : 0);
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "quad format fill"); break; }
-        ctx->nq = nq;
-        ctx->q_ok = true;
+        *nq_out = nq;
     } while (0);
     cleanup();
     return rc;
+}
+
+int ensure_quads(nw_ctx* ctx) {
+    if (ctx->q_ok) return NW_OK;
+    if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "quad format: needs the batched format (neurons <= 65,535)");
+    NW_CHECK(build_quads<uint16_t>(ctx, true, ctx->q_rowptr, ctx->q_base, ctx->q_val, &ctx->nq));
+    ctx->q_ok = true;
+    return NW_OK;
+}
+
+int ensure_wide_quads(nw_ctx* ctx) {
+    if (ctx->wq_ok) return NW_OK;
+    if (ctx->n_seg < 4) return fail(ctx, NW_ERR_LIMIT, "quad format: fewer than 4 segments");
+    NW_CHECK(ensure_wide(ctx));                 // the leak comes with the wide row format
+    NW_CHECK(build_quads<int32_t>(ctx, false, ctx->wq_rowptr, ctx->wq_base, ctx->wq_val, &ctx->nwq));
+    ctx->wq_ok = true;
+    return NW_OK;
 }
 
 // Called whenever the FP64 propagator changes: rebuilds the batched format (if

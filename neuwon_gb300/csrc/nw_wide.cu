@@ -68,6 +68,39 @@ wide_rows_kernel(const int64_t* __restrict__ rowptr, const int32_t* __restrict__
     }
 }
 
+// Quad format with global bases: each window's four x are consecutive in memory
+// (one or two cache sectors instead of four).
+template <typename real, int LPR>
+__global__ void __launch_bounds__(kWideThreads)
+wide_quads_kernel(const int64_t* __restrict__ qrow, const int32_t* __restrict__ qbase,
+                  const real* __restrict__ qval, const real* __restrict__ leak, const real* __restrict__ x,
+                  real* __restrict__ y, const int64_t n, int* status) {
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPR;
+    const int l = threadIdx.x % LPR;
+    const bool valid = g < n;
+    real s = real(0), c = real(0), xi = real(0);
+    if (valid) {
+        xi = __ldg(x + g);
+        const int64_t beg = qrow[g], end = qrow[g + 1];
+        for (int64_t k = beg + l; k < end; k += LPR) {
+            real v[4];
+            Vec4Loader<real>::load(qval + 4 * k, v);
+            const real* xb = x + __ldcs(qbase + k);
+            const real p = v[0] * (__ldg(xb) - xi) + v[1] * (__ldg(xb + 1) - xi);
+            const real q = v[2] * (__ldg(xb + 2) - xi) + v[3] * (__ldg(xb + 3) - xi);
+            kahan_add(s, c, p + q);
+        }
+    }
+    real t = s - c;
+#pragma unroll
+    for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off, LPR);
+    if (valid && l == 0) {
+        const real vnew = (xi - leak[g] * xi) + t;
+        if (!isfinite(vnew)) atomicOr(status, kStatusNonFinite);
+        y[g] = vnew;
+    }
+}
+
 template <typename real>
 __global__ void __launch_bounds__(kWideThreads)
 wide_mechanism_kernel(const StepArgs<real> a, const int s_off, const int64_t n_hh, const int64_t n_kin,
@@ -146,6 +179,26 @@ static int launch_rows(nw_ctx* ctx, int lanes, const int64_t* R, const int32_t* 
     return NW_OK;
 }
 
+template <typename real>
+static int launch_quads(nw_ctx* ctx, const StepArgs<real>& a) {
+    const int64_t n = ctx->n_seg;
+    const double avg = n ? (double)ctx->nwq / (double)n : 0.0;
+    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg >= 24 ? 8 : 4);
+    const unsigned blocks = (unsigned)((n * lanes + kWideThreads - 1) / kWideThreads);
+    const int64_t* R = ctx->wq_rowptr.as<int64_t>();
+    const int32_t* B = ctx->wq_base.as<int32_t>();
+    const real* V = ctx->wq_val.as<real>();
+    const real* L = ctx->w_leak.as<real>();
+    switch (lanes) {
+        case 4: wide_quads_kernel<real, 4><<<blocks, kWideThreads, 0, ctx->stream>>>(R, B, V, L, a.px, a.V, n, a.status); break;
+        case 8: wide_quads_kernel<real, 8><<<blocks, kWideThreads, 0, ctx->stream>>>(R, B, V, L, a.px, a.V, n, a.status); break;
+        case 16: wide_quads_kernel<real, 16><<<blocks, kWideThreads, 0, ctx->stream>>>(R, B, V, L, a.px, a.V, n, a.status); break;
+        default: wide_quads_kernel<real, 32><<<blocks, kWideThreads, 0, ctx->stream>>>(R, B, V, L, a.px, a.V, n, a.status); break;
+    }
+    NW_CUDA(ctx, cudaGetLastError());
+    return NW_OK;
+}
+
 // The launches of `steps` steps (no host synchronisation: also a graph body).
 template <typename real>
 static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lanes) {
@@ -159,7 +212,8 @@ static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lan
             const int last = (s == steps - 1 && half == 1) ? 1 : 0;
             wide_membrane_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a, s, half, last);
             NW_CUDA(ctx, cudaGetLastError());
-            NW_CHECK(launch_rows<real>(ctx, lanes, a.wrow, a.wcol, a.wval, a.wleak, a.px, a.V, a.status));
+            if (ctx->prop_format == 2 && ctx->wq_ok) NW_CHECK(launch_quads<real>(ctx, a));
+            else NW_CHECK(launch_rows<real>(ctx, lanes, a.wrow, a.wcol, a.wval, a.wleak, a.px, a.V, a.status));
             if (a.ca_on) {
                 wide_calcium_prepare_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
                 NW_CUDA(ctx, cudaGetLastError());
@@ -217,6 +271,12 @@ static int wide_graph(nw_ctx* ctx, const StepArgs<real>& a0, int steps, int lane
     key_bytes(key, &ctx->kin.m, sizeof(ctx->kin.m));
     key_bytes(key, &ctx->syn.n, sizeof(ctx->syn.n));
     key_bytes(key, &ctx->ca.on, sizeof(ctx->ca.on));
+    key_bytes(key, &ctx->prop_format, sizeof(ctx->prop_format));
+    key_bytes(key, &ctx->wq_ok, sizeof(ctx->wq_ok));
+    key_bytes(key, &ctx->wq_rowptr.ptr, sizeof(void*));
+    key_bytes(key, &ctx->wq_base.ptr, sizeof(void*));
+    key_bytes(key, &ctx->wq_val.ptr, sizeof(void*));
+    key_bytes(key, &ctx->nwq, sizeof(ctx->nwq));
     for (auto& g : ctx->graphs) {
         if (g.key == key) {
             g.last_use = ++ctx->graph_uses;
@@ -259,6 +319,7 @@ static int wide_graph(nw_ctx* ctx, const StepArgs<real>& a0, int steps, int lane
 template <typename real>
 static int wide_steps(nw_ctx* ctx, int k_steps) {
     NW_CHECK(ensure_wide(ctx));
+    if (ctx->prop_format == 2 && ctx->n_seg >= 4) NW_CHECK(ensure_wide_quads(ctx));
     if (ctx->ca.on) NW_CHECK(calcium_ensure_wide(ctx));
     const int lanes = wide_lanes(ctx);
     // Every phase is its own launch, so a spike written by one step's detector

@@ -67,3 +67,25 @@ def test_wide_graph_chunks_are_bit_identical_to_direct_launches():
             assert m._ctx.get_option("graph_captures") == 2
         m.close()
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_wide_quads_equal_wide_rows(precision):
+    """The wide path's quad format (global 32-bit window bases) holds the row
+    format's entries; a 2-segment neuron's windows reach into its neighbour."""
+    trees = [random_tree(n, seed=30 + n) for n in (1500, 2, 400)]
+    out = []
+    for fmt in ("rows", "quads"):
+        m = nw.RxD_Model(time_step=0.1, temperature=6.3, precision=precision, path="wide", propagator_tolerance=1e-8,
+                         propagator_conserve=True, propagator_format=fmt,
+                         mechanisms=[nw.HH.configure(ena=50.0, ek=-77.0, el=-54.3)])
+        for t in trees:
+            nr = m.add_tree(t)
+            nr.root.inject_current(0.4, 1e6)
+        m.insert_everywhere("hh")
+        m.advance(200)
+        out.append((m.get_data("Segment.voltage"), m.get_data("Neuron.spike_count")))
+        m.close()
+    tol = 1e-9 if precision == "f64" else 2e-3
+    assert np.abs(out[0][0] - out[1][0]).max() < tol
+    assert np.array_equal(out[0][1], out[1][1])
