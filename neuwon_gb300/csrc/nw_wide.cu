@@ -82,13 +82,28 @@ wide_quads_kernel(const int64_t* __restrict__ qrow, const int32_t* __restrict__ 
     if (valid) {
         xi = __ldg(x + g);
         const int64_t beg = qrow[g], end = qrow[g + 1];
-        for (int64_t k = beg + l; k < end; k += LPR) {
-            real v[4];
-            Vec4Loader<real>::load(qval + 4 * k, v);
-            const real* xb = x + __ldcs(qbase + k);
-            const real p = v[0] * (__ldg(xb) - xi) + v[1] * (__ldg(xb + 1) - xi);
-            const real q = v[2] * (__ldg(xb + 2) - xi) + v[3] * (__ldg(xb + 3) - xi);
-            kahan_add(s, c, p + q);
+        // Two windows per lane in flight.
+        for (int64_t k0 = beg + l; k0 < end; k0 += 2 * LPR) {
+            real v[2][4];
+            int32_t b[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int64_t k = k0 + LPR * u;
+                if (k < end) {
+                    Vec4Loader<real>::load(qval + 4 * k, v[u]);
+                    b[u] = __ldcs(qbase + k);
+                } else {
+                    v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                    b[u] = 0;                 // zero weights on x[0..3] (n >= 4)
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const real* xb = x + b[u];
+                const real p = v[u][0] * (__ldg(xb) - xi) + v[u][1] * (__ldg(xb + 1) - xi);
+                const real q = v[u][2] * (__ldg(xb + 2) - xi) + v[u][3] * (__ldg(xb + 3) - xi);
+                kahan_add(s, c, p + q);
+            }
         }
     }
     real t = s - c;
@@ -183,7 +198,7 @@ template <typename real>
 static int launch_quads(nw_ctx* ctx, const StepArgs<real>& a) {
     const int64_t n = ctx->n_seg;
     const double avg = n ? (double)ctx->nwq / (double)n : 0.0;
-    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg >= 24 ? 8 : 4);
+    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg >= 48 ? 16 : avg >= 12 ? 8 : 4);
     const unsigned blocks = (unsigned)((n * lanes + kWideThreads - 1) / kWideThreads);
     const int64_t* R = ctx->wq_rowptr.as<int64_t>();
     const int32_t* B = ctx->wq_base.as<int32_t>();
