@@ -151,19 +151,20 @@ __global__ void edge_pivots_kernel(const BuildArgs a) {
 // value reaches the exploration threshold (the top one, if it does not, still
 // leads down the chain), so the visited set is the same as a plain walk's.
 __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a, const int fill) {
-    const int lane = threadIdx.x & 31;
-    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    // Two rows per warp: each half-warp walks one row, one lane per pole.
+    static_assert(kPoles == 16, "a half-warp carries the 16 poles");
+    const int lane = threadIdx.x & 15;
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 4;
+    const unsigned half_mask = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;
     if (row >= a.n_seg) return;
-    const bool act = lane < kPoles;
-    const int k = act ? lane : 0;
-    const cplx w = act ? cplx(c_w[k].x, c_w[k].y) : cplx(0.0, 0.0);
+    const int k = lane;
+    const cplx w = cplx(c_w[k].x, c_w[k].y);
     const double scale_out = 2.0 / kNodes;
     auto value = [&](cplx yy) -> double {
-        const cplx wy = w * yy;
-        double v = act ? wy.im : 0.0;
+        double v = (w * yy).im;
 #pragma unroll
-        for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        return __shfl_sync(0xffffffffu, v, 0) * scale_out;
+        for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(half_mask, v, off, 16);
+        return __shfl_sync(half_mask, v, 0, 16) * scale_out;
     };
     int32_t chain[kChainDepth];
     cplx chain_y[kChainDepth];
@@ -319,8 +320,8 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
             int64_t threads = 128, blocks = (nn * kPoles + threads - 1) / threads;
             edge_pivots_kernel<<<(unsigned)blocks, (unsigned)threads, 0, ctx->stream>>>(a);
         }
-        const int64_t rows_per_block = 8;
-        const int64_t rblocks = (n + rows_per_block - 1) / rows_per_block;
+        const int64_t rows_per_block = 16;
+        const int64_t rblocks = (n + rows_per_block - 1) / rows_per_block;   // 16 rows per 256-thread block
         propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 0);
         if (cudaGetLastError() != cudaSuccess) { rc = fail(ctx, NW_ERR_CUDA, "propagator build launch failed"); break; }
         std::vector<int64_t> cnt(n);
