@@ -351,7 +351,7 @@ def precision_study(args, device):
     log(f"precision study: tree of {len(tree)} segments in {time.perf_counter() - t0:.1f} s")
     out = {"metric": "precision study: FP32 vs FP64, max |dV| (mV) and max relative d[Ca]",
            "config": {"workload": f"one tree of {len(tree)} segments, HH + calcium (diffusion 0.6 um2/ms, 3-state "
-                                  "pump, 0.5 % of the Na current as Ca), 1 nA soma clamp, dt 0.025 ms",
+                                  f"pump, 0.5 % of the Na current as Ca), {args.study_current:g} nA soma clamp, dt 0.025 ms",
                       "steps": steps, "path": "wide", "pruning": "charge/mass-conserving"},
            "results": []}
     for tol in (1e-6, 1e-9):
@@ -363,7 +363,7 @@ def precision_study(args, device):
                              mechanisms=[nw.HH.configure(ena=50.0, ek=-77.0, el=-54.3)])
             nr = m.add_tree(tree)
             m.insert_everywhere("hh")
-            nr.root.inject_current(1.0, 1e9)
+            nr.root.inject_current(args.study_current, 1e9)
             m._sync()
             m._ctx.call("nw_synchronize")
             models[precision] = (m, time.perf_counter() - t0)
@@ -426,6 +426,7 @@ def main():
                     help="run only the 1 M-segment FP32-vs-FP64 calcium precision study")
     ap.add_argument("--study-segments", type=int, default=1_000_000)
     ap.add_argument("--study-steps", type=int, default=20000)
+    ap.add_argument("--study-current", type=float, default=10.0, help="soma clamp of the precision study (nA)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
