@@ -300,6 +300,11 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * (< N), the spike ring covers all N neurons with this model's neuron j at o + j, and
  * its length is at least R steps (a common value for all ranks); the ranks sum their
  * rings (own neurons only) after every epoch of at most the shortest delay.
+ * "propagator_lump" (default 0), taken by the next nw_propagator_build / nw_calcium_set:
+ * an entry below the tolerance is added to the nearest kept entry on the tree path
+ * from its segment towards the row's segment instead of being dropped (row sums are
+ * kept; far lower error than dropping at the same tolerance, so fewer entries for
+ * the same accuracy); unvisited remainders still need nw_propagator_conserve.
  * "set_steps" (k): resume at step k (clock, input ticks 2k, conductances valid when
  * k > 0 and mechanisms exist; probes start empty), for restoring a checkpoint.
  * "fusion_depth" (default 50, 0 = the whole call in one launch): steps per launch of

@@ -554,7 +554,8 @@ int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out) {
     NW_CHECK(propagator_build(ctx, prune_tolerance, nnz_out));
     NW_CHECK(propagator_to_batched(ctx));
     ctx->prop_valid = true;
-    ctx->prop_built = true;
+    ctx->prop_built = !ctx->prop_lump;           // lumped rows break detailed balance
+    if (ctx->prop_lump && ctx->prop_format == 1) ctx->prop_format = 0;
     return NW_OK;
 }
 
@@ -1084,6 +1085,13 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         ctx->pair_shared_limit = (int)value;
         return NW_OK;
     }
+    if (nm == "propagator_lump") {
+        // Taken by the next propagator build: a value below the tolerance is added to
+        // the nearest kept entry on the tree path towards the row's segment instead
+        // of being dropped (row sums unchanged; pair format unavailable).
+        ctx->prop_lump = value != 0;
+        return NW_OK;
+    }
     if (nm == "propagator_format") {
         // 0: rows (every P_ij stored in its row); 1: pairs (each coupling once,
         // applied to both rows through detailed balance; built propagators only).
@@ -1144,6 +1152,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "bulk_pipeline_active") { *value = uses_bulk_pipeline(ctx) ? 1 : 0; return NW_OK; }
     if (nm == "cuda_graph") { *value = ctx->use_graph ? 1 : 0; return NW_OK; }
     if (nm == "propagator_format") { *value = ctx->prop_format; return NW_OK; }
+    if (nm == "propagator_lump") { *value = ctx->prop_lump ? 1 : 0; return NW_OK; }
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "quads") { *value = ctx->nq; return NW_OK; }
     if (nm == "fusion_depth") { *value = ctx->fusion; return NW_OK; }

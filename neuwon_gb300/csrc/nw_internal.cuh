@@ -168,6 +168,7 @@ struct nw_ctx {
     // columns, rows padded to 4 entries, per-row leak = 1 - row sum).
     bool prop_valid = false;
     bool prop_built = false;    // built here (detailed balance holds): the pair format may be used
+    bool prop_lump = false;     // next build moves dropped values to the nearest kept node (option "propagator_lump")
     bool b_ok = false;          // batched format present (every neuron <= 65,535 segments)
     bool w_ok = false;          // wide format present (built on first use of the wide path)
     int64_t nnz64 = 0, nnz_b = 0, nnz_w = 0;
@@ -251,7 +252,7 @@ int propagator_from_host(nw_ctx* ctx, const int64_t* rowptr, const int64_t* col,
                          const double* val, int64_t nnz);
 int propagator_to_batched(nw_ctx* ctx);
 int propagator_conserve(nw_ctx* ctx);
-int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap, double h_s, double tol,
+int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap, double h_s, double tol, int lump,
                           DevBuf& out_rowptr, DevBuf& out_col, DevBuf& out_val, int64_t* nnz_out);
 int csr_conserve(nw_ctx* ctx, DevBuf& rowptr, DevBuf& col, DevBuf& val);
 template <typename CT>

@@ -33,7 +33,7 @@ namespace nw {
 constexpr int kPoles = 16;            // N/2 for N = 32
 constexpr int kNodes = 2 * kPoles;
 constexpr int kStackDepth = 64;
-constexpr int kChainDepth = 384;
+constexpr int kChainDepth = 256;
 constexpr double kExploreFactor = 1e-2;
 constexpr int kStatusStackOverflow = 2;
 constexpr int kStatusRowMismatch = 4;
@@ -79,6 +79,7 @@ struct BuildArgs {
     double2* up;                // pivot of the rest of the tree, seen from c
     double2* invT;              // 1 / total pivot: diagonal of the resolvent
     double tol, explore;
+    int lump;                   // fill pass: move dropped values to the nearest kept node toward the row
     int64_t* count;             // [n_seg] kept entries per row
     const int64_t* rowptr;      // fill pass
     int32_t* out_col;
@@ -168,8 +169,17 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
     };
     int32_t chain[kChainDepth];
     cplx chain_y[kChainDepth];
-    int32_t st_node[kStackDepth], st_cp[kStackDepth];
+    int32_t st_node[kStackDepth], st_cp[kStackDepth], st_tchain[kStackDepth];
+    int64_t st_tslot[kStackDepth];
     cplx st_y[kStackDepth];
+    // Lumping: a dropped value goes to the nearest kept node on the tree path to the
+    // row's segment.  Off the chain that is an already emitted ancestor (its slot is
+    // carried down the stack) or a chain position; chain positions are settled after
+    // the walk, flowing down the chain to the first kept node (the row's own
+    // segment is always kept).
+    int64_t chain_slot[kChainDepth];
+    double carry[kChainDepth];
+    const bool lump = fill && a.lump;
     int64_t kept = 0;
     int64_t out = fill ? a.rowptr[row] : 0;
     const int64_t out_end = fill ? a.rowptr[row + 1] : 0;
@@ -194,21 +204,37 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
         chain_y[depth] = y;
         v = value(y);
     }
+    if (lump)
+        for (int m = 0; m <= depth; ++m) { carry[m] = 0.0; chain_slot[m] = -1; }
     {
         // Preorder from the top; st_cp = position on the chain, -1 off it.
         int sp = 0;
-        st_node[0] = chain[depth]; st_cp[0] = depth; st_y[0] = chain_y[depth]; sp = 1;
+        st_node[0] = chain[depth]; st_cp[0] = depth; st_y[0] = chain_y[depth];
+        st_tslot[0] = -1; st_tchain[0] = depth; sp = 1;
         while (sp > 0) {
             --sp;
             const int64_t u = st_node[sp];
             const int cp = st_cp[sp];
             const cplx yu = st_y[sp];
+            const int64_t tslot = st_tslot[sp];
+            const int tchain = st_tchain[sp];
             const double vu = value(yu);
-            if (fabs(vu) >= a.tol) {
+            const bool keep = fabs(vu) >= a.tol;
+            int64_t myslot = -1;
+            if (keep) {
                 if (fill && lane == 0 && out < out_end) { a.out_col[out] = (int32_t)u; a.out_val[out] = vu; }
+                myslot = out;
                 ++out;
                 ++kept;
+            } else if (lump) {
+                if (cp >= 0) carry[cp] += vu;
+                else if (tslot >= 0) { if (lane == 0 && tslot < out_end) a.out_val[tslot] += vu; }
+                else carry[tchain] += vu;
             }
+            if (lump && cp >= 0) chain_slot[cp] = myslot;
+            // Where this node's dropped descendants go.
+            const int64_t child_tslot = keep ? myslot : (cp >= 0 ? -1 : tslot);
+            const int child_tchain = cp >= 0 ? cp : tchain;
             const bool expand = fabs(vu) >= a.explore;
             const int64_t chain_child = cp > 0 ? chain[cp - 1] : -1;
             if (!expand) {
@@ -217,7 +243,8 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
                     if (lane == 0) atomicOr(a.status, kStatusStackOverflow);
                     goto done;
                 }
-                st_node[sp] = (int32_t)chain_child; st_cp[sp] = cp - 1; st_y[sp] = chain_y[cp - 1]; ++sp;
+                st_node[sp] = (int32_t)chain_child; st_cp[sp] = cp - 1; st_y[sp] = chain_y[cp - 1];
+                st_tslot[sp] = -1; st_tchain[sp] = cp - 1; ++sp;
                 continue;
             }
             // Children pushed last-first so that they come off the stack in index order.
@@ -229,10 +256,22 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
                 }
                 if (c == chain_child) {
                     st_node[sp] = (int32_t)c; st_cp[sp] = cp - 1; st_y[sp] = chain_y[cp - 1];
+                    st_tslot[sp] = -1; st_tchain[sp] = cp - 1;
                 } else {
                     st_node[sp] = (int32_t)c; st_cp[sp] = -1; st_y[sp] = ld(&a.down[c * kPoles + k]) * yu;
+                    st_tslot[sp] = child_tslot; st_tchain[sp] = child_tchain;
                 }
                 ++sp;
+            }
+        }
+        if (lump && lane == 0) {
+            double acc = 0.0;
+            for (int m = depth; m >= 0; --m) {
+                acc += carry[m];
+                if (chain_slot[m] >= 0) {
+                    if (chain_slot[m] < out_end) a.out_val[chain_slot[m]] += acc;
+                    acc = 0.0;
+                }
             }
         }
     }
@@ -262,7 +301,7 @@ static void contour_nodes(double2* z, double2* w) {
 // expm(A h) of the tree operator with edge "resistances" d_res (child edge) and
 // node "capacities" d_cap (coefficients h_s / (R C), electric.py:85-109 form),
 // pruned at tol, into an FP64 CSR with global int32 columns.
-int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap, double h_s, double tol,
+int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap, double h_s, double tol, int lump,
                           DevBuf& out_rowptr, DevBuf& out_col, DevBuf& out_val, int64_t* nnz_out) {
     const int64_t n = ctx->n_seg, nn = ctx->n_neuron;
     // Children lists and edge conductance sums (host, O(n)).
@@ -314,6 +353,7 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
         a.h_s = h_s;
         a.down = d_down.as<double2>(); a.up = d_up.as<double2>(); a.invT = d_invT.as<double2>();
         a.tol = tol; a.explore = tol * kExploreFactor;
+        a.lump = lump;
         a.count = d_count.as<int64_t>();
         a.status = ctx->status.as<int>();
         {
@@ -364,7 +404,8 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
 int propagator_build(nw_ctx* ctx, double tol, int64_t* nnz_out) {
     int64_t nnz = 0;
     NW_CHECK(tree_propagator_build(ctx, ctx->res64.as<double>(), ctx->cap64.as<double>(),
-                                   0.5 * ctx->time_step * 1e-3, tol, ctx->p_rowptr, ctx->p_col, ctx->p_val, &nnz));
+                                   0.5 * ctx->time_step * 1e-3, tol, ctx->prop_lump ? 1 : 0, ctx->p_rowptr, ctx->p_col,
+                                   ctx->p_val, &nnz));
     ctx->nnz64 = nnz;
     if (nnz_out) *nnz_out = nnz;
     return NW_OK;

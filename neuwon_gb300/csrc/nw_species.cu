@@ -76,7 +76,7 @@ int nw_calcium_set(nw_ctx* ctx, double diffusivity, const double* cross_area_um2
     NW_CHECK(upload_convert(ctx, C.vol.ptr, NW_DTYPE_F64, vol.data(), NW_DTYPE_F64, n));
     int64_t nnz = 0;
     NW_CHECK(tree_propagator_build(ctx, C.res.as<double>(), C.vol.as<double>(), 0.5 * ctx->time_step * 1e-3,
-                                   prune_tolerance, C.p_rowptr, C.p_col, C.p_val, &nnz));
+                                   prune_tolerance, ctx->prop_lump ? 1 : 0, C.p_rowptr, C.p_col, C.p_val, &nnz));
     if (conserve) NW_CHECK(csr_conserve(ctx, C.p_rowptr, C.p_col, C.p_val));
     C.nnz64 = nnz;
     if (ctx->max_neuron <= 65535) {

@@ -260,6 +260,10 @@ class RxD_Model:
       propagator_tolerance  prune |P_ij| below this (reference: machine epsilon)
       propagator_conserve   return the pruned mass of each row to its diagonal
                             (charge-conserving pruning; the reference does not)
+      propagator_lump       move each pruned entry to the nearest kept entry on
+                            the tree path to the row's segment (charge stays
+                            near where it was: far smaller error than
+                            propagator_conserve at the same tolerance)
       propagator_format     'rows' (every P_ij in its row, 16-bit column each),
                             'quads' (windows of 4 consecutive columns with one
                             16-bit base: ~16 % fewer bytes with the model's
@@ -276,7 +280,7 @@ class RxD_Model:
                  extracellular_tortuosity=1.55, extracellular_max_distance=20e-6,
                  species=(), mechanisms=(), precision="f32", device=0,
                  propagator_tolerance=EPSILON, propagator_conserve=False, path="batched",
-                 propagator_format="quads"):
+                 propagator_format="quads", propagator_lump=False):
         from .species import Calcium
         self._calcium = None
         for sp in species:
@@ -295,6 +299,7 @@ class RxD_Model:
         self.propagator_conserve = bool(propagator_conserve)
         self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN, "wide": _lib.PATH_WIDE}[path]
         self.propagator_format = {"rows": 0, "pairs": 1, "quads": 2}[propagator_format]
+        self.propagator_lump = bool(propagator_lump)
         self.input_hook = Clock(0.5 * self.time_step, units="ms")
         self.advance_hook = self.clock = Clock(self.time_step, units="ms")
         # Segment table (creation order).
@@ -398,7 +403,8 @@ class RxD_Model:
         L = np.ascontiguousarray(g["length"][order], dtype=np.float64)
         vol = np.ascontiguousarray(g["volume"][order], dtype=np.float64)
         self._ctx.call("nw_calcium_set", ca.diffusivity, _lib.ptr(A), _lib.ptr(L), _lib.ptr(vol), ca.initial,
-                       self.propagator_tolerance, int(self.propagator_conserve), _lib.ctypes.byref(nnz))
+                       self.propagator_tolerance, int(self.propagator_conserve or self.propagator_lump),
+                       _lib.ctypes.byref(nnz))
         self.calcium_nnz = nnz.value
         geom_sorted = {k: np.asarray(v)[order] for k, v in g.items() if k in ("volume", "surface_area")}
         influx, efflux = (np.ascontiguousarray(x) for x in ca.coefficients(geom_sorted))
@@ -746,8 +752,9 @@ class RxD_Model:
         ctx.set_data("Segment.axial_resistance", np.where(par < 0, 1.0, g["axial_resistance"][order]))
         ctx.set_data("Segment.voltage", np.full(n, self.initial_voltage))
         nnz = _lib.ctypes.c_int64()
+        ctx.set_option("propagator_lump", int(self.propagator_lump))
         ctx.call("nw_propagator_build", self.propagator_tolerance, _lib.ctypes.byref(nnz))
-        if self.propagator_conserve:
+        if self.propagator_conserve or self.propagator_lump:
             ctx.call("nw_propagator_conserve")
         ctx.set_option("propagator_format", self.propagator_format)
         self.propagator_nnz = nnz.value

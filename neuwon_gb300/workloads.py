@@ -51,13 +51,13 @@ def batched_currents(num_neurons=1024, seed=0):
 
 
 def build_model(trees, currents_nA, *, precision="f32", tolerance=1e-7, conserve=True,
-                duration_ms=1e9, path="batched", device=0, kinetic=True, fmt="rows"):
+                duration_ms=1e9, path="batched", device=0, kinetic=True, fmt="rows", lump=False):
     """RxD_Model with HH (and na8) on every segment and a constant soma clamp per neuron."""
     from .model import RxD_Model
     mechs = [HH.configure(**HH_PARAMS)] + ([Kinetic] if kinetic else [])
     m = RxD_Model(time_step=TIME_STEP, temperature=CELSIUS, precision=precision, device=device,
                   propagator_tolerance=tolerance, propagator_conserve=conserve, path=path,
-                  propagator_format=fmt, mechanisms=mechs)
+                  propagator_format=fmt, propagator_lump=lump, mechanisms=mechs)
     neurons = [m.add_tree(t) for t in trees]
     m.insert_everywhere("hh")
     if kinetic:

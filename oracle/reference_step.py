@@ -70,6 +70,43 @@ def propagator(parent, R, C, time_step_ms, prune=EPSILON, dense_above=400):
     return P
 
 
+def lump_and_conserve(P, parent, tol, explore_factor=1e-2):
+    """Pruning that keeps charge where it belongs (this project's option; the
+    reference drops |P_ij| < epsilon, electric.py:114-115): walking the tree
+    outward from each row's segment i, expanding nodes whose |P_ij| reaches
+    tol * explore_factor, a visited entry below tol is added to the nearest kept
+    entry on the path back to i; what the walk never reaches is returned to the
+    diagonal.  Rows keep their sums.  Dense input, CSR output."""
+    A = np.asarray(P.toarray() if scipy.sparse.issparse(P) else P, dtype=np.float64)
+    parent = np.asarray(parent, dtype=np.int64)
+    n = len(A)
+    children = [[] for _ in range(n)]
+    for c, p in enumerate(parent):
+        if p >= 0:
+            children[p].append(c)
+    explore = tol * explore_factor
+    out = np.zeros_like(A)
+    for i in range(n):
+        total = A[i].sum()
+        stack = [(i, -1, i)]                      # (node, came from, nearest kept toward i)
+        while stack:
+            u, w, t = stack.pop()
+            v = A[i, u]
+            if abs(v) >= tol or u == i:
+                out[i, u] += v
+                t = u
+            else:
+                out[i, t] += v
+            if abs(v) < explore and u != i:
+                continue
+            nbrs = children[u] + ([parent[u]] if parent[u] >= 0 else [])
+            for x in nbrs:
+                if x != w:
+                    stack.append((x, u, t))
+        out[i, i] += total - out[i].sum()
+    return scipy.sparse.csr_matrix(out)
+
+
 # ---------------------------------------------------------------- HH (hh.mod)
 
 def _vtrap(x, y):

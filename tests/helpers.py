@@ -71,7 +71,9 @@ def gpu_model(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(),
     import neuwon_gb300 as nw
     hh_kw = dict(hh_kw or {})
     kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
-    if conserve:
+    if conserve == "lump":
+        kw["propagator_lump"] = True
+    elif conserve:
         kw["propagator_conserve"] = True
     kw["propagator_format"] = fmt
     mechs = [nw.HH.configure(**hh_kw)] + ([nw.Kinetic] if kinetic else [])

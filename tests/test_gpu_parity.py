@@ -67,6 +67,24 @@ def test_propagator_build_matches_scipy_expm(tol):
     assert np.abs(cp - cp.T)[both].max() < 1e-13 * C.max()
 
 
+@pytest.mark.parametrize("tol", [1e-8, 1e-6])
+def test_lumped_propagator_matches_oracle(tol):
+    """GPU lumping (pruned entries moved along the tree path to the nearest kept
+    entry, then the unvisited remainder to the diagonal) equals the oracle's."""
+    from oracle.reference_step import lump_and_conserve
+    trees = [random_tree(300, seed=3), random_tree(1, seed=0), random_tree(120, seed=8)]
+    ctx, parent, R, C = _ctx_with_tree(trees)
+    ctx.set_option("propagator_lump", 1)
+    nnz = ctypes.c_int64()
+    ctx.call("nw_propagator_build", tol, ctypes.byref(nnz))
+    ctx.call("nw_propagator_conserve")
+    P = _read_csr(ctx, len(parent)).toarray()
+    ref = lump_and_conserve(propagator(parent, R, C, 0.05, prune=0.0), parent, tol).toarray()
+    assert np.abs(P - ref).max() < 1e-12
+    assert np.abs(P.sum(axis=1) - 1.0).max() < 1e-12
+    ctx.close()
+
+
 def test_propagator_reference_fixture():
     t = Tree(F["geom_parent"], F["geom_coordinates"], F["geom_diameter"])
     ctx, parent, R, C = _ctx_with_tree([t])
@@ -147,6 +165,7 @@ def test_f32_batched_single_neuron_config_short():
 
 
 @pytest.mark.parametrize("precision,tol,conserve,bound,path", [
+    ("f32", 1e-6, "lump", 0.1, "batched"),
     ("f64", EPSILON, False, 1e-6, "batched"),
     ("f32", EPSILON, False, 0.1, "batched"),
     ("f32", 1e-8, True, 0.1, "batched"),

@@ -13,7 +13,7 @@ import scipy.sparse
 
 from neuwon_gb300.morphology import Tree, geometry, passive_electric, random_tree
 from oracle.reference_step import OracleModel, clamp_ticks, propagator
-from tests.helpers import FIXTURES, oracle_case, tree11
+from tests.helpers import FIXTURES, concat, oracle_case, tree11
 
 F = np.load(FIXTURES)
 
@@ -243,3 +243,34 @@ def test_clamp_ticks_match_reference_timeseries():
     assert clamp_ticks(5.0, 1.0, 0.1) == (101, 20)
     assert clamp_ticks(5.0, 75.0, 0.1) == (101, math.ceil(75.0 / 0.05))
     assert clamp_ticks(0.0, 0.3, 0.1) == (1, 6)
+
+
+def test_lumped_pruning_keeps_rows_and_beats_dropping():
+    """Moving each pruned entry to the nearest kept entry on the tree path keeps
+    every row sum and is far closer to the unpruned step than returning the
+    pruned mass to the diagonal."""
+    from oracle.reference_step import lump_and_conserve
+    trees = [random_tree(200, seed=41), random_tree(120, seed=42)]
+    clamps = [(0, 0, 0.4, 0.0, 30.0), (1, 0, 0.5, 0.0, 30.0)]
+    parent, R, C, area, offs = concat(trees)
+    full = propagator(parent, R, C, 0.05, prune=0.0)
+    tol = 1e-6
+    L = lump_and_conserve(full, parent, tol)
+    assert np.abs(np.asarray(L.sum(axis=1)).ravel() - np.asarray(full.sum(axis=1)).ravel()).max() < 1e-13
+    D = full.toarray().copy()
+    drop = np.abs(D) < tol
+    np.fill_diagonal(drop, False)
+    D[np.arange(len(D)), np.arange(len(D))] += np.where(drop, D, 0).sum(axis=1)
+    D[drop] = 0.0
+    assert (L.toarray() != 0).sum() <= (D != 0).sum()
+    errs = []
+    for P in (L, scipy.sparse.csr_matrix(D)):
+        ref, _ = oracle_case(trees, clamps, hh_kw=dict(ena=50., ek=-77.), prune=0.0)
+        om, _ = oracle_case(trees, clamps, hh_kw=dict(ena=50., ek=-77.))
+        om.P = P
+        worst = 0.0
+        for _ in range(300):
+            ref.advance(); om.advance()
+            worst = max(worst, np.abs(ref.voltage - om.voltage).max())
+        errs.append(worst)
+    assert errs[0] < errs[1] / 5, errs
