@@ -186,7 +186,7 @@ def log(msg):
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
-def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows"):
+def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows", lump=False):
     """FP32 batched at the bench tolerance against FP64 with a propagator pruned at ref_tol
     (both charge-conserving); the FP64 reference runs on the wide path, which spreads the
     few sample neurons over every SM."""
@@ -195,7 +195,8 @@ def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows"):
     t0 = time.perf_counter()
     ref, nref = build_model(trees, currents, precision="f64", tolerance=ref_tol, conserve=True, device=device,
                             path="wide")
-    test, ntest = build_model(trees, currents, precision="f32", tolerance=tol, conserve=True, device=device, fmt=fmt)
+    test, ntest = build_model(trees, currents, precision="f32", tolerance=tol, conserve=True, device=device, fmt=fmt,
+                              lump=lump)
     probes = []
     for m, ns in ((ref, nref), (test, ntest)):
         probes.append([TimeSeries().record(nr.root, "voltage") for nr in ns])
@@ -412,6 +413,8 @@ def main():
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
     ap.add_argument("--autotune", type=int, default=10,
                     help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
+    ap.add_argument("--lump", type=int, default=1,
+                    help="lumped pruning (pruned entries moved to the nearest kept entry on the tree path)")
     ap.add_argument("--format", default="quads", choices=["rows", "pairs", "quads"],
                     help="propagator storage: every P_ij in its row; windows of 4 consecutive columns; "
                          "or each coupling once (detailed balance)")
@@ -462,7 +465,7 @@ def main():
     if not args.quick and rank == 0:
         k = args.acc_neurons
         extra["accuracy"] = accuracy(trees[:k], currents[:k], args.tol, local, args.acc_steps, args.ref_tol,
-                                     args.format)
+                                     args.format, bool(args.lump))
         log(f"accuracy: {extra['accuracy']}")
         extra["plain_fp64"] = plain_timing(trees[:64], currents[:64], args.tol, local)
         log(f"plain: {extra['plain_fp64']}")
@@ -476,7 +479,7 @@ def main():
         log(f"network: {extra['network']}")
     t_build = time.perf_counter()
     model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, conserve=True,
-                                 device=local, fmt=args.format)
+                                 device=local, fmt=args.format, lump=bool(args.lump))
     log(f"host model built in {time.perf_counter() - t_build:.1f} s")
     model._sync()
     ctx = model._ctx
@@ -592,7 +595,9 @@ def main():
                                "FP32 state, FP64-built propagator",
                    "segments": n_total, "segments_rank0": n, "neurons": len(neurons) * world,
                    "propagator_tolerance": args.tol,
-                   "propagator_pruning": "charge-conserving (pruned mass returned to the diagonal)",
+                   "propagator_pruning": ("lumped (each pruned entry moved to the nearest kept entry on the tree "
+                                          "path to the row's segment; unvisited remainder to the diagonal)"
+                                          if args.lump else "charge-conserving (pruned mass returned to the diagonal)"),
                    "propagator_format": args.format,
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
                    "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
