@@ -29,11 +29,12 @@ sys.path.insert(0, ROOT)
 METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoint ms/step"
 
 # DRAM bytes (read + write) per segment-step of batched_advance_kernel, from one ncu
-# capture of one full-size launch per propagator format (tolerance 1e-8, 1,024
-# neurons, 5,593,190 segments): quads 742.6 GB per 25-step launch, rows 1,741.6 GB per
-# 50-step launch.  Commands and figures: profiles/batched_advance_kernel.md.
-NCU_TRAFFIC_PER_SEGMENT_STEP = {"quads": 5310.6, "rows": 6227.5}
-NCU_TRAFFIC_CONFIG = (1e-8, 5593190)
+# capture of one full-size launch (1,024 neurons, 5,593,190 segments), keyed by
+# (propagator format, tolerance, lumped): quads at 1e-8 charge-conserving 742.6 GB per
+# 25-step launch, rows at 1e-8 1,741.6 GB per 50-step launch.  Commands and figures:
+# profiles/batched_advance_kernel.md.
+NCU_TRAFFIC_PER_SEGMENT_STEP = {("quads", 1e-8, 0): 5310.6, ("rows", 1e-8, 0): 6227.5}
+NCU_TRAFFIC_SEGMENTS = 5593190
 
 
 def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
@@ -404,7 +405,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--neurons", type=int, default=1024)
-    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--tol", type=float, default=3e-7)
     ap.add_argument("--ref-tol", type=float, default=1e-10,
                     help="pruning of the FP64 accuracy reference (machine epsilon makes rows dense)")
     ap.add_argument("--size-range", default="500,20000", help="neuron size range (segments)")
@@ -413,7 +414,7 @@ def main():
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
     ap.add_argument("--autotune", type=int, default=10,
                     help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
-    ap.add_argument("--lump", type=int, default=1,
+    ap.add_argument("--lump", type=int, default=1, choices=[0, 1],
                     help="lumped pruning (pruned entries moved to the nearest kept entry on the tree path)")
     ap.add_argument("--format", default="quads", choices=["rows", "pairs", "quads"],
                     help="propagator storage: every P_ij in its row; windows of 4 consecutive columns; "
@@ -609,9 +610,9 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "traffic": (NCU_TRAFFIC_PER_SEGMENT_STEP[args.format] * n * F
-                                 if (args.tol, n) == NCU_TRAFFIC_CONFIG and args.format in NCU_TRAFFIC_PER_SEGMENT_STEP
-                                 else None),
+                     "traffic": (NCU_TRAFFIC_PER_SEGMENT_STEP[(args.format, args.tol, args.lump)] * n * F
+                                 if n == NCU_TRAFFIC_SEGMENTS
+                                 and (args.format, args.tol, args.lump) in NCU_TRAFFIC_PER_SEGMENT_STEP else None),
                      "traffic_unit": f"bytes per launch of {F} steps (ncu dram__bytes_read+write)",
                      "algorithmic_bytes_per_launch": B_alg * n * F,
                      "peak_source": peak_src,

@@ -474,6 +474,8 @@ static int adjoint_backward_impl(nw_ctx* ctx, double Ra, double* g_gna, double* 
 static int adjoint_check(nw_ctx* ctx) {
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "adjoint before nw_model_init");
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "adjoint: no propagator installed");
+    if (ctx->prop_lumped)
+        return fail(ctx, NW_ERR_STATE, "adjoint: a lumped propagator has no detailed-balance transpose");
     if (!ctx->have_cap || !ctx->have_res) return fail(ctx, NW_ERR_STATE, "adjoint: capacitance/resistance not set");
     if (ctx->hh.m == 0 || !ctx->hh.identity)
         return fail(ctx, NW_ERR_STATE, "adjoint: needs exactly one HH instance on every segment");

@@ -555,6 +555,7 @@ int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out) {
     NW_CHECK(propagator_to_batched(ctx));
     ctx->prop_valid = true;
     ctx->prop_built = !ctx->prop_lump;           // lumped rows break detailed balance
+    ctx->prop_lumped = ctx->prop_lump;
     if (ctx->prop_lump && ctx->prop_format == 1) ctx->prop_format = 0;
     return NW_OK;
 }
@@ -581,6 +582,7 @@ int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr, const i
     NW_CHECK(propagator_to_batched(ctx));
     ctx->prop_valid = true;
     ctx->prop_built = false;
+    ctx->prop_lumped = false;
     ctx->prop_format = 0;
     return NW_OK;
 }

@@ -169,6 +169,7 @@ struct nw_ctx {
     bool prop_valid = false;
     bool prop_built = false;    // built here (detailed balance holds): the pair format may be used
     bool prop_lump = false;     // next build moves dropped values to the nearest kept node (option "propagator_lump")
+    bool prop_lumped = false;   // the installed propagator was built with lumping (no detailed balance)
     bool b_ok = false;          // batched format present (every neuron <= 65,535 segments)
     bool w_ok = false;          // wide format present (built on first use of the wide path)
     int64_t nnz64 = 0, nnz_b = 0, nnz_w = 0;

@@ -7,6 +7,7 @@ import pytest
 import torch
 
 import neuwon_gb300 as nw
+from neuwon_gb300._lib import NeuwonError
 from neuwon_gb300.adjoint import loss_and_gradients, trace_loss
 from neuwon_gb300.morphology import random_tree
 from tests import torch_reference
@@ -147,4 +148,17 @@ def test_autograd_function_wraps_the_adjoint():
     assert L.item() == pytest.approx(ref[0], rel=1e-12)
     assert np.allclose(gna.grad.numpy(), 3.0 * ref[1], rtol=1e-10, atol=0)
     assert ra.grad.item() == pytest.approx(3.0 * ref[4], rel=1e-10)
+    m.close()
+
+
+def test_adjoint_refuses_a_lumped_propagator():
+    """The reverse sweep takes P^T from detailed balance, which lumped pruning breaks."""
+    m = nw.RxD_Model(time_step=DT, temperature=CELSIUS, precision="f64", propagator_tolerance=1e-6,
+                     propagator_lump=True, mechanisms=[nw.HH.configure(**HH_KW)])
+    nr = m.add_tree(random_tree(60, seed=2))
+    m.insert_everywhere("hh")
+    nr.root.inject_current(0.3, 1e6)
+    m._sync()
+    with pytest.raises(NeuwonError, match="lumped"):
+        loss_and_gradients(m, 20, np.full((20, 1), -65.0), checkpoint_every=10)
     m.close()
