@@ -259,7 +259,7 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     free_adj(ctx->adj);
     free_flux(ctx);
     free_quads(ctx);
-    DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec,
+    DevBuf* bufs[] = {&ctx->neuron_start, &ctx->parent, &ctx->V, &ctx->Vint, &ctx->Inonspec, &ctx->gcache,
                       &ctx->kI, &ctx->kG, &ctx->cap64, &ctx->res64, &ctx->p_rowptr, &ctx->p_col,
                       &ctx->p_val, &ctx->b_rowptr, &ctx->b_col, &ctx->b_val, &ctx->b_leak,
                       &ctx->clamp_seg, &ctx->clamp_amp, &ctx->clamp_first, &ctx->clamp_count,
@@ -350,6 +350,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     NW_CHECK(dev_alloc(ctx, ctx->parent, 8 * num_segments));
     NW_CHECK(dev_alloc(ctx, ctx->V, rs * num_segments));
     NW_CHECK(dev_alloc(ctx, ctx->Vint, rs * num_segments));
+    NW_CHECK(dev_alloc(ctx, ctx->gcache, 2 * rs * num_segments));
     NW_CHECK(dev_alloc(ctx, ctx->Inonspec, rs * num_segments));
     NW_CHECK(dev_alloc(ctx, ctx->kI, rs * num_segments));
     NW_CHECK(dev_alloc(ctx, ctx->kG, rs * num_segments));

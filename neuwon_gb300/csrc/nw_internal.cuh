@@ -160,6 +160,7 @@ struct nw_ctx {
 
     // Electric state (context precision) and FP64 passive properties.
     nw::DevBuf V, Vint, Inonspec, kI, kG;
+    nw::DevBuf gcache;          // 2 x n_seg reals: G and G*E cached between the steps of one launch
     nw::DevBuf cap64, res64;    // f64 [n_seg]
     bool have_cap = false, have_res = false, nonspec_nonzero = false;
 

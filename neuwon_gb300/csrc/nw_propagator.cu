@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
             const int64_t tslot = st_tslot[sp];
             const int tchain = st_tchain[sp];
             const double vu = value(yu);
-            const bool keep = fabs(vu) >= a.tol;
+            const bool keep = fabs(vu) >= a.tol || (a.lump && u == row);   // lumping keeps the row's own entry
             int64_t myslot = -1;
             if (keep) {
                 if (fill && lane == 0 && out < out_end) { a.out_col[out] = (int32_t)u; a.out_val[out] = vu; }

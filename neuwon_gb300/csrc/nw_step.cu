@@ -412,6 +412,14 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         // With one instance per segment the thread that updates a segment's
         // instances is the one that gathers them next; otherwise synchronise.
         const bool mech_sync = (a.hh_on && !a.hh_identity) || (a.kin_on && !a.kin_identity) || ye > yb;
+        const bool fuse = !BULK && a.fuse_mech;
+        // Stimulus of segment i at a tick: nonspecific current plus the clamps playing.
+        auto stim = [&](int64_t i, int64_t tick) {
+            real I = a.has_nonspec ? a.Inonspec[i] : real(0);
+            for (int c = 0; c < nclamp; ++c)
+                if (s_cseg[c] == (uint32_t)i && tick >= s_cfirst[c] && tick < s_cend[c]) I += s_camp[c];
+            return I;
+        };
         // AP detector state lives in thread 0's registers across the K steps.
         bool ap_state = false, ap_det = false;
         uint32_t spikes = 0;
@@ -431,15 +439,18 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                 const bool last = (s == a.k_steps - 1) && (half == 1);
                 // The propagator does not depend on x: start streaming it now.
                 if (BULK) bulk_prologue(a, ring, slice);
-                for (int li = tid; li < n; li += nthr) {
-                    const int64_t i = base + li;
-                    real G, GE;
-                    if (gv) segment_conductance(a, i, G, GE);
-                    else { G = real(0); GE = real(0); }
-                    real I = a.has_nonspec ? a.Inonspec[i] : real(0);
-                    for (int c = 0; c < nclamp; ++c)
-                        if (s_cseg[c] == (uint32_t)i && tick >= s_cfirst[c] && tick < s_cend[c]) I += s_camp[c];
-                    xs[li] = membrane_x(a, i, G, GE, I, last);
+                // With fused mechanisms the second half's x comes from the mechanism
+                // pass, and later steps' first halves take G from the cache (the
+                // state it was computed from does not change in between).
+                if (!(fuse && half == 1)) {
+                    for (int li = tid; li < n; li += nthr) {
+                        const int64_t i = base + li;
+                        real G, GE;
+                        if (fuse && s > 0) { G = a.gc[i]; GE = a.gc[a.gc_n + i]; }
+                        else if (gv) segment_conductance(a, i, G, GE);
+                        else { G = real(0); GE = real(0); }
+                        xs[li] = membrane_x(a, i, G, GE, stim(i, tick), last);
+                    }
                 }
                 __syncthreads();
                 if (FLUX) {
@@ -472,7 +483,27 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                                                [&](int64_t r, int, real, real cnew) { a.ca_c[r] = cnew; });
                     __syncthreads();
                 }
-                if (half == 0) {
+                if (half == 0 && fuse) {
+                    // Mechanisms (rxd_model.py:115-123) at the mid-step voltage, then
+                    // the segment's conductance and the second half's x, in one pass.
+                    const bool last1 = s == a.k_steps - 1;
+                    const bool keep = s + 1 < a.k_steps;
+                    for (int li = tid; li < n; li += nthr) {
+                        const int64_t i = base + li;
+                        const real v = a.V[i];
+                        if (a.hh_on) {
+                            real m = a.gm[i], h = a.gh[i], nn = a.gn[i];
+                            hh_gates(v, a.dtq10, m, h, nn);
+                            a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
+                        }
+                        if (a.kin_on) kinetic_step(a, i, v);
+                        real G, GE;
+                        segment_conductance(a, i, G, GE);
+                        if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
+                        xs[li] = membrane_x(a, i, G, GE, stim(i, tick + 1), last1);
+                    }
+                    __syncthreads();
+                } else if (half == 0) {
                     // Mechanisms (rxd_model.py:115-123) at the mid-step voltage.
                     if (a.hh_on) {
                         for (int64_t k = ib + tid; k < ie; k += nthr) {

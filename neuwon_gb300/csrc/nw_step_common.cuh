@@ -122,6 +122,11 @@ struct StepArgs {
     const int64_t* ca_wrow; const int32_t* ca_wcol; const real* ca_wval; const real* ca_wleak;
     int64_t ca_n;
     real ca_log2min, ca_frq, ca_scale, h_ms;
+    // Conductance cache of the batched kernel (G at gc, G*E at gc + n): written by the
+    // fused mechanism pass of step s, read by the first half of step s + 1 in the
+    // same launch; fuse_mech when every conductance source maps one-to-one onto
+    // segments (HH and kinetic instances in segment order, no synapses or calcium).
+    real* gc; int64_t gc_n; int fuse_mech;
     // clamps (sorted by segment)
     const uint32_t* clamp_seg_ptr;
     const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
@@ -578,6 +583,8 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.kin_vmin = (real)K.vmin; a.kin_frq = (real)K.frq; a.kin_cs = (real)K.conserve; a.kin_erev = (real)K.erev;
     const CalciumState& Ca = ctx->ca;
     a.ca_on = Ca.on ? 1 : 0;
+    a.gc = ctx->gcache.as<real>(); a.gc_n = ctx->n_seg;
+    a.fuse_mech = (a.gc && ctx->syn.n == 0 && !Ca.on && (hh.m == 0 || hh.identity) && (K.m == 0 || K.identity)) ? 1 : 0;
     a.h_ms = (real)(0.5 * ctx->time_step);
     if (Ca.on) {
         a.ca_pump = Ca.pump ? 1 : 0; a.ca_nb = Ca.nb; a.ca_T = Ca.T;
