@@ -313,7 +313,7 @@ __device__ __forceinline__ void flux_finalize(const StepArgs<real>& a, int64_t b
     }
 }
 
-template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false>
+template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false, bool FUSE = false>
 __global__ void __launch_bounds__(1024)
 batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_off) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -412,7 +412,9 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         // With one instance per segment the thread that updates a segment's
         // instances is the one that gathers them next; otherwise synchronise.
         const bool mech_sync = (a.hh_on && !a.hh_identity) || (a.kin_on && !a.kin_identity) || ye > yb;
-        const bool fuse = !BULK && a.fuse_mech;
+        // The fused mechanism pass is compiled only into the FUSE instances, so the
+        // kernels for synapses, calcium or scattered instances keep their own code.
+        const bool fuse = FUSE && !BULK && a.fuse_mech;
         // Stimulus of segment i at a tick: nonspecific current plus the clamps playing.
         auto stim = [&](int64_t i, int64_t tick) {
             real I = a.has_nonspec ? a.Inonspec[i] : real(0);
@@ -634,9 +636,9 @@ struct BatchedCfg {
     int rc_smem;      // pair format: c_max / c staged in shared memory
 };
 
-template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false>
+template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false, bool FUSE = false>
 static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
-    auto kern = batched_advance_kernel<real, LPR, BULK, FLUX, QUAD>;
+    auto kern = batched_advance_kernel<real, LPR, BULK, FLUX, QUAD, FUSE>;
     const size_t xs_bytes = ((size_t)ctx->max_neuron * sizeof(real) + 127) & ~(size_t)127;
     const int threads = ctx->threads;
     size_t smem = xs_bytes;
@@ -690,6 +692,14 @@ static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron has more than 65,535 segments (use the wide path)");
     if (ctx->prop_format == 2) {
         NW_CHECK(ensure_quads(ctx));
+        if (fuse_mechanisms(ctx)) {
+            switch (choose_lanes_per_row(ctx)) {
+                case 4: return config_batched_lpr<real, 4, false, false, true, true>(ctx, c);
+                case 8: return config_batched_lpr<real, 8, false, false, true, true>(ctx, c);
+                case 16: return config_batched_lpr<real, 16, false, false, true, true>(ctx, c);
+                default: return config_batched_lpr<real, 32, false, false, true, true>(ctx, c);
+            }
+        }
         switch (choose_lanes_per_row(ctx)) {
             case 4: return config_batched_lpr<real, 4, false, false, true>(ctx, c);
             case 8: return config_batched_lpr<real, 8, false, false, true>(ctx, c);

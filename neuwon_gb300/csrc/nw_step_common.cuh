@@ -541,6 +541,14 @@ __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_
 }
 
 
+// The batched kernel's fused mechanism pass applies: every conductance source maps
+// one-to-one onto segments (HH and kinetic instances in segment order, no synapses,
+// no calcium) and the conductance cache exists.
+inline bool fuse_mechanisms(const nw_ctx* ctx) {
+    return ctx->gcache.ptr && ctx->syn.n == 0 && !ctx->ca.on && (ctx->hh.m == 0 || ctx->hh.identity) &&
+           (ctx->kin.m == 0 || ctx->kin.identity);
+}
+
 template <typename real>
 inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     StepArgs<real> a;
@@ -584,7 +592,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     const CalciumState& Ca = ctx->ca;
     a.ca_on = Ca.on ? 1 : 0;
     a.gc = ctx->gcache.as<real>(); a.gc_n = ctx->n_seg;
-    a.fuse_mech = (a.gc && ctx->syn.n == 0 && !Ca.on && (hh.m == 0 || hh.identity) && (K.m == 0 || K.identity)) ? 1 : 0;
+    a.fuse_mech = fuse_mechanisms(ctx) ? 1 : 0;
     a.h_ms = (real)(0.5 * ctx->time_step);
     if (Ca.on) {
         a.ca_pump = Ca.pump ? 1 : 0; a.ca_nb = Ca.nb; a.ca_T = Ca.T;
