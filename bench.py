@@ -28,12 +28,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoint ms/step"
 
-# DRAM bytes (read + write) per segment-step of batched_advance_kernel, from one ncu
-# capture of one full-size launch (1,024 neurons, 5,593,190 segments), keyed by
-# (propagator format, tolerance, lumped): quads at 1e-8 charge-conserving 742.6 GB per
-# 25-step launch, rows at 1e-8 1,741.6 GB per 50-step launch.  Commands and figures:
-# profiles/batched_advance_kernel.md.
-NCU_TRAFFIC_PER_SEGMENT_STEP = {("quads", 1e-8, 0): 5310.6, ("rows", 1e-8, 0): 6227.5}
+# DRAM bytes (read + write) per segment-step of batched_advance_kernel, from ncu
+# captures of full-size launches (1,024 neurons, 5,593,190 segments), keyed by
+# (propagator format, tolerance, lumped): quads lumped at 3e-7 464.9 GB per 25-step
+# launch (mean of the four timed launches), quads at 1e-8 charge-conserving 742.6 GB
+# per 25-step launch, rows at 1e-8 1,741.6 GB per 50-step launch.  Commands and
+# figures: profiles/batched_advance_kernel.md.
+NCU_TRAFFIC_PER_SEGMENT_STEP = {("quads", 3e-7, 1): 3324.7, ("quads", 1e-8, 0): 5310.6, ("rows", 1e-8, 0): 6227.5}
 NCU_TRAFFIC_SEGMENTS = 5593190
 
 
