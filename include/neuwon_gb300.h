@@ -304,7 +304,9 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * an entry below the tolerance is added to the nearest kept entry on the tree path
  * from its segment towards the row's segment instead of being dropped (row sums are
  * kept; far lower error than dropping at the same tolerance, so fewer entries for
- * the same accuracy); unvisited remainders still need nw_propagator_conserve.
+ * the same accuracy); the row's own entry is always kept; unvisited remainders still
+ * need nw_propagator_conserve.  A lumped propagator has no detailed balance: the pair
+ * format falls back to rows and the adjoint refuses it.
  * "set_steps" (k): resume at step k (clock, input ticks 2k, conductances valid when
  * k > 0 and mechanisms exist; probes start empty), for restoring a checkpoint.
  * "fusion_depth" (default 50, 0 = the whole call in one launch): steps per launch of
