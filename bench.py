@@ -226,6 +226,60 @@ def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows", lump=Fals
             "sample": f"first {len(trees)} neurons of the batch ({n} segments)"}
 
 
+def cpu_baseline_config1(device, steps=1000):
+    """The single-neuron configuration (one seeded 2,000-segment HH tree, 0.2 nA soma
+    clamp 5-80 ms, dt 0.1 ms for 100 ms, FP64, propagator pruned at machine epsilon as
+    the reference prunes it): the reference's own path as it runs without numba (scipy
+    CSR SpMV + numpy mechanisms, restated in the oracle: rxd_model.py:63-80,
+    electric.py:56-76) timed on one host core, and this package's batched and wide
+    paths on the GPU over the same 1,000 steps, with each one's max voltage difference
+    from the oracle's at the end and its spike count."""
+    import neuwon_gb300 as nw
+    from neuwon_gb300.morphology import geometry, passive_electric, random_tree
+    from oracle.reference_step import HHInstances, OracleModel, clamp_ticks
+    tree = random_tree(2000, seed=0)
+    hh_kw = dict(ena=50.0, ek=-77.0, el=-54.3)
+    g = geometry(tree)
+    R, C = passive_electric(g)
+    n = len(tree)
+    f, c = clamp_ticks(5.0, 75.0, 0.1)
+    t0 = time.perf_counter()
+    om = OracleModel(tree.parent, R, C, time_step=0.1, celsius=6.3,
+                     hh=HHInstances(np.arange(n), g["surface_area"], celsius=6.3, **hh_kw),
+                     clamps=[(0, 0.2e-9, f, c)], detectors=[(0, 20.0)])
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        om.advance()
+    ref_s = time.perf_counter() - t0
+    out = {"config": "one 2,000-segment HH tree (seed 0), 0.2 nA soma clamp 5-80 ms, dt 0.1 ms, "
+                     f"{steps} steps, propagator at machine epsilon ({om.P.nnz / n:.0f} entries/row)",
+           "reference_path": {"value": n * steps / ref_s, "unit": "segment-steps/s", "ms_per_step": ref_s / steps * 1e3,
+                              "cores": 1, "kind": "port",
+                              "sample": "the reference's numba-less path restated (oracle/reference_step.py: "
+                                        "scipy CSR SpMV + numpy HH), FP64, all 1,000 steps",
+                              "build_s": build_s, "spikes": int(om.spike_count[0])}}
+    for precision, path in (("f64", "batched"), ("f64", "wide"), ("f32", "batched"), ("f32", "wide")):
+        m = nw.RxD_Model(time_step=0.1, temperature=6.3, precision=precision, path=path, device=device,
+                         mechanisms=[nw.HH.configure(**hh_kw)])
+        nr = m.add_tree(tree)
+        m.insert_everywhere("hh")
+        m._sync()
+        m._ctx.call("nw_synchronize")
+        t0 = time.perf_counter()
+        m.advance(50)
+        nr.root.inject_current(0.2, 75.0)
+        m.advance(steps - 50)
+        m._ctx.call("nw_synchronize")
+        dt = time.perf_counter() - t0
+        out[f"gpu_{precision}_{path}"] = {
+            "value": n * steps / dt, "unit": "segment-steps/s", "ms_per_step": dt / steps * 1e3,
+            "max_err_mV": float(np.abs(m.get_data("Segment.voltage") - om.voltage).max()),
+            "spikes": int(m.get_data("Neuron.spike_count")[0])}
+        m.close()
+    return out
+
+
 def plain_timing(trees, currents, tol, device, steps=10):
     """The plain per-neuron FP64 path (reference GPU design) on a subset of the batch."""
     from neuwon_gb300.workloads import build_model
@@ -584,6 +638,8 @@ def main():
     cpu = None
     if not args.quick and rank == 0:
         cpu = cpu_sample(trees, currents, args.tol, steps=100000, time_budget_s=15.0)
+        cpu["config1"] = cpu_baseline_config1(local)
+        log(f"config 1: {cpu['config1']}")
     spikes = model.get_data("Neuron.spike_count")
     model.close()
     if rank != 0:

@@ -274,3 +274,15 @@ def test_lumped_pruning_keeps_rows_and_beats_dropping():
             worst = max(worst, np.abs(ref.voltage - om.voltage).max())
         errs.append(worst)
     assert errs[0] < errs[1] / 5, errs
+
+
+def test_lumping_keeps_the_row_entry_at_any_tolerance():
+    """Every diagonal below the tolerance: lumping still keeps each row's own entry
+    (the target of everything dropped near it), so the result is the identity."""
+    from oracle.reference_step import lump_and_conserve
+    t = random_tree(120, seed=8)
+    parent, R, C, area, offs = concat([t])
+    full = propagator(parent, R, C, 0.05, prune=0.0)
+    assert full.diagonal().max() < 0.9
+    L = lump_and_conserve(full, parent, 0.9).toarray()
+    assert np.abs(L - np.eye(len(L))).max() < 1e-13
