@@ -266,14 +266,23 @@ def cpu_baseline_config1(device, steps=1000):
         m.insert_everywhere("hh")
         m._sync()
         m._ctx.call("nw_synchronize")
+        # The first 50 steps (untimed) also build the row formats and capture the
+        # launch graph; the clamp starts at 5 ms; the other steps are timed as
+        # calls of 50 steps each.
         t0 = time.perf_counter()
         m.advance(50)
+        m._ctx.call("nw_synchronize")
+        first_s = time.perf_counter() - t0
         nr.root.inject_current(0.2, 75.0)
-        m.advance(steps - 50)
+        t0 = time.perf_counter()
+        for _ in range(steps // 50 - 1):
+            m.advance(50)
         m._ctx.call("nw_synchronize")
         dt = time.perf_counter() - t0
+        timed = 50 * (steps // 50 - 1)
         out[f"gpu_{precision}_{path}"] = {
-            "value": n * steps / dt, "unit": "segment-steps/s", "ms_per_step": dt / steps * 1e3,
+            "value": n * timed / dt, "unit": "segment-steps/s", "ms_per_step": dt / timed * 1e3,
+            "first_50_steps_s": first_s,
             "max_err_mV": float(np.abs(m.get_data("Segment.voltage") - om.voltage).max()),
             "spikes": int(m.get_data("Neuron.spike_count")[0])}
         m.close()
