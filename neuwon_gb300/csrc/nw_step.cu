@@ -490,19 +490,69 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     // the segment's conductance and the second half's x, in one pass.
                     const bool last1 = s == a.k_steps - 1;
                     const bool keep = s + 1 < a.k_steps;
-                    for (int li = tid; li < n; li += nthr) {
-                        const int64_t i = base + li;
-                        const real v = a.V[i];
-                        if (a.hh_on) {
-                            real m = a.gm[i], h = a.gh[i], nn = a.gn[i];
-                            hh_gates(v, a.dtq10, m, h, nn);
-                            a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
+                    if (!a.kin_on || (a.kin_S == 8 && a.kin_T == 2)) {
+                        // Every input of the segment is loaded before the first store, and
+                        // the conductances come from registers (same helpers and order as
+                        // segment_conductance, so the same bits).
+                        for (int li = tid; li < n; li += nthr) {
+                            const int64_t i = base + li;
+                            const real v = a.V[i], kGi = a.kG[i], kIi = a.kI[i];
+                            const real I = stim(i, tick + 1);
+                            real m = real(0), h = real(0), nn = real(0);
+                            real cna = real(0), ck = real(0), cl = real(0), gco = real(0);
+                            real st[8];
+                            if (a.hh_on) {
+                                m = a.gm[i]; h = a.gh[i]; nn = a.gn[i];
+                                cna = a.cna[i]; ck = a.ck[i]; cl = a.cl[i];
+                            }
+                            if (a.kin_on) {
+#pragma unroll
+                                for (int c = 0; c < 8; ++c) st[c] = a.kin_state[(int64_t)c * a.kin_m + i];
+                                gco = a.kin_gcoef[i];
+                            }
+                            real G = real(0), GE = real(0);
+                            if (a.hh_on) {
+                                hh_gates(v, a.dtq10, m, h, nn);
+                                real gna = real(0), gk = real(0), gl = real(0);
+                                hh_conductance_add(cna, ck, cl, m, h, nn, gna, gk, gl);
+                                hh_conductance_total(a, gna, gk, gl, G, GE);
+                            }
+                            if (a.kin_on) {
+                                kinetic_advance<real, 8, 2>(a, v, st);
+                                const real open = kinetic_open(a, [&](int c) {
+                                    real x = st[0];
+#pragma unroll
+                                    for (int q = 1; q < 8; ++q) x = (c == q) ? st[q] : x;
+                                    return x;
+                                });
+                                real gkin = real(0);
+                                gkin += gco * open;
+                                G += gkin;
+                                GE += gkin * a.kin_erev;
+                            }
+                            if (a.hh_on) { a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn; }
+                            if (a.kin_on) {
+#pragma unroll
+                                for (int c = 0; c < 8; ++c) a.kin_state[(int64_t)c * a.kin_m + i] = st[c];
+                            }
+                            if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
+                            xs[li] = membrane_x_of(a, i, v, kGi, kIi, G, GE, I, last1);
                         }
-                        if (a.kin_on) kinetic_step(a, i, v);
-                        real G, GE;
-                        segment_conductance(a, i, G, GE);
-                        if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
-                        xs[li] = membrane_x(a, i, G, GE, stim(i, tick + 1), last1);
+                    } else {
+                        for (int li = tid; li < n; li += nthr) {
+                            const int64_t i = base + li;
+                            const real v = a.V[i];
+                            if (a.hh_on) {
+                                real m = a.gm[i], h = a.gh[i], nn = a.gn[i];
+                                hh_gates(v, a.dtq10, m, h, nn);
+                                a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
+                            }
+                            if (a.kin_on) kinetic_step(a, i, v);
+                            real G, GE;
+                            segment_conductance(a, i, G, GE);
+                            if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
+                            xs[li] = membrane_x(a, i, G, GE, stim(i, tick + 1), last1);
+                        }
                     }
                     __syncthreads();
                 } else if (half == 0) {

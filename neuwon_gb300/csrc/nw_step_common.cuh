@@ -147,33 +147,53 @@ struct StepArgs {
 // Sum of a segment's mechanism conductances and conductance-weighted reversal
 // potentials (species.py:389-393 scatter, done here as a gather over the
 // segment's instances in registration order: deterministic, no atomics).
+// One HH instance's conductances added to the segment's running sums.
+template <typename real>
+__device__ __forceinline__ void hh_conductance_add(real cna, real ck, real cl, real m, real h, real n,
+                                                   real& gna, real& gk, real& gl) {
+    gna += cna * m * m * m * h;
+    gk += ck * n * n * n * n;
+    gl += cl;
+}
+
+// Sum of the conductances and conductance-weighted reversal potentials of HH.
+template <typename real>
+__device__ __forceinline__ void hh_conductance_total(const StepArgs<real>& a, real gna, real gk, real gl,
+                                                     real& G, real& GE) {
+    G = (gna + gk) + gl;
+    GE = (gna * a.ena + gk * a.ek) + gl * a.el;
+}
+
+// A kinetic instance's open probability: its open states summed in list order.
+template <typename real, typename Get>
+__device__ __forceinline__ real kinetic_open(const StepArgs<real>& a, Get state) {
+    real open = real(0);
+    for (int o = 0; o < a.kin_nopen; ++o) open += state(a.kin_open[o]);
+    return open;
+}
+
 template <typename real>
 __device__ __forceinline__ void segment_conductance(const StepArgs<real>& a, int64_t i, real& G, real& GE) {
     G = real(0); GE = real(0);
     if (a.hh_on) {
-        int64_t b, e;
-        if (a.hh_identity) { b = i; e = i + 1; }
-        else { b = a.hh_seg_ptr[i]; e = a.hh_seg_ptr[i + 1]; }
         real gna = real(0), gk = real(0), gl = real(0);
-        for (int64_t k = b; k < e; ++k) {
-            real m = a.gm[k], h = a.gh[k], n = a.gn[k];
-            gna += a.cna[k] * m * m * m * h;
-            gk += a.ck[k] * n * n * n * n;
-            gl += a.cl[k];
+        if (a.hh_identity) {
+            hh_conductance_add(a.cna[i], a.ck[i], a.cl[i], a.gm[i], a.gh[i], a.gn[i], gna, gk, gl);
+        } else {
+            const int64_t b = a.hh_seg_ptr[i], e = a.hh_seg_ptr[i + 1];
+            for (int64_t k = b; k < e; ++k)
+                hh_conductance_add(a.cna[k], a.ck[k], a.cl[k], a.gm[k], a.gh[k], a.gn[k], gna, gk, gl);
         }
-        G = (gna + gk) + gl;
-        GE = (gna * a.ena + gk * a.ek) + gl * a.el;
+        hh_conductance_total(a, gna, gk, gl, G, GE);
     }
     if (a.kin_on) {
-        int64_t b, e;
-        if (a.kin_identity) { b = i; e = i + 1; }
-        else { b = a.kin_seg_ptr[i]; e = a.kin_seg_ptr[i + 1]; }
         real gkin = real(0);
-        for (int64_t k = b; k < e; ++k) {
-            real open = real(0);
-            for (int o = 0; o < a.kin_nopen; ++o) open += a.kin_state[(int64_t)a.kin_open[o] * a.kin_m + k];
+        auto add = [&](int64_t k) {
+            const real open = kinetic_open(a, [&](int s) { return a.kin_state[(int64_t)s * a.kin_m + k]; });
             gkin += a.kin_gcoef[k] * open;
-        }
+        };
+        if (a.kin_identity) add(i);
+        else for (int64_t k = a.kin_seg_ptr[i], e = a.kin_seg_ptr[i + 1]; k < e; ++k) add(k);
         G += gkin;
         GE += gkin * a.kin_erev;
     }
@@ -305,7 +325,7 @@ __device__ __forceinline__ int kinetic_locate(const StepArgs<real>& a, real v, r
 // polynomial approximation of the column-normalised propagator, evaluated per
 // (col, row) as table[bucket][col][row][term], times the state, then CONSERVE.
 template <typename real, int S, int T>
-__device__ __forceinline__ void kinetic_step_fixed(const StepArgs<real>& a, int64_t k, real v) {
+__device__ __forceinline__ void kinetic_advance(const StepArgs<real>& a, real v, real (&st)[S]) {
     real loc;
     const int b = kinetic_locate(a, v, loc);
     real basis[T];
@@ -313,9 +333,9 @@ __device__ __forceinline__ void kinetic_step_fixed(const StepArgs<real>& a, int6
 #pragma unroll
     for (int t = 1; t < T; ++t) basis[t] = basis[t - 1] * loc;
     const real* __restrict__ tb = a.kin_table + (int64_t)b * (S * S * T);
-    real st[S], out[S];
+    real out[S];
 #pragma unroll
-    for (int c = 0; c < S; ++c) { st[c] = a.kin_state[(int64_t)c * a.kin_m + k]; out[c] = real(0); }
+    for (int c = 0; c < S; ++c) out[c] = real(0);
 #pragma unroll
     for (int col = 0; col < S; ++col) {
 #pragma unroll
@@ -336,7 +356,17 @@ __device__ __forceinline__ void kinetic_step_fixed(const StepArgs<real>& a, int6
         for (int c = 0; c < S; ++c) out[c] *= f;
     }
 #pragma unroll
-    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = out[c];
+    for (int c = 0; c < S; ++c) st[c] = out[c];
+}
+
+template <typename real, int S, int T>
+__device__ __forceinline__ void kinetic_step_fixed(const StepArgs<real>& a, int64_t k, real v) {
+    real st[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) st[c] = a.kin_state[(int64_t)c * a.kin_m + k];
+    kinetic_advance<real, S, T>(a, v, st);
+#pragma unroll
+    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = st[c];
 }
 
 // Same step for any S <= 16 and T <= 4.
@@ -373,17 +403,22 @@ __device__ __forceinline__ void kinetic_step(const StepArgs<real>& a, int64_t k,
 
 // Exact exponential membrane update of one segment (electric.py:60-76).
 template <typename real>
-__device__ __forceinline__ real membrane_x(const StepArgs<real>& a, int64_t i, real G, real GE, real I,
-                                           bool store_integral) {
-    real v = a.V[i];
+__device__ __forceinline__ real membrane_x_of(const StepArgs<real>& a, int64_t i, real v, real kG, real kI,
+                                              real G, real GE, real I, bool store_integral) {
     real E = (G != real(0)) ? GE / G : real(0);          // nan_to_num(GE/G), rxd_model.py:106-109
-    real expo = -a.kG[i] * G;
+    real expo = -kG * G;
     real alpha = d_exp(expo);
-    real dv = a.kI[i] * I;
+    real dv = kI * I;
     real diff = E - v;
     real x = E - diff * alpha + dv;
     if (store_integral) a.Vint[i] = a.h_s * E - expo * diff * alpha + real(0.5) * a.h_s * dv;
     return x;
+}
+
+template <typename real>
+__device__ __forceinline__ real membrane_x(const StepArgs<real>& a, int64_t i, real G, real GE, real I,
+                                           bool store_integral) {
+    return membrane_x_of(a, i, a.V[i], a.kG[i], a.kI[i], G, GE, I, store_integral);
 }
 
 // Propagator entries are streamed once per half step and do not fit in L2, so
