@@ -166,6 +166,12 @@ def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, max_neuron=3000,
                       f"(oracle/cpu_step.c) with OpenMP, built on the CPU in {build_s:.0f} s"}
 
 
+def workload_name(neurons, lo, hi):
+    """The bench workload as both arms name it in config.workload."""
+    return (f"batched: {neurons} neurons, log-uniform {lo}-{hi} segments, HH + 8-state Markov Na on every "
+            "segment, soma current U(0.05,0.5) nA, dt 0.1 ms, FP32 state, FP64-built propagator")
+
+
 def run_reference(args, rank):
     from neuwon_gb300.workloads import batched_currents, batched_trees
     lo, hi = (int(x) for x in args.size_range.split(","))
@@ -175,8 +181,7 @@ def run_reference(args, rank):
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "segment-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "batched: 1024 neurons, log-uniform 500-20000 segments, HH + "
-                                                        "8-state Markov Na on every segment, dt 0.1 ms",
+            "data": "synthetic", "config": {"workload": workload_name(args.neurons, lo, hi),
                                             "sample": res["sample"], "propagator_tolerance": args.tol},
             "cpu_baseline": res,
             "e2e": {"value": res["value"], "unit": "segment-steps/s", "h2d_bytes_per_step": 0,
@@ -657,9 +662,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "segment-steps/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded trees; no dataset involved)",
-        "config": {"workload": f"batched: {len(neurons)} neurons, log-uniform {lo}-{hi} segments, HH + "
-                               "8-state Markov Na on every segment, soma current U(0.05,0.5) nA, dt 0.1 ms, "
-                               "FP32 state, FP64-built propagator",
+        "config": {"workload": workload_name(len(neurons), lo, hi),
                    "segments": n_total, "segments_rank0": n, "neurons": len(neurons) * world,
                    "propagator_tolerance": args.tol,
                    "propagator_pruning": ("lumped (each pruned entry moved to the nearest kept entry on the tree "
