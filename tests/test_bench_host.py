@@ -1,0 +1,39 @@
+"""Host-side pieces of bench.py: the byte counts behind the roofline fields and the
+ncu traffic figure of the default configuration (no GPU needed)."""
+
+import pytest
+
+import bench
+
+
+def test_algorithmic_bytes_formula():
+    # B = 2(8r + 4) + 4(2 + 2 S_total + P_seg + 1) with S_total = 11, P_seg = 5.
+    assert bench.algorithmic_bytes_per_segment_step(1.0) == 2 * 12 + 4 * (2 + 22 + 5 + 1)
+    assert bench.algorithmic_bytes_per_segment_step(302.5) == pytest.approx(2 * (8 * 302.5 + 4) + 120)
+
+
+def test_format_bytes_quads_count_windows():
+    rows = bench.format_bytes_per_segment_step(100.0)
+    quads = bench.format_bytes_per_segment_step(100.0, quads=True)
+    # 100 value slots = 25 windows of 4 values + one 16-bit base, per half step.
+    assert rows - quads == pytest.approx(2 * (100 * 6 - 25 * 18))
+
+
+def _defaults():
+    """The parser's defaults, read from bench.main's argument definitions."""
+    import inspect
+    import re
+    src = inspect.getsource(bench.main)
+    fmt = re.search(r'"--format", default="(\w+)"', src).group(1)
+    tol = float(re.search(r'"--tol", type=float, default=([0-9.e-]+)\)', src).group(1))
+    lump = int(re.search(r'"--lump", type=int, default=(\d)', src).group(1))
+    return fmt, tol, lump
+
+
+def test_default_configuration_has_an_ncu_traffic_figure():
+    assert _defaults() in bench.NCU_TRAFFIC_PER_SEGMENT_STEP
+
+
+def test_both_arms_name_the_same_workload():
+    name = bench.workload_name(1024, 500, 20000)
+    assert name.startswith("batched: 1024 neurons, log-uniform 500-20000 segments")
