@@ -109,7 +109,8 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, max_neuron=3000, target_segments=20000):
+def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, max_neuron=3000, target_segments=20000,
+               warmup=2):
     """Time the C oracle (FP64, OpenMP, all host threads) on a sample of the batch: its
     first neurons of at most max_neuron segments, up to target_segments segments, with
     the same mechanisms (HH + na8), soma clamps and detectors.  Everything is built on
@@ -154,7 +155,7 @@ def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, max_neuron=3000,
     co = CpuOracle(P.indptr, P.indices.astype(np.int32), P.data, C, time_step=TIME_STEP, celsius=CELSIUS,
                    hh=hh, clamps=clamps, detectors=[(r, 20.0) for r in roots], kinetic=kin)
     build_s = time.perf_counter() - t_build
-    co.advance(2)
+    co.advance(max(warmup, 1))                   # untimed
     done, t0 = 0, time.perf_counter()
     while done < steps and time.perf_counter() - t0 < time_budget_s:
         co.advance(1)
@@ -177,7 +178,7 @@ def run_reference(args, rank):
     lo, hi = (int(x) for x in args.size_range.split(","))
     trees = batched_trees(args.neurons, first=0, count=64, processes=8, lo=lo, hi=hi)
     currents = batched_currents(args.neurons)
-    res = cpu_sample(trees, currents, args.tol, steps=args.steps + args.warmup, time_budget_s=60.0)
+    res = cpu_sample(trees, currents, args.tol, steps=args.steps, warmup=args.warmup, time_budget_s=60.0)
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "segment-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
