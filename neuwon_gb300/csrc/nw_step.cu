@@ -15,7 +15,12 @@
 // rows are streamed from HBM as (fp32 value, u16 neuron-relative column)
 // in 16-byte vectors, LPR lanes per row, with a compensated sum of
 //   V_i = x_i - leak_i * x_i + sum_{j != i} P_ij (x_j - x_i),
-// which equals sum_j P_ij x_j exactly when leak_i = 1 - sum_j P_ij.
+// which equals sum_j P_ij x_j exactly when leak_i = 1 - sum_j P_ij.  The
+// default storage is the quad format: windows of 4 consecutive columns (one
+// 16-byte value vector and a u16 base per window).  When every conductance
+// source maps one-to-one onto segments (the FUSE instances), the mid-step
+// mechanism update, the new conductance and the second half step's x are one
+// pass, and the conductances are cached for the next step's first half.
 //
 // Plain path: the reference's GPU design (neuwon/database/compute.py:360-418):
 // per-neuron launches, one thread per row or per instance, 32 threads per
