@@ -33,7 +33,7 @@ METRIC = "segment-steps/s on 1 GB300: batched FP32 vs plain, <=0.1 mV err; adjoi
 # (propagator format, tolerance, lumped): quads lumped at 3e-7 464.9 GB per 25-step
 # launch (mean of the four timed launches), quads at 1e-8 charge-conserving 742.6 GB
 # per 25-step launch, rows at 1e-8 1,741.6 GB per 50-step launch.  Commands and
-# figures: profiles/batched_advance_kernel.md.
+# figures: profiles/batched_advance_kernel_lumped_quads.md, _quads_1e-8.md, _rows_1e-8.md.
 NCU_TRAFFIC_PER_SEGMENT_STEP = {("quads", 3e-7, 1): 3324.7, ("quads", 1e-8, 0): 5310.6, ("rows", 1e-8, 0): 6227.5}
 NCU_TRAFFIC_SEGMENTS = 5593190
 
