@@ -68,7 +68,7 @@ int nw_synchronize(nw_ctx* ctx);
 /* ---- model structure ------------------------------------------------ */
 
 /* Segment tree of all neurons (neuwon/rxd/neuron/segment.py:11-25 "parent",
- * neuron.py:119-137 sort_key='neuron').  Segments are in the reference's sorted
+ * neuron.py:11-12 sort_key='neuron').  Segments are in the reference's sorted
  * order: neurons contiguous, neuron k owning [neuron_start[k], neuron_start[k+1]).
  * parent[i] is a global segment index or -1 for a root; parents precede children.
  * time_step is the model dt in ms (rxd_model.py:9); the electric half step is dt/2. */
@@ -104,7 +104,7 @@ int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr,
 /* Charge-conserving pruning: returns the pruned mass of every row of the installed
  * propagator to its diagonal, so each row sums to 1 again.  The unpruned matrix has
  * unit row sums (the reference tests this charge conservation,
- * neuwon/rxd/tests/test_electric.py:216-217); pruning without this correction
+ * neuwon/rxd/tests/test_electric.py:84-85); pruning without this correction
  * (the reference's own behaviour, electric.py:114-115) leaks voltage toward 0 mV
  * at coarse tolerances.  Requires a stored diagonal entry in every row. */
 int nw_propagator_conserve(nw_ctx* ctx);
@@ -196,7 +196,7 @@ int nw_calcium_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_
 
 /* No counterpart in the reference: its neuwon/rxd/synapses.py grows synapse
  * geometry only, and no mechanism has a NET_RECEIVE block.  Spikes are the AP
- * detector's output (neuwon/rxd/neuron/neuron.py:184-188, one detector per neuron,
+ * detector's output (neuwon/rxd/neuron/neuron.py:72-75, one detector per neuron,
  * nw_detectors_set).  A spike of neuron pre_neuron[k] at step t arrives at synapse k
  * at step t + delay_steps[k] (>= 1), and keeps transmitter present for the
  * mechanism updates of pulse_steps steps.  Each synapse holds a 2-state AMPA scheme
@@ -223,7 +223,7 @@ int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron
 int nw_clamps_set(nw_ctx* ctx, int64_t count, const int64_t* segment, const double* amps,
                   const int64_t* first_tick, const int64_t* num_ticks);
 
-/* AP detectors, one per neuron (neuwon/rxd/neuron/neuron.py:139-146, 184-188). */
+/* AP detectors, one per neuron (neuwon/rxd/neuron/neuron.py:27-33, 65-75). */
 int nw_detectors_set(nw_ctx* ctx, const int64_t* segment, const double* threshold_mV);
 
 /* Voltage probes: replaces TimeSeries.record of Segment.voltage after each
@@ -334,31 +334,43 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
 /* Largest num_segments accepted by nw_electric_half_step_noalloc. */
 #define NW_NOALLOC_MAX_SEGMENTS (1 << 20)
 
-/* No counterpart in the reference: one electric half step (membrane update and
- * propagator multiply, the arithmetic of Segment._advance_electric) on arrays the
- * caller allocated, for callers that cannot call cudaMalloc -- e.g. a host whose
- * device memory must all come from its own pool allocator, or a loop that must
- * not allocate between steps.  Nothing is allocated by the call: the scratch
- * vector the propagator multiplies is a static device array of
- * NW_NOALLOC_MAX_SEGMENTS doubles (8 MiB, held on every GPU that loads this
- * library until the process exits).
- *   rowptr/col/val: the propagator in CSR, FP64, diagonal included (n x n);
- *   voltage (mV): read, then overwritten with the result;
- *   capacitance (F), sum_conductance (S), driving_voltage (mV), sum_current (A): inputs;
- *   half_step_ms: the time step of this half step (dt/2);
+/* No counterpart in the reference.  One electric half step on arrays the caller
+ * allocated, for callers that cannot call cudaMalloc: a host application whose
+ * device memory must all come from its own pool allocator (a library's own
+ * cudaMalloc would escape the pool's accounting or fail under its limit), or a
+ * time loop that must not allocate between steps.  Per segment i, with
+ * h = half_step_ms:
+ *   x_i    = E_i - (E_i - V_i) exp(-h 1e-3 G_i / C_i) + h I_i / C_i
+ *   V      = P x                                   (CSR matrix-vector product)
+ *   Vint_i = h 1e-3 E_i + (h 1e-3 G_i / C_i)(E_i - V_i) exp(-h 1e-3 G_i / C_i)
+ *            + 0.5 h 1e-3 (h I_i / C_i)            (V_i before the update)
+ * Nothing is allocated by the call: the scratch vector x is a static device
+ * array of NW_NOALLOC_MAX_SEGMENTS doubles (8 MiB).  The CUDA runtime creates it
+ * on a GPU when this library's device code is loaded there -- with lazy module
+ * loading (the default) at the first call on that GPU, at library load with
+ * CUDA_MODULE_LOADING=EAGER -- and keeps it until the process exits.
+ *   rowptr/col/val: the propagator P in CSR, FP64, diagonal included (n x n);
+ *   voltage V (mV): read, then overwritten with the result;
+ *   capacitance C (F), sum_conductance G (S), driving_voltage E (mV),
+ *   sum_current I (A): inputs;
+ *   integral_voltage Vint (mV s, may be NULL: not written): output;
+ *   half_step_ms: the length of this half step (dt/2, ms);
  *   stream: cudaStream_t to launch on (NULL = default stream); the call returns
  *   after enqueueing, without synchronising.
  * All device pointers must be on the current device.  Returns NW_ERR_LIMIT when
  * num_segments > NW_NOALLOC_MAX_SEGMENTS, NW_ERR_ARG for null pointers or a
- * non-positive step.  The first call on each device looks up the scratch
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  Every call shares the one scratch array, so calls that
- * overlap on the GPU (different streams, or different threads) race; each call
- * overwrites the part it uses before reading it, so nothing needs clearing. */
+ * non-positive step, NW_ERR_CUDA when a CUDA error is pending before the call
+ * (it is left pending) or a launch fails.  The first call in each CUDA context
+ * looks up the scratch array's device address (cudaGetSymbolAddress) and keeps
+ * it for that context; make that first call before any stream capture.  Every
+ * call shares the one scratch array, so calls that overlap on the GPU
+ * (different streams, or different threads) race; each call overwrites the
+ * part it uses before reading it, so nothing needs clearing. */
 int nw_electric_half_step_noalloc(int64_t num_segments, const int64_t* rowptr, const int32_t* col,
                                   const double* val, double* voltage, const double* capacitance,
                                   const double* sum_conductance, const double* driving_voltage,
-                                  const double* sum_current, double half_step_ms, void* stream);
+                                  const double* sum_current, double* integral_voltage, double half_step_ms,
+                                  void* stream);
 
 #ifdef __cplusplus
 }

@@ -77,7 +77,7 @@ def load(build_if_missing=True):
         "nw_set_option": ([c_void_p, ctypes.c_char_p, c_i64], c_int),
         "nw_get_option": ([c_void_p, ctypes.c_char_p, P(c_i64)], c_int),
         "nw_electric_half_step_noalloc": ([c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
-                                           c_void_p, c_void_p, c_void_p, c_double, c_void_p], c_int),
+                                           c_void_p, c_void_p, c_void_p, c_void_p, c_double, c_void_p], c_int),
         "nw_adjoint_forward": ([c_void_p, c_i64, ctypes.c_int32, c_void_p, P(c_double)], c_int),
         "nw_adjoint_backward": ([c_void_p, c_double, c_void_p, c_void_p, c_void_p, P(c_double)], c_int),
         "nw_get_tuning": ([c_void_p, P(c_int), P(c_int), P(c_int)], c_int),

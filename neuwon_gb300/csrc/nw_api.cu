@@ -364,7 +364,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     NW_CHECK(fill(ctx, ctx->V, -70.0, num_segments));   // rxd_model.py:12 initial_voltage
     NW_CUDA(ctx, cudaMemsetAsync(ctx->Vint.ptr, 0, rs * num_segments, ctx->stream));
     NW_CUDA(ctx, cudaMemsetAsync(ctx->Inonspec.ptr, 0, rs * num_segments, ctx->stream));
-    // Default AP detectors: each neuron's first segment (its root), 20 mV (neuron.py:141,156).
+    // Default AP detectors: each neuron's first segment (its root), 20 mV (neuron.py:28, 43).
     std::vector<int64_t> dseg(num_neurons);
     std::vector<double> dthr(num_neurons, 20.0);
     for (int64_t k = 0; k < num_neurons; ++k) dseg[k] = neuron_start[k];

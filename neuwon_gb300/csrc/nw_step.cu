@@ -583,7 +583,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                 }
             }
             if (BULK && s_abort) break;
-            // AP detector (neuron.py:184-188) and probes after the full step.
+            // AP detector (neuron.py:72-75) and probes after the full step.
             if (tid == 0 && a.has_det) {
                 const bool over = a.V[a.det_seg[j]] >= a.det_thr[j];
                 ap_det = over && !ap_state;

@@ -145,7 +145,7 @@ struct StepArgs {
 };
 
 // Sum of a segment's mechanism conductances and conductance-weighted reversal
-// potentials (species.py:389-393 scatter, done here as a gather over the
+// potentials (species.py:256-260 scatter, done here as a gather over the
 // segment's instances in registration order: deterministic, no atomics).
 // One HH instance's conductances added to the segment's running sums.
 template <typename real>

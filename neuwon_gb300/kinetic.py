@@ -4,7 +4,7 @@ Restates the reference's lti_sim pipeline (neuwon/rxd/lti_sim/):
 
 * the propagator of one step is expm(A(v) dt) with every column renormalised
   to sum to 1 (lti_model.py:51-65);
-* the input range is cut into equal buckets (inputs.py:150-161) and, in every
+* the input range is cut into equal buckets (inputs.py:26-48, 72-83) and, in every
   bucket, each matrix entry is fitted by least squares with a polynomial in
   the location within the bucket (approx.py:159-174, polynomial.py:3-20);
 * at run time an instance locates its voltage, evaluates the polynomials and
@@ -120,7 +120,7 @@ class LTITable:
         self.vmin, self.vmax = float(vmin), float(vmax)
         self.num_buckets = int(num_buckets)
         self.num_terms = int(degree) + 1
-        self.bucket_frq = self.num_buckets / (self.vmax - self.vmin)       # inputs.py:152-155
+        self.bucket_frq = self.num_buckets / (self.vmax - self.vmin)       # inputs.py:74-77
         self.bucket_width = (self.vmax - self.vmin) / self.num_buckets
         S, T, nb = scheme.num_states, self.num_terms, self.num_buckets
         if sample_inputs is None:

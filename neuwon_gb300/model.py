@@ -2,10 +2,10 @@
 
 ``RxD_Model`` keeps the reference's public surface for the hot path
 (neuwon/rxd/rxd_model.py:9-80): the constructor arguments, ``Neuron`` and
-``Segment`` factories (neuwon/rxd/neuron/neuron.py:148-156,
+``Segment`` factories (neuwon/rxd/neuron/neuron.py:35-43,
 segment.py:27-104), mechanism insertion (segment.py:124-160,
 mechanisms.py:56-99), ``Segment.inject_current`` (electric.py:119-125),
-AP detectors (neuron.py:178-188), the clocks (database/time.py:54-121) and
+AP detectors (neuron.py:65-75), the clocks (database/time.py:54-121) and
 ``TimeSeries.record`` of voltages (time.py:189-231).
 
 The segment table is a structure of arrays in creation order.  Before the

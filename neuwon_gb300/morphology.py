@@ -3,7 +3,7 @@
 The geometry functions restate, as vectorised numpy over whole trees, the
 per-segment rules of the reference:
 
-* ``neuwon/rxd/neuron/geometry.py:255-315`` -- length, primary flag, secondary
+* ``neuwon/rxd/neuron/geometry.py:75-155`` -- length, primary flag, secondary
   length, surface area (end caps on leaves, attachment disks of lateral
   children subtracted), cross-sectional area and volume;
 * ``neuwon/rxd/neuron/electric.py:49-54`` -- axial resistance
@@ -11,7 +11,7 @@ per-segment rules of the reference:
 
 One quirk is kept on purpose: the reference computes a segment's capacitance
 once, when the segment is created (``segment.py:36-37``), while its surface
-area is recomputed every time a child is attached (``geometry.py:251``).  So
+area is recomputed every time a child is attached (``geometry.py:91``).  So
 capacitance uses the *creation-time* area (the segment as a leaf, with its
 end cap and no children), and mechanism magnitudes use the area at insertion
 time, which for mechanisms inserted after the tree is grown is the final area.
@@ -128,7 +128,7 @@ def neuron_sizes(num_neurons, seed, lo=500, hi=20000):
 
 
 def geometry(tree):
-    """Reference geometry of a whole tree (neuwon/rxd/neuron/geometry.py:164-315).
+    """Reference geometry of a whole tree (neuwon/rxd/neuron/geometry.py:75-155).
 
     Returns a dict of float64 arrays: length, primary (bool), secondary_length,
     surface_area (final, with all children attached), creation_area (the

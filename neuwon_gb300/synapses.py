@@ -3,7 +3,7 @@
 The reference grows synapse geometry (neuwon/rxd/synapses.py) but has no
 synaptic kinetics and no event delivery: no mechanism in it has a NET_RECEIVE
 block.  This module defines them for the GPU path.  A spike is the AP
-detector's output (neuwon/rxd/neuron/neuron.py:184-188); it reaches each
+detector's output (neuwon/rxd/neuron/neuron.py:72-75); it reaches each
 outgoing synapse after that synapse's axonal delay, rounded to whole steps.
 An arrival keeps transmitter present for ``pulse`` ms (Destexhe, Mainen &
 Sejnowski 1994).  Each synapse has a 2-state AMPA scheme C <-> O and a

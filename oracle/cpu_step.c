@@ -5,10 +5,10 @@
  * FP64, OpenMP over segments / instances.  Follows:
  *   neuwon/rxd/rxd_model.py:63-80     advance: species(dt/2), mechanisms, species(dt/2), AP
  *   neuwon/rxd/rxd_model.py:91-113    accumulators, input clock tick, driving voltage
- *   neuwon/rxd/species.py:389-393     nonspecific conductance scatter (summed here)
+ *   neuwon/rxd/species.py:256-260     nonspecific conductance scatter (summed here)
  *   neuwon/rxd/neuron/electric.py:56-76  exact membrane update and V <- P x
  *   nmodl_library/artificial/hh.mod + neuwon/rxd/nmodl/solver.py:48-55  HH gates
- *   neuwon/rxd/neuron/neuron.py:184-188  AP detector
+ *   neuwon/rxd/neuron/neuron.py:72-75  AP detector
  *   neuwon/database/time.py:287-302   current clamps on the half-step clock
  *   neuwon/rxd/lti_sim/codegen.py:39-106  kinetic scheme: voltage bucket, polynomial
  *                                     table [bucket][col][row][term], CONSERVE renormalisation

@@ -145,7 +145,7 @@ class HHInstances:
       by the instance magnitude (um2); neuwon/rxd/nmodl/__init__.py:99-107, 404-406;
     * ``USEION na WRITE gna, ena`` writes the equilibrium, so each conductance
       is a *nonspecific* conductance stored on the instance and scattered to
-      its segment; nmodl/__init__.py:179-208, species.py:359-396;
+      its segment; nmodl/__init__.py:179-208, species.py:229-263;
     * ``SOLVE states`` without METHOD uses the exact solution of the linear
       gate ODEs, x <- xinf + (x - xinf)*exp(-dt/xtau); nmodl/solver.py:48-55,105-106.
     """
@@ -164,7 +164,7 @@ class HHInstances:
         self.g = {"na": np.zeros(m), "k": np.zeros(m), "l": np.zeros(m)}
 
     def zero_accumulators(self):
-        """species.py:385-387 (nonspecific conductances reset before mechanisms run)."""
+        """species.py:251-253 (nonspecific conductances reset before mechanisms run)."""
         for g in self.g.values():
             g.fill(0.0)
 
@@ -239,7 +239,7 @@ class KineticInstances:
 # The reference has no synaptic kinetics and no event delivery (its
 # neuwon/rxd/synapses.py only grows synapse geometry; there is no NET_RECEIVE).
 # What follows is this project's definition, restated here as the oracle for the
-# GPU kernels: spikes are the AP detector's output (neuron.py:184-188), routed
+# GPU kernels: spikes are the AP detector's output (neuron.py:72-75), routed
 # through a priority queue to synapses after an axonal delay of whole steps.
 
 def synapse_matrices(time_step, alpha, beta, delta=None, rho=None, t_max=1.0):
@@ -382,7 +382,7 @@ class OracleModel:
 
     ``duplicates='sum'`` adds every mechanism instance's conductance into its
     segment.  ``duplicates='numpy'`` reproduces the reference's fancy-index
-    ``a[idx] += b`` (species.py:392-393), under which only one of several
+    ``a[idx] += b`` (species.py:256-260), under which only one of several
     instances on the same segment is counted.
     """
 
@@ -394,7 +394,7 @@ class OracleModel:
         self.R = np.asarray(R, dtype=np.float64)
         self.C = np.asarray(C, dtype=np.float64)
         self.time_step = float(time_step)
-        self.half_step = 0.5 * self.time_step     # rxd_model.py:21, species.py:406
+        self.half_step = 0.5 * self.time_step     # rxd_model.py:21, species.py:273
         self.celsius = float(celsius)
         self.voltage = np.full(self.n, float(v_init))
         self.integral_voltage = np.zeros(self.n)
@@ -480,7 +480,7 @@ class OracleModel:
         if self.calcium is not None:
             self.calcium.mechanisms(self.voltage, self.hh)
 
-    # neuwon/rxd/neuron/neuron.py:184-188
+    # neuwon/rxd/neuron/neuron.py:72-75
     def _advance_AP_detector(self):
         for k, (seg, thr) in enumerate(self.detectors):
             over = self.voltage[seg] >= thr

@@ -1,9 +1,9 @@
 """Generate golden fixtures by running the reference NEUWON itself.
 
-Run from the repository root with the reference checked out at
-``/root/reference`` (or ``NEUWON_REFERENCE``):
+Run from the repository root with the path of a checkout of the reference
+as the first argument (or in the environment variable ``NEUWON_REFERENCE``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 The reference imports four third-party packages that are absent here
 (numba, graph_algorithms, matplotlib, BlueBrain nmodl).  They are replaced by
@@ -31,7 +31,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REFERENCE = os.environ.get("NEUWON_REFERENCE", "/root/reference")
+REFERENCE = None        # set by main() from argv[1] or NEUWON_REFERENCE
 
 STUBS = {
     "numba/__init__.py": """
@@ -74,7 +74,19 @@ STUBS = {
 }
 
 
+def reference_path(argv=None):
+    """The reference checkout: first argument, else NEUWON_REFERENCE; no default."""
+    argv = sys.argv[1:] if argv is None else argv
+    path = argv[0] if argv else os.environ.get("NEUWON_REFERENCE")
+    if not path or not os.path.isdir(os.path.join(path, "neuwon")):
+        raise SystemExit("usage: make_golden.py <reference checkout> (or set NEUWON_REFERENCE)")
+    return os.path.abspath(path)
+
+
 def install_stubs():
+    global REFERENCE
+    if REFERENCE is None:
+        REFERENCE = reference_path()
     root = tempfile.mkdtemp(prefix="neuwon_stubs_")
     for rel, src in STUBS.items():
         path = os.path.join(root, rel)

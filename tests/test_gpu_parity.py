@@ -244,7 +244,7 @@ def test_k_step_fusion_equals_single_steps():
 
 
 def test_passive_soma_only_and_no_mechanisms():
-    """A lone sphere without mechanisms: injected charge ΔQ = I·t (test_electric.py:264-282)."""
+    """A lone sphere without mechanisms: injected charge ΔQ = I·t (test_electric.py:132-150)."""
     m = nw.RxD_Model(time_step=0.01, precision="f64")
     root = m.Neuron([0, 0, 0], 10).root
     m.advance(300)

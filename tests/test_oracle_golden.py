@@ -59,7 +59,7 @@ def test_propagator_matches_reference():
     P = propagator(t.parent, R, C, 0.05)
     Pr = scipy.sparse.csr_matrix((F["prop_data"], F["prop_indices"], F["prop_indptr"]))
     assert abs(P - Pr).max() < 1e-14
-    # Charge conservation check of neuwon/rxd/tests/test_electric.py:216-217.
+    # Charge conservation check of neuwon/rxd/tests/test_electric.py:84-85.
     assert np.sum(P.data) / P.shape[0] == pytest.approx(1.0)
 
 
@@ -108,7 +108,7 @@ def test_oracle_single_neuron_config_matches_reference():
 
 
 def test_duplicate_instances_reference_drops_one():
-    """species.py:392-393 drops duplicate segment indices; the sum differs."""
+    """species.py:256-260 drops duplicate segment indices; the sum differs."""
     trees = [random_tree(40, seed=21), random_tree(25, seed=22), random_tree(60, seed=23)]
     clamps = [(0, 0, 0.3, 1., 6.), (1, 5, 0.2, 2., 3.), (2, 30, 0.25, 0.5, 8.)]
     a, _ = oracle_case(trees, clamps, hh_kw=dict(ena=50., ek=-77.), dups=[(0, 3)], duplicates="numpy")
@@ -136,7 +136,7 @@ def _sphere(diameter=20.0):
 
 
 def test_time_constant():
-    """neuwon/rxd/tests/test_electric.py:160-178."""
+    """neuwon/rxd/tests/test_electric.py:28-46."""
     t = _sphere(20.0)
     R, C = passive_electric(geometry(t))
     G = 1e-10
@@ -154,7 +154,7 @@ def test_time_constant():
 
 
 def test_inject_current_charge():
-    """neuwon/rxd/tests/test_electric.py:264-282: delta Q = I t on a passive sphere."""
+    """neuwon/rxd/tests/test_electric.py:132-150: delta Q = I t on a passive sphere."""
     t = _sphere(10.0)
     R, C = passive_electric(geometry(t))
     f, c = clamp_ticks(3.0, 2.0, 0.01)
@@ -170,7 +170,7 @@ def test_inject_current_charge():
 
 @pytest.mark.parametrize("diam,rm,max_len,dt,ptol", [(1, 4e11, 2, .01, .05), (.9, 2e11, 10, .025, .15)])
 def test_length_constant(diam, rm, max_len, dt, ptol):
-    """neuwon/rxd/tests/test_electric.py:180-235 on a 3 mm cable."""
+    """neuwon/rxd/tests/test_electric.py:48-130 on a 3 mm cable."""
     from neuwon_gb300 import RxD_Model
     m = RxD_Model()
     root = m.Neuron([0, 0, 0], diam).root

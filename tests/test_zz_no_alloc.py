@@ -1,13 +1,16 @@
 """The allocation-free half step, called through the C ABI on caller-owned arrays.
 
-Callers whose device memory all comes from their own allocator cannot let a
-library call cudaMalloc; nw_electric_half_step_noalloc runs the membrane
-update and propagator multiply of one half step on arrays they provide, with
-its scratch in a static device array.  Here two calls in a row (one full step
-of a passive model with a current clamp) must reproduce what the existing
-entry point nw_advance (plain FP64 path) computes, within the FP64 parity
-tolerance of the other GPU tests (1e-7 mV); and again for a second pair of
-calls, so the shared scratch array is reused.
+Callers whose device memory all comes from their own pool allocator, or whose
+time loop must not allocate, cannot let a library call cudaMalloc;
+nw_electric_half_step_noalloc runs the membrane update and propagator
+multiply of one half step on arrays they provide, with its scratch vector in
+a static device array.  Here pairs of calls in a row (full steps of a model
+with a leak conductance on every segment and a current clamp) must reproduce
+what the existing entry point nw_advance (plain FP64 path) computes, within the
+FP64 parity tolerance of the other GPU tests (1e-7 mV): voltages and integral
+voltages, over three pairs, so the shared scratch array is reused, and the
+exponential branch exp(-dt G / C) is exercised with nonzero G and E.  Free
+device memory must not change across the calls.
 """
 import ctypes
 
@@ -39,42 +42,56 @@ def test_noalloc_half_step_matches_advance_on_two_calls():
     from neuwon_gb300.morphology import random_tree
 
     tree = random_tree(400, seed=77)
-    amps = 0.3e-9
-    m = nw.RxD_Model(time_step=0.1, precision="f64", path="plain")
+    el = -54.3
+    # HH with only its leak: a constant conductance gl on every segment with reversal el.
+    m = nw.RxD_Model(time_step=0.1, precision="f64", path="plain",
+                     mechanisms=[nw.HH.configure(gnabar=0.0, gkbar=0.0, glbar=0.002, el=el)])
     m.add_tree(tree)
+    m.insert_everywhere("hh")
     nw.Segment(m, 0).inject_current(0.3, 10.0)            # active on ticks 1..200
     m._sync()
     rowptr, col, val = _propagator(m)
-    C = m._geometry()["capacitance"][m._order]            # device order (depth-first within the neuron)
     n = m._n
+    C = m._geometry()["capacitance"][m._order]            # device order (depth-first within the neuron)
+    gl = np.empty(n)
+    gl[m._inv] = m.get_data("hh.gl_coef")                  # instance k sits on creation segment k
+    assert gl.min() > 0
     lib = _lib.load()
 
     dev = torch.device("cuda", 0)
-    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in dict(
-        rowptr=rowptr, col=col, val=val, C=C, G=np.zeros(n), E=np.zeros(n),
-        V=np.full(n, -70.0)).items()}
+    to_dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d = {k: to_dev(v) for k, v in dict(rowptr=rowptr, col=col, val=val, C=C, V=np.full(n, -70.0),
+                                       Vint=np.zeros(n), G0=np.zeros(n), E0=np.zeros(n),
+                                       G=gl, E=np.full(n, el)).items()}
     I = np.zeros(n)
-    I[0] = amps
-    d["I"] = torch.from_numpy(I).to(dev)
+    I[m._inv[0]] = 0.3e-9
+    d["I"] = to_dev(I)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
 
-    def half_step():
-        torch.cuda.synchronize()
+    def half_step(G, E):
         rc = lib.nw_electric_half_step_noalloc(
-            n, ctypes.c_void_p(d["rowptr"].data_ptr()), ctypes.c_void_p(d["col"].data_ptr()),
-            ctypes.c_void_p(d["val"].data_ptr()), ctypes.c_void_p(d["V"].data_ptr()),
-            ctypes.c_void_p(d["C"].data_ptr()), ctypes.c_void_p(d["G"].data_ptr()),
-            ctypes.c_void_p(d["E"].data_ptr()), ctypes.c_void_p(d["I"].data_ptr()), 0.05, None)
-        torch.cuda.synchronize()
+            n, p(d["rowptr"]), p(d["col"]), p(d["val"]), p(d["V"]), p(d["C"]), p(G), p(E), p(d["I"]),
+            p(d["Vint"]), 0.05, None)
         assert rc == 0
 
-    for _ in range(2):
-        half_step()
-        half_step()
+    for k in range(3):
+        # The first half step of the first step sees no mechanism conductance yet
+        # (rxd_model.py:63-80: the accumulators are filled by the mechanism phase).
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(0)[0]
+        half_step(d["G0"] if k == 0 else d["G"], d["E0"] if k == 0 else d["E"])
+        half_step(d["G"], d["E"])
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info(0)[0] == free0     # nothing allocated by the two calls
         m.advance(1)
         want = m.get_data("Segment.voltage")              # creation order
         got = d["V"].cpu().numpy()[m._inv]
         assert np.abs(got - want).max() < TOL_MV
-        assert np.abs(got + 70.0).max() > 1e-6        # the clamp moved the voltage
+        assert np.abs(got + 70.0).max() > 1e-3            # the clamp and the leak moved the voltage
+        want_int = m.get_data("Segment.integral_voltage")
+        got_int = d["Vint"].cpu().numpy()[m._inv]
+        assert np.abs(got_int - want_int).max() < TOL_MV * 1e-3
+        assert np.abs(got_int).max() > 0
     m.close()
 
 
@@ -83,5 +100,5 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     lib = _lib.load()
     dummy = ctypes.c_void_p(1)
     rc = lib.nw_electric_half_step_noalloc((1 << 20) + 1, dummy, dummy, dummy, dummy, dummy, dummy,
-                                           dummy, dummy, 0.05, None)
+                                           dummy, dummy, None, 0.05, None)
     assert rc == -6   # NW_ERR_LIMIT, checked before anything is launched
