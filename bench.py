@@ -109,62 +109,89 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_sample(trees, currents, tol, steps, time_budget_s=20.0, max_neuron=3000, target_segments=20000,
-               warmup=2):
-    """Time the C oracle (FP64, OpenMP, all host threads) on a sample of the batch: its
-    first neurons of at most max_neuron segments, up to target_segments segments, with
-    the same mechanisms (HH + na8), soma clamps and detectors.  Everything is built on
-    the CPU (scipy expm per neuron, pruned, charge-conserving; host lti_sim table): no
-    GPU and none of this package's kernels are involved."""
-    from neuwon_gb300.kinetic import Kinetic, LTITable, na8
-    from neuwon_gb300.morphology import geometry, passive_electric
-    from neuwon_gb300.workloads import CELSIUS, HH_PARAMS, TIME_STEP
-    from oracle.cpu_oracle import CpuOracle
-    from oracle.reference_step import propagator
-    sample, idx, segs = [], [], 0
-    for k, t in enumerate(trees):
-        if len(t) <= max_neuron:
-            sample.append(t)
-            idx.append(k)
-            segs += len(t)
-            if segs >= target_segments:
-                break
-    parents, R, C, area, roots, off = [], [], [], [], [], 0
-    for t in sample:
-        g = geometry(t)
-        r, c = passive_electric(g)
-        parents.append(np.where(t.parent < 0, -1, t.parent + off))
-        R.append(r); C.append(c); area.append(g["surface_area"]); roots.append(off)
-        off += len(t)
-    parent, R, C, area = (np.concatenate(x) for x in (parents, R, C, area))
-    n = len(parent)
-    t_build = time.perf_counter()
-    P = propagator(parent, R, C, 0.5 * TIME_STEP, prune=tol).tocsr()
-    rows = np.repeat(np.arange(n), np.diff(P.indptr))
-    diag = np.flatnonzero(P.indices == rows)
-    P.data[diag] += 1.0 - np.asarray(P.sum(axis=1)).ravel()[rows[diag]]   # charge-conserving
-    seg = np.arange(n)
-    hh = dict(segment=seg, gna=HH_PARAMS["gnabar"] * 1e-8 * area, gk=HH_PARAMS["gkbar"] * 1e-8 * area,
-              gl=HH_PARAMS["glbar"] * 1e-8 * area, ena=HH_PARAMS["ena"], ek=HH_PARAMS["ek"], el=HH_PARAMS["el"])
-    sch = na8()
-    tbl = LTITable(sch, TIME_STEP, CELSIUS)
-    kin = dict(segment=seg, gcoef=Kinetic.gbar * 1e-8 * area, table=tbl.layout, vmin=tbl.vmin,
-               bucket_frq=tbl.bucket_frq, open=sch.open_states, erev=Kinetic.erev, conserve=sch.conserve_sum,
-               init=sch.steady_state(-70.0, CELSIUS))
-    clamps = [(r, float(currents[k]) * 1e-9, 1, 1 << 40) for r, k in zip(roots, idx)]
-    co = CpuOracle(P.indptr, P.indices.astype(np.int32), P.data, C, time_step=TIME_STEP, celsius=CELSIUS,
-                   hh=hh, clamps=clamps, detectors=[(r, 20.0) for r in roots], kinetic=kin)
-    build_s = time.perf_counter() - t_build
-    co.advance(max(warmup, 1))                   # untimed
-    done, t0 = 0, time.perf_counter()
-    while done < steps and time.perf_counter() - t0 < time_budget_s:
-        co.advance(1)
-        done += 1
+class CpuSample:
+    """The C oracle (FP64, OpenMP, all host threads) on a sample of the batch: its first
+    neurons of at most max_neuron segments, up to target_segments segments, with the
+    same mechanisms (HH + na8), soma clamps, detectors and propagator pruning as the
+    batch (lumped at the bench tolerance: oracle_lump in C, the walk of the GPU build;
+    else charge-conserving).  Everything is built on the CPU (scipy expm per neuron,
+    host lti_sim table): no GPU and none of this package's kernels are involved."""
+
+    def __init__(self, trees, currents, tol, lump=True, max_neuron=3000, target_segments=20000):
+        from neuwon_gb300.kinetic import Kinetic, LTITable, na8
+        from neuwon_gb300.morphology import geometry, passive_electric
+        from neuwon_gb300.workloads import CELSIUS, HH_PARAMS, TIME_STEP
+        from oracle.cpu_oracle import CpuOracle, lump as c_lump
+        from oracle.reference_step import propagator
+        import scipy.sparse
+        sample, idx, segs = [], [], 0
+        for k, t in enumerate(trees):
+            if len(t) <= max_neuron:
+                sample.append(t)
+                idx.append(k)
+                segs += len(t)
+                if segs >= target_segments:
+                    break
+        t0 = time.perf_counter()
+        blocks, roots, area, C, off = [], [], [], [], 0
+        for t in sample:
+            g = geometry(t)
+            r, c = passive_electric(g)
+            P = propagator(t.parent, r, c, 0.5 * TIME_STEP, prune=0.0).toarray()
+            if lump:
+                P = c_lump(P, t.parent, tol)
+            else:
+                P[np.abs(P) < tol] = 0.0
+                P[np.diag_indices(len(t))] += 1.0 - P.sum(axis=1)        # charge-conserving
+            blocks.append(scipy.sparse.csr_matrix(P))
+            roots.append(off); area.append(g["surface_area"]); C.append(c)
+            off += len(t)
+        P = scipy.sparse.block_diag(blocks, format="csr")
+        P.sort_indices()
+        area, C = np.concatenate(area), np.concatenate(C)
+        n = off
+        seg = np.arange(n)
+        hh = dict(segment=seg, gna=HH_PARAMS["gnabar"] * 1e-8 * area, gk=HH_PARAMS["gkbar"] * 1e-8 * area,
+                  gl=HH_PARAMS["glbar"] * 1e-8 * area, ena=HH_PARAMS["ena"], ek=HH_PARAMS["ek"], el=HH_PARAMS["el"])
+        sch = na8()
+        tbl = LTITable(sch, TIME_STEP, CELSIUS)
+        kin = dict(segment=seg, gcoef=Kinetic.gbar * 1e-8 * area, table=tbl.layout, vmin=tbl.vmin,
+                   bucket_frq=tbl.bucket_frq, open=sch.open_states, erev=Kinetic.erev, conserve=sch.conserve_sum,
+                   init=sch.steady_state(-70.0, CELSIUS))
+        clamps = [(r, float(currents[k]) * 1e-9, 1, 1 << 40) for r, k in zip(roots, idx)]
+        self.co = CpuOracle(P.indptr, P.indices.astype(np.int32), P.data, C, time_step=TIME_STEP, celsius=CELSIUS,
+                            hh=hh, clamps=clamps, detectors=[(r, 20.0) for r in roots], kinetic=kin)
+        self.build_s = time.perf_counter() - t0
+        self.n, self.neurons, self.entries_per_row = n, len(sample), P.nnz / n
+        self.max_neuron, self.lump, self.tol = max_neuron, lump, tol
+
+    def describe(self, steps):
+        pruning = "lumped" if self.lump else "charge-conserving"
+        return (f"{self.neurons} neurons of the batch of <= {self.max_neuron} segments ({self.n} segments, "
+                f"{self.entries_per_row:.0f} propagator entries/row, {pruning} at {self.tol:g}), HH + na8, {steps} "
+                f"steps, FP64 C restatement (oracle/cpu_step.c) with OpenMP, built on the CPU in {self.build_s:.0f} s")
+
+    def steps_for(self, seconds):
+        """Steps that take about `seconds` (measured on a short run; advances the model)."""
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < 0.2:
+            self.co.advance(1)
+            k += 1
+        return max(1, int(k * seconds / (time.perf_counter() - t0)))
+
+
+def cpu_sample(trees, currents, tol, lump=True, time_budget_s=15.0, warmup=2):
+    """Segment-steps/s of the C oracle on the batch sample over about time_budget_s
+    seconds of CPU work (after `warmup` untimed steps)."""
+    cs = CpuSample(trees, currents, tol, lump)
+    cs.co.advance(max(warmup, 1))                 # untimed
+    k = cs.steps_for(time_budget_s)
+    t0 = time.perf_counter()
+    cs.co.advance(k)
     dt = time.perf_counter() - t0
-    return {"value": n * done / dt, "unit": "segment-steps/s", "cores": co.threads(), "kind": "port",
-            "sample": f"{len(sample)} neurons of the batch of <= {max_neuron} segments ({n} segments, "
-                      f"{P.nnz / n:.0f} propagator entries/row), HH + na8, {done} steps, FP64 C restatement "
-                      f"(oracle/cpu_step.c) with OpenMP, built on the CPU in {build_s:.0f} s"}
+    return {"value": cs.n * k / dt, "unit": "segment-steps/s", "cores": cs.co.threads(), "kind": "port",
+            "sample": cs.describe(k), "entries_per_row": cs.entries_per_row, "seconds": dt}
 
 
 def workload_name(neurons, lo, hi):
@@ -174,18 +201,35 @@ def workload_name(neurons, lo, hi):
 
 
 def run_reference(args, rank):
+    """The reference arm: the CPU path restated in C (the reference's own numba path
+    cannot run here: numba is absent) on the batch sample, all host threads.  A step
+    is a bounded chunk of that sample: max(0.5 s, 10 s / K) of CPU work, so the K
+    timed steps always cover at least 10 s whatever K is; W chunks warm up first."""
     from neuwon_gb300.workloads import batched_currents, batched_trees
     lo, hi = (int(x) for x in args.size_range.split(","))
     trees = batched_trees(args.neurons, first=0, count=64, processes=8, lo=lo, hi=hi)
     currents = batched_currents(args.neurons)
-    res = cpu_sample(trees, currents, args.tol, steps=args.steps, warmup=args.warmup, time_budget_s=60.0)
-    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "segment-steps/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+    cs = CpuSample(trees, currents, args.tol, bool(args.lump))
+    K = max(1, args.steps)
+    chunk = cs.steps_for(max(0.5, 10.0 / K))
+    for _ in range(max(args.warmup, 1)):
+        cs.co.advance(chunk)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        cs.co.advance(chunk)
+    dt = time.perf_counter() - t0
+    value = cs.n * chunk * K / dt
+    res = {"value": value, "unit": "segment-steps/s", "cores": cs.co.threads(), "kind": "port",
+           "sample": cs.describe(chunk * K) + f"; one step = {chunk} sample steps", "seconds": dt,
+           "entries_per_row": cs.entries_per_row}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "segment-steps/s",
+            "n_gpus": args.gpus, "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * dt / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": workload_name(args.neurons, lo, hi),
-                                            "sample": res["sample"], "propagator_tolerance": args.tol},
+                                            "sample": res["sample"], "propagator_tolerance": args.tol,
+                                            "propagator_pruning": "lumped" if args.lump else "charge-conserving"},
             "cpu_baseline": res,
-            "e2e": {"value": res["value"], "unit": "segment-steps/s", "h2d_bytes_per_step": 0,
+            "e2e": {"value": value, "unit": "segment-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -194,10 +238,11 @@ def log(msg):
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
-def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows", lump=False):
-    """FP32 batched at the bench tolerance against FP64 with a propagator pruned at ref_tol
-    (both charge-conserving); the FP64 reference runs on the wide path, which spreads the
-    few sample neurons over every SM."""
+def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows", lump=False, label="sample"):
+    """FP32 batched at the bench tolerance and pruning against FP64 with a propagator
+    pruned at ref_tol (charge-conserving); the FP64 reference runs on the wide path,
+    which spreads the sample neurons over every SM.  Max |dV| at every soma after every
+    step and at every segment every 50 steps (also per 100 ms of simulated time)."""
     from neuwon_gb300 import Segment, TimeSeries
     from neuwon_gb300.workloads import build_model
     t0 = time.perf_counter()
@@ -213,23 +258,59 @@ def accuracy(trees, currents, tol, device, steps, ref_tol, fmt="rows", lump=Fals
         f"(reference {ref.propagator_nnz / ref._n:.0f} entries/row)")
     t0 = time.perf_counter()
     worst_all, chunk = 0.0, 50
-    for _ in range(steps // chunk):
+    by_period, period = [], 1000                       # max error over all segments per 100 ms
+    for k in range(steps // chunk):
         ref.advance(chunk); test.advance(chunk)
-        worst_all = max(worst_all, float(np.abs(ref.get_data("Segment.voltage") -
-                                                test.get_data("Segment.voltage")).max()))
+        err = float(np.abs(ref.get_data("Segment.voltage") - test.get_data("Segment.voltage")).max())
+        worst_all = max(worst_all, err)
+        if (k * chunk) % period == 0:
+            by_period.append(err)
+        else:
+            by_period[-1] = max(by_period[-1], err)
     log(f"accuracy run of {steps} steps in {time.perf_counter() - t0:.1f} s")
     soma_ref = np.array([p.get_data() for p in probes[0]])
     soma_test = np.array([p.get_data() for p in probes[1]])
+    soma_err = np.abs(soma_ref - soma_test)
     sp_ref = ref.get_data("Neuron.spike_count"); sp_test = test.get_data("Neuron.spike_count")
     n = ref._n
     ref.close(); test.close()
-    return {"max_err_mV": max(worst_all, float(np.abs(soma_ref - soma_test).max())),
-            "max_err_soma_every_step_mV": float(np.abs(soma_ref - soma_test).max()),
+    return {"max_err_mV": max(worst_all, float(soma_err.max())),
+            "max_err_soma_every_step_mV": float(soma_err.max()),
+            "max_err_soma_per_neuron_mV": [float(x) for x in soma_err.max(axis=1)],
             "max_err_all_segments_every_50_steps_mV": worst_all,
+            "max_err_all_segments_per_100ms_mV": by_period,
             "spikes_equal": bool(np.array_equal(sp_ref, sp_test)), "spikes_total": int(sp_ref.sum()),
             "steps": steps,
             "against": f"FP64 GPU (wide path), propagator pruned at {ref_tol:g} (charge-conserving)",
-            "sample": f"first {len(trees)} neurons of the batch ({n} segments)"}
+            "sample": f"{label} ({len(trees)} neurons of {min(len(t) for t in trees)}-{max(len(t) for t in trees)} "
+                      f"segments, {n} segments)"}
+
+
+def epsilon_gap(trees, currents, device, steps, ref_tol):
+    """How far the accuracy reference (FP64, pruned at ref_tol, charge-conserving) is from
+    the reference's own pruning at machine epsilon, on neurons of at most 2,000 segments."""
+    from neuwon_gb300.morphology import EPSILON
+    from neuwon_gb300.workloads import build_model
+    models = []
+    for tol, conserve in ((EPSILON, False), (ref_tol, True)):
+        m, _ = build_model(trees, currents, precision="f64", tolerance=tol, conserve=conserve, device=device,
+                           path="wide")
+        m._sync()
+        models.append(m)
+    worst, chunk = 0.0, 50
+    for _ in range(steps // chunk):
+        for m in models:
+            m.advance(chunk)
+        worst = max(worst, float(np.abs(models[0].get_data("Segment.voltage") -
+                                        models[1].get_data("Segment.voltage")).max()))
+    spikes = [int(m.get_data("Neuron.spike_count").sum()) for m in models]
+    out = {"max_dV_mV": worst, "steps": steps, "spikes": spikes,
+           "entries_per_row": [m.propagator_nnz / m._n for m in models],
+           "sample": f"{len(trees)} neurons of the batch of <= 2,000 segments ({models[0]._n} segments)",
+           "compared": f"FP64 at machine epsilon (the reference's pruning) vs FP64 at {ref_tol:g} charge-conserving"}
+    for m in models:
+        m.close()
+    return out
 
 
 def cpu_baseline_config1(device, steps=1000):
@@ -314,30 +395,29 @@ def plain_timing(trees, currents, tol, device, steps=10):
                       "32 threads/block, FP64 CSR, same propagator tolerance"}
 
 
-def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
-    """Config 4 shape: 256 HH neurons of 2,000 segments, dt 0.025 ms, FP32, targets = FP64
-    soma traces of the same neurons with densities drawn +-30 % around the defaults;
-    gradients of the soma MSE w.r.t. per-segment gNa/gK/gL and Ra (checkpoint every 100)."""
-    import torch
+def adjoint_build(trees, precision, device, ra=100.0, amps=None):
+    """The differentiation configuration's model: HH on every segment of the given
+    trees, dt 0.025 ms, a constant soma clamp per neuron (0.3 nA unless amps gives
+    one per tree), propagator pruned at 1e-8 (charge-conserving)."""
     from neuwon_gb300 import HH, RxD_Model
-    from neuwon_gb300.adjoint import _backward, _forward
-    from neuwon_gb300.morphology import random_tree
     from neuwon_gb300.workloads import HH_PARAMS
-    trees = [random_tree(size, seed=5000 + k) for k in range(neurons)]
-    rng = np.random.default_rng(4)
+    m = RxD_Model(time_step=0.025, temperature=6.3, precision=precision, device=device,
+                  propagator_tolerance=1e-8, propagator_conserve=True, cytoplasmic_resistance=ra,
+                  mechanisms=[HH.configure(**HH_PARAMS)])
+    ns = [m.add_tree(t) for t in trees]
+    m.insert_everywhere("hh")
+    for k, nr in enumerate(ns):
+        nr.root.inject_current(0.3 if amps is None or amps[k] is None else amps[k], 1e9)
+    m._sync()
+    return m
 
-    def build(precision):
-        m = RxD_Model(time_step=0.025, temperature=6.3, precision=precision, device=device,
-                      propagator_tolerance=1e-8, propagator_conserve=True,
-                      mechanisms=[HH.configure(**HH_PARAMS)])
-        ns = [m.add_tree(t) for t in trees]
-        m.insert_everywhere("hh")
-        for nr in ns:
-            nr.root.inject_current(0.3, 1e9)
-        m._sync()
-        return m
-    k = neurons * size
-    m64 = build("f64")
+
+def adjoint_target(trees, steps, device, seed=4):
+    """FP64 soma traces of the same neurons with densities drawn +-30 % around the defaults."""
+    from neuwon_gb300.workloads import HH_PARAMS
+    rng = np.random.default_rng(seed)
+    k = sum(len(t) for t in trees)
+    m64 = adjoint_build(trees, "f64", device)
     m64.set_hh_densities(*(rng.uniform(0.7, 1.3, k) * HH_PARAMS[g] for g in ("gnabar", "gkbar", "glbar")))
     m64.reset_state()
     roots = np.array(m64._neuron_root, dtype=np.int64)
@@ -347,7 +427,70 @@ def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
     s_out = ctypes.c_int64()
     m64._ctx.call("nw_probes_read", _lib_ptr(target), 1, steps, ctypes.byref(s_out))
     m64.close()
-    m = build("f32")
+    return target
+
+
+def diff_check(args, device):
+    """The differentiation configuration as specified: 256 HH neurons of 2,000 segments,
+    dt 0.025 ms, --diff-steps steps (8,000 = 200 ms), checkpoint every 100; FP32 adjoint
+    gradients (and the FP64 adjoint) against FP64 central differences (h = 1e-4 relative)
+    on 31 random per-segment densities (gNa / gK / gL) and Ra, relative error per parameter."""
+    from neuwon_gb300.adjoint import central_differences, loss_and_gradients
+    from neuwon_gb300.morphology import random_tree
+    steps, neurons, size = args.diff_steps, args.diff_neurons, 2000
+    trees = [random_tree(size, seed=5000 + k) for k in range(neurons)]
+    t0 = time.perf_counter()
+    target = adjoint_target(trees, steps, device)
+    log(f"diff check: target in {time.perf_counter() - t0:.1f} s")
+    rng = np.random.default_rng(11)
+    kinds = rng.choice(["gna", "gk", "gl"], 31)
+    params = [(str(kd), int(rng.integers(neurons)), int(rng.integers(size))) for kd in kinds]
+    params[0] = ("gna", params[0][1], 0)                      # a soma
+    params.append(("ra",))
+    res = {}
+    for precision in ("f32", "f64"):
+        t0 = time.perf_counter()
+        m = adjoint_build(trees, precision, device)
+        loss, gna, gk, gl, gra = loss_and_gradients(m, steps, target, checkpoint_every=100)
+        m.close()
+        g = {"gna": gna, "gk": gk, "gl": gl}
+        res[precision] = [gra if p[0] == "ra" else float(g[p[0]][p[1] * size + p[2]]) for p in params]
+        res[precision + "_loss"] = loss
+        log(f"diff check: {precision} adjoint in {time.perf_counter() - t0:.1f} s, loss {loss}")
+    t0 = time.perf_counter()
+    fd = central_differences(lambda ts, prec, ra, amps: adjoint_build(ts, prec, device, ra, amps),
+                             trees, steps, target, params)
+    log(f"diff check: central differences in {time.perf_counter() - t0:.1f} s")
+    rel = lambda a, b: abs(a - b) / max(abs(b), 1e-300)
+    rows = [{"param": (p[0] if p[0] == "ra" else f"{p[0]}[neuron {p[1]}, segment {p[2]}]"), "fd_f64": f,
+             "adjoint_f32": a32, "adjoint_f64": a64, "rel_err_f32": rel(a32, f), "rel_err_f64": rel(a64, f)}
+            for p, f, a32, a64 in zip(params, fd, res["f32"], res["f64"])]
+    # Parameters whose derivative is below 1e-3 of the largest one are reported but
+    # not in the maxima: their relative error measures cancellation in the differences.
+    big = max(abs(r["fd_f64"]) for r in rows)
+    sig = [r for r in rows if abs(r["fd_f64"]) >= 1e-3 * big]
+    out = {"metric": "adjoint check: FP32 / FP64 adjoint gradients vs FP64 central differences",
+           "config": {"workload": f"{neurons} HH neurons x {size} segments, dt 0.025 ms, {steps} steps, checkpoint "
+                                  "every 100, propagator 1e-8 (charge-conserving), targets from FP64 runs with "
+                                  "densities +-30 %", "parameters": len(params), "h_rel": 1e-4},
+           "loss_f32": res["f32_loss"], "loss_f64": res["f64_loss"],
+           "max_rel_err_f32": max(r["rel_err_f32"] for r in sig), "max_rel_err_f64": max(r["rel_err_f64"] for r in sig),
+           "median_rel_err_f32": float(np.median([r["rel_err_f32"] for r in sig])),
+           "parameters_in_maxima": len(sig), "rows": rows}
+    print(json.dumps(out), flush=True)
+
+
+def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
+    """Config 4 shape: 256 HH neurons of 2,000 segments, dt 0.025 ms, FP32, targets = FP64
+    soma traces of the same neurons with densities drawn +-30 % around the defaults;
+    gradients of the soma MSE w.r.t. per-segment gNa/gK/gL and Ra (checkpoint every 100)."""
+    import torch
+    from neuwon_gb300.adjoint import _backward, _forward
+    from neuwon_gb300.morphology import random_tree
+    trees = [random_tree(size, seed=5000 + k) for k in range(neurons)]
+    k = neurons * size
+    target = adjoint_target(trees, steps, device)
+    m = adjoint_build(trees, "f32", device)
     m.reset_state()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -479,8 +622,9 @@ def main():
     ap.add_argument("--ref-tol", type=float, default=1e-10,
                     help="pruning of the FP64 accuracy reference (machine epsilon makes rows dense)")
     ap.add_argument("--size-range", default="500,20000", help="neuron size range (segments)")
-    ap.add_argument("--acc-neurons", type=int, default=64)
-    ap.add_argument("--acc-steps", type=int, default=2000)
+    ap.add_argument("--acc-neurons", type=int, default=32,
+                    help="accuracy sample: the batch's largest half and its first other half")
+    ap.add_argument("--acc-steps", type=int, default=10000, help="accuracy run (10,000 steps = the full 1 s)")
     ap.add_argument("--fusion", type=int, default=50, help="steps fused per kernel launch (without --autotune)")
     ap.add_argument("--autotune", type=int, default=10,
                     help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
@@ -501,6 +645,10 @@ def main():
     ap.add_argument("--study-segments", type=int, default=1_000_000)
     ap.add_argument("--study-steps", type=int, default=20000)
     ap.add_argument("--study-current", type=float, default=10.0, help="soma clamp of the precision study (nA)")
+    ap.add_argument("--diff-check", action="store_true",
+                    help="differentiation configuration: FP32/FP64 adjoint vs FP64 central differences (own JSON line)")
+    ap.add_argument("--diff-steps", type=int, default=8000)
+    ap.add_argument("--diff-neurons", type=int, default=256)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -515,6 +663,12 @@ def main():
         torch.cuda.set_device(local)
         if rank == 0:
             precision_study(args, local)
+        return
+    if args.diff_check:
+        import torch
+        torch.cuda.set_device(local)
+        if rank == 0:
+            diff_check(args, local)
         return
 
     from neuwon_gb300.workloads import batched_currents, batched_trees, build_model
@@ -534,10 +688,20 @@ def main():
     log(f"trees ready ({sum(len(t) for t in trees)} segments) in {time.perf_counter() - t_setup:.1f} s")
     extra = {}
     if not args.quick and rank == 0:
+        # The sample: the batch's largest neurons and its first others, half each.
         k = args.acc_neurons
-        extra["accuracy"] = accuracy(trees[:k], currents[:k], args.tol, local, args.acc_steps, args.ref_tol,
-                                     args.format, bool(args.lump))
+        sizes = np.array([len(t) for t in trees])
+        largest = [int(i) for i in np.argsort(-sizes, kind="stable")[:k // 2]]
+        pick = largest + [i for i in range(len(trees)) if i not in largest][:k - len(largest)]
+        extra["accuracy"] = accuracy([trees[i] for i in pick], [currents[i] for i in pick], args.tol, local,
+                                     args.acc_steps, args.ref_tol, args.format, bool(args.lump),
+                                     label=f"the batch's {len(largest)} largest neurons and its first "
+                                           f"{len(pick) - len(largest)} others")
         log(f"accuracy: {extra['accuracy']}")
+        small = [i for i in range(len(trees)) if sizes[i] <= 2000][:4]
+        extra["accuracy"]["reference_gap"] = epsilon_gap([trees[i] for i in small], [currents[i] for i in small],
+                                                         local, 2000, args.ref_tol)
+        log(f"epsilon gap: {extra['accuracy']['reference_gap']}")
         extra["plain_fp64"] = plain_timing(trees[:64], currents[:64], args.tol, local)
         log(f"plain: {extra['plain_fp64']}")
 
@@ -652,7 +816,7 @@ def main():
     log(f"timed: {ms / K:.3f} ms/step; e2e {e2e_s / E * 1e3:.3f} ms/step")
     cpu = None
     if not args.quick and rank == 0:
-        cpu = cpu_sample(trees, currents, args.tol, steps=100000, time_budget_s=15.0)
+        cpu = cpu_sample(trees, currents, args.tol, bool(args.lump), time_budget_s=15.0)
         cpu["config1"] = cpu_baseline_config1(local)
         log(f"config 1: {cpu['config1']}")
     spikes = model.get_data("Neuron.spike_count")
@@ -678,17 +842,23 @@ def main():
                    "threads": thr.value, "l2": "inputs larger than L2 (propagator "
                    f"{pbytes.value / 1e9:.1f} GB), no flush", "mechanisms": ["hh", "na8 (8-state Markov Na, LTI voltage table 1600 x 0.1 mV, linear)"],
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
+        # achieved / frac: the compulsory bytes of the stored layout (quads: 18 B per
+        # window of 4 column slots, no diagonal) per launch over the launch time, the
+        # bytes the kernel must move (ncu traffic is 1.00x of them); the formula of
+        # 8 B per kept entry (value + int32 column, diagonal included) is kept as
+        # achieved_alg / frac_alg: the compressed layout moves fewer bytes than it
+        # counts, so frac_alg can exceed 1.
+        "roofline": {"bound": "hbm", "achieved": achieved_fmt, "peak": peak, "unit": "GB/s",
+                     "frac": achieved_fmt / peak,
                      "traffic": (NCU_TRAFFIC_PER_SEGMENT_STEP[(args.format, args.tol, args.lump)] * n * F
                                  if n == NCU_TRAFFIC_SEGMENTS
                                  and (args.format, args.tol, args.lump) in NCU_TRAFFIC_PER_SEGMENT_STEP else None),
                      "traffic_unit": f"bytes per launch of {F} steps (ncu dram__bytes_read+write)",
-                     "algorithmic_bytes_per_launch": B_alg * n * F,
+                     "algorithmic_bytes_per_launch": B_fmt * n * F,
                      "peak_source": peak_src,
-                     "bytes_per_segment_step": B_alg,
-                     "format_bytes_per_segment_step": B_fmt,
-                     "format_achieved": achieved_fmt, "format_frac": achieved_fmt / peak,
+                     "bytes_per_segment_step": B_fmt,
+                     "achieved_alg": achieved, "frac_alg": achieved / peak,
+                     "alg_bytes_per_segment_step": B_alg, "alg_bytes_per_launch": B_alg * n * F,
                      "kernel": "batched_advance_kernel", "launch_ms_per_step": per_step_launch_ms},
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_value, "unit": "segment-steps/s", "steps": E,

@@ -81,7 +81,8 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
  *   Segment.voltage, Segment.integral_voltage, Segment.capacitance,
  *   Segment.axial_resistance, Segment.nonspecific_current,
  *   hh.m, hh.h, hh.n, hh.gna_coef, hh.gk_coef, hh.gl_coef (instance order as registered),
- *   kinetic.state (num_instances * S values, [instance][state], registration order),
+ *   kinetic.<q>.state (kinetic mechanism q: num_instances * S values,
+ *   [instance][state], registration order; "kinetic.state" is mechanism 0),
  *   Neuron.AP_detected, Neuron.spike_count.
  * Values are converted between dtype and the context precision. */
 int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int64_t count);
@@ -127,17 +128,46 @@ int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
                    const double* gna_coef, const double* gk_coef, const double* gl_coef,
                    double ena, double ek, double el, double v_init);
 
-/* Registers the instances of one linear kinetic scheme solved by exact integration
- * with a voltage table (lti_sim: neuwon/rxd/lti_sim/lti_model.py:5-65, approx.py:159-174,
- * codegen.py:29-106; NMODL "SOLVE ... METHOD sparse", nmodl/__init__.py:298-306).
- *   num_states S (1..16), open_states: indices whose sum is the open probability;
+/* Electric species with a constant reversal potential: replaces the accumulators of
+ * _SpeciesType (neuwon/rxd/species.py:85-142, 155-160), whose per-segment
+ * {name}_conductance sums feed the segment's total conductance and
+ * conductance-weighted driving voltage with the species' reversal potential.
+ * Species are numbered 0..count-1 in the order given; kinetic mechanisms name the
+ * species their conductance feeds (nw_kinetic_add).  Calling it again replaces the
+ * reversal potentials (mechanisms already registered take the new values). */
+int nw_species_set(nw_ctx* ctx, int32_t count, const double* reversal_potential_mV);
+
+/* A species' {name}_conductance accumulator (species.py:129-133) as the last mechanism
+ * phase leaves it: per segment (device order, n_seg values, S), the summed
+ * conductance of the kinetic mechanisms that feed the species. */
+int nw_species_conductance(nw_ctx* ctx, int32_t species, double* conductance_out);
+
+/* Appends one linear kinetic mechanism solved by exact integration with a voltage
+ * table (lti_sim: neuwon/rxd/lti_sim/lti_model.py:5-65, approx.py:159-174,
+ * codegen.py:29-106; NMODL "SOLVE ... METHOD sparse", nmodl/__init__.py:298-306), one
+ * of the mechanisms _advance_mechanisms advances (neuwon/rxd/rxd_model.py:115-123);
+ * a model holds up to 8, advanced and summed per segment in the order added.
+ *   num_states S (1..16), open_states: 1..8 indices whose sum is the open probability;
  *   g_coef[i]: instance i's maximal conductance in siemens (gbar * 1e-8 * magnitude);
- *   erev: reversal potential of its nonspecific conductance (mV);
+ *   species: the electric species (nw_species_set) whose conductance accumulator it
+ *   writes (USEION, nmodl/__init__.py:168-208), or -1 for a nonspecific conductance
+ *   with reversal potential erev (mV; ignored when species >= 0);
  *   table: [num_buckets][S (col)][S (row)][num_terms] polynomial coefficients, the
  *   layout of codegen.py:35-37; the voltage v falls in bucket trunc((v - vmin) * bucket_frq)
  *   clamped as in codegen.py:43-59;
  *   conserve_sum: states are rescaled to this sum after each step (<= 0: no CONSERVE);
- *   init_state: S initial occupancies for every instance. */
+ *   init_state: S initial occupancies for every instance.
+ * *mechanism_out (may be NULL) receives the mechanism's index q: its states read and
+ * write as "kinetic.<q>.state", its table is nw_lti_table_build target 16 + q. */
+int nw_kinetic_add(nw_ctx* ctx, int64_t num_instances, const int64_t* segment, const double* g_coef,
+                   int num_states, int num_open, const int32_t* open_states, double erev, int32_t species,
+                   const double* table, int num_buckets, int num_terms, double vmin, double bucket_frq,
+                   double conserve_sum, const double* init_state, int32_t* mechanism_out);
+
+/* Removes every kinetic mechanism (before registering a new set). */
+int nw_kinetic_clear(nw_ctx* ctx);
+
+/* nw_kinetic_clear followed by nw_kinetic_add of one nonspecific mechanism (index 0). */
 int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
                         const double* g_coef, int num_states, int num_open, const int32_t* open_states,
                         double erev, const double* table, int num_buckets, int num_terms,
@@ -151,9 +181,9 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
  * S <= 16; FP64 scaling and squaring), then per bucket the polynomial fit
  * table[b][col][row][t] = sum_s fit[t][s] * P[b, s][row][col] (fit = the
  * least-squares pseudo-inverse of the in-bucket sample locations, the same for
- * every bucket).  target 1 installs the table as the kinetic mechanism's, 2 as the
- * calcium pump's (shapes must match what is registered), 0 only returns it;
- * table_out (may be NULL) receives it in FP64. */
+ * every bucket).  target 16 + q installs the table as kinetic mechanism q's (1 is
+ * the same as 16: mechanism 0), 2 as the calcium pump's (shapes must match what is
+ * registered), 0 only returns it; table_out (may be NULL) receives it in FP64. */
 int nw_lti_table_build(nw_ctx* ctx, int32_t S, int32_t num_buckets, int32_t samples_per_bucket,
                        int32_t num_terms, const double* rates, const double* fit, double dt,
                        int32_t target, double* table_out);
@@ -300,6 +330,11 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * (< N), the spike ring covers all N neurons with this model's neuron j at o + j, and
  * its length is at least R steps (a common value for all ranks); the ranks sum their
  * rings (own neurons only) after every epoch of at most the shortest delay.
+ * "duplicates" (default 0): several instances of one mechanism on one segment all
+ * count; 1 = the reference's behaviour for nonspecific conductances (HH and kinetic
+ * mechanisms without a species), whose fancy-index "+=" keeps only the last
+ * instance's value (neuwon/rxd/species.py:256-260): only the last-registered
+ * instance of each segment counts (all of them still advance).
  * "propagator_lump" (default 0), taken by the next nw_propagator_build / nw_calcium_set:
  * an entry below the tolerance is added to the nearest kept entry on the tree path
  * from its segment towards the row's segment instead of being dropped (row sums are

@@ -75,3 +75,65 @@ def trace_loss(model, gnabar, gkbar, glbar, ra, steps, target, checkpoint_every=
     """Differentiable loss; see the module docstring.  gnabar/gkbar/glbar: tensors with
     one density per HH instance (S/cm2); ra: scalar tensor (ohm cm)."""
     return _TraceLoss.apply(gnabar, gkbar, glbar, ra, model, int(steps), target, int(checkpoint_every))
+
+
+def central_differences(build, trees, steps, target, params, ra=100.0, h_rel=1e-4, amps=None):
+    """FP64 central differences of the trace loss for a list of parameters, without
+    running the whole model per parameter: a per-segment density touches one neuron
+    only, and the loss is a sum over neurons, so each (neuron, +h / -h) pair runs as
+    two copies of that neuron inside one FP64 model, and the difference of their
+    loss terms is the whole loss's difference.  Ra touches every neuron: two FP64
+    runs of the whole model.
+
+    build(trees, precision, ra, amps) -> RxD_Model with one HH instance per segment
+    (registration order = segment order) and a soma clamp per neuron;
+    params: list of ("gna" | "gk" | "gl", neuron, local segment) or ("ra",);
+    target: (steps, neurons) soma voltages.  Returns the derivatives (S/cm2 or
+    ohm cm units, matching loss_and_gradients) in the order of params."""
+    from .workloads import HH_PARAMS
+    n_neurons = len(trees)
+    amps = list(amps) if amps is not None else [None] * n_neurons
+    base = {"gna": HH_PARAMS["gnabar"], "gk": HH_PARAMS["gkbar"], "gl": HH_PARAMS["glbar"]}
+    out = [None] * len(params)
+    dens_idx = [k for k, p in enumerate(params) if p[0] != "ra"]
+    if dens_idx:
+        copies, cols, dens = [], [], []
+        for k in dens_idx:
+            kind, j, local = params[k]
+            for sign in (1.0, -1.0):
+                copies.append(trees[j])
+                cols.append(j)
+                d = {g: np.full(len(trees[j]), v) for g, v in base.items()}
+                d[kind][local] += sign * h_rel * base[kind]
+                dens.append(d)
+        m = build(copies, "f64", ra, [amps[j] for j in cols])
+        m.set_hh_densities(*(np.concatenate([d[g] for d in dens]) for g in ("gna", "gk", "gl")))
+        m.reset_state()
+        roots = np.asarray(m._neuron_root, dtype=np.int64)
+        m._ctx.call("nw_probes_set", len(roots), _lib.ptr(roots), int(steps))
+        m._ctx.advance(int(steps))
+        v = np.empty((steps, len(roots)))
+        got = ctypes.c_int64()
+        m._ctx.call("nw_probes_read", _lib.ptr(v), 1, int(steps), ctypes.byref(got))
+        m.close()
+        terms = ((v - np.asarray(target)[:, cols]) ** 2).sum(axis=0) / (steps * n_neurons)
+        for q, k in enumerate(dens_idx):
+            h = h_rel * base[params[k][0]]
+            out[k] = (terms[2 * q] - terms[2 * q + 1]) / (2 * h)
+    for k, p in enumerate(params):
+        if p[0] != "ra":
+            continue
+        losses = []
+        for sign in (1.0, -1.0):
+            m = build(trees, "f64", ra + sign * h_rel * ra, amps)
+            m.reset_state()
+            roots = np.asarray(m._neuron_root, dtype=np.int64)
+            m._ctx.call("nw_probes_set", len(roots), _lib.ptr(roots), int(steps))
+            m._ctx.advance(int(steps))
+            v = np.empty((steps, len(roots)))
+            got = ctypes.c_int64()
+            m._ctx.call("nw_probes_read", _lib.ptr(v), 1, int(steps), ctypes.byref(got))
+            m.close()
+            losses.append(((v - np.asarray(target)) ** 2).mean())
+        out[k] = (losses[0] - losses[1]) / (2 * h_rel * ra)
+    return out

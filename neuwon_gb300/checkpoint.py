@@ -115,7 +115,7 @@ def load_sqlite(model, filename):
         if issubclass(cls, Kinetic):
             S = len(cls.scheme_factory().states)
             s = np.stack([_column(cur, name, f"s{k}") for k in range(S)], axis=1)
-            ctx.set_data("kinetic.state", np.ascontiguousarray(s.ravel()))
+            ctx.set_data(m.kinetic_state_name(name), np.ascontiguousarray(s.ravel()))
         else:
             for a in ("m", "h", "n"):
                 ctx.set_data(f"hh.{a}", _column(cur, name, a))

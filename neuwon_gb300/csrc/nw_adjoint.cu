@@ -479,7 +479,7 @@ static int adjoint_check(nw_ctx* ctx) {
     if (!ctx->have_cap || !ctx->have_res) return fail(ctx, NW_ERR_STATE, "adjoint: capacitance/resistance not set");
     if (ctx->hh.m == 0 || !ctx->hh.identity)
         return fail(ctx, NW_ERR_STATE, "adjoint: needs exactly one HH instance on every segment");
-    if (ctx->kin.m != 0) return fail(ctx, NW_ERR_STATE, "adjoint: kinetic mechanisms are not differentiated");
+    if (kinetic_instances(ctx) != 0) return fail(ctx, NW_ERR_STATE, "adjoint: kinetic mechanisms are not differentiated");
     if (ctx->syn.n != 0) return fail(ctx, NW_ERR_STATE, "adjoint: synapses are not differentiated");
     if (ctx->ca.on) return fail(ctx, NW_ERR_STATE, "adjoint: calcium is not differentiated");
     if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "adjoint: a neuron has more than 65,535 segments");

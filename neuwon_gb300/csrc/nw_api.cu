@@ -178,6 +178,25 @@ static void free_kin(KineticState& k) {
     k = KineticState();
 }
 
+static void free_kinetics(nw_ctx* ctx) {
+    for (int q = 0; q < kMaxKinetic; ++q) free_kin(ctx->kin[q]);
+    ctx->n_kin = 0;
+}
+
+// "kinetic.state" names mechanism 0; "kinetic.<q>.state" mechanism q.  Returns
+// the index, -1 when the name is not a kinetic state name, -2 when q is out of range.
+static int kinetic_state_name(const nw_ctx* ctx, const std::string& nm) {
+    if (nm == "kinetic.state") return ctx->n_kin > 0 ? 0 : -2;
+    const std::string pre = "kinetic.", post = ".state";
+    if (nm.size() <= pre.size() + post.size() || nm.compare(0, pre.size(), pre) != 0 ||
+        nm.compare(nm.size() - post.size(), post.size(), post) != 0)
+        return -1;
+    const std::string mid = nm.substr(pre.size(), nm.size() - pre.size() - post.size());
+    if (mid.empty() || mid.size() > 3 || mid.find_first_not_of("0123456789") != std::string::npos) return -1;
+    const int q = std::stoi(mid);
+    return q < ctx->n_kin ? q : -2;
+}
+
 void free_syn(SynState& y) {
     for (DevBuf* b : {&y.seg, &y.pre, &y.delay, &y.wa, &y.wn, &y.oa, &y.on, &y.od, &y.pulse_end, &y.events,
                       &y.last_event, &y.mats, &y.seg_ptr, &y.neuron_ptr, &y.ring})
@@ -253,7 +272,7 @@ int nw_ctx_destroy(nw_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     graphs_clear(ctx);
     free_hh(ctx->hh);
-    free_kin(ctx->kin);
+    free_kinetics(ctx);
     free_syn(ctx->syn);
     free_calcium(ctx->ca);
     free_adj(ctx->adj);
@@ -339,7 +358,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     cudaStreamSynchronize(ctx->stream);
     graphs_clear(ctx);
     free_hh(ctx->hh);
-    free_kin(ctx->kin);
+    free_kinetics(ctx);
     free_syn(ctx->syn);
     free_calcium(ctx->ca);
     free_adj(ctx->adj);
@@ -434,8 +453,9 @@ int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int6
                     nm == "hh.gna_coef" ? hh.cna : nm == "hh.gk_coef" ? hh.ck : hh.cl;
         return upload_convert(ctx, b.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
     }
-    if (nm == "kinetic.state") {
-        const KineticState& K = ctx->kin;
+    if (const int q = kinetic_state_name(ctx, nm); q != -1) {
+        if (q < 0) return fail(ctx, NW_ERR_ARG, nm + ": no such kinetic mechanism");
+        const KineticState& K = ctx->kin[q];
         NW_CHECK(need(K.m * K.S));
         std::vector<double> sorted((size_t)K.S * K.m);
         for (int64_t u = 0; u < K.m; ++u)
@@ -507,8 +527,9 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
         for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[ctx->hh.user_to_sorted[i]]);
         return NW_OK;
     }
-    if (nm == "kinetic.state") {
-        const KineticState& K = ctx->kin;
+    if (const int q = kinetic_state_name(ctx, nm); q != -1) {
+        if (q < 0) return fail(ctx, NW_ERR_ARG, nm + ": no such kinetic mechanism");
+        const KineticState& K = ctx->kin[q];
         NW_CHECK(need(K.m * K.S));
         std::vector<double> sorted((size_t)K.S * K.m);
         NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, K.state.ptr, rd, count));
@@ -728,31 +749,45 @@ int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
     return NW_OK;
 }
 
-int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
-                        const double* g_coef, int num_states, int num_open, const int32_t* open_states,
-                        double erev, const double* table, int num_buckets, int num_terms,
-                        double vmin, double bucket_frq, double conserve_sum, const double* init_state) {
+}  // extern "C"
+
+namespace nw {
+
+// Appends one kinetic mechanism (see nw_kinetic_add) and stores its index in *id_out.
+static int kinetic_add(nw_ctx* ctx, const char* who, int64_t num_instances, const int64_t* segment,
+                       const double* g_coef, int num_states, int num_open, const int32_t* open_states,
+                       double erev, int32_t species, const double* table, int num_buckets, int num_terms,
+                       double vmin, double bucket_frq, double conserve_sum, const double* init_state,
+                       int32_t* id_out) {
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
-    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_kinetic_register before nw_model_init");
+    const std::string w(who);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, w + " before nw_model_init");
     const int S = num_states, T = num_terms;
-    if (S < 1 || S > 16 || T < 1 || T > 4 || num_buckets < 1 || num_open < 1 || num_open > 4 ||
+    if (S < 1 || S > 16 || T < 1 || T > 4 || num_buckets < 1 || num_open < 1 || num_open > kMaxOpen ||
         !open_states || !table || !init_state || !(bucket_frq > 0))
-        return fail(ctx, NW_ERR_ARG, "nw_kinetic_register: need 1<=S<=16, 1<=terms<=4, 1..4 open states, "
-                                     "a table and an initial state");
+        return fail(ctx, NW_ERR_ARG, w + ": need 1<=S<=16, 1<=terms<=4, 1.." + std::to_string(kMaxOpen) +
+                                     " open states, a table and an initial state");
     for (int k = 0; k < num_open; ++k)
         if (open_states[k] < 0 || open_states[k] >= S)
-            return fail(ctx, NW_ERR_ARG, "nw_kinetic_register: open state index out of range");
+            return fail(ctx, NW_ERR_ARG, w + ": open state index out of range");
+    if (species >= (int32_t)ctx->species_erev.size() || species < -1)
+        return fail(ctx, NW_ERR_ARG, w + ": species " + std::to_string(species) + " was not declared (nw_species_set)");
+    if (ctx->n_kin >= kMaxKinetic)
+        return fail(ctx, NW_ERR_LIMIT, w + ": at most " + std::to_string(kMaxKinetic) + " kinetic mechanisms");
     const int64_t m = num_instances;
-    if (m < 0 || (m && (!segment || !g_coef))) return fail(ctx, NW_ERR_ARG, "nw_kinetic_register: null arrays");
+    if (m < 0 || (m && (!segment || !g_coef))) return fail(ctx, NW_ERR_ARG, w + ": null arrays");
     InstanceLayout L;
-    NW_CHECK(layout_instances(ctx, m, segment, "nw_kinetic_register", L));
-    KineticState& K = ctx->kin;
+    NW_CHECK(layout_instances(ctx, m, segment, who, L));
+    const int q = ctx->n_kin;
+    KineticState& K = ctx->kin[q];
     free_kin(K);
     K.m = m; K.S = S; K.T = T; K.nb = num_buckets; K.n_open = num_open;
     for (int k = 0; k < num_open; ++k) K.open[k] = open_states[k];
     K.identity = L.identity;
-    K.erev = erev; K.vmin = vmin; K.frq = bucket_frq; K.conserve = conserve_sum;
+    K.species = species;
+    K.erev = species >= 0 ? ctx->species_erev[species] : erev;
+    K.vmin = vmin; K.frq = bucket_frq; K.conserve = conserve_sum;
     K.user_to_sorted = L.user_to_sorted;
     K.h_neuron_ptr = L.nptr;
     size_t rs = (size_t)ctx->precision;
@@ -769,8 +804,66 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
     NW_CHECK(upload_convert(ctx, K.gcoef.ptr, rd, g.data(), NW_DTYPE_F64, m));
     NW_CHECK(upload_convert(ctx, K.state.ptr, rd, st.data(), NW_DTYPE_F64, (int64_t)S * m));
     NW_CHECK(upload_convert(ctx, K.table.ptr, rd, table, NW_DTYPE_F64, tsize));
+    ctx->n_kin = q + 1;
+    ctx->g_valid = false;
+    if (id_out) *id_out = q;
+    return NW_OK;
+}
+
+}  // namespace nw
+
+extern "C" {
+
+int nw_species_set(nw_ctx* ctx, int32_t count, const double* reversal_potential_mV) {
+    if (!ctx || count < 0 || (count && !reversal_potential_mV)) return NW_ERR_ARG;
+    for (int32_t s = 0; s < count; ++s)
+        if (!std::isfinite(reversal_potential_mV[s]))
+            return fail(ctx, NW_ERR_ARG, "nw_species_set: reversal potentials must be finite");
+    for (int q = 0; q < ctx->n_kin; ++q)
+        if (ctx->kin[q].species >= count)
+            return fail(ctx, NW_ERR_STATE, "nw_species_set: a registered kinetic mechanism feeds species " +
+                                           std::to_string(ctx->kin[q].species));
+    ctx->species_erev.assign(reversal_potential_mV, reversal_potential_mV + count);
+    for (int q = 0; q < ctx->n_kin; ++q)
+        if (ctx->kin[q].species >= 0) ctx->kin[q].erev = ctx->species_erev[ctx->kin[q].species];
+    return NW_OK;
+}
+
+int nw_species_conductance(nw_ctx* ctx, int32_t species, double* conductance_out) {
+    if (!ctx || !conductance_out) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_species_conductance before nw_model_init");
+    if (species < 0 || species >= (int32_t)ctx->species_erev.size())
+        return fail(ctx, NW_ERR_ARG, "nw_species_conductance: no such species");
+    return species_conductance(ctx, species, conductance_out);
+}
+
+int nw_kinetic_clear(nw_ctx* ctx) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    free_kinetics(ctx);
     ctx->g_valid = false;
     return NW_OK;
+}
+
+int nw_kinetic_add(nw_ctx* ctx, int64_t num_instances, const int64_t* segment, const double* g_coef,
+                   int num_states, int num_open, const int32_t* open_states, double erev, int32_t species,
+                   const double* table, int num_buckets, int num_terms, double vmin, double bucket_frq,
+                   double conserve_sum, const double* init_state, int32_t* mechanism_out) {
+    return kinetic_add(ctx, "nw_kinetic_add", num_instances, segment, g_coef, num_states, num_open, open_states,
+                       erev, species, table, num_buckets, num_terms, vmin, bucket_frq, conserve_sum, init_state,
+                       mechanism_out);
+}
+
+int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
+                        const double* g_coef, int num_states, int num_open, const int32_t* open_states,
+                        double erev, const double* table, int num_buckets, int num_terms,
+                        double vmin, double bucket_frq, double conserve_sum, const double* init_state) {
+    NW_CHECK(nw_kinetic_clear(ctx));
+    return kinetic_add(ctx, "nw_kinetic_register", num_instances, segment, g_coef, num_states, num_open,
+                       open_states, erev, -1, table, num_buckets, num_terms, vmin, bucket_frq, conserve_sum,
+                       init_state, nullptr);
 }
 
 int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron, const int64_t* post_segment,
@@ -1088,6 +1181,14 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         ctx->pair_shared_limit = (int)value;
         return NW_OK;
     }
+    if (nm == "duplicates") {
+        // 0: every instance on a segment counts; 1: the reference's fancy-index "+="
+        // for nonspecific conductances (only the last-registered instance of a
+        // segment counts, per mechanism kind).
+        if (value < 0 || value > 1) return fail(ctx, NW_ERR_ARG, "duplicates must be 0 or 1");
+        ctx->duplicates = (int)value;
+        return NW_OK;
+    }
     if (nm == "propagator_lump") {
         // Taken by the next propagator build: a value below the tolerance is added to
         // the nearest kept entry on the tree path towards the row's segment instead
@@ -1127,7 +1228,7 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         if (value < 0) return fail(ctx, NW_ERR_ARG, "set_steps: negative step");
         ctx->steps = value;
         ctx->input_ticks = 2 * value;
-        ctx->g_valid = value > 0 && (ctx->hh.m > 0 || ctx->kin.m > 0);
+        ctx->g_valid = value > 0 && has_channel_mechanisms(ctx);
         ctx->probe_len = 0;
         return NW_OK;
     }
@@ -1156,6 +1257,8 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "cuda_graph") { *value = ctx->use_graph ? 1 : 0; return NW_OK; }
     if (nm == "propagator_format") { *value = ctx->prop_format; return NW_OK; }
     if (nm == "propagator_lump") { *value = ctx->prop_lump ? 1 : 0; return NW_OK; }
+    if (nm == "duplicates") { *value = ctx->duplicates; return NW_OK; }
+    if (nm == "kinetic_mechanisms") { *value = ctx->n_kin; return NW_OK; }
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "quads") { *value = ctx->nq; return NW_OK; }
     if (nm == "fusion_depth") { *value = ctx->fusion; return NW_OK; }

@@ -64,11 +64,17 @@ struct HHState {
     std::vector<int64_t> h_neuron_ptr;    // host copy of neuron_ptr
 };
 
+// Most kinetic mechanisms (kinds, each with its own scheme, table and instances)
+// and most open states per scheme a model may have.
+constexpr int kMaxKinetic = 8;
+constexpr int kMaxOpen = 8;
+
 struct KineticState {
     int64_t m = 0;
     int S = 0, T = 0, nb = 0, n_open = 0;
-    int open[4] = {0, 0, 0, 0};
+    int open[kMaxOpen] = {0, 0, 0, 0, 0, 0, 0, 0};
     bool identity = false;
+    int species = -1;           // electric species its conductance feeds (-1: nonspecific, own erev)
     double erev = 0, vmin = 0, frq = 0, conserve = 0;
     DevBuf seg;                 // u32 [m] segment-sorted
     DevBuf state;               // real [S][m]
@@ -196,9 +202,19 @@ struct nw_ctx {
     int prop_format = 0;                               // 0: rows, 1: pairs, 2: quads
     int pair_shared_limit = -1;                        // cap on neurons with shared-memory sums (-1: none)
 
-    // Mechanisms.
+    // Mechanisms.  Kinetic mechanisms are kept in registration order; their
+    // conductances are summed per segment in that order.
     nw::HHState hh;
-    nw::KineticState kin;
+    nw::KineticState kin[nw::kMaxKinetic];
+    int n_kin = 0;
+    // Electric species (neuwon/rxd/species.py:90-142 with a constant reversal
+    // potential): a kinetic mechanism's conductance feeds one of them or is
+    // nonspecific.
+    std::vector<double> species_erev;
+    // Duplicate instances on one segment: 0 = all summed, 1 = the reference's
+    // fancy-index "+=" for nonspecific conductances (species.py:256-260): only the
+    // last-registered instance of a segment counts.
+    int duplicates = 0;
     nw::SynState syn;
     int64_t spike_neurons = 0, spike_offset = 0;   // partition settings applied by nw_synapses_set
     int spike_ring_min = 0;
@@ -242,6 +258,20 @@ struct nw_ctx {
 
 namespace nw {
 
+// Any HH or kinetic instance: after a mechanism phase the conductances are valid.
+inline bool has_channel_mechanisms(const nw_ctx* ctx) {
+    if (ctx->hh.m > 0) return true;
+    for (int q = 0; q < ctx->n_kin; ++q)
+        if (ctx->kin[q].m > 0) return true;
+    return false;
+}
+
+inline int64_t kinetic_instances(const nw_ctx* ctx) {
+    int64_t m = 0;
+    for (int q = 0; q < ctx->n_kin; ++q) m += ctx->kin[q].m;
+    return m;
+}
+
 int fail(nw_ctx* ctx, int code, const std::string& msg);
 int cuda_fail(nw_ctx* ctx, cudaError_t e, const char* what);
 int dev_alloc(nw_ctx* ctx, DevBuf& b, size_t bytes);
@@ -265,6 +295,7 @@ int csr_to_rows(nw_ctx* ctx, const DevBuf& src_row, const DevBuf& src_col, const
 int advance_batched(nw_ctx* ctx, int k_steps);
 int advance_plain(nw_ctx* ctx, int k_steps);
 int advance_wide(nw_ctx* ctx, int k_steps);
+int species_conductance(nw_ctx* ctx, int32_t species, double* host_out);
 int ensure_wide(nw_ctx* ctx);
 int ensure_flux(nw_ctx* ctx);
 int ensure_quads(nw_ctx* ctx);

@@ -117,13 +117,17 @@ int nw_lti_table_build(nw_ctx* ctx, int32_t S, int32_t num_buckets, int32_t samp
                        const double* rates, const double* fit, double dt, int32_t target, double* table_out) {
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
+    const bool kin_target = target == 1 || (target >= 16 && target < 16 + kMaxKinetic);
     if (S < 1 || S > kLtiMaxStates || num_buckets < 1 || samples_per_bucket < 1 || num_terms < 1 ||
-        num_terms > 4 || !rates || !fit || !(dt > 0.0) || target < 0 || target > 2)
+        num_terms > 4 || !rates || !fit || !(dt > 0.0) || !(target == 0 || target == 2 || kin_target))
         return fail(ctx, NW_ERR_ARG, "nw_lti_table_build: bad arguments");
     const int64_t count = (int64_t)num_buckets * samples_per_bucket;
     const int64_t tn = (int64_t)num_buckets * S * S * num_terms;
-    if (target == 1 && (ctx->kin.m == 0 || ctx->kin.S != S || ctx->kin.nb != num_buckets || ctx->kin.T != num_terms))
-        return fail(ctx, NW_ERR_STATE, "nw_lti_table_build: the kinetic mechanism's table has another shape");
+    const int kq = target == 1 ? 0 : target - 16;
+    if (kin_target && (kq >= ctx->n_kin || ctx->kin[kq].S != S || ctx->kin[kq].nb != num_buckets ||
+                       ctx->kin[kq].T != num_terms))
+        return fail(ctx, NW_ERR_STATE, "nw_lti_table_build: no kinetic mechanism " + std::to_string(kq) +
+                                       " with a table of this shape");
     if (target == 2 && (!ctx->ca.pump || S != 3 || ctx->ca.nb != num_buckets || ctx->ca.T != num_terms))
         return fail(ctx, NW_ERR_STATE, "nw_lti_table_build: the calcium pump's table has another shape");
     DevBuf dq, dp, dw, dt_tab;
@@ -143,7 +147,7 @@ int nw_lti_table_build(nw_ctx* ctx, int32_t S, int32_t num_buckets, int32_t samp
             dp.as<double>(), dw.as<double>(), num_buckets, samples_per_bucket, S, num_terms, dt_tab.as<double>());
         if (cudaGetLastError() != cudaSuccess) { rc = fail(ctx, NW_ERR_CUDA, "nw_lti_table_build: launch failed"); break; }
         if (target) {
-            DevBuf& dst = target == 1 ? ctx->kin.table : ctx->ca.table;
+            DevBuf& dst = kin_target ? ctx->kin[kq].table : ctx->ca.table;
             std::vector<double> host(tn);
             cudaMemcpyAsync(host.data(), dt_tab.ptr, (size_t)tn * 8, cudaMemcpyDeviceToHost, ctx->stream);
             cudaError_t e = cudaStreamSynchronize(ctx->stream);

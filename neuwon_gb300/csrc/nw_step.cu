@@ -403,20 +403,17 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         const real* const rcs = a.frc_smem ? reinterpret_cast<const real*>(smem_raw + xs_bytes) : a.frc + base;
         acc_t* const sacc = reinterpret_cast<acc_t*>(smem_raw + (a.frc_smem ? 2 : 1) * xs_bytes);
         acc_t* const gacc = reinterpret_cast<acc_t*>(a.facc) + base;
-        // Mechanism instance ranges of this neuron.
-        int64_t ib = 0, ie = 0, kb = 0, ke = 0, yb = 0, ye = 0;
+        // Mechanism instance ranges of this neuron (kinetic ones per mechanism, below).
+        int64_t ib = 0, ie = 0, yb = 0, ye = 0;
         if (a.syn_on) { yb = a.syn_neuron_ptr[j]; ye = a.syn_neuron_ptr[j + 1]; }
         if (a.hh_on) {
             if (a.hh_identity) { ib = base; ie = base + n; }
             else { ib = a.hh_neuron_ptr[j]; ie = a.hh_neuron_ptr[j + 1]; }
         }
-        if (a.kin_on) {
-            if (a.kin_identity) { kb = base; ke = base + n; }
-            else { kb = a.kin_neuron_ptr[j]; ke = a.kin_neuron_ptr[j + 1]; }
-        }
         // With one instance per segment the thread that updates a segment's
         // instances is the one that gathers them next; otherwise synchronise.
-        const bool mech_sync = (a.hh_on && !a.hh_identity) || (a.kin_on && !a.kin_identity) || ye > yb;
+        bool mech_sync = (a.hh_on && !a.hh_identity) || ye > yb;
+        for (int q = 0; q < a.n_kin; ++q) mech_sync = mech_sync || !a.kin[q].identity;
         // The fused mechanism pass is compiled only into the FUSE instances, so the
         // kernels for synapses, calcium or scattered instances keep their own code.
         const bool fuse = FUSE && !BULK && a.fuse_mech;
@@ -495,10 +492,12 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     // the segment's conductance and the second half's x, in one pass.
                     const bool last1 = s == a.k_steps - 1;
                     const bool keep = s + 1 < a.k_steps;
-                    if (!a.kin_on || (a.kin_S == 8 && a.kin_T == 2)) {
+                    const bool kin_on = a.n_kin > 0;
+                    if (a.n_kin == 0 || (a.n_kin == 1 && a.kin[0].S == 8 && a.kin[0].T == 2)) {
                         // Every input of the segment is loaded before the first store, and
                         // the conductances come from registers (same helpers and order as
                         // segment_conductance, so the same bits).
+                        const KinArgs<real>& K = a.kin[0];
                         for (int li = tid; li < n; li += nthr) {
                             const int64_t i = base + li;
                             const real v = a.V[i], kGi = a.kG[i], kIi = a.kI[i];
@@ -510,10 +509,10 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                                 m = a.gm[i]; h = a.gh[i]; nn = a.gn[i];
                                 cna = a.cna[i]; ck = a.ck[i]; cl = a.cl[i];
                             }
-                            if (a.kin_on) {
+                            if (kin_on) {
 #pragma unroll
-                                for (int c = 0; c < 8; ++c) st[c] = a.kin_state[(int64_t)c * a.kin_m + i];
-                                gco = a.kin_gcoef[i];
+                                for (int c = 0; c < 8; ++c) st[c] = K.state[(int64_t)c * K.m + i];
+                                gco = K.gcoef[i];
                             }
                             real G = real(0), GE = real(0);
                             if (a.hh_on) {
@@ -522,9 +521,9 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                                 hh_conductance_add(cna, ck, cl, m, h, nn, gna, gk, gl);
                                 hh_conductance_total(a, gna, gk, gl, G, GE);
                             }
-                            if (a.kin_on) {
-                                kinetic_advance<real, 8, 2>(a, v, st);
-                                const real open = kinetic_open(a, [&](int c) {
+                            if (kin_on) {
+                                kinetic_advance<real, 8, 2>(K, v, st);
+                                const real open = kinetic_open(K, [&](int c) {
                                     real x = st[0];
 #pragma unroll
                                     for (int q = 1; q < 8; ++q) x = (c == q) ? st[q] : x;
@@ -533,12 +532,12 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                                 real gkin = real(0);
                                 gkin += gco * open;
                                 G += gkin;
-                                GE += gkin * a.kin_erev;
+                                GE += gkin * K.erev;
                             }
                             if (a.hh_on) { a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn; }
-                            if (a.kin_on) {
+                            if (kin_on) {
 #pragma unroll
-                                for (int c = 0; c < 8; ++c) a.kin_state[(int64_t)c * a.kin_m + i] = st[c];
+                                for (int c = 0; c < 8; ++c) K.state[(int64_t)c * K.m + i] = st[c];
                             }
                             if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
                             xs[li] = membrane_x_of(a, i, v, kGi, kIi, G, GE, I, last1);
@@ -552,7 +551,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                                 hh_gates(v, a.dtq10, m, h, nn);
                                 a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
                             }
-                            if (a.kin_on) kinetic_step(a, i, v);
+                            for (int q = 0; q < a.n_kin; ++q) kinetic_step(a.kin[q], i, v);
                             real G, GE;
                             segment_conductance(a, i, G, GE);
                             if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
@@ -570,9 +569,12 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                             a.gm[k] = m; a.gh[k] = h; a.gn[k] = nn;
                         }
                     }
-                    if (a.kin_on) {
+                    for (int q = 0; q < a.n_kin; ++q) {
+                        const KinArgs<real>& K = a.kin[q];
+                        const int64_t kb = K.identity ? base : K.neuron_ptr[j];
+                        const int64_t ke = K.identity ? base + n : K.neuron_ptr[j + 1];
                         for (int64_t k = kb + tid; k < ke; k += nthr)
-                            kinetic_step(a, k, a.V[a.kin_identity ? k : (int64_t)a.kin_seg[k]]);
+                            kinetic_step(K, k, a.V[K.identity ? k : (int64_t)K.seg[k]]);
                     }
                     for (int64_t k = yb + tid; k < ye; k += nthr) synapse_step(a, k, step_base + s);
                     if (mech_sync) __syncthreads();
@@ -645,10 +647,11 @@ __global__ void plain_hh_kernel(const StepArgs<real> a, int64_t ib, int64_t ie) 
 }
 
 template <typename real>
-__global__ void plain_kinetic_kernel(const StepArgs<real> a, int64_t kb, int64_t ke) {
+__global__ void plain_kinetic_kernel(const StepArgs<real> a, int q, int64_t kb, int64_t ke) {
     int64_t k = kb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= ke) return;
-    kinetic_step_generic(a, k, a.V[a.kin_identity ? k : (int64_t)a.kin_seg[k]]);
+    const KinArgs<real>& K = a.kin[q];
+    kinetic_step_generic(K, k, a.V[K.identity ? k : (int64_t)K.seg[k]]);
 }
 
 template <typename real>
@@ -922,7 +925,7 @@ static void finish_steps(nw_ctx* ctx, int k_steps) {
     ctx->input_ticks += 2 * (int64_t)k_steps;
     ctx->steps += k_steps;
     if (ctx->n_probes) ctx->probe_len += k_steps;
-    if (ctx->hh.m > 0 || ctx->kin.m > 0) ctx->g_valid = true;
+    if (has_channel_mechanisms(ctx)) ctx->g_valid = true;
 }
 
 int advance_batched(nw_ctx* ctx, int k_steps) {
@@ -956,14 +959,17 @@ static int plain_steps(nw_ctx* ctx, int k_steps) {
                         if (ie > ib)
                             plain_hh_kernel<real><<<(unsigned)((ie - ib + T - 1) / T), T, 0, ctx->stream>>>(a, ib, ie);
                     }
-                    if (ctx->kin.m > 0) {
-                        const int64_t kb = ctx->kin.h_neuron_ptr[j], ke = ctx->kin.h_neuron_ptr[j + 1];
+                    for (int q = 0; q < ctx->n_kin; ++q) {
+                        const KineticState& K = ctx->kin[q];
+                        if (K.m == 0) continue;
+                        const int64_t kb = K.h_neuron_ptr[j], ke = K.h_neuron_ptr[j + 1];
                         if (ke > kb)
-                            plain_kinetic_kernel<real><<<(unsigned)((ke - kb + T - 1) / T), T, 0, ctx->stream>>>(a, kb, ke);
+                            plain_kinetic_kernel<real><<<(unsigned)((ke - kb + T - 1) / T), T, 0, ctx->stream>>>(
+                                a, q, kb, ke);
                     }
                 }
             }
-            ctx->g_valid = ctx->g_valid || ctx->hh.m > 0 || ctx->kin.m > 0;
+            ctx->g_valid = ctx->g_valid || has_channel_mechanisms(ctx);
         }
         int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
         StepArgs<real> d = make_args<real>(ctx, 1);

@@ -74,6 +74,17 @@ __device__ __forceinline__ void hh_gates(real v, real dtq10, real& m, real& h, r
     n = inf + (n - inf) * d_exp(-dtq10 * s);
 }
 
+// One kinetic mechanism (lti_sim scheme) as the step kernels see it.
+template <typename real>
+struct KinArgs {
+    int identity, S, T, nb, nopen, dup_last;
+    int open[kMaxOpen];
+    int64_t m;
+    const uint32_t* seg_ptr; const int64_t* neuron_ptr; const uint32_t* seg;
+    real* state; const real* gcoef; const real* table;
+    real vmin, frq, cs, erev;
+};
+
 template <typename real>
 struct StepArgs {
     int64_t n_neuron;
@@ -94,18 +105,15 @@ struct StepArgs {
     unsigned long long* facc; int facc_cap; int frc_smem;
     // wide propagator (global int32 columns)
     const int64_t* wrow; const int32_t* wcol; const real* wval; const real* wleak;
-    // hh
-    int hh_on, hh_identity;
+    // hh (hh_dup_last: only the last instance of a segment counts, the reference's
+    // fancy-index "+=" for nonspecific conductances)
+    int hh_on, hh_identity, hh_dup_last;
     const uint32_t* hh_seg_ptr; const int64_t* hh_neuron_ptr; const uint32_t* hh_seg;
     real* gm; real* gh; real* gn; const real* cna; const real* ck; const real* cl;
     real ena, ek, el, dtq10;
-    // kinetic scheme (lti_sim)
-    int kin_on, kin_identity, kin_S, kin_T, kin_nb, kin_nopen;
-    int kin_open[4];
-    int64_t kin_m;
-    const uint32_t* kin_seg_ptr; const int64_t* kin_neuron_ptr; const uint32_t* kin_seg;
-    real* kin_state; const real* kin_gcoef; const real* kin_table;
-    real kin_vmin, kin_frq, kin_cs, kin_erev;
+    // kinetic schemes (lti_sim), in registration order
+    int n_kin;
+    KinArgs<real> kin[kMaxKinetic];
     // synapses
     int syn_on, syn_ring_words, syn_ring_mask, syn_pulse;
     const uint32_t* syn_seg_ptr; const int64_t* syn_neuron_ptr;
@@ -166,10 +174,27 @@ __device__ __forceinline__ void hh_conductance_total(const StepArgs<real>& a, re
 
 // A kinetic instance's open probability: its open states summed in list order.
 template <typename real, typename Get>
-__device__ __forceinline__ real kinetic_open(const StepArgs<real>& a, Get state) {
+__device__ __forceinline__ real kinetic_open(const KinArgs<real>& K, Get state) {
     real open = real(0);
-    for (int o = 0; o < a.kin_nopen; ++o) open += state(a.kin_open[o]);
+    for (int o = 0; o < K.nopen; ++o) open += state(K.open[o]);
     return open;
+}
+
+// The conductance (S) of kinetic mechanism K's instances on segment i.
+template <typename real>
+__device__ __forceinline__ real kinetic_conductance(const KinArgs<real>& K, int64_t i) {
+    real gkin = real(0);
+    auto add = [&](int64_t k) {
+        const real open = kinetic_open(K, [&](int s) { return K.state[(int64_t)s * K.m + k]; });
+        gkin += K.gcoef[k] * open;
+    };
+    if (K.identity) add(i);
+    else {
+        const int64_t b = K.seg_ptr[i], e = K.seg_ptr[i + 1];
+        if (K.dup_last) { if (e > b) add(e - 1); }
+        else for (int64_t k = b; k < e; ++k) add(k);
+    }
+    return gkin;
 }
 
 template <typename real>
@@ -180,22 +205,17 @@ __device__ __forceinline__ void segment_conductance(const StepArgs<real>& a, int
         if (a.hh_identity) {
             hh_conductance_add(a.cna[i], a.ck[i], a.cl[i], a.gm[i], a.gh[i], a.gn[i], gna, gk, gl);
         } else {
-            const int64_t b = a.hh_seg_ptr[i], e = a.hh_seg_ptr[i + 1];
+            const int64_t e = a.hh_seg_ptr[i + 1];
+            const int64_t b = a.hh_dup_last && e > a.hh_seg_ptr[i] ? e - 1 : a.hh_seg_ptr[i];
             for (int64_t k = b; k < e; ++k)
                 hh_conductance_add(a.cna[k], a.ck[k], a.cl[k], a.gm[k], a.gh[k], a.gn[k], gna, gk, gl);
         }
         hh_conductance_total(a, gna, gk, gl, G, GE);
     }
-    if (a.kin_on) {
-        real gkin = real(0);
-        auto add = [&](int64_t k) {
-            const real open = kinetic_open(a, [&](int s) { return a.kin_state[(int64_t)s * a.kin_m + k]; });
-            gkin += a.kin_gcoef[k] * open;
-        };
-        if (a.kin_identity) add(i);
-        else for (int64_t k = a.kin_seg_ptr[i], e = a.kin_seg_ptr[i + 1]; k < e; ++k) add(k);
+    for (int q = 0; q < a.n_kin; ++q) {
+        const real gkin = kinetic_conductance(a.kin[q], i);
         G += gkin;
-        GE += gkin * a.kin_erev;
+        GE += gkin * a.kin[q].erev;
     }
     if (a.syn_on) {
         const uint32_t b = a.syn_seg_ptr[i], e = a.syn_seg_ptr[i + 1];
@@ -310,12 +330,12 @@ __device__ __forceinline__ void spike_ring_write(const StepArgs<real>& a, int64_
 // computes them (codegen.py:43-59): bucket = trunc((v - vmin) * frq), clamped to
 // the table, location 1 above it and 0 below it.  Non-finite voltages land in bucket 0.
 template <typename real>
-__device__ __forceinline__ int kinetic_locate(const StepArgs<real>& a, real v, real& loc) {
-    real x = (v - a.kin_vmin) * a.kin_frq;
+__device__ __forceinline__ int kinetic_locate(const KinArgs<real>& K, real v, real& loc) {
+    real x = (v - K.vmin) * K.frq;
     if (!(x > real(-2))) x = real(-2);
-    if (x > real(a.kin_nb + 1)) x = real(a.kin_nb + 1);
+    if (x > real(K.nb + 1)) x = real(K.nb + 1);
     int b = (int)x;
-    if (b > a.kin_nb - 1) { b = a.kin_nb - 1; loc = real(1); }
+    if (b > K.nb - 1) { b = K.nb - 1; loc = real(1); }
     else if (b < 0) { b = 0; loc = real(0); }
     else loc = x - real(b);
     return b;
@@ -324,34 +344,52 @@ __device__ __forceinline__ int kinetic_locate(const StepArgs<real>& a, real v, r
 // One exact-integration step of a kinetic instance (codegen.py:60-106): the
 // polynomial approximation of the column-normalised propagator, evaluated per
 // (col, row) as table[bucket][col][row][term], times the state, then CONSERVE.
+// FP32 linear tables with an even number of states are read as 16-byte vectors
+// (two rows' terms per load; the same arithmetic in the same order).
 template <typename real, int S, int T>
-__device__ __forceinline__ void kinetic_advance(const StepArgs<real>& a, real v, real (&st)[S]) {
+__device__ __forceinline__ void kinetic_advance(const KinArgs<real>& K, real v, real (&st)[S]) {
     real loc;
-    const int b = kinetic_locate(a, v, loc);
+    const int b = kinetic_locate(K, v, loc);
     real basis[T];
     basis[0] = real(1);
 #pragma unroll
     for (int t = 1; t < T; ++t) basis[t] = basis[t - 1] * loc;
-    const real* __restrict__ tb = a.kin_table + (int64_t)b * (S * S * T);
+    const real* __restrict__ tb = K.table + (int64_t)b * (S * S * T);
     real out[S];
 #pragma unroll
     for (int c = 0; c < S; ++c) out[c] = real(0);
+    if constexpr (std::is_same<real, float>::value && T == 2 && S % 2 == 0) {
 #pragma unroll
-    for (int col = 0; col < S; ++col) {
+        for (int col = 0; col < S; ++col) {
 #pragma unroll
-        for (int row = 0; row < S; ++row) {
-            const real* p = tb + (col * S + row) * T;
-            real poly = real(0) + __ldg(p);
+            for (int row = 0; row < S; row += 2) {
+                const float4 q = __ldg(reinterpret_cast<const float4*>(tb + (col * S + row) * 2));
+                real p0 = real(0) + q.x;
+                p0 += basis[1] * q.y;
+                out[row] += p0 * st[col];
+                real p1 = real(0) + q.z;
+                p1 += basis[1] * q.w;
+                out[row + 1] += p1 * st[col];
+            }
+        }
+    } else {
 #pragma unroll
-            for (int t = 1; t < T; ++t) poly += basis[t] * __ldg(p + t);
-            out[row] += poly * st[col];
+        for (int col = 0; col < S; ++col) {
+#pragma unroll
+            for (int row = 0; row < S; ++row) {
+                const real* p = tb + (col * S + row) * T;
+                real poly = real(0) + __ldg(p);
+#pragma unroll
+                for (int t = 1; t < T; ++t) poly += basis[t] * __ldg(p + t);
+                out[row] += poly * st[col];
+            }
         }
     }
-    if (a.kin_cs > real(0)) {
+    if (K.cs > real(0)) {
         real sum = out[0];
 #pragma unroll
         for (int c = 1; c < S; ++c) sum += out[c];
-        const real f = a.kin_cs / sum;
+        const real f = K.cs / sum;
 #pragma unroll
         for (int c = 0; c < S; ++c) out[c] *= f;
     }
@@ -360,25 +398,25 @@ __device__ __forceinline__ void kinetic_advance(const StepArgs<real>& a, real v,
 }
 
 template <typename real, int S, int T>
-__device__ __forceinline__ void kinetic_step_fixed(const StepArgs<real>& a, int64_t k, real v) {
+__device__ __forceinline__ void kinetic_step_fixed(const KinArgs<real>& K, int64_t k, real v) {
     real st[S];
 #pragma unroll
-    for (int c = 0; c < S; ++c) st[c] = a.kin_state[(int64_t)c * a.kin_m + k];
-    kinetic_advance<real, S, T>(a, v, st);
+    for (int c = 0; c < S; ++c) st[c] = K.state[(int64_t)c * K.m + k];
+    kinetic_advance<real, S, T>(K, v, st);
 #pragma unroll
-    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = st[c];
+    for (int c = 0; c < S; ++c) K.state[(int64_t)c * K.m + k] = st[c];
 }
 
 // Same step for any S <= 16 and T <= 4.
 template <typename real>
-__device__ __noinline__ void kinetic_step_generic(const StepArgs<real>& a, int64_t k, real v) {
-    const int S = a.kin_S, T = a.kin_T;
+__device__ __noinline__ void kinetic_step_generic(const KinArgs<real>& K, int64_t k, real v) {
+    const int S = K.S, T = K.T;
     real loc;
-    const int b = kinetic_locate(a, v, loc);
+    const int b = kinetic_locate(K, v, loc);
     real basis[4] = {real(1), loc, loc * loc, loc * loc * loc};
-    const real* tb = a.kin_table + (int64_t)b * (S * S * T);
+    const real* tb = K.table + (int64_t)b * (S * S * T);
     real st[16], out[16];
-    for (int c = 0; c < S; ++c) { st[c] = a.kin_state[(int64_t)c * a.kin_m + k]; out[c] = real(0); }
+    for (int c = 0; c < S; ++c) { st[c] = K.state[(int64_t)c * K.m + k]; out[c] = real(0); }
     for (int col = 0; col < S; ++col)
         for (int row = 0; row < S; ++row) {
             const real* p = tb + (col * S + row) * T;
@@ -386,19 +424,22 @@ __device__ __noinline__ void kinetic_step_generic(const StepArgs<real>& a, int64
             for (int t = 1; t < T; ++t) poly += basis[t] * p[t];
             out[row] += poly * st[col];
         }
-    if (a.kin_cs > real(0)) {
+    if (K.cs > real(0)) {
         real sum = out[0];
         for (int c = 1; c < S; ++c) sum += out[c];
-        const real f = a.kin_cs / sum;
+        const real f = K.cs / sum;
         for (int c = 0; c < S; ++c) out[c] *= f;
     }
-    for (int c = 0; c < S; ++c) a.kin_state[(int64_t)c * a.kin_m + k] = out[c];
+    for (int c = 0; c < S; ++c) K.state[(int64_t)c * K.m + k] = out[c];
 }
 
+// Unrolled instances for the shapes of the schemes this package defines
+// (8-state sodium, 6-state Nav1.1 / Kv1.1 with linear tables); others generic.
 template <typename real>
-__device__ __forceinline__ void kinetic_step(const StepArgs<real>& a, int64_t k, real v) {
-    if (a.kin_S == 8 && a.kin_T == 2) kinetic_step_fixed<real, 8, 2>(a, k, v);
-    else kinetic_step_generic(a, k, v);
+__device__ __forceinline__ void kinetic_step(const KinArgs<real>& K, int64_t k, real v) {
+    if (K.S == 8 && K.T == 2) kinetic_step_fixed<real, 8, 2>(K, k, v);
+    else if (K.S == 6 && K.T == 2) kinetic_step_fixed<real, 6, 2>(K, k, v);
+    else kinetic_step_generic(K, k, v);
 }
 
 // Exact exponential membrane update of one segment (electric.py:60-76).
@@ -580,8 +621,10 @@ __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_
 // one-to-one onto segments (HH and kinetic instances in segment order, no synapses,
 // no calcium) and the conductance cache exists.
 inline bool fuse_mechanisms(const nw_ctx* ctx) {
-    return ctx->gcache.ptr && ctx->syn.n == 0 && !ctx->ca.on && (ctx->hh.m == 0 || ctx->hh.identity) &&
-           (ctx->kin.m == 0 || ctx->kin.identity);
+    if (!ctx->gcache.ptr || ctx->syn.n != 0 || ctx->ca.on || (ctx->hh.m != 0 && !ctx->hh.identity)) return false;
+    for (int q = 0; q < ctx->n_kin; ++q)
+        if (!ctx->kin[q].identity) return false;
+    return true;
 }
 
 template <typename real>
@@ -614,16 +657,21 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.gm = hh.gm.as<real>(); a.gh = hh.gh.as<real>(); a.gn = hh.gn.as<real>();
     a.cna = hh.cna.as<real>(); a.ck = hh.ck.as<real>(); a.cl = hh.cl.as<real>();
     a.ena = (real)hh.ena; a.ek = (real)hh.ek; a.el = (real)hh.el;
-    const KineticState& K = ctx->kin;
-    a.kin_on = K.m > 0 ? 1 : 0;
-    a.kin_identity = K.identity ? 1 : 0;
-    a.kin_S = K.S; a.kin_T = K.T; a.kin_nb = K.nb; a.kin_nopen = K.n_open;
-    for (int o = 0; o < 4; ++o) a.kin_open[o] = K.open[o];
-    a.kin_m = K.m;
-    a.kin_seg_ptr = K.seg_ptr.as<uint32_t>(); a.kin_neuron_ptr = K.neuron_ptr.as<int64_t>();
-    a.kin_seg = K.seg.as<uint32_t>();
-    a.kin_state = K.state.as<real>(); a.kin_gcoef = K.gcoef.as<real>(); a.kin_table = K.table.as<real>();
-    a.kin_vmin = (real)K.vmin; a.kin_frq = (real)K.frq; a.kin_cs = (real)K.conserve; a.kin_erev = (real)K.erev;
+    a.hh_dup_last = ctx->duplicates == 1 ? 1 : 0;
+    a.n_kin = ctx->n_kin;
+    for (int q = 0; q < ctx->n_kin; ++q) {
+        const KineticState& K = ctx->kin[q];
+        KinArgs<real>& k = a.kin[q];
+        k.identity = K.identity ? 1 : 0;
+        k.dup_last = (ctx->duplicates == 1 && K.species < 0) ? 1 : 0;
+        k.S = K.S; k.T = K.T; k.nb = K.nb; k.nopen = K.n_open;
+        for (int o = 0; o < kMaxOpen; ++o) k.open[o] = K.open[o];
+        k.m = K.m;
+        k.seg_ptr = K.seg_ptr.as<uint32_t>(); k.neuron_ptr = K.neuron_ptr.as<int64_t>();
+        k.seg = K.seg.as<uint32_t>();
+        k.state = K.state.as<real>(); k.gcoef = K.gcoef.as<real>(); k.table = K.table.as<real>();
+        k.vmin = (real)K.vmin; k.frq = (real)K.frq; k.cs = (real)K.conserve; k.erev = (real)K.erev;
+    }
     const CalciumState& Ca = ctx->ca;
     a.ca_on = Ca.on ? 1 : 0;
     a.gc = ctx->gcache.as<real>(); a.gc_n = ctx->n_seg;

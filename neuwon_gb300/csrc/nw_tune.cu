@@ -25,11 +25,12 @@ struct Saved {
 // Every device buffer a step writes (probes are switched off during trials).
 std::vector<DevBuf*> stepped_buffers(nw_ctx* ctx) {
     std::vector<DevBuf*> v = {&ctx->V, &ctx->Vint, &ctx->hh.gm, &ctx->hh.gh, &ctx->hh.gn,
-                              &ctx->kin.state, &ctx->ap_detected, &ctx->ap_state,
+                              &ctx->ap_detected, &ctx->ap_state,
                               &ctx->spike_count, &ctx->status, &ctx->syn.oa, &ctx->syn.on,
                               &ctx->syn.od, &ctx->syn.pulse_end, &ctx->syn.events,
                               &ctx->syn.last_event, &ctx->syn.ring, &ctx->ca.c, &ctx->ca.dcdt,
                               &ctx->ca.state};
+    for (int q = 0; q < ctx->n_kin; ++q) v.push_back(&ctx->kin[q].state);
     std::vector<DevBuf*> out;
     for (DevBuf* b : v)
         if (b->ptr && b->bytes) out.push_back(b);

@@ -130,7 +130,11 @@ wide_mechanism_kernel(const StepArgs<real> a, const int s_off, const int64_t n_h
     }
     k -= n_hh;
     if (k < n_kin) {
-        kinetic_step(a, k, a.V[a.kin_identity ? k : (int64_t)a.kin_seg[k]]);
+        // n_kin counts the instances of all kinetic mechanisms, in registration order.
+        int q = 0;
+        while (k >= a.kin[q].m) { k -= a.kin[q].m; ++q; }
+        const KinArgs<real>& K = a.kin[q];
+        kinetic_step(K, k, a.V[K.identity ? k : (int64_t)K.seg[k]]);
         return;
     }
     k -= n_kin;
@@ -219,7 +223,7 @@ template <typename real>
 static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lanes) {
     const int64_t n = ctx->n_seg;
     const unsigned seg_blocks = (unsigned)((n + kWideThreads - 1) / kWideThreads);
-    const int64_t n_hh = ctx->hh.m, n_kin = ctx->kin.m, n_syn = ctx->syn.n;
+    const int64_t n_hh = ctx->hh.m, n_kin = kinetic_instances(ctx), n_syn = ctx->syn.n;
     const int64_t n_mech = n_hh + n_kin + n_syn;
     const int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
     for (int s = 0; s < steps; ++s) {
@@ -283,7 +287,8 @@ static int wide_graph(nw_ctx* ctx, const StepArgs<real>& a0, int steps, int lane
     key_bytes(key, &lanes, sizeof(lanes));
     key_bytes(key, &ctx->n_seg, sizeof(ctx->n_seg));
     key_bytes(key, &ctx->hh.m, sizeof(ctx->hh.m));
-    key_bytes(key, &ctx->kin.m, sizeof(ctx->kin.m));
+    const int64_t n_kin = kinetic_instances(ctx);
+    key_bytes(key, &n_kin, sizeof(n_kin));
     key_bytes(key, &ctx->syn.n, sizeof(ctx->syn.n));
     key_bytes(key, &ctx->ca.on, sizeof(ctx->ca.on));
     key_bytes(key, &ctx->prop_format, sizeof(ctx->prop_format));
@@ -350,7 +355,7 @@ static int wide_steps(nw_ctx* ctx, int k_steps) {
         ctx->input_ticks += 2 * (int64_t)steps;
         ctx->steps += steps;
         if (ctx->n_probes) ctx->probe_len += steps;
-        if (ctx->hh.m > 0 || ctx->kin.m > 0) ctx->g_valid = true;
+        if (has_channel_mechanisms(ctx)) ctx->g_valid = true;
         done += steps;
     }
     return NW_OK;
@@ -358,6 +363,43 @@ static int wide_steps(nw_ctx* ctx, int k_steps) {
 
 int advance_wide(nw_ctx* ctx, int k_steps) {
     return ctx->precision == NW_F64 ? wide_steps<double>(ctx, k_steps) : wide_steps<float>(ctx, k_steps);
+}
+
+// Per segment, the summed conductance (S) of the kinetic mechanisms feeding
+// `species` at their present state: the species' conductance accumulator as a
+// mechanism phase leaves it (neuwon/rxd/species.py:129-133, 155-160).
+template <typename real>
+__global__ void species_conductance_kernel(const StepArgs<real> a, int32_t species, int32_t feeds_mask,
+                                           double* out, int64_t n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double g = 0.0;
+    for (int q = 0; q < a.n_kin; ++q)
+        if ((feeds_mask >> q) & 1) g += (double)kinetic_conductance(a.kin[q], i);
+    out[i] = g;
+}
+
+template <typename real>
+static int species_conductance_t(nw_ctx* ctx, int32_t species, double* host) {
+    const StepArgs<real> a = make_args<real>(ctx, 1);
+    int32_t mask = 0;
+    for (int q = 0; q < ctx->n_kin; ++q)
+        if (ctx->kin[q].species == species) mask |= 1 << q;
+    DevBuf out;
+    NW_CHECK(dev_alloc(ctx, out, 8 * ctx->n_seg));
+    species_conductance_kernel<real><<<(unsigned)((ctx->n_seg + 255) / 256), 256, 0, ctx->stream>>>(
+        a, species, mask, out.as<double>(), ctx->n_seg);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, out.ptr, 8 * ctx->n_seg, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(out);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "nw_species_conductance");
+    return NW_OK;
+}
+
+int species_conductance(nw_ctx* ctx, int32_t species, double* host_out) {
+    return ctx->precision == NW_F64 ? species_conductance_t<double>(ctx, species, host_out)
+                                    : species_conductance_t<float>(ctx, species, host_out);
 }
 
 }  // namespace nw

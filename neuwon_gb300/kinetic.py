@@ -61,8 +61,11 @@ class KineticScheme:
         return M
 
     def steady_state(self, v, celsius):
-        """State after a very long time at voltage v, scaled to the conserve sum."""
+        """State after an hour at voltage v from equal occupancies summing to the
+        conserve sum, through the column-renormalised propagator
+        (LTI_Model.get_initial_state, neuwon/rxd/lti_sim/lti_model.py:67-79)."""
         M = scipy.linalg.expm(self.matrix([v], celsius)[0] * 3600e3)
+        M = M / M.sum(axis=0, keepdims=True)
         s = M @ np.full(self.num_states, (self.conserve_sum or 1.0) / self.num_states)
         return s
 
@@ -98,6 +101,82 @@ def na8():
             out.append((4 + k, k, ah))
         return out
     return KineticScheme("na8", states, transitions, open_states=["O"], conserve_sum=1.0)
+
+
+def _boltzmann(v, b, vv, k):
+    """FUNCTION rates2 of nmodl_library/kinetic/Nav11.mod:144-146: b / (1 + exp((v - vv) / k))."""
+    with np.errstate(over="ignore"):
+        return b / (1.0 + np.exp((v - vv) / k))
+
+
+def nav11():
+    """Six-state Nav1.1 channel of nmodl_library/kinetic/Nav11.mod (SUFFIX na11a,
+    USEION na): states C1 C2 O1 O2 I1 I2, open = O1 + O2, CONSERVE sum 1; rate
+    constants of its PARAMETER block (Nav11.mod:21-87), q10 = 3^((celsius - 20)/10)
+    (INITIAL, :120) and PROCEDURE rates (:148-163), reactions of KINETIC kin (:131-142)."""
+    states = ["C1", "C2", "O1", "O2", "I1", "I2"]
+    C1, C2, O1, O2, I1, I2 = range(6)
+
+    def transitions(v, celsius):
+        q = 3.0 ** ((celsius - 20.0) / 10.0)
+        r = lambda *terms: q * sum(_boltzmann(v, *t) for t in terms)
+        c1c2 = r((18.0, -7.0, -10.0))
+        c2c1 = r((3.0, -37.0, 10.0), (18.0, -7.0, -10.0))
+        c2o1 = r((18.0, -7.0, -10.0))
+        o1c2 = r((3.0, -37.0, 10.0), (18.0, -7.0, -10.0))
+        c2o2 = r((0.08, -10.0, -15.0))
+        o2c2 = r((2.0, -50.0, 7.0), (0.2, -20.0, -10.0))
+        o1i1 = r((8.0, -37.0, 13.0), (17.0, -7.0, -15.0))
+        i1o1 = r((0.00001, -37.0, 10.0))
+        i1c1 = r((0.21, -61.0, 7.0))
+        c1i1 = r((0.3, -61.0, -5.5))
+        i1i2 = r((0.0015, -90.0, -5.0))
+        i2i1 = r((0.0075, -90.0, 15.0))
+        return [(C1, C2, c1c2), (C2, C1, c2c1), (C2, O1, c2o1), (O1, C2, o1c2), (C2, O2, c2o2), (O2, C2, o2c2),
+                (O1, I1, o1i1), (I1, O1, i1o1), (I1, C1, i1c1), (C1, I1, c1i1), (I1, I2, i1i2), (I2, I1, i2i1)]
+    return KineticScheme("na11a", states, transitions, open_states=["O1", "O2"], conserve_sum=1.0)
+
+
+# PARAMETER block of nmodl_library/kinetic/Kv11.mod:10-34 (temperature factors per degC).
+_KV11 = dict(Hkc=0.12166, Hki=0.44916, Hkn=-0.85022, Hri=0.0026028, Hric_n=-0.066541, Hrn=-0.048079,
+             Hvc=0.91934, Hvic_c=-0.71121, Hvic_n=-0.29515, Hvn_ic=0.94495, Ri=0.78718, Rn=1.6611,
+             Vc=-17.6122, Zc=1.6756, kc=0.030179, ki=0.00025091, kn=0.010089, ric_c=0.01189, ric_n=5.55,
+             vc_ic=1.6111, vic_c=999.9351, vic_n=0.66208, vn_ic=0.10006)
+
+
+def kv11():
+    """Six-state Kv1.1 channel of nmodl_library/kinetic/Kv11.mod (SUFFIX
+    Kv11_6States_temperature2, USEION k): states CS OS IC1 CIC1 IN INC1, open = OS,
+    CONSERVE sum 1; INITIAL constants F = 96.485, A = 8.134 (celsius + 273.15),
+    rc_ic = ric_c, rn_ic = ric_n, Hrn_ic = Hric_n (:55-62), PROCEDURE rates (:76-79),
+    reactions of KINETIC kin (:64-74)."""
+    states = ["CS", "OS", "IC1", "CIC1", "IN", "INC1"]
+    CS, OS, IC1, CIC1, IN, INC1 = range(6)
+    p = _KV11
+
+    def transitions(v, celsius):
+        t = celsius - 25.0
+        FA = 96.485 / (8.134 * (celsius + 273.15))
+        e = lambda x: math.exp(x * t)
+        shift = v - p["Vc"] - p["Hvc"] * t
+        kco = p["kc"] * np.exp(p["Zc"] * FA * shift) * e(p["Hkc"])
+        koc = p["kc"] * np.exp(-p["Zc"] * FA * shift) * e(p["Hkc"])
+        rc_ic, rn_ic, Hrn_ic = p["ric_c"], p["ric_n"], p["Hric_n"]
+        ki_t, kn_t = p["ki"] * e(p["Hki"]), p["kn"] * e(p["Hkn"])
+        one = np.ones_like(kco)
+        return [
+            (CS, OS, kco), (OS, CS, koc),
+            (CIC1, IC1, p["vc_ic"] * kco), (IC1, CIC1, rc_ic * p["vc_ic"] * koc),
+            (CS, CIC1, one * p["ric_c"] * p["vic_c"] * ki_t * e(p["Hvic_c"])),
+            (CIC1, CS, one * p["vic_c"] * ki_t * p["Ri"] * e(p["Hri"]) * e(p["Hvic_c"])),
+            (OS, IC1, one * ki_t), (IC1, OS, one * ki_t * p["Ri"] * e(p["Hri"])),
+            (OS, IN, one * kn_t), (IN, OS, one * kn_t * p["Rn"] * e(p["Hrn"])),
+            (IC1, INC1, one * p["vn_ic"] * rn_ic * kn_t * e(Hrn_ic) * e(p["Hvn_ic"])),
+            (INC1, IC1, one * p["vn_ic"] * kn_t * p["Rn"] * e(p["Hrn"]) * e(p["Hvn_ic"])),
+            (IN, INC1, one * p["ric_n"] * p["vic_n"] * ki_t * e(p["Hric_n"]) * e(p["Hvic_n"])),
+            (INC1, IN, one * p["vic_n"] * ki_t * p["Ri"] * e(p["Hri"]) * e(p["Hvic_n"])),
+        ]
+    return KineticScheme("Kv11_6States_temperature2", states, transitions, open_states=["OS"], conserve_sum=1.0)
 
 
 def binomial_state(m, h):
@@ -274,22 +353,31 @@ def optimize_table(ctx, scheme, dt, celsius, accuracy, vmin=-100.0, vmax=60.0, d
 
 
 class Kinetic(Mechanism):
-    """A kinetic-scheme channel with one nonspecific conductance.
+    """A kinetic-scheme channel with one conductance.
 
-    conductance = gbar[S/cm2] * 1e-8 * magnitude[um2] * sum(open states), reversal
-    potential ``erev``; the step uses an ``LTITable`` built for the model's dt and
-    temperature when the model is first advanced.
+    conductance = gbar[S/cm2] * 1e-8 * magnitude[um2] * sum(open states).  With
+    ``ion`` None it is a nonspecific conductance with reversal potential ``erev``;
+    with ``ion`` the name of an electric species of the model (``USEION``,
+    neuwon/rxd/nmodl/__init__.py:168-208) it is written into that species'
+    conductance accumulator and takes the species' reversal potential
+    (species.py:155-160).  The step uses a voltage table (LinearInput over
+    [vmin, vmax]) built on the GPU for the model's dt and temperature when the
+    model is first advanced, or ``table``: a table made elsewhere for that dt and
+    temperature, in lti_sim's layout [bucket][col][row][term] (e.g. the
+    ``table_data`` lti_sim's code generator emits, reshaped; codegen.py:29-37).
     """
     name = "na8"
     scheme_factory = staticmethod(na8)
     gbar = 0.012
     erev = 50.0
+    ion = None
+    table = None
     vmin, vmax, num_buckets, degree = -100.0, 60.0, 1600, 1
     _model = None
 
     @classmethod
     def configure(cls, **params):
-        ok = {"name", "scheme_factory", "gbar", "erev", "vmin", "vmax", "num_buckets", "degree"}
+        ok = {"name", "scheme_factory", "gbar", "erev", "ion", "table", "vmin", "vmax", "num_buckets", "degree"}
         bad = set(params) - ok
         if bad:
             raise ValueError(f"unknown kinetic parameters {sorted(bad)}")
@@ -321,3 +409,15 @@ class Kinetic(Mechanism):
     @classmethod
     def build_table(cls, dt, celsius):
         return LTITable(cls.scheme_factory(), dt, celsius, cls.vmin, cls.vmax, cls.num_buckets, cls.degree)
+
+
+# The reference library's kinetic channels restated above, as mechanisms: the
+# conductance feeds the channel's ion species (USEION na / USEION k), gbar is the
+# PARAMETER default in S/cm2 (Nav11.mod: 0.1 mho/cm2; Kv11.mod: 36 mmho/cm2), and
+# the voltage table spans the range the reference's NMODL front end gives a
+# voltage input (LinearInput -100..100 mV, neuwon/rxd/nmodl/__init__.py:321-322),
+# in 0.1 mV buckets with linear polynomials.
+Nav11 = Kinetic.configure(name="na11a", scheme_factory=nav11, gbar=0.1, ion="na", vmin=-100.0, vmax=100.0,
+                          num_buckets=2000, degree=1)
+Kv11 = Kinetic.configure(name="Kv11_6States_temperature2", scheme_factory=kv11, gbar=0.036, ion="k",
+                         vmin=-100.0, vmax=100.0, num_buckets=2000, degree=1)

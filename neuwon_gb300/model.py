@@ -24,6 +24,8 @@ from .morphology import EPSILON, Tree, device_order, geometry, passive_electric
 from .kinetic import Kinetic
 from .mechanisms import HH, Mechanism, hh_steady_state
 
+MAX_KINETIC = 8     # kinetic mechanisms per model (the device's table of them)
+
 
 class Clock:
     """Tick counter; neuwon/database/time.py:54-121."""
@@ -273,6 +275,15 @@ class RxD_Model:
       path                  'batched' (fused persistent kernel, one CTA per neuron),
                             'wide' (whole-model launches per phase: neurons of any
                             size) or 'plain' (per-neuron launches)
+      duplicates            'sum' (default: every instance of a mechanism on a
+                            segment counts) or 'reference' (nonspecific
+                            conductances count only the last instance of each
+                            segment, as the reference's fancy-index "+=" does,
+                            neuwon/rxd/species.py:256-260)
+
+    ``species`` takes the reference's keyword dicts (``_SpeciesType``,
+    species.py:90-142, see ``species.SpeciesType``) and ``Calcium`` objects; the
+    electric ones are listed by name in ``model.species``.
     """
 
     def __init__(self, time_step=0.1, *, temperature=37, initial_voltage=-70,
@@ -280,14 +291,26 @@ class RxD_Model:
                  extracellular_tortuosity=1.55, extracellular_max_distance=20e-6,
                  species=(), mechanisms=(), precision="f32", device=0,
                  propagator_tolerance=EPSILON, propagator_conserve=False, path="batched",
-                 propagator_format="quads", propagator_lump=False):
-        from .species import Calcium
+                 propagator_format="quads", propagator_lump=False, duplicates="sum"):
+        from .species import Calcium, SpeciesType
         self._calcium = None
+        self.species = {}
         for sp in species:
-            ca = sp if isinstance(sp, Calcium) else Calcium.from_reference_kwargs(sp)
-            if self._calcium is not None:
-                raise NotImplementedError("one diffusing species (calcium) per model")
-            self._calcium = ca
+            if isinstance(sp, Calcium):
+                ca = sp
+            else:
+                st = sp if isinstance(sp, SpeciesType) else SpeciesType(**dict(sp))
+                if st.name in self.species:
+                    raise ValueError(f"duplicate species {st.name}")
+                self.species[st.name] = st
+                ca = st.calcium
+            if ca is not None:
+                if self._calcium is not None:
+                    raise NotImplementedError("one diffusing species (calcium) per model")
+                self._calcium = ca
+        if duplicates not in ("sum", "reference"):
+            raise ValueError("duplicates must be 'sum' or 'reference'")
+        self.duplicates = duplicates
         self.time_step = float(time_step)
         self.temperature = float(temperature)
         self.initial_voltage = float(initial_voltage)
@@ -547,7 +570,7 @@ class RxD_Model:
                 m = self._instance_count(name)
                 sch = cls.scheme_factory()
                 init = sch.steady_state(self.initial_voltage, self.temperature)
-                self._ctx.set_data("kinetic.state", np.tile(init, m))
+                self._ctx.set_data(self.kinetic_state_name(name), np.tile(init, m))
         self._ctx.call("nw_set_option", b"reset_clock", 1)
         self.input_hook.ticks = 0
         self.advance_hook.ticks = 0
@@ -557,8 +580,23 @@ class RxD_Model:
         v = self.get_data("Segment.voltage")
         assert np.all(np.isfinite(v)), "non-finite voltage"
 
+    def kinetic_state_name(self, mechanism):
+        """The C-ABI attribute name of a kinetic mechanism's states ("kinetic.<q>.state")."""
+        self._sync()
+        return f"kinetic.{self._kin_index[mechanism]}.state"
+
     def get_data(self, name):
-        """Whole-attribute read in creation order ('Segment.voltage', 'hh.m', ...)."""
+        """Whole-attribute read in creation order ('Segment.voltage', 'hh.m',
+        'na11a.state', 'Segment.na_conductance', ...)."""
+        if name.startswith("Segment.") and name.endswith("_conductance"):
+            ion = name[len("Segment."):-len("_conductance")]
+            if ion in self.species and self.species[ion].electric:
+                # The species' conductance accumulator as the last mechanism phase
+                # left it (species.py:129-133): device gather, creation order.
+                self._sync()
+                out = np.empty(self._n)
+                self._ctx.call("nw_species_conductance", self._species_index[ion], _lib.ptr(out))
+                return out[self._inv]
         if name.startswith("Segment."):
             return self._get_segment_values(name).copy()
         if name.startswith("Neuron."):
@@ -578,7 +616,7 @@ class RxD_Model:
         n = self._instance_count(cls.get_name())
         if issubclass(cls, Kinetic):
             S = len(cls.scheme_factory().states)
-            return self._ctx.get_data("kinetic.state", n * S).reshape(n, S)
+            return self._ctx.get_data(self.kinetic_state_name(mech), n * S).reshape(n, S)
         return self._ctx.get_data(f"hh.{attr}", n)
 
     def close(self):
@@ -599,9 +637,15 @@ class RxD_Model:
         name = bound.get_name()
         if name in self.mechanisms:
             raise ValueError(f"duplicate mechanism {name}")
-        for kind in (HH, Kinetic):
-            if issubclass(bound, kind) and any(issubclass(c, kind) for c in self.mechanisms.values()):
-                raise NotImplementedError(f"one {kind.__name__} mechanism per model")
+        if issubclass(bound, HH) and any(issubclass(c, HH) for c in self.mechanisms.values()):
+            raise NotImplementedError("one HH mechanism per model")
+        if issubclass(bound, Kinetic):
+            if sum(issubclass(c, Kinetic) for c in self.mechanisms.values()) >= MAX_KINETIC:
+                raise NotImplementedError(f"at most {MAX_KINETIC} kinetic mechanisms per model")
+            ion = bound.ion
+            if ion is not None and not (ion in self.species and self.species[ion].electric):
+                raise ValueError(f"mechanism {name} writes the conductance of ion {ion!r}, but the model declares no "
+                                 f"electric species {ion!r} (species=[{{'name': {ion!r}, 'reversal_potential': ...}}])")
         self.mechanisms[name] = bound
         self._mech_instances[name] = {"seg": [], "mag": [], "n_at": [], "gnabar": [], "gkbar": [],
                                       "glbar": [], "gbar": []}
@@ -758,6 +802,14 @@ class RxD_Model:
             ctx.call("nw_propagator_conserve")
         ctx.set_option("propagator_format", self.propagator_format)
         self.propagator_nnz = nnz.value
+        # Electric species, numbered in declaration order (species.py:90-142).
+        electric = [s for s in self.species.values() if s.electric]
+        self._species_index = {s.name: k for k, s in enumerate(electric)}
+        erev = np.array([s.reversal_potential for s in electric], dtype=np.float64)
+        ctx.call("nw_species_set", len(electric), _lib.ptr(erev) if len(erev) else None)
+        ctx.set_option("duplicates", 1 if self.duplicates == "reference" else 0)
+        ctx.call("nw_kinetic_clear")
+        self._kin_index = {}
         for name, cls in self.mechanisms.items():
             if issubclass(cls, Kinetic):
                 self._sync_kinetic(cls)
@@ -823,6 +875,11 @@ class RxD_Model:
         key = (cls, self.time_step, self.temperature)
         cache = getattr(self, "_tables", {})
         self._tables = cache
+        if cls.table is not None:
+            cache[key] = np.asarray(cls.table, dtype=np.float64)
+            if cache[key].shape != (nb, sch.num_states, sch.num_states, T):
+                raise ValueError(f"{cls.get_name()}: table shape {cache[key].shape}, expected "
+                                 f"{(nb, sch.num_states, sch.num_states, T)} [bucket][col][row][term]")
         layout = cache.get(key)
         placeholder = layout is None
         if placeholder:
@@ -832,13 +889,17 @@ class RxD_Model:
         seg_dev = np.ascontiguousarray(self._inv[seg]) if len(seg) else seg
         cs = float(sch.conserve_sum) if sch.conserve_sum is not None else 0.0
         frq = nb / (cls.vmax - cls.vmin)
-        self._ctx.call("nw_kinetic_register", len(seg), _lib.ptr(seg_dev), _lib.ptr(g), sch.num_states,
-                       len(open_idx), _lib.ptr(open_idx), float(cls.erev), _lib.ptr(np.ascontiguousarray(layout.ravel())),
-                       nb, T, float(cls.vmin), frq, cs, _lib.ptr(init))
+        species = -1 if cls.ion is None else self._species_index[cls.ion]
+        q = _lib.ctypes.c_int32()
+        self._ctx.call("nw_kinetic_add", len(seg), _lib.ptr(seg_dev), _lib.ptr(g), sch.num_states,
+                       len(open_idx), _lib.ptr(open_idx), float(cls.erev), species,
+                       _lib.ptr(np.ascontiguousarray(layout.ravel())), nb, T, float(cls.vmin), frq, cs, _lib.ptr(init),
+                       _lib.ctypes.byref(q))
+        self._kin_index[cls.get_name()] = q.value
         if placeholder and len(seg):
             from .kinetic import scheme_table_gpu
             cache[key] = scheme_table_gpu(self._ctx, sch, self.time_step, self.temperature, cls.vmin, cls.vmax, nb,
-                                          cls.degree, target=1)
+                                          cls.degree, target=16 + q.value)
 
     def _sync_clamps(self):
         c = self._clamps

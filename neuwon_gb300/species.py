@@ -20,6 +20,67 @@ import scipy.linalg
 FARADAY = 96485.3321233100184      # C/mol (species.py:8)
 
 
+class SpeciesType:
+    """One entry of ``RxD_Model(species=[...])``: the keywords of the reference's
+    ``_SpeciesType`` (neuwon/rxd/species.py:90-142).
+
+    A species with a ``reversal_potential`` is electric: mechanisms that name it as
+    their ion write its per-segment conductance accumulator, which enters every
+    segment's total conductance and conductance-weighted driving voltage with the
+    species' constant reversal potential (``_apply_accumulators``,
+    species.py:155-160).  The device computes exactly that sum per segment (no
+    mechanism here writes a current into a species: conductances go in,
+    nmodl/__init__.py:185).  Keywords without a device path raise instead of
+    being ignored:
+
+    * ``reversal_potential="nerst"`` / ``"ghk"``: the reference computes neither
+      (``_compute_reversal_potential`` is ``1/0`` past the constant case,
+      species.py:165);
+    * ``outside_global_constant=False``: extracellular concentrations are not
+      stepped on the device;
+    * ``inside_global_constant=False`` for a species other than calcium, and a
+      finite ``decay_period``: intracellular calcium (``Calcium``) is the one
+      diffusing species with a device path.
+    """
+
+    def __init__(self, name, *, charge=0, reversal_potential=None, diffusivity=0.0, decay_period=np.inf,
+                 inside_initial_concentration=0.0, inside_global_constant=True,
+                 outside_initial_concentration=0.0, outside_global_constant=True):
+        self.name = str(name)
+        self.charge = int(charge)
+        self.electric = reversal_potential is not None
+        self.reversal_potential = None
+        if self.electric:
+            try:
+                self.reversal_potential = float(reversal_potential)
+            except (TypeError, ValueError):
+                raise NotImplementedError(
+                    f"species {self.name}: reversal potential {reversal_potential!r} has no device path (the "
+                    "reference's own Nernst/GHK computation is unfinished); give a constant in mV") from None
+            if not np.isfinite(self.reversal_potential):
+                raise ValueError(f"species {self.name}: reversal potential must be finite")
+        self.diffusivity = float(diffusivity)
+        self.decay_period = float(decay_period)
+        self.inside_initial_concentration = float(inside_initial_concentration)
+        self.inside_global_constant = bool(inside_global_constant)
+        self.outside_initial_concentration = float(outside_initial_concentration)
+        self.outside_global_constant = bool(outside_global_constant)
+        assert self.decay_period > 0.0 and self.diffusivity >= 0.0      # species.py:20-21
+        if not self.outside_global_constant:
+            raise NotImplementedError(f"species {self.name}: extracellular concentrations have no device path")
+        self.calcium = None
+        if not self.inside_global_constant:
+            if self.name.lower() != "ca":
+                raise NotImplementedError(f"species {self.name}: only intracellular calcium is stepped on the device")
+            if self.decay_period < np.inf:
+                raise NotImplementedError("species ca: a decay period has no device path (diffusion does)")
+            self.calcium = Calcium(diffusivity=self.diffusivity, initial=self.inside_initial_concentration,
+                                   na_fraction=0.0, pump=False)
+
+    def __repr__(self):
+        return f"<Species: {self.name}>"
+
+
 class Calcium:
     """Parameters of the calcium system (units: um2/ms, mM, 1/ms, mol/um2).
 
@@ -40,23 +101,6 @@ class Calcium:
         self.c_max, self.scale = float(c_max), float(scale)
         self.num_buckets, self.degree = int(num_buckets), int(degree)
         self.samples_per_bucket = int(samples_per_bucket)
-
-    @classmethod
-    def from_reference_kwargs(cls, kw):
-        """A ``_SpeciesType`` keyword set (species.py:90-99) for intracellular calcium."""
-        kw = dict(kw)
-        if str(kw.pop("name", "")).lower() != "ca":
-            raise NotImplementedError("only intracellular calcium has a device path")
-        if kw.pop("inside_global_constant", True):
-            raise NotImplementedError("a global-constant species has nothing to advance")
-        D = float(kw.pop("diffusivity", 0.0))
-        c0 = float(kw.pop("inside_initial_concentration", 0.0))
-        for ignored in ("charge", "reversal_potential", "outside_initial_concentration",
-                        "outside_global_constant", "decay_period"):
-            kw.pop(ignored, None)
-        if kw:
-            raise NotImplementedError(f"species keywords without a device path: {sorted(kw)}")
-        return cls(diffusivity=D, initial=c0, na_fraction=0.0, pump=False)
 
     # -------------------------------------------------------------- pump
     def generator(self, c):

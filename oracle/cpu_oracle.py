@@ -144,3 +144,20 @@ class CpuOracle:
 
     def threads(self):
         return int(self.lib.oracle_threads())
+
+
+def lump(P, parent, tol, explore_factor=1e-2):
+    """Lumped pruning of one neuron's dense propagator in C (oracle_lump in
+    oracle/cpu_step.c; the same walk as reference_step.lump_and_conserve).
+    Returns a dense array."""
+    lib = ctypes.CDLL(build())
+    lib.oracle_lump.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_void_p]
+    lib.oracle_lump.restype = ctypes.c_int
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    parent = np.ascontiguousarray(parent, dtype=np.int64)
+    out = np.empty_like(P)
+    rc = lib.oracle_lump(_p(P), _p(parent), len(parent), float(tol), float(explore_factor), _p(out))
+    if rc != 0:
+        raise MemoryError("oracle_lump: scratch allocation failed")
+    return out

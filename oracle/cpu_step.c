@@ -174,3 +174,74 @@ int oracle_threads(void) {
     return 1;
 #endif
 }
+
+/*
+ * Lumped pruning of one neuron's dense propagator P (n x n, row-major; parent[i]
+ * = parent within the neuron or -1), the restatement in
+ * oracle/reference_step.py: lump_and_conserve in C: walking the tree outward
+ * from row i's segment, expanding nodes whose |P_iu| reaches tol *
+ * explore_factor, a visited entry below tol is added to the nearest kept entry
+ * on the path back to i; what the walk never reaches goes to the diagonal.
+ * Neighbours are pushed children first (creation order), then the parent, and
+ * popped last-in first-out, as the restatement does.  out (n x n) is
+ * overwritten.  Returns 0, or -1 when a scratch allocation fails.
+ */
+int oracle_lump(const double* P, const int64_t* parent, int64_t n, double tol, double explore_factor,
+                double* out) {
+    int64_t* child_ptr = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+    int64_t* child = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+    if (!child_ptr || !child) { free(child_ptr); free(child); return -1; }
+    for (int64_t c = 0; c < n; ++c)
+        if (parent[c] >= 0) child_ptr[parent[c] + 1]++;
+    for (int64_t u = 0; u < n; ++u) child_ptr[u + 1] += child_ptr[u];
+    {
+        int64_t* fill = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+        if (!fill) { free(child_ptr); free(child); return -1; }
+        for (int64_t u = 0; u < n; ++u) fill[u] = child_ptr[u];
+        for (int64_t c = 0; c < n; ++c)
+            if (parent[c] >= 0) child[fill[parent[c]]++] = c;
+        free(fill);
+    }
+    const double explore = tol * explore_factor;
+    int failed = 0;
+#pragma omp parallel
+    {
+        /* (node, came from, nearest kept toward i); a tree node is reached once per row. */
+        int64_t* stack = (int64_t*)malloc((size_t)3 * (size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+        if (!stack) {
+#pragma omp atomic write
+            failed = 1;
+        }
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t i = 0; i < n; ++i) {
+            if (!stack) continue;
+            const double* row = P + i * n;
+            double* o = out + i * n;
+            double total = 0.0, kept = 0.0;
+            for (int64_t u = 0; u < n; ++u) { total += row[u]; o[u] = 0.0; }
+            int64_t top = 0;
+            stack[0] = i; stack[1] = -1; stack[2] = i; top = 1;
+            while (top > 0) {
+                --top;
+                const int64_t u = stack[3 * top], w = stack[3 * top + 1];
+                int64_t t = stack[3 * top + 2];
+                const double v = row[u];
+                if (fabs(v) >= tol || u == i) { o[u] += v; t = u; }
+                else o[t] += v;
+                if (fabs(v) < explore && u != i) continue;
+                for (int64_t k = child_ptr[u]; k < child_ptr[u + 1]; ++k) {
+                    const int64_t x = child[k];
+                    if (x != w) { stack[3 * top] = x; stack[3 * top + 1] = u; stack[3 * top + 2] = t; ++top; }
+                }
+                const int64_t p = parent[u];
+                if (p >= 0 && p != w) { stack[3 * top] = p; stack[3 * top + 1] = u; stack[3 * top + 2] = t; ++top; }
+            }
+            for (int64_t u = 0; u < n; ++u) kept += o[u];
+            o[i] += total - kept;
+        }
+        free(stack);
+    }
+    free(child_ptr);
+    free(child);
+    return failed ? -1 : 0;
+}

@@ -164,7 +164,7 @@ class HHInstances:
         self.g = {"na": np.zeros(m), "k": np.zeros(m), "l": np.zeros(m)}
 
     def zero_accumulators(self):
-        """species.py:251-253 (nonspecific conductances reset before mechanisms run)."""
+        """species.py:252-254 (nonspecific conductances reset before mechanisms run)."""
         for g in self.g.values():
             g.fill(0.0)
 
@@ -185,12 +185,16 @@ class KineticInstances:
     """Instances of one lti_sim kinetic mechanism, stepped as the kernel that
     neuwon/rxd/lti_sim/codegen.py:39-106 generates, with its conductance
     gbar*magnitude*(open states) written by the BREAKPOINT block after the
-    LTI call (nmodl/__init__.py:415-429) as a nonspecific conductance.
+    LTI call (nmodl/__init__.py:415-429): into the accumulator of its ion's
+    species (``species`` = the species name, USEION, nmodl/__init__.py:168-208;
+    ``erev`` unused) or, with ``species`` None, as a nonspecific conductance with
+    reversal potential ``erev``.
 
     ``layout`` is the flattened table [bucket][col][row][term] (codegen.py:29-37)."""
 
     def __init__(self, segment, g_coef, layout, vmin, bucket_frq, open_states, erev,
-                 conserve_sum, init_state):
+                 conserve_sum, init_state, species=None):
+        self.species = species
         self.segment = np.asarray(segment, dtype=np.int64)
         m = len(self.segment)
         self.g_coef = np.broadcast_to(np.asarray(g_coef, np.float64), (m,)).copy()
@@ -383,12 +387,17 @@ class OracleModel:
     ``duplicates='sum'`` adds every mechanism instance's conductance into its
     segment.  ``duplicates='numpy'`` reproduces the reference's fancy-index
     ``a[idx] += b`` (species.py:256-260), under which only one of several
-    instances on the same segment is counted.
+    instances on the same segment is counted (nonspecific conductances; species
+    accumulators are written per instance and count every one).
+
+    ``species`` maps electric species names to constant reversal potentials (mV),
+    in declaration order (the ``_SpeciesType`` accumulators, species.py:85-160);
+    ``kinetic`` is one ``KineticInstances`` or a list of them.
     """
 
     def __init__(self, parent, R, C, *, time_step=0.1, celsius=6.3, v_init=-70.0,
                  prune=EPSILON, propagator_matrix=None, hh=None, clamps=(),
-                 detectors=(), duplicates="sum", kinetic=None, synapses=None, calcium=None):
+                 detectors=(), duplicates="sum", kinetic=None, synapses=None, calcium=None, species=None):
         self.parent = np.asarray(parent, dtype=np.int64)
         self.n = len(self.parent)
         self.R = np.asarray(R, dtype=np.float64)
@@ -405,7 +414,13 @@ class OracleModel:
         self.P = propagator_matrix if propagator_matrix is not None else \
             propagator(self.parent, self.R, self.C, self.half_step, prune)
         self.hh = hh
-        self.kinetic = kinetic
+        self.kinetic = [] if kinetic is None else (list(kinetic) if isinstance(kinetic, (list, tuple)) else [kinetic])
+        self.species = dict(species or {})
+        # {name}_current / {name}_conductance segment accumulators (species.py:125-133).
+        self.species_current = {s: np.zeros(self.n) for s in self.species}
+        self.species_conductance = {s: np.zeros(self.n) for s in self.species}
+        for k in self.kinetic:
+            assert k.species is None or k.species in self.species, f"undeclared species {k.species}"
         self.synapses = synapses
         self.calcium = calcium
         self.clamps = [(int(s), float(a), int(f), int(k)) for (s, a, f, k) in clamps]
@@ -422,6 +437,13 @@ class OracleModel:
         self.sum_current[:] = self.nonspecific_current
         self.sum_conductance.fill(0.0)
         self.driving_voltage.fill(0.0)
+        # _SpeciesType._apply_accumulators (species.py:155-160), declared species
+        # first, then the nonspecific conductances the mechanisms registered.
+        for name, erev in self.species.items():
+            g = self.species_conductance[name]
+            self.sum_current += self.species_current[name]
+            self.sum_conductance += g
+            self.driving_voltage += g * erev
         if self.hh is not None:
             seg = self.hh.segment
             for ion in ("na", "k", "l"):
@@ -432,10 +454,15 @@ class OracleModel:
                 else:
                     np.add.at(self.sum_conductance, seg, g)
                     np.add.at(self.driving_voltage, seg, g * self.hh.E[ion])
-        if self.kinetic is not None:
-            k = self.kinetic
-            np.add.at(self.sum_conductance, k.segment, k.g)
-            np.add.at(self.driving_voltage, k.segment, k.g * k.erev)
+        for k in self.kinetic:
+            if k.species is not None:
+                continue
+            if self.duplicates == "numpy":
+                self.sum_conductance[k.segment] += k.g
+                self.driving_voltage[k.segment] += k.g * k.erev
+            else:
+                np.add.at(self.sum_conductance, k.segment, k.g)
+                np.add.at(self.driving_voltage, k.segment, k.g * k.erev)
         if self.synapses is not None:
             sy = self.synapses
             g = sy.conductance(self.voltage)
@@ -472,9 +499,14 @@ class OracleModel:
         if self.hh is not None:
             self.hh.zero_accumulators()
             self.hh.advance(self.voltage, self.time_step, self.celsius)
-        if self.kinetic is not None:
-            self.kinetic.zero_accumulators()
-            self.kinetic.advance(self.voltage)
+        for acc in list(self.species_current.values()) + list(self.species_conductance.values()):
+            acc.fill(0.0)                                   # species.py:147-153
+        for k in self.kinetic:
+            k.zero_accumulators()
+            k.advance(self.voltage)
+            if k.species is not None:
+                # self.segment.{ion}_conductance += g, one instance at a time.
+                np.add.at(self.species_conductance[k.species], k.segment, k.g)
         if self.synapses is not None:
             self.synapses.advance(self.steps)
         if self.calcium is not None:

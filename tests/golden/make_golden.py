@@ -9,8 +9,9 @@ The reference imports four third-party packages that are absent here
 (numba, graph_algorithms, matplotlib, BlueBrain nmodl).  They are replaced by
 import-only stubs written to a temporary directory: numba's ``njit`` becomes
 the identity and ``prange`` becomes ``range`` (so the reference's ``@Compute``
-kernels run as plain Python), ``topological_sort`` is a ten-line DFS, and the
-rest are empty modules.  None of them is on the computed path except the
+kernels run as plain Python; ``from_dtype`` gives the dtype's name, which is what the
+host entry point needs to allocate local arrays), ``topological_sort`` is a ten-line
+DFS, and the rest are empty modules.  None of them is on the computed path except the
 identity JIT.
 
 Because the NMODL parser is absent, the Hodgkin-Huxley channel is inserted
@@ -42,6 +43,11 @@ STUBS = {
         jit = njit
         prange = range
         cuda = None
+        def from_dtype(dtype):
+            # The type's name: the host entry point allocates local arrays with
+            # numpy.empty(size, dtype=numpy.<name>) (database/compute.py:317).
+            import numpy
+            return numpy.dtype(dtype).name
     """,
     "graph_algorithms/__init__.py": """
         def topological_sort(nodes, dependencies):
@@ -96,6 +102,8 @@ def install_stubs():
     sys.path.insert(0, REFERENCE)
     sys.path.insert(0, root)
     sys.path.insert(0, REPO)
+    if not hasattr(np, "product"):
+        np.product = np.prod            # removed in numpy 2; used by lti_sim/approx.py:78, 81
 
 
 def make_hh(gnabar=.12, gkbar=.036, glbar=.0003, ena=60., ek=-88., el=-54.3):
@@ -171,6 +179,202 @@ def make_hh(gnabar=.12, gkbar=.036, glbar=.0003, ena=60., ek=-88., el=-54.3):
             self.segment = segment
             self.magnitude = magnitude * segment.surface_area
     return hh
+
+
+def make_kinetic(name, scheme, ion, gbar, num_buckets, v_init, record):
+    """Developers-API kinetic channel whose step is the reference's own lti_sim
+    output: LTI_Model + MatrixSamples + Approx1D build the table (seeded numpy RNG),
+    Codegen._kernel emits the run-time kernel, and the advance method calls it and
+    adds gbar * 1e-8 * magnitude * (open states) to the segment's {ion}_conductance
+    accumulator, as the NMODL front end compiles a KINETIC mechanism
+    (nmodl/__init__.py:298-306, 415-432).  The derivative is this package's
+    restatement of the .mod file's KINETIC block (the NMODL parser is absent).
+    record(key, value) receives the table, its sample inputs and the initial state."""
+    from neuwon.rxd.mechanisms import Mechanism
+    from neuwon.database import Compute
+    from neuwon.rxd.lti_sim import LTI_Model, LinearInput
+    from neuwon.rxd.lti_sim.approx import Approx1D, MatrixSamples
+    from neuwon.rxd.lti_sim.codegen import Codegen
+    from neuwon.rxd.nmodl.code_gen import exec_string
+
+    class kinetic(Mechanism):
+        __slots__ = ()
+
+        @classmethod
+        def initialize(cls, model):
+            db = model.get_database()
+            celsius = model.get_temperature()
+            dt = model.get_time_step()
+
+            def derivative(v, *state):
+                return list(scheme.matrix([v], celsius)[0] @ np.array(state))
+            inp = LinearInput('v', 'self.segment.voltage', -100, 100, initial=v_init)
+            lti = LTI_Model(name, [inp], scheme.states, derivative, 1.0, dt)
+            inp.set_num_buckets(num_buckets)
+            samples = MatrixSamples(lti)
+            approx = Approx1D(samples, 1)
+            cg = Codegen.__new__(Codegen)              # Codegen.__init__ minus its timing run
+            cg.model, cg.table, cg.polynomial, cg.target = lti, approx.table, approx.polynomial, 'host'
+            cg.name, cg.inputs, cg.input_names = lti.name, lti.inputs, lti.input_names
+            cg.state_names, cg.num_states, cg.conserve_sum = lti.state_names, lti.num_states, lti.conserve_sum
+            cg.initial_state = lti.get_initial_state()
+            table_data = cg._table_data()
+            init = cg.initial_state
+            record("table", np.asarray(table_data, dtype=np.float64).reshape(num_buckets, lti.num_states,
+                                                                                lti.num_states, -1))
+            record("samples", samples.inputs[0])
+            record("init", np.array([init[s] for s in scheme.states]))
+            data = db.add_class(cls)
+            data.add_attribute('segment', dtype='Segment')
+            data.add_attribute('magnitude', units='um2')
+            for s in scheme.states:
+                data.add_attribute(s, init[s])
+            cls_ = data.get_instance_type()
+            opened = " + ".join(f"self.{scheme.states[k]}" for k in scheme.open_states)
+            # The NMODL front end emits one advance that calls the generated kernel
+            # (nmodl/__init__.py:415-429); the reference's JIT does not pass that
+            # kernel's local arrays (its Alloc annotations) through a nested call
+            # (NameError at run time), so the kernel and the conductance write run
+            # as two methods over all instances, in that order.
+            src = (cg._kernel() + "\n"
+                   "@Compute\n"
+                   "def write_conductance(self):\n"
+                   f"    self.segment.{ion}_conductance += {gbar * 1e-8!r} * self.magnitude * ({opened})\n")
+            scope = {"Compute": Compute, "table": table_data, "numpy": np}
+            exec_string(src, scope)
+            lti_step = data.add_method(scope[f"{name}_advance"])
+            write = data.add_method(scope["write_conductance"])
+
+            def advance():
+                lti_step()
+                write()
+            cls_.advance = staticmethod(advance)
+            return cls_
+
+        @classmethod
+        def get_name(cls):
+            return name
+
+        def __init__(self, segment, outside=None, magnitude=1.0):
+            self.segment = segment
+            self.magnitude = magnitude * segment.surface_area
+    kinetic.__name__ = kinetic.__qualname__ = name        # the database class is named after it
+    return kinetic
+
+
+def run_species(out):
+    """Electric species (constant reversal potentials) fed by two kinetic channels of
+    the reference library, Nav1.1 -> na and Kv1.1 -> k (tables and kernels from the
+    reference's lti_sim), plus the restated hh with weaker sodium and potassium, on
+    two neurons; a second Nav1.1 instance on two segments (a species accumulator
+    counts both).  Records traces, spikes and each channel's table."""
+    from neuwon.rxd.rxd_model import RxD_Model
+    from neuwon_gb300.kinetic import kv11, nav11
+    from neuwon_gb300.morphology import random_tree
+    np.random.seed(4321)
+    spec = dict(time_step=0.1, celsius=6.3, t_stop=25.0, v_init=-70.0,
+                hh=dict(gnabar=0.12, gkbar=0.036, glbar=0.0003, ena=50.0, ek=-77.0, el=-54.3),
+                nav=dict(gbar=0.03, buckets=2000), kv=dict(gbar=0.01, buckets=2000))
+    rec = {}
+    mechs = [make_hh(**spec["hh"]),
+             make_kinetic("na11a", nav11(), "na", spec["nav"]["gbar"], spec["nav"]["buckets"], spec["v_init"],
+                          lambda k, v: rec.__setitem__("nav_" + k, v)),
+             make_kinetic("Kv11_6States_temperature2", kv11(), "k", spec["kv"]["gbar"], spec["kv"]["buckets"],
+                          spec["v_init"], lambda k, v: rec.__setitem__("kv_" + k, v))]
+    m = RxD_Model(time_step=spec["time_step"], temperature=spec["celsius"], initial_voltage=spec["v_init"],
+                  species=[dict(name="na", charge=1, reversal_potential=50.0),
+                           dict(name="k", charge=1, reversal_potential=-77.0)],
+                  mechanisms=mechs)
+    trees = [random_tree(80, seed=31), random_tree(50, seed=32)]
+    all_segs = [build_reference_tree(m, t) for t in trees]
+    flat = [s for segs in all_segs for s in segs]
+    hh, nav, kv = (m.mechanisms[n] for n in ("hh", "na11a", "Kv11_6States_temperature2"))
+    for s in flat:
+        hh(s)
+        nav(s)
+    for k, s in enumerate(flat):
+        if k % 7 != 3:                     # Kv1.1 on most segments only
+            kv(s)
+    dup = [5, 90]
+    for k in dup:
+        nav(flat[k])
+    clamps = [(0, 0, 0.5, 2.0, 15.0), (1, 0, 0.4, 4.0, 12.0)]
+    probes = [0, 10, 40, 79, 80, 100, 129]
+    trace = [np.array([flat[p].voltage for p in probes])]
+    ap = []
+    steps = int(round(spec["t_stop"] / spec["time_step"]))
+    for k in range(steps):
+        for (t, s, nA, start, dur) in clamps:
+            if m.clock.is_now(start):
+                all_segs[t][s].inject_current(nA, dur)
+        m.advance()
+        trace.append(np.array([flat[p].voltage for p in probes]))
+        ap.append(np.array(m.database.get_data("Neuron.AP_detected"), dtype=bool).copy())
+        if k + 1 in (100, 250):
+            out[f"species_snap{k + 1}"] = seg_array(m, "voltage")
+            out[f"species_gna_snap{k + 1}"] = seg_array(m, "na_conductance")
+            out[f"species_gk_snap{k + 1}"] = seg_array(m, "k_conductance")
+    # Each channel's sample points and initial state in full; of its table every
+    # 10th bucket (the full table is rebuilt from the sample points and checked
+    # against these buckets).
+    for key in ("nav", "kv"):
+        out[f"species_{key}_samples"] = rec[f"{key}_samples"]
+        out[f"species_{key}_init"] = rec[f"{key}_init"]
+        out[f"species_{key}_table10"] = rec[f"{key}_table"][::10]
+    out["species_trace"] = np.array(trace)
+    out["species_probes"] = np.asarray(probes, dtype=np.int64)
+    out["species_ap"] = np.array(ap)
+    out["species_kv_skip"] = np.array([k for k in range(len(flat)) if k % 7 == 3], dtype=np.int64)
+    out["species_dup"] = np.asarray(dup, dtype=np.int64)
+    out["species_clamps"] = np.array(clamps, dtype=np.float64)
+    out["species_meta"] = np.array([spec["time_step"], spec["celsius"], spec["t_stop"], spec["v_init"],
+                                    spec["hh"]["gnabar"], spec["hh"]["gkbar"], spec["hh"]["glbar"],
+                                    spec["hh"]["ena"], spec["hh"]["ek"], spec["hh"]["el"],
+                                    spec["nav"]["gbar"], spec["kv"]["gbar"], 50.0, -77.0])
+
+
+def run_dropin(out, prefix, tree, clamps, hh_kwargs, t_stop, insert_as_created):
+    """The drop-in backend's view of a reference model: neuwon_gb300.dropin.extract
+    (the arrays GB300Advance reads from the reference's Database after db.sort())
+    at time 0, and before every step the device clamps clamp_players derives from
+    the reference's own input-clock players, while the reference advances itself;
+    plus the reference's voltages of every segment after every step."""
+    from neuwon.rxd.rxd_model import RxD_Model
+    from neuwon_gb300.dropin import clamp_players, extract
+    m = RxD_Model(time_step=0.1, temperature=6.3, mechanisms=[make_hh(**hh_kwargs)])
+    hh = m.mechanisms["hh"]
+    segs = []
+    for i in range(len(tree)):
+        p = int(tree.parent[i])
+        xyz = [float(x) for x in tree.coordinates[i]]
+        d = float(tree.diameter[i])
+        segs.append(m.Neuron(xyz, d).root if p < 0 else m.Segment(segs[p], xyz, d))
+        if insert_as_created:
+            hh(segs[-1])
+    if not insert_as_created:
+        for s in segs:
+            hh(s)
+    dens = {"hh": {k: hh_kwargs.get(k, d) for k, d in (("gnabar", .12), ("gkbar", .036), ("glbar", .0003))}}
+    arrays = extract(m, dens)
+    for key in ("parent", "neuron_start", "capacitance", "axial_resistance", "voltage"):
+        out[f"{prefix}_{key}"] = arrays[key]
+    for key in ("segment", "magnitude", "m", "h", "n"):
+        out[f"{prefix}_hh_{key}"] = arrays["hh"][key]
+    h = arrays["hh"]
+    out[f"{prefix}_meta"] = np.array([arrays["time_step"], arrays["celsius"], h["gnabar"], h["gkbar"], h["glbar"],
+                                      h["ena"], h["ek"], h["el"]])
+    steps = int(round(t_stop / 0.1))
+    played, volts = [], [seg_array(m, "voltage")]
+    for k in range(steps):
+        for (s, nA, start, dur) in clamps:
+            if m.clock.is_now(start):
+                segs[s].inject_current(nA, dur)
+        for c in clamp_players(m, 2 * k):
+            played.append((k,) + c)
+        m.advance()
+        volts.append(seg_array(m, "voltage"))
+    out[f"{prefix}_clamps"] = np.array(played, dtype=np.float64).reshape(-1, 5)
+    out[f"{prefix}_volts"] = np.array(volts)
 
 
 def build_reference_tree(model, tree):
@@ -297,49 +501,83 @@ def run_lti(out):
     out["lti_v"], out["lti_state"], out["lti_new"] = v, st, np.array(new)
 
 
-def main():
-    install_stubs()
+def scenarios():
+    """Fixture groups by key prefix, each a function of the output dict."""
     from neuwon_gb300.morphology import random_tree, Tree
-    out = {}
-    run_geometry_and_propagator(out)
 
-    # (1) The reference test's 11-segment HH scenario (test_model.py:35-66).
-    coords = [[-1, 0, 7]] + [[x, 0, 7] for x in range(10)]
-    t11 = Tree([-1] + list(range(10)), coords, [5.7] + [1.0] * 10)
-    run_hh_tree(out, "hh11", [t11], time_step=0.1, celsius=6.3, t_stop=20.0,
-                clamps=[(0, 0, .1, 5.0, 1.0), (0, 0, .1, 15.0, 1.0)],
-                hh_kwargs={}, probes=list(range(11)), snapshots={100, 200}, insert_as_created=True)
+    def hh11(out):
+        # The reference test's 11-segment HH scenario (test_model.py:35-66).
+        coords = [[-1, 0, 7]] + [[x, 0, 7] for x in range(10)]
+        t11 = Tree([-1] + list(range(10)), coords, [5.7] + [1.0] * 10)
+        run_hh_tree(out, "hh11", [t11], time_step=0.1, celsius=6.3, t_stop=20.0,
+                    clamps=[(0, 0, .1, 5.0, 1.0), (0, 0, .1, 15.0, 1.0)],
+                    hh_kwargs={}, probes=list(range(11)), snapshots={100, 200}, insert_as_created=True)
 
-    # (2) A 200-segment tree, workload parameters of the single-neuron config.
-    t200 = random_tree(200, seed=11)
-    run_hh_tree(out, "hh200", [t200], time_step=0.1, celsius=6.3, t_stop=30.0,
-                clamps=[(0, 0, 0.2, 5.0, 20.0)],
-                hh_kwargs=dict(ena=50.0, ek=-77.0, el=-54.3),
-                probes=[0, 1, 50, 100, 150, 199], snapshots={100, 300})
+    def hh200(out):
+        # A 200-segment tree, workload parameters of the single-neuron config.
+        run_hh_tree(out, "hh200", [random_tree(200, seed=11)], time_step=0.1, celsius=6.3, t_stop=30.0,
+                    clamps=[(0, 0, 0.2, 5.0, 20.0)],
+                    hh_kwargs=dict(ena=50.0, ek=-77.0, el=-54.3),
+                    probes=[0, 1, 50, 100, 150, 199], snapshots={100, 300})
 
-    # (3) Three neurons (block-diagonal propagator), clamps on different segments,
-    #     plus a second hh instance on two segments (reference drops duplicates).
-    ts = [random_tree(40, seed=21), random_tree(25, seed=22), random_tree(60, seed=23)]
-    run_hh_tree(out, "multi", ts, time_step=0.1, celsius=6.3, t_stop=15.0,
-                clamps=[(0, 0, 0.3, 1.0, 6.0), (1, 5, 0.2, 2.0, 3.0), (2, 30, 0.25, 0.5, 8.0)],
-                hh_kwargs=dict(ena=50.0, ek=-77.0),
-                probes=[0, 10, 40, 45, 65, 95, 124], snapshots={150},
-                duplicate_segments=[(0, 3), (2, 30)])
+    def multi(out):
+        # Three neurons (block-diagonal propagator), clamps on different segments,
+        # plus a second hh instance on two segments (reference drops duplicates).
+        ts = [random_tree(40, seed=21), random_tree(25, seed=22), random_tree(60, seed=23)]
+        run_hh_tree(out, "multi", ts, time_step=0.1, celsius=6.3, t_stop=15.0,
+                    clamps=[(0, 0, 0.3, 1.0, 6.0), (1, 5, 0.2, 2.0, 3.0), (2, 30, 0.25, 0.5, 8.0)],
+                    hh_kwargs=dict(ena=50.0, ek=-77.0),
+                    probes=[0, 10, 40, 45, 65, 95, 124], snapshots={150},
+                    duplicate_segments=[(0, 3), (2, 30)])
 
-    # (4) The single-neuron configuration at full size: 2,000 segments (seed 0),
-    #     HH everywhere, 0.2 nA soma clamp 5-80 ms, dt 0.1 ms for 100 ms, the
-    #     reference's own epsilon-pruned propagator.  All segment voltages every
-    #     100 steps.
-    t2000 = random_tree(2000, seed=0)
-    run_hh_tree(out, "c1", [t2000], time_step=0.1, celsius=6.3, t_stop=100.0,
-                clamps=[(0, 0, 0.2, 5.0, 75.0)],
-                hh_kwargs=dict(ena=50.0, ek=-77.0, el=-54.3),
-                probes=[0, 1, 500, 1000, 1500, 1999],
-                snapshots={100 * i for i in range(1, 11)})
+    def c1(out):
+        # The single-neuron configuration at full size: 2,000 segments (seed 0), HH
+        # everywhere, 0.2 nA soma clamp 5-80 ms, dt 0.1 ms for 100 ms, the reference's
+        # own epsilon-pruned propagator.  All segment voltages every 100 steps.
+        run_hh_tree(out, "c1", [random_tree(2000, seed=0)], time_step=0.1, celsius=6.3, t_stop=100.0,
+                    clamps=[(0, 0, 0.2, 5.0, 75.0)],
+                    hh_kwargs=dict(ena=50.0, ek=-77.0, el=-54.3),
+                    probes=[0, 1, 500, 1000, 1500, 1999],
+                    snapshots={100 * i for i in range(1, 11)})
 
-    run_lti(out)
+    def dropin(out):
+        # The drop-in backend's arrays and clamps, read live from the reference:
+        # the 11-segment cable (instances inserted as segments are created) and a
+        # 200-segment tree.
+        coords = [[-1, 0, 7]] + [[x, 0, 7] for x in range(10)]
+        t11 = Tree([-1] + list(range(10)), coords, [5.7] + [1.0] * 10)
+        run_dropin(out, "dropin_hh11", t11, [(0, .1, 5.0, 1.0), (0, .1, 15.0, 1.0)], {}, 20.0, True)
+        run_dropin(out, "dropin_hh200", random_tree(200, seed=11), [(0, 0.2, 5.0, 20.0)],
+                   dict(ena=50.0, ek=-77.0, el=-54.3), 30.0, False)
 
+    return {"geom": run_geometry_and_propagator, "hh11": hh11, "hh200": hh200, "multi": multi, "c1": c1,
+            "lti": run_lti, "species": run_species, "dropin": dropin}
+
+
+def main():
+    """make_golden.py <reference checkout> [--only name,name]: with --only, the named
+    groups are regenerated and merged into the existing fixture file."""
+    args = sys.argv[1:]
+    only = None
+    if "--only" in args:
+        k = args.index("--only")
+        only = args[k + 1].split(",")
+        del args[k:k + 2]
+    global REFERENCE
+    REFERENCE = reference_path(args)
+    install_stubs()
     path = os.path.join(HERE, "reference_fixtures.npz")
+    groups = scenarios()
+    out = {}
+    if only:
+        prefixes = {"geom": ("geom_", "prop_")}
+        with np.load(path) as old:
+            for key in old.files:
+                if not any(key.startswith(p) for g in only for p in prefixes.get(g, (g + "_",))):
+                    out[key] = old[key]
+    for name, fn in groups.items():
+        if only is None or name in only:
+            fn(out)
     np.savez_compressed(path, **out)
     print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
 

@@ -38,6 +38,120 @@ def kinetic_oracle(seg, area, time_step, celsius, gbar=0.012, erev=50.0, v_init=
                             sch.open_states, erev, sch.conserve_sum, init)
 
 
+def species_spec(fx):
+    """The species scenario recorded from the reference (make_golden.run_species)."""
+    meta = fx["species_meta"]
+    return dict(time_step=float(meta[0]), celsius=float(meta[1]), t_stop=float(meta[2]), v_init=float(meta[3]),
+                hh=dict(gnabar=meta[4], gkbar=meta[5], glbar=meta[6], ena=meta[7], ek=meta[8], el=meta[9]),
+                nav_gbar=float(meta[10]), kv_gbar=float(meta[11]),
+                species={"na": float(meta[12]), "k": float(meta[13])},
+                trees=[random_tree(80, seed=31), random_tree(50, seed=32)],
+                clamps=[(int(t), int(s), nA, start, dur) for t, s, nA, start, dur in fx["species_clamps"]],
+                probes=fx["species_probes"], dup=fx["species_dup"], kv_skip=fx["species_kv_skip"])
+
+
+def species_tables(fx):
+    """The reference's Nav1.1 and Kv1.1 tables, rebuilt by this package's host table
+    builder from the reference's own random sample points (equal to the reference's
+    tables to 1e-12: tests/test_species.py), with the reference's initial states."""
+    from neuwon_gb300.kinetic import LTITable, kv11, nav11
+    meta = fx["species_meta"]
+    out = {}
+    for key, factory in (("nav", nav11), ("kv", kv11)):
+        tbl = LTITable(factory(), float(meta[0]), float(meta[1]), -100.0, 100.0, 2000, 1,
+                       sample_inputs=fx[f"species_{key}_samples"])
+        out[key] = (tbl.layout, fx[f"species_{key}_init"])
+    return out
+
+
+def species_instances(spec):
+    """Segments of the Nav1.1 instances (every segment, then the duplicates) and of the
+    Kv1.1 instances (all but the skipped segments), in registration order."""
+    n = sum(len(t) for t in spec["trees"])
+    nav = np.concatenate([np.arange(n), spec["dup"]]).astype(np.int64)
+    kv = np.setdiff1d(np.arange(n), spec["kv_skip"]).astype(np.int64)
+    return nav, kv
+
+
+def species_oracle(fx, tables=None):
+    """Oracle of the species scenario: HH + Nav1.1 (-> na) + Kv1.1 (-> k) with the
+    reference's tables and initial states (or ``tables`` = {"nav": (layout, init),
+    "kv": (layout, init)})."""
+    from oracle.reference_step import KineticInstances
+    spec = species_spec(fx)
+    parent, R, C, area, offs = concat(spec["trees"])
+    n = len(parent)
+    hh = HHInstances(np.arange(n), area, celsius=spec["celsius"], v_init=spec["v_init"],
+                     **{k: float(v) for k, v in spec["hh"].items()})
+    nav_seg, kv_seg = species_instances(spec)
+    tables = tables or species_tables(fx)
+    frq = 2000 / 200.0
+    nav = KineticInstances(nav_seg, spec["nav_gbar"] * 1e-8 * area[nav_seg], tables["nav"][0], -100.0, frq, [2, 3],
+                           0.0, 1.0, tables["nav"][1], species="na")
+    kv = KineticInstances(kv_seg, spec["kv_gbar"] * 1e-8 * area[kv_seg], tables["kv"][0], -100.0, frq, [1],
+                          0.0, 1.0, tables["kv"][1], species="k")
+    cl = []
+    for (ti, s, nA, start, dur) in spec["clamps"]:
+        f, c = clamp_ticks(start, dur, spec["time_step"])
+        cl.append((offs[ti] + s, nA * 1e-9, f, c))
+    om = OracleModel(parent, R, C, time_step=spec["time_step"], celsius=spec["celsius"], v_init=spec["v_init"],
+                     hh=hh, kinetic=[nav, kv], species=spec["species"], clamps=cl,
+                     detectors=[(o, 20.0) for o in offs])
+    return om, spec
+
+
+def install_propagator(m, P, fmt=2):
+    """Replace a synced model's propagator by P (scipy CSR over creation indices,
+    e.g. the oracle's), permuted to the device's segment order."""
+    import ctypes
+    import scipy.sparse
+    from neuwon_gb300 import _lib
+    Pd = scipy.sparse.csr_matrix(P)[m._order][:, m._order].tocsr()
+    Pd.sort_indices()
+    rowptr = np.ascontiguousarray(Pd.indptr, dtype=np.int64)
+    col = np.ascontiguousarray(Pd.indices, dtype=np.int64)
+    val = np.ascontiguousarray(Pd.data, dtype=np.float64)
+    m._ctx.call("nw_propagator_set_csr", m._n, _lib.ptr(rowptr), _lib.ptr(col), _lib.ptr(val), len(val))
+    m._ctx.set_option("propagator_format", fmt)
+
+
+def species_gpu(fx, precision="f64", path="batched", reference_tables=True, tolerance=None, propagator=None):
+    """The species scenario through the public API: species declared with their
+    reversal potentials, hh + Nav11 + Kv11 mechanisms.  propagator (scipy CSR over
+    creation indices) replaces the one the model builds."""
+    import neuwon_gb300 as nw
+    spec = species_spec(fx)
+    extra = {}
+    if reference_tables:
+        tables = species_tables(fx)
+        nav_kw, kv_kw = dict(table=tables["nav"][0]), dict(table=tables["kv"][0])
+    else:
+        nav_kw, kv_kw = {}, {}
+    if tolerance is not None:
+        extra = dict(propagator_tolerance=tolerance, propagator_conserve=True)
+    m = nw.RxD_Model(time_step=spec["time_step"], temperature=spec["celsius"], initial_voltage=spec["v_init"],
+                     precision=precision, path=path,
+                     species=[dict(name=k, charge=1, reversal_potential=v) for k, v in spec["species"].items()],
+                     mechanisms=[nw.HH.configure(**{k: float(v) for k, v in spec["hh"].items()}),
+                                 nw.Nav11.configure(gbar=spec["nav_gbar"], **nav_kw),
+                                 nw.Kv11.configure(gbar=spec["kv_gbar"], **kv_kw)], **extra)
+    offs = np.cumsum([0] + [len(t) for t in spec["trees"]])[:-1]
+    for t in spec["trees"]:
+        m.add_tree(t)
+    m.insert_everywhere("hh")
+    m.insert_everywhere("na11a")
+    nav_seg, kv_seg = species_instances(spec)
+    for s in nav_seg[len(nav_seg) - len(spec["dup"]):]:
+        m.mechanisms["na11a"](nw.Segment(m, int(s)))
+    for s in kv_seg:
+        m.mechanisms["Kv11_6States_temperature2"](nw.Segment(m, int(s)))
+    recs = [nw.TimeSeries().record(nw.Segment(m, int(p)), "voltage") for p in spec["probes"]]
+    if propagator is not None:
+        m._sync()
+        install_propagator(m, propagator)
+    return m, spec, offs, recs
+
+
 def oracle_case(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(),
                 duplicates="sum", prune=None, insert_as_created=False, kinetic=False):
     """clamps: [(tree, seg, nA, start_ms, dur_ms)]; dups: [(tree, seg)] extra hh instances.
@@ -66,11 +180,12 @@ def oracle_case(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(
 
 def gpu_model(trees, clamps, *, time_step=0.1, celsius=6.3, hh_kw=None, dups=(), precision="f32",
               path="batched", tolerance=None, probes=(), insert_as_created=False, kinetic=False,
-              conserve=False, fmt="rows"):
+              conserve=False, fmt="rows", duplicates="sum"):
     """The same case through the public RxD_Model API."""
     import neuwon_gb300 as nw
     hh_kw = dict(hh_kw or {})
     kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
+    kw["duplicates"] = duplicates
     if conserve == "lump":
         kw["propagator_lump"] = True
     elif conserve:

@@ -49,8 +49,23 @@ def test_diffusion_conserves_calcium():
 
 
 def test_reference_species_keywords():
-    ca = nw.Calcium.from_reference_kwargs(dict(name="ca", charge=2, diffusivity=0.6,
-                                               inside_initial_concentration=1e-4, inside_global_constant=False))
+    """The _SpeciesType keywords (species.py:90-142): every one is kept or refused, none dropped."""
+    from neuwon_gb300.species import SpeciesType
+    sp = SpeciesType(name="ca", charge=2, reversal_potential=120.0, diffusivity=0.6,
+                     inside_initial_concentration=1e-4, inside_global_constant=False)
+    assert sp.charge == 2 and sp.electric and sp.reversal_potential == 120.0
+    ca = sp.calcium
     assert ca.diffusivity == 0.6 and ca.initial == 1e-4 and not ca.pump
+    na = SpeciesType(name="na", charge=1, reversal_potential=50)
+    assert na.electric and na.reversal_potential == 50.0 and na.calcium is None
+    assert not SpeciesType(name="cl", charge=-1).electric
     with pytest.raises(NotImplementedError):
-        nw.Calcium.from_reference_kwargs(dict(name="na", inside_global_constant=False))
+        SpeciesType(name="na", inside_global_constant=False)
+    with pytest.raises(NotImplementedError):
+        SpeciesType(name="k", reversal_potential="nerst")
+    with pytest.raises(NotImplementedError):
+        SpeciesType(name="k", outside_global_constant=False)
+    with pytest.raises(NotImplementedError):
+        SpeciesType(name="ca", inside_global_constant=False, decay_period=10.0)
+    with pytest.raises(TypeError):
+        SpeciesType(name="k", bogus=1)

@@ -54,7 +54,7 @@ def test_subsets_duplicates_one_segment_neuron_and_many_clamps(path):
         if k % 10 == 9:
             worst = max(worst, np.abs(m.get_data("Segment.voltage") - om.voltage).max())
     assert worst < 1e-7, worst
-    assert np.abs(m.get_data("na8.state") - om.kinetic.state).max() < 1e-9
+    assert np.abs(m.get_data("na8.state") - om.kinetic[0].state).max() < 1e-9
     np.testing.assert_array_equal(m.get_data("Neuron.spike_count"), om.spike_count)
     m.close()
 

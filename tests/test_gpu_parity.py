@@ -299,7 +299,7 @@ def test_f64_hh_plus_na8_kinetic_matches_oracle(path):
             worst = max(worst, np.abs(m.get_data("Segment.voltage") - om.voltage).max())
     assert worst < 1e-7
     st = m.get_data("na8.state")
-    assert np.abs(st - om.kinetic.state).max() < 1e-9
+    assert np.abs(st - om.kinetic[0].state).max() < 1e-9
     np.testing.assert_array_equal(m.get_data("Neuron.spike_count"), om.spike_count)
     m.close()
 

@@ -222,7 +222,7 @@ def test_c_oracle_with_kinetic_matches_numpy_oracle():
                         [(0, 0, 0.3, 1., 10.), (1, 10, 0.25, 2., 5.)], hh_kw=dict(ena=50., ek=-77.),
                         kinetic=True)
     P = om.P
-    k = om.kinetic
+    k = om.kinetic[0]
     co = CpuOracle(P.indptr, P.indices, P.data, d["C"], time_step=0.1, celsius=6.3,
                    hh=dict(segment=d["seg"], gna=om.hh.gna_coef, gk=om.hh.gk_coef, gl=om.hh.gl_coef,
                            ena=50., ek=-77., el=-54.3),
@@ -234,7 +234,7 @@ def test_c_oracle_with_kinetic_matches_numpy_oracle():
         om.advance()
         co.advance()
     assert np.abs(om.voltage - co.V).max() < 1e-9
-    assert np.abs(om.kinetic.state - co.kstate.T).max() < 1e-12
+    assert np.abs(om.kinetic[0].state - co.kstate.T).max() < 1e-12
     np.testing.assert_array_equal(om.spike_count, co.spike_count)
 
 
@@ -286,3 +286,17 @@ def test_lumping_keeps_the_row_entry_at_any_tolerance():
     assert full.diagonal().max() < 0.9
     L = lump_and_conserve(full, parent, 0.9).toarray()
     assert np.abs(L - np.eye(len(L))).max() < 1e-13
+
+
+@pytest.mark.parametrize("tol", [1e-8, 3e-7, 1e-5])
+def test_c_lumping_matches_numpy_lumping(tol):
+    """The C walk the CPU baseline prunes with equals the oracle's lump_and_conserve."""
+    from oracle.cpu_oracle import lump
+    from oracle.reference_step import lump_and_conserve
+    t = random_tree(250, seed=5)
+    parent, R, C, area, offs = concat([t])
+    full = propagator(parent, R, C, 0.05, prune=0.0).toarray()
+    a = lump_and_conserve(full, parent, tol).toarray()
+    b = lump(full, parent, tol)
+    assert np.array_equal(a != 0, b != 0)
+    assert np.abs(a - b).max() < 1e-13

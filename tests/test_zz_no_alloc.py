@@ -82,7 +82,13 @@ def test_noalloc_half_step_matches_advance_on_two_calls():
         half_step(d["G0"] if k == 0 else d["G"], d["E0"] if k == 0 else d["E"])
         half_step(d["G"], d["E"])
         torch.cuda.synchronize()
-        assert torch.cuda.mem_get_info(0)[0] == free0     # nothing allocated by the two calls
+        used = free0 - torch.cuda.mem_get_info(0)[0]
+        if k == 0:
+            # With lazy module loading the first call loads the library's device code
+            # on this GPU, which creates the 8 MiB static scratch array (and no more).
+            assert 0 <= used <= (8 << 20) + (2 << 20)
+        else:
+            assert used == 0                              # nothing allocated by the two calls
         m.advance(1)
         want = m.get_data("Segment.voltage")              # creation order
         got = d["V"].cpu().numpy()[m._inv]
