@@ -105,12 +105,15 @@ def hh_steady_state(v, celsius=6.3):
     return m, h, n
 
 
-def NMODL(filename, use_cache=True):
-    """Minimal NMODL front end: maps a .mod file onto a GPU mechanism.
+def NMODL(filename, use_cache=True, **table):
+    """NMODL front end: maps a .mod file onto a GPU mechanism.
 
     The reference parses NMODL with BlueBrain's nmodl library
-    (neuwon/rxd/nmodl/parser.py); here only files whose SUFFIX has a device
-    kernel are accepted, and their PARAMETER defaults are read from the file.
+    (neuwon/rxd/nmodl/parser.py).  Here ``SUFFIX hh`` becomes the HH mechanism
+    with the file's PARAMETER defaults, and linear kinetic channels (KINETIC
+    block, ``SOLVE ... METHOD sparse``) and passive channels become ``Kinetic``
+    mechanisms through ``neuwon_gb300.nmodl`` (table keywords: vmin, vmax,
+    num_buckets, degree); other files raise.
     """
     filename = os.path.abspath(str(filename))
     with open(filename, "rt") as f:
@@ -127,4 +130,5 @@ def NMODL(filename, use_cache=True):
     if suffix == "hh":
         keep = {k: v for k, v in params.items() if k in ("gnabar", "gkbar", "glbar", "ena", "ek", "el")}
         return HH.configure(**keep)
-    raise NotImplementedError(f"{os.path.basename(filename)}: SUFFIX {suffix} has no GPU kernel in neuwon_gb300")
+    from .nmodl import kinetic_mechanism
+    return kinetic_mechanism(filename, text, **table)

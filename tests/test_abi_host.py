@@ -138,9 +138,14 @@ def test_nmodl_front_end_reads_hh_parameters(tmp_path):
     assert issubclass(cls, nw.HH)
     assert (cls.gnabar, cls.ek, cls.el) == (0.12, -88.0, -54.3)
     bad = tmp_path / "pas.mod"
-    bad.write_text("NEURON { SUFFIX pas NONSPECIFIC_CURRENT i }\n")
+    bad.write_text("NEURON { SUFFIX pas NONSPECIFIC_CURRENT i }\n")       # no density parameter
     with pytest.raises(NotImplementedError):
         nw.NMODL(str(bad))
+    ode = tmp_path / "ode.mod"
+    ode.write_text("NEURON { SUFFIX ode NONSPECIFIC_CURRENT i }\nPARAMETER { g = 1 (S/cm2) }\nSTATE { x }\n"
+                   "BREAKPOINT { SOLVE d METHOD cnexp  g = g*x }\nDERIVATIVE d { x' = -x }\n")
+    with pytest.raises(NotImplementedError, match="DERIVATIVE"):
+        nw.NMODL(str(ode))
 
 
 def test_user_python_mechanisms_are_rejected():

@@ -149,3 +149,47 @@ def test_duplicates_reference_mode_matches_reference_fixture(path):
         om.advance()
     assert np.abs(m.get_data("Segment.voltage") - om.voltage).max() > 1e-3    # the modes differ on this case
     m.close()
+
+
+def test_nmodl_channels_on_device_match_oracle(tmp_path):
+    """Channel files read by the NMODL front end (a three-state K channel feeding
+    species k, a passive leak) run on the device next to HH: FP64 against the
+    oracle holding the host build of the same tables, 1e-7 mV."""
+    from neuwon_gb300.kinetic import LTITable
+    from oracle.reference_step import HHInstances, KineticInstances, OracleModel, clamp_ticks
+    from tests.helpers import concat
+    from tests.test_nmodl import KTEST, PASSIVE
+    (tmp_path / "ktest.mod").write_text(KTEST)
+    (tmp_path / "leak.mod").write_text(PASSIVE)
+    tree = nw.random_tree(150, seed=3)
+    celsius, dt, steps = 6.3, 0.1, 300
+    hh_kw = dict(ena=50.0, ek=-77.0, el=-54.3)
+    m = nw.RxD_Model(time_step=dt, temperature=celsius, precision="f64",
+                     species=[dict(name="k", charge=1, reversal_potential=-80.0)],
+                     mechanisms=[nw.HH.configure(**hh_kw), str(tmp_path / "ktest.mod"), str(tmp_path / "leak.mod")])
+    nr = m.add_tree(tree)
+    for name in ("hh", "ktest", "leak"):
+        m.insert_everywhere(name)
+    nr.root.inject_current(0.3, 20.0)
+    parent, R, C, area, offs = concat([tree])
+    n = len(tree)
+    seg = np.arange(n)
+    kins = []
+    for name, species, erev in (("ktest", "k", 0.0), ("leak", None, m.mechanisms["leak"].erev)):
+        cls = m.mechanisms[name]
+        sch = cls.scheme_factory()
+        tbl = LTITable(sch, dt, celsius, -100.0, 100.0, 2000, 1)
+        kins.append(KineticInstances(seg, cls.gbar * 1e-8 * area, tbl.layout, -100.0, tbl.bucket_frq,
+                                     sch.open_states, erev, sch.conserve_sum, sch.steady_state(-70.0, celsius),
+                                     species=species))
+    f, c = clamp_ticks(0.0, 20.0, dt)
+    om = OracleModel(parent, R, C, time_step=dt, celsius=celsius, hh=HHInstances(seg, area, celsius=celsius, **hh_kw),
+                     kinetic=kins, species={"k": -80.0}, clamps=[(0, 0.3e-9, f, c)], detectors=[(0, 20.0)])
+    m.advance(steps)
+    for _ in range(steps):
+        om.advance()
+    assert np.abs(m.get_data("Segment.voltage") - om.voltage).max() < 1e-7
+    assert np.abs(m.get_data("ktest.state") - om.kinetic[0].state).max() < 1e-9
+    np.testing.assert_array_equal(m.get_data("Neuron.spike_count"), om.spike_count)
+    assert om.spike_count[0] >= 1
+    m.close()
