@@ -45,18 +45,14 @@ def algorithmic_bytes_per_segment_step(r, s_total=11, p_seg=5):
     return 2 * (8 * r + 4) + 4 * (2 + 2 * s_total + p_seg + 1)
 
 
-def format_bytes_per_segment_step(r_stored, prec=4, pairs=False, quads=False):
-    """Compulsory HBM bytes of this implementation's layout per segment-step:
-    per half step, (value + u16 column) per stored entry (pair format: per stored
-    pair), an 8 B row pointer, the leak (pairs: and c_max / c_i), V read + write,
-    kI and kG, HH gates (3) and coefficients (3), the na8 open state and
-    coefficient; per step the mechanism update reads V and reads + writes 3 HH
-    gates and 8 na8 states."""
-    per_half = r_stored * (prec + 2) + 8 + prec + 2 * prec + 2 * prec + 6 * prec + 2 * prec
-    if pairs:
-        per_half += prec
-    if quads:                                   # r_stored = value slots: 4 per quad, one u16 base
-        per_half -= r_stored * (prec + 2) - (r_stored / 4) * (4 * prec + 2)
+def format_bytes_per_segment_step(prop_bytes_per_row, prec=4):
+    """Compulsory HBM bytes of this implementation's layout per segment-step: per
+    half step the stored propagator bytes of one row (nw_propagator_stats: values,
+    16-bit columns or window bases, row offsets, the leak; pairs also c_max / c_i),
+    V read + write, kI and kG, HH gates (3) and coefficients (3), the na8 open
+    state and coefficient; per step the mechanism update reads V and reads + writes
+    3 HH gates and 8 na8 states."""
+    per_half = prop_bytes_per_row + 2 * prec + 2 * prec + 6 * prec + 2 * prec
     mech = prec + 2 * (3 + 8) * prec
     return 2 * per_half + mech
 
@@ -630,7 +626,7 @@ def main():
                     help="trial steps of the autotuner (lanes, threads, fusion depth); 0 = use the flags")
     ap.add_argument("--lump", type=int, default=1, choices=[0, 1],
                     help="lumped pruning (pruned entries moved to the nearest kept entry on the tree path)")
-    ap.add_argument("--format", default="quads", choices=["rows", "pairs", "quads"],
+    ap.add_argument("--format", default="quads", choices=["rows", "pairs", "quads", "windows"],
                     help="propagator storage: every P_ij in its row; windows of 4 consecutive columns; "
                          "or each coupling once (detailed balance)")
     ap.add_argument("--lanes", type=int, default=0)
@@ -809,7 +805,7 @@ def main():
         peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     B_alg = algorithmic_bytes_per_segment_step(r_kept)
-    B_fmt = format_bytes_per_segment_step(r_stored, pairs=args.format == "pairs", quads=args.format == "quads")
+    B_fmt = format_bytes_per_segment_step(pbytes.value / n)
     achieved = B_alg * n / (per_step_launch_ms * 1e-3) / 1e9
     achieved_fmt = B_fmt * n / (per_step_launch_ms * 1e-3) / 1e9
 

@@ -324,7 +324,12 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * coupling (i, j) stored once, in the row of the segment with the smaller
  * capacitance, and applied to both rows through detailed balance c_i P_ij = c_j P_ji
  * (propagators from nw_propagator_build only; kept when the other row pruned it, so
- * a pair survives if either P_ij or P_ji reaches the tolerance).
+ * a pair survives if either P_ij or P_ji reaches the tolerance); 3 = windows: each
+ * row's entries covered by windows of 8, 4, 2 or 1 consecutive columns (a 16-bit
+ * base and the window's values, zeros where a column is not kept), each window the
+ * width of fewest bytes per entry it covers; needs rows sorted by column (the
+ * batched step returns NW_ERR_STATE otherwise); nw_get_option("windows") reports
+ * the window count.
  * "spike_neurons" (N), "spike_neuron_offset" (o), "spike_ring_steps" (R): for a network
  * split across ranks, taken by the next nw_synapses_set: presynaptic ids are global
  * (< N), the spike ring covers all N neurons with this model's neuron j at o + j, and
@@ -360,7 +365,8 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value);
 /* Statistics of the installed propagator: rows, kept entries (with diagonal),
  * stored off-diagonal entries including padding, bytes of the batched format (of
  * the pair format when "propagator_format" is 1: stored pairs, bytes with the
- * per-row c_max / c_i). */
+ * per-row c_max / c_i; quads (2) and windows (3): value slots, bytes with bases and
+ * row offsets). */
 int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* stored,
                         int64_t* bytes);
 

@@ -638,6 +638,16 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "no propagator installed");
     if (rows) *rows = ctx->n_seg;
     if (nnz) *nnz = ctx->nnz64;
+    if (ctx->prop_format == 3 && ctx->b_ok) {
+        // Windows format: per window its values and a 16-bit base; per row 4 x u32
+        // window offsets and the leak.
+        NW_CHECK(ensure_windows(ctx));
+        const int64_t slots = 8 * ctx->nwin[0] + 4 * ctx->nwin[1] + 2 * ctx->nwin[2] + ctx->nwin[3];
+        const int64_t windows = ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3];
+        if (stored) *stored = slots;
+        if (bytes) *bytes = slots * ctx->precision + 2 * windows + ctx->n_seg * (16 + ctx->precision);
+        return NW_OK;
+    }
     if (ctx->prop_format == 2 && ctx->b_ok) {
         // Quad format: 4 value slots + a 16-bit base per quad.
         NW_CHECK(ensure_quads(ctx));
@@ -1198,8 +1208,9 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     }
     if (nm == "propagator_format") {
         // 0: rows (every P_ij stored in its row); 1: pairs (each coupling once,
-        // applied to both rows through detailed balance; built propagators only).
-        if (value < 0 || value > 2) return fail(ctx, NW_ERR_ARG, "propagator_format must be 0, 1 or 2");
+        // applied to both rows through detailed balance; built propagators only);
+        // 2: quads; 3: windows of 8, 4, 2 or 1 columns (rows sorted by column).
+        if (value < 0 || value > 3) return fail(ctx, NW_ERR_ARG, "propagator_format must be 0, 1, 2 or 3");
         if (value == 1 && !ctx->prop_built)
             return fail(ctx, NW_ERR_STATE, "pair format needs a propagator built by nw_propagator_build");
         ctx->prop_format = (int)value;
@@ -1261,6 +1272,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "kinetic_mechanisms") { *value = ctx->n_kin; return NW_OK; }
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "quads") { *value = ctx->nq; return NW_OK; }
+    if (nm == "windows") { *value = ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3]; return NW_OK; }
     if (nm == "fusion_depth") { *value = ctx->fusion; return NW_OK; }
     if (nm == "graphs_cached") { *value = (int64_t)ctx->graphs.size(); return NW_OK; }
     if (nm == "graph_captures") { *value = ctx->graph_captures; return NW_OK; }

@@ -199,7 +199,14 @@ struct nw_ctx {
     bool wq_ok = false;                                // wide path: global 32-bit bases
     int64_t nwq = 0;
     nw::DevBuf wq_rowptr, wq_base, wq_val;
-    int prop_format = 0;                               // 0: rows, 1: pairs, 2: quads
+    // Windows format of the batched path: each row's off-diagonal entries covered
+    // by windows of 8, 4, 2 or 1 consecutive columns (u16 neuron-relative base +
+    // the window's values), grouped by width; win_row holds 4 x u32 window offsets
+    // per row (one per width), n_seg + 1 rows.
+    bool win_ok = false;
+    int64_t nwin[4] = {0, 0, 0, 0};                    // windows of width 8, 4, 2, 1
+    nw::DevBuf win_row, win_base[4], win_val[4];
+    int prop_format = 0;                               // 0: rows, 1: pairs, 2: quads, 3: windows
     int pair_shared_limit = -1;                        // cap on neurons with shared-memory sums (-1: none)
 
     // Mechanisms.  Kinetic mechanisms are kept in registration order; their
@@ -300,6 +307,7 @@ int ensure_wide(nw_ctx* ctx);
 int ensure_flux(nw_ctx* ctx);
 int ensure_quads(nw_ctx* ctx);
 int ensure_wide_quads(nw_ctx* ctx);
+int ensure_windows(nw_ctx* ctx);
 void free_quads(nw_ctx* ctx);
 void free_flux(nw_ctx* ctx);
 void free_wide(nw_ctx* ctx);

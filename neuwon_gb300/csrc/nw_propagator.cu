@@ -741,7 +741,173 @@ __global__ void quad_fill_kernel(int64_t n, const int64_t* nstart_of_row, const 
     }
 }
 
+// ------------------------------------------------- windows format (8, 4, 2, 1)
+//
+// Each row's off-diagonal entries (neuron-relative columns, increasing) are
+// covered by windows of 8, 4, 2 or 1 consecutive columns: one 16-bit base per
+// window and the window's values (zeros where a column is not kept), grouped by
+// width.  Walking the row, the window opened at the first uncovered entry c is
+// the width with the fewest bytes per entry it covers (2 B base + width values;
+// ties go to the wider window).  Windows may reach up to 7 columns past the
+// neuron's last segment, where the kernel keeps x at zero.
+template <typename real>
+__device__ __forceinline__ int window_width(const int32_t* pcol, int64_t k, int64_t end, int64_t row,
+                                            int64_t* next) {
+    const int widths[4] = {8, 4, 2, 1};
+    const int64_t c = pcol[k];
+    int best = -1;
+    double best_per = 0.0;
+    int64_t best_next = k + 1;
+    for (int w = 0; w < 4; ++w) {
+        int64_t j = k, cnt = 0;
+        while (j < end && (pcol[j] == row || pcol[j] < c + widths[w])) {
+            if (pcol[j] != row) ++cnt;
+            ++j;
+        }
+        const double per = (2.0 + (double)widths[w] * sizeof(real)) / (double)cnt;
+        if (best < 0 || per < best_per - 1e-12) { best = w; best_per = per; best_next = j; }
+    }
+    *next = best_next;
+    return best;
+}
+
+// Per row: its window count of each width; flags[0] |= 1 when a row's columns
+// do not increase (the format needs them sorted).
+template <typename real>
+__global__ void window_count_kernel(int64_t n, const int64_t* prow, const int32_t* pcol, int32_t* cnt,
+                                    int* flags) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int32_t c4[4] = {0, 0, 0, 0};
+    const int64_t end = prow[r + 1];
+    for (int64_t k = prow[r] + 1; k < end; ++k)
+        if (pcol[k] <= pcol[k - 1]) { atomicOr(flags, 1); break; }
+    int64_t k = prow[r];
+    while (k < end && pcol[k] == r) ++k;
+    while (k < end) {
+        int64_t next;
+        ++c4[window_width<real>(pcol, k, end, r, &next)];
+        k = next;
+        while (k < end && pcol[k] == r) ++k;
+    }
+    for (int w = 0; w < 4; ++w) cnt[4 * r + w] = c4[w];
+}
+
+template <typename real>
+__global__ void window_fill_kernel(int64_t n, const int64_t* row_lo, const int64_t* prow, const int32_t* pcol,
+                                   const double* pval, const uint32_t* wrow, uint16_t* b8, uint16_t* b4,
+                                   uint16_t* b2, uint16_t* b1, real* v8, real* v4, real* v2, real* v1) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int widths[4] = {8, 4, 2, 1};
+    uint16_t* bases[4] = {b8, b4, b2, b1};
+    real* vals[4] = {v8, v4, v2, v1};
+    uint32_t pos[4] = {wrow[4 * r], wrow[4 * r + 1], wrow[4 * r + 2], wrow[4 * r + 3]};
+    const int64_t lo = row_lo[r], end = prow[r + 1];
+    int64_t k = prow[r];
+    while (k < end && pcol[k] == r) ++k;
+    while (k < end) {
+        int64_t next;
+        const int w = window_width<real>(pcol, k, end, r, &next);
+        const int64_t c = pcol[k];
+        const uint32_t q = pos[w]++;
+        bases[w][q] = (uint16_t)(c - lo);
+        real* v = vals[w] + (int64_t)q * widths[w];
+        for (int j = 0; j < widths[w]; ++j) v[j] = real(0);
+        for (int64_t e = k; e < next; ++e)
+            if (pcol[e] != r) v[pcol[e] - c] = (real)pval[e];
+        k = next;
+        while (k < end && pcol[k] == r) ++k;
+    }
+}
+
+static void free_windows(nw_ctx* ctx) {
+    dev_free(ctx->win_row);
+    for (int w = 0; w < 4; ++w) {
+        dev_free(ctx->win_base[w]);
+        dev_free(ctx->win_val[w]);
+        ctx->nwin[w] = 0;
+    }
+    ctx->win_ok = false;
+}
+
+int ensure_windows(nw_ctx* ctx) {
+    if (ctx->win_ok) return NW_OK;
+    if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "windows format: needs the batched format (neurons <= 65,535)");
+    const int64_t n = ctx->n_seg;
+    free_windows(ctx);
+    DevBuf d_cnt, d_flag, d_lo;
+    int rc = NW_OK;
+    do {
+        if ((rc = dev_alloc(ctx, d_cnt, 16 * n)) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, d_flag, 4)) != NW_OK) break;
+        cudaError_t e = cudaMemsetAsync(d_flag.ptr, 0, 4, ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "windows format count"); break; }
+        const unsigned blocks = (unsigned)((n + 127) / 128);
+        if (ctx->precision == NW_F64)
+            window_count_kernel<double><<<blocks, 128, 0, ctx->stream>>>(
+                n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), d_cnt.as<int32_t>(), d_flag.as<int>());
+        else
+            window_count_kernel<float><<<blocks, 128, 0, ctx->stream>>>(
+                n, ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), d_cnt.as<int32_t>(), d_flag.as<int>());
+        std::vector<int32_t> cnt(4 * n);
+        int flag = 0;
+        cudaMemcpyAsync(cnt.data(), d_cnt.ptr, 16 * n, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(&flag, d_flag.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "windows format count"); break; }
+        if (flag) { rc = fail(ctx, NW_ERR_STATE, "windows format: propagator rows are not sorted by column"); break; }
+        // Window offsets of each row, per width (4 x u32 per row).
+        std::vector<uint32_t> wrow(4 * (n + 1), 0);
+        uint64_t tot[4] = {0, 0, 0, 0};
+        for (int64_t i = 0; i < n; ++i)
+            for (int w = 0; w < 4; ++w) {
+                wrow[4 * i + w] = (uint32_t)tot[w];
+                tot[w] += (uint64_t)cnt[4 * i + w];
+            }
+        for (int w = 0; w < 4 && rc == NW_OK; ++w) {
+            if (tot[w] > UINT32_MAX) rc = fail(ctx, NW_ERR_LIMIT, "windows format: 2^32 or more windows of one width");
+            else wrow[4 * n + w] = (uint32_t)tot[w];
+        }
+        if (rc != NW_OK) break;
+        const int widths[4] = {8, 4, 2, 1};
+        if ((rc = dev_alloc(ctx, ctx->win_row, 16 * (n + 1))) != NW_OK) break;
+        for (int w = 0; w < 4 && rc == NW_OK; ++w) {
+            rc = dev_alloc(ctx, ctx->win_base[w], 2 * std::max<uint64_t>(tot[w], 8));
+            if (rc == NW_OK)
+                rc = dev_alloc(ctx, ctx->win_val[w], (size_t)ctx->precision * widths[w] * std::max<uint64_t>(tot[w], 1));
+            ctx->nwin[w] = (int64_t)tot[w];
+        }
+        if (rc != NW_OK) break;
+        std::vector<int64_t> lo(n);
+        for (int64_t j = 0; j < ctx->n_neuron; ++j)
+            for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) lo[i] = ctx->h_neuron_start[j];
+        if ((rc = dev_alloc(ctx, d_lo, 8 * std::max<int64_t>(n, 1))) != NW_OK) break;
+        cudaMemcpyAsync(ctx->win_row.ptr, wrow.data(), 16 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(d_lo.ptr, lo.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+        uint16_t* B[4];
+        for (int w = 0; w < 4; ++w) B[w] = ctx->win_base[w].as<uint16_t>();
+        if (ctx->precision == NW_F64)
+            window_fill_kernel<double><<<blocks, 128, 0, ctx->stream>>>(
+                n, d_lo.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
+                ctx->win_row.as<uint32_t>(), B[0], B[1], B[2], B[3], ctx->win_val[0].as<double>(),
+                ctx->win_val[1].as<double>(), ctx->win_val[2].as<double>(), ctx->win_val[3].as<double>());
+        else
+            window_fill_kernel<float><<<blocks, 128, 0, ctx->stream>>>(
+                n, d_lo.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
+                ctx->win_row.as<uint32_t>(), B[0], B[1], B[2], B[3], ctx->win_val[0].as<float>(),
+                ctx->win_val[1].as<float>(), ctx->win_val[2].as<float>(), ctx->win_val[3].as<float>());
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "windows format fill"); break; }
+        ctx->win_ok = true;
+    } while (0);
+    dev_free(d_cnt); dev_free(d_flag); dev_free(d_lo);
+    if (rc != NW_OK) free_windows(ctx);
+    return rc;
+}
+
 void free_quads(nw_ctx* ctx) {
+    free_windows(ctx);
     for (DevBuf* b : {&ctx->q_rowptr, &ctx->q_base, &ctx->q_val, &ctx->wq_rowptr, &ctx->wq_base, &ctx->wq_val})
         dev_free(*b);
     ctx->q_ok = ctx->wq_ok = false;

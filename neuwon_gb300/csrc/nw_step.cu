@@ -318,7 +318,7 @@ __device__ __forceinline__ void flux_finalize(const StepArgs<real>& a, int64_t b
     }
 }
 
-template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false, bool FUSE = false>
+template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false, bool FUSE = false, bool WIN = false>
 __global__ void __launch_bounds__(1024)
 batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_off) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -363,6 +363,10 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         if (QUAD && n < 4) {
             // Quad windows of a neuron of fewer than 4 segments reach past it: zeros there.
             for (int li = n + threadIdx.x; li < 4; li += blockDim.x) xs[li] = real(0);
+        }
+        if (WIN) {
+            // Windows reach up to 7 columns past the neuron's last segment: zeros there.
+            for (int li = n + threadIdx.x; li < n + 8; li += blockDim.x) xs[li] = real(0);
         }
         if (FLUX) {
             // c_max / c of the neuron's segments next to x; sums start at zero (the
@@ -469,6 +473,11 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     }
                 } else if (QUAD) {
                     propagate_quads<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real vnew) {
+                        if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
+                        a.V[r] = vnew;
+                    });
+                } else if (WIN) {
+                    propagate_windows<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real vnew) {
                         if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
                         a.V[r] = vnew;
                     });
@@ -676,6 +685,8 @@ int choose_lanes_per_row(nw_ctx* ctx) {
     if (ctx->lanes_per_row) return ctx->lanes_per_row;
     int64_t nnz = (ctx->prop_format == 1 && ctx->f_ok) ? ctx->nnz_f : ctx->nnz_b;
     if (ctx->prop_format == 2 && ctx->q_ok) nnz = ctx->nq;   // quads per row: one per lane and load
+    if (ctx->prop_format == 3 && ctx->win_ok)                // windows per row
+        nnz = ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3];
     double avg = ctx->n_seg ? (double)nnz / (double)ctx->n_seg : 0.0;
     if (avg >= 48) return 16;
     if (avg >= 20) return 8;
@@ -694,10 +705,10 @@ struct BatchedCfg {
     int rc_smem;      // pair format: c_max / c staged in shared memory
 };
 
-template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false, bool FUSE = false>
+template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false, bool FUSE = false, bool WIN = false>
 static int config_batched_lpr(nw_ctx* ctx, BatchedCfg<real>& c) {
-    auto kern = batched_advance_kernel<real, LPR, BULK, FLUX, QUAD, FUSE>;
-    const size_t xs_bytes = ((size_t)ctx->max_neuron * sizeof(real) + 127) & ~(size_t)127;
+    auto kern = batched_advance_kernel<real, LPR, BULK, FLUX, QUAD, FUSE, WIN>;
+    const size_t xs_bytes = ((size_t)(ctx->max_neuron + (WIN ? 8 : 0)) * sizeof(real) + 127) & ~(size_t)127;
     const int threads = ctx->threads;
     size_t smem = xs_bytes;
     if (BULK) smem += (size_t)(threads / 32) * kBulkStages * (BulkGeom<real>::kStageBytes + 8);
@@ -748,6 +759,19 @@ template <typename real>
 static int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
     if (!ctx->b_ok || (ctx->ca.on && !ctx->ca.b_ok))
         return fail(ctx, NW_ERR_LIMIT, "batched path: a neuron has more than 65,535 segments (use the wide path)");
+    if (ctx->prop_format == 3) {
+        NW_CHECK(ensure_windows(ctx));
+        const bool fuse = fuse_mechanisms(ctx);
+        switch (choose_lanes_per_row(ctx)) {
+            case 4:
+            case 8: return fuse ? config_batched_lpr<real, 8, false, false, false, true, true>(ctx, c)
+                                : config_batched_lpr<real, 8, false, false, false, false, true>(ctx, c);
+            case 16: return fuse ? config_batched_lpr<real, 16, false, false, false, true, true>(ctx, c)
+                                 : config_batched_lpr<real, 16, false, false, false, false, true>(ctx, c);
+            default: return fuse ? config_batched_lpr<real, 32, false, false, false, true, true>(ctx, c)
+                                 : config_batched_lpr<real, 32, false, false, false, false, true>(ctx, c);
+        }
+    }
     if (ctx->prop_format == 2) {
         NW_CHECK(ensure_quads(ctx));
         if (fuse_mechanisms(ctx)) {

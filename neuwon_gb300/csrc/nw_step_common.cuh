@@ -100,6 +100,11 @@ struct StepArgs {
     const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
     // quad propagator: windows of 4 consecutive columns
     const int64_t* qrow; const uint16_t* qbase; const real* qval;
+    // windows propagator: per row 4 x u32 window offsets (widths 8, 4, 2, 1), then
+    // per width the u16 bases and the values
+    const uint4* wnrow;
+    const uint16_t* wnb8; const uint16_t* wnb4; const uint16_t* wnb2; const uint16_t* wnb1;
+    const real* wnv8; const real* wnv4; const real* wnv2; const real* wnv1;
     // pair ("flux") propagator: rows of owned pairs, leak, c_max / c_i, global accumulators
     const int64_t* frow; const uint16_t* fcol; const real* fval; const real* fleak; const real* frc;
     unsigned long long* facc; int facc_cap; int frc_smem;
@@ -479,6 +484,20 @@ template <> struct Vec4Loader<double> {
     }
 };
 
+template <typename real> struct Vec2Loader;
+template <> struct Vec2Loader<float> {
+    static __device__ __forceinline__ void load(const float* p, float (&v)[2]) {
+        float2 q = __ldcs(reinterpret_cast<const float2*>(p));
+        v[0] = q.x; v[1] = q.y;
+    }
+};
+template <> struct Vec2Loader<double> {
+    static __device__ __forceinline__ void load(const double* p, double (&v)[2]) {
+        double2 q = __ldcs(reinterpret_cast<const double2*>(p));
+        v[0] = q.x; v[1] = q.y;
+    }
+};
+
 template <typename real>
 __device__ __forceinline__ void kahan_add(real& s, real& c, real term) {
     real y = term - c;
@@ -606,6 +625,88 @@ __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t
     }
 }
 
+// Windows format: row i is four lists of windows, of widths 8, 4, 2 and 1 (base b,
+// values for columns b..b+w-1).  Lane l of the row takes window l + LPR t of every
+// width in round t, so one round has a window of each width in flight; a round's
+// four window sums are added pairwise into the compensated row sum.  Windows may
+// reach 7 columns past the neuron's last segment: x holds zeros there.
+template <typename real, int LPR, typename Fin>
+__device__ __forceinline__ void propagate_windows(const StepArgs<real>& a, int64_t base, int n,
+                                                  const real* __restrict__ xs, Fin fin) {
+    constexpr int GPW = 32 / LPR;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int q = lane / LPR, l = lane % LPR;
+    for (int rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int row = rb + q;
+        const bool valid = row < n;
+        real s = real(0), c = real(0), xi = real(0);
+        if (valid) {
+            const int64_t r = base + row;
+            const uint4 o0 = __ldg(a.wnrow + r), o1 = __ldg(a.wnrow + r + 1);
+            const uint32_t n8 = o1.x - o0.x, n4 = o1.y - o0.y, n2 = o1.z - o0.z, n1 = o1.w - o0.w;
+            const uint32_t nmax = max(max(n8, n4), max(n2, n1));
+            xi = xs[row];
+            for (uint32_t t = l; t < nmax; t += LPR) {
+                real v8[8], v4[4], v2[2], v1 = real(0);
+                int b8 = 0, b4 = 0, b2 = 0, b1 = 0;
+                const bool h8 = t < n8, h4 = t < n4, h2 = t < n2, h1 = t < n1;
+                if (h8) {
+                    const int64_t k = (int64_t)o0.x + t;
+                    real lo[4], hi[4];
+                    Vec4Loader<real>::load(a.wnv8 + 8 * k, lo);
+                    Vec4Loader<real>::load(a.wnv8 + 8 * k + 4, hi);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) { v8[j] = lo[j]; v8[4 + j] = hi[j]; }
+                    b8 = __ldcs(a.wnb8 + k);
+                }
+                if (h4) {
+                    const int64_t k = (int64_t)o0.y + t;
+                    Vec4Loader<real>::load(a.wnv4 + 4 * k, v4);
+                    b4 = __ldcs(a.wnb4 + k);
+                }
+                if (h2) {
+                    const int64_t k = (int64_t)o0.z + t;
+                    Vec2Loader<real>::load(a.wnv2 + 2 * k, v2);
+                    b2 = __ldcs(a.wnb2 + k);
+                }
+                if (h1) {
+                    const int64_t k = (int64_t)o0.w + t;
+                    v1 = __ldcs(a.wnv1 + k);
+                    b1 = __ldcs(a.wnb1 + k);
+                }
+                real p8 = real(0), p4 = real(0), p2 = real(0), p1 = real(0);
+                if (h8) {
+                    const real* x = xs + b8;
+                    const real e0 = v8[0] * (x[0] - xi) + v8[1] * (x[1] - xi);
+                    const real e1 = v8[2] * (x[2] - xi) + v8[3] * (x[3] - xi);
+                    const real e2 = v8[4] * (x[4] - xi) + v8[5] * (x[5] - xi);
+                    const real e3 = v8[6] * (x[6] - xi) + v8[7] * (x[7] - xi);
+                    p8 = (e0 + e1) + (e2 + e3);
+                }
+                if (h4) {
+                    const real* x = xs + b4;
+                    p4 = (v4[0] * (x[0] - xi) + v4[1] * (x[1] - xi)) + (v4[2] * (x[2] - xi) + v4[3] * (x[3] - xi));
+                }
+                if (h2) {
+                    const real* x = xs + b2;
+                    p2 = v2[0] * (x[0] - xi) + v2[1] * (x[1] - xi);
+                }
+                if (h1) p1 = v1 * (xs[b1] - xi);
+                kahan_add(s, c, (p8 + p4) + (p2 + p1));
+            }
+        }
+        real t = s - c;
+#pragma unroll
+        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        if (valid && l == 0) {
+            const int64_t r = base + row;
+            fin(r, row, xi, (xi - a.leak[r] * xi) + t);
+        }
+    }
+}
+
 // V_i <- propagator row i applied to xs, for every row of one neuron.
 template <typename real, int LPR>
 __device__ __forceinline__ void propagate_neuron(const StepArgs<real>& a, int64_t base, int n,
@@ -644,6 +745,13 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.prow = ctx->p_rowptr.as<int64_t>(); a.pcol = ctx->p_col.as<int32_t>(); a.pval = ctx->p_val.as<double>();
     a.px = ctx->plain_x.as<real>();
     a.qrow = ctx->q_rowptr.as<int64_t>(); a.qbase = ctx->q_base.as<uint16_t>(); a.qval = ctx->q_val.as<real>();
+    if (ctx->win_ok) {
+        a.wnrow = ctx->win_row.as<uint4>();
+        a.wnb8 = ctx->win_base[0].as<uint16_t>(); a.wnb4 = ctx->win_base[1].as<uint16_t>();
+        a.wnb2 = ctx->win_base[2].as<uint16_t>(); a.wnb1 = ctx->win_base[3].as<uint16_t>();
+        a.wnv8 = ctx->win_val[0].as<real>(); a.wnv4 = ctx->win_val[1].as<real>();
+        a.wnv2 = ctx->win_val[2].as<real>(); a.wnv1 = ctx->win_val[3].as<real>();
+    }
     a.frow = ctx->f_rowptr.as<int64_t>(); a.fcol = ctx->f_col.as<uint16_t>();
     a.fval = ctx->f_val.as<real>(); a.fleak = ctx->f_leak.as<real>(); a.frc = ctx->f_rc.as<real>();
     a.facc = ctx->f_acc.as<unsigned long long>();

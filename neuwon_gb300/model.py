@@ -269,7 +269,9 @@ class RxD_Model:
       propagator_format     'rows' (every P_ij in its row, 16-bit column each),
                             'quads' (windows of 4 consecutive columns with one
                             16-bit base: ~16 % fewer bytes with the model's
-                            depth-first numbering) or 'pairs' (each coupling
+                            depth-first numbering), 'windows' (windows of 8, 4,
+                            2 or 1 consecutive columns, each the width of fewest
+                            bytes per entry it covers) or 'pairs' (each coupling
                             stored once and applied to both segments through
                             detailed balance)
       path                  'batched' (fused persistent kernel, one CTA per neuron),
@@ -321,7 +323,7 @@ class RxD_Model:
         self.propagator_tolerance = float(propagator_tolerance)
         self.propagator_conserve = bool(propagator_conserve)
         self.path = {"batched": _lib.PATH_BATCHED, "plain": _lib.PATH_PLAIN, "wide": _lib.PATH_WIDE}[path]
-        self.propagator_format = {"rows": 0, "pairs": 1, "quads": 2}[propagator_format]
+        self.propagator_format = {"rows": 0, "pairs": 1, "quads": 2, "windows": 3}[propagator_format]
         self.propagator_lump = bool(propagator_lump)
         self.input_hook = Clock(0.5 * self.time_step, units="ms")
         self.advance_hook = self.clock = Clock(self.time_step, units="ms")

@@ -12,11 +12,14 @@ def test_algorithmic_bytes_formula():
     assert bench.algorithmic_bytes_per_segment_step(302.5) == pytest.approx(2 * (8 * 302.5 + 4) + 120)
 
 
-def test_format_bytes_quads_count_windows():
-    rows = bench.format_bytes_per_segment_step(100.0)
-    quads = bench.format_bytes_per_segment_step(100.0, quads=True)
-    # 100 value slots = 25 windows of 4 values + one 16-bit base, per half step.
-    assert rows - quads == pytest.approx(2 * (100 * 6 - 25 * 18))
+def test_format_bytes_add_the_step_state_to_the_stored_propagator():
+    # Per half step: the row's stored propagator bytes + V r/w, kI, kG, 3 HH gates,
+    # 3 HH coefficients, na8 open state and coefficient (4 B each); per step the
+    # mechanism pass reads V and reads + writes 11 states.
+    assert bench.format_bytes_per_segment_step(0.0) == 2 * 12 * 4 + 4 + 2 * 11 * 4
+    # A row of 100 stored 4 B values with u16 columns, an 8 B row pointer and the leak.
+    b = bench.format_bytes_per_segment_step(100 * 6 + 8 + 4)
+    assert b - bench.format_bytes_per_segment_step(0.0) == 2 * (100 * 6 + 12)
 
 
 def _defaults():

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import neuwon_gb300 as nw
+from neuwon_gb300 import _lib
 from neuwon_gb300.morphology import EPSILON, random_tree
 from tests.helpers import FIXTURES, gpu_model, run_with_clamps, tree11
 
@@ -127,3 +128,84 @@ def test_quads_equal_rows(precision):
     tol = 1e-9 if precision == "f64" else 2e-3
     assert np.abs(out[0][0] - out[1][0]).max() < tol
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_windows_equal_rows(precision):
+    """The windows format (windows of 8, 4, 2 or 1 consecutive columns, zeros where
+    a column is not kept) holds exactly the row format's entries, so results agree
+    to rounding; neurons of 1 to 7 segments put windows past their last segment,
+    onto the zero padding of x."""
+    trees = [random_tree(n, seed=90 + n) for n in (2500, 600, 40, 7, 4, 2, 1)]
+    clamps = [(0, 0, 0.5, 0.0, 50.0), (1, 0, 0.3, 0.0, 50.0), (2, 0, 0.2, 0.0, 50.0), (3, 0, 0.05, 0.0, 50.0)]
+    out = []
+    for fmt in ("rows", "windows"):
+        m, _, offs, _ = gpu_model(trees, clamps, precision=precision, tolerance=1e-8, conserve=True, fmt=fmt,
+                                  kinetic=True)
+        for (ti, s, nA, start, dur) in clamps:
+            nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance(300)
+        out.append((m.get_data("Segment.voltage"), m.get_data("Neuron.spike_count")))
+        if fmt == "windows":
+            assert m._ctx.get_option("propagator_format") == 3
+            rows, nnz, stored, pbytes = (ctypes.c_int64() for _ in range(4))
+            m._ctx.call("nw_propagator_stats", ctypes.byref(rows), ctypes.byref(nnz), ctypes.byref(stored),
+                        ctypes.byref(pbytes))
+            off_diag = m.propagator_nnz - m._n
+            assert off_diag <= stored.value < 1.25 * off_diag
+            nwin = m._ctx.get_option("windows")
+            assert pbytes.value == stored.value * (8 if precision == "f64" else 4) + 2 * nwin + \
+                m._n * (16 + (8 if precision == "f64" else 4))
+        m.close()
+    tol = 1e-9 if precision == "f64" else 2e-3
+    assert np.abs(out[0][0] - out[1][0]).max() < tol
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_windows_fused_steps_and_graphs_bit_identical():
+    """Fusion depth and graph replay change nothing in the windows format (FP32)."""
+    trees = [random_tree(n, seed=300 + n) for n in (1800, 700, 9)]
+    clamps = [(0, 0, 0.4, 0.0, 30.0), (1, 0, 0.3, 0.0, 30.0)]
+    res = []
+    for fusion, graph in ((1, 0), (7, 1), (0, 1)):
+        m, _, offs, _ = gpu_model(trees, clamps, precision="f32", tolerance=3e-7, conserve="lump", fmt="windows",
+                                  kinetic=True)
+        m._sync()
+        m._ctx.set_option("fusion_depth", fusion)
+        m._ctx.set_option("cuda_graph", graph)
+        for (ti, s, nA, start, dur) in clamps:
+            nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance(60)
+        res.append(m.get_data("Segment.voltage"))
+        m.close()
+    assert np.array_equal(res[0], res[1]) and np.array_equal(res[0], res[2])
+
+
+def test_windows_need_sorted_rows():
+    """A propagator whose rows are not sorted by column is refused by the windows
+    format (the quad and row formats take it)."""
+    m, _, _, _ = gpu_model([random_tree(30, seed=5)], [], precision="f64", fmt="windows")
+    m._sync()
+    n = m._n
+    cols, vals, ptr = [], [], [0]
+    for i in range(n):                       # row 0 lists column 1 before its diagonal
+        if i == 0:
+            cols += [1, 0]
+            vals += [1e-3, 1 - 1e-3]
+        elif i == 1:
+            cols += [0, 1]
+            vals += [1e-3, 1 - 1e-3]
+        else:
+            cols += [i]
+            vals += [1.0]
+        ptr.append(len(cols))
+    rowptr = np.array(ptr, dtype=np.int64)
+    col = np.array(cols, dtype=np.int64)
+    val = np.array(vals)
+    m._ctx.call("nw_propagator_set_csr", n, _lib.ptr(rowptr), _lib.ptr(col), _lib.ptr(val), len(val))
+    m._ctx.set_option("propagator_format", 3)
+    rc = m._ctx.lib.nw_advance(m._ctx.handle, 1, _lib.PATH_BATCHED)
+    assert rc == -3                                                    # NW_ERR_STATE
+    m._ctx.set_option("propagator_format", 2)
+    m._ctx.advance(1)
+    m.close()
