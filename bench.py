@@ -731,6 +731,8 @@ def main():
     n = model._n
     r_kept = nnz.value / n
     r_stored = stored.value / n
+    windows_per_row = ({w: ctx.get_option(f"windows_{w}") / n for w in (8, 4, 2, 1)}
+                       if args.format == "windows" else None)
     bulk_active = ctypes.c_int64()
     ctx.call("nw_get_option", b"bulk_pipeline_active", ctypes.byref(bulk_active))
     lanes = ctypes.c_int(); thr = ctypes.c_int(); cps = ctypes.c_int()
@@ -831,6 +833,7 @@ def main():
                                           if args.lump else "charge-conserving (pruned mass returned to the diagonal)"),
                    "propagator_format": args.format,
                    "propagator_entries_per_row": r_kept, "stored_entries_per_row": r_stored,
+                   **({"windows_per_row": windows_per_row} if windows_per_row else {}),
                    "propagator_build_s": build_s, "steps_per_launch": F, "lanes_per_row": lanes.value,
                    "autotune": tuned, "cuda_graph": {"replayed": graph_replayed, "launches_in_graph": n_launch},
                    "propagator_stream": "cp.async.bulk ring (4 x 256 entries per warp)" if bulk_active.value

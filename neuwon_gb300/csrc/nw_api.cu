@@ -1273,6 +1273,10 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "quads") { *value = ctx->nq; return NW_OK; }
     if (nm == "windows") { *value = ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3]; return NW_OK; }
+    if (nm == "windows_8") { *value = ctx->nwin[0]; return NW_OK; }
+    if (nm == "windows_4") { *value = ctx->nwin[1]; return NW_OK; }
+    if (nm == "windows_2") { *value = ctx->nwin[2]; return NW_OK; }
+    if (nm == "windows_1") { *value = ctx->nwin[3]; return NW_OK; }
     if (nm == "fusion_depth") { *value = ctx->fusion; return NW_OK; }
     if (nm == "graphs_cached") { *value = (int64_t)ctx->graphs.size(); return NW_OK; }
     if (nm == "graph_captures") { *value = ctx->graph_captures; return NW_OK; }

@@ -685,8 +685,8 @@ int choose_lanes_per_row(nw_ctx* ctx) {
     if (ctx->lanes_per_row) return ctx->lanes_per_row;
     int64_t nnz = (ctx->prop_format == 1 && ctx->f_ok) ? ctx->nnz_f : ctx->nnz_b;
     if (ctx->prop_format == 2 && ctx->q_ok) nnz = ctx->nq;   // quads per row: one per lane and load
-    if (ctx->prop_format == 3 && ctx->win_ok)                // windows per row
-        nnz = ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3];
+    if (ctx->prop_format == 3 && ctx->win_ok)                // window items (halves of 8-wide windows)
+        nnz = 2 * ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3];
     double avg = ctx->n_seg ? (double)nnz / (double)ctx->n_seg : 0.0;
     if (avg >= 48) return 16;
     if (avg >= 20) return 8;

@@ -626,11 +626,13 @@ __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t
 }
 
 // Windows format: row i is four lists of windows, of widths 8, 4, 2 and 1 (base b,
-// values for columns b..b+w-1).  Lane l of the row takes window l + LPR t of every
-// width in round t, so one round has a window of each width in flight; a round's
-// four window sums are added pairwise into the compensated row sum.  Windows may
-// reach 7 columns past the neuron's last segment: x holds zeros there.
-template <typename real, int LPR, typename Fin>
+// values for columns b..b+w-1).  The row's windows form one list of items of at
+// most 4 values: an 8-wide window is two items (its halves), the others one each;
+// the row's lanes take consecutive items, UNROLL items per lane loaded before any
+// is used (as in the quad format), and every item is summed as a 4-column window
+// with zero weights past its width.  Windows may reach 7 columns past the neuron's
+// last segment, where x holds zeros.
+template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
 __device__ __forceinline__ void propagate_windows(const StepArgs<real>& a, int64_t base, int n,
                                                   const real* __restrict__ xs, Fin fin) {
     constexpr int GPW = 32 / LPR;
@@ -645,56 +647,45 @@ __device__ __forceinline__ void propagate_windows(const StepArgs<real>& a, int64
         if (valid) {
             const int64_t r = base + row;
             const uint4 o0 = __ldg(a.wnrow + r), o1 = __ldg(a.wnrow + r + 1);
-            const uint32_t n8 = o1.x - o0.x, n4 = o1.y - o0.y, n2 = o1.z - o0.z, n1 = o1.w - o0.w;
-            const uint32_t nmax = max(max(n8, n4), max(n2, n1));
+            const uint32_t e8 = 2 * (o1.x - o0.x), e4 = e8 + (o1.y - o0.y), e2 = e4 + (o1.z - o0.z);
+            const uint32_t e1 = e2 + (o1.w - o0.w);
             xi = xs[row];
-            for (uint32_t t = l; t < nmax; t += LPR) {
-                real v8[8], v4[4], v2[2], v1 = real(0);
-                int b8 = 0, b4 = 0, b2 = 0, b1 = 0;
-                const bool h8 = t < n8, h4 = t < n4, h2 = t < n2, h1 = t < n1;
-                if (h8) {
-                    const int64_t k = (int64_t)o0.x + t;
-                    real lo[4], hi[4];
-                    Vec4Loader<real>::load(a.wnv8 + 8 * k, lo);
-                    Vec4Loader<real>::load(a.wnv8 + 8 * k + 4, hi);
+            for (uint32_t t0 = l; t0 < e1; t0 += LPR * UNROLL) {
+                real v[UNROLL][4];
+                int b[UNROLL];
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) { v8[j] = lo[j]; v8[4 + j] = hi[j]; }
-                    b8 = __ldcs(a.wnb8 + k);
+                for (int u = 0; u < UNROLL; ++u) {
+                    const uint32_t t = t0 + LPR * u;
+                    v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                    b[u] = 0;                                 // zero weights on x[0..3]
+                    if (t < e8) {
+                        const int64_t k = (int64_t)o0.x + (t >> 1);
+                        const int h = 4 * (int)(t & 1);
+                        Vec4Loader<real>::load(a.wnv8 + 8 * k + h, v[u]);
+                        b[u] = __ldcs(a.wnb8 + k) + h;
+                    } else if (t < e4) {
+                        const int64_t k = (int64_t)o0.y + (t - e8);
+                        Vec4Loader<real>::load(a.wnv4 + 4 * k, v[u]);
+                        b[u] = __ldcs(a.wnb4 + k);
+                    } else if (t < e2) {
+                        const int64_t k = (int64_t)o0.z + (t - e4);
+                        real w2[2];
+                        Vec2Loader<real>::load(a.wnv2 + 2 * k, w2);
+                        v[u][0] = w2[0]; v[u][1] = w2[1];
+                        b[u] = __ldcs(a.wnb2 + k);
+                    } else if (t < e1) {
+                        const int64_t k = (int64_t)o0.w + (t - e2);
+                        v[u][0] = __ldcs(a.wnv1 + k);
+                        b[u] = __ldcs(a.wnb1 + k);
+                    }
                 }
-                if (h4) {
-                    const int64_t k = (int64_t)o0.y + t;
-                    Vec4Loader<real>::load(a.wnv4 + 4 * k, v4);
-                    b4 = __ldcs(a.wnb4 + k);
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const real* x = xs + b[u];
+                    const real p = v[u][0] * (x[0] - xi) + v[u][1] * (x[1] - xi);
+                    const real t = v[u][2] * (x[2] - xi) + v[u][3] * (x[3] - xi);
+                    kahan_add(s, c, p + t);
                 }
-                if (h2) {
-                    const int64_t k = (int64_t)o0.z + t;
-                    Vec2Loader<real>::load(a.wnv2 + 2 * k, v2);
-                    b2 = __ldcs(a.wnb2 + k);
-                }
-                if (h1) {
-                    const int64_t k = (int64_t)o0.w + t;
-                    v1 = __ldcs(a.wnv1 + k);
-                    b1 = __ldcs(a.wnb1 + k);
-                }
-                real p8 = real(0), p4 = real(0), p2 = real(0), p1 = real(0);
-                if (h8) {
-                    const real* x = xs + b8;
-                    const real e0 = v8[0] * (x[0] - xi) + v8[1] * (x[1] - xi);
-                    const real e1 = v8[2] * (x[2] - xi) + v8[3] * (x[3] - xi);
-                    const real e2 = v8[4] * (x[4] - xi) + v8[5] * (x[5] - xi);
-                    const real e3 = v8[6] * (x[6] - xi) + v8[7] * (x[7] - xi);
-                    p8 = (e0 + e1) + (e2 + e3);
-                }
-                if (h4) {
-                    const real* x = xs + b4;
-                    p4 = (v4[0] * (x[0] - xi) + v4[1] * (x[1] - xi)) + (v4[2] * (x[2] - xi) + v4[3] * (x[3] - xi));
-                }
-                if (h2) {
-                    const real* x = xs + b2;
-                    p2 = v2[0] * (x[0] - xi) + v2[1] * (x[1] - xi);
-                }
-                if (h1) p1 = v1 * (xs[b1] - xi);
-                kahan_add(s, c, (p8 + p4) + (p2 + p1));
             }
         }
         real t = s - c;
