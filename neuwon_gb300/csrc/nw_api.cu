@@ -639,10 +639,10 @@ int nw_propagator_stats(nw_ctx* ctx, int64_t* rows, int64_t* nnz, int64_t* store
     if (rows) *rows = ctx->n_seg;
     if (nnz) *nnz = ctx->nnz64;
     if (ctx->prop_format == 3 && ctx->b_ok) {
-        // Windows format: per window its values and a 16-bit base; per row 4 x u32
-        // window offsets and the leak.
+        // Windows format: per window its values and a 16-bit base (value blocks
+        // padded to 4 values); per row a 16-byte descriptor and the leak.
         NW_CHECK(ensure_windows(ctx));
-        const int64_t slots = 8 * ctx->nwin[0] + 4 * ctx->nwin[1] + 2 * ctx->nwin[2] + ctx->nwin[3];
+        const int64_t slots = ctx->win_slots;
         const int64_t windows = ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3];
         if (stored) *stored = slots;
         if (bytes) *bytes = slots * ctx->precision + 2 * windows + ctx->n_seg * (16 + ctx->precision);

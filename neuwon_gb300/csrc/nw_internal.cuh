@@ -201,11 +201,14 @@ struct nw_ctx {
     nw::DevBuf wq_rowptr, wq_base, wq_val;
     // Windows format of the batched path: each row's off-diagonal entries covered
     // by windows of 8, 4, 2 or 1 consecutive columns (u16 neuron-relative base +
-    // the window's values), grouped by width; win_row holds 4 x u32 window offsets
-    // per row (one per width), n_seg + 1 rows.
+    // the window's values).  Per row one block of values (its 8-, 4-, 2- then 1-wide
+    // windows' values; blocks start on 4-value boundaries) and one block of bases in
+    // the same order; win_row holds per row {value block / 4, first base, n8 | n4 << 16,
+    // n2 | n1 << 16}.
     bool win_ok = false;
     int64_t nwin[4] = {0, 0, 0, 0};                    // windows of width 8, 4, 2, 1
-    nw::DevBuf win_row, win_base[4], win_val[4];
+    int64_t win_slots = 0;                             // value slots, block padding included
+    nw::DevBuf win_row, win_base, win_val;
     int prop_format = 0;                               // 0: rows, 1: pairs, 2: quads, 3: windows
     int pair_shared_limit = -1;                        // cap on neurons with shared-memory sums (-1: none)
 

@@ -746,10 +746,10 @@ __global__ void quad_fill_kernel(int64_t n, const int64_t* nstart_of_row, const 
 // Each row's off-diagonal entries (neuron-relative columns, increasing) are
 // covered by windows of 8, 4, 2 or 1 consecutive columns: one 16-bit base per
 // window and the window's values (zeros where a column is not kept), grouped by
-// width.  Walking the row, the window opened at the first uncovered entry c is
-// the width with the fewest bytes per entry it covers (2 B base + width values;
-// ties go to the wider window).  Windows may reach up to 7 columns past the
-// neuron's last segment, where the kernel keeps x at zero.
+// width within the row.  Walking the row, the window opened at the first
+// uncovered entry c is the width with the fewest bytes per entry it covers (2 B
+// base + width values; ties go to the wider window).  Windows may reach up to 7
+// columns past the neuron's last segment, where the kernel keeps x at zero.
 template <typename real>
 __device__ __forceinline__ int window_width(const int32_t* pcol, int64_t k, int64_t end, int64_t row,
                                             int64_t* next) {
@@ -793,16 +793,23 @@ __global__ void window_count_kernel(int64_t n, const int64_t* prow, const int32_
     for (int w = 0; w < 4; ++w) cnt[4 * r + w] = c4[w];
 }
 
+// Writes row r's windows into its blocks: values of the 8-, 4-, 2- then 1-wide
+// windows from 4 * d.x, bases in the same order from d.y.
 template <typename real>
 __global__ void window_fill_kernel(int64_t n, const int64_t* row_lo, const int64_t* prow, const int32_t* pcol,
-                                   const double* pval, const uint32_t* wrow, uint16_t* b8, uint16_t* b4,
-                                   uint16_t* b2, uint16_t* b1, real* v8, real* v4, real* v2, real* v1) {
+                                   const double* pval, const uint4* desc, uint16_t* wbase, real* wval) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= n) return;
     const int widths[4] = {8, 4, 2, 1};
-    uint16_t* bases[4] = {b8, b4, b2, b1};
-    real* vals[4] = {v8, v4, v2, v1};
-    uint32_t pos[4] = {wrow[4 * r], wrow[4 * r + 1], wrow[4 * r + 2], wrow[4 * r + 3]};
+    const uint4 d = desc[r];
+    const uint32_t cnt[4] = {d.z & 0xffffu, d.z >> 16, d.w & 0xffffu, d.w >> 16};
+    int64_t voff[4], boff[4];
+    voff[0] = 4 * (int64_t)d.x;
+    boff[0] = d.y;
+    for (int w = 1; w < 4; ++w) {
+        voff[w] = voff[w - 1] + (int64_t)widths[w - 1] * cnt[w - 1];
+        boff[w] = boff[w - 1] + cnt[w - 1];
+    }
     const int64_t lo = row_lo[r], end = prow[r + 1];
     int64_t k = prow[r];
     while (k < end && pcol[k] == r) ++k;
@@ -810,9 +817,9 @@ __global__ void window_fill_kernel(int64_t n, const int64_t* row_lo, const int64
         int64_t next;
         const int w = window_width<real>(pcol, k, end, r, &next);
         const int64_t c = pcol[k];
-        const uint32_t q = pos[w]++;
-        bases[w][q] = (uint16_t)(c - lo);
-        real* v = vals[w] + (int64_t)q * widths[w];
+        wbase[boff[w]++] = (uint16_t)(c - lo);
+        real* v = wval + voff[w];
+        voff[w] += widths[w];
         for (int j = 0; j < widths[w]; ++j) v[j] = real(0);
         for (int64_t e = k; e < next; ++e)
             if (pcol[e] != r) v[pcol[e] - c] = (real)pval[e];
@@ -823,11 +830,10 @@ __global__ void window_fill_kernel(int64_t n, const int64_t* row_lo, const int64
 
 static void free_windows(nw_ctx* ctx) {
     dev_free(ctx->win_row);
-    for (int w = 0; w < 4; ++w) {
-        dev_free(ctx->win_base[w]);
-        dev_free(ctx->win_val[w]);
-        ctx->nwin[w] = 0;
-    }
+    dev_free(ctx->win_base);
+    dev_free(ctx->win_val);
+    for (int w = 0; w < 4; ++w) ctx->nwin[w] = 0;
+    ctx->win_slots = 0;
     ctx->win_ok = false;
 }
 
@@ -857,46 +863,45 @@ int ensure_windows(nw_ctx* ctx) {
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "windows format count"); break; }
         if (flag) { rc = fail(ctx, NW_ERR_STATE, "windows format: propagator rows are not sorted by column"); break; }
-        // Window offsets of each row, per width (4 x u32 per row).
-        std::vector<uint32_t> wrow(4 * (n + 1), 0);
-        uint64_t tot[4] = {0, 0, 0, 0};
-        for (int64_t i = 0; i < n; ++i)
-            for (int w = 0; w < 4; ++w) {
-                wrow[4 * i + w] = (uint32_t)tot[w];
-                tot[w] += (uint64_t)cnt[4 * i + w];
+        // Row descriptors: value blocks rounded up to 4 values, bases back to back.
+        std::vector<uint32_t> desc(4 * std::max<int64_t>(n, 1), 0);
+        uint64_t vq = 0, nb = 0, tot[4] = {0, 0, 0, 0};
+        for (int64_t i = 0; i < n && rc == NW_OK; ++i) {
+            const int32_t* c = &cnt[4 * i];
+            if (vq > UINT32_MAX || nb > UINT32_MAX) {
+                rc = fail(ctx, NW_ERR_LIMIT, "windows format: more than 2^32 windows or value quads");
+                break;
             }
-        for (int w = 0; w < 4 && rc == NW_OK; ++w) {
-            if (tot[w] > UINT32_MAX) rc = fail(ctx, NW_ERR_LIMIT, "windows format: 2^32 or more windows of one width");
-            else wrow[4 * n + w] = (uint32_t)tot[w];
+            desc[4 * i] = (uint32_t)vq;
+            desc[4 * i + 1] = (uint32_t)nb;
+            desc[4 * i + 2] = (uint32_t)c[0] | ((uint32_t)c[1] << 16);
+            desc[4 * i + 3] = (uint32_t)c[2] | ((uint32_t)c[3] << 16);
+            vq += (uint64_t)(8 * c[0] + 4 * c[1] + 2 * c[2] + c[3] + 3) / 4;
+            nb += (uint64_t)(c[0] + c[1] + c[2] + c[3]);
+            for (int w = 0; w < 4; ++w) tot[w] += (uint64_t)c[w];
         }
         if (rc != NW_OK) break;
-        const int widths[4] = {8, 4, 2, 1};
-        if ((rc = dev_alloc(ctx, ctx->win_row, 16 * (n + 1))) != NW_OK) break;
-        for (int w = 0; w < 4 && rc == NW_OK; ++w) {
-            rc = dev_alloc(ctx, ctx->win_base[w], 2 * std::max<uint64_t>(tot[w], 8));
-            if (rc == NW_OK)
-                rc = dev_alloc(ctx, ctx->win_val[w], (size_t)ctx->precision * widths[w] * std::max<uint64_t>(tot[w], 1));
-            ctx->nwin[w] = (int64_t)tot[w];
-        }
-        if (rc != NW_OK) break;
+        for (int w = 0; w < 4; ++w) ctx->nwin[w] = (int64_t)tot[w];
+        ctx->win_slots = (int64_t)(4 * vq);
+        if ((rc = dev_alloc(ctx, ctx->win_row, 16 * std::max<int64_t>(n, 1))) != NW_OK) break;
+        if ((rc = dev_alloc(ctx, ctx->win_base, 2 * std::max<uint64_t>(nb, 8))) != NW_OK) break;
+        const size_t vbytes = (size_t)ctx->precision * 4 * std::max<uint64_t>(vq, 1);
+        if ((rc = dev_alloc(ctx, ctx->win_val, vbytes)) != NW_OK) break;
         std::vector<int64_t> lo(n);
         for (int64_t j = 0; j < ctx->n_neuron; ++j)
             for (int64_t i = ctx->h_neuron_start[j]; i < ctx->h_neuron_start[j + 1]; ++i) lo[i] = ctx->h_neuron_start[j];
         if ((rc = dev_alloc(ctx, d_lo, 8 * std::max<int64_t>(n, 1))) != NW_OK) break;
-        cudaMemcpyAsync(ctx->win_row.ptr, wrow.data(), 16 * (n + 1), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemsetAsync(ctx->win_val.ptr, 0, vbytes, ctx->stream);        // block padding reads as zero
+        cudaMemcpyAsync(ctx->win_row.ptr, desc.data(), 16 * n, cudaMemcpyHostToDevice, ctx->stream);
         cudaMemcpyAsync(d_lo.ptr, lo.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream);
-        uint16_t* B[4];
-        for (int w = 0; w < 4; ++w) B[w] = ctx->win_base[w].as<uint16_t>();
         if (ctx->precision == NW_F64)
             window_fill_kernel<double><<<blocks, 128, 0, ctx->stream>>>(
                 n, d_lo.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
-                ctx->win_row.as<uint32_t>(), B[0], B[1], B[2], B[3], ctx->win_val[0].as<double>(),
-                ctx->win_val[1].as<double>(), ctx->win_val[2].as<double>(), ctx->win_val[3].as<double>());
+                ctx->win_row.as<uint4>(), ctx->win_base.as<uint16_t>(), ctx->win_val.as<double>());
         else
             window_fill_kernel<float><<<blocks, 128, 0, ctx->stream>>>(
                 n, d_lo.as<int64_t>(), ctx->p_rowptr.as<int64_t>(), ctx->p_col.as<int32_t>(), ctx->p_val.as<double>(),
-                ctx->win_row.as<uint32_t>(), B[0], B[1], B[2], B[3], ctx->win_val[0].as<float>(),
-                ctx->win_val[1].as<float>(), ctx->win_val[2].as<float>(), ctx->win_val[3].as<float>());
+                ctx->win_row.as<uint4>(), ctx->win_base.as<uint16_t>(), ctx->win_val.as<float>());
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "windows format fill"); break; }
         ctx->win_ok = true;

@@ -100,11 +100,9 @@ struct StepArgs {
     const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
     // quad propagator: windows of 4 consecutive columns
     const int64_t* qrow; const uint16_t* qbase; const real* qval;
-    // windows propagator: per row 4 x u32 window offsets (widths 8, 4, 2, 1), then
-    // per width the u16 bases and the values
-    const uint4* wnrow;
-    const uint16_t* wnb8; const uint16_t* wnb4; const uint16_t* wnb2; const uint16_t* wnb1;
-    const real* wnv8; const real* wnv4; const real* wnv2; const real* wnv1;
+    // windows propagator: per row a descriptor {value block / 4, first base,
+    // n8 | n4 << 16, n2 | n1 << 16}, the u16 bases and the values
+    const uint4* wnrow; const uint16_t* wnbase; const real* wnval;
     // pair ("flux") propagator: rows of owned pairs, leak, c_max / c_i, global accumulators
     const int64_t* frow; const uint16_t* fcol; const real* fval; const real* fleak; const real* frc;
     unsigned long long* facc; int facc_cap; int frc_smem;
@@ -625,13 +623,14 @@ __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t
     }
 }
 
-// Windows format: row i is four lists of windows, of widths 8, 4, 2 and 1 (base b,
-// values for columns b..b+w-1).  The row's windows form one list of items of at
-// most 4 values: an 8-wide window is two items (its halves), the others one each;
-// the row's lanes take consecutive items, UNROLL items per lane loaded before any
-// is used (as in the quad format), and every item is summed as a 4-column window
-// with zero weights past its width.  Windows may reach 7 columns past the neuron's
-// last segment, where x holds zeros.
+// Windows format: row i is a list of windows of widths 8, 4, 2 and 1 (base b,
+// values for columns b..b+w-1), stored as one contiguous block of values and one
+// of bases.  The row's windows form one list of items of at most 4 values: an
+// 8-wide window is two items (its halves), the others one each, so items t < e4
+// are 4 values at 4t in the block; the row's lanes take consecutive items, UNROLL
+// items per lane loaded before any is used (as in the quad format), and every item
+// is summed as a 4-column window with zero weights past its width.  Windows may
+// reach 7 columns past the neuron's last segment, where x holds zeros.
 template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
 __device__ __forceinline__ void propagate_windows(const StepArgs<real>& a, int64_t base, int n,
                                                   const real* __restrict__ xs, Fin fin) {
@@ -646,9 +645,11 @@ __device__ __forceinline__ void propagate_windows(const StepArgs<real>& a, int64
         real s = real(0), c = real(0), xi = real(0);
         if (valid) {
             const int64_t r = base + row;
-            const uint4 o0 = __ldg(a.wnrow + r), o1 = __ldg(a.wnrow + r + 1);
-            const uint32_t e8 = 2 * (o1.x - o0.x), e4 = e8 + (o1.y - o0.y), e2 = e4 + (o1.z - o0.z);
-            const uint32_t e1 = e2 + (o1.w - o0.w);
+            const uint4 d = __ldg(a.wnrow + r);
+            const real* __restrict__ vb = a.wnval + 4 * (int64_t)d.x;
+            const uint16_t* __restrict__ bb = a.wnbase + d.y;
+            const uint32_t n8 = d.z & 0xffffu;
+            const uint32_t e8 = 2 * n8, e4 = e8 + (d.z >> 16), e2 = e4 + (d.w & 0xffffu), e1 = e2 + (d.w >> 16);
             xi = xs[row];
             for (uint32_t t0 = l; t0 < e1; t0 += LPR * UNROLL) {
                 real v[UNROLL][4];
@@ -658,25 +659,17 @@ __device__ __forceinline__ void propagate_windows(const StepArgs<real>& a, int64
                     const uint32_t t = t0 + LPR * u;
                     v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
                     b[u] = 0;                                 // zero weights on x[0..3]
-                    if (t < e8) {
-                        const int64_t k = (int64_t)o0.x + (t >> 1);
-                        const int h = 4 * (int)(t & 1);
-                        Vec4Loader<real>::load(a.wnv8 + 8 * k + h, v[u]);
-                        b[u] = __ldcs(a.wnb8 + k) + h;
-                    } else if (t < e4) {
-                        const int64_t k = (int64_t)o0.y + (t - e8);
-                        Vec4Loader<real>::load(a.wnv4 + 4 * k, v[u]);
-                        b[u] = __ldcs(a.wnb4 + k);
+                    if (t < e4) {
+                        Vec4Loader<real>::load(vb + 4 * t, v[u]);
+                        b[u] = t < e8 ? __ldcs(bb + (t >> 1)) + 4 * (int)(t & 1) : __ldcs(bb + (t - n8));
                     } else if (t < e2) {
-                        const int64_t k = (int64_t)o0.z + (t - e4);
                         real w2[2];
-                        Vec2Loader<real>::load(a.wnv2 + 2 * k, w2);
+                        Vec2Loader<real>::load(vb + 4 * e4 + 2 * (t - e4), w2);
                         v[u][0] = w2[0]; v[u][1] = w2[1];
-                        b[u] = __ldcs(a.wnb2 + k);
+                        b[u] = __ldcs(bb + (t - n8));
                     } else if (t < e1) {
-                        const int64_t k = (int64_t)o0.w + (t - e2);
-                        v[u][0] = __ldcs(a.wnv1 + k);
-                        b[u] = __ldcs(a.wnb1 + k);
+                        v[u][0] = __ldcs(vb + 4 * e4 + 2 * (e2 - e4) + (t - e2));
+                        b[u] = __ldcs(bb + (t - n8));
                     }
                 }
 #pragma unroll
@@ -738,10 +731,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.qrow = ctx->q_rowptr.as<int64_t>(); a.qbase = ctx->q_base.as<uint16_t>(); a.qval = ctx->q_val.as<real>();
     if (ctx->win_ok) {
         a.wnrow = ctx->win_row.as<uint4>();
-        a.wnb8 = ctx->win_base[0].as<uint16_t>(); a.wnb4 = ctx->win_base[1].as<uint16_t>();
-        a.wnb2 = ctx->win_base[2].as<uint16_t>(); a.wnb1 = ctx->win_base[3].as<uint16_t>();
-        a.wnv8 = ctx->win_val[0].as<real>(); a.wnv4 = ctx->win_val[1].as<real>();
-        a.wnv2 = ctx->win_val[2].as<real>(); a.wnv1 = ctx->win_val[3].as<real>();
+        a.wnbase = ctx->win_base.as<uint16_t>(); a.wnval = ctx->win_val.as<real>();
     }
     a.frow = ctx->f_rowptr.as<int64_t>(); a.fcol = ctx->f_col.as<uint16_t>();
     a.fval = ctx->f_val.as<real>(); a.fleak = ctx->f_leak.as<real>(); a.frc = ctx->f_rc.as<real>();
