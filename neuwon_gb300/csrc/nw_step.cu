@@ -752,7 +752,8 @@ static bool bulk_fits(nw_ctx* ctx) {
 }
 
 bool uses_bulk_pipeline(nw_ctx* ctx) {
-    return ctx->precision == NW_F32 && ctx->use_bulk && ctx->lanes_per_row == 0 && bulk_fits(ctx);
+    return ctx->precision == NW_F32 && ctx->use_bulk && ctx->lanes_per_row == 0 && ctx->prop_format == 0 &&
+           bulk_fits(ctx);
 }
 
 template <typename real>
