@@ -13,8 +13,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libneuwon_gb300.so")
-SOURCES = ["nw_api.cu", "nw_step.cu", "nw_propagator.cu", "nw_noalloc.cu", "nw_adjoint.cu", "nw_tune.cu", "nw_wide.cu", "nw_species.cu", "nw_lti.cu"]
-HEADERS = ["nw_internal.cuh", "nw_step_common.cuh", os.path.join("..", "..", "include", "neuwon_gb300.h")]
+SOURCES = ["nw_step_f32.cu", "nw_step_f64.cu", "nw_api.cu", "nw_step.cu", "nw_propagator.cu", "nw_noalloc.cu", "nw_adjoint.cu", "nw_tune.cu", "nw_wide.cu", "nw_species.cu", "nw_lti.cu"]
+HEADERS = ["nw_internal.cuh", "nw_step_common.cuh", "nw_step_batched.cuh", os.path.join("..", "..", "include", "neuwon_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
          "--expt-relaxed-constexpr"]

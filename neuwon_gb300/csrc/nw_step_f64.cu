@@ -1,0 +1,7 @@
+// FP64 instances of the batched step kernel (one translation unit per
+// precision, so the two compile in parallel).
+#include "nw_step_batched.cuh"
+
+namespace nw {
+template int config_batched<double>(nw_ctx*, BatchedCfg<double>&);
+}  // namespace nw
