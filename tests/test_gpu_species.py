@@ -170,7 +170,7 @@ def test_nmodl_channels_on_device_match_oracle(tmp_path):
     nr = m.add_tree(tree)
     for name in ("hh", "ktest", "leak"):
         m.insert_everywhere(name)
-    nr.root.inject_current(0.3, 20.0)
+    nr.root.inject_current(1.0, 20.0)
     parent, R, C, area, offs = concat([tree])
     n = len(tree)
     seg = np.arange(n)
@@ -184,7 +184,7 @@ def test_nmodl_channels_on_device_match_oracle(tmp_path):
                                      species=species))
     f, c = clamp_ticks(0.0, 20.0, dt)
     om = OracleModel(parent, R, C, time_step=dt, celsius=celsius, hh=HHInstances(seg, area, celsius=celsius, **hh_kw),
-                     kinetic=kins, species={"k": -80.0}, clamps=[(0, 0.3e-9, f, c)], detectors=[(0, 20.0)])
+                     kinetic=kins, species={"k": -80.0}, clamps=[(0, 1.0e-9, f, c)], detectors=[(0, 20.0)])
     m.advance(steps)
     for _ in range(steps):
         om.advance()
