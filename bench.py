@@ -168,13 +168,17 @@ class CpuSample:
                 f"steps, FP64 C restatement (oracle/cpu_step.c) with OpenMP, built on the CPU in {self.build_s:.0f} s")
 
     def steps_for(self, seconds):
-        """Steps that take about `seconds` (measured on a short run; advances the model)."""
-        t0 = time.perf_counter()
-        k = 0
-        while time.perf_counter() - t0 < 0.2:
-            self.co.advance(1)
-            k += 1
-        return max(1, int(k * seconds / (time.perf_counter() - t0)))
+        """Steps that take about `seconds`, from calls of 1, 2, 4, ... steps until one
+        takes 0.5 s (multi-step calls, as timed, so the per-call thread start-up is
+        not charged to every step; advances the model)."""
+        k = 1
+        while True:
+            t0 = time.perf_counter()
+            self.co.advance(k)
+            dt = time.perf_counter() - t0
+            if dt >= 0.5:
+                return max(1, int(k * seconds / dt))
+            k *= 2
 
 
 def cpu_sample(trees, currents, tol, lump=True, time_budget_s=15.0, warmup=2):
@@ -207,7 +211,7 @@ def run_reference(args, rank):
     currents = batched_currents(args.neurons)
     cs = CpuSample(trees, currents, args.tol, bool(args.lump))
     K = max(1, args.steps)
-    chunk = cs.steps_for(max(0.5, 10.0 / K))
+    chunk = cs.steps_for(max(0.5, 11.0 / K))
     for _ in range(max(args.warmup, 1)):
         cs.co.advance(chunk)
     t0 = time.perf_counter()
