@@ -547,6 +547,28 @@ def network_leg(device, steps, neurons=4096, synapses=2_000_000):
     return out
 
 
+def run_leg(args, rank, local):
+    """One side leg alone (rank 0), at its configuration's shape or a smaller case."""
+    if rank != 0:
+        return
+    if args.leg == "plain":
+        from neuwon_gb300.workloads import batched_currents, batched_trees
+        k = args.leg_neurons or 64
+        lo, hi = (int(x) for x in args.size_range.split(","))
+        trees = batched_trees(args.neurons, first=0, count=k, processes=min(16, os.cpu_count() or 1), lo=lo, hi=hi)
+        currents = batched_currents(args.neurons)[:k]
+    import torch
+    torch.cuda.set_device(local)
+    if args.leg == "adjoint":
+        out = adjoint_leg(local, args.adjoint_steps, neurons=args.leg_neurons or 256, size=args.leg_size or 2000)
+    elif args.leg == "network":
+        out = network_leg(local, args.network_steps, neurons=args.leg_neurons or 4096,
+                          synapses=args.leg_synapses or 2_000_000)
+    else:
+        out = plain_timing(trees, currents, args.tol, local)
+    print(json.dumps({"leg": args.leg, **out}), flush=True)
+
+
 def _lib_ptr(a):
     from neuwon_gb300 import _lib
     return _lib.ptr(a)
@@ -649,6 +671,12 @@ def main():
                     help="differentiation configuration: FP32/FP64 adjoint vs FP64 central differences (own JSON line)")
     ap.add_argument("--diff-steps", type=int, default=8000)
     ap.add_argument("--diff-neurons", type=int, default=256)
+    ap.add_argument("--leg", choices=["adjoint", "network", "plain"],
+                    help="run one side leg alone and print its JSON line (a small case with --leg-neurons, "
+                         "--leg-size, --leg-synapses, --adjoint-steps / --network-steps)")
+    ap.add_argument("--leg-neurons", type=int, default=0)
+    ap.add_argument("--leg-size", type=int, default=0, help="segments per neuron (adjoint leg)")
+    ap.add_argument("--leg-synapses", type=int, default=0)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -669,6 +697,9 @@ def main():
         torch.cuda.set_device(local)
         if rank == 0:
             diff_check(args, local)
+        return
+    if args.leg:
+        run_leg(args, rank, local)
         return
 
     from neuwon_gb300.workloads import batched_currents, batched_trees, build_model

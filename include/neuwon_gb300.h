@@ -290,7 +290,9 @@ int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_s
 /* Autotuner of the batched path (replaces the fixed 32-threads-per-block launch of
  * the reference's GPU kernels, neuwon/database/compute.py:360-418): times short runs
  * of this model over lanes per row {4, 8, 16, 32} x threads {512, 768, 1024} (plus the
- * bulk-copy pipeline for FP32), then the fusion depth over {1, 2, 5, ..., 500} steps
+ * bulk-copy pipeline for FP32), then (quad format, 8 or more lanes) the row-length
+ * split "lanes_split" over {1, 2, 3, 4, 6} x lanes quads per row (kept only when 0.5 %
+ * faster than none), then the fusion depth over {1, 2, 5, ..., 500} steps
  * up to 4 x trial_steps, and keeps the fastest (ties within 1 % go to deeper fusion).
  * The model's state, clock and probes are restored afterwards.  Outputs may be NULL;
  * lanes_per_row 0 means the bulk pipeline was chosen. */
@@ -349,6 +351,9 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * format falls back to rows and the adjoint refuses it.
  * "set_steps" (k): resume at step k (clock, input ticks 2k, conductances valid when
  * k > 0 and mechanisms exist; probes start empty), for restoring a checkpoint.
+ * "lanes_split" (default 0; set by nw_autotune): with the quad format, neurons whose
+ * mean quads per row are below this value take half the kernel's lanes per row (the
+ * SpMV shape chosen by row length); nw_get_option("narrow_neurons") counts them.
  * "fusion_depth" (default 50, 0 = the whole call in one launch): steps per launch of
  * the batched kernel.  "cuda_graph" (default 1): replay batched launch sequences as
  * CUDA graphs; "prepare_graph" (k) captures, without running, the graph that a later

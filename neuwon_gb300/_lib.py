@@ -183,13 +183,16 @@ class Context:
 
     def autotune(self, trial_steps=10):
         """Times the batched path's launch shapes on this model and keeps the fastest;
-        returns dict(lanes_per_row, threads, fusion_depth, ms_per_step)."""
+        returns dict(lanes_per_row, threads, fusion_depth, ms_per_step, lanes_split,
+        narrow_neurons): with the quad format, neurons whose mean quads per row are
+        below lanes_split (narrow_neurons of them) take half the lanes per row."""
         l, t, f = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         ms = ctypes.c_double()
         self.call("nw_autotune", int(trial_steps), ctypes.byref(l), ctypes.byref(t), ctypes.byref(f),
                   ctypes.byref(ms))
         return {"lanes_per_row": l.value, "threads": t.value, "fusion_depth": f.value,
-                "ms_per_step": ms.value}
+                "ms_per_step": ms.value, "lanes_split": self.get_option("lanes_split"),
+                "narrow_neurons": self.get_option("narrow_neurons")}
 
     def propagator_csr(self):
         nnz = ctypes.c_int64()

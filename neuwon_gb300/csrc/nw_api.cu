@@ -1216,6 +1216,13 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         ctx->prop_format = (int)value;
         return NW_OK;
     }
+    if (nm == "lanes_split") {
+        // Quad format: neurons whose mean quads per row are below this take half the
+        // lanes per row of the kernel's choice (0: all neurons the same).
+        if (value < 0 || value > 65535) return fail(ctx, NW_ERR_ARG, "lanes_split must be in [0, 65535]");
+        ctx->lanes_split = value;
+        return NW_OK;
+    }
     if (nm == "fusion_depth") {
         if (value < 0 || value > (1 << 20)) return fail(ctx, NW_ERR_ARG, "fusion_depth must be in [0, 2^20]");
         ctx->fusion = (int)value;
@@ -1272,6 +1279,14 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "kinetic_mechanisms") { *value = ctx->n_kin; return NW_OK; }
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "quads") { *value = ctx->nq; return NW_OK; }
+    if (nm == "lanes_split") { *value = ctx->lanes_split; return NW_OK; }
+    if (nm == "narrow_neurons") {
+        int64_t k = 0;
+        if (ctx->q_ok && ctx->lanes_split > 0)
+            for (float q : ctx->h_neuron_qpr) k += q < (float)ctx->lanes_split ? 1 : 0;
+        *value = k;
+        return NW_OK;
+    }
     if (nm == "windows") { *value = ctx->nwin[0] + ctx->nwin[1] + ctx->nwin[2] + ctx->nwin[3]; return NW_OK; }
     if (nm == "windows_8") { *value = ctx->nwin[0]; return NW_OK; }
     if (nm == "windows_4") { *value = ctx->nwin[1]; return NW_OK; }

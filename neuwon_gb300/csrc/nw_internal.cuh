@@ -195,6 +195,12 @@ struct nw_ctx {
     // column is not kept); rows with depth-first numbering form long runs.
     bool q_ok = false;
     int64_t nq = 0;
+    // Lane count by row length: neurons whose mean quads per row are below
+    // lanes_split take half the kernel's lanes per row (0: every neuron the same).
+    std::vector<float> h_neuron_qpr;                   // mean quads per row, per neuron
+    int64_t lanes_split = 0;
+    int64_t narrow_for = -1;                           // lanes_split the flags were made for
+    nw::DevBuf neuron_narrow;                          // u8 per neuron
     nw::DevBuf q_rowptr, q_base, q_val;                // i64 (in quads), u16 (neuron-relative), real x 4
     bool wq_ok = false;                                // wide path: global 32-bit bases
     int64_t nwq = 0;
@@ -311,6 +317,7 @@ int ensure_flux(nw_ctx* ctx);
 int ensure_quads(nw_ctx* ctx);
 int ensure_wide_quads(nw_ctx* ctx);
 int ensure_windows(nw_ctx* ctx);
+int ensure_narrow(nw_ctx* ctx);
 void free_quads(nw_ctx* ctx);
 void free_flux(nw_ctx* ctx);
 void free_wide(nw_ctx* ctx);

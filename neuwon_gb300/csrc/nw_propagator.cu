@@ -913,6 +913,8 @@ int ensure_windows(nw_ctx* ctx) {
 
 void free_quads(nw_ctx* ctx) {
     free_windows(ctx);
+    dev_free(ctx->neuron_narrow);
+    ctx->narrow_for = -1;
     for (DevBuf* b : {&ctx->q_rowptr, &ctx->q_base, &ctx->q_val, &ctx->wq_rowptr, &ctx->wq_base, &ctx->wq_val})
         dev_free(*b);
     ctx->q_ok = ctx->wq_ok = false;
@@ -923,7 +925,8 @@ void free_quads(nw_ctx* ctx) {
 // 32-bit bases (wide path; windows of neurons of fewer than 4 segments may
 // reach into the neighbouring segments, whose weights are zero).
 template <typename BT>
-static int build_quads(nw_ctx* ctx, bool relative, DevBuf& R, DevBuf& B, DevBuf& V, int64_t* nq_out) {
+static int build_quads(nw_ctx* ctx, bool relative, DevBuf& R, DevBuf& B, DevBuf& V, int64_t* nq_out,
+                       std::vector<int64_t>* qrow_out = nullptr) {
     const int64_t n = ctx->n_seg;
     std::vector<int64_t> lo(n), hi(n);
     for (int64_t j = 0; j < ctx->n_neuron; ++j) {
@@ -967,6 +970,7 @@ static int build_quads(nw_ctx* ctx, bool relative, DevBuf& R, DevBuf& B, DevBuf&
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "quad format fill"); break; }
         *nq_out = nq;
+        if (qrow_out) qrow_out->swap(qrow);
     } while (0);
     cleanup();
     return rc;
@@ -975,8 +979,29 @@ static int build_quads(nw_ctx* ctx, bool relative, DevBuf& R, DevBuf& B, DevBuf&
 int ensure_quads(nw_ctx* ctx) {
     if (ctx->q_ok) return NW_OK;
     if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "quad format: needs the batched format (neurons <= 65,535)");
-    NW_CHECK(build_quads<uint16_t>(ctx, true, ctx->q_rowptr, ctx->q_base, ctx->q_val, &ctx->nq));
+    std::vector<int64_t> qrow;
+    NW_CHECK(build_quads<uint16_t>(ctx, true, ctx->q_rowptr, ctx->q_base, ctx->q_val, &ctx->nq, &qrow));
+    ctx->h_neuron_qpr.assign(ctx->n_neuron, 0.f);
+    for (int64_t j = 0; j < ctx->n_neuron; ++j) {
+        const int64_t a = ctx->h_neuron_start[j], b = ctx->h_neuron_start[j + 1];
+        if (b > a) ctx->h_neuron_qpr[j] = (float)((double)(qrow[b] - qrow[a]) / (double)(b - a));
+    }
+    ctx->narrow_for = -1;
     ctx->q_ok = true;
+    return NW_OK;
+}
+
+// Per-neuron flags of the quad format's narrow rows (mean quads per row below
+// lanes_split), rebuilt when the threshold or the format changes.
+int ensure_narrow(nw_ctx* ctx) {
+    if (ctx->lanes_split <= 0 || !ctx->q_ok) return NW_OK;
+    if (ctx->narrow_for == ctx->lanes_split && ctx->neuron_narrow.ptr) return NW_OK;
+    std::vector<uint8_t> f(std::max<int64_t>(ctx->n_neuron, 1), 0);
+    for (int64_t j = 0; j < ctx->n_neuron; ++j) f[j] = ctx->h_neuron_qpr[j] < (float)ctx->lanes_split ? 1 : 0;
+    if (!ctx->neuron_narrow.ptr) NW_CHECK(dev_alloc(ctx, ctx->neuron_narrow, f.size()));
+    NW_CUDA(ctx, cudaMemcpyAsync(ctx->neuron_narrow.ptr, f.data(), f.size(), cudaMemcpyHostToDevice, ctx->stream));
+    NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->narrow_for = ctx->lanes_split;
     return NW_OK;
 }
 

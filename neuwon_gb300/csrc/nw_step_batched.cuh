@@ -451,10 +451,16 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                         flux_finalize(a, base, n, xs, gacc);
                     }
                 } else if (QUAD) {
-                    propagate_quads<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real vnew) {
+                    auto store = [&](int64_t r, int, real, real vnew) {
                         if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
                         a.V[r] = vnew;
-                    });
+                    };
+                    // Neurons of short rows (mean quads per row below the tuned split)
+                    // take half the lanes per row, the others the kernel's LPR.
+                    if (LPR >= 8 && a.neuron_narrow && a.neuron_narrow[j])
+                        propagate_quads<real, (LPR >= 8 ? LPR / 2 : LPR)>(a, base, n, xs, store);
+                    else
+                        propagate_quads<real, LPR>(a, base, n, xs, store);
                 } else if (WIN) {
                     propagate_windows<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real vnew) {
                         if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
@@ -657,6 +663,7 @@ int config_batched(nw_ctx* ctx, BatchedCfg<real>& c) {
     }
     if (ctx->prop_format == 2) {
         NW_CHECK(ensure_quads(ctx));
+        NW_CHECK(ensure_narrow(ctx));
         if (fuse_mechanisms(ctx)) {
             switch (choose_lanes_per_row(ctx)) {
                 case 4: return config_batched_lpr<real, 4, false, false, true, true>(ctx, c);

@@ -100,6 +100,7 @@ struct StepArgs {
     const int64_t* prow; const int32_t* pcol; const double* pval; real* px;
     // quad propagator: windows of 4 consecutive columns
     const int64_t* qrow; const uint16_t* qbase; const real* qval;
+    const uint8_t* neuron_narrow;     // quad rows of these neurons take half the lanes (null: none)
     // windows propagator: per row a descriptor {value block / 4, first base,
     // n8 | n4 << 16, n2 | n1 << 16}, the u16 bases and the values
     const uint4* wnrow; const uint16_t* wnbase; const real* wnval;
@@ -729,6 +730,8 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.prow = ctx->p_rowptr.as<int64_t>(); a.pcol = ctx->p_col.as<int32_t>(); a.pval = ctx->p_val.as<double>();
     a.px = ctx->plain_x.as<real>();
     a.qrow = ctx->q_rowptr.as<int64_t>(); a.qbase = ctx->q_base.as<uint16_t>(); a.qval = ctx->q_val.as<real>();
+    a.neuron_narrow = (ctx->lanes_split > 0 && ctx->narrow_for == ctx->lanes_split)
+                          ? ctx->neuron_narrow.as<uint8_t>() : nullptr;
     if (ctx->win_ok) {
         a.wnrow = ctx->win_row.as<uint4>();
         a.wnbase = ctx->win_base.as<uint16_t>(); a.wnval = ctx->win_val.as<real>();

@@ -17,6 +17,7 @@ namespace nw {
 namespace {
 
 struct Saved {
+    int64_t split;
     int lanes, threads, fusion, ctas;
     bool graph, bulk, g_valid;
     int64_t n_probes, input_ticks, steps, probe_len;
@@ -50,7 +51,7 @@ struct Timer {
 int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes_out, int32_t* threads_out, int32_t* fusion_out,
              double* ms_out) {
     if (trial_steps < 1 || trial_steps > 10000) return fail(ctx, NW_ERR_ARG, "autotune: trial_steps in [1, 10000]");
-    Saved sv{ctx->lanes_per_row, ctx->threads, ctx->fusion, ctx->ctas_per_sm, ctx->use_graph, ctx->use_bulk,
+    Saved sv{ctx->lanes_split, ctx->lanes_per_row, ctx->threads, ctx->fusion, ctx->ctas_per_sm, ctx->use_graph, ctx->use_bulk,
              ctx->g_valid, ctx->n_probes, ctx->input_ticks, ctx->steps, ctx->probe_len};
 
     // Snapshot of the stepped state.
@@ -70,6 +71,7 @@ int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes_out, int32_t* threads_
         return NW_OK;
     };
     auto restore_settings = [&]() {
+        ctx->lanes_split = sv.split;
         ctx->lanes_per_row = sv.lanes; ctx->threads = sv.threads; ctx->fusion = sv.fusion;
         ctx->ctas_per_sm = sv.ctas; ctx->use_graph = sv.graph; ctx->use_bulk = sv.bulk;
         ctx->g_valid = sv.g_valid; ctx->n_probes = sv.n_probes; ctx->input_ticks = sv.input_ticks;
@@ -110,6 +112,7 @@ int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes_out, int32_t* threads_
     // Phase 1: row shape at one launch per trial.
     int best = -1;
     ctx->fusion = trial_steps;
+    ctx->lanes_split = 0;
     for (size_t i = 0; i < cands.size(); ++i) {
         ctx->lanes_per_row = cands[i].lanes;
         ctx->threads = cands[i].threads;
@@ -124,9 +127,28 @@ int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes_out, int32_t* threads_
     }
     if (rc == NW_OK && best < 0) rc = fail(ctx, NW_ERR_LIMIT, "autotune: no launch shape fits this model");
 
+    // Phase 1b (quad format, 8 or more lanes): the row length below which a neuron's
+    // rows take half the lanes, from the spread of the neurons' mean quads per row.
+    int64_t best_split = 0;
+    double best_ms = best >= 0 ? cands[best].ms : 0.0;
+    if (rc == NW_OK && ctx->prop_format == 2 && cands[best].lanes >= 8) {
+        ctx->lanes_per_row = cands[best].lanes;
+        ctx->threads = cands[best].threads;
+        ctx->use_bulk = cands[best].bulk;
+        const int64_t lanes = cands[best].lanes;
+        const int64_t split_opts[] = {lanes, 2 * lanes, 3 * lanes, 4 * lanes, 6 * lanes};
+        for (int64_t sp : split_opts) {
+            ctx->lanes_split = sp;
+            double ms = 0;
+            rc = trial(1, trial_steps, &ms);
+            if (rc != NW_OK) break;
+            if (ms < best_ms * 0.995) { best_ms = ms; best_split = sp; }
+        }
+    }
+    ctx->lanes_split = best_split;
+
     // Phase 2: fusion depth with that row shape, over the same step count.
     int best_f = trial_steps;
-    double best_ms = best >= 0 ? cands[best].ms : 0.0;
     if (rc == NW_OK) {
         ctx->lanes_per_row = cands[best].lanes;
         ctx->threads = cands[best].threads;
@@ -161,6 +183,7 @@ int autotune(nw_ctx* ctx, int trial_steps, int32_t* lanes_out, int32_t* threads_
     ctx->lanes_per_row = cands[best].lanes;
     ctx->threads = cands[best].threads;
     ctx->use_bulk = cands[best].bulk;
+    ctx->lanes_split = best_split;
     ctx->fusion = best_f;
     if (lanes_out) *lanes_out = cands[best].lanes;
     if (threads_out) *threads_out = cands[best].threads;

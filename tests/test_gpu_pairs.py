@@ -209,3 +209,42 @@ def test_windows_need_sorted_rows():
     m._ctx.set_option("propagator_format", 2)
     m._ctx.advance(1)
     m.close()
+
+
+def test_quads_lanes_split_by_row_length():
+    """Neurons of short rows (mean quads per row below "lanes_split") take half the
+    lanes per row: the same windows summed in another order, so FP32 results agree
+    to rounding with equal spikes, and fusion depth and graph replay still change
+    no bit."""
+    trees = [random_tree(n, seed=400 + n) for n in (3000, 900, 120, 30)]
+    clamps = [(0, 0, 0.5, 0.0, 40.0), (1, 0, 0.3, 0.0, 40.0), (2, 0, 0.2, 0.0, 40.0)]
+    out = {}
+    for split, fusion, graph in ((0, 7, 1), (65535, 1, 0), (65535, 7, 1)):
+        m, _, offs, _ = gpu_model(trees, clamps, precision="f32", tolerance=3e-7, conserve="lump", fmt="quads",
+                                  kinetic=True)
+        m._sync()
+        m._ctx.call("nw_set_tuning", 16, 1024, 0)
+        m._ctx.set_option("lanes_split", split)
+        m._ctx.set_option("fusion_depth", fusion)
+        m._ctx.set_option("cuda_graph", graph)
+        for (ti, s, nA, start, dur) in clamps:
+            nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+        m.advance(150)
+        assert m._ctx.get_option("narrow_neurons") == (4 if split else 0)
+        out[(split, fusion)] = (m.get_data("Segment.voltage"), m.get_data("Neuron.spike_count"))
+        m.close()
+    assert np.array_equal(out[(65535, 1)][0], out[(65535, 7)][0])
+    assert np.abs(out[(0, 7)][0] - out[(65535, 7)][0]).max() < 2e-3
+    assert np.array_equal(out[(0, 7)][1], out[(65535, 7)][1])
+
+
+def test_autotune_reports_lanes_split():
+    trees = [random_tree(n, seed=500 + n) for n in (2500, 1500, 300, 60)]
+    m, _, _, _ = gpu_model(trees, [], precision="f32", tolerance=3e-7, conserve="lump", fmt="quads", kinetic=True)
+    m._sync()
+    v0 = m.get_data("Segment.voltage")
+    tuned = m.autotune(3)
+    assert set(tuned) >= {"lanes_per_row", "threads", "fusion_depth", "ms_per_step", "lanes_split", "narrow_neurons"}
+    assert m._ctx.get_option("lanes_split") == tuned["lanes_split"]
+    assert np.array_equal(m.get_data("Segment.voltage"), v0)       # state restored
+    m.close()
