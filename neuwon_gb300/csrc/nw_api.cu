@@ -286,7 +286,8 @@ int nw_ctx_destroy(nw_ctx* ctx) {
                       &ctx->ap_detected, &ctx->ap_state, &ctx->spike_count, &ctx->probe_seg,
                       &ctx->probe_neuron_ptr, &ctx->probe_slot, &ctx->trace, &ctx->neuron_order,
                       &ctx->work_counter, &ctx->status, &ctx->plain_x, &ctx->dclock,
-                      &ctx->clamp_seg_ptr, &ctx->w_rowptr, &ctx->w_col, &ctx->w_val, &ctx->w_leak};
+                      &ctx->clamp_seg_ptr, &ctx->w_rowptr, &ctx->w_col, &ctx->w_val, &ctx->w_leak,
+                      &ctx->wide_x2, &ctx->wide_cs2};
     for (DevBuf* b : bufs) dev_free(*b);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -1216,6 +1217,7 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         ctx->prop_format = (int)value;
         return NW_OK;
     }
+    if (nm == "wide_fusion") { ctx->wide_fusion = value != 0; return NW_OK; }
     if (nm == "lanes_split") {
         // Quad format: neurons whose mean quads per row are below this take half the
         // lanes per row of the kernel's choice (0: all neurons the same).
@@ -1279,7 +1281,9 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "kinetic_mechanisms") { *value = ctx->n_kin; return NW_OK; }
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "quads") { *value = ctx->nq; return NW_OK; }
+    if (nm == "wide_fusion") { ctx->wide_fusion = value != 0; return NW_OK; }
     if (nm == "lanes_split") { *value = ctx->lanes_split; return NW_OK; }
+    if (nm == "wide_fusion") { *value = ctx->wide_fusion ? 1 : 0; return NW_OK; }
     if (nm == "narrow_neurons") {
         int64_t k = 0;
         if (ctx->q_ok && ctx->lanes_split > 0)

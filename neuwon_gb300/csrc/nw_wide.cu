@@ -173,7 +173,137 @@ __global__ void wide_detect_kernel(const StepArgs<real> a, const int s_off) {
         a.trace[(a.clk->probe_len + s_off) * a.n_probes + a.probe_slot[j]] = a.V[a.probe_seg[j]];
 }
 
+// ------------------------------------------------------------ fused half step
+//
+// When every conductance source maps one-to-one onto segments (HH and kinetic
+// instances in segment order, no synapses), a half step is one launch: each warp
+// applies the propagator to 32 consecutive rows (LPR lanes per row, the row
+// format's or the quad format's loop as in wide_rows_kernel / wide_quads_kernel,
+// reading x from x_in), parks the 32 results in shared memory, and then each lane
+// finishes its own segment i: V_i, the calcium row i (one lane per row, reading
+// the scratch cs_in), and, after the first half, the mechanisms at the mid-step
+// voltage (HH, kinetic, calcium, rxd_model.py:115-123), the new conductance and
+// the second half's x_i and calcium scratch; after the second half (when the
+// launch sequence goes on), the next step's first-half x_i and scratch.  The next
+// x goes to x_out (other rows of this launch still read x_in).  Per step: two
+// launches and the detector launch, instead of up to ten.
+template <typename real, int LPR, bool QUAD>
+__global__ void __launch_bounds__(kWideThreads)
+wide_fused_kernel(const StepArgs<real> a, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+                  const real* __restrict__ val, const real* __restrict__ leak, const real* __restrict__ x_in,
+                  real* __restrict__ x_out, const real* __restrict__ cs_in, real* __restrict__ cs_out,
+                  const int s_off, const int phase, const int last, const int next) {
+    __shared__ real vnew_s[kWideThreads];
+    constexpr int GPW = 32 / LPR;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t n = a.neuron_start[a.n_neuron];
+    const int64_t r0 = ((int64_t)blockIdx.x * (kWideThreads / 32) + warp) * 32;
+    if (r0 >= n) return;                                  // the whole warp leaves
+    const int q = lane / LPR, l = lane % LPR;
+    real* vb = vnew_s + warp * 32;
+    for (int g = 0; g < 32; g += GPW) {
+        const int64_t r = r0 + g + q;
+        const bool valid = r < n;
+        real s = real(0), c = real(0), xi = real(0);
+        if (valid) {
+            xi = __ldg(x_in + r);
+            const int64_t beg = rowptr[r], end = rowptr[r + 1];
+            if (QUAD) {
+                for (int64_t k0 = beg + l; k0 < end; k0 += 2 * LPR) {
+                    real v[2][4];
+                    int32_t b[2];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int64_t k = k0 + LPR * u;
+                        if (k < end) {
+                            Vec4Loader<real>::load(val + 4 * k, v[u]);
+                            b[u] = __ldcs(colidx + k);
+                        } else {
+                            v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                            b[u] = 0;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const real* xb = x_in + b[u];
+                        const real p = v[u][0] * (__ldg(xb) - xi) + v[u][1] * (__ldg(xb + 1) - xi);
+                        const real t = v[u][2] * (__ldg(xb + 2) - xi) + v[u][3] * (__ldg(xb + 3) - xi);
+                        kahan_add(s, c, p + t);
+                    }
+                }
+            } else {
+                for (int64_t k = beg + 4 * l; k < end; k += 4 * LPR) {
+                    real v[4];
+                    Vec4Loader<real>::load(val + k, v);
+                    const int4 cc = __ldcs(reinterpret_cast<const int4*>(colidx + k));
+                    const real p = v[0] * (__ldg(x_in + cc.x) - xi) + v[1] * (__ldg(x_in + cc.y) - xi);
+                    const real t = v[2] * (__ldg(x_in + cc.z) - xi) + v[3] * (__ldg(x_in + cc.w) - xi);
+                    kahan_add(s, c, p + t);
+                }
+            }
+        }
+        real t = s - c;
+#pragma unroll
+        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off, LPR);
+        if (l == 0) vb[g + q] = valid ? (xi - leak[r] * xi) + t : real(0);
+    }
+    __syncwarp();
+    const int64_t i = r0 + lane;
+    if (i >= n) return;
+    const real v = vb[lane];
+    if (!isfinite(v)) atomicOr(a.status, kStatusNonFinite);
+    a.V[i] = v;
+    real cnew = real(0);
+    if (a.ca_on) {
+        const real si = __ldg(cs_in + i);
+        real s = real(0), c = real(0);
+        for (int64_t k = a.ca_wrow[i]; k < a.ca_wrow[i + 1]; k += 4) {
+            real w[4];
+            Vec4Loader<real>::load(a.ca_wval + k, w);
+            const int4 cc = __ldcs(reinterpret_cast<const int4*>(a.ca_wcol + k));
+            const real p = w[0] * (__ldg(cs_in + cc.x) - si) + w[1] * (__ldg(cs_in + cc.y) - si);
+            const real t = w[2] * (__ldg(cs_in + cc.z) - si) + w[3] * (__ldg(cs_in + cc.w) - si);
+            kahan_add(s, c, p + t);
+        }
+        cnew = (si - a.ca_wleak[i] * si) + (s - c);
+        if (!isfinite(cnew)) atomicOr(a.status, kStatusNonFinite);
+        a.ca_c[i] = cnew;
+    }
+    if (phase == 0) {
+        if (a.hh_on) {
+            real m = a.gm[i], h = a.gh[i], nn = a.gn[i];
+            hh_gates(v, a.dtq10, m, h, nn);
+            a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
+        }
+        for (int qq = 0; qq < a.n_kin; ++qq) kinetic_step(a.kin[qq], i, v);
+        if (a.ca_on) calcium_mechanisms(a, i);
+    }
+    if (phase == 0 || next) {
+        // The next half step's x_i: after the first half, the second half of this
+        // step; after the second, the first half of the next step.
+        const int64_t tick = a.clk->input_ticks + 2 * (int64_t)s_off + (phase == 0 ? 2 : 3);
+        real I = a.has_nonspec ? a.Inonspec[i] : real(0);
+        if (a.clamp_seg_ptr) {
+            for (uint32_t cc = a.clamp_seg_ptr[i]; cc < a.clamp_seg_ptr[i + 1]; ++cc)
+                if (tick >= a.clamp_first[cc] && tick < a.clamp_first[cc] + a.clamp_count[cc]) I += a.clamp_amp[cc];
+        }
+        real G, GE;
+        segment_conductance(a, i, G, GE);
+        x_out[i] = membrane_x_of(a, i, v, a.kG[i], a.kI[i], G, GE, I, phase == 0 && last != 0);
+        if (a.ca_on) cs_out[i] = fmax(real(0), cnew + a.ca_dcdt[i] * a.h_ms);
+    }
+}
+
 // ------------------------------------------------------------ host side
+
+// The fused half step applies: every conductance source maps one-to-one onto
+// segments (HH and kinetic instances in segment order) and there are no synapses.
+static bool wide_fusable(const nw_ctx* ctx) {
+    if (!ctx->wide_fusion || ctx->syn.n != 0 || (ctx->hh.m != 0 && !ctx->hh.identity)) return false;
+    for (int q = 0; q < ctx->n_kin; ++q)
+        if (!ctx->kin[q].identity) return false;
+    return true;
+}
 
 static int wide_lanes(nw_ctx* ctx) {
     if (ctx->lanes_per_row) return ctx->lanes_per_row;
@@ -218,9 +348,61 @@ static int launch_quads(nw_ctx* ctx, const StepArgs<real>& a) {
     return NW_OK;
 }
 
+template <typename real, int LPR>
+static void launch_fused_lpr(nw_ctx* ctx, const StepArgs<real>& a, bool quad, const real* x_in, real* x_out,
+                             const real* cs_in, real* cs_out, int s, int phase, int last, int next) {
+    const unsigned blocks = (unsigned)((ctx->n_seg + kWideThreads - 1) / kWideThreads);
+    if (quad)
+        wide_fused_kernel<real, LPR, true><<<blocks, kWideThreads, 0, ctx->stream>>>(
+            a, ctx->wq_rowptr.as<int64_t>(), ctx->wq_base.as<int32_t>(), ctx->wq_val.as<real>(),
+            ctx->w_leak.as<real>(), x_in, x_out, cs_in, cs_out, s, phase, last, next);
+    else
+        wide_fused_kernel<real, LPR, false><<<blocks, kWideThreads, 0, ctx->stream>>>(
+            a, a.wrow, a.wcol, a.wval, a.wleak, x_in, x_out, cs_in, cs_out, s, phase, last, next);
+}
+
+// The fused sequence: the first half's x (and calcium scratch) of the first step
+// by the phase kernels, then per step the two fused half steps (x and scratch
+// alternating between two buffers) and the detector launch.
+template <typename real>
+static int enqueue_wide_fused(nw_ctx* ctx, const StepArgs<real>& a, int steps) {
+    const int64_t n = ctx->n_seg;
+    const unsigned seg_blocks = (unsigned)((n + kWideThreads - 1) / kWideThreads);
+    const int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
+    const bool quad = ctx->prop_format == 2 && ctx->wq_ok;
+    const double avg = n ? (double)(quad ? ctx->nwq : ctx->nnz_w / 4) / (double)n : 0.0;
+    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg >= 24 ? 16 : 8);
+    real* x0 = a.px;
+    real* x1 = ctx->wide_x2.as<real>();
+    real* c0 = a.ca_scratch;
+    real* c1 = ctx->wide_cs2.as<real>();
+    wide_membrane_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a, 0, 0, 0);
+    NW_CUDA(ctx, cudaGetLastError());
+    if (a.ca_on) {
+        wide_calcium_prepare_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
+        NW_CUDA(ctx, cudaGetLastError());
+    }
+    for (int s = 0; s < steps; ++s) {
+        const int last = s == steps - 1 ? 1 : 0;
+        for (int phase = 0; phase < 2; ++phase) {
+            const real* xi = phase == 0 ? x0 : x1;
+            real* xo = phase == 0 ? x1 : x0;
+            const real* ci = phase == 0 ? c0 : c1;
+            real* co = phase == 0 ? c1 : c0;
+            if (lanes >= 16) launch_fused_lpr<real, 16>(ctx, a, quad, xi, xo, ci, co, s, phase, last, !last);
+            else launch_fused_lpr<real, 8>(ctx, a, quad, xi, xo, ci, co, s, phase, last, !last);
+            NW_CUDA(ctx, cudaGetLastError());
+        }
+        wide_detect_kernel<real><<<(unsigned)((cover + 127) / 128), 128, 0, ctx->stream>>>(a, s);
+        NW_CUDA(ctx, cudaGetLastError());
+    }
+    return NW_OK;
+}
+
 // The launches of `steps` steps (no host synchronisation: also a graph body).
 template <typename real>
 static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lanes) {
+    if (wide_fusable(ctx)) return enqueue_wide_fused<real>(ctx, a, steps);
     const int64_t n = ctx->n_seg;
     const unsigned seg_blocks = (unsigned)((n + kWideThreads - 1) / kWideThreads);
     const int64_t n_hh = ctx->hh.m, n_kin = kinetic_instances(ctx), n_syn = ctx->syn.n;
@@ -297,6 +479,10 @@ static int wide_graph(nw_ctx* ctx, const StepArgs<real>& a0, int steps, int lane
     key_bytes(key, &ctx->wq_base.ptr, sizeof(void*));
     key_bytes(key, &ctx->wq_val.ptr, sizeof(void*));
     key_bytes(key, &ctx->nwq, sizeof(ctx->nwq));
+    const int fused = wide_fusable(ctx) ? 1 : 0;
+    key_bytes(key, &fused, sizeof(fused));
+    key_bytes(key, &ctx->wide_x2.ptr, sizeof(void*));
+    key_bytes(key, &ctx->wide_cs2.ptr, sizeof(void*));
     for (auto& g : ctx->graphs) {
         if (g.key == key) {
             g.last_use = ++ctx->graph_uses;
@@ -341,6 +527,11 @@ static int wide_steps(nw_ctx* ctx, int k_steps) {
     NW_CHECK(ensure_wide(ctx));
     if (ctx->prop_format == 2 && ctx->n_seg >= 4) NW_CHECK(ensure_wide_quads(ctx));
     if (ctx->ca.on) NW_CHECK(calcium_ensure_wide(ctx));
+    if (wide_fusable(ctx)) {
+        NW_CHECK(dev_alloc(ctx, ctx->wide_x2, (size_t)ctx->precision * std::max<int64_t>(ctx->n_seg, 1)));
+        if (ctx->ca.on)
+            NW_CHECK(dev_alloc(ctx, ctx->wide_cs2, (size_t)ctx->precision * std::max<int64_t>(ctx->n_seg, 1)));
+    }
     const int lanes = wide_lanes(ctx);
     // Every phase is its own launch, so a spike written by one step's detector
     // launch is visible to every later mechanism launch: no cap by the delays.

@@ -89,3 +89,42 @@ def test_wide_quads_equal_wide_rows(precision):
     tol = 1e-9 if precision == "f64" else 2e-3
     assert np.abs(out[0][0] - out[1][0]).max() < tol
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_wide_fused_half_steps_equal_phase_launches(precision):
+    """One launch per half step (propagator rows, then each segment's mechanisms
+    and next x in the same launch) against one launch per phase: HH + na8 and HH +
+    calcium models agree to rounding (the calcium rows are summed in another
+    order), spikes and probes included."""
+    from tests.helpers import calcium_case
+    trees = [random_tree(n, seed=60 + n) for n in (900, 2500, 40)]
+    clamps = [(0, 0, 0.4, 0.0, 1e6), (1, 0, 0.6, 1.0, 40.0), (2, 3, 0.1, 2.0, 5.0)]
+    tol = 1e-9 if precision == "f64" else 2e-3
+    for case in ("kinetic", "calcium"):
+        out = []
+        for fusion in (0, 1):
+            if case == "kinetic":
+                m, _, offs, recs = gpu_model(trees, clamps, precision=precision, path="wide", kinetic=True,
+                                             probes=[0, 950])
+            else:
+                m, _, offs = calcium_case(trees, clamps, precision=precision, path="wide", oracle=False)
+                recs = []
+            m._sync()
+            m._ctx.set_option("wide_fusion", fusion)
+            if case == "kinetic":
+                run_with_clamps(m, clamps, offs, 250)
+            else:
+                m.advance(250)
+            res = [m.get_data("Segment.voltage"), m.get_data("Neuron.spike_count")]
+            res.append(m.get_data("na8.state") if case == "kinetic" else m.get_data("Species.ca"))
+            res += [np.asarray(r.get_data()) for r in recs]
+            out.append(res)
+            m.close()
+        assert np.array_equal(out[0][1], out[1][1]) and out[0][1].sum() > 0
+        assert np.abs(out[0][0] - out[1][0]).max() < tol                       # voltages (mV)
+        a, b = np.asarray(out[0][2], float), np.asarray(out[1][2], float)
+        scale = np.abs(a).max() if case == "calcium" else 1.0                  # calcium: relative
+        assert np.abs(a - b).max() < tol * scale, (case, np.abs(a - b).max())
+        for a, b in zip(out[0][3:], out[1][3:]):                               # probe traces
+            assert np.abs(np.asarray(a, float) - np.asarray(b, float)).max() < tol
