@@ -167,6 +167,25 @@ int nw_kinetic_add(nw_ctx* ctx, int64_t num_instances, const int64_t* segment, c
 /* Removes every kinetic mechanism (before registering a new set). */
 int nw_kinetic_clear(nw_ctx* ctx);
 
+/* Replaces the voltage input of kinetic mechanism `mechanism` by two inputs: lti_sim's
+ * two-input tables (Approx2D, neuwon/rxd/lti_sim/approx.py:242-337, indexed as the
+ * generated kernel indexes them, codegen.py:43-70; the reference's NMODL front end
+ * makes them for KINETIC blocks that read the voltage and a POINTER, e.g.
+ * nmodl_library/kinetic/NMDA.mod with its glutamate concentration C, and sorts the
+ * inputs by name, lti_model.py:8).  The table given to nw_kinetic_add is then
+ * [b1][b2][col][row][term] with num_buckets = num_buckets1 * num_buckets2 and
+ * num_terms terms, term t = loc1^powers[2t] * loc2^powers[2t+1] (loc_d the location
+ * of input d within its bucket).  Input kinds: 0 = the segment voltage,
+ * LinearInput: bucket value (v - minimum) * bucket_frq; 1 = the instance value
+ * "kinetic.<q>.input", LogarithmicInput: (log2(x + scale) - log2(minimum + scale)) *
+ * bucket_frq; 2 = the instance value, linear.  Instance values start at
+ * input_initial (real, per instance, read and written through nw_get_data /
+ * nw_set_data). */
+int nw_kinetic_inputs(nw_ctx* ctx, int32_t mechanism, int32_t kind1, int32_t num_buckets1, double minimum1,
+                      double bucket_frq1, double scale1, int32_t kind2, int32_t num_buckets2, double minimum2,
+                      double bucket_frq2, double scale2, int32_t num_terms, const int32_t* powers,
+                      double input_initial);
+
 /* nw_kinetic_clear followed by nw_kinetic_add of one nonspecific mechanism (index 0). */
 int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
                         const double* g_coef, int num_states, int num_open, const int32_t* open_states,

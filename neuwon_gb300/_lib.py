@@ -27,7 +27,7 @@ EXPORTS = [
     "nw_kinetic_register", "nw_set_option", "nw_get_option", "nw_electric_half_step_noalloc",
     "nw_adjoint_forward", "nw_adjoint_backward", "nw_autotune", "nw_synapses_set",
     "nw_calcium_set", "nw_calcium_pump_set", "nw_calcium_data", "nw_lti_table_build", "nw_lti_expm",
-    "nw_species_set", "nw_species_conductance", "nw_kinetic_add", "nw_kinetic_clear",
+    "nw_species_set", "nw_species_conductance", "nw_kinetic_add", "nw_kinetic_clear", "nw_kinetic_inputs",
 ]
 
 _lib = None
@@ -70,6 +70,9 @@ def load(build_if_missing=True):
         "nw_kinetic_add": ([c_void_p, c_i64, c_void_p, c_void_p, c_int, c_int, c_void_p, c_double, ctypes.c_int32,
                             c_void_p, c_int, c_int, c_double, c_double, c_double, c_void_p, P(ctypes.c_int32)], c_int),
         "nw_kinetic_clear": ([c_void_p], c_int),
+        "nw_kinetic_inputs": ([c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, c_double, c_double, c_double,
+                               ctypes.c_int32, ctypes.c_int32, c_double, c_double, c_double, ctypes.c_int32, c_void_p,
+                               c_double], c_int),
         "nw_species_set": ([c_void_p, ctypes.c_int32, c_void_p], c_int),
         "nw_species_conductance": ([c_void_p, ctypes.c_int32, c_void_p], c_int),
         "nw_clamps_set": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p], c_int),

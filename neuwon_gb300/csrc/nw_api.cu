@@ -174,7 +174,7 @@ static void free_adj(AdjointState& a) {
 }
 
 static void free_kin(KineticState& k) {
-    for (DevBuf* b : {&k.seg, &k.state, &k.gcoef, &k.table, &k.seg_ptr, &k.neuron_ptr}) dev_free(*b);
+    for (DevBuf* b : {&k.seg, &k.state, &k.gcoef, &k.table, &k.seg_ptr, &k.neuron_ptr, &k.input}) dev_free(*b);
     k = KineticState();
 }
 
@@ -183,11 +183,12 @@ static void free_kinetics(nw_ctx* ctx) {
     ctx->n_kin = 0;
 }
 
-// "kinetic.state" names mechanism 0; "kinetic.<q>.state" mechanism q.  Returns
-// the index, -1 when the name is not a kinetic state name, -2 when q is out of range.
-static int kinetic_state_name(const nw_ctx* ctx, const std::string& nm) {
-    if (nm == "kinetic.state") return ctx->n_kin > 0 ? 0 : -2;
-    const std::string pre = "kinetic.", post = ".state";
+// "kinetic.state" names mechanism 0; "kinetic.<q>.<post>" mechanism q's array `post`
+// ("state", or "input": the instance values of a two-input table).  Returns the
+// index, -1 when the name is not of that form, -2 when q is out of range.
+static int kinetic_array_name(const nw_ctx* ctx, const std::string& nm, const std::string& post) {
+    if (post == ".state" && nm == "kinetic.state") return ctx->n_kin > 0 ? 0 : -2;
+    const std::string pre = "kinetic.";
     if (nm.size() <= pre.size() + post.size() || nm.compare(0, pre.size(), pre) != 0 ||
         nm.compare(nm.size() - post.size(), post.size(), post) != 0)
         return -1;
@@ -195,6 +196,10 @@ static int kinetic_state_name(const nw_ctx* ctx, const std::string& nm) {
     if (mid.empty() || mid.size() > 3 || mid.find_first_not_of("0123456789") != std::string::npos) return -1;
     const int q = std::stoi(mid);
     return q < ctx->n_kin ? q : -2;
+}
+
+static int kinetic_state_name(const nw_ctx* ctx, const std::string& nm) {
+    return kinetic_array_name(ctx, nm, ".state");
 }
 
 void free_syn(SynState& y) {
@@ -454,6 +459,14 @@ int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int6
                     nm == "hh.gna_coef" ? hh.cna : nm == "hh.gk_coef" ? hh.ck : hh.cl;
         return upload_convert(ctx, b.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
     }
+    if (const int q = kinetic_array_name(ctx, nm, ".input"); q != -1) {
+        if (q < 0 || ctx->kin[q].ninp != 2) return fail(ctx, NW_ERR_ARG, nm + ": no two-input kinetic mechanism");
+        const KineticState& K = ctx->kin[q];
+        NW_CHECK(need(K.m));
+        std::vector<double> sorted(count);
+        for (int64_t i = 0; i < count; ++i) sorted[K.user_to_sorted[i]] = read_as_double(host, dtype, i);
+        return upload_convert(ctx, K.input.ptr, rd, sorted.data(), NW_DTYPE_F64, count);
+    }
     if (const int q = kinetic_state_name(ctx, nm); q != -1) {
         if (q < 0) return fail(ctx, NW_ERR_ARG, nm + ": no such kinetic mechanism");
         const KineticState& K = ctx->kin[q];
@@ -526,6 +539,15 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
         std::vector<double> sorted(count);
         NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, b.ptr, rd, count));
         for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[ctx->hh.user_to_sorted[i]]);
+        return NW_OK;
+    }
+    if (const int q = kinetic_array_name(ctx, nm, ".input"); q != -1) {
+        if (q < 0 || ctx->kin[q].ninp != 2) return fail(ctx, NW_ERR_ARG, nm + ": no two-input kinetic mechanism");
+        const KineticState& K = ctx->kin[q];
+        NW_CHECK(need(K.m));
+        std::vector<double> sorted(count);
+        NW_CHECK(download_convert(ctx, sorted.data(), NW_DTYPE_F64, K.input.ptr, rd, count));
+        for (int64_t i = 0; i < count; ++i) write_from_double(host, dtype, i, sorted[K.user_to_sorted[i]]);
         return NW_OK;
     }
     if (const int q = kinetic_state_name(ctx, nm); q != -1) {
@@ -775,10 +797,10 @@ static int kinetic_add(nw_ctx* ctx, const char* who, int64_t num_instances, cons
     const std::string w(who);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, w + " before nw_model_init");
     const int S = num_states, T = num_terms;
-    if (S < 1 || S > 16 || T < 1 || T > 4 || num_buckets < 1 || num_open < 1 || num_open > kMaxOpen ||
+    if (S < 1 || S > 16 || T < 1 || T > kMaxTerms || num_buckets < 1 || num_open < 1 || num_open > kMaxOpen ||
         !open_states || !table || !init_state || !(bucket_frq > 0))
-        return fail(ctx, NW_ERR_ARG, w + ": need 1<=S<=16, 1<=terms<=4, 1.." + std::to_string(kMaxOpen) +
-                                     " open states, a table and an initial state");
+        return fail(ctx, NW_ERR_ARG, w + ": need 1<=S<=16, 1<=terms<=" + std::to_string(kMaxTerms) + ", 1.." +
+                                     std::to_string(kMaxOpen) + " open states, a table and an initial state");
     for (int k = 0; k < num_open; ++k)
         if (open_states[k] < 0 || open_states[k] >= S)
             return fail(ctx, NW_ERR_ARG, w + ": open state index out of range");
@@ -865,6 +887,50 @@ int nw_kinetic_add(nw_ctx* ctx, int64_t num_instances, const int64_t* segment, c
     return kinetic_add(ctx, "nw_kinetic_add", num_instances, segment, g_coef, num_states, num_open, open_states,
                        erev, species, table, num_buckets, num_terms, vmin, bucket_frq, conserve_sum, init_state,
                        mechanism_out);
+}
+
+int nw_kinetic_inputs(nw_ctx* ctx, int32_t mechanism, int32_t kind1, int32_t num_buckets1, double minimum1,
+                      double bucket_frq1, double scale1, int32_t kind2, int32_t num_buckets2, double minimum2,
+                      double bucket_frq2, double scale2, int32_t num_terms, const int32_t* powers,
+                      double input_initial) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (mechanism < 0 || mechanism >= ctx->n_kin)
+        return fail(ctx, NW_ERR_ARG, "nw_kinetic_inputs: no such kinetic mechanism");
+    KineticState& K = ctx->kin[mechanism];
+    const int32_t kinds[2] = {kind1, kind2}, nbs[2] = {num_buckets1, num_buckets2};
+    const double mins[2] = {minimum1, minimum2}, frqs[2] = {bucket_frq1, bucket_frq2}, scs[2] = {scale1, scale2};
+    for (int d = 0; d < 2; ++d) {
+        if (kinds[d] < 0 || kinds[d] > 2 || nbs[d] < 1 || !(frqs[d] > 0) || !std::isfinite(mins[d]))
+            return fail(ctx, NW_ERR_ARG, "nw_kinetic_inputs: kinds 0..2, buckets >= 1, bucket_frq > 0");
+        if (kinds[d] == 1 && !(mins[d] + scs[d] > 0))
+            return fail(ctx, NW_ERR_ARG, "nw_kinetic_inputs: a logarithmic input needs minimum + scale > 0");
+    }
+    if ((int64_t)num_buckets1 * num_buckets2 != K.nb || num_terms != K.T || !powers)
+        return fail(ctx, NW_ERR_ARG, "nw_kinetic_inputs: buckets1 * buckets2 and terms must match the table (" +
+                                     std::to_string(K.nb) + " buckets, " + std::to_string(K.T) + " terms)");
+    for (int t = 0; t < num_terms; ++t)
+        if (powers[2 * t] < 0 || powers[2 * t] > 9 || powers[2 * t + 1] < 0 || powers[2 * t + 1] > 9)
+            return fail(ctx, NW_ERR_ARG, "nw_kinetic_inputs: powers in 0..9");
+    if (!std::isfinite(input_initial)) return fail(ctx, NW_ERR_ARG, "nw_kinetic_inputs: finite input_initial");
+    cudaStreamSynchronize(ctx->stream);
+    for (int d = 0; d < 2; ++d) {
+        K.kind[d] = kinds[d];
+        K.nbi[d] = nbs[d];
+        K.offi[d] = kinds[d] == 1 ? std::log2(mins[d] + scs[d]) : mins[d];
+        K.frqi[d] = frqs[d];
+        K.sci[d] = scs[d];
+    }
+    for (int t = 0; t < kMaxTerms; ++t) {
+        K.pw[t][0] = t < num_terms ? (signed char)powers[2 * t] : 0;
+        K.pw[t][1] = t < num_terms ? (signed char)powers[2 * t + 1] : 0;
+    }
+    NW_CHECK(dev_alloc(ctx, K.input, (size_t)ctx->precision * std::max<int64_t>(K.m, 1)));
+    std::vector<double> init(std::max<int64_t>(K.m, 1), input_initial);
+    NW_CHECK(upload_convert(ctx, K.input.ptr, real_dtype(ctx), init.data(), NW_DTYPE_F64, K.m));
+    K.ninp = 2;
+    graphs_clear(ctx);
+    return NW_OK;
 }
 
 int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,

@@ -68,6 +68,7 @@ struct HHState {
 // and most open states per scheme a model may have.
 constexpr int kMaxKinetic = 8;
 constexpr int kMaxOpen = 8;
+constexpr int kMaxTerms = 10;      // polynomial terms of a kinetic table
 
 struct KineticState {
     int64_t m = 0;
@@ -76,6 +77,15 @@ struct KineticState {
     bool identity = false;
     int species = -1;           // electric species its conductance feeds (-1: nonspecific, own erev)
     double erev = 0, vmin = 0, frq = 0, conserve = 0;
+    // Two-input tables (nw_kinetic_inputs): per input its kind (0 voltage, linear;
+    // 1 instance value, logarithmic; 2 instance value, linear), buckets, offset
+    // (minimum, or log2(minimum + scale)), buckets per unit and log scale; the
+    // terms' powers; the instance values.
+    int ninp = 1;
+    int kind[2] = {0, 0}, nbi[2] = {0, 0};
+    double offi[2] = {0, 0}, frqi[2] = {0, 0}, sci[2] = {0, 0};
+    signed char pw[kMaxTerms][2] = {};
+    DevBuf input;               // real [m] (sorted order)
     DevBuf seg;                 // u32 [m] segment-sorted
     DevBuf state;               // real [S][m]
     DevBuf gcoef;               // real [m]

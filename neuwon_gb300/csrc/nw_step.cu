@@ -77,7 +77,9 @@ __global__ void plain_kinetic_kernel(const StepArgs<real> a, int q, int64_t kb, 
     int64_t k = kb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= ke) return;
     const KinArgs<real>& K = a.kin[q];
-    kinetic_step_generic(K, k, a.V[K.identity ? k : (int64_t)K.seg[k]]);
+    const real v = a.V[K.identity ? k : (int64_t)K.seg[k]];
+    if (K.ninp == 2) kinetic_step_2d(K, k, v);
+    else kinetic_step_generic(K, k, v);
 }
 
 template <typename real>

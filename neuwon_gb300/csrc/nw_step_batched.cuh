@@ -487,7 +487,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     const bool last1 = s == a.k_steps - 1;
                     const bool keep = s + 1 < a.k_steps;
                     const bool kin_on = a.n_kin > 0;
-                    if (a.n_kin == 0 || (a.n_kin == 1 && a.kin[0].S == 8 && a.kin[0].T == 2)) {
+                    if (a.n_kin == 0 || (a.n_kin == 1 && a.kin[0].S == 8 && a.kin[0].T == 2 && a.kin[0].ninp == 1)) {
                         // Every input of the segment is loaded before the first store, and
                         // the conductances come from registers (same helpers and order as
                         // segment_conductance, so the same bits).

@@ -83,6 +83,14 @@ struct KinArgs {
     const uint32_t* seg_ptr; const int64_t* neuron_ptr; const uint32_t* seg;
     real* state; const real* gcoef; const real* table;
     real vmin, frq, cs, erev;
+    // two-input tables (ninp 2): per input kind (0 voltage, 1 instance value on a
+    // log2 scale, 2 instance value), buckets, offset, buckets per unit, log scale;
+    // term powers; instance values
+    int ninp;
+    int kind[2], nbi[2];
+    real offi[2], frqi[2], sci[2];
+    signed char pw[kMaxTerms][2];
+    const real* input;
 };
 
 template <typename real>
@@ -417,7 +425,9 @@ __device__ __noinline__ void kinetic_step_generic(const KinArgs<real>& K, int64_
     const int S = K.S, T = K.T;
     real loc;
     const int b = kinetic_locate(K, v, loc);
-    real basis[4] = {real(1), loc, loc * loc, loc * loc * loc};
+    real basis[kMaxTerms];
+    basis[0] = real(1);
+    for (int t = 1; t < T; ++t) basis[t] = basis[t - 1] * loc;
     const real* tb = K.table + (int64_t)b * (S * S * T);
     real st[16], out[16];
     for (int c = 0; c < S; ++c) { st[c] = K.state[(int64_t)c * K.m + k]; out[c] = real(0); }
@@ -437,11 +447,66 @@ __device__ __noinline__ void kinetic_step_generic(const KinArgs<real>& K, int64_
     for (int c = 0; c < S; ++c) K.state[(int64_t)c * K.m + k] = out[c];
 }
 
+// One input of a two-input table -> (bucket, location), as the generated lti_sim
+// kernel locates it (codegen.py:43-59): LinearInput (value - minimum) * frq,
+// LogarithmicInput (log2(value + scale) - log2(minimum + scale)) * frq; clamped
+// to the table like the voltage (location 1 above it, 0 below it).
+template <typename real>
+__device__ __forceinline__ int kinetic_locate_input(const KinArgs<real>& K, int d, real value, real& loc) {
+    real x = K.kind[d] == 1 ? (d_log2(value + K.sci[d]) - K.offi[d]) * K.frqi[d] : (value - K.offi[d]) * K.frqi[d];
+    const int nb = K.nbi[d];
+    if (!(x > real(-2))) x = real(-2);
+    if (x > real(nb + 1)) x = real(nb + 1);
+    int b = (int)x;
+    if (b > nb - 1) { b = nb - 1; loc = real(1); }
+    else if (b < 0) { b = 0; loc = real(0); }
+    else loc = x - real(b);
+    return b;
+}
+
+// One step of an instance of a two-input table (lti_sim's Approx2D,
+// neuwon/rxd/lti_sim/approx.py:242-337, run as codegen.py:60-106 runs it): table
+// [b1][b2][col][row][term], term t = loc1^pw[t][0] * loc2^pw[t][1] (products taken
+// factor by factor, as the generated code writes them).
+template <typename real>
+__device__ __noinline__ void kinetic_step_2d(const KinArgs<real>& K, int64_t k, real v) {
+    const int S = K.S, T = K.T;
+    const real u = K.input[k];
+    real loc[2];
+    int b[2];
+    for (int d = 0; d < 2; ++d) b[d] = kinetic_locate_input(K, d, K.kind[d] == 0 ? v : u, loc[d]);
+    real basis[kMaxTerms];
+    for (int t = 0; t < T; ++t) {
+        real x = real(1);
+        for (int p = 0; p < K.pw[t][0]; ++p) x = p == 0 ? loc[0] : x * loc[0];
+        for (int p = 0; p < K.pw[t][1]; ++p) x = (p == 0 && K.pw[t][0] == 0) ? loc[1] : x * loc[1];
+        basis[t] = x;
+    }
+    const real* tb = K.table + ((int64_t)b[0] * K.nbi[1] + b[1]) * (S * S * T);
+    real st[16], out[16];
+    for (int c = 0; c < S; ++c) { st[c] = K.state[(int64_t)c * K.m + k]; out[c] = real(0); }
+    for (int col = 0; col < S; ++col)
+        for (int row = 0; row < S; ++row) {
+            const real* p = tb + (col * S + row) * T;
+            real poly = real(0);
+            for (int t = 0; t < T; ++t) poly += (K.pw[t][0] == 0 && K.pw[t][1] == 0) ? p[t] : basis[t] * p[t];
+            out[row] += poly * st[col];
+        }
+    if (K.cs > real(0)) {
+        real sum = out[0];
+        for (int c = 1; c < S; ++c) sum += out[c];
+        const real f = K.cs / sum;
+        for (int c = 0; c < S; ++c) out[c] *= f;
+    }
+    for (int c = 0; c < S; ++c) K.state[(int64_t)c * K.m + k] = out[c];
+}
+
 // Unrolled instances for the shapes of the schemes this package defines
 // (8-state sodium, 6-state Nav1.1 / Kv1.1 with linear tables); others generic.
 template <typename real>
 __device__ __forceinline__ void kinetic_step(const KinArgs<real>& K, int64_t k, real v) {
-    if (K.S == 8 && K.T == 2) kinetic_step_fixed<real, 8, 2>(K, k, v);
+    if (K.ninp == 2) kinetic_step_2d(K, k, v);
+    else if (K.S == 8 && K.T == 2) kinetic_step_fixed<real, 8, 2>(K, k, v);
     else if (K.S == 6 && K.T == 2) kinetic_step_fixed<real, 6, 2>(K, k, v);
     else kinetic_step_generic(K, k, v);
 }
@@ -763,6 +828,13 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
         k.seg = K.seg.as<uint32_t>();
         k.state = K.state.as<real>(); k.gcoef = K.gcoef.as<real>(); k.table = K.table.as<real>();
         k.vmin = (real)K.vmin; k.frq = (real)K.frq; k.cs = (real)K.conserve; k.erev = (real)K.erev;
+        k.ninp = K.ninp;
+        for (int d = 0; d < 2; ++d) {
+            k.kind[d] = K.kind[d]; k.nbi[d] = K.nbi[d];
+            k.offi[d] = (real)K.offi[d]; k.frqi[d] = (real)K.frqi[d]; k.sci[d] = (real)K.sci[d];
+        }
+        for (int t = 0; t < kMaxTerms; ++t) { k.pw[t][0] = K.pw[t][0]; k.pw[t][1] = K.pw[t][1]; }
+        k.input = K.ninp == 2 ? K.input.as<real>() : nullptr;
     }
     const CalciumState& Ca = ctx->ca;
     a.ca_on = Ca.on ? 1 : 0;

@@ -179,6 +179,224 @@ def kv11():
     return KineticScheme("Kv11_6States_temperature2", states, transitions, open_states=["OS"], conserve_sum=1.0)
 
 
+class TableInput:
+    """One input of a kinetic table, located as lti_sim's inputs locate theirs
+    (neuwon/rxd/lti_sim/inputs.py): the segment voltage ("voltage", LinearInput),
+    an instance value on a log2 scale ("log", LogarithmicInput: minimum 0, bucket
+    value (log2(x + scale) - log2(minimum + scale)) * frq) or on a linear one
+    ("linear")."""
+
+    KINDS = {"voltage": 0, "log": 1, "linear": 2}
+
+    def __init__(self, name, kind, minimum, maximum, num_buckets, scale=1.0, initial=None):
+        if kind not in self.KINDS:
+            raise ValueError(f"input kind {kind!r}: one of {sorted(self.KINDS)}")
+        self.name, self.kind = str(name), kind
+        self.code = self.KINDS[kind]
+        self.minimum, self.maximum = float(minimum), float(maximum)
+        self.num_buckets = int(num_buckets)
+        self.scale = float(scale)
+        self.initial = self.minimum if initial is None else float(initial)
+        if kind == "log":
+            self.offset = math.log2(self.minimum + self.scale)                        # inputs.py:90-96
+            span = math.log2(self.maximum + self.scale) - self.offset
+        else:
+            self.offset = self.minimum                                                # inputs.py:74-77
+            span = self.maximum - self.minimum
+        self.bucket_frq = self.num_buckets / span
+        self.bucket_width = span / self.num_buckets
+
+    def position(self, x):
+        x = np.asarray(x, dtype=np.float64)
+        if self.kind == "log":
+            return (np.log2(x + self.scale) - self.offset) * self.bucket_frq
+        return (x - self.offset) * self.bucket_frq
+
+    def value(self, pos):
+        y = self.offset + np.asarray(pos, dtype=np.float64) * self.bucket_width
+        return 2.0 ** y - self.scale if self.kind == "log" else y
+
+    def locate(self, x):
+        """(bucket, location) clamped to the table (codegen.py:43-59)."""
+        pos = self.position(x)
+        b = np.trunc(pos).astype(np.int64)
+        hi, lo = b > self.num_buckets - 1, b < 0
+        loc = np.where(hi, 1.0, np.where(lo, 0.0, pos - b))
+        return np.where(hi, self.num_buckets - 1, np.where(lo, 0, b)), loc
+
+
+def canonical_terms(terms):
+    """Polynomial terms in lti_sim's canonical order (polynomial.py:19-20): by total
+    degree, then by the reversed powers."""
+    return sorted({tuple(int(p) for p in t) for t in terms}, key=lambda t: (sum(t), tuple(reversed(t))))
+
+
+class KineticScheme2(KineticScheme):
+    """A linear kinetic scheme dS/dt = A(x1, x2) S over two table inputs, in table
+    order (lti_sim sorts a model's inputs by name, lti_model.py:8)."""
+
+    def __init__(self, name, states, transitions, open_states, input_names, conserve_sum=1.0):
+        """transitions(x1, x2, celsius) -> list of (src, dst, rate) with numpy rates."""
+        super().__init__(name, states, transitions, open_states, conserve_sum)
+        self.input_names = tuple(input_names)
+
+    def matrix(self, x1, x2, celsius):
+        x1 = np.atleast_1d(np.asarray(x1, dtype=np.float64))
+        x2 = np.broadcast_to(np.asarray(x2, dtype=np.float64), x1.shape)
+        S = self.num_states
+        A = np.zeros((len(x1), S, S))
+        for src, dst, rate in self.transitions(x1, x2, celsius):
+            A[:, dst, src] += rate
+            A[:, src, src] -= rate
+        return A
+
+    def exact_propagator(self, x1, x2, dt, celsius):
+        M = scipy.linalg.expm(self.matrix(x1, x2, celsius) * dt)
+        M /= M.sum(axis=1, keepdims=True)
+        return M
+
+    def steady_state(self, x1, x2, celsius):
+        M = scipy.linalg.expm(self.matrix([x1], [x2], celsius)[0] * 3600e3)
+        M = M / M.sum(axis=0, keepdims=True)
+        return M @ np.full(self.num_states, (self.conserve_sum or 1.0) / self.num_states)
+
+
+def nmda():
+    """Ten-state NMDA receptor with magnesium block of nmodl_library/kinetic/NMDA.mod
+    (Kampa et al. 2004; POINT_PROCESS NMDA_Mg): rate constants of its PARAMETER block
+    (mg = 1 mM, valence -2, memb_fraction 0.8), the voltage- and glutamate-dependent
+    rates and the thirteen reactions of KINETIC kstates, CONSERVE sum 1, open state O.
+    Inputs in lti_sim's order (sorted by name): C (glutamate, mM) then v (mV)."""
+    states = ["U", "Cl", "D1", "D2", "O", "UMg", "ClMg", "D1Mg", "D2Mg", "OMg"]
+    U, Cl, D1, D2, O, UMg, ClMg, D1Mg, D2Mg, OMg = range(10)
+    P = dict(Rb=10e-3, Ru=5.6e-3, Ro=10e-3, Rc=273e-3, Rd1=2.2e-3, Rr1=1.6e-3, Rd2=0.43e-3, Rr2=0.5e-3,
+             Rmb=0.05e-3, Rmu=12800e-3, Rmc1b=0.00005e-3, Rmc1u=2.438312e-3, Rmc2b=0.00005e-3,
+             Rmc2u=5.041915e-3, Rmd1b=0.00005e-3, Rmd1u=2.98874e-3, Rmd2b=0.00005e-3, Rmd2u=2.953408e-3,
+             RbMg=10e-3, RuMg=17.1e-3, RoMg=10e-3, RcMg=548e-3, Rd1Mg=2.1e-3, Rr1Mg=0.87e-3, Rd2Mg=0.26e-3,
+             Rr2Mg=0.42e-3, mg=1.0, valence=-2.0, memb_fraction=0.8)
+
+    def transitions(C, v, celsius):
+        p = P
+        block = np.exp((v - 40.0) * p["valence"] * p["memb_fraction"] / 25.0)
+        unblock = np.exp(-1.0 * (v - 40.0) * p["valence"] * (1.0 - p["memb_fraction"]) / 25.0)
+        rb = p["Rb"] * 1e3 * C
+        rbMg = p["RbMg"] * 1e3 * C
+        rmb, rmu = p["Rmb"] * p["mg"] * 1e3 * block, p["Rmu"] * unblock
+        rmc1b, rmc1u = p["Rmc1b"] * p["mg"] * 1e3 * block, p["Rmc1u"] * unblock
+        rmc2b, rmc2u = p["Rmc2b"] * p["mg"] * 1e3 * block, p["Rmc2u"] * unblock
+        rmd1b, rmd1u = p["Rmd1b"] * p["mg"] * 1e3 * block, p["Rmd1u"] * unblock
+        rmd2b, rmd2u = p["Rmd2b"] * p["mg"] * 1e3 * block, p["Rmd2u"] * unblock
+        one = np.ones_like(v)
+        pairs = [(U, Cl, rb, p["Ru"] * one), (Cl, O, p["Ro"] * one, p["Rc"] * one),
+                 (Cl, D1, p["Rd1"] * one, p["Rr1"] * one), (D1, D2, p["Rd2"] * one, p["Rr2"] * one),
+                 (O, OMg, rmb, rmu), (UMg, ClMg, rbMg, p["RuMg"] * one), (ClMg, OMg, p["RoMg"] * one, p["RcMg"] * one),
+                 (ClMg, D1Mg, p["Rd1Mg"] * one, p["Rr1Mg"] * one), (D1Mg, D2Mg, p["Rd2Mg"] * one, p["Rr2Mg"] * one),
+                 (U, UMg, rmc1b, rmc1u), (Cl, ClMg, rmc2b, rmc2u), (D1, D1Mg, rmd1b, rmd1u), (D2, D2Mg, rmd2b, rmd2u)]
+        out = []
+        for a, b, kf, kb in pairs:
+            out.append((a, b, kf))
+            out.append((b, a, kb))
+        return out
+    return KineticScheme2("NMDA_Mg", states, transitions, open_states=["O"], input_names=("C", "v"), conserve_sum=1.0)
+
+
+class LTITable2:
+    """Two-input polynomial approximation of the per-step propagator (lti_sim's
+    Approx2D, approx.py:242-275): per bucket pair (b1, b2), every matrix entry is
+    fitted by least squares over samples in the bucket with the terms
+    loc1^p1 * loc2^p2.  Samples sit on a grid of ``samples_per_axis`` sub-bucket
+    midpoints per input, or are given (``sample_inputs`` = (x1, x2), e.g. the
+    reference's own random samples).  ``layout`` is [b1 * nb2 + b2][col][row][term]."""
+
+    def __init__(self, scheme, dt, celsius, input1, input2, terms, samples_per_axis=4, sample_inputs=None):
+        self.scheme, self.dt, self.celsius = scheme, float(dt), float(celsius)
+        self.inputs = (input1, input2)
+        self.terms = canonical_terms(terms)
+        self.powers = np.array(self.terms, dtype=np.int32)
+        S, T = scheme.num_states, len(self.terms)
+        nb1, nb2 = input1.num_buckets, input2.num_buckets
+        if sample_inputs is None:
+            sub = (np.arange(samples_per_axis) + 0.5) / samples_per_axis
+            g1, g2 = np.meshgrid(sub, sub, indexing="ij")
+            p1 = (np.arange(nb1)[:, None, None] + np.zeros(nb2)[None, :, None] + g1.ravel()[None, None, :]).ravel()
+            p2 = (np.zeros(nb1)[:, None, None] + np.arange(nb2)[None, :, None] + g2.ravel()[None, None, :]).ravel()
+            x1, x2 = input1.value(p1), input2.value(p2)
+        else:
+            x1, x2 = (np.asarray(x, dtype=np.float64) for x in sample_inputs)
+        exact = scheme.exact_propagator(x1, x2, self.dt, self.celsius)
+        pos1, pos2 = input1.position(x1), input2.position(x2)
+        b1, b2 = pos1.astype(np.int64), pos2.astype(np.int64)                  # approx.py:16-18
+        flat = b1 * nb2 + b2
+        order = np.argsort(flat, kind="stable")
+        flat, pos1, pos2, b1, b2, exact = flat[order], pos1[order], pos2[order], b1[order], b2[order], exact[order]
+        bounds = np.searchsorted(flat, np.arange(nb1 * nb2 + 1))
+        table = np.empty((nb1 * nb2, S, S, T))
+        for f in range(nb1 * nb2):
+            lo, hi = bounds[f], bounds[f + 1]
+            l1, l2 = pos1[lo:hi] - b1[lo:hi], pos2[lo:hi] - b2[lo:hi]
+            A = np.stack([l1 ** a * l2 ** b for a, b in self.terms], axis=1)
+            coef = np.linalg.lstsq(A, exact[lo:hi].reshape(-1, S * S), rcond=None)[0]
+            table[f] = coef.reshape(T, S, S).transpose(1, 2, 0)
+        self.table = table                                                     # [b][row][col][term]
+        self.layout = np.ascontiguousarray(table.transpose(0, 2, 1, 3))        # [b][col][row][term]
+
+    def basis(self, loc1, loc2):
+        out = []
+        for a, b in self.terms:
+            x = np.ones_like(loc1)
+            for k in range(a):
+                x = loc1 if k == 0 else x * loc1
+            for k in range(b):
+                x = loc2 if (k == 0 and a == 0) else x * loc2
+            out.append(x)
+        return np.stack(out, axis=-1)
+
+    def approximate(self, x1, x2):
+        """The table's matrices at inputs (x1, x2): shape (n, row, col)."""
+        (b1, l1), (b2, l2) = self.inputs[0].locate(x1), self.inputs[1].locate(x2)
+        f = b1 * self.inputs[1].num_buckets + b2
+        return np.einsum("ncrt,nt->nrc", self.layout[f], self.basis(l1, l2))
+
+    def max_error(self, samples_per_axis=5):
+        """Max |table - exact| over a grid of points in every bucket pair."""
+        i1, i2 = self.inputs
+        sub = (np.arange(samples_per_axis) + 0.37) / samples_per_axis
+        p1 = (np.arange(i1.num_buckets)[:, None] + sub[None, :]).ravel()
+        p2 = (np.arange(i2.num_buckets)[:, None] + sub[None, :]).ravel()
+        P1, P2 = np.meshgrid(p1, p2, indexing="ij")
+        x1, x2 = i1.value(P1.ravel()), i2.value(P2.ravel())
+        err = 0.0
+        for k in range(0, len(x1), 20000):
+            exact = self.scheme.exact_propagator(x1[k:k + 20000], x2[k:k + 20000], self.dt, self.celsius)
+            err = max(err, float(np.abs(self.approximate(x1[k:k + 20000], x2[k:k + 20000]) - exact).max()))
+        return err
+
+
+def table_inputs2(scheme, celsius, input1, input2, terms, samples_per_axis=4):
+    """Rate matrices at the grid samples of every bucket pair (bucket-major, flat bucket
+    b1 * nb2 + b2) and the pseudo-inverse of the two-input fit (the same for every
+    bucket pair): the inputs of nw_lti_table_build for a two-input table."""
+    terms = canonical_terms(terms)
+    k = int(samples_per_axis)
+    sub = (np.arange(k) + 0.5) / k
+    g1, g2 = np.meshgrid(sub, sub, indexing="ij")
+    g1, g2 = g1.ravel(), g2.ravel()
+    nb1, nb2 = input1.num_buckets, input2.num_buckets
+    p1 = (np.arange(nb1)[:, None, None] + np.zeros(nb2)[None, :, None] + g1[None, None, :]).ravel()
+    p2 = (np.zeros(nb1)[:, None, None] + np.arange(nb2)[None, :, None] + g2[None, None, :]).ravel()
+    rates = np.ascontiguousarray(scheme.matrix(input1.value(p1), input2.value(p2), celsius), dtype=np.float64)
+    A = np.stack([g1 ** a * g2 ** b for a, b in terms], axis=1)
+    fit = np.ascontiguousarray(np.linalg.pinv(A))
+    return rates, fit, terms
+
+
+def scheme_table_gpu2(ctx, scheme, dt, celsius, input1, input2, terms, samples_per_axis=4, target=0):
+    """A two-input table built on the GPU in FP64 (nw_lti_table_build over the flat
+    bucket pairs)."""
+    rates, fit, terms = table_inputs2(scheme, celsius, input1, input2, terms, samples_per_axis)
+    return gpu_table(ctx, rates, fit, input1.num_buckets * input2.num_buckets, dt, target)
+
+
 def binomial_state(m, h):
     """Na8 occupancy equivalent to HH gates (m, h)."""
     s = np.zeros(8)
@@ -373,11 +591,20 @@ class Kinetic(Mechanism):
     ion = None
     table = None
     vmin, vmax, num_buckets, degree = -100.0, 60.0, 1600, 1
+    # Two-input schemes (KineticScheme2): the table inputs (TableInput, in the
+    # scheme's input order), the polynomial terms (powers per input) and the grid
+    # samples per input and bucket; the instance value input starts at its
+    # TableInput's initial value and reads / writes as "<name>.input".
+    inputs, terms, samples_per_axis = None, None, 4
+    # A point process (POINT_PROCESS): gbar in S per instance, times the instance's
+    # magnitude, instead of a density in S/cm2 times its area.
+    point_process = False
     _model = None
 
     @classmethod
     def configure(cls, **params):
-        ok = {"name", "scheme_factory", "gbar", "erev", "ion", "table", "vmin", "vmax", "num_buckets", "degree"}
+        ok = {"name", "scheme_factory", "gbar", "erev", "ion", "table", "vmin", "vmax", "num_buckets", "degree",
+              "inputs", "terms", "samples_per_axis", "point_process"}
         bad = set(params) - ok
         if bad:
             raise ValueError(f"unknown kinetic parameters {sorted(bad)}")
@@ -408,7 +635,20 @@ class Kinetic(Mechanism):
 
     @classmethod
     def build_table(cls, dt, celsius):
+        if cls.inputs is not None:
+            return LTITable2(cls.scheme_factory(), dt, celsius, cls.inputs[0], cls.inputs[1], cls.terms,
+                             cls.samples_per_axis)
         return LTITable(cls.scheme_factory(), dt, celsius, cls.vmin, cls.vmax, cls.num_buckets, cls.degree)
+
+    @classmethod
+    def initial_state(cls, voltage, celsius):
+        """The steady state at the initial inputs (voltage; instance values at their
+        TableInput's initial value)."""
+        sch = cls.scheme_factory()
+        if cls.inputs is None:
+            return sch.steady_state(voltage, celsius)
+        x = [voltage if inp.kind == "voltage" else inp.initial for inp in cls.inputs]
+        return sch.steady_state(x[0], x[1], celsius)
 
 
 # The reference library's kinetic channels restated above, as mechanisms: the
@@ -421,3 +661,15 @@ Nav11 = Kinetic.configure(name="na11a", scheme_factory=nav11, gbar=0.1, ion="na"
                           num_buckets=2000, degree=1)
 Kv11 = Kinetic.configure(name="Kv11_6States_temperature2", scheme_factory=kv11, gbar=0.036, ion="k",
                          vmin=-100.0, vmax=100.0, num_buckets=2000, degree=1)
+
+# The reference library's NMDA receptor (nmodl_library/kinetic/NMDA.mod, POINT_PROCESS
+# NMDA_Mg): gmax 500 pS per synapse, Erev 5 mV, NONSPECIFIC_CURRENT; a two-input table
+# over the glutamate concentration C (LogarithmicInput 0..1000 mM, the range the
+# reference's NMODL front end gives a POINTER, nmodl/__init__.py:323-324; log scale
+# 0.01 mM, 30 buckets) and the voltage (LinearInput -100..100 mV, 100 buckets), with
+# quadratic polynomials: max entry error 7e-5 at dt 0.1 ms, below the 1e-4 the
+# reference's front end asks of lti_sim (nmodl/__init__.py:305).
+NMDA = Kinetic.configure(name="NMDA_Mg", scheme_factory=nmda, gbar=500e-12, erev=5.0, point_process=True,
+                         inputs=(TableInput("C", "log", 0.0, 1000.0, 30, scale=1e-2),
+                                 TableInput("v", "voltage", -100.0, 100.0, 100)),
+                         terms=[(0, 0), (1, 0), (0, 1), (2, 0), (1, 1), (0, 2)])

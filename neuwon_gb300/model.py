@@ -570,8 +570,7 @@ class RxD_Model:
                     self._ctx.set_data(attr, np.full(m, float(val)))
             elif issubclass(cls, Kinetic):
                 m = self._instance_count(name)
-                sch = cls.scheme_factory()
-                init = sch.steady_state(self.initial_voltage, self.temperature)
+                init = cls.initial_state(self.initial_voltage, self.temperature)
                 self._ctx.set_data(self.kinetic_state_name(name), np.tile(init, m))
         self._ctx.call("nw_set_option", b"reset_clock", 1)
         self.input_hook.ticks = 0
@@ -617,9 +616,28 @@ class RxD_Model:
         cls = self.mechanisms[mech]
         n = self._instance_count(cls.get_name())
         if issubclass(cls, Kinetic):
+            if attr == "input":
+                return self._ctx.get_data(self.kinetic_state_name(mech)[:-len("state")] + "input", n)
             S = len(cls.scheme_factory().states)
             return self._ctx.get_data(self.kinetic_state_name(mech), n * S).reshape(n, S)
         return self._ctx.get_data(f"hh.{attr}", n)
+
+    def set_data(self, name, values):
+        """Whole-attribute write in creation order: a kinetic mechanism's states
+        ('<name>.state', instances x states) or the instance values of a two-input
+        table ('<name>.input', e.g. NMDA_Mg.input: the glutamate concentration, mM)."""
+        mech, attr = name.split(".")
+        self._sync()
+        cls = self.mechanisms.get(mech)
+        if cls is None or not issubclass(cls, Kinetic) or attr not in ("state", "input"):
+            raise KeyError(f"{name}: set_data takes '<kinetic mechanism>.state' or '.input'")
+        n = self._instance_count(cls.get_name())
+        values = np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64),
+                                                      (n,) if attr == "input" else (n, len(cls.scheme_factory().states))))
+        target = self.kinetic_state_name(mech)
+        if attr == "input":
+            target = target[:-len("state")] + "input"
+        self._ctx.set_data(target, values.ravel())
 
     def close(self):
         if self._ctx is not None:
@@ -869,11 +887,21 @@ class RxD_Model:
         seg, magnitude = self._insertion_magnitude(rec)
         gbar = np.concatenate(rec["gbar"]) if rec["gbar"] else np.empty(0)
         gbar = np.where(np.isnan(gbar), cls.gbar, gbar)
-        g = np.ascontiguousarray(gbar * 1e-8 * magnitude)
+        if cls.point_process:                  # S per instance times its magnitude (default 1)
+            raw = np.concatenate(rec["mag"]) if rec["mag"] else np.empty(0)
+            g = np.ascontiguousarray(gbar * raw)
+        else:
+            g = np.ascontiguousarray(gbar * 1e-8 * magnitude)
         # The table is generated on the GPU in FP64 (nw_lti_table_build) the first
         # time this mechanism, step and temperature are seen, then reused.
         sch = cls.scheme_factory()
-        nb, T = cls.num_buckets, cls.degree + 1
+        two = cls.inputs is not None
+        if two:
+            from .kinetic import canonical_terms
+            terms = canonical_terms(cls.terms)
+            nb, T = cls.inputs[0].num_buckets * cls.inputs[1].num_buckets, len(terms)
+        else:
+            nb, T = cls.num_buckets, cls.degree + 1
         key = (cls, self.time_step, self.temperature)
         cache = getattr(self, "_tables", {})
         self._tables = cache
@@ -886,7 +914,7 @@ class RxD_Model:
         placeholder = layout is None
         if placeholder:
             layout = np.zeros((nb, sch.num_states, sch.num_states, T))
-        init = np.ascontiguousarray(sch.steady_state(self.initial_voltage, self.temperature))
+        init = np.ascontiguousarray(cls.initial_state(self.initial_voltage, self.temperature))
         open_idx = np.asarray(sch.open_states, dtype=np.int32)
         seg_dev = np.ascontiguousarray(self._inv[seg]) if len(seg) else seg
         cs = float(sch.conserve_sum) if sch.conserve_sum is not None else 0.0
@@ -898,10 +926,22 @@ class RxD_Model:
                        _lib.ptr(np.ascontiguousarray(layout.ravel())), nb, T, float(cls.vmin), frq, cs, _lib.ptr(init),
                        _lib.ctypes.byref(q))
         self._kin_index[cls.get_name()] = q.value
+        if two:
+            i1, i2 = cls.inputs
+            inst = [inp for inp in cls.inputs if inp.kind != "voltage"]
+            powers = np.ascontiguousarray(np.array(terms, dtype=np.int32).ravel())
+            self._ctx.call("nw_kinetic_inputs", q.value, i1.code, i1.num_buckets, i1.minimum, i1.bucket_frq, i1.scale,
+                           i2.code, i2.num_buckets, i2.minimum, i2.bucket_frq, i2.scale, T, _lib.ptr(powers),
+                           float(inst[0].initial if inst else 0.0))
         if placeholder and len(seg):
-            from .kinetic import scheme_table_gpu
-            cache[key] = scheme_table_gpu(self._ctx, sch, self.time_step, self.temperature, cls.vmin, cls.vmax, nb,
-                                          cls.degree, target=16 + q.value)
+            if two:
+                from .kinetic import scheme_table_gpu2
+                cache[key] = scheme_table_gpu2(self._ctx, sch, self.time_step, self.temperature, cls.inputs[0],
+                                               cls.inputs[1], cls.terms, cls.samples_per_axis, target=16 + q.value)
+            else:
+                from .kinetic import scheme_table_gpu
+                cache[key] = scheme_table_gpu(self._ctx, sch, self.time_step, self.temperature, cls.vmin, cls.vmax,
+                                              nb, cls.degree, target=16 + q.value)
 
     def _sync_clamps(self):
         c = self._clamps

@@ -193,8 +193,16 @@ class KineticInstances:
     ``layout`` is the flattened table [bucket][col][row][term] (codegen.py:29-37)."""
 
     def __init__(self, segment, g_coef, layout, vmin, bucket_frq, open_states, erev,
-                 conserve_sum, init_state, species=None):
+                 conserve_sum, init_state, species=None, inputs=None, powers=None, input_values=None):
+        """Two-input tables (lti_sim Approx2D, approx.py:242-337): ``inputs`` is a pair
+        of (kind, num_buckets, minimum, bucket_frq, scale) with kind "voltage",
+        "log" (LogarithmicInput) or "linear", ``powers`` the terms' (p1, p2), and
+        ``input_values`` the instances' value of the non-voltage input; the layout
+        is [b1 * nb2 + b2][col][row][term]."""
         self.species = species
+        self.inputs = inputs
+        self.powers = None if powers is None else [tuple(p) for p in powers]
+        self.input_values = None if input_values is None else np.asarray(input_values, dtype=np.float64)
         self.segment = np.asarray(segment, dtype=np.int64)
         m = len(self.segment)
         self.g_coef = np.broadcast_to(np.asarray(g_coef, np.float64), (m,)).copy()
@@ -212,7 +220,53 @@ class KineticInstances:
     def zero_accumulators(self):
         self.g.fill(0.0)
 
+    def _locate2(self, voltage):
+        """Flat bucket and the basis of every instance for a two-input table
+        (codegen.py:43-70: inputs located one by one, flat index b1 * nb2 + b2)."""
+        v = voltage[self.segment]
+        locs, buckets = [], []
+        for kind, nb, minimum, frq, scale in self.inputs:
+            x = v if kind == "voltage" else self.input_values
+            if kind == "log":
+                pos = (np.log2(x + scale) - np.log2(minimum + scale)) * frq          # codegen.py:47-48
+            else:
+                pos = (x - minimum) * frq                                          # codegen.py:45
+            b = np.trunc(pos).astype(np.int64)
+            hi = b > nb - 1
+            lo = (~hi) & (b < 0)
+            locs.append(np.where(hi, 1.0, np.where(lo, 0.0, pos - b)))
+            buckets.append(np.where(hi, nb - 1, np.where(lo, 0, b)))
+        flat = buckets[0] * self.inputs[1][1] + buckets[1]
+        basis = []
+        for a, b in self.powers:                                   # factors in order, codegen.py:64-69
+            x = np.ones(len(v))
+            for k in range(a):
+                x = locs[0] if k == 0 else x * locs[0]
+            for k in range(b):
+                x = locs[1] if (k == 0 and a == 0) else x * locs[1]
+            basis.append(x)
+        return flat, basis
+
     def advance(self, voltage):
+        if self.inputs is not None:
+            flat, basis = self._locate2(voltage)
+            tbl = self.layout[flat]
+            scratch = np.zeros((len(flat), self.S))
+            for col in range(self.S):
+                s = self.state[:, col]
+                for row in range(self.S):
+                    poly = np.zeros(len(flat))
+                    for t, (a, b) in enumerate(self.powers):
+                        poly = poly + (tbl[:, col, row, t] if a == 0 and b == 0 else basis[t] * tbl[:, col, row, t])
+                    scratch[:, row] += poly * s
+            if self.conserve_sum is not None:
+                total = scratch[:, 0].copy()
+                for x in range(1, self.S):
+                    total += scratch[:, x]
+                scratch *= (self.conserve_sum / total)[:, None]
+            self.state = scratch
+            self.g += self.g_coef * self.state[:, self.open_states].sum(axis=1)
+            return
         v = voltage[self.segment]
         inp = (v - self.vmin) * self.frq                         # codegen.py:45
         bucket = np.trunc(inp).astype(np.int64)                  # int(input0)

@@ -501,6 +501,42 @@ def run_lti(out):
     out["lti_v"], out["lti_state"], out["lti_new"] = v, st, np.array(new)
 
 
+def run_lti2(out):
+    """The reference's two-input table builder (Approx2D, approx.py:242-275) on the
+    NMDA receptor scheme of nmodl_library/kinetic/NMDA.mod (restated as
+    neuwon_gb300.kinetic.nmda, inputs sorted by name as lti_model.py:8 sorts them: C,
+    then v), with quadratic terms on 4 x 8 buckets: its table, its random sample
+    inputs, its approximate matrices at test points and its initial state."""
+    np.random.seed(4321)
+    if not hasattr(np, "product"):
+        np.product = np.prod            # removed in numpy 2; used by approx.py:81
+    from neuwon.rxd.lti_sim import LTI_Model, LinearInput, LogarithmicInput
+    from neuwon.rxd.lti_sim.approx import Approx2D, MatrixSamples
+    from neuwon_gb300.kinetic import nmda
+    sch = nmda()
+
+    def derivative(C, v, *state):
+        return list(sch.matrix([C], [v], 6.3)[0] @ np.array(state))
+    c_in = LogarithmicInput('C', 'self.C', 0, 1000)
+    v_in = LinearInput('v', 'self.segment.voltage', -100, 100)
+    model = LTI_Model('NMDA_Mg', [v_in, c_in], sch.states, derivative, 1.0, 0.1)
+    c_in.set_num_buckets(4, scale=1e-2)
+    v_in.set_num_buckets(8)
+    terms = [(0, 0), (1, 0), (0, 1), (2, 0), (1, 1), (0, 2)]
+    samples = MatrixSamples(model)
+    approx = Approx2D(samples, terms)
+    out["lti2_table"] = approx.table                               # [bC][bv][row][col][term]
+    out["lti2_terms"] = np.array(approx.polynomial.terms)
+    out["lti2_samples_C"], out["lti2_samples_v"] = samples.inputs[0], samples.inputs[1]
+    rng = np.random.default_rng(9)
+    C = np.concatenate([10.0 ** rng.uniform(-4, 3, 40), [0.0, 1000.0, 0.5]])
+    v = np.concatenate([rng.uniform(-100, 100, 40), [-100.0, 100.0, 120.0]])
+    out["lti2_C"], out["lti2_v"] = C, v
+    out["lti2_approx"] = np.array([approx.approximate_matrix(c, x) for c, x in zip(C, v)])
+    init = model.get_initial_state()
+    out["lti2_init"] = np.array([init[x] for x in sch.states])     # at the inputs' minimum (C 0, v -100)
+
+
 def scenarios():
     """Fixture groups by key prefix, each a function of the output dict."""
     from neuwon_gb300.morphology import random_tree, Tree
@@ -551,7 +587,7 @@ def scenarios():
                    dict(ena=50.0, ek=-77.0, el=-54.3), 30.0, False)
 
     return {"geom": run_geometry_and_propagator, "hh11": hh11, "hh200": hh200, "multi": multi, "c1": c1,
-            "lti": run_lti, "species": run_species, "dropin": dropin}
+            "lti": run_lti, "lti2": run_lti2, "species": run_species, "dropin": dropin}
 
 
 def main():

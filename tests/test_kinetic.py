@@ -85,3 +85,55 @@ def test_table_inputs_fit_equals_host_least_squares():
     table = np.einsum("ts,bsrc->bcrt", fit, P.reshape(nb, spb, 8, 8))
     host = LTITable(sch, 0.1, 6.3, num_buckets=nb, degree=deg, samples_per_bucket=spb)
     assert np.abs(table - host.layout).max() < 1e-12
+
+
+def _nmda_inputs(nb_c=4, nb_v=8):
+    from neuwon_gb300.kinetic import TableInput
+    return (TableInput("C", "log", 0.0, 1000.0, nb_c, scale=1e-2), TableInput("v", "voltage", -100.0, 100.0, nb_v))
+
+
+def test_two_input_table_matches_reference_approx2d():
+    """NMDA.mod's scheme on the reference's own random samples: the least-squares
+    table, the approximate matrices at test points (clamped outside the table) and
+    the canonical term order equal the reference's Approx2D."""
+    from neuwon_gb300.kinetic import LTITable2, canonical_terms, nmda
+    terms = [(0, 0), (1, 0), (0, 1), (2, 0), (1, 1), (0, 2)]
+    assert [tuple(t) for t in F["lti2_terms"]] == canonical_terms(terms)
+    i1, i2 = _nmda_inputs()
+    t = LTITable2(nmda(), 0.1, 6.3, i1, i2, terms, sample_inputs=(F["lti2_samples_C"], F["lti2_samples_v"]))
+    ref = F["lti2_table"].reshape(t.table.shape)
+    assert np.abs(t.table - ref).max() < 1e-10 * max(1.0, np.abs(ref).max())
+    assert np.abs(t.approximate(F["lti2_C"], F["lti2_v"]) - F["lti2_approx"]).max() < 1e-9
+
+
+def test_two_input_initial_state_matches_reference():
+    from neuwon_gb300.kinetic import nmda
+    assert np.abs(nmda().steady_state(0.0, -100.0, 6.3) - F["lti2_init"]).max() < 1e-10
+
+
+def test_oracle_two_input_step_matches_reference_approximation():
+    """The oracle's restatement of the generated two-input kernel, on the reference's
+    table: state' = M(C, v) state, then CONSERVE."""
+    from neuwon_gb300.kinetic import nmda
+    sch = nmda()
+    i1, i2 = _nmda_inputs()
+    layout = F["lti2_table"].reshape(32, 10, 10, 6).transpose(0, 2, 1, 3)
+    C, v = F["lti2_C"], F["lti2_v"]
+    ki = KineticInstances(np.arange(len(v)), 1.0, layout, 0.0, 1.0, sch.open_states, 5.0, 1.0, np.zeros(10),
+                          inputs=[("log", 4, 0.0, i1.bucket_frq, 1e-2), ("voltage", 8, -100.0, i2.bucket_frq, 1.0)],
+                          powers=F["lti2_terms"], input_values=C)
+    rng = np.random.default_rng(3)
+    st = rng.dirichlet(np.ones(10), len(v))
+    ki.state = st.copy()
+    ki.advance(v)
+    want = np.einsum("nrc,nc->nr", F["lti2_approx"], st)
+    want /= want.sum(axis=1, keepdims=True)
+    assert np.abs(ki.state - want).max() < 1e-12
+
+
+def test_nmda_table_within_reference_target():
+    """The default NMDA table (30 log buckets of C, 100 of v, quadratic) meets the
+    1e-4 max entry error the reference's front end asks of lti_sim."""
+    from neuwon_gb300.kinetic import NMDA
+    t = NMDA.build_table(0.1, 6.3)
+    assert t.max_error(2) < 1e-4
