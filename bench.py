@@ -589,7 +589,8 @@ def precision_study(args, device):
     out = {"metric": "precision study: FP32 vs FP64, max |dV| (mV) and max relative d[Ca]",
            "config": {"workload": f"one tree of {len(tree)} segments, HH + calcium (diffusion 0.6 um2/ms, 3-state "
                                   f"pump, 0.5 % of the Na current as Ca), {args.study_current:g} nA soma clamp, dt 0.025 ms",
-                      "steps": steps, "path": "wide", "pruning": "charge/mass-conserving"},
+                      "steps": steps, "path": "wide", "pruning": "charge/mass-conserving",
+                      "wide_fusion": args.wide_fusion},
            "results": []}
     for tol in (1e-6, 1e-9):
         models = {}
@@ -602,6 +603,7 @@ def precision_study(args, device):
             m.insert_everywhere("hh")
             nr.root.inject_current(args.study_current, 1e9)
             m._sync()
+            m._ctx.set_option("wide_fusion", args.wide_fusion)
             m._ctx.call("nw_synchronize")
             models[precision] = (m, time.perf_counter() - t0)
         dv = dca = 0.0
@@ -667,6 +669,8 @@ def main():
     ap.add_argument("--study-segments", type=int, default=1_000_000)
     ap.add_argument("--study-steps", type=int, default=20000)
     ap.add_argument("--study-current", type=float, default=10.0, help="soma clamp of the precision study (nA)")
+    ap.add_argument("--wide-fusion", type=int, default=1, choices=[0, 1],
+                    help="precision study: one launch per half step (1) or one per phase (0)")
     ap.add_argument("--diff-check", action="store_true",
                     help="differentiation configuration: FP32/FP64 adjoint vs FP64 central differences (own JSON line)")
     ap.add_argument("--diff-steps", type=int, default=8000)
