@@ -547,6 +547,81 @@ def network_leg(device, steps, neurons=4096, synapses=2_000_000):
     return out
 
 
+def wide_bytes_per_segment_step(windows_per_row, ca_entries_per_row, calcium=True, prec=4):
+    """Compulsory HBM bytes of one step of the fused wide path per segment (FP32):
+    per half step the voltage propagator's quad windows (16 B of values and a 4 B
+    base each), its row pointer (8 B) and leak, x read and the next x and V written;
+    with calcium the same for its propagator (entries in 4-entry vectors of 4 B
+    values and 4 B columns), scratch read and written and c written; per step the
+    HH gates (read and written), their conductance coefficients and kG, kI, and
+    with calcium the pump states (read and written), dc/dt and the influx and
+    efflux coefficients."""
+    half = 20 * windows_per_row + 8 + prec + 3 * prec + 2 * prec
+    if calcium:
+        half += 2 * prec * ca_entries_per_row + 8 + prec + 3 * prec
+    step = 2 * half + 2 * 3 * prec + 3 * prec
+    if calcium:
+        step += 2 * 3 * prec + 3 * prec
+    return step
+
+
+def wide_leg(device, segments, tol, steps, variants=((1, 0),)):
+    """The precision configuration's step on the wide path, timed: one seeded tree
+    (same length and diameter laws), HH + calcium (diffusion, pump, Na influx),
+    FP32, dt 0.025 ms, propagators pruned at `tol` (charge/mass-conserving), 10 nA
+    soma clamp.  For each (wide_fusion, lanes per row; 0 = by row length) variant:
+    64 untimed steps (formats built, graphs captured), then `steps` steps timed
+    with CUDA events on the library's stream."""
+    import torch
+    import neuwon_gb300 as nw
+    from neuwon_gb300.morphology import random_tree
+    tree = random_tree(segments, seed=3)
+    m = nw.RxD_Model(time_step=0.025, temperature=6.3, precision="f32", path="wide", species=[nw.Calcium()],
+                     propagator_tolerance=tol, propagator_conserve=True, device=device,
+                     mechanisms=[nw.HH.configure(ena=50.0, ek=-77.0, el=-54.3)])
+    nr = m.add_tree(tree)
+    m.insert_everywhere("hh")
+    nr.root.inject_current(10.0, 1e9)
+    m._sync()
+    ctx = m._ctx
+    sptr = ctypes.c_void_p()
+    ctx.call("nw_get_stream", ctypes.byref(sptr))
+    stream = torch.cuda.ExternalStream(sptr.value, device=torch.device("cuda", device))
+    peak, src = 6800.0, "fallback"
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    runs = []
+    for wide_fusion, lanes in variants:
+        ctx.call("nw_set_tuning", lanes, 1024, 0)
+        ctx.set_option("wide_fusion", wide_fusion)
+        m.advance(64)
+        ctx.call("nw_synchronize")
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        m.advance(steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        n = m._n
+        wpr = ctx.get_option("wide_quads") / n
+        epr = ctx.get_option("calcium_wide_entries") / n
+        B = wide_bytes_per_segment_step(wpr, epr)
+        achieved = B * n / (ms * 1e-3) / 1e9
+        runs.append({"wide_fusion": wide_fusion, "lanes_per_row": lanes or "by row length", "ms_per_step": ms,
+                     "segment_steps_per_s": n * 1e3 / ms,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved / peak, "peak_source": src}})
+        log(f"wide leg {runs[-1]}")
+    spikes = int(m.get_data("Neuron.spike_count")[0])
+    m.close()
+    return {"segments": n, "steps": steps, "tolerance": tol, "windows_per_row": wpr, "calcium_entries_per_row": epr,
+            "bytes_per_segment_step": B, "runs": runs, "spikes": spikes,
+            "config": f"one tree of {n} segments, HH + calcium, FP32, dt 0.025 ms, propagators {tol:g} "
+                      "(charge/mass-conserving), quad format, 10 nA soma clamp"}
+
+
 def run_leg(args, rank, local):
     """One side leg alone (rank 0), at its configuration's shape or a smaller case."""
     if rank != 0:
@@ -561,6 +636,9 @@ def run_leg(args, rank, local):
     torch.cuda.set_device(local)
     if args.leg == "adjoint":
         out = adjoint_leg(local, args.adjoint_steps, neurons=args.leg_neurons or 256, size=args.leg_size or 2000)
+    elif args.leg == "wide":
+        variants = [tuple(int(x) for x in v.split(":")) for v in args.wide_variants.split(",")]
+        out = wide_leg(local, args.study_segments, args.wide_tol, args.wide_steps, variants)
     elif args.leg == "network":
         out = network_leg(local, args.network_steps, neurons=args.leg_neurons or 4096,
                           synapses=args.leg_synapses or 2_000_000)
@@ -607,8 +685,10 @@ def precision_study(args, device):
             m._ctx.call("nw_synchronize")
             models[precision] = (m, time.perf_counter() - t0)
         dv = dca = 0.0
+        # Step times leave out the first chunk (wide formats built, graphs captured)
+        # when there is more than one.
         times = {"f64": 0.0, "f32": 0.0}
-        done = 0
+        done = timed = 0
         while done < steps:
             k = min(chunk, steps - done)
             for precision, (m, _) in models.items():
@@ -616,7 +696,10 @@ def precision_study(args, device):
                 t0 = time.perf_counter()
                 m.advance(k)
                 m._ctx.call("nw_synchronize")
-                times[precision] += time.perf_counter() - t0
+                if done > 0 or steps <= chunk:
+                    times[precision] += time.perf_counter() - t0
+            if done > 0 or steps <= chunk:
+                timed += k
             done += k
             v64, v32 = (models[p][0].get_data("Segment.voltage") for p in ("f64", "f32"))
             c64, c32 = (models[p][0].get_data("Species.ca") for p in ("f64", "f32"))
@@ -626,7 +709,7 @@ def precision_study(args, device):
         nnz = models["f32"][0].propagator_nnz / len(tree)
         res = {"tolerance": tol, "max_abs_dV_mV": dv, "max_rel_dCa": dca, "spikes": spikes,
                "entries_per_row": nnz, "calcium_entries_per_row": models["f32"][0].calcium_nnz / len(tree),
-               "ms_per_step": {p: 1e3 * times[p] / steps for p in times},
+               "ms_per_step": {p: 1e3 * times[p] / timed for p in times}, "timed_steps": timed,
                "build_s": {p: models[p][1] for p in models}}
         log(f"precision study {res}")
         out["results"].append(res)
@@ -660,6 +743,8 @@ def main():
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
+    ap.add_argument("--l2-prefetch", type=int, default=1, choices=[0, 1],
+                    help="fused pass: bulk L2 prefetch of each neuron's mechanism state")
     ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu/adjoint legs")
     ap.add_argument("--adjoint-steps", type=int, default=800)
     ap.add_argument("--network-steps", type=int, default=200,
@@ -675,7 +760,11 @@ def main():
                     help="differentiation configuration: FP32/FP64 adjoint vs FP64 central differences (own JSON line)")
     ap.add_argument("--diff-steps", type=int, default=8000)
     ap.add_argument("--diff-neurons", type=int, default=256)
-    ap.add_argument("--leg", choices=["adjoint", "network", "plain"],
+    ap.add_argument("--wide-tol", type=float, default=1e-9, help="propagator tolerance of the wide leg")
+    ap.add_argument("--wide-steps", type=int, default=320, help="timed steps of the wide leg")
+    ap.add_argument("--wide-variants", default="1:0",
+                    help="wide leg: comma-separated wide_fusion:lanes_per_row (0 = by row length)")
+    ap.add_argument("--leg", choices=["adjoint", "network", "plain", "wide"],
                     help="run one side leg alone and print its JSON line (a small case with --leg-neurons, "
                          "--leg-size, --leg-synapses, --adjoint-steps / --network-steps)")
     ap.add_argument("--leg-neurons", type=int, default=0)
@@ -755,6 +844,7 @@ def main():
     ctx = model._ctx
     ctx.call("nw_set_tuning", args.lanes, args.threads, 0)
     ctx.call("nw_set_option", b"bulk_pipeline", args.bulk)
+    ctx.set_option("l2_prefetch", args.l2_prefetch)
     ctx.set_option("fusion_depth", max(1, min(args.fusion, args.steps)))
     ctx.call("nw_synchronize")
     build_s = time.perf_counter() - t_build

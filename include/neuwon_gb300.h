@@ -200,7 +200,7 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
  * S <= 16; FP64 scaling and squaring), then per bucket the polynomial fit
  * table[b][col][row][t] = sum_s fit[t][s] * P[b, s][row][col] (fit = the
  * least-squares pseudo-inverse of the in-bucket sample locations, the same for
- * every bucket).  target 16 + q installs the table as kinetic mechanism q's (1 is
+ * every bucket; 1 <= num_terms <= 10).  target 16 + q installs the table as kinetic mechanism q's (1 is
  * the same as 16: mechanism 0), 2 as the calcium pump's (shapes must match what is
  * registered), 0 only returns it; table_out (may be NULL) receives it in FP64. */
 int nw_lti_table_build(nw_ctx* ctx, int32_t S, int32_t num_buckets, int32_t samples_per_bucket,
@@ -382,7 +382,15 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * "bulk_pipeline" (default 0): stream the propagator of the FP32
  * batched path through shared memory with cp.async.bulk copies (needs lanes_per_row
  * 0 in nw_set_tuning); nw_get_option("bulk_pipeline_active") tells whether the next
- * batched launch will use it. */
+ * batched launch will use it.
+ * "wide_fusion" (default 1): the wide path runs one launch per half step when the
+ * mechanisms map one-to-one onto segments.
+ * "l2_prefetch" (default 1): when the batched kernel fuses the mechanism pass, one
+ * warp asks L2 (cp.async.bulk.prefetch) for the neuron's mechanism state at the start
+ * of each step, so the pass between the two half steps reads it from L2 (no change
+ * in results).  nw_get_option also reports "wide_quads", "wide_entries" and
+ * "calcium_wide_entries" (stored windows / entries of the wide path's voltage and
+ * calcium propagators, once built). */
 int nw_set_option(nw_ctx* ctx, const char* name, int64_t value);
 int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value);
 

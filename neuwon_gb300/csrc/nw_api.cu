@@ -1242,6 +1242,7 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     if (!ctx || !name) return NW_ERR_ARG;
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
+    if (nm == "l2_prefetch") { ctx->l2_prefetch = value != 0; return NW_OK; }
     if (nm == "cuda_graph") { ctx->use_graph = value != 0; return NW_OK; }
     if (nm == "spike_neurons" || nm == "spike_neuron_offset" || nm == "spike_ring_steps") {
         // Partitioned networks: taken by the next nw_synapses_set.
@@ -1339,6 +1340,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (!ctx || !name || !value) return NW_ERR_ARG;
     std::string nm(name);
     if (nm == "bulk_pipeline") { *value = ctx->use_bulk ? 1 : 0; return NW_OK; }
+    if (nm == "l2_prefetch") { *value = ctx->l2_prefetch ? 1 : 0; return NW_OK; }
     if (nm == "bulk_pipeline_active") { *value = uses_bulk_pipeline(ctx) ? 1 : 0; return NW_OK; }
     if (nm == "cuda_graph") { *value = ctx->use_graph ? 1 : 0; return NW_OK; }
     if (nm == "propagator_format") { *value = ctx->prop_format; return NW_OK; }
@@ -1347,7 +1349,9 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "kinetic_mechanisms") { *value = ctx->n_kin; return NW_OK; }
     if (nm == "pair_entries") { *value = ctx->nnz_f; return NW_OK; }
     if (nm == "quads") { *value = ctx->nq; return NW_OK; }
-    if (nm == "wide_fusion") { ctx->wide_fusion = value != 0; return NW_OK; }
+    if (nm == "wide_quads") { *value = ctx->nwq; return NW_OK; }
+    if (nm == "wide_entries") { *value = ctx->nnz_w; return NW_OK; }
+    if (nm == "calcium_wide_entries") { *value = ctx->ca.on ? ctx->ca.nnz_w : 0; return NW_OK; }
     if (nm == "lanes_split") { *value = ctx->lanes_split; return NW_OK; }
     if (nm == "wide_fusion") { *value = ctx->wide_fusion ? 1 : 0; return NW_OK; }
     if (nm == "narrow_neurons") {

@@ -73,7 +73,8 @@ __global__ void lti_fit_kernel(const double* __restrict__ P, const double* __res
     const int b = (int)(t / (S * S));
     const int c = (int)((t / S) % S);
     const int r = (int)(t % S);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    double acc[kMaxTerms];
+    for (int k = 0; k < kMaxTerms; ++k) acc[k] = 0.0;
     for (int s = 0; s < spb; ++s) {
         const double* p = P + ((int64_t)b * spb + s) * S * S;
         double col = 0.0;
@@ -119,7 +120,7 @@ int nw_lti_table_build(nw_ctx* ctx, int32_t S, int32_t num_buckets, int32_t samp
     cudaSetDevice(ctx->device);
     const bool kin_target = target == 1 || (target >= 16 && target < 16 + kMaxKinetic);
     if (S < 1 || S > kLtiMaxStates || num_buckets < 1 || samples_per_bucket < 1 || num_terms < 1 ||
-        num_terms > 4 || !rates || !fit || !(dt > 0.0) || !(target == 0 || target == 2 || kin_target))
+        num_terms > kMaxTerms || !rates || !fit || !(dt > 0.0) || !(target == 0 || target == 2 || kin_target))
         return fail(ctx, NW_ERR_ARG, "nw_lti_table_build: bad arguments");
     const int64_t count = (int64_t)num_buckets * samples_per_bucket;
     const int64_t tn = (int64_t)num_buckets * S * S * num_terms;

@@ -297,6 +297,120 @@ __device__ __forceinline__ void flux_finalize(const StepArgs<real>& a, int64_t b
     }
 }
 
+// ------------------------------------------------------------ fused mechanism pass
+
+// The fused pass's register form applies: no kinetic mechanism, or one of 8
+// states, 2 terms and one input.
+template <typename real>
+__device__ __forceinline__ bool fused_fast_form(const StepArgs<real>& a) {
+    return a.n_kin == 0 || (a.n_kin == 1 && a.kin[0].S == 8 && a.kin[0].T == 2 && a.kin[0].ninp == 1);
+}
+
+// Lane `lane` of one warp asks L2 for one of the per-segment arrays the fused
+// pass of neuron [base, base + n) reads (kG, kI, the HH gates and coefficients,
+// the nonspecific current, each kinetic mechanism's coefficient and states), so
+// that the pass, which runs between two barriers while the CTA's stream is
+// idle, finds them in L2 instead of HBM.
+template <typename real>
+__device__ __forceinline__ void prefetch_fused_inputs(const StepArgs<real>& a, int64_t base, int n, int lane) {
+    const size_t bytes = (size_t)n * sizeof(real);
+    const real* p = nullptr;
+    if (lane < 2) p = lane == 0 ? a.kG : a.kI;
+    else if (lane < 8) {
+        if (a.hh_on) {
+            switch (lane) {
+                case 2: p = a.gm; break;
+                case 3: p = a.gh; break;
+                case 4: p = a.gn; break;
+                case 5: p = a.cna; break;
+                case 6: p = a.ck; break;
+                default: p = a.cl; break;
+            }
+        }
+    } else if (lane == 8) {
+        if (a.has_nonspec) p = a.Inonspec;
+    } else {
+        int k = lane - 9;
+        for (int q = 0; q < a.n_kin && !p; ++q) {
+            const KinArgs<real>& K = a.kin[q];
+            if (k == 0) p = K.gcoef;
+            else if (k <= K.S) p = K.state + (int64_t)(k - 1) * K.m;
+            k -= K.S + 1;
+        }
+    }
+    if (p) l2_prefetch(p + base, bytes);
+}
+
+// One segment of the fused mechanism pass (instances in segment order): the
+// mechanisms at the mid-step voltage v (rxd_model.py:115-123), the segment's
+// conductance and G*E (cached for the next step's first half when `keep`), and
+// the second half step's x, which it returns (I = the segment's stimulus then).
+// Register form: every input of the segment is loaded before the first store,
+// and the conductances come from registers through the helpers
+// segment_conductance uses, in its order, so the same bits as the general form.
+template <typename real>
+__device__ __forceinline__ real fused_segment_fast(const StepArgs<real>& a, int64_t i, real v, real I, bool keep,
+                                                   bool last1) {
+    const KinArgs<real>& K = a.kin[0];
+    const bool kin_on = a.n_kin > 0;
+    const real kGi = a.kG[i], kIi = a.kI[i];
+    real m = real(0), h = real(0), nn = real(0);
+    real cna = real(0), ck = real(0), cl = real(0), gco = real(0);
+    real st[8];
+    if (a.hh_on) {
+        m = a.gm[i]; h = a.gh[i]; nn = a.gn[i];
+        cna = a.cna[i]; ck = a.ck[i]; cl = a.cl[i];
+    }
+    if (kin_on) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) st[c] = K.state[(int64_t)c * K.m + i];
+        gco = K.gcoef[i];
+    }
+    real G = real(0), GE = real(0);
+    if (a.hh_on) {
+        hh_gates(v, a.dtq10, m, h, nn);
+        real gna = real(0), gk = real(0), gl = real(0);
+        hh_conductance_add(cna, ck, cl, m, h, nn, gna, gk, gl);
+        hh_conductance_total(a, gna, gk, gl, G, GE);
+    }
+    if (kin_on) {
+        kinetic_advance<real, 8, 2>(K, v, st);
+        const real open = kinetic_open(K, [&](int c) {
+            real x = st[0];
+#pragma unroll
+            for (int q = 1; q < 8; ++q) x = (c == q) ? st[q] : x;
+            return x;
+        });
+        real gkin = real(0);
+        gkin += gco * open;
+        G += gkin;
+        GE += gkin * K.erev;
+    }
+    if (a.hh_on) { a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn; }
+    if (kin_on) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) K.state[(int64_t)c * K.m + i] = st[c];
+    }
+    if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
+    return membrane_x_of(a, i, v, kGi, kIi, G, GE, I, last1);
+}
+
+// The same for any set of one-to-one mechanisms (state through memory).
+template <typename real>
+__device__ __forceinline__ real fused_segment_general(const StepArgs<real>& a, int64_t i, real v, real I, bool keep,
+                                                      bool last1) {
+    if (a.hh_on) {
+        real m = a.gm[i], h = a.gh[i], nn = a.gn[i];
+        hh_gates(v, a.dtq10, m, h, nn);
+        a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
+    }
+    for (int q = 0; q < a.n_kin; ++q) kinetic_step(a.kin[q], i, v);
+    real G, GE;
+    segment_conductance(a, i, G, GE);
+    if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
+    return membrane_x_of(a, i, v, a.kG[i], a.kI[i], G, GE, I, last1);
+}
+
 template <typename real, int LPR, bool BULK, bool FLUX, bool QUAD = false, bool FUSE = false, bool WIN = false>
 __global__ void __launch_bounds__(1024)
 batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_off) {
@@ -426,6 +540,8 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                 const bool last = (s == a.k_steps - 1) && (half == 1);
                 // The propagator does not depend on x: start streaming it now.
                 if (BULK) bulk_prologue(a, ring, slice);
+                // The fused pass's inputs into L2 while the first half's rows stream.
+                if (fuse && half == 0 && a.l2_prefetch && tid < 32) prefetch_fused_inputs(a, base, n, tid);
                 // With fused mechanisms the second half's x comes from the mechanism
                 // pass, and later steps' first halves take G from the cache (the
                 // state it was computed from does not change in between).
@@ -486,70 +602,17 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     // the segment's conductance and the second half's x, in one pass.
                     const bool last1 = s == a.k_steps - 1;
                     const bool keep = s + 1 < a.k_steps;
-                    const bool kin_on = a.n_kin > 0;
-                    if (a.n_kin == 0 || (a.n_kin == 1 && a.kin[0].S == 8 && a.kin[0].T == 2 && a.kin[0].ninp == 1)) {
-                        // Every input of the segment is loaded before the first store, and
-                        // the conductances come from registers (same helpers and order as
-                        // segment_conductance, so the same bits).
-                        const KinArgs<real>& K = a.kin[0];
+                    if (fused_fast_form(a)) {
                         for (int li = tid; li < n; li += nthr) {
                             const int64_t i = base + li;
-                            const real v = a.V[i], kGi = a.kG[i], kIi = a.kI[i];
-                            const real I = stim(i, tick + 1);
-                            real m = real(0), h = real(0), nn = real(0);
-                            real cna = real(0), ck = real(0), cl = real(0), gco = real(0);
-                            real st[8];
-                            if (a.hh_on) {
-                                m = a.gm[i]; h = a.gh[i]; nn = a.gn[i];
-                                cna = a.cna[i]; ck = a.ck[i]; cl = a.cl[i];
-                            }
-                            if (kin_on) {
-#pragma unroll
-                                for (int c = 0; c < 8; ++c) st[c] = K.state[(int64_t)c * K.m + i];
-                                gco = K.gcoef[i];
-                            }
-                            real G = real(0), GE = real(0);
-                            if (a.hh_on) {
-                                hh_gates(v, a.dtq10, m, h, nn);
-                                real gna = real(0), gk = real(0), gl = real(0);
-                                hh_conductance_add(cna, ck, cl, m, h, nn, gna, gk, gl);
-                                hh_conductance_total(a, gna, gk, gl, G, GE);
-                            }
-                            if (kin_on) {
-                                kinetic_advance<real, 8, 2>(K, v, st);
-                                const real open = kinetic_open(K, [&](int c) {
-                                    real x = st[0];
-#pragma unroll
-                                    for (int q = 1; q < 8; ++q) x = (c == q) ? st[q] : x;
-                                    return x;
-                                });
-                                real gkin = real(0);
-                                gkin += gco * open;
-                                G += gkin;
-                                GE += gkin * K.erev;
-                            }
-                            if (a.hh_on) { a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn; }
-                            if (kin_on) {
-#pragma unroll
-                                for (int c = 0; c < 8; ++c) K.state[(int64_t)c * K.m + i] = st[c];
-                            }
-                            if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
-                            xs[li] = membrane_x_of(a, i, v, kGi, kIi, G, GE, I, last1);
+                            const real v = a.V[i];
+                            xs[li] = fused_segment_fast(a, i, v, stim(i, tick + 1), keep, last1);
                         }
                     } else {
                         for (int li = tid; li < n; li += nthr) {
                             const int64_t i = base + li;
                             const real v = a.V[i];
-                            if (a.hh_on) {
-                                real m = a.gm[i], h = a.gh[i], nn = a.gn[i];
-                                hh_gates(v, a.dtq10, m, h, nn);
-                                a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
-                            }
-                            for (int q = 0; q < a.n_kin; ++q) kinetic_step(a.kin[q], i, v);
-                            real G, GE;
-                            segment_conductance(a, i, G, GE);
-                            if (keep) { a.gc[i] = G; a.gc[a.gc_n + i] = GE; }
-                            xs[li] = membrane_x(a, i, G, GE, stim(i, tick + 1), last1);
+                            xs[li] = fused_segment_general(a, i, v, stim(i, tick + 1), keep, last1);
                         }
                     }
                     __syncthreads();

@@ -147,6 +147,8 @@ struct StepArgs {
     // same launch; fuse_mech when every conductance source maps one-to-one onto
     // segments (HH and kinetic instances in segment order, no synapses or calcium).
     real* gc; int64_t gc_n; int fuse_mech;
+    // Fused pass: ask L2 for the neuron's mechanism state at the start of each step.
+    int l2_prefetch;
     // clamps (sorted by segment)
     const uint32_t* clamp_seg_ptr;
     const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
@@ -562,6 +564,19 @@ template <> struct Vec2Loader<double> {
     }
 };
 
+// Asks L2 for the whole 16-byte blocks of [p, p + bytes) ahead of their use
+// (cp.async.bulk.prefetch; no data moves to the SM, no completion to wait for).
+// The range is shrunk to 16-byte boundaries inside it, in pieces of at most 64 KB.
+__device__ __forceinline__ void l2_prefetch(const void* p, size_t bytes) {
+    uint64_t a = ((uint64_t)p + 15) & ~(uint64_t)15;
+    const uint64_t e = ((uint64_t)p + bytes) & ~(uint64_t)15;
+    while (a < e) {
+        const uint32_t len = (uint32_t)((e - a) < 65536 ? (e - a) : 65536);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(a), "r"(len) : "memory");
+        a += len;
+    }
+}
+
 template <typename real>
 __device__ __forceinline__ void kahan_add(real& s, real& c, real term) {
     real y = term - c;
@@ -640,6 +655,47 @@ __device__ __forceinline__ void propagate_rows(const StepArgs<real>& a, int64_t 
 // Quad format: row i is a list of windows (base b, values v0..v3 for columns
 // b..b+3); the window's four x are consecutive in shared memory (neurons of
 // fewer than 4 segments keep zeros in x[n..3]).
+//
+// One row r of a row group of LPR lanes (lane l of the group; every lane of the
+// warp calls this, valid or not): sum over the row's windows of P_ij (x_j - x_i),
+// each lane taking every LPR-th window with UNROLL windows loaded before any is
+// used, compensated lane sums reduced over the group, so every lane of the
+// group returns the row's sum.
+template <typename real, int LPR, int UNROLL>
+__device__ __forceinline__ real quad_row_sum(const StepArgs<real>& a, bool valid, int64_t r, int l,
+                                             const real* __restrict__ xs, real xi) {
+    real s = real(0), c = real(0);
+    if (valid) {
+        const int64_t beg = a.qrow[r], end = a.qrow[r + 1];
+        for (int64_t k0 = beg + l; k0 < end; k0 += LPR * UNROLL) {
+            real v[UNROLL][4];
+            int b[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                const int64_t k = k0 + LPR * u;
+                if (k < end) {
+                    Vec4Loader<real>::load(a.qval + 4 * k, v[u]);
+                    b[u] = __ldcs(a.qbase + k);
+                } else {
+                    v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                    b[u] = 0;                         // zero weights on x[0..3]
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                const real* x = xs + b[u];
+                const real p = v[u][0] * (x[0] - xi) + v[u][1] * (x[1] - xi);
+                const real t = v[u][2] * (x[2] - xi) + v[u][3] * (x[3] - xi);
+                kahan_add(s, c, p + t);
+            }
+        }
+    }
+    real t = s - c;
+#pragma unroll
+    for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    return t;
+}
+
 template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
 __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t base, int n,
                                                 const real* __restrict__ xs, Fin fin) {
@@ -651,41 +707,10 @@ __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t
     for (int rb = warp * GPW; rb < n; rb += nwarps * GPW) {
         const int row = rb + q;
         const bool valid = row < n;
-        real s = real(0), c = real(0), xi = real(0);
-        if (valid) {
-            const int64_t r = base + row;
-            const int64_t beg = a.qrow[r], end = a.qrow[r + 1];
-            xi = xs[row];
-            for (int64_t k0 = beg + l; k0 < end; k0 += LPR * UNROLL) {
-                real v[UNROLL][4];
-                int b[UNROLL];
-#pragma unroll
-                for (int u = 0; u < UNROLL; ++u) {
-                    const int64_t k = k0 + LPR * u;
-                    if (k < end) {
-                        Vec4Loader<real>::load(a.qval + 4 * k, v[u]);
-                        b[u] = __ldcs(a.qbase + k);
-                    } else {
-                        v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
-                        b[u] = 0;                         // zero weights on x[0..3]
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < UNROLL; ++u) {
-                    const real* x = xs + b[u];
-                    const real p = v[u][0] * (x[0] - xi) + v[u][1] * (x[1] - xi);
-                    const real t = v[u][2] * (x[2] - xi) + v[u][3] * (x[3] - xi);
-                    kahan_add(s, c, p + t);
-                }
-            }
-        }
-        real t = s - c;
-#pragma unroll
-        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-        if (valid && l == 0) {
-            const int64_t r = base + row;
-            fin(r, row, xi, (xi - a.leak[r] * xi) + t);
-        }
+        const int64_t r = base + row;
+        const real xi = valid ? xs[row] : real(0);
+        const real t = quad_row_sum<real, LPR, UNROLL>(a, valid, r, l, xs, xi);
+        if (valid && l == 0) fin(r, row, xi, (xi - a.leak[r] * xi) + t);
     }
 }
 
@@ -840,6 +865,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.ca_on = Ca.on ? 1 : 0;
     a.gc = ctx->gcache.as<real>(); a.gc_n = ctx->n_seg;
     a.fuse_mech = fuse_mechanisms(ctx) ? 1 : 0;
+    a.l2_prefetch = ctx->l2_prefetch ? 1 : 0;
     a.h_ms = (real)(0.5 * ctx->time_step);
     if (Ca.on) {
         a.ca_pump = Ca.pump ? 1 : 0; a.ca_nb = Ca.nb; a.ca_T = Ca.T;

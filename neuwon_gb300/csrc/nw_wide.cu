@@ -178,8 +178,10 @@ __global__ void wide_detect_kernel(const StepArgs<real> a, const int s_off) {
 // When every conductance source maps one-to-one onto segments (HH and kinetic
 // instances in segment order, no synapses), a half step is one launch: each warp
 // applies the propagator to 32 consecutive rows (LPR lanes per row, the row
-// format's or the quad format's loop as in wide_rows_kernel / wide_quads_kernel,
-// reading x from x_in), parks the 32 results in shared memory, and then each lane
+// format's or the quad format's sums as in wide_rows_kernel / wide_quads_kernel,
+// reading x from x_in; the 32 row pointers and x_i come in one coalesced load
+// each, and every lane has UNROLL windows in flight before it sums any), parks
+// the 32 results in shared memory, and then each lane
 // finishes its own segment i: V_i, the calcium row i (one lane per row, reading
 // the scratch cs_in), and, after the first half, the mechanisms at the mid-step
 // voltage (HH, kinetic, calcium, rxd_model.py:115-123), the new conductance and
@@ -195,49 +197,72 @@ wide_fused_kernel(const StepArgs<real> a, const int64_t* __restrict__ rowptr, co
                   const int s_off, const int phase, const int last, const int next) {
     __shared__ real vnew_s[kWideThreads];
     constexpr int GPW = 32 / LPR;
+    constexpr int UNROLL = 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t n = a.neuron_start[a.n_neuron];
     const int64_t r0 = ((int64_t)blockIdx.x * (kWideThreads / 32) + warp) * 32;
     if (r0 >= n) return;                                  // the whole warp leaves
     const int q = lane / LPR, l = lane % LPR;
+    // Row starts and x of the warp's 32 rows, one coalesced load each (lane k holds
+    // row r0 + k), handed to the row groups by shuffles: no row waits for its own
+    // row pointer before its propagator loads.
+    const int64_t rk = r0 + lane;
+    const int64_t beg_k = rowptr[rk < n ? rk : n];
+    const int64_t end_32 = rowptr[r0 + 32 < n ? r0 + 32 : n];
+    const real x_k = rk < n ? __ldg(x_in + rk) : real(0);
     real* vb = vnew_s + warp * 32;
     for (int g = 0; g < 32; g += GPW) {
         const int64_t r = r0 + g + q;
         const bool valid = r < n;
-        real s = real(0), c = real(0), xi = real(0);
-        if (valid) {
-            xi = __ldg(x_in + r);
-            const int64_t beg = rowptr[r], end = rowptr[r + 1];
-            if (QUAD) {
-                for (int64_t k0 = beg + l; k0 < end; k0 += 2 * LPR) {
-                    real v[2][4];
-                    int32_t b[2];
+        const int64_t beg = __shfl_sync(0xffffffffu, beg_k, g + q);
+        const int64_t nxt = __shfl_sync(0xffffffffu, beg_k, (g + q + 1) & 31);
+        const int64_t end = g + q + 1 < 32 ? nxt : end_32;
+        const real xi = __shfl_sync(0xffffffffu, x_k, g + q);
+        real s = real(0), c = real(0);
+        // UNROLL windows (quads) or 4-entry vectors (rows) per lane are loaded before
+        // any is used.
+        if (QUAD) {
+            for (int64_t k0 = beg + l; k0 < end; k0 += LPR * UNROLL) {
+                real v[UNROLL][4];
+                int32_t b[UNROLL];
 #pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const int64_t k = k0 + LPR * u;
-                        if (k < end) {
-                            Vec4Loader<real>::load(val + 4 * k, v[u]);
-                            b[u] = __ldcs(colidx + k);
-                        } else {
-                            v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
-                            b[u] = 0;
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const real* xb = x_in + b[u];
-                        const real p = v[u][0] * (__ldg(xb) - xi) + v[u][1] * (__ldg(xb + 1) - xi);
-                        const real t = v[u][2] * (__ldg(xb + 2) - xi) + v[u][3] * (__ldg(xb + 3) - xi);
-                        kahan_add(s, c, p + t);
+                for (int u = 0; u < UNROLL; ++u) {
+                    const int64_t k = k0 + LPR * u;
+                    if (k < end) {
+                        Vec4Loader<real>::load(val + 4 * k, v[u]);
+                        b[u] = __ldcs(colidx + k);
+                    } else {
+                        v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                        b[u] = 0;
                     }
                 }
-            } else {
-                for (int64_t k = beg + 4 * l; k < end; k += 4 * LPR) {
-                    real v[4];
-                    Vec4Loader<real>::load(val + k, v);
-                    const int4 cc = __ldcs(reinterpret_cast<const int4*>(colidx + k));
-                    const real p = v[0] * (__ldg(x_in + cc.x) - xi) + v[1] * (__ldg(x_in + cc.y) - xi);
-                    const real t = v[2] * (__ldg(x_in + cc.z) - xi) + v[3] * (__ldg(x_in + cc.w) - xi);
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const real* xb = x_in + b[u];
+                    const real p = v[u][0] * (__ldg(xb) - xi) + v[u][1] * (__ldg(xb + 1) - xi);
+                    const real t = v[u][2] * (__ldg(xb + 2) - xi) + v[u][3] * (__ldg(xb + 3) - xi);
+                    kahan_add(s, c, p + t);
+                }
+            }
+        } else {
+            for (int64_t k0 = beg + 4 * l; k0 < end; k0 += 4 * LPR * UNROLL) {
+                real v[UNROLL][4];
+                int4 cc[UNROLL];
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const int64_t k = k0 + 4 * LPR * u;
+                    if (k < end) {
+                        Vec4Loader<real>::load(val + k, v[u]);
+                        cc[u] = __ldcs(reinterpret_cast<const int4*>(colidx + k));
+                    } else {
+                        v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                        cc[u] = make_int4(0, 0, 0, 0);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < UNROLL; ++u) {
+                    const real p = v[u][0] * (__ldg(x_in + cc[u].x) - xi) + v[u][1] * (__ldg(x_in + cc[u].y) - xi);
+                    const real t = v[u][2] * (__ldg(x_in + cc[u].z) - xi) + v[u][3] * (__ldg(x_in + cc[u].w) - xi);
                     kahan_add(s, c, p + t);
                 }
             }
@@ -370,8 +395,10 @@ static int enqueue_wide_fused(nw_ctx* ctx, const StepArgs<real>& a, int steps) {
     const unsigned seg_blocks = (unsigned)((n + kWideThreads - 1) / kWideThreads);
     const int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
     const bool quad = ctx->prop_format == 2 && ctx->wq_ok;
+    // Lanes per row by the mean windows (or 4-entry vectors) per row: about 2-4 per
+    // lane, so one round of UNROLL loads covers most rows.
     const double avg = n ? (double)(quad ? ctx->nwq : ctx->nnz_w / 4) / (double)n : 0.0;
-    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg >= 24 ? 16 : 8);
+    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg > 32 ? 16 : avg > 12 ? 8 : 4);
     real* x0 = a.px;
     real* x1 = ctx->wide_x2.as<real>();
     real* c0 = a.ca_scratch;
@@ -390,7 +417,8 @@ static int enqueue_wide_fused(nw_ctx* ctx, const StepArgs<real>& a, int steps) {
             const real* ci = phase == 0 ? c0 : c1;
             real* co = phase == 0 ? c1 : c0;
             if (lanes >= 16) launch_fused_lpr<real, 16>(ctx, a, quad, xi, xo, ci, co, s, phase, last, !last);
-            else launch_fused_lpr<real, 8>(ctx, a, quad, xi, xo, ci, co, s, phase, last, !last);
+            else if (lanes == 8) launch_fused_lpr<real, 8>(ctx, a, quad, xi, xo, ci, co, s, phase, last, !last);
+            else launch_fused_lpr<real, 4>(ctx, a, quad, xi, xo, ci, co, s, phase, last, !last);
             NW_CUDA(ctx, cudaGetLastError());
         }
         wide_detect_kernel<real><<<(unsigned)((cover + 127) / 128), 128, 0, ctx->stream>>>(a, s);

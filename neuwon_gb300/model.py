@@ -68,8 +68,11 @@ class Segment:
     __slots__ = ("_model", "_idx")
 
     def __init__(self, model, idx):
+        idx = int(idx)
+        if not 0 <= idx < model._n:
+            raise IndexError(f"segment {idx} out of range (the model has {model._n} segments)")
         self._model = model
-        self._idx = int(idx)
+        self._idx = idx
 
     def __eq__(self, other):
         return isinstance(other, Segment) and other._model is self._model and other._idx == self._idx

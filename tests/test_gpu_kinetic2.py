@@ -86,7 +86,7 @@ def test_two_input_gpu_table_equals_host_table():
     """nw_lti_table_build over the flat bucket pairs (FP64 expm and fit on the GPU)
     equals the host FP64 build on the same grid."""
     from neuwon_gb300.kinetic import scheme_table_gpu2
-    m = _model(random_tree(20, seed=1), "f64", "batched")
+    m = _model(random_tree(200, seed=1), "f64", "batched")
     m._sync()
     i1, i2 = NMDA.inputs
     gpu = scheme_table_gpu2(m._ctx, nmda(), 0.1, 6.3, i1, i2, NMDA.terms, NMDA.samples_per_axis)
