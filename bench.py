@@ -743,8 +743,6 @@ def main():
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
-    ap.add_argument("--l2-prefetch", type=int, default=1, choices=[0, 1],
-                    help="fused pass: bulk L2 prefetch of each neuron's mechanism state")
     ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu/adjoint legs")
     ap.add_argument("--adjoint-steps", type=int, default=800)
     ap.add_argument("--network-steps", type=int, default=200,
@@ -844,7 +842,6 @@ def main():
     ctx = model._ctx
     ctx.call("nw_set_tuning", args.lanes, args.threads, 0)
     ctx.call("nw_set_option", b"bulk_pipeline", args.bulk)
-    ctx.set_option("l2_prefetch", args.l2_prefetch)
     ctx.set_option("fusion_depth", max(1, min(args.fusion, args.steps)))
     ctx.call("nw_synchronize")
     build_s = time.perf_counter() - t_build

@@ -385,10 +385,7 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * batched launch will use it.
  * "wide_fusion" (default 1): the wide path runs one launch per half step when the
  * mechanisms map one-to-one onto segments.
- * "l2_prefetch" (default 1): when the batched kernel fuses the mechanism pass, one
- * warp asks L2 (cp.async.bulk.prefetch) for the neuron's mechanism state at the start
- * of each step, so the pass between the two half steps reads it from L2 (no change
- * in results).  nw_get_option also reports "wide_quads", "wide_entries" and
+ * nw_get_option also reports "wide_quads", "wide_entries" and
  * "calcium_wide_entries" (stored windows / entries of the wide path's voltage and
  * calcium propagators, once built). */
 int nw_set_option(nw_ctx* ctx, const char* name, int64_t value);

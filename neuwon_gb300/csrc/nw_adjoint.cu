@@ -44,11 +44,16 @@ struct AdjArgs {
     int update_detectors;
     // reverse sweep
     real* lamV; real* lamV2; real* lamM; real* lamH; real* lamN;
-    double* gGna; double* gGk; double* gGl;
-    double* ra_part;            // [n_neuron]
+    // Density gradients as compensated sums: sum at [0, n_seg), compensation at
+    // [n_seg, 2 n_seg) of each (true value = sum - compensation).
+    real* gGna; real* gGk; real* gGl;
+    double* ra_part;            // [n_neuron]: sums of flow * d(lambda / C), scaled on the host
     const int64_t* parent;
     const double* res;
     const double* cap;
+    // 1/C, C and 1/R per segment in the state precision (the reverse sweep's
+    // per-segment arithmetic stays off the FP64 pipe).
+    const real* inv_cap; const real* cap_r; const real* inv_res;
     double loss_scale;          // 2 / (total_steps * n_neuron)
     double inv_ra;
     double h_s;                 // half step in seconds
@@ -179,26 +184,25 @@ __global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<rea
 // Reverse sweep of one half step of segment i's neuron (called by all threads).
 // lam_out holds lambda of the half step's output voltage, lam_in receives lambda
 // of its input voltage; the gate adjoints of `gates` accumulate in lamM/H/N.
+// The dP/dRa term of the half step (electric.py's coefficients scale with 1/Ra)
+// accumulates flow_i * (lambda_i / C_i - lambda_p / C_p) per segment with a parent,
+// into the thread's compensated sum (ra_s, ra_c); the factor -h / Ra is applied
+// once per neuron.  Density gradients accumulate in compensated sums per segment.
 template <typename real, int LPR>
 __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_t base, int n, real* xs,
                                                   const real* V_in, const real* V_out, const real* gm,
                                                   const real* gh, const real* gn, const real* lam_out,
-                                                  real* lam_in, bool gv, double& ra_acc) {
+                                                  real* lam_in, bool gv, real& ra_s, real& ra_c) {
     const StepArgs<real>& a = A.a;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    const int64_t ns = A.n_seg;
     for (int li = tid; li < n; li += nthr) {
         const int64_t i = base + li;
-        const double ci = A.cap[i];
-        xs[li] = (real)((double)lam_out[i] / ci);
-        const int64_t p = A.parent[i];
-        if (p >= 0) {
-            const double flow = ((double)V_out[p] - (double)V_out[i]) / A.res[i];
-            ra_acc += -A.inv_ra * A.h_s * flow * ((double)lam_out[i] / ci - (double)lam_out[p] / A.cap[p]);
-        }
+        xs[li] = lam_out[i] * A.inv_cap[i];
     }
     __syncthreads();
     propagate_rows<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real nu) {
-        const real lx = (real)((double)nu * A.cap[r]);
+        const real lx = nu * A.cap_r[r];
         if (!gv) {                       // G = 0: x = V, no parameter dependence
             lam_in[r] = lx;
             return;
@@ -216,14 +220,29 @@ __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_
         const real lG = -a.kG[r] * alpha * lalpha - (E / G) * lE;
         const real lGE = lE / G;
         const real wna = lG + lGE * a.ena, wk = lG + lGE * a.ek, wl = lG + lGE * a.el;
-        A.gGna[r] += (double)wna * (double)M;
-        A.gGk[r] += (double)wk * (double)N4;
-        A.gGl[r] += (double)wl;
+        auto acc = [&](real* g, real term) {
+            real sg = g[r], cg = g[ns + r];
+            kahan_add(sg, cg, term);
+            g[r] = sg;
+            g[ns + r] = cg;
+        };
+        acc(A.gGna, wna * M);
+        acc(A.gGk, wk * N4);
+        acc(A.gGl, wl);
         const real lM = wna * a.cna[r], lN4 = wk * a.ck[r];
         A.lamM[r] += lM * real(3) * m * m * h;
         A.lamH[r] += lM * m * m * m;
         A.lamN[r] += lN4 * real(4) * nn * nn * nn;
     });
+    // xs still holds lambda / C of every segment of the neuron (the rows only read it).
+    for (int li = tid; li < n; li += nthr) {
+        const int64_t i = base + li;
+        const int64_t p = A.parent[i];
+        if (p >= 0) {
+            const real flow = (V_out[p] - V_out[i]) * A.inv_res[i];
+            kahan_add(ra_s, ra_c, flow * (xs[li] - xs[p - base]));
+        }
+    }
     __syncthreads();
 }
 
@@ -243,7 +262,7 @@ __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<rea
         const int j = a.neuron_order[job];
         const int64_t base = a.neuron_start[j];
         const int n = (int)(a.neuron_start[j + 1] - base);
-        double ra_acc = 0.0;
+        real ra_s = real(0), ra_c = real(0);
         for (int s = a.k_steps - 1; s >= 0; --s) {
             const int64_t gs = A.step0 + s;
             if (tid == 0 && A.target) {
@@ -255,7 +274,7 @@ __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<rea
             // Second half step: V_mid, gates(s+1) -> V(s+1).
             half_step_reverse<real, LPR>(A, base, n, xs, tape_slot(A, s, 1), tape_slot(A, s + 1, 0),
                                          tape_slot(A, s + 1, 2), tape_slot(A, s + 1, 3), tape_slot(A, s + 1, 4),
-                                         A.lamV, A.lamV2, true, ra_acc);
+                                         A.lamV, A.lamV2, true, ra_s, ra_c);
             // Mechanisms: gates(s+1) = f(gates(s), V_mid).
             for (int li = tid; li < n; li += nthr) {
                 const int64_t i = base + li;
@@ -276,18 +295,29 @@ __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<rea
             const bool gv = (gs > 0) || A.g_valid_first;
             half_step_reverse<real, LPR>(A, base, n, xs, tape_slot(A, s, 0), tape_slot(A, s, 1),
                                          tape_slot(A, s, 2), tape_slot(A, s, 3), tape_slot(A, s, 4),
-                                         A.lamV2, A.lamV, gv, ra_acc);
+                                         A.lamV2, A.lamV, gv, ra_s, ra_c);
         }
-        // Fixed-order reduction of the Ra partial sums.
-        s_red[tid] = ra_acc;
+        // Fixed-order reduction of the Ra partial sums, scaled by -h / Ra.
+        s_red[tid] = (double)ra_s - (double)ra_c;
         __syncthreads();
         if (tid == 0) {
             double r = 0.0;
             for (int t = 0; t < nthr; ++t) r += s_red[t];
-            A.ra_part[j] += r;
+            A.ra_part[j] += -A.inv_ra * A.h_s * r;
         }
         __syncthreads();
     }
+}
+
+// 1/C, C and 1/R of every segment in the state precision (1/R = 0 for a root).
+template <typename real>
+__global__ void adj_coef_kernel(int64_t n, const double* __restrict__ cap, const double* __restrict__ res,
+                                real* __restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = (real)(1.0 / cap[i]);
+    out[n + i] = (real)cap[i];
+    out[2 * n + i] = res[i] > 0.0 ? (real)(1.0 / res[i]) : real(0);
 }
 
 // ---------------------------------------------------------------- host
@@ -425,9 +455,13 @@ static int adjoint_backward_impl(nw_ctx* ctx, double Ra, double* g_gna, double* 
         NW_CUDA(ctx, cudaMemsetAsync(buf->ptr, 0, b, ctx->stream));
     }
     for (DevBuf* buf : {&S.gGna, &S.gGk, &S.gGl}) {
-        NW_CHECK(dev_alloc(ctx, *buf, 8 * n));
-        NW_CUDA(ctx, cudaMemsetAsync(buf->ptr, 0, 8 * n, ctx->stream));
+        NW_CHECK(dev_alloc(ctx, *buf, 2 * b));
+        NW_CUDA(ctx, cudaMemsetAsync(buf->ptr, 0, 2 * b, ctx->stream));
     }
+    NW_CHECK(dev_alloc(ctx, S.coef, 3 * b));
+    adj_coef_kernel<real><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+        n, ctx->cap64.as<double>(), ctx->res64.as<double>(), S.coef.as<real>());
+    NW_CUDA(ctx, cudaGetLastError());
     NW_CHECK(dev_alloc(ctx, S.ra_part, 8 * nn));
     NW_CUDA(ctx, cudaMemsetAsync(S.ra_part.ptr, 0, 8 * nn, ctx->stream));
     for (int64_t sg = nseg - 1; sg >= 0; --sg) {
@@ -445,18 +479,26 @@ static int adjoint_backward_impl(nw_ctx* ctx, double Ra, double* g_gna, double* 
         A.target = S.target.as<real>();
         A.lamV = S.lamV.as<real>(); A.lamV2 = S.lamV2.as<real>();
         A.lamM = S.lamM.as<real>(); A.lamH = S.lamH.as<real>(); A.lamN = S.lamN.as<real>();
-        A.gGna = S.gGna.as<double>(); A.gGk = S.gGk.as<double>(); A.gGl = S.gGl.as<double>();
+        A.gGna = S.gGna.as<real>(); A.gGk = S.gGk.as<real>(); A.gGl = S.gGl.as<real>();
+        A.inv_cap = S.coef.as<real>(); A.cap_r = A.inv_cap + n; A.inv_res = A.inv_cap + 2 * n;
         A.ra_part = S.ra_part.as<double>();
         A.inv_ra = 1.0 / Ra;
         NW_CHECK(launch_reverse(ctx, A));
     }
     NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * nseg, false));
-    std::vector<double> gna(n), gk(n), gl(n), rp(nn);
-    NW_CUDA(ctx, cudaMemcpyAsync(gna.data(), S.gGna.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
-    NW_CUDA(ctx, cudaMemcpyAsync(gk.data(), S.gGk.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
-    NW_CUDA(ctx, cudaMemcpyAsync(gl.data(), S.gGl.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<real> gsum[3] = {std::vector<real>(2 * n), std::vector<real>(2 * n), std::vector<real>(2 * n)};
+    std::vector<double> rp(nn);
+    DevBuf* gbuf[3] = {&S.gGna, &S.gGk, &S.gGl};
+    for (int k = 0; k < 3; ++k)
+        NW_CUDA(ctx, cudaMemcpyAsync(gsum[k].data(), gbuf[k]->ptr, 2 * b, cudaMemcpyDeviceToHost, ctx->stream));
     NW_CUDA(ctx, cudaMemcpyAsync(rp.data(), S.ra_part.ptr, 8 * nn, cudaMemcpyDeviceToHost, ctx->stream));
     NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<double> gna(n), gk(n), gl(n);
+    for (int64_t i = 0; i < n; ++i) {
+        gna[i] = (double)gsum[0][i] - (double)gsum[0][n + i];
+        gk[i] = (double)gsum[1][i] - (double)gsum[1][n + i];
+        gl[i] = (double)gsum[2][i] - (double)gsum[2][n + i];
+    }
     const std::vector<int64_t>& u2s = ctx->hh.user_to_sorted;
     for (int64_t u = 0; u < ctx->hh.m; ++u) {
         if (g_gna) g_gna[u] = gna[u2s[u]];

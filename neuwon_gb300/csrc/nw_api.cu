@@ -168,7 +168,7 @@ static void free_hh(HHState& hh) {
 
 static void free_adj(AdjointState& a) {
     for (DevBuf* b : {&a.ckpt, &a.target, &a.loss_part, &a.tape, &a.lamV, &a.lamV2, &a.lamM, &a.lamH, &a.lamN,
-                      &a.gGna, &a.gGk, &a.gGl, &a.ra_part})
+                      &a.gGna, &a.gGk, &a.gGl, &a.ra_part, &a.coef})
         dev_free(*b);
     a = AdjointState();
 }
@@ -1242,7 +1242,6 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     if (!ctx || !name) return NW_ERR_ARG;
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
-    if (nm == "l2_prefetch") { ctx->l2_prefetch = value != 0; return NW_OK; }
     if (nm == "cuda_graph") { ctx->use_graph = value != 0; return NW_OK; }
     if (nm == "spike_neurons" || nm == "spike_neuron_offset" || nm == "spike_ring_steps") {
         // Partitioned networks: taken by the next nw_synapses_set.
@@ -1340,7 +1339,6 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (!ctx || !name || !value) return NW_ERR_ARG;
     std::string nm(name);
     if (nm == "bulk_pipeline") { *value = ctx->use_bulk ? 1 : 0; return NW_OK; }
-    if (nm == "l2_prefetch") { *value = ctx->l2_prefetch ? 1 : 0; return NW_OK; }
     if (nm == "bulk_pipeline_active") { *value = uses_bulk_pipeline(ctx) ? 1 : 0; return NW_OK; }
     if (nm == "cuda_graph") { *value = ctx->use_graph ? 1 : 0; return NW_OK; }
     if (nm == "propagator_format") { *value = ctx->prop_format; return NW_OK; }

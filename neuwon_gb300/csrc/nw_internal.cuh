@@ -155,6 +155,7 @@ struct AdjointState {
     DevBuf ckpt, target, loss_part, tape;
     DevBuf lamV, lamV2, lamM, lamH, lamN;
     DevBuf gGna, gGk, gGl, ra_part;
+    DevBuf coef;                // 1/C, C and 1/R per segment in the state precision
 };
 
 }  // namespace nw
@@ -274,7 +275,6 @@ struct nw_ctx {
     int lanes_per_row = 0, threads = 1024, ctas_per_sm = 0;
     int fusion = 50;            // steps fused per launch (0: one launch per call)
     bool use_bulk = false;      // asynchronous bulk-copy pipeline (FP32 batched path)
-    bool l2_prefetch = true;    // fused pass: bulk L2 prefetch of the neuron's mechanism state
     bool use_graph = true;      // replay batched launch sequences as CUDA graphs
     nw::DevBuf dclock;          // nw::DevClock
     std::vector<nw::GraphEntry> graphs;

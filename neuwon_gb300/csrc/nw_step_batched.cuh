@@ -306,41 +306,6 @@ __device__ __forceinline__ bool fused_fast_form(const StepArgs<real>& a) {
     return a.n_kin == 0 || (a.n_kin == 1 && a.kin[0].S == 8 && a.kin[0].T == 2 && a.kin[0].ninp == 1);
 }
 
-// Lane `lane` of one warp asks L2 for one of the per-segment arrays the fused
-// pass of neuron [base, base + n) reads (kG, kI, the HH gates and coefficients,
-// the nonspecific current, each kinetic mechanism's coefficient and states), so
-// that the pass, which runs between two barriers while the CTA's stream is
-// idle, finds them in L2 instead of HBM.
-template <typename real>
-__device__ __forceinline__ void prefetch_fused_inputs(const StepArgs<real>& a, int64_t base, int n, int lane) {
-    const size_t bytes = (size_t)n * sizeof(real);
-    const real* p = nullptr;
-    if (lane < 2) p = lane == 0 ? a.kG : a.kI;
-    else if (lane < 8) {
-        if (a.hh_on) {
-            switch (lane) {
-                case 2: p = a.gm; break;
-                case 3: p = a.gh; break;
-                case 4: p = a.gn; break;
-                case 5: p = a.cna; break;
-                case 6: p = a.ck; break;
-                default: p = a.cl; break;
-            }
-        }
-    } else if (lane == 8) {
-        if (a.has_nonspec) p = a.Inonspec;
-    } else {
-        int k = lane - 9;
-        for (int q = 0; q < a.n_kin && !p; ++q) {
-            const KinArgs<real>& K = a.kin[q];
-            if (k == 0) p = K.gcoef;
-            else if (k <= K.S) p = K.state + (int64_t)(k - 1) * K.m;
-            k -= K.S + 1;
-        }
-    }
-    if (p) l2_prefetch(p + base, bytes);
-}
-
 // One segment of the fused mechanism pass (instances in segment order): the
 // mechanisms at the mid-step voltage v (rxd_model.py:115-123), the segment's
 // conductance and G*E (cached for the next step's first half when `keep`), and
@@ -540,8 +505,6 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                 const bool last = (s == a.k_steps - 1) && (half == 1);
                 // The propagator does not depend on x: start streaming it now.
                 if (BULK) bulk_prologue(a, ring, slice);
-                // The fused pass's inputs into L2 while the first half's rows stream.
-                if (fuse && half == 0 && a.l2_prefetch && tid < 32) prefetch_fused_inputs(a, base, n, tid);
                 // With fused mechanisms the second half's x comes from the mechanism
                 // pass, and later steps' first halves take G from the cache (the
                 // state it was computed from does not change in between).

@@ -147,8 +147,6 @@ struct StepArgs {
     // same launch; fuse_mech when every conductance source maps one-to-one onto
     // segments (HH and kinetic instances in segment order, no synapses or calcium).
     real* gc; int64_t gc_n; int fuse_mech;
-    // Fused pass: ask L2 for the neuron's mechanism state at the start of each step.
-    int l2_prefetch;
     // clamps (sorted by segment)
     const uint32_t* clamp_seg_ptr;
     const int32_t* clamp_neuron_ptr; const uint32_t* clamp_seg; const real* clamp_amp;
@@ -564,19 +562,6 @@ template <> struct Vec2Loader<double> {
     }
 };
 
-// Asks L2 for the whole 16-byte blocks of [p, p + bytes) ahead of their use
-// (cp.async.bulk.prefetch; no data moves to the SM, no completion to wait for).
-// The range is shrunk to 16-byte boundaries inside it, in pieces of at most 64 KB.
-__device__ __forceinline__ void l2_prefetch(const void* p, size_t bytes) {
-    uint64_t a = ((uint64_t)p + 15) & ~(uint64_t)15;
-    const uint64_t e = ((uint64_t)p + bytes) & ~(uint64_t)15;
-    while (a < e) {
-        const uint32_t len = (uint32_t)((e - a) < 65536 ? (e - a) : 65536);
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(a), "r"(len) : "memory");
-        a += len;
-    }
-}
-
 template <typename real>
 __device__ __forceinline__ void kahan_add(real& s, real& c, real term) {
     real y = term - c;
@@ -865,7 +850,6 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.ca_on = Ca.on ? 1 : 0;
     a.gc = ctx->gcache.as<real>(); a.gc_n = ctx->n_seg;
     a.fuse_mech = fuse_mechanisms(ctx) ? 1 : 0;
-    a.l2_prefetch = ctx->l2_prefetch ? 1 : 0;
     a.h_ms = (real)(0.5 * ctx->time_step);
     if (Ca.on) {
         a.ca_pump = Ca.pump ? 1 : 0; a.ca_nb = Ca.nb; a.ca_T = Ca.T;
