@@ -480,7 +480,7 @@ def diff_check(args, device):
     print(json.dumps(out), flush=True)
 
 
-def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
+def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000, threads=0):
     """Config 4 shape: 256 HH neurons of 2,000 segments, dt 0.025 ms, FP32, targets = FP64
     soma traces of the same neurons with densities drawn +-30 % around the defaults;
     gradients of the soma MSE w.r.t. per-segment gNa/gK/gL and Ra (checkpoint every 100)."""
@@ -491,6 +491,8 @@ def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
     k = neurons * size
     target = adjoint_target(trees, steps, device)
     m = adjoint_build(trees, "f32", device)
+    if threads:
+        m._ctx.call("nw_set_tuning", 0, threads, 0)
     m.reset_state()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -501,7 +503,7 @@ def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000):
     m.close()
     return {"ms_per_step": 1e3 * (t2 - t0) / steps, "forward_ms_per_step": 1e3 * (t1 - t0) / steps,
             "backward_ms_per_step": 1e3 * (t2 - t1) / steps, "steps": steps,
-            "checkpoint_every": checkpoint_every, "loss_mV2": loss,
+            "checkpoint_every": checkpoint_every, "threads": threads or "context default", "loss_mV2": loss,
             "grad_norm": float(np.sqrt((gna ** 2).sum() + (gk ** 2).sum() + (gl ** 2).sum())),
             "grad_ra": gra, "parameters": 3 * k + 1,
             "config": f"{neurons} HH neurons x {size} segments, dt 0.025 ms, FP32, propagator 1e-8 "
@@ -635,7 +637,8 @@ def run_leg(args, rank, local):
     import torch
     torch.cuda.set_device(local)
     if args.leg == "adjoint":
-        out = adjoint_leg(local, args.adjoint_steps, neurons=args.leg_neurons or 256, size=args.leg_size or 2000)
+        out = adjoint_leg(local, args.adjoint_steps, neurons=args.leg_neurons or 256, size=args.leg_size or 2000,
+                          threads=args.adjoint_threads)
     elif args.leg == "wide":
         variants = [tuple(int(x) for x in v.split(":")) for v in args.wide_variants.split(",")]
         out = wide_leg(local, args.study_segments, args.wide_tol, args.wide_steps, variants)
@@ -745,6 +748,7 @@ def main():
     ap.add_argument("--bulk", type=int, default=0, help="cp.async.bulk propagator stream (FP32)")
     ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu/adjoint legs")
     ap.add_argument("--adjoint-steps", type=int, default=800)
+    ap.add_argument("--adjoint-threads", type=int, default=0, help="threads per CTA of the adjoint kernels (0: default)")
     ap.add_argument("--network-steps", type=int, default=200,
                     help="steps of the 4,096-neuron, 2 M-synapse network leg (0 = skip)")
     ap.add_argument("--precision-study", action="store_true",
@@ -752,7 +756,7 @@ def main():
     ap.add_argument("--study-segments", type=int, default=1_000_000)
     ap.add_argument("--study-steps", type=int, default=20000)
     ap.add_argument("--study-current", type=float, default=10.0, help="soma clamp of the precision study (nA)")
-    ap.add_argument("--wide-fusion", type=int, default=1, choices=[0, 1],
+    ap.add_argument("--wide-fusion", type=int, default=0, choices=[0, 1],
                     help="precision study: one launch per half step (1) or one per phase (0)")
     ap.add_argument("--diff-check", action="store_true",
                     help="differentiation configuration: FP32/FP64 adjoint vs FP64 central differences (own JSON line)")

@@ -383,8 +383,10 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * batched path through shared memory with cp.async.bulk copies (needs lanes_per_row
  * 0 in nw_set_tuning); nw_get_option("bulk_pipeline_active") tells whether the next
  * batched launch will use it.
- * "wide_fusion" (default 1): the wide path runs one launch per half step when the
- * mechanisms map one-to-one onto segments.
+ * "wide_fusion" (default 0): the wide path runs one launch per half step when the
+ * mechanisms map one-to-one onto segments (each warp's 32 rows, then their segments'
+ * mechanisms and next x) instead of one launch per phase; on a GB300 the phase
+ * launches are faster from 2,000 to 1,000,000 segments (more rows in flight per SM).
  * nw_get_option also reports "wide_quads", "wide_entries" and
  * "calcium_wide_entries" (stored windows / entries of the wide path's voltage and
  * calcium propagators, once built). */

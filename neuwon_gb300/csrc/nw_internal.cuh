@@ -271,7 +271,7 @@ struct nw_ctx {
     nw::DevBuf status;          // i32 [1]
     nw::DevBuf plain_x;         // real [n_seg] scratch of the plain path (the wide path's x)
     nw::DevBuf wide_x2, wide_cs2;   // real [n_seg]: the fused wide path's second x / calcium scratch
-    bool wide_fusion = true;    // wide path: one launch per half step when mechanisms allow it
+    bool wide_fusion = false;   // wide path: one launch per half step when mechanisms allow it
     int lanes_per_row = 0, threads = 1024, ctas_per_sm = 0;
     int fusion = 50;            // steps fused per launch (0: one launch per call)
     bool use_bulk = false;      // asynchronous bulk-copy pipeline (FP32 batched path)

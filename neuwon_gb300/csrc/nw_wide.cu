@@ -33,29 +33,47 @@ wide_membrane_kernel(const StepArgs<real> a, const int s_off, const int half, co
             if (tick >= a.clamp_first[c] && tick < a.clamp_first[c] + a.clamp_count[c]) I += a.clamp_amp[c];
     }
     a.px[i] = membrane_x(a, i, G, GE, I, last != 0);
+    // species._advance (species.py:56-70), first part: c + dc/dt h into the scratch
+    // the calcium rows multiply (the same launch: independent of x).
+    if (a.ca_on) a.ca_scratch[i] = fmax(real(0), a.ca_c[i] + a.ca_dcdt[i] * a.h_ms);
 }
 
 // V_i = x_i - leak_i x_i + sum_j P_ij (x_j - x_i), LPR lanes per row, 4-entry
 // vectors with the evict-first hint, Kahan-compensated lane sums.
+// gt: the thread's index in the launch's part for these rows (LPR threads per row).
 template <typename real, int LPR>
-__global__ void __launch_bounds__(kWideThreads)
-wide_rows_kernel(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                 const real* __restrict__ val, const real* __restrict__ leak, const real* __restrict__ x,
-                 real* __restrict__ y, const int64_t n, int* status) {
-    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPR;
+__device__ __forceinline__ void rows_body(const int64_t gt, const int64_t* __restrict__ rowptr,
+                                          const int32_t* __restrict__ col, const real* __restrict__ val,
+                                          const real* __restrict__ leak, const real* __restrict__ x,
+                                          real* __restrict__ y, const int64_t n, int* status) {
+    const int64_t g = gt / LPR;
     const int l = threadIdx.x % LPR;
     const bool valid = g < n;
     real s = real(0), c = real(0), xi = real(0);
     if (valid) {
         xi = __ldg(x + g);
         const int64_t beg = rowptr[g], end = rowptr[g + 1];
-        for (int64_t k = beg + 4 * l; k < end; k += 4 * LPR) {
-            real v[4];
-            Vec4Loader<real>::load(val + k, v);
-            const int4 cc = __ldcs(reinterpret_cast<const int4*>(col + k));
-            const real p = v[0] * (__ldg(x + cc.x) - xi) + v[1] * (__ldg(x + cc.y) - xi);
-            const real q = v[2] * (__ldg(x + cc.z) - xi) + v[3] * (__ldg(x + cc.w) - xi);
-            kahan_add(s, c, p + q);
+        // Two 4-entry vectors per lane in flight.
+        for (int64_t k0 = beg + 4 * l; k0 < end; k0 += 8 * LPR) {
+            real v[2][4];
+            int4 cc[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int64_t k = k0 + 4 * LPR * u;
+                if (k < end) {
+                    Vec4Loader<real>::load(val + k, v[u]);
+                    cc[u] = __ldcs(reinterpret_cast<const int4*>(col + k));
+                } else {
+                    v[u][0] = v[u][1] = v[u][2] = v[u][3] = real(0);
+                    cc[u] = make_int4(g, g, g, g);     // zero weights on x_i
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const real p = v[u][0] * (__ldg(x + cc[u].x) - xi) + v[u][1] * (__ldg(x + cc[u].y) - xi);
+                const real q = v[u][2] * (__ldg(x + cc[u].z) - xi) + v[u][3] * (__ldg(x + cc[u].w) - xi);
+                kahan_add(s, c, p + q);
+            }
         }
     }
     real t = s - c;
@@ -68,26 +86,36 @@ wide_rows_kernel(const int64_t* __restrict__ rowptr, const int32_t* __restrict__
     }
 }
 
+template <typename real, int LPR>
+__global__ void __launch_bounds__(kWideThreads)
+wide_rows_kernel(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                 const real* __restrict__ val, const real* __restrict__ leak, const real* __restrict__ x,
+                 real* __restrict__ y, const int64_t n, int* status) {
+    rows_body<real, LPR>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, rowptr, col, val, leak, x, y, n, status);
+}
+
 // Quad format with global bases: each window's four x are consecutive in memory
 // (one or two cache sectors instead of four).
 template <typename real, int LPR>
-__global__ void __launch_bounds__(kWideThreads)
-wide_quads_kernel(const int64_t* __restrict__ qrow, const int32_t* __restrict__ qbase,
-                  const real* __restrict__ qval, const real* __restrict__ leak, const real* __restrict__ x,
-                  real* __restrict__ y, const int64_t n, int* status) {
-    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPR;
+__device__ __forceinline__ void quads_body(const int64_t gt, const int64_t* __restrict__ qrow,
+                                           const int32_t* __restrict__ qbase, const real* __restrict__ qval,
+                                           const real* __restrict__ leak, const real* __restrict__ x,
+                                           real* __restrict__ y, const int64_t n, int* status) {
+    const int64_t g = gt / LPR;
     const int l = threadIdx.x % LPR;
     const bool valid = g < n;
     real s = real(0), c = real(0), xi = real(0);
     if (valid) {
         xi = __ldg(x + g);
         const int64_t beg = qrow[g], end = qrow[g + 1];
-        // Two windows per lane in flight.
-        for (int64_t k0 = beg + l; k0 < end; k0 += 2 * LPR) {
-            real v[2][4];
-            int32_t b[2];
+        // Four FP32 windows per lane in flight (FP64: two; more only costs registers
+        // on that slower path).
+        constexpr int UNROLL = sizeof(real) == 4 ? 4 : 2;
+        for (int64_t k0 = beg + l; k0 < end; k0 += UNROLL * LPR) {
+            real v[UNROLL][4];
+            int32_t b[UNROLL];
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
+            for (int u = 0; u < UNROLL; ++u) {
                 const int64_t k = k0 + LPR * u;
                 if (k < end) {
                     Vec4Loader<real>::load(qval + 4 * k, v[u]);
@@ -98,7 +126,7 @@ wide_quads_kernel(const int64_t* __restrict__ qrow, const int32_t* __restrict__ 
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
+            for (int u = 0; u < UNROLL; ++u) {
                 const real* xb = x + b[u];
                 const real p = v[u][0] * (__ldg(xb) - xi) + v[u][1] * (__ldg(xb + 1) - xi);
                 const real q = v[u][2] * (__ldg(xb + 2) - xi) + v[u][3] * (__ldg(xb + 3) - xi);
@@ -114,6 +142,31 @@ wide_quads_kernel(const int64_t* __restrict__ qrow, const int32_t* __restrict__ 
         if (!isfinite(vnew)) atomicOr(status, kStatusNonFinite);
         y[g] = vnew;
     }
+}
+
+template <typename real, int LPR>
+__global__ void __launch_bounds__(kWideThreads)
+wide_quads_kernel(const int64_t* __restrict__ qrow, const int32_t* __restrict__ qbase,
+                  const real* __restrict__ qval, const real* __restrict__ leak, const real* __restrict__ x,
+                  real* __restrict__ y, const int64_t n, int* status) {
+    quads_body<real, LPR>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, qrow, qbase, qval, leak, x, y, n, status);
+}
+
+// The voltage rows (quad format, LPR lanes per row) and the calcium rows (row
+// format, 4 lanes per row) of one half step in one launch: blocks below
+// `vblocks` take voltage rows, the others calcium rows (the two read different x
+// and write different outputs).
+template <typename real, int LPR>
+__global__ void __launch_bounds__(kWideThreads)
+wide_quads_calcium_kernel(const StepArgs<real> a, const int64_t* __restrict__ qrow, const int32_t* __restrict__ qbase,
+                          const real* __restrict__ qval, const real* __restrict__ leak, const int64_t vblocks) {
+    const int64_t n = a.neuron_start[a.n_neuron];
+    if (blockIdx.x < vblocks)
+        quads_body<real, LPR>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, qrow, qbase, qval, leak, a.px, a.V, n,
+                              a.status);
+    else
+        rows_body<real, 4>((blockIdx.x - vblocks) * (int64_t)blockDim.x + threadIdx.x, a.ca_wrow, a.ca_wcol,
+                           a.ca_wval, a.ca_wleak, a.ca_scratch, a.ca_c, a.ca_n, a.status);
 }
 
 template <typename real>
@@ -139,14 +192,6 @@ wide_mechanism_kernel(const StepArgs<real> a, const int s_off, const int64_t n_h
     }
     k -= n_kin;
     if (k < n_syn) synapse_step(a, k, a.clk->steps + s_off);
-}
-
-template <typename real>
-__global__ void __launch_bounds__(kWideThreads)
-wide_calcium_prepare_kernel(const StepArgs<real> a) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= a.ca_n) return;
-    a.ca_scratch[i] = fmax(real(0), a.ca_c[i] + a.ca_dcdt[i] * a.h_ms);
 }
 
 template <typename real>
@@ -357,12 +402,25 @@ template <typename real>
 static int launch_quads(nw_ctx* ctx, const StepArgs<real>& a) {
     const int64_t n = ctx->n_seg;
     const double avg = n ? (double)ctx->nwq / (double)n : 0.0;
-    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg >= 48 ? 16 : avg >= 12 ? 8 : 4);
+    // About 2-4 windows per lane: one round of the kernel's four loads per row.
+    const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg > 32 ? 16 : avg > 12 ? 8 : 4);
     const unsigned blocks = (unsigned)((n * lanes + kWideThreads - 1) / kWideThreads);
     const int64_t* R = ctx->wq_rowptr.as<int64_t>();
     const int32_t* B = ctx->wq_base.as<int32_t>();
     const real* V = ctx->wq_val.as<real>();
     const real* L = ctx->w_leak.as<real>();
+    if (a.ca_on) {
+        // The calcium rows in the same launch (4 lanes per row, blocks after the voltage rows').
+        const unsigned cb = (unsigned)((a.ca_n * 4 + kWideThreads - 1) / kWideThreads);
+        switch (lanes) {
+            case 4: wide_quads_calcium_kernel<real, 4><<<blocks + cb, kWideThreads, 0, ctx->stream>>>(a, R, B, V, L, blocks); break;
+            case 8: wide_quads_calcium_kernel<real, 8><<<blocks + cb, kWideThreads, 0, ctx->stream>>>(a, R, B, V, L, blocks); break;
+            case 16: wide_quads_calcium_kernel<real, 16><<<blocks + cb, kWideThreads, 0, ctx->stream>>>(a, R, B, V, L, blocks); break;
+            default: wide_quads_calcium_kernel<real, 32><<<blocks + cb, kWideThreads, 0, ctx->stream>>>(a, R, B, V, L, blocks); break;
+        }
+        NW_CUDA(ctx, cudaGetLastError());
+        return NW_OK;
+    }
     switch (lanes) {
         case 4: wide_quads_kernel<real, 4><<<blocks, kWideThreads, 0, ctx->stream>>>(R, B, V, L, a.px, a.V, n, a.status); break;
         case 8: wide_quads_kernel<real, 8><<<blocks, kWideThreads, 0, ctx->stream>>>(R, B, V, L, a.px, a.V, n, a.status); break;
@@ -403,12 +461,8 @@ static int enqueue_wide_fused(nw_ctx* ctx, const StepArgs<real>& a, int steps) {
     real* x1 = ctx->wide_x2.as<real>();
     real* c0 = a.ca_scratch;
     real* c1 = ctx->wide_cs2.as<real>();
-    wide_membrane_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a, 0, 0, 0);
+    wide_membrane_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a, 0, 0, 0);   // x and calcium scratch
     NW_CUDA(ctx, cudaGetLastError());
-    if (a.ca_on) {
-        wide_calcium_prepare_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
-        NW_CUDA(ctx, cudaGetLastError());
-    }
     for (int s = 0; s < steps; ++s) {
         const int last = s == steps - 1 ? 1 : 0;
         for (int phase = 0; phase < 2; ++phase) {
@@ -439,16 +493,14 @@ static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lan
     for (int s = 0; s < steps; ++s) {
         for (int half = 0; half < 2; ++half) {
             const int last = (s == steps - 1 && half == 1) ? 1 : 0;
+            // x of every segment and, with calcium, its scratch c + dc/dt h.
             wide_membrane_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a, s, half, last);
             NW_CUDA(ctx, cudaGetLastError());
-            if (ctx->prop_format == 2 && ctx->wq_ok) NW_CHECK(launch_quads<real>(ctx, a));
+            if (ctx->prop_format == 2 && ctx->wq_ok) NW_CHECK(launch_quads<real>(ctx, a));   // + calcium rows
             else NW_CHECK(launch_rows<real>(ctx, lanes, a.wrow, a.wcol, a.wval, a.wleak, a.px, a.V, a.status));
-            if (a.ca_on) {
-                wide_calcium_prepare_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
-                NW_CUDA(ctx, cudaGetLastError());
+            if (a.ca_on && !(ctx->prop_format == 2 && ctx->wq_ok))
                 NW_CHECK(launch_rows<real>(ctx, 4, a.ca_wrow, a.ca_wcol, a.ca_wval, a.ca_wleak, a.ca_scratch, a.ca_c,
                                            a.status));
-            }
             if (half == 0 && n_mech > 0) {
                 wide_mechanism_kernel<real><<<(unsigned)((n_mech + kWideThreads - 1) / kWideThreads), kWideThreads, 0,
                                               ctx->stream>>>(a, s, n_hh, n_kin, n_syn);
