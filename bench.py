@@ -567,7 +567,7 @@ def wide_bytes_per_segment_step(windows_per_row, ca_entries_per_row, calcium=Tru
     return step
 
 
-def wide_leg(device, segments, tol, steps, variants=((1, 0),)):
+def wide_leg(device, segments, tol, steps, variants=((0, 0),)):
     """The precision configuration's step on the wide path, timed: one seeded tree
     (same length and diameter laws), HH + calcium (diffusion, pump, Na influx),
     FP32, dt 0.025 ms, propagators pruned at `tol` (charge/mass-conserving), 10 nA
@@ -764,7 +764,7 @@ def main():
     ap.add_argument("--diff-neurons", type=int, default=256)
     ap.add_argument("--wide-tol", type=float, default=1e-9, help="propagator tolerance of the wide leg")
     ap.add_argument("--wide-steps", type=int, default=320, help="timed steps of the wide leg")
-    ap.add_argument("--wide-variants", default="1:0",
+    ap.add_argument("--wide-variants", default="0:0",
                     help="wide leg: comma-separated wide_fusion:lanes_per_row (0 = by row length)")
     ap.add_argument("--leg", choices=["adjoint", "network", "plain", "wide"],
                     help="run one side leg alone and print its JSON line (a small case with --leg-neurons, "
@@ -838,6 +838,9 @@ def main():
     if not args.quick and rank == 0 and args.network_steps > 0:
         extra["network"] = network_leg(local, args.network_steps)
         log(f"network: {extra['network']}")
+    if not args.quick and rank == 0 and args.wide_steps > 0:
+        extra["wide"] = wide_leg(local, args.study_segments, args.wide_tol, args.wide_steps)
+        log(f"wide: {extra['wide']}")
     t_build = time.perf_counter()
     model, neurons = build_model(trees, currents, precision="f32", tolerance=args.tol, conserve=True,
                                  device=local, fmt=args.format, lump=bool(args.lump))
