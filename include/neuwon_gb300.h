@@ -298,6 +298,18 @@ int nw_advance(nw_ctx* ctx, int32_t k_steps, int path);
 int nw_advance_host(nw_ctx* ctx, int32_t k_steps, const double* stim_amps,
                     void* v_out, int v_dtype);
 
+/* The same step without waiting for it: the voltages are copied on the device into
+ * one of two staging buffers, then to v_out on a second stream while the next call's
+ * step runs, so a loop of calls keeps the GPU busy.  Returns after enqueueing.
+ * stim_amps and v_out must stay valid and unmodified until nw_synchronize() (which
+ * waits for both streams) has returned; give each call in flight its own v_out
+ * (alternating two buffers is enough when the caller synchronises every two calls, or
+ * once at the end).  Pinned host memory makes the copies asynchronous.  v_dtype must
+ * be the context precision.  A non-finite voltage is reported by the next nw_advance
+ * or nw_advance_host call. */
+int nw_advance_host_async(nw_ctx* ctx, int32_t k_steps, const double* stim_amps,
+                          void* v_out, int v_dtype);
+
 /* Simulation clock (rxd_model.py:22-23): completed steps and input ticks. */
 int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks);
 

@@ -22,7 +22,7 @@ EXPORTS = [
     "nw_version", "nw_ctx_create", "nw_ctx_destroy", "nw_last_error", "nw_get_stream",
     "nw_synchronize", "nw_model_init", "nw_set_data", "nw_get_data", "nw_propagator_build",
     "nw_propagator_set_csr", "nw_propagator_get_csr", "nw_hh_register", "nw_clamps_set",
-    "nw_detectors_set", "nw_probes_set", "nw_probes_read", "nw_advance", "nw_advance_host",
+    "nw_detectors_set", "nw_probes_set", "nw_probes_read", "nw_advance", "nw_advance_host", "nw_advance_host_async",
     "nw_get_clock", "nw_set_tuning", "nw_get_tuning", "nw_propagator_stats", "nw_propagator_conserve",
     "nw_kinetic_register", "nw_set_option", "nw_get_option", "nw_electric_half_step_noalloc",
     "nw_adjoint_forward", "nw_adjoint_backward", "nw_autotune", "nw_synapses_set",
@@ -81,6 +81,7 @@ def load(build_if_missing=True):
         "nw_probes_read": ([c_void_p, c_void_p, c_int, c_i64, P(c_i64)], c_int),
         "nw_advance": ([c_void_p, ctypes.c_int32, c_int], c_int),
         "nw_advance_host": ([c_void_p, ctypes.c_int32, c_void_p, c_void_p, c_int], c_int),
+        "nw_advance_host_async": ([c_void_p, ctypes.c_int32, c_void_p, c_void_p, c_int], c_int),
         "nw_get_clock": ([c_void_p, P(c_i64), P(c_i64)], c_int),
         "nw_set_tuning": ([c_void_p, c_int, c_int, c_int], c_int),
         "nw_set_option": ([c_void_p, ctypes.c_char_p, c_i64], c_int),

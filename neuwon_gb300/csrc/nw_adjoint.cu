@@ -67,8 +67,10 @@ __device__ __forceinline__ real* tape_slot(const AdjArgs<real>& A, int s, int sl
 
 // Forward steps of one neuron per CTA (HH, one instance per segment), with an
 // optional tape and the loss; the arithmetic is that of the batched path.
+// Bounds (1024, 1): one CTA per SM, so ptxas may use all 64 registers a thread
+// can have (with the thread bound alone it chose 32 and spilled).
 template <typename real, int LPR>
-__global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<real> A) {
+__global__ void __launch_bounds__(1024, 1) adjoint_forward_kernel(const AdjArgs<real> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     real* xs = reinterpret_cast<real*>(smem_raw);
     __shared__ int s_job;
@@ -201,12 +203,23 @@ __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_
         xs[li] = lam_out[i] * A.inv_cap[i];
     }
     __syncthreads();
-    propagate_rows<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real nu) {
-        const real lx = nu * A.cap_r[r];
-        if (!gv) {                       // G = 0: x = V, no parameter dependence
-            lam_in[r] = lx;
-            return;
+    // The rows leave lambda of x (C P^T applied) in lam_in; the membrane update's
+    // adjoint follows per segment below, with every lane of the CTA.
+    propagate_rows<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real nu) { lam_in[r] = nu * A.cap_r[r]; });
+    // xs still holds lambda / C of every segment of the neuron (the rows only read it).
+    for (int li = tid; li < n; li += nthr) {
+        const int64_t i = base + li;
+        const int64_t p = A.parent[i];
+        if (p >= 0) {
+            const real flow = (V_out[p] - V_out[i]) * A.inv_res[i];
+            kahan_add(ra_s, ra_c, flow * (xs[li] - xs[p - base]));
         }
+    }
+    __syncthreads();
+    if (!gv) return;                     // G = 0: x = V, no parameter dependence
+    for (int li = tid; li < n; li += nthr) {
+        const int64_t r = base + li;
+        const real lx = lam_in[r];
         const real m = gm[r], h = gh[r], nn = gn[r];
         const real M = m * m * m * h, N4 = nn * nn * nn * nn;
         const real gna = a.cna[r] * M, gk = a.ck[r] * N4, gl = a.cl[r];
@@ -233,15 +246,6 @@ __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_
         A.lamM[r] += lM * real(3) * m * m * h;
         A.lamH[r] += lM * m * m * m;
         A.lamN[r] += lN4 * real(4) * nn * nn * nn;
-    });
-    // xs still holds lambda / C of every segment of the neuron (the rows only read it).
-    for (int li = tid; li < n; li += nthr) {
-        const int64_t i = base + li;
-        const int64_t p = A.parent[i];
-        if (p >= 0) {
-            const real flow = (V_out[p] - V_out[i]) * A.inv_res[i];
-            kahan_add(ra_s, ra_c, flow * (xs[li] - xs[p - base]));
-        }
     }
     __syncthreads();
 }
@@ -280,15 +284,15 @@ __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<rea
                 const int64_t i = base + li;
                 const real v = tape_slot(A, s, 1)[i];
                 const real m0 = tape_slot(A, s, 2)[i], h0 = tape_slot(A, s, 3)[i], n0 = tape_slot(A, s, 4)[i];
-                Dual<real> dv(v, real(1)), dm(m0), dh(h0), dn(n0), dq(a.dtq10);
-                hh_gates(dv, dq, dm, dh, dn);                 // d gates(s+1) / d V_mid
-                Dual<real> ev(v), em(m0, real(1)), eh(h0, real(1)), en(n0, real(1));
-                hh_gates(ev, dq, em, eh, en);                 // d gate(s+1) / d gate(s)
+                // d gates(s+1) / d V_mid in the dual parts; d gate(s+1) / d gate(s) is
+                // each gate's decay factor exp(-dt/xtau), the value parts of em, eh, en.
+                Dual<real> dv(v, real(1)), dm(m0), dh(h0), dn(n0), dq(a.dtq10), em, eh, en;
+                hh_gates_decay(dv, dq, dm, dh, dn, em, eh, en);
                 const real lm = A.lamM[i], lh = A.lamH[i], ln = A.lamN[i];
                 A.lamV2[i] += dm.d * lm + dh.d * lh + dn.d * ln;
-                A.lamM[i] = em.d * lm;
-                A.lamH[i] = eh.d * lh;
-                A.lamN[i] = en.d * ln;
+                A.lamM[i] = em.v * lm;
+                A.lamH[i] = eh.v * lh;
+                A.lamN[i] = en.v * ln;
             }
             __syncthreads();
             // First half step: V(s), gates(s) -> V_mid.

@@ -292,8 +292,14 @@ int nw_ctx_destroy(nw_ctx* ctx) {
                       &ctx->probe_neuron_ptr, &ctx->probe_slot, &ctx->trace, &ctx->neuron_order,
                       &ctx->work_counter, &ctx->status, &ctx->plain_x, &ctx->dclock,
                       &ctx->clamp_seg_ptr, &ctx->w_rowptr, &ctx->w_col, &ctx->w_val, &ctx->w_leak,
-                      &ctx->wide_x2, &ctx->wide_cs2};
+                      &ctx->wide_x2, &ctx->wide_cs2, &ctx->vstage[0], &ctx->vstage[1]};
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     for (DevBuf* b : bufs) dev_free(*b);
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->stage_ready[k]) cudaEventDestroy(ctx->stage_ready[k]);
+        if (ctx->stage_done[k]) cudaEventDestroy(ctx->stage_done[k]);
+    }
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return NW_OK;
@@ -316,6 +322,7 @@ int nw_get_stream(nw_ctx* ctx, void** stream) {
 int nw_synchronize(nw_ctx* ctx) {
     if (!ctx) return NW_ERR_ARG;
     NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->copy_stream) NW_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
     return NW_OK;
 }
 
@@ -1216,6 +1223,52 @@ int nw_advance_host(nw_ctx* ctx, int32_t k_steps, const double* stim_amps, void*
         }
     }
     return read_status(ctx);
+}
+
+int nw_advance_host_async(nw_ctx* ctx, int32_t k_steps, const double* stim_amps, void* v_out, int v_dtype) {
+    if (!ctx) return NW_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (v_out && v_dtype != real_dtype(ctx))
+        return fail(ctx, NW_ERR_ARG, "nw_advance_host_async: v_dtype must be the context precision");
+    NW_CHECK(check_ready(ctx, k_steps));
+    if (stim_amps && ctx->n_clamps) {
+        size_t half = ctx->clamp_amp_stage.bytes / 2;
+        const int64_t* s2u = (const int64_t*)((char*)ctx->clamp_amp_stage.ptr + half);
+        NW_CUDA(ctx, cudaMemcpyAsync(ctx->clamp_amp_stage.ptr, stim_amps, 8 * ctx->n_clamps,
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        int threads = 256;
+        int64_t blocks = (ctx->n_clamps + threads - 1) / threads;
+        if (ctx->precision == NW_F64)
+            stage_clamp_amps<double><<<blocks, threads, 0, ctx->stream>>>(
+                ctx->clamp_amp_stage.as<double>(), s2u, ctx->clamp_amp.as<double>(), ctx->n_clamps);
+        else
+            stage_clamp_amps<float><<<blocks, threads, 0, ctx->stream>>>(
+                ctx->clamp_amp_stage.as<double>(), s2u, ctx->clamp_amp.as<float>(), ctx->n_clamps);
+        NW_CUDA(ctx, cudaGetLastError());
+    }
+    if (k_steps) NW_CHECK(advance_batched(ctx, k_steps));
+    if (v_out) {
+        if (!ctx->copy_stream) {
+            NW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+            for (int k = 0; k < 2; ++k) {
+                NW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->stage_ready[k], cudaEventDisableTiming));
+                NW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->stage_done[k], cudaEventDisableTiming));
+            }
+        }
+        const size_t bytes = (size_t)ctx->precision * ctx->n_seg;
+        const int b = ctx->stage_slot;
+        ctx->stage_slot ^= 1;
+        // The slot's previous copy to the host must be done before it is overwritten.
+        if (ctx->stage_pending[b]) NW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->stage_done[b], 0));
+        NW_CHECK(dev_alloc(ctx, ctx->vstage[b], bytes));
+        NW_CUDA(ctx, cudaMemcpyAsync(ctx->vstage[b].ptr, ctx->V.ptr, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        NW_CUDA(ctx, cudaEventRecord(ctx->stage_ready[b], ctx->stream));
+        NW_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->stage_ready[b], 0));
+        NW_CUDA(ctx, cudaMemcpyAsync(v_out, ctx->vstage[b].ptr, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream));
+        NW_CUDA(ctx, cudaEventRecord(ctx->stage_done[b], ctx->copy_stream));
+        ctx->stage_pending[b] = true;
+    }
+    return NW_OK;
 }
 
 int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks) {

@@ -167,6 +167,13 @@ struct nw_ctx {
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
     std::string err;
+    // nw_advance_host_async: voltages staged on the device (two slots) and copied to
+    // the host on a second stream while the next step runs.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t stage_ready[2] = {nullptr, nullptr}, stage_done[2] = {nullptr, nullptr};
+    nw::DevBuf vstage[2];
+    bool stage_pending[2] = {false, false};
+    int stage_slot = 0;
 
     // Topology.
     int64_t n_seg = 0, n_neuron = 0, max_neuron = 0;

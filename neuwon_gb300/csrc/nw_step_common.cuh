@@ -58,20 +58,32 @@ __device__ __forceinline__ real vtrap(real x, real y) {
 // rates(v) and the exact gate update x <- xinf + (x - xinf) exp(-dt/xtau)
 // (hh.mod:55-86, nmodl/solver.py:48-55); dtq10 = dt * q10, so
 // dt/xtau = dtq10 * (alpha + beta).
+// Also returns each gate's decay factor exp(-dt/xtau), which is d gate_new /
+// d gate_old (the adjoint's Jacobian).
 template <typename real>
-__device__ __forceinline__ void hh_gates(real v, real dtq10, real& m, real& h, real& n) {
+__device__ __forceinline__ void hh_gates_decay(real v, real dtq10, real& m, real& h, real& n, real& em, real& eh,
+                                               real& en) {
     real a = real(0.1) * vtrap(-(v + real(40)), real(10));
     real b = real(4) * d_exp(-(v + real(65)) / real(18));
     real s = a + b, inf = a / s;
-    m = inf + (m - inf) * d_exp(-dtq10 * s);
+    em = d_exp(-dtq10 * s);
+    m = inf + (m - inf) * em;
     a = real(0.07) * d_exp(-(v + real(65)) / real(20));
     b = real(1) / (d_exp(-(v + real(35)) / real(10)) + real(1));
     s = a + b; inf = a / s;
-    h = inf + (h - inf) * d_exp(-dtq10 * s);
+    eh = d_exp(-dtq10 * s);
+    h = inf + (h - inf) * eh;
     a = real(0.01) * vtrap(-(v + real(55)), real(10));
     b = real(0.125) * d_exp(-(v + real(65)) / real(80));
     s = a + b; inf = a / s;
-    n = inf + (n - inf) * d_exp(-dtq10 * s);
+    en = d_exp(-dtq10 * s);
+    n = inf + (n - inf) * en;
+}
+
+template <typename real>
+__device__ __forceinline__ void hh_gates(real v, real dtq10, real& m, real& h, real& n) {
+    real em, eh, en;
+    hh_gates_decay(v, dtq10, m, h, n, em, eh, en);
 }
 
 // One kinetic mechanism (lti_sim scheme) as the step kernels see it.
