@@ -67,10 +67,8 @@ __device__ __forceinline__ real* tape_slot(const AdjArgs<real>& A, int s, int sl
 
 // Forward steps of one neuron per CTA (HH, one instance per segment), with an
 // optional tape and the loss; the arithmetic is that of the batched path.
-// Bounds (1024, 1): one CTA per SM, so ptxas may use all 64 registers a thread
-// can have (with the thread bound alone it chose 32 and spilled).
 template <typename real, int LPR>
-__global__ void __launch_bounds__(1024, 1) adjoint_forward_kernel(const AdjArgs<real> A) {
+__global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<real> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     real* xs = reinterpret_cast<real*>(smem_raw);
     __shared__ int s_job;
