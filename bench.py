@@ -550,14 +550,14 @@ def network_leg(device, steps, neurons=4096, synapses=2_000_000):
 
 
 def wide_bytes_per_segment_step(windows_per_row, ca_entries_per_row, calcium=True, prec=4):
-    """Compulsory HBM bytes of one step of the fused wide path per segment (FP32):
-    per half step the voltage propagator's quad windows (16 B of values and a 4 B
-    base each), its row pointer (8 B) and leak, x read and the next x and V written;
-    with calcium the same for its propagator (entries in 4-entry vectors of 4 B
-    values and 4 B columns), scratch read and written and c written; per step the
-    HH gates (read and written), their conductance coefficients and kG, kI, and
-    with calcium the pump states (read and written), dc/dt and the influx and
-    efflux coefficients."""
+    """Compulsory HBM bytes of one step of the wide path per segment (FP32): per
+    half step the voltage propagator's quad windows (16 B of values and a 4 B base
+    each), its row pointer (8 B) and leak, x read, kG and kI read, the next x and V
+    written; with calcium the same for its propagator (entries in 4-entry vectors of
+    4 B values and 4 B columns), scratch read and written and c written; per step
+    the HH gates (read and written) and their conductance coefficients, and with
+    calcium the pump states (read and written), dc/dt and the influx and efflux
+    coefficients."""
     half = 20 * windows_per_row + 8 + prec + 3 * prec + 2 * prec
     if calcium:
         half += 2 * prec * ca_entries_per_row + 8 + prec + 3 * prec

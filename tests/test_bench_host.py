@@ -40,3 +40,17 @@ def test_default_configuration_has_an_ncu_traffic_figure():
 def test_both_arms_name_the_same_workload():
     name = bench.workload_name(1024, 500, 20000)
     assert name.startswith("batched: 1024 neurons, log-uniform 500-20000 segments")
+
+
+def test_wide_bytes_count_windows_rows_and_state():
+    # Per half step: 20 B per quad window (16 B values + 4 B base), row pointer (8 B)
+    # and leak, x, kG and kI read, next x and V written; with calcium 8 B per stored
+    # entry, its row pointer and leak, scratch read, c and next scratch written; per
+    # step the HH gates (read and written) with their 3 coefficients, and the calcium
+    # pump's 3 states (read and written), dc/dt and the influx and efflux coefficients.
+    no_ca = bench.wide_bytes_per_segment_step(0.0, 0.0, calcium=False)
+    assert no_ca == 2 * (8 + 4 + 12 + 8) + 2 * 12 + 12
+    assert bench.wide_bytes_per_segment_step(10.0, 0.0, calcium=False) - no_ca == 2 * 10 * 20
+    ca = bench.wide_bytes_per_segment_step(0.0, 0.0)
+    assert ca - no_ca == 2 * (8 + 4 + 12) + 2 * 12 + 12
+    assert bench.wide_bytes_per_segment_step(0.0, 5.0) - ca == 2 * 5 * 8
