@@ -63,7 +63,7 @@ class KineticScheme:
     def steady_state(self, v, celsius):
         """State after an hour at voltage v from equal occupancies summing to the
         conserve sum, through the column-renormalised propagator
-        (LTI_Model.get_initial_state, neuwon/rxd/lti_sim/lti_model.py:67-79)."""
+        (LTI_Model.get_initial_state, neuwon/rxd/lti_sim/lti_model.py:67-78)."""
         M = scipy.linalg.expm(self.matrix([v], celsius)[0] * 3600e3)
         M = M / M.sum(axis=0, keepdims=True)
         s = M @ np.full(self.num_states, (self.conserve_sum or 1.0) / self.num_states)

@@ -45,7 +45,7 @@ def test_oracle_species_matches_reference():
 def test_library_channel_tables_match_reference_lti_sim(factory, key):
     """This package's table builder, given the reference's sample points, equals the
     reference's Approx1D table (approx.py:159-174); the initial state equals
-    LTI_Model.get_initial_state (lti_model.py:67-79)."""
+    LTI_Model.get_initial_state (lti_model.py:67-78)."""
     spec_meta = F["species_meta"]
     dt, celsius, v_init = spec_meta[0], spec_meta[1], spec_meta[3]
     sch = factory()
