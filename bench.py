@@ -521,7 +521,7 @@ def network_leg(device, steps, neurons=4096, synapses=2_000_000):
     trees = batched_trees(neurons, seed=7, processes=min(16, os.cpu_count() or 1), lo=200, hi=5000)
     currents = batched_currents(neurons, seed=7)
     m, _ = build_model(trees, currents, precision="f32", tolerance=1e-8, conserve=True, device=device,
-                       kinetic=False)
+                       kinetic=False, fmt="quads")
     net = random_network([len(t) for t in trees], synapses, 7)
     offs = np.cumsum([0] + [len(t) for t in trees])[:-1]
     m.add_synapses(net["pre"], offs[net["post_neuron"]] + net["post_local"], net["weight_nS"], net["weight_nS"],
@@ -544,7 +544,7 @@ def network_leg(device, steps, neurons=4096, synapses=2_000_000):
            "spikes": int(m.get_data("Neuron.spike_count").sum()) - sp0,
            "fusion_depth": min(tuned["fusion_depth"], int(net["delay_steps"].min())), "autotune": tuned,
            "config": f"{neurons} HH neurons, log-uniform 200-5000 segments, {synapses} AMPA+NMDA synapses, "
-                     "delays U(1, 20) ms, FP32, dt 0.1 ms, propagator 1e-8 (charge-conserving)"}
+                     "delays U(1, 20) ms, FP32, dt 0.1 ms, propagator 1e-8 (charge-conserving), quad format"}
     m.close()
     return out
 

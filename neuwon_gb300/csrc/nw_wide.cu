@@ -95,33 +95,22 @@ wide_rows_kernel(const int64_t* __restrict__ rowptr, const int32_t* __restrict__
 }
 
 // Quad format with global bases: each window's four x are consecutive in memory
-// (one or two cache sectors instead of four).  Grid-stride over row groups: gt is
-// the thread's index in the launch's part of `threads` threads (a multiple of 32);
-// a warp takes GPW rows at a time, every threads / LPR rows, and loads the next
-// rows' pointers and x_i before its current rows' windows, so each row's windows
-// follow its pointers without waiting on them.
+// (one or two cache sectors instead of four).
 template <typename real, int LPR>
-__device__ __forceinline__ void quads_body(const int64_t gt, const int64_t threads, const int64_t* __restrict__ qrow,
+__device__ __forceinline__ void quads_body(const int64_t gt, const int64_t* __restrict__ qrow,
                                            const int32_t* __restrict__ qbase, const real* __restrict__ qval,
                                            const real* __restrict__ leak, const real* __restrict__ x,
                                            real* __restrict__ y, const int64_t n, int* status) {
-    constexpr int GPW = 32 / LPR;
-    // Four FP32 windows per lane in flight (FP64: two; more only costs registers on
-    // that slower path).
-    constexpr int UNROLL = sizeof(real) == 4 ? 4 : 2;
-    const int lane = threadIdx.x & 31, q = lane / LPR, l = lane % LPR;
-    const int64_t stride = threads / LPR;
-    const int64_t wrow0 = (gt >> 5) * GPW;
-    int64_t g = wrow0 + q;
-    int64_t beg = 0, end = 0;
-    real xi = real(0);
-    if (g < n) { beg = qrow[g]; end = qrow[g + 1]; xi = __ldg(x + g); }
-    for (int64_t r0 = wrow0; r0 < n; r0 += stride) {   // uniform in the warp
-        const int64_t gn = g + stride;
-        int64_t begn = 0, endn = 0;
-        real xin = real(0);
-        if (gn < n) { begn = qrow[gn]; endn = qrow[gn + 1]; xin = __ldg(x + gn); }
-        real s = real(0), c = real(0);
+    const int64_t g = gt / LPR;
+    const int l = threadIdx.x % LPR;
+    const bool valid = g < n;
+    real s = real(0), c = real(0), xi = real(0);
+    if (valid) {
+        xi = __ldg(x + g);
+        const int64_t beg = qrow[g], end = qrow[g + 1];
+        // Four FP32 windows per lane in flight (FP64: two; more only costs registers
+        // on that slower path).
+        constexpr int UNROLL = sizeof(real) == 4 ? 4 : 2;
         for (int64_t k0 = beg + l; k0 < end; k0 += UNROLL * LPR) {
             real v[UNROLL][4];
             int32_t b[UNROLL];
@@ -140,19 +129,18 @@ __device__ __forceinline__ void quads_body(const int64_t gt, const int64_t threa
             for (int u = 0; u < UNROLL; ++u) {
                 const real* xb = x + b[u];
                 const real p = v[u][0] * (__ldg(xb) - xi) + v[u][1] * (__ldg(xb + 1) - xi);
-                const real qq = v[u][2] * (__ldg(xb + 2) - xi) + v[u][3] * (__ldg(xb + 3) - xi);
-                kahan_add(s, c, p + qq);
+                const real q = v[u][2] * (__ldg(xb + 2) - xi) + v[u][3] * (__ldg(xb + 3) - xi);
+                kahan_add(s, c, p + q);
             }
         }
-        real t = s - c;
+    }
+    real t = s - c;
 #pragma unroll
-        for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off, LPR);
-        if (g < n && l == 0) {
-            const real vnew = (xi - leak[g] * xi) + t;
-            if (!isfinite(vnew)) atomicOr(status, kStatusNonFinite);
-            y[g] = vnew;
-        }
-        g = gn; beg = begn; end = endn; xi = xin;
+    for (int off = LPR / 2; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off, LPR);
+    if (valid && l == 0) {
+        const real vnew = (xi - leak[g] * xi) + t;
+        if (!isfinite(vnew)) atomicOr(status, kStatusNonFinite);
+        y[g] = vnew;
     }
 }
 
@@ -161,8 +149,7 @@ __global__ void __launch_bounds__(kWideThreads)
 wide_quads_kernel(const int64_t* __restrict__ qrow, const int32_t* __restrict__ qbase,
                   const real* __restrict__ qval, const real* __restrict__ leak, const real* __restrict__ x,
                   real* __restrict__ y, const int64_t n, int* status) {
-    quads_body<real, LPR>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x, qrow,
-                          qbase, qval, leak, x, y, n, status);
+    quads_body<real, LPR>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, qrow, qbase, qval, leak, x, y, n, status);
 }
 
 // The voltage rows (quad format, LPR lanes per row) and the calcium rows (row
@@ -175,8 +162,8 @@ wide_quads_calcium_kernel(const StepArgs<real> a, const int64_t* __restrict__ qr
                           const real* __restrict__ qval, const real* __restrict__ leak, const int64_t vblocks) {
     const int64_t n = a.neuron_start[a.n_neuron];
     if (blockIdx.x < vblocks)
-        quads_body<real, LPR>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, vblocks * blockDim.x, qrow, qbase, qval,
-                              leak, a.px, a.V, n, a.status);
+        quads_body<real, LPR>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, qrow, qbase, qval, leak, a.px, a.V, n,
+                              a.status);
     else
         rows_body<real, 4>((blockIdx.x - vblocks) * (int64_t)blockDim.x + threadIdx.x, a.ca_wrow, a.ca_wcol,
                            a.ca_wval, a.ca_wleak, a.ca_scratch, a.ca_c, a.ca_n, a.status);
@@ -417,19 +404,7 @@ static int launch_quads(nw_ctx* ctx, const StepArgs<real>& a) {
     const double avg = n ? (double)ctx->nwq / (double)n : 0.0;
     // About 2-4 windows per lane: one round of the kernel's four loads per row.
     const int lanes = ctx->lanes_per_row ? ctx->lanes_per_row : (avg > 32 ? 16 : avg > 12 ? 8 : 4);
-    // Row groups are taken grid-stride by one wave of blocks (as many per SM as fit),
-    // several rows per warp.
-    const void* kern = nullptr;
-    switch (lanes) {
-        case 4: kern = a.ca_on ? (const void*)wide_quads_calcium_kernel<real, 4> : (const void*)wide_quads_kernel<real, 4>; break;
-        case 8: kern = a.ca_on ? (const void*)wide_quads_calcium_kernel<real, 8> : (const void*)wide_quads_kernel<real, 8>; break;
-        case 16: kern = a.ca_on ? (const void*)wide_quads_calcium_kernel<real, 16> : (const void*)wide_quads_kernel<real, 16>; break;
-        default: kern = a.ca_on ? (const void*)wide_quads_calcium_kernel<real, 32> : (const void*)wide_quads_kernel<real, 32>; break;
-    }
-    int occ = 0;
-    NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWideThreads, 0));
-    const unsigned blocks = (unsigned)std::min<int64_t>((n * lanes + kWideThreads - 1) / kWideThreads,
-                                                        (int64_t)ctx->num_sms * std::max(occ, 1));
+    const unsigned blocks = (unsigned)((n * lanes + kWideThreads - 1) / kWideThreads);
     const int64_t* R = ctx->wq_rowptr.as<int64_t>();
     const int32_t* B = ctx->wq_base.as<int32_t>();
     const real* V = ctx->wq_val.as<real>();

@@ -232,7 +232,7 @@ def run_with_clamps(model, clamps, offs, steps):
 
 
 def network_case(sizes, num_synapses, *, seed=0, time_step=0.1, precision="f64", currents=None,
-                 delay_lo=1.0, delay_hi=5.0, oracle=True, tolerance=None, path="batched"):
+                 delay_lo=1.0, delay_hi=5.0, oracle=True, tolerance=None, path="batched", fmt="rows"):
     """Random trees wired by random_network; HH everywhere, a soma current per neuron.
 
     Returns (gpu model, oracle model or None, net dict, offsets)."""
@@ -248,7 +248,7 @@ def network_case(sizes, num_synapses, *, seed=0, time_step=0.1, precision="f64",
     hh_kw = dict(ena=50.0, ek=-77.0, el=-54.3)
     kw = {} if tolerance is None else {"propagator_tolerance": tolerance}
     m = nw.RxD_Model(time_step=time_step, temperature=6.3, precision=precision, path=path,
-                     mechanisms=[nw.HH.configure(**hh_kw)], **kw)
+                     propagator_format=fmt, mechanisms=[nw.HH.configure(**hh_kw)], **kw)
     neurons = [m.add_tree(t) for t in trees]
     m.insert_everywhere("hh")
     offs = np.cumsum([0] + [len(t) for t in trees])[:-1]

@@ -39,9 +39,10 @@ def _run_recording(m, steps):
     return spikes
 
 
-@pytest.mark.parametrize("path", ["batched", "wide"])
-def test_f64_network_matches_oracle(path):
-    m, om, net, offs = network_case([150, 90, 200, 60], 300, seed=2, delay_lo=1.0, delay_hi=4.0, path=path)
+@pytest.mark.parametrize("path,fmt", [("batched", "rows"), ("batched", "quads"), ("wide", "rows")])
+def test_f64_network_matches_oracle(path, fmt):
+    m, om, net, offs = network_case([150, 90, 200, 60], 300, seed=2, delay_lo=1.0, delay_hi=4.0, path=path,
+                                    fmt=fmt)
     steps = 400
     spikes = []
     worst = 0.0
