@@ -202,6 +202,24 @@ wide_calcium_mechanism_kernel(const StepArgs<real> a) {
     calcium_mechanisms(a, i);
 }
 
+// HH gates (one instance per segment, in segment order) and the calcium mechanisms
+// of each segment in one launch: a thread updates segment i's gates, then its
+// calcium, which reads the new gates for the sodium influx (the order of the two
+// launches this replaces).
+template <typename real>
+__global__ void __launch_bounds__(kWideThreads)
+wide_hh_calcium_kernel(const StepArgs<real> a) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= a.ca_n) return;
+    if (a.hh_on) {
+        const real v = a.V[i];
+        real m = a.gm[i], h = a.gh[i], nn = a.gn[i];
+        hh_gates(v, a.dtq10, m, h, nn);
+        a.gm[i] = m; a.gh[i] = h; a.gn[i] = nn;
+    }
+    calcium_mechanisms(a, i);
+}
+
 template <typename real>
 __global__ void wide_detect_kernel(const StepArgs<real> a, const int s_off) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -490,6 +508,8 @@ static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lan
     const int64_t n_hh = ctx->hh.m, n_kin = kinetic_instances(ctx), n_syn = ctx->syn.n;
     const int64_t n_mech = n_hh + n_kin + n_syn;
     const int64_t cover = std::max<int64_t>(ctx->n_neuron, ctx->n_probes);
+    // HH (one instance per segment) and calcium as the only mechanisms: one launch.
+    const bool hh_calcium = a.ca_on && n_kin == 0 && n_syn == 0 && (n_hh == 0 || ctx->hh.identity);
     for (int s = 0; s < steps; ++s) {
         for (int half = 0; half < 2; ++half) {
             const int last = (s == steps - 1 && half == 1) ? 1 : 0;
@@ -501,14 +521,19 @@ static int enqueue_wide(nw_ctx* ctx, const StepArgs<real>& a, int steps, int lan
             if (a.ca_on && !(ctx->prop_format == 2 && ctx->wq_ok))
                 NW_CHECK(launch_rows<real>(ctx, 4, a.ca_wrow, a.ca_wcol, a.ca_wval, a.ca_wleak, a.ca_scratch, a.ca_c,
                                            a.status));
-            if (half == 0 && n_mech > 0) {
-                wide_mechanism_kernel<real><<<(unsigned)((n_mech + kWideThreads - 1) / kWideThreads), kWideThreads, 0,
-                                              ctx->stream>>>(a, s, n_hh, n_kin, n_syn);
+            if (half == 0 && hh_calcium) {
+                wide_hh_calcium_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
                 NW_CUDA(ctx, cudaGetLastError());
-            }
-            if (half == 0 && a.ca_on) {
-                wide_calcium_mechanism_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
-                NW_CUDA(ctx, cudaGetLastError());
+            } else if (half == 0) {
+                if (n_mech > 0) {
+                    wide_mechanism_kernel<real><<<(unsigned)((n_mech + kWideThreads - 1) / kWideThreads),
+                                                  kWideThreads, 0, ctx->stream>>>(a, s, n_hh, n_kin, n_syn);
+                    NW_CUDA(ctx, cudaGetLastError());
+                }
+                if (a.ca_on) {
+                    wide_calcium_mechanism_kernel<real><<<seg_blocks, kWideThreads, 0, ctx->stream>>>(a);
+                    NW_CUDA(ctx, cudaGetLastError());
+                }
             }
         }
         wide_detect_kernel<real><<<(unsigned)((cover + 127) / 128), 128, 0, ctx->stream>>>(a, s);
