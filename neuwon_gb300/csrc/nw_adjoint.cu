@@ -65,9 +65,24 @@ __device__ __forceinline__ real* tape_slot(const AdjArgs<real>& A, int s, int sl
     return A.tape + ((int64_t)s * kTapeSlots + slot) * A.n_seg;
 }
 
+// V_r-like sums of one neuron's rows applied to xs in the row format or, when the
+// model stores it, the quad format (the same entries); fin(r, row, xi, y).
+template <typename real, int LPR, bool QUAD, typename Fin>
+__device__ __forceinline__ void propagate_adj(const StepArgs<real>& a, int64_t base, int n, const real* xs, Fin fin) {
+    if constexpr (QUAD) propagate_quads<real, LPR>(a, base, n, xs, fin);
+    else propagate_rows<real, LPR>(a, base, n, xs, fin);
+}
+
+// Quad windows of a neuron of fewer than 4 segments reach past it: zeros there.
+template <typename real, bool QUAD>
+__device__ __forceinline__ void pad_quad_x(real* xs, int n) {
+    if (QUAD)
+        for (int li = n + threadIdx.x; li < 4; li += blockDim.x) xs[li] = real(0);
+}
+
 // Forward steps of one neuron per CTA (HH, one instance per segment), with an
 // optional tape and the loss; the arithmetic is that of the batched path.
-template <typename real, int LPR>
+template <typename real, int LPR, bool QUAD>
 __global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<real> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     real* xs = reinterpret_cast<real*>(smem_raw);
@@ -86,6 +101,7 @@ __global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<rea
         const int j = a.neuron_order[job];
         const int64_t base = a.neuron_start[j];
         const int n = (int)(a.neuron_start[j + 1] - base);
+        pad_quad_x<real, QUAD>(xs, n);
         if (tid == 0) {
             const int c0 = a.clamp_neuron_ptr ? a.clamp_neuron_ptr[j] : 0;
             const int c1 = a.clamp_neuron_ptr ? a.clamp_neuron_ptr[j + 1] : 0;
@@ -133,7 +149,10 @@ __global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<rea
                     xs[li] = membrane_x(a, i, G, GE, I, last);
                 }
                 __syncthreads();
-                propagate_neuron<real, LPR>(a, base, n, xs);
+                propagate_adj<real, LPR, QUAD>(a, base, n, xs, [&](int64_t r, int, real, real vnew) {
+                    if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
+                    a.V[r] = vnew;
+                });
                 __syncthreads();
                 if (half == 0) {
                     for (int li = tid; li < n; li += nthr) {
@@ -188,7 +207,7 @@ __global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<rea
 // accumulates flow_i * (lambda_i / C_i - lambda_p / C_p) per segment with a parent,
 // into the thread's compensated sum (ra_s, ra_c); the factor -h / Ra is applied
 // once per neuron.  Density gradients accumulate in compensated sums per segment.
-template <typename real, int LPR>
+template <typename real, int LPR, bool QUAD>
 __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_t base, int n, real* xs,
                                                   const real* V_in, const real* V_out, const real* gm,
                                                   const real* gh, const real* gn, const real* lam_out,
@@ -203,7 +222,7 @@ __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_
     __syncthreads();
     // The rows leave lambda of x (C P^T applied) in lam_in; the membrane update's
     // adjoint follows per segment below, with every lane of the CTA.
-    propagate_rows<real, LPR>(a, base, n, xs, [&](int64_t r, int, real, real nu) { lam_in[r] = nu * A.cap_r[r]; });
+    propagate_adj<real, LPR, QUAD>(a, base, n, xs, [&](int64_t r, int, real, real nu) { lam_in[r] = nu * A.cap_r[r]; });
     // xs still holds lambda / C of every segment of the neuron (the rows only read it).
     for (int li = tid; li < n; li += nthr) {
         const int64_t i = base + li;
@@ -248,7 +267,7 @@ __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_
     __syncthreads();
 }
 
-template <typename real, int LPR>
+template <typename real, int LPR, bool QUAD>
 __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<real> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     real* xs = reinterpret_cast<real*>(smem_raw);
@@ -264,6 +283,7 @@ __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<rea
         const int j = a.neuron_order[job];
         const int64_t base = a.neuron_start[j];
         const int n = (int)(a.neuron_start[j + 1] - base);
+        pad_quad_x<real, QUAD>(xs, n);
         real ra_s = real(0), ra_c = real(0);
         for (int s = a.k_steps - 1; s >= 0; --s) {
             const int64_t gs = A.step0 + s;
@@ -274,7 +294,7 @@ __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<rea
             }
             __syncthreads();
             // Second half step: V_mid, gates(s+1) -> V(s+1).
-            half_step_reverse<real, LPR>(A, base, n, xs, tape_slot(A, s, 1), tape_slot(A, s + 1, 0),
+            half_step_reverse<real, LPR, QUAD>(A, base, n, xs, tape_slot(A, s, 1), tape_slot(A, s + 1, 0),
                                          tape_slot(A, s + 1, 2), tape_slot(A, s + 1, 3), tape_slot(A, s + 1, 4),
                                          A.lamV, A.lamV2, true, ra_s, ra_c);
             // Mechanisms: gates(s+1) = f(gates(s), V_mid).
@@ -295,7 +315,7 @@ __global__ void __launch_bounds__(1024) adjoint_reverse_kernel(const AdjArgs<rea
             __syncthreads();
             // First half step: V(s), gates(s) -> V_mid.
             const bool gv = (gs > 0) || A.g_valid_first;
-            half_step_reverse<real, LPR>(A, base, n, xs, tape_slot(A, s, 0), tape_slot(A, s, 1),
+            half_step_reverse<real, LPR, QUAD>(A, base, n, xs, tape_slot(A, s, 0), tape_slot(A, s, 1),
                                          tape_slot(A, s, 2), tape_slot(A, s, 3), tape_slot(A, s, 4),
                                          A.lamV2, A.lamV, gv, ra_s, ra_c);
         }
@@ -345,10 +365,17 @@ static int adj_lpr(nw_ctx* ctx) {
     return l >= 16 ? 16 : (l >= 8 ? 8 : 4);
 }
 
-template <typename real, int LPR>
+// x of the largest neuron (at least 4 entries: quad windows of smaller neurons
+// reach past them).
+template <typename real>
+static size_t adj_smem(const nw_ctx* ctx) {
+    return ((size_t)std::max<int64_t>(ctx->max_neuron, 4) * sizeof(real) + 15) & ~(size_t)15;
+}
+
+template <typename real, int LPR, bool QUAD>
 static int launch_forward_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
-    auto kern = adjoint_forward_kernel<real, LPR>;
-    const size_t smem = ((size_t)ctx->max_neuron * sizeof(real) + 15) & ~(size_t)15;
+    auto kern = adjoint_forward_kernel<real, LPR, QUAD>;
+    const size_t smem = adj_smem<real>(ctx);
     NW_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, ctx->threads, smem));
@@ -360,10 +387,10 @@ static int launch_forward_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
     return NW_OK;
 }
 
-template <typename real, int LPR>
+template <typename real, int LPR, bool QUAD>
 static int launch_reverse_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
-    auto kern = adjoint_reverse_kernel<real, LPR>;
-    const size_t smem = ((size_t)ctx->max_neuron * sizeof(real) + 15) & ~(size_t)15;
+    auto kern = adjoint_reverse_kernel<real, LPR, QUAD>;
+    const size_t smem = adj_smem<real>(ctx);
     NW_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, ctx->threads, smem));
@@ -375,21 +402,27 @@ static int launch_reverse_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
     return NW_OK;
 }
 
+// The quad format when the model stores its propagator that way (the same entries
+// as the rows, fewer bytes), else the row format.
+static bool adj_quads(const nw_ctx* ctx) { return ctx->prop_format == 2 && ctx->q_ok; }
+
 template <typename real>
 static int launch_forward(nw_ctx* ctx, AdjArgs<real>& A) {
+    const bool q = adj_quads(ctx);
     switch (adj_lpr(ctx)) {
-        case 4: return launch_forward_cfg<real, 4>(ctx, A);
-        case 8: return launch_forward_cfg<real, 8>(ctx, A);
-        default: return launch_forward_cfg<real, 16>(ctx, A);
+        case 4: return q ? launch_forward_cfg<real, 4, true>(ctx, A) : launch_forward_cfg<real, 4, false>(ctx, A);
+        case 8: return q ? launch_forward_cfg<real, 8, true>(ctx, A) : launch_forward_cfg<real, 8, false>(ctx, A);
+        default: return q ? launch_forward_cfg<real, 16, true>(ctx, A) : launch_forward_cfg<real, 16, false>(ctx, A);
     }
 }
 
 template <typename real>
 static int launch_reverse(nw_ctx* ctx, AdjArgs<real>& A) {
+    const bool q = adj_quads(ctx);
     switch (adj_lpr(ctx)) {
-        case 4: return launch_reverse_cfg<real, 4>(ctx, A);
-        case 8: return launch_reverse_cfg<real, 8>(ctx, A);
-        default: return launch_reverse_cfg<real, 16>(ctx, A);
+        case 4: return q ? launch_reverse_cfg<real, 4, true>(ctx, A) : launch_reverse_cfg<real, 4, false>(ctx, A);
+        case 8: return q ? launch_reverse_cfg<real, 8, true>(ctx, A) : launch_reverse_cfg<real, 8, false>(ctx, A);
+        default: return q ? launch_reverse_cfg<real, 16, true>(ctx, A) : launch_reverse_cfg<real, 16, false>(ctx, A);
     }
 }
 
@@ -528,6 +561,7 @@ static int adjoint_check(nw_ctx* ctx) {
     if (ctx->ca.on) return fail(ctx, NW_ERR_STATE, "adjoint: calcium is not differentiated");
     if (!ctx->b_ok) return fail(ctx, NW_ERR_LIMIT, "adjoint: a neuron has more than 65,535 segments");
     if (ctx->nonspec_nonzero) return fail(ctx, NW_ERR_STATE, "adjoint: nonspecific currents are not supported");
+    if (ctx->prop_format == 2) NW_CHECK(ensure_quads(ctx));
     return NW_OK;
 }
 
