@@ -31,7 +31,7 @@ typedef struct nw_ctx nw_ctx;
 #define NW_ERR_STATE    -3   /* call made in the wrong order                 */
 #define NW_ERR_NOMEM    -4   /* device allocation failed                     */
 #define NW_ERR_NUMERIC  -5   /* a kernel flagged a non-finite voltage        */
-#define NW_ERR_LIMIT    -6   /* a size exceeds what this build supports      */
+#define NW_ERR_LIMIT    -6   /* a size exceeds what the library supports    */
 
 /* Arithmetic precision of a context's state and step kernels. */
 #define NW_F32 4

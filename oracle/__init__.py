@@ -2,7 +2,7 @@
 
 This package restates, in plain FP64 numpy (``reference_step``) and in C
 (``cpu_step.c``), the reference's algorithm for one staggered time step.  It is
-the checker, never the product: only ``tests/``, ``__graft_entry__.smoke()`` and
+test infrastructure, never the product: only ``tests/``, ``__graft_entry__.smoke()`` and
 ``bench.py``'s CPU-baseline / reference arm may import, link or run anything in
 this directory.  The product path (``neuwon_gb300``) never calls it and fails
 loudly when its CUDA library is missing.
