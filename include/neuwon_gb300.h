@@ -399,6 +399,9 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * mechanisms map one-to-one onto segments (each warp's 32 rows, then their segments'
  * mechanisms and next x) instead of one launch per phase; on a GB300 the phase
  * launches are faster from 2,000 to 1,000,000 segments (more rows in flight per SM).
+ * "adjoint_overlap" (default 1): nw_adjoint_backward recomputes checkpoint segment
+ * k-1 on a second stream while the reverse sweep of segment k runs (two tapes on the
+ * device instead of one); the gradients are the same bit for bit with 0.
  * nw_get_option also reports "wide_quads", "wide_entries" and
  * "calcium_wide_entries" (stored windows / entries of the wide path's voltage and
  * calcium propagators, once built). */

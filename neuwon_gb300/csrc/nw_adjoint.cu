@@ -376,7 +376,7 @@ static size_t adj_smem(const nw_ctx* ctx) {
 }
 
 template <typename real, int LPR, bool QUAD>
-static int launch_forward_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
+static int launch_forward_cfg(nw_ctx* ctx, AdjArgs<real>& A, cudaStream_t st) {
     auto kern = adjoint_forward_kernel<real, LPR, QUAD>;
     const size_t smem = adj_smem<real>(ctx);
     NW_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -384,14 +384,14 @@ static int launch_forward_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
     NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, ctx->threads, smem));
     if (occ < 1) return fail(ctx, NW_ERR_LIMIT, "adjoint forward kernel does not fit on an SM");
     const int64_t grid = std::min<int64_t>(ctx->n_neuron, (int64_t)occ * ctx->num_sms);
-    NW_CUDA(ctx, cudaMemsetAsync(ctx->work_counter.ptr, 0, sizeof(int), ctx->stream));
-    kern<<<(unsigned)grid, ctx->threads, smem, ctx->stream>>>(A);
+    NW_CUDA(ctx, cudaMemsetAsync(A.a.work_counter, 0, sizeof(int), st));
+    kern<<<(unsigned)grid, ctx->threads, smem, st>>>(A);
     NW_CUDA(ctx, cudaGetLastError());
     return NW_OK;
 }
 
 template <typename real, int LPR, bool QUAD>
-static int launch_reverse_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
+static int launch_reverse_cfg(nw_ctx* ctx, AdjArgs<real>& A, cudaStream_t st) {
     auto kern = adjoint_reverse_kernel<real, LPR, QUAD>;
     const size_t smem = adj_smem<real>(ctx);
     NW_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -399,8 +399,8 @@ static int launch_reverse_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
     NW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, ctx->threads, smem));
     if (occ < 1) return fail(ctx, NW_ERR_LIMIT, "adjoint reverse kernel does not fit on an SM");
     const int64_t grid = std::min<int64_t>(ctx->n_neuron, (int64_t)occ * ctx->num_sms);
-    NW_CUDA(ctx, cudaMemsetAsync(ctx->work_counter.ptr, 0, sizeof(int), ctx->stream));
-    kern<<<(unsigned)grid, ctx->threads, smem, ctx->stream>>>(A);
+    NW_CUDA(ctx, cudaMemsetAsync(A.a.work_counter, 0, sizeof(int), st));
+    kern<<<(unsigned)grid, ctx->threads, smem, st>>>(A);
     NW_CUDA(ctx, cudaGetLastError());
     return NW_OK;
 }
@@ -410,32 +410,32 @@ static int launch_reverse_cfg(nw_ctx* ctx, AdjArgs<real>& A) {
 static bool adj_quads(const nw_ctx* ctx) { return ctx->prop_format == 2 && ctx->q_ok; }
 
 template <typename real>
-static int launch_forward(nw_ctx* ctx, AdjArgs<real>& A) {
+static int launch_forward(nw_ctx* ctx, AdjArgs<real>& A, cudaStream_t st) {
     const bool q = adj_quads(ctx);
     switch (adj_lpr(ctx)) {
-        case 4: return q ? launch_forward_cfg<real, 4, true>(ctx, A) : launch_forward_cfg<real, 4, false>(ctx, A);
-        case 8: return q ? launch_forward_cfg<real, 8, true>(ctx, A) : launch_forward_cfg<real, 8, false>(ctx, A);
-        default: return q ? launch_forward_cfg<real, 16, true>(ctx, A) : launch_forward_cfg<real, 16, false>(ctx, A);
+        case 4: return q ? launch_forward_cfg<real, 4, true>(ctx, A, st) : launch_forward_cfg<real, 4, false>(ctx, A, st);
+        case 8: return q ? launch_forward_cfg<real, 8, true>(ctx, A, st) : launch_forward_cfg<real, 8, false>(ctx, A, st);
+        default: return q ? launch_forward_cfg<real, 16, true>(ctx, A, st) : launch_forward_cfg<real, 16, false>(ctx, A, st);
     }
 }
 
 template <typename real>
-static int launch_reverse(nw_ctx* ctx, AdjArgs<real>& A) {
+static int launch_reverse(nw_ctx* ctx, AdjArgs<real>& A, cudaStream_t st) {
     const bool q = adj_quads(ctx);
     switch (adj_lpr(ctx)) {
-        case 4: return q ? launch_reverse_cfg<real, 4, true>(ctx, A) : launch_reverse_cfg<real, 4, false>(ctx, A);
-        case 8: return q ? launch_reverse_cfg<real, 8, true>(ctx, A) : launch_reverse_cfg<real, 8, false>(ctx, A);
-        default: return q ? launch_reverse_cfg<real, 16, true>(ctx, A) : launch_reverse_cfg<real, 16, false>(ctx, A);
+        case 4: return q ? launch_reverse_cfg<real, 4, true>(ctx, A, st) : launch_reverse_cfg<real, 4, false>(ctx, A, st);
+        case 8: return q ? launch_reverse_cfg<real, 8, true>(ctx, A, st) : launch_reverse_cfg<real, 8, false>(ctx, A, st);
+        default: return q ? launch_reverse_cfg<real, 16, true>(ctx, A, st) : launch_reverse_cfg<real, 16, false>(ctx, A, st);
     }
 }
 
 // State copied at checkpoints: V, m, h, n.
-static int copy_state(nw_ctx* ctx, char* dst, bool to_ckpt) {
+static int copy_state(nw_ctx* ctx, char* dst, bool to_ckpt, cudaStream_t st) {
     const size_t b = (size_t)ctx->precision * ctx->n_seg;
     void* arrs[4] = {ctx->V.ptr, ctx->hh.gm.ptr, ctx->hh.gh.ptr, ctx->hh.gn.ptr};
     for (int k = 0; k < 4; ++k) {
-        if (to_ckpt) NW_CUDA(ctx, cudaMemcpyAsync(dst + k * b, arrs[k], b, cudaMemcpyDeviceToDevice, ctx->stream));
-        else NW_CUDA(ctx, cudaMemcpyAsync(arrs[k], dst + k * b, b, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (to_ckpt) NW_CUDA(ctx, cudaMemcpyAsync(dst + k * b, arrs[k], b, cudaMemcpyDeviceToDevice, st));
+        else NW_CUDA(ctx, cudaMemcpyAsync(arrs[k], dst + k * b, b, cudaMemcpyDeviceToDevice, st));
     }
     return NW_OK;
 }
@@ -454,7 +454,7 @@ static int adjoint_forward_impl(nw_ctx* ctx, int64_t T, int K, const double* tar
     NW_CUDA(ctx, cudaMemsetAsync(S.loss_part.ptr, 0, 8 * nn, ctx->stream));
     S.K = K; S.total_steps = T; S.tick0 = ctx->input_ticks; S.g_valid0 = ctx->g_valid;
     for (int64_t sg = 0; sg < nseg; ++sg) {
-        NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * sg, true));
+        NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * sg, true, ctx->stream));
         const int k = (int)std::min<int64_t>(K, T - sg * K);
         AdjArgs<real> A = adj_args<real>(ctx);
         A.a.k_steps = k;
@@ -462,12 +462,12 @@ static int adjoint_forward_impl(nw_ctx* ctx, int64_t T, int K, const double* tar
         A.a.g_valid = ctx->g_valid ? 1 : 0;
         A.step0 = sg * K;
         A.update_detectors = 1;
-        NW_CHECK(launch_forward(ctx, A));
+        NW_CHECK(launch_forward(ctx, A, ctx->stream));
         ctx->input_ticks += 2 * (int64_t)k;
         ctx->steps += k;
         ctx->g_valid = true;
     }
-    NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * nseg, true));
+    NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * nseg, true, ctx->stream));
     std::vector<double> lp(nn);
     NW_CUDA(ctx, cudaMemcpyAsync(lp.data(), S.loss_part.ptr, 8 * nn, cudaMemcpyDeviceToHost, ctx->stream));
     NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -487,7 +487,20 @@ static int adjoint_backward_impl(nw_ctx* ctx, double Ra, double* g_gna, double* 
     const int K = S.K;
     const int64_t nseg = (T + K - 1) / K;
     const size_t b = (size_t)ctx->precision * n;
-    NW_CHECK(dev_alloc(ctx, S.tape, b * kTapeSlots * (size_t)(K + 1)));
+    // Two tapes (by the parity of the checkpoint segment) when the recompute of
+    // segment k-1 runs beside the reverse sweep of segment k, else one.
+    const bool overlap = ctx->adjoint_overlap && nseg > 1;
+    const size_t tape_elems = (size_t)n * kTapeSlots * (size_t)(K + 1);
+    NW_CHECK(dev_alloc(ctx, S.tape, (size_t)ctx->precision * tape_elems * (overlap ? 2 : 1)));
+    if (overlap && !S.stream) {
+        NW_CUDA(ctx, cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&S.rec_done, &S.rev_done[0], &S.rev_done[1], &S.start})
+            NW_CUDA(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    // Recompute and reverse sweep count their neurons on separate counters.
+    int* const wc_rec = ctx->work_counter.as<int>();
+    int* const wc_rev = overlap ? wc_rec + 4 : wc_rec;
+    const cudaStream_t rs = overlap ? S.stream : ctx->stream;
     for (DevBuf* buf : {&S.lamV, &S.lamV2, &S.lamM, &S.lamH, &S.lamN}) {
         NW_CHECK(dev_alloc(ctx, *buf, b));
         NW_CUDA(ctx, cudaMemsetAsync(buf->ptr, 0, b, ctx->stream));
@@ -502,18 +515,31 @@ static int adjoint_backward_impl(nw_ctx* ctx, double Ra, double* g_gna, double* 
     NW_CUDA(ctx, cudaGetLastError());
     NW_CHECK(dev_alloc(ctx, S.ra_part, 8 * nn));
     NW_CUDA(ctx, cudaMemsetAsync(S.ra_part.ptr, 0, 8 * nn, ctx->stream));
+    if (overlap) {
+        NW_CUDA(ctx, cudaEventRecord(S.start, ctx->stream));
+        NW_CUDA(ctx, cudaStreamWaitEvent(rs, S.start, 0));
+    }
     for (int64_t sg = nseg - 1; sg >= 0; --sg) {
         const int k = (int)std::min<int64_t>(K, T - sg * K);
-        NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * sg, false));
+        const int par = overlap ? (int)(sg & 1) : 0;
+        // This tape was last read by the reverse sweep of segment sg + 2.
+        if (overlap && sg + 2 <= nseg - 1) NW_CUDA(ctx, cudaStreamWaitEvent(rs, S.rev_done[par], 0));
+        NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * sg, false, rs));
         AdjArgs<real> A = adj_args<real>(ctx);
         A.a.k_steps = k;
         A.a.tick0 = S.tick0 + 2 * sg * (int64_t)K;
         A.a.g_valid = (sg == 0) ? (S.g_valid0 ? 1 : 0) : 1;
+        A.a.work_counter = wc_rec;
         A.step0 = sg * K;
-        A.tape = S.tape.as<real>();
+        A.tape = S.tape.as<real>() + (size_t)par * tape_elems;
         A.target = nullptr;
         A.update_detectors = 0;
-        NW_CHECK(launch_forward(ctx, A));
+        NW_CHECK(launch_forward(ctx, A, rs));
+        if (overlap) {
+            NW_CUDA(ctx, cudaEventRecord(S.rec_done, rs));
+            NW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, S.rec_done, 0));
+        }
+        A.a.work_counter = wc_rev;
         A.target = S.target.as<real>();
         A.lamV = S.lamV.as<real>(); A.lamV2 = S.lamV2.as<real>();
         A.lamM = S.lamM.as<real>(); A.lamH = S.lamH.as<real>(); A.lamN = S.lamN.as<real>();
@@ -521,9 +547,11 @@ static int adjoint_backward_impl(nw_ctx* ctx, double Ra, double* g_gna, double* 
         A.inv_cap = S.coef.as<real>(); A.cap_r = A.inv_cap + n; A.inv_res = A.inv_cap + 2 * n;
         A.ra_part = S.ra_part.as<double>();
         A.inv_ra = 1.0 / Ra;
-        NW_CHECK(launch_reverse(ctx, A));
+        NW_CHECK(launch_reverse(ctx, A, ctx->stream));
+        if (overlap) NW_CUDA(ctx, cudaEventRecord(S.rev_done[par], ctx->stream));
     }
-    NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * nseg, false));
+    // Every recompute precedes a reverse sweep that the context's stream waited for.
+    NW_CHECK(copy_state(ctx, S.ckpt.as<char>() + 4 * b * nseg, false, ctx->stream));
     std::vector<real> gsum[3] = {std::vector<real>(2 * n), std::vector<real>(2 * n), std::vector<real>(2 * n)};
     std::vector<double> rp(nn);
     DevBuf* gbuf[3] = {&S.gGna, &S.gGk, &S.gGl};

@@ -167,9 +167,13 @@ static void free_hh(HHState& hh) {
 }
 
 static void free_adj(AdjointState& a) {
+    if (a.stream) cudaStreamSynchronize(a.stream);
     for (DevBuf* b : {&a.ckpt, &a.target, &a.loss_part, &a.tape, &a.lamV, &a.lamV2, &a.lamM, &a.lamH, &a.lamN,
                       &a.gGna, &a.gGk, &a.gGl, &a.ra_part, &a.coef})
         dev_free(*b);
+    for (cudaEvent_t e : {a.rec_done, a.rev_done[0], a.rev_done[1], a.start})
+        if (e) cudaEventDestroy(e);
+    if (a.stream) cudaStreamDestroy(a.stream);
     a = AdjointState();
 }
 
@@ -1337,6 +1341,7 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
         return NW_OK;
     }
     if (nm == "wide_fusion") { ctx->wide_fusion = value != 0; return NW_OK; }
+    if (nm == "adjoint_overlap") { ctx->adjoint_overlap = value != 0; return NW_OK; }
     if (nm == "lanes_split") {
         // Quad format: neurons whose mean quads per row are below this take half the
         // lanes per row of the kernel's choice (0: all neurons the same).
@@ -1405,6 +1410,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "calcium_wide_entries") { *value = ctx->ca.on ? ctx->ca.nnz_w : 0; return NW_OK; }
     if (nm == "lanes_split") { *value = ctx->lanes_split; return NW_OK; }
     if (nm == "wide_fusion") { *value = ctx->wide_fusion ? 1 : 0; return NW_OK; }
+    if (nm == "adjoint_overlap") { *value = ctx->adjoint_overlap ? 1 : 0; return NW_OK; }
     if (nm == "narrow_neurons") {
         int64_t k = 0;
         if (ctx->q_ok && ctx->lanes_split > 0)

@@ -156,6 +156,10 @@ struct AdjointState {
     DevBuf lamV, lamV2, lamM, lamH, lamN;
     DevBuf gGna, gGk, gGl, ra_part;
     DevBuf coef;                // 1/C, C and 1/R per segment in the state precision
+    // Backward: the recompute of checkpoint segment k-1 runs on `stream` while the
+    // reverse sweep of segment k runs on the context's stream; two tapes by parity.
+    cudaStream_t stream = nullptr;
+    cudaEvent_t rec_done = nullptr, rev_done[2] = {nullptr, nullptr}, start = nullptr;
 };
 
 }  // namespace nw
@@ -279,6 +283,7 @@ struct nw_ctx {
     nw::DevBuf plain_x;         // real [n_seg] scratch of the plain path (the wide path's x)
     nw::DevBuf wide_x2, wide_cs2;   // real [n_seg]: the fused wide path's second x / calcium scratch
     bool wide_fusion = false;   // wide path: one launch per half step when mechanisms allow it
+    bool adjoint_overlap = true; // backward: recompute of segment k-1 beside the reverse sweep of k
     int lanes_per_row = 0, threads = 1024, ctas_per_sm = 0;
     int fusion = 50;            // steps fused per launch (0: one launch per call)
     bool use_bulk = false;      // asynchronous bulk-copy pipeline (FP32 batched path)

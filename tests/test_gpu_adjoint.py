@@ -118,6 +118,29 @@ def test_checkpoint_interval_does_not_change_gradients():
     m.close()
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_overlapped_recompute_gives_the_serial_gradients(precision):
+    """The recompute of checkpoint segment k-1 on a second stream beside the reverse
+    sweep of segment k (two tapes) changes no operation: bit-identical to one stream."""
+    trees = [random_tree(120 + 37 * i, seed=300 + i) for i in range(12)]
+    steps, K = 230, 40
+    m, _ = _model(trees, precision=precision, amps=tuple(0.2 + 0.03 * i for i in range(12)))
+    target = np.random.default_rng(4).uniform(-70.0, -55.0, (steps, len(trees)))
+    runs = []
+    for overlap in (0, 1, 1):
+        m._ctx.set_option("adjoint_overlap", overlap)
+        m.reset_state()
+        runs.append(loss_and_gradients(m, steps, target, checkpoint_every=K))
+        runs[-1] = runs[-1] + (m.get_data("Segment.voltage").copy(),)
+    assert m._ctx.get_option("adjoint_overlap") == 1
+    for r in runs[1:]:
+        assert r[0] == runs[0][0] and r[4] == runs[0][4]
+        for x, y in zip(r[1:4], runs[0][1:4]):
+            assert np.array_equal(x, y)
+        assert np.array_equal(r[5], runs[0][5])
+    m.close()
+
+
 def test_fp32_adjoint_close_to_fp64():
     trees = [random_tree(300, seed=91)]
     steps = 200
