@@ -480,7 +480,7 @@ def diff_check(args, device):
     print(json.dumps(out), flush=True)
 
 
-def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000, threads=0, overlap=1):
+def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000, threads=0, overlap=1, lanes=0):
     """Config 4 shape: 256 HH neurons of 2,000 segments, dt 0.025 ms, FP32, targets = FP64
     soma traces of the same neurons with densities drawn +-30 % around the defaults;
     gradients of the soma MSE w.r.t. per-segment gNa/gK/gL and Ra (checkpoint every 100)."""
@@ -491,8 +491,8 @@ def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000, thr
     k = neurons * size
     target = adjoint_target(trees, steps, device)
     m = adjoint_build(trees, "f32", device)
-    if threads:
-        m._ctx.call("nw_set_tuning", 0, threads, 0)
+    if threads or lanes:
+        m._ctx.call("nw_set_tuning", lanes, threads or 1024, 0)
     m._ctx.set_option("adjoint_overlap", overlap)
     m.reset_state()
     torch.cuda.synchronize()
@@ -505,6 +505,7 @@ def adjoint_leg(device, steps, checkpoint_every=100, neurons=256, size=2000, thr
     return {"ms_per_step": 1e3 * (t2 - t0) / steps, "forward_ms_per_step": 1e3 * (t1 - t0) / steps,
             "backward_ms_per_step": 1e3 * (t2 - t1) / steps, "steps": steps,
             "checkpoint_every": checkpoint_every, "threads": threads or "context default",
+            "lanes_per_row": lanes or "by quads per row",
             "recompute_beside_reverse": bool(overlap), "loss_mV2": loss,
             "grad_norm": float(np.sqrt((gna ** 2).sum() + (gk ** 2).sum() + (gl ** 2).sum())),
             "grad_ra": gra, "parameters": 3 * k + 1,
@@ -640,7 +641,7 @@ def run_leg(args, rank, local):
     torch.cuda.set_device(local)
     if args.leg == "adjoint":
         out = adjoint_leg(local, args.adjoint_steps, neurons=args.leg_neurons or 256, size=args.leg_size or 2000,
-                          threads=args.adjoint_threads, overlap=args.adjoint_overlap)
+                          threads=args.adjoint_threads, overlap=args.adjoint_overlap, lanes=args.adjoint_lanes)
     elif args.leg == "wide":
         variants = [tuple(int(x) for x in v.split(":")) for v in args.wide_variants.split(",")]
         out = wide_leg(local, args.study_segments, args.wide_tol, args.wide_steps, variants)
@@ -751,6 +752,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip accuracy/plain/cpu/adjoint legs")
     ap.add_argument("--adjoint-steps", type=int, default=800)
     ap.add_argument("--adjoint-threads", type=int, default=0, help="threads per CTA of the adjoint kernels (0: default)")
+    ap.add_argument("--adjoint-lanes", type=int, default=0, help="lanes per row of the adjoint kernels (0: by quads per row)")
     ap.add_argument("--adjoint-overlap", type=int, default=1,
                     help="1: the backward recomputes segment k-1 on a second stream beside the reverse sweep of k")
     ap.add_argument("--network-steps", type=int, default=200,
