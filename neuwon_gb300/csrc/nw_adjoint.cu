@@ -596,7 +596,15 @@ static int adjoint_check(nw_ctx* ctx) {
     return NW_OK;
 }
 
+// A backward that stopped on an error may have left recomputes queued on the
+// second stream; nothing it reads is reallocated before they finish.
+static int adjoint_quiesce(nw_ctx* ctx) {
+    if (ctx->adj.stream) NW_CUDA(ctx, cudaStreamSynchronize(ctx->adj.stream));
+    return NW_OK;
+}
+
 int adjoint_forward(nw_ctx* ctx, int64_t T, int K, const double* target, double* loss_out) {
+    NW_CHECK(adjoint_quiesce(ctx));
     NW_CHECK(adjoint_check(ctx));
     if (T <= 0 || K <= 0 || !target) return fail(ctx, NW_ERR_ARG, "nw_adjoint_forward: bad steps or target");
     return ctx->precision == NW_F64 ? adjoint_forward_impl<double>(ctx, T, K, target, loss_out)
@@ -604,11 +612,15 @@ int adjoint_forward(nw_ctx* ctx, int64_t T, int K, const double* target, double*
 }
 
 int adjoint_backward(nw_ctx* ctx, double Ra, double* g_gna, double* g_gk, double* g_gl, double* g_ra) {
+    NW_CHECK(adjoint_quiesce(ctx));
     NW_CHECK(adjoint_check(ctx));
     if (!ctx->adj.ready) return fail(ctx, NW_ERR_STATE, "nw_adjoint_backward before nw_adjoint_forward");
     if (!(Ra > 0)) return fail(ctx, NW_ERR_ARG, "nw_adjoint_backward: Ra must be > 0");
-    return ctx->precision == NW_F64 ? adjoint_backward_impl<double>(ctx, Ra, g_gna, g_gk, g_gl, g_ra)
-                                    : adjoint_backward_impl<float>(ctx, Ra, g_gna, g_gk, g_gl, g_ra);
+    const int rc = ctx->precision == NW_F64 ? adjoint_backward_impl<double>(ctx, Ra, g_gna, g_gk, g_gl, g_ra)
+                                            : adjoint_backward_impl<float>(ctx, Ra, g_gna, g_gk, g_gl, g_ra);
+    // On an error nothing stays queued on the second stream.
+    if (rc != NW_OK && ctx->adj.stream) cudaStreamSynchronize(ctx->adj.stream);
+    return rc;
 }
 
 }  // namespace nw

@@ -327,6 +327,7 @@ int nw_synchronize(nw_ctx* ctx) {
     if (!ctx) return NW_ERR_ARG;
     NW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->copy_stream) NW_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+    if (ctx->adj.stream) NW_CUDA(ctx, cudaStreamSynchronize(ctx->adj.stream));
     return NW_OK;
 }
 
@@ -373,6 +374,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
     ctx->n_probes = 0;
     ctx->probe_len = 0;
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->adj.stream) cudaStreamSynchronize(ctx->adj.stream);
     graphs_clear(ctx);
     free_hh(ctx->hh);
     free_kinetics(ctx);
