@@ -402,6 +402,12 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * "adjoint_overlap" (default 1): nw_adjoint_backward recomputes checkpoint segment
  * k-1 on a second stream while the reverse sweep of segment k runs (two tapes on the
  * device instead of one); the gradients are the same bit for bit with 0.
+ * "propagator_single_walk" (default 1): nw_propagator_build walks each row once,
+ * writing its entries into 64-entry chunks of a pool of at most a quarter of the free
+ * device memory ("propagator_pool_chunks" > 0 caps its chunks), then packs them into
+ * the CSR; with 0, or when the pool fills up, a counting walk and a filling walk.
+ * The CSR is the same bit for bit; nw_get_option("propagator_walks") tells which
+ * (1 or 2) the last build used.
  * nw_get_option also reports "wide_quads", "wide_entries" and
  * "calcium_wide_entries" (stored windows / entries of the wide path's voltage and
  * calcium propagators, once built). */

@@ -1344,6 +1344,12 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     }
     if (nm == "wide_fusion") { ctx->wide_fusion = value != 0; return NW_OK; }
     if (nm == "adjoint_overlap") { ctx->adjoint_overlap = value != 0; return NW_OK; }
+    if (nm == "propagator_single_walk") { ctx->prop_walk_once = value != 0; return NW_OK; }
+    if (nm == "propagator_pool_chunks") {
+        if (value < 0) return fail(ctx, NW_ERR_ARG, "propagator_pool_chunks must be >= 0");
+        ctx->prop_pool_chunks = value;
+        return NW_OK;
+    }
     if (nm == "lanes_split") {
         // Quad format: neurons whose mean quads per row are below this take half the
         // lanes per row of the kernel's choice (0: all neurons the same).
@@ -1413,6 +1419,9 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "lanes_split") { *value = ctx->lanes_split; return NW_OK; }
     if (nm == "wide_fusion") { *value = ctx->wide_fusion ? 1 : 0; return NW_OK; }
     if (nm == "adjoint_overlap") { *value = ctx->adjoint_overlap ? 1 : 0; return NW_OK; }
+    if (nm == "propagator_single_walk") { *value = ctx->prop_walk_once ? 1 : 0; return NW_OK; }
+    if (nm == "propagator_walks") { *value = ctx->prop_walks; return NW_OK; }
+    if (nm == "propagator_pool_chunks") { *value = ctx->prop_pool_chunks; return NW_OK; }
     if (nm == "narrow_neurons") {
         int64_t k = 0;
         if (ctx->q_ok && ctx->lanes_split > 0)

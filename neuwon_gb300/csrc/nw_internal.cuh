@@ -221,6 +221,9 @@ struct nw_ctx {
     // lanes_split take half the kernel's lanes per row (0: every neuron the same).
     std::vector<float> h_neuron_qpr;                   // mean quads per row, per neuron
     int64_t lanes_split = 0;
+    bool prop_walk_once = true;  // tree propagator build: one walk per row into a pool when it fits
+    int prop_walks = 0;          // walks per row of the last tree propagator build
+    int64_t prop_pool_chunks = 0;   // cap on the pool's chunks (0: a quarter of free memory)
     int64_t narrow_for = -1;                           // lanes_split the flags were made for
     nw::DevBuf neuron_narrow;                          // u8 per neuron
     nw::DevBuf q_rowptr, q_base, q_val;                // i64 (in quads), u16 (neuron-relative), real x 4

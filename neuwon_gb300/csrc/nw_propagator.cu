@@ -37,6 +37,9 @@ constexpr int kChainDepth = 256;
 constexpr double kExploreFactor = 1e-2;
 constexpr int kStatusStackOverflow = 2;
 constexpr int kStatusRowMismatch = 4;
+constexpr int kStatusPoolFull = 8;
+constexpr int kChunk = 64;            // entries per chunk of the single-walk pool
+constexpr int kMaxChunks = 256;       // chunks per row (16,384 entries)
 
 __constant__ double2 c_z[kPoles];     // contour nodes z_k
 __constant__ double2 c_w[kPoles];     // weights e^{z_k} z'_k
@@ -85,6 +88,14 @@ struct BuildArgs {
     int32_t* out_col;
     double* out_val;
     int* status;
+    // Single walk: each row's entries in chunks of kChunk taken from a pool (the
+    // row's first chunk, then a link per chunk), packed into the CSR afterwards.
+    int32_t* pool_col;
+    double* pool_val;
+    int32_t* pool_first;        // [n_seg], -1: none
+    int32_t* pool_next;         // [pool_chunks]
+    int* pool_top;
+    int pool_chunks;
 };
 
 // One thread per (neuron, pole): the two sweeps over the neuron's tree.
@@ -138,8 +149,10 @@ __global__ void edge_pivots_kernel(const BuildArgs a) {
     }
 }
 
-// One warp per row; lanes 0..15 carry one pole each.  fill = 0 counts, 1 writes.
-// Both passes run this same code, so they take identical decisions; the fill
+// One warp per row; lanes 0..15 carry one pole each.  fill = 0 counts, 1 writes
+// the CSR, 2 counts and writes the row's entries into chunks of the pool (one walk
+// instead of two; a full pool sets kStatusPoolFull and the host walks twice).
+// Every mode runs this same code, so they take identical decisions; the fill
 // pass still checks that the row's entries land exactly in [rowptr[r], rowptr[r+1]).
 //
 // The walk emits a row's columns in increasing order when segments are numbered
@@ -181,8 +194,19 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
     double carry[kChainDepth];
     const bool lump = fill && a.lump;
     int64_t kept = 0;
-    int64_t out = fill ? a.rowptr[row] : 0;
-    const int64_t out_end = fill ? a.rowptr[row + 1] : 0;
+    int64_t out = 0;                                   // the row's next slot
+    const int64_t obase = fill == 1 ? a.rowptr[row] : 0;
+    const int64_t cap = fill == 1 ? a.rowptr[row + 1] - obase : 0;
+    // fill = 2: the row's chunks (lane 0 alone writes entries and keeps the list).
+    int32_t chunks[kMaxChunks];
+    int nchunks = 0;
+    auto slot = [&](int64_t sl) -> int64_t {          // index into the destination, -1: none
+        if (fill == 1) return sl < cap ? obase + sl : -1;
+        if (fill == 2) return (sl / kChunk) < nchunks ? (int64_t)chunks[sl / kChunk] * kChunk + sl % kChunk : -1;
+        return -1;
+    };
+    double* const dval = fill == 2 ? a.pool_val : a.out_val;
+    int32_t* const dcol = fill == 2 ? a.pool_col : a.out_col;
     // Climb.
     int depth = 0;
     int64_t cur = row;
@@ -222,13 +246,31 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
             const bool keep = fabs(vu) >= a.tol || (a.lump && u == row);   // lumping keeps the row's own entry
             int64_t myslot = -1;
             if (keep) {
-                if (fill && lane == 0 && out < out_end) { a.out_col[out] = (int32_t)u; a.out_val[out] = vu; }
+                if (fill == 2 && lane == 0 && out % kChunk == 0) {
+                    const int c = nchunks < kMaxChunks ? atomicAdd(a.pool_top, 1) : a.pool_chunks;
+                    if (c < a.pool_chunks) {
+                        if (nchunks == 0) a.pool_first[row] = c;
+                        else a.pool_next[chunks[nchunks - 1]] = c;
+                        chunks[nchunks++] = c;
+                    } else {
+                        atomicOr(a.status, kStatusPoolFull);
+                    }
+                }
+                if (fill && lane == 0) {
+                    const int64_t d = slot(out);
+                    if (d >= 0) { dcol[d] = (int32_t)u; dval[d] = vu; }
+                }
                 myslot = out;
                 ++out;
                 ++kept;
             } else if (lump) {
                 if (cp >= 0) carry[cp] += vu;
-                else if (tslot >= 0) { if (lane == 0 && tslot < out_end) a.out_val[tslot] += vu; }
+                else if (tslot >= 0) {
+                    if (lane == 0) {
+                        const int64_t d = slot(tslot);
+                        if (d >= 0) dval[d] += vu;
+                    }
+                }
                 else carry[tchain] += vu;
             }
             if (lump && cp >= 0) chain_slot[cp] = myslot;
@@ -269,15 +311,36 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
             for (int m = depth; m >= 0; --m) {
                 acc += carry[m];
                 if (chain_slot[m] >= 0) {
-                    if (chain_slot[m] < out_end) a.out_val[chain_slot[m]] += acc;
+                    const int64_t d = slot(chain_slot[m]);
+                    if (d >= 0) dval[d] += acc;
                     acc = 0.0;
                 }
             }
         }
     }
 done:
-    if (!fill && lane == 0) a.count[row] = kept;
-    if (fill && lane == 0 && out != out_end) atomicOr(a.status, kStatusRowMismatch);
+    if (fill != 1 && lane == 0) a.count[row] = kept;
+    if (fill == 1 && lane == 0 && out != cap) atomicOr(a.status, kStatusRowMismatch);
+}
+
+// One warp per row: the row's chunks of the pool, in order, into its CSR range.
+__global__ void pool_to_rows_kernel(int64_t n, const int64_t* __restrict__ count,
+                                    const int32_t* __restrict__ first, const int32_t* __restrict__ next,
+                                    const int32_t* __restrict__ pcol, const double* __restrict__ pval,
+                                    const int64_t* __restrict__ rowptr, int32_t* __restrict__ out_col,
+                                    double* __restrict__ out_val) {
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const int64_t cnt = count[row], dst = rowptr[row];
+    int c = first[row];
+    for (int64_t e = 0; e < cnt; e += kChunk) {
+        for (int k = lane; k < kChunk && e + k < cnt; k += 32) {
+            out_col[dst + e + k] = pcol[(int64_t)c * kChunk + k];
+            out_val[dst + e + k] = pval[(int64_t)c * kChunk + k];
+        }
+        if (e + kChunk < cnt) c = next[c];
+    }
 }
 
 // ---------------------------------------------------------------- host
@@ -327,9 +390,22 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
     NW_CUDA(ctx, cudaMemcpyToSymbol(c_w, w, sizeof(w)));
 
     DevBuf d_cptr, d_cidx, d_gsum, d_down, d_up, d_invT, d_count;
+    DevBuf d_pcol, d_pval, d_pfirst, d_pnext, d_ptop;
+    auto free_pool = [&]() { dev_free(d_pcol); dev_free(d_pval); dev_free(d_pfirst); dev_free(d_pnext); dev_free(d_ptop); };
     auto cleanup = [&]() {
         dev_free(d_cptr); dev_free(d_cidx); dev_free(d_gsum); dev_free(d_down);
         dev_free(d_up); dev_free(d_invT); dev_free(d_count);
+        free_pool();
+    };
+    // A pool buffer is optional: a failed allocation only means two walks.
+    auto try_alloc = [&](DevBuf& b, size_t bytes) {
+        if (cudaMalloc(&b.ptr, bytes) != cudaSuccess) {
+            b.ptr = nullptr;
+            cudaGetLastError();
+            return false;
+        }
+        b.bytes = bytes;
+        return true;
     };
     int rc = NW_OK;
     do {
@@ -362,7 +438,31 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
         }
         const int64_t rows_per_block = 16;
         const int64_t rblocks = (n + rows_per_block - 1) / rows_per_block;   // 16 rows per 256-thread block
-        propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 0);
+        // One walk per row into a pool of chunks, sized to a quarter of the free
+        // device memory (at most 32 chunks per row); without room, or when the pool
+        // fills up, a counting walk and a filling walk as before.
+        bool pooled = false;
+        {
+            size_t free_b = 0, total_b = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); free_b = 0; }
+            const int64_t per_chunk = (int64_t)kChunk * (4 + 8) + 4;
+            int64_t chunks = (int64_t)(0.25 * (double)free_b) / per_chunk;
+            chunks = std::min<int64_t>(std::min<int64_t>(chunks, 32 * n), (int64_t)INT32_MAX - 1);
+            if (ctx->prop_pool_chunks > 0) chunks = std::min<int64_t>(chunks, ctx->prop_pool_chunks);
+            if (ctx->prop_walk_once && chunks >= 1 && try_alloc(d_pcol, 4 * (size_t)kChunk * chunks) &&
+                try_alloc(d_pval, 8 * (size_t)kChunk * chunks) && try_alloc(d_pnext, 4 * (size_t)chunks) &&
+                try_alloc(d_pfirst, 4 * (size_t)n) && try_alloc(d_ptop, 16)) {
+                cudaMemsetAsync(d_pfirst.ptr, 0xff, 4 * n, ctx->stream);
+                cudaMemsetAsync(d_ptop.ptr, 0, 16, ctx->stream);
+                a.pool_col = d_pcol.as<int32_t>(); a.pool_val = d_pval.as<double>();
+                a.pool_first = d_pfirst.as<int32_t>(); a.pool_next = d_pnext.as<int32_t>();
+                a.pool_top = d_ptop.as<int>(); a.pool_chunks = (int)chunks;
+                pooled = true;
+            } else {
+                free_pool();
+            }
+        }
+        propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, pooled ? 2 : 0);
         if (cudaGetLastError() != cudaSuccess) { rc = fail(ctx, NW_ERR_CUDA, "propagator build launch failed"); break; }
         std::vector<int64_t> cnt(n);
         int st = 0;
@@ -370,6 +470,18 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
         cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream);
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "propagator build (count pass)"); break; }
+        if (pooled && (st & kStatusPoolFull) && !(st & kStatusStackOverflow)) {
+            pooled = false;
+            free_pool();
+            cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
+            propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 0);
+            if (cudaGetLastError() != cudaSuccess) { rc = fail(ctx, NW_ERR_CUDA, "propagator build launch failed"); break; }
+            cudaMemcpyAsync(cnt.data(), d_count.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream);
+            cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream);
+            e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "propagator build (count pass)"); break; }
+        }
+        ctx->prop_walks = pooled ? 1 : 2;
         if (st & kStatusStackOverflow) {
             cudaMemsetAsync(ctx->status.ptr, 0, 4, ctx->stream);
             rc = fail(ctx, NW_ERR_LIMIT, "propagator build: walk stack or ancestor chain overflow (reach too large "
@@ -386,7 +498,14 @@ int tree_propagator_build(nw_ctx* ctx, const double* d_res, const double* d_cap,
         a.rowptr = out_rowptr.as<int64_t>();
         a.out_col = out_col.as<int32_t>();
         a.out_val = out_val.as<double>();
-        propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 1);
+        if (pooled) {
+            pool_to_rows_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(
+                n, d_count.as<int64_t>(), d_pfirst.as<int32_t>(), d_pnext.as<int32_t>(), d_pcol.as<int32_t>(),
+                d_pval.as<double>(), a.rowptr, a.out_col, a.out_val);
+        } else {
+            propagator_rows_kernel<<<(unsigned)rblocks, 256, 0, ctx->stream>>>(a, 1);
+        }
+        if (cudaGetLastError() != cudaSuccess) { rc = fail(ctx, NW_ERR_CUDA, "propagator build launch failed"); break; }
         cudaMemcpyAsync(&st, ctx->status.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream);
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "propagator build (fill pass)"); break; }

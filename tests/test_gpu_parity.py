@@ -85,6 +85,31 @@ def test_lumped_propagator_matches_oracle(tol):
     ctx.close()
 
 
+@pytest.mark.parametrize("lump,tol", [(0, EPSILON), (0, 1e-8), (1, 1e-8), (1, 1e-6)])
+def test_single_walk_build_equals_two_walks(lump, tol):
+    """One walk per row into pool chunks gives the CSR of the counting and filling
+    walks bit for bit; a pool too small for the rows falls back to two walks."""
+    trees = [random_tree(300, seed=3), random_tree(1, seed=0), random_tree(120, seed=8), random_tree(700, seed=9)]
+    out = []
+    for once, chunks in ((0, 0), (1, 0), (1, 40)):
+        ctx, parent, R, C = _ctx_with_tree(trees)
+        ctx.set_option("propagator_lump", lump)
+        ctx.set_option("propagator_single_walk", once)
+        ctx.set_option("propagator_pool_chunks", chunks)
+        nnz = ctypes.c_int64()
+        ctx.call("nw_propagator_build", tol, ctypes.byref(nnz))
+        walks = ctx.get_option("propagator_walks")
+        P = _read_csr(ctx, len(parent))
+        out.append((walks, P.indptr.copy(), P.indices.copy(), P.data.copy()))
+        ctx.close()
+    assert [o[0] for o in out] == [2, 1, 2]
+    if tol <= 1e-8:
+        assert np.diff(out[1][1]).max() > 2 * 64   # rows span several chunks
+    for o in out[1:]:
+        for x, y in zip(o[1:], out[0][1:]):
+            assert np.array_equal(x, y)
+
+
 def test_propagator_reference_fixture():
     t = Tree(F["geom_parent"], F["geom_coordinates"], F["geom_diameter"])
     ctx, parent, R, C = _ctx_with_tree([t])
