@@ -172,13 +172,16 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
     const unsigned half_mask = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;
     if (row >= a.n_seg) return;
     const int k = lane;
-    const cplx w = cplx(c_w[k].x, c_w[k].y);
-    const double scale_out = 2.0 / kNodes;
+    // Each lane carries its pole's resolvent entry already multiplied by the
+    // quadrature weight e^{z_k} z'_k and 2/N (the walk only multiplies it by edge
+    // ratios, so the factor can be applied once at the row's start): the entry
+    // P_ij is then the sum over the poles of the imaginary parts.
+    const cplx wk = scale(2.0 / kNodes, cplx(c_w[k].x, c_w[k].y));
     auto value = [&](cplx yy) -> double {
-        double v = (w * yy).im;
+        double v = yy.im;
 #pragma unroll
         for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(half_mask, v, off, 16);
-        return __shfl_sync(half_mask, v, 0, 16) * scale_out;
+        return __shfl_sync(half_mask, v, 0, 16);
     };
     int32_t chain[kChainDepth];
     cplx chain_y[kChainDepth];
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(256) propagator_rows_kernel(const BuildArgs a,
     // Climb.
     int depth = 0;
     int64_t cur = row;
-    cplx y = ld(&a.invT[row * kPoles + k]);
+    cplx y = wk * ld(&a.invT[row * kPoles + k]);
     chain[0] = (int32_t)row;
     chain_y[0] = y;
     double v = value(y);
