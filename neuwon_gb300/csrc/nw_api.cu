@@ -334,6 +334,7 @@ int nw_synchronize(nw_ctx* ctx) {
 int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
                   const int64_t* neuron_start, const int64_t* parent,
                   double time_step_ms, double celsius) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (num_segments <= 0 || num_neurons <= 0 || !neuron_start || !parent)
@@ -421,6 +422,7 @@ int nw_model_init(nw_ctx* ctx, int64_t num_segments, int64_t num_neurons,
 }
 
 int nw_set_data(nw_ctx* ctx, const char* name, const void* host, int dtype, int64_t count) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx || !name || (!host && count)) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     std::string nm(name);
@@ -603,6 +605,7 @@ int nw_get_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t co
 }
 
 int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_propagator_build before nw_model_init");
@@ -620,6 +623,7 @@ int nw_propagator_build(nw_ctx* ctx, double prune_tolerance, int64_t* nnz_out) {
 
 int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr, const int64_t* col,
                           const double* val, int64_t nnz) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_propagator_set_csr before nw_model_init");
@@ -646,6 +650,7 @@ int nw_propagator_set_csr(nw_ctx* ctx, int64_t n, const int64_t* rowptr, const i
 }
 
 int nw_propagator_conserve(nw_ctx* ctx) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (!ctx->prop_valid) return fail(ctx, NW_ERR_STATE, "nw_propagator_conserve: no propagator installed");
@@ -755,6 +760,7 @@ static int upload_layout(nw_ctx* ctx, const InstanceLayout& L, DevBuf& seg, DevB
 int nw_hh_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segment,
                    const double* gna_coef, const double* gk_coef, const double* gl_coef,
                    double ena, double ek, double el, double v_init) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_hh_register before nw_model_init");
@@ -861,6 +867,7 @@ static int kinetic_add(nw_ctx* ctx, const char* who, int64_t num_instances, cons
 extern "C" {
 
 int nw_species_set(nw_ctx* ctx, int32_t count, const double* reversal_potential_mV) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx || count < 0 || (count && !reversal_potential_mV)) return NW_ERR_ARG;
     for (int32_t s = 0; s < count; ++s)
         if (!std::isfinite(reversal_potential_mV[s]))
@@ -885,6 +892,7 @@ int nw_species_conductance(nw_ctx* ctx, int32_t species, double* conductance_out
 }
 
 int nw_kinetic_clear(nw_ctx* ctx) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
@@ -897,6 +905,7 @@ int nw_kinetic_add(nw_ctx* ctx, int64_t num_instances, const int64_t* segment, c
                    int num_states, int num_open, const int32_t* open_states, double erev, int32_t species,
                    const double* table, int num_buckets, int num_terms, double vmin, double bucket_frq,
                    double conserve_sum, const double* init_state, int32_t* mechanism_out) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     return kinetic_add(ctx, "nw_kinetic_add", num_instances, segment, g_coef, num_states, num_open, open_states,
                        erev, species, table, num_buckets, num_terms, vmin, bucket_frq, conserve_sum, init_state,
                        mechanism_out);
@@ -906,6 +915,7 @@ int nw_kinetic_inputs(nw_ctx* ctx, int32_t mechanism, int32_t kind1, int32_t num
                       double bucket_frq1, double scale1, int32_t kind2, int32_t num_buckets2, double minimum2,
                       double bucket_frq2, double scale2, int32_t num_terms, const int32_t* powers,
                       double input_initial) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (mechanism < 0 || mechanism >= ctx->n_kin)
@@ -950,6 +960,7 @@ int nw_kinetic_register(nw_ctx* ctx, int64_t num_instances, const int64_t* segme
                         const double* g_coef, int num_states, int num_open, const int32_t* open_states,
                         double erev, const double* table, int num_buckets, int num_terms,
                         double vmin, double bucket_frq, double conserve_sum, const double* init_state) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     NW_CHECK(nw_kinetic_clear(ctx));
     return kinetic_add(ctx, "nw_kinetic_register", num_instances, segment, g_coef, num_states, num_open,
                        open_states, erev, -1, table, num_buckets, num_terms, vmin, bucket_frq, conserve_sum,
@@ -960,6 +971,7 @@ int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron
                     const double* w_ampa, const double* w_nmda, const int32_t* delay_steps,
                     const double* ampa_on, const double* ampa_off, const double* nmda_on, const double* nmda_off,
                     int32_t pulse_steps, double e_syn, double mg) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_synapses_set before nw_model_init");
@@ -1039,6 +1051,7 @@ int nw_synapses_set(nw_ctx* ctx, int64_t num_synapses, const int64_t* pre_neuron
 
 int nw_clamps_set(nw_ctx* ctx, int64_t count, const int64_t* segment, const double* amps,
                   const int64_t* first_tick, const int64_t* num_ticks) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_clamps_set before nw_model_init");
@@ -1093,6 +1106,7 @@ int nw_clamps_set(nw_ctx* ctx, int64_t count, const int64_t* segment, const doub
 }
 
 int nw_detectors_set(nw_ctx* ctx, const int64_t* segment, const double* threshold_mV) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx || !segment || !threshold_mV) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_detectors_set before nw_model_init");
@@ -1120,6 +1134,7 @@ int nw_detectors_set(nw_ctx* ctx, const int64_t* segment, const double* threshol
 }
 
 int nw_probes_set(nw_ctx* ctx, int64_t count, const int64_t* segment, int64_t max_steps) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_probes_set before nw_model_init");
@@ -1191,6 +1206,7 @@ int nw_advance(nw_ctx* ctx, int32_t k_steps, int path) {
     cudaSetDevice(ctx->device);
     NW_CHECK(check_ready(ctx, k_steps));
     if (k_steps == 0) return NW_OK;
+    if (path != NW_PATH_BATCHED) ctx->gc_valid = false;   // these paths do not fill the cache
     if (path == NW_PATH_BATCHED) NW_CHECK(advance_batched(ctx, k_steps));
     else if (path == NW_PATH_PLAIN) NW_CHECK(advance_plain(ctx, k_steps));
     else if (path == NW_PATH_WIDE) NW_CHECK(advance_wide(ctx, k_steps));
@@ -1285,6 +1301,7 @@ int nw_get_clock(nw_ctx* ctx, int64_t* steps, int64_t* input_ticks) {
 }
 
 int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     if (lanes_per_row != 0 && lanes_per_row != 4 && lanes_per_row != 8 && lanes_per_row != 16 && lanes_per_row != 32)
         return fail(ctx, NW_ERR_ARG, "lanes_per_row must be 0, 4, 8, 16 or 32");
@@ -1298,6 +1315,7 @@ int nw_set_tuning(nw_ctx* ctx, int lanes_per_row, int threads, int ctas_per_sm) 
 }
 
 int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx || !name) return NW_ERR_ARG;
     std::string nm(name);
     if (nm == "bulk_pipeline") { ctx->use_bulk = value != 0; return NW_OK; }
@@ -1421,6 +1439,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "adjoint_overlap") { *value = ctx->adjoint_overlap ? 1 : 0; return NW_OK; }
     if (nm == "propagator_single_walk") { *value = ctx->prop_walk_once ? 1 : 0; return NW_OK; }
     if (nm == "propagator_walks") { *value = ctx->prop_walks; return NW_OK; }
+    if (nm == "conductance_cache_valid") { *value = ctx->gc_valid ? 1 : 0; return NW_OK; }
     if (nm == "propagator_pool_chunks") { *value = ctx->prop_pool_chunks; return NW_OK; }
     if (nm == "narrow_neurons") {
         int64_t k = 0;
@@ -1446,6 +1465,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
 
 int nw_adjoint_forward(nw_ctx* ctx, int64_t num_steps, int32_t checkpoint_every, const double* target,
                        double* loss_out) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     return adjoint_forward(ctx, num_steps, checkpoint_every, target, loss_out);
@@ -1453,6 +1473,7 @@ int nw_adjoint_forward(nw_ctx* ctx, int64_t num_steps, int32_t checkpoint_every,
 
 int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad_gna, double* grad_gk,
                         double* grad_gl, double* grad_ra) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     return adjoint_backward(ctx, cytoplasmic_resistance, grad_gna, grad_gk, grad_gl, grad_ra);
@@ -1460,10 +1481,13 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
 
 int nw_autotune(nw_ctx* ctx, int32_t trial_steps, int32_t* lanes_per_row, int32_t* threads,
                 int32_t* fusion_depth, double* ms_per_step) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     NW_CHECK(check_ready(ctx, 0));
-    return autotune(ctx, trial_steps, lanes_per_row, threads, fusion_depth, ms_per_step);
+    const int rc = autotune(ctx, trial_steps, lanes_per_row, threads, fusion_depth, ms_per_step);
+    ctx->gc_valid = false;   // the trials advanced the model and then restored its state
+    return rc;
 }
 
 int nw_get_tuning(nw_ctx* ctx, int* lanes_per_row, int* threads, int* ctas_per_sm) {

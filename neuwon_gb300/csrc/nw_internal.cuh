@@ -39,7 +39,7 @@ struct DevClock {
     int64_t steps;              // completed steps before the sequence
     int64_t probe_len;          // probe rows already recorded
     int32_t g_valid;            // mechanism conductances valid at the first half step
-    int32_t pad;
+    int32_t gc_valid;           // the conductance cache holds G, G*E of the mechanism state
 };
 
 // One instantiated CUDA graph of a batched launch sequence, keyed by every
@@ -221,6 +221,10 @@ struct nw_ctx {
     // lanes_split take half the kernel's lanes per row (0: every neuron the same).
     std::vector<float> h_neuron_qpr;                   // mean quads per row, per neuron
     int64_t lanes_split = 0;
+    // The conductance cache (gcache) holds G and G*E of the present mechanism state:
+    // set by a batched advance whose kernel ran the fused mechanism pass, cleared by
+    // every other entry point that can change the model (its next launch gathers).
+    bool gc_valid = false;
     bool prop_walk_once = true;  // tree propagator build: one walk per row into a pool when it fits
     int prop_walks = 0;          // walks per row of the last tree propagator build
     int64_t prop_pool_chunks = 0;   // cap on the pool's chunks (0: a quarter of free memory)

@@ -116,6 +116,7 @@ int nw_lti_expm(nw_ctx* ctx, int32_t S, int64_t count, const double* rates, doub
 
 int nw_lti_table_build(nw_ctx* ctx, int32_t S, int32_t num_buckets, int32_t samples_per_bucket, int32_t num_terms,
                        const double* rates, const double* fit, double dt, int32_t target, double* table_out) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     const bool kin_target = target == 1 || (target >= 16 && target < 16 + kMaxKinetic);

@@ -42,6 +42,7 @@ extern "C" {
 int nw_calcium_set(nw_ctx* ctx, double diffusivity, const double* cross_area_um2, const double* length_um,
                    const double* volume_um3, double initial_mM, double prune_tolerance, int conserve,
                    int64_t* nnz_out) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n_seg == 0) return fail(ctx, NW_ERR_STATE, "nw_calcium_set before nw_model_init");
@@ -98,6 +99,7 @@ int nw_calcium_set(nw_ctx* ctx, double diffusivity, const double* cross_area_um2
 int nw_calcium_pump_set(nw_ctx* ctx, const double* influx_coef, const double* efflux_coef, const double* table,
                         int32_t num_buckets, int32_t num_terms, double log2_min, double bucket_frq, double scale,
                         const double* initial_state) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     CalciumState& C = ctx->ca;
@@ -130,6 +132,7 @@ int nw_calcium_pump_set(nw_ctx* ctx, const double* influx_coef, const double* ef
 }
 
 int nw_calcium_data(nw_ctx* ctx, const char* name, void* host, int dtype, int64_t count, int write) {
+    if (ctx) ctx->gc_valid = false;   // the model may change: the next launch gathers G
     if (!ctx || !name || (!host && count)) return NW_ERR_ARG;
     cudaSetDevice(ctx->device);
     CalciumState& C = ctx->ca;

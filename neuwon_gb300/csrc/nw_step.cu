@@ -157,6 +157,7 @@ static int push_clock(nw_ctx* ctx) {
     v.steps = ctx->steps;
     v.probe_len = ctx->probe_len;
     v.g_valid = ctx->g_valid ? 1 : 0;
+    v.gc_valid = ctx->gc_valid ? 1 : 0;
     set_clock_kernel<<<1, 1, 0, ctx->stream>>>(ctx->dclock.as<DevClock>(), v);
     NW_CUDA(ctx, cudaGetLastError());
     return NW_OK;
@@ -271,8 +272,15 @@ static void finish_steps(nw_ctx* ctx, int k_steps) {
 int advance_batched(nw_ctx* ctx, int k_steps) {
     int rc = ctx->precision == NW_F64 ? launch_batched<double>(ctx, k_steps)
                                       : launch_batched<float>(ctx, k_steps);
-    if (rc != NW_OK) return rc;
+    if (rc != NW_OK) {
+        ctx->gc_valid = false;
+        return rc;
+    }
     finish_steps(ctx, k_steps);
+    // The fused mechanism pass (compiled into the quad and windows kernels) ran and
+    // left the cache filled from the state the next step starts from.
+    if (k_steps > 0)
+        ctx->gc_valid = (ctx->prop_format == 2 || ctx->prop_format == 3) && fuse_mechanisms(ctx);
     return NW_OK;
 }
 

@@ -386,6 +386,10 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
     const int64_t row_base = a.clk->probe_len + s_off;
     const int64_t step_base = a.clk->steps + s_off;
     const bool g_valid0 = s_off > 0 || a.clk->g_valid != 0;
+    // The fused pass leaves G, G*E in the cache at every step, the last one of a
+    // launch included, so a launch's first step reads them too unless the host
+    // changed the model since.
+    const bool gc_in0 = s_off > 0 || a.clk->gc_valid != 0;
     __shared__ int s_job;
     __shared__ int s_abort;
     BulkRing ring;
@@ -512,7 +516,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     for (int li = tid; li < n; li += nthr) {
                         const int64_t i = base + li;
                         real G, GE;
-                        if (fuse && s > 0) { G = a.gc[i]; GE = a.gc[a.gc_n + i]; }
+                        if (fuse && (s > 0 || gc_in0)) { G = a.gc[i]; GE = a.gc[a.gc_n + i]; }
                         else if (gv) segment_conductance(a, i, G, GE);
                         else { G = real(0); GE = real(0); }
                         xs[li] = membrane_x(a, i, G, GE, stim(i, tick), last);
@@ -564,7 +568,7 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     // Mechanisms (rxd_model.py:115-123) at the mid-step voltage, then
                     // the segment's conductance and the second half's x, in one pass.
                     const bool last1 = s == a.k_steps - 1;
-                    const bool keep = s + 1 < a.k_steps;
+                    const bool keep = true;
                     if (fused_fast_form(a)) {
                         for (int li = tid; li < n; li += nthr) {
                             const int64_t i = base + li;

@@ -49,6 +49,58 @@ def test_graph_replay_and_fusion_are_bit_identical(fusion):
     ref.close(); m.close()
 
 
+def _quad_case(precision):
+    trees = [random_tree(n, seed=s) for s, n in ((3, 400), (4, 150), (5, 900))]
+    clamps = [(0, 0, 0.3, 0.0, 30.0), (1, 0, 0.25, 2.0, 10.0), (2, 0, 0.4, 1.0, 40.0)]
+    m, neurons, offs, recs = gpu_model(trees, clamps, precision=precision, kinetic=True, fmt="quads")
+    for (ti, s, nA, start, dur) in clamps:
+        nw.Segment(m, offs[ti] + s).inject_current(nA, dur)
+    m._sync()
+    m._ctx.set_option("fusion_depth", 1)
+    return m
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_conductance_cache_carries_over_calls_until_the_model_changes(precision):
+    """One-step calls start from the conductances the previous call's fused pass
+    cached; any change made between calls (gates, densities, kinetic states,
+    another path's steps) makes the next launch gather them again.  Bit-identical
+    to a model whose cache is dropped after every call."""
+    from neuwon_gb300 import _lib
+    runs = []
+    for drop in (False, True):
+        m = _quad_case(precision)
+        used = []
+
+        def steps(k):
+            for _ in range(k):
+                m.advance(1)
+                used.append(m._ctx.get_option("conductance_cache_valid"))
+                if drop:
+                    m._ctx.set_option("cuda_graph", 1)      # every option call drops the cache
+        steps(6)
+        gm = m._ctx.get_data("hh.m", m._instance_count("hh"))
+        gm[::3] *= 0.7
+        m._ctx.set_data("hh.m", gm)
+        steps(4)
+        k = m._instance_count("hh")
+        m.set_hh_densities(np.full(k, 0.15), 0.036, np.full(k, 0.0004))
+        steps(4)
+        st = m.get_data("na8.state")
+        m.set_data("na8.state", np.roll(st, 1, axis=0))
+        steps(4)
+        m._ctx.advance(2, _lib.PATH_PLAIN)
+        m.input_hook.ticks += 4
+        m.advance_hook._tick(2)
+        steps(4)
+        if not drop:
+            assert all(u == 1 for u in used)             # the cache was in use after every call
+        runs.append(_state(m))
+        m.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+
+
 def test_graph_cache_follows_launch_shape():
     m, _ = _case(probes=())
     m._ctx.set_option("fusion_depth", 10)
