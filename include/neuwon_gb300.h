@@ -408,9 +408,18 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * the CSR; with 0, or when the pool fills up, a counting walk and a filling walk.
  * The CSR is the same bit for bit; nw_get_option("propagator_walks") tells which
  * (1 or 2) the last build used.
+ * "pair_shared_limit" (default -1): pair format, the largest neuron whose integer
+ * pair sums stay in shared memory (-1: as many as fit); larger ones use global
+ * memory, with the same sums.
  * nw_get_option also reports "wide_quads", "wide_entries" and
  * "calcium_wide_entries" (stored windows / entries of the wide path's voltage and
- * calcium propagators, once built). */
+ * calcium propagators, once built), "quads" (stored quad windows of the batched
+ * path), "windows_8", "windows_4", "windows_2", "windows_1" (windows of each width
+ * in the windows format), "pair_entries" (couplings of the pair format),
+ * "kinetic_mechanisms" (kinetic mechanisms registered) and
+ * "conductance_cache_valid" (1 when the next batched launch reads its first step's
+ * conductances from the cache the last fused launch left; every entry point that
+ * can change the model clears it). */
 int nw_set_option(nw_ctx* ctx, const char* name, int64_t value);
 int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value);
 

@@ -34,6 +34,15 @@ def test_library_builds_and_exports_every_declared_symbol():
     assert set(syms) == set(_lib.EXPORTS)
 
 
+def test_every_option_name_is_documented_in_the_header():
+    """nw_set_option / nw_get_option accept exactly the names the header documents."""
+    src = open(os.path.join(ROOT, "neuwon_gb300", "csrc", "nw_api.cu")).read()
+    names = set(re.findall(r'nm == "([a-z0-9_]+)"', src))
+    header = open(HEADER).read()
+    assert len(names) > 30
+    assert sorted(n for n in names if f'"{n}"' not in header) == []
+
+
 def test_version_call_needs_no_gpu():
     lib = _lib.load()
     assert lib.nw_version() >= 100
