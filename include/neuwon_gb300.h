@@ -408,6 +408,10 @@ int nw_adjoint_backward(nw_ctx* ctx, double cytoplasmic_resistance, double* grad
  * the CSR; with 0, or when the pool fills up, a counting walk and a filling walk.
  * The CSR is the same bit for bit; nw_get_option("propagator_walks") tells which
  * (1 or 2) the last build used.
+ * "rows_claimed" (default 1): in the batched quad-format step the warps of a neuron's
+ * CTA take its rows from a shared counter, two row groups at a time, each claiming its
+ * next chunk before it works on the current one, instead of a fixed share each; a row
+ * is summed by the same lanes in the same order either way (same bits).
  * "pair_shared_limit" (default -1): pair format, the largest neuron whose integer
  * pair sums stay in shared memory (-1: as many as fit); larger ones use global
  * memory, with the same sums.

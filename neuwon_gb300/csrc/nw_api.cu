@@ -1363,6 +1363,7 @@ int nw_set_option(nw_ctx* ctx, const char* name, int64_t value) {
     if (nm == "wide_fusion") { ctx->wide_fusion = value != 0; return NW_OK; }
     if (nm == "adjoint_overlap") { ctx->adjoint_overlap = value != 0; return NW_OK; }
     if (nm == "propagator_single_walk") { ctx->prop_walk_once = value != 0; return NW_OK; }
+    if (nm == "rows_claimed") { ctx->rows_claimed = value != 0; return NW_OK; }
     if (nm == "propagator_pool_chunks") {
         if (value < 0) return fail(ctx, NW_ERR_ARG, "propagator_pool_chunks must be >= 0");
         ctx->prop_pool_chunks = value;
@@ -1439,6 +1440,7 @@ int nw_get_option(nw_ctx* ctx, const char* name, int64_t* value) {
     if (nm == "adjoint_overlap") { *value = ctx->adjoint_overlap ? 1 : 0; return NW_OK; }
     if (nm == "propagator_single_walk") { *value = ctx->prop_walk_once ? 1 : 0; return NW_OK; }
     if (nm == "propagator_walks") { *value = ctx->prop_walks; return NW_OK; }
+    if (nm == "rows_claimed") { *value = ctx->rows_claimed ? 1 : 0; return NW_OK; }
     if (nm == "conductance_cache_valid") { *value = ctx->gc_valid ? 1 : 0; return NW_OK; }
     if (nm == "propagator_pool_chunks") { *value = ctx->prop_pool_chunks; return NW_OK; }
     if (nm == "narrow_neurons") {

@@ -225,6 +225,7 @@ struct nw_ctx {
     // set by a batched advance whose kernel ran the fused mechanism pass, cleared by
     // every other entry point that can change the model (its next launch gathers).
     bool gc_valid = false;
+    bool rows_claimed = true;   // batched quad rows: warps claim row chunks from a shared counter
     bool prop_walk_once = true;  // tree propagator build: one walk per row into a pool when it fits
     int prop_walks = 0;          // walks per row of the last tree propagator build
     int64_t prop_pool_chunks = 0;   // cap on the pool's chunks (0: a quarter of free memory)

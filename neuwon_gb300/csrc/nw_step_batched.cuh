@@ -409,6 +409,8 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
         __syncthreads();
     }
     __shared__ int s_nclamp;
+    __shared__ int s_rowctr[2];          // quad rows claimed, one counter per half step
+    if (QUAD && threadIdx.x == 0) { s_rowctr[0] = 0; s_rowctr[1] = 0; }
     __shared__ uint32_t s_cseg[kMaxClampsPerNeuron];
     __shared__ real s_camp[kMaxClampsPerNeuron];
     __shared__ int64_t s_cfirst[kMaxClampsPerNeuron], s_cend[kMaxClampsPerNeuron];
@@ -540,7 +542,12 @@ batched_advance_kernel(const StepArgs<real> a, const int xs_bytes, const int s_o
                     };
                     // Neurons of short rows (mean quads per row below the tuned split)
                     // take half the lanes per row, the others the kernel's LPR.
-                    if (LPR >= 8 && a.neuron_narrow && a.neuron_narrow[j])
+                    if (a.rows_claimed && !(LPR >= 8 && a.neuron_narrow && a.neuron_narrow[j])) {
+                        // This half step's counter starts at zero; the other half's is
+                        // reset for its next use (no warp reads it before a barrier).
+                        if (tid == 0) s_rowctr[half ^ 1] = 0;
+                        propagate_quads_claimed<real, LPR>(a, base, n, xs, store, &s_rowctr[half]);
+                    } else if (LPR >= 8 && a.neuron_narrow && a.neuron_narrow[j])
                         propagate_quads<real, (LPR >= 8 ? LPR / 2 : LPR)>(a, base, n, xs, store);
                     else
                         propagate_quads<real, LPR>(a, base, n, xs, store);

@@ -121,6 +121,7 @@ struct StepArgs {
     // quad propagator: windows of 4 consecutive columns
     const int64_t* qrow; const uint16_t* qbase; const real* qval;
     const uint8_t* neuron_narrow;     // quad rows of these neurons take half the lanes (null: none)
+    int rows_claimed;                 // quad rows taken by the warps from a shared counter
     // windows propagator: per row a descriptor {value block / 4, first base,
     // n8 | n4 << 16, n2 | n1 << 16}, the u16 bases and the values
     const uint4* wnrow; const uint16_t* wnbase; const real* wnval;
@@ -693,6 +694,36 @@ __device__ __forceinline__ real quad_row_sum(const StepArgs<real>& a, bool valid
     return t;
 }
 
+// Rows of a neuron taken by the warps from a shared counter (ctr, zero at the
+// phase's start) in chunks of kRowChunk row groups, each warp claiming its next
+// chunk before it works on the current one; a row's sum is the same whichever
+// warp computes it.
+constexpr int kRowChunk = 2;
+template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
+__device__ __forceinline__ void propagate_quads_claimed(const StepArgs<real>& a, int64_t base, int n,
+                                                        const real* __restrict__ xs, Fin fin, int* ctr) {
+    constexpr int GPW = 32 / LPR;
+    const int lane = threadIdx.x & 31;
+    const int q = lane / LPR, l = lane % LPR;
+    int next = 0;
+    if (lane == 0) next = atomicAdd(ctr, kRowChunk * GPW);
+    next = __shfl_sync(0xffffffffu, next, 0);
+    while (next < n) {
+        const int cur = next;
+        if (lane == 0) next = atomicAdd(ctr, kRowChunk * GPW);
+#pragma unroll 1
+        for (int c = 0; c < kRowChunk; ++c) {
+            const int row = cur + c * GPW + q;
+            const bool valid = row < n;
+            const int64_t r = base + row;
+            const real xi = valid ? xs[row] : real(0);
+            const real t = quad_row_sum<real, LPR, UNROLL>(a, valid, r, l, xs, xi);
+            if (valid && l == 0) fin(r, row, xi, (xi - a.leak[r] * xi) + t);
+        }
+        next = __shfl_sync(0xffffffffu, next, 0);
+    }
+}
+
 template <typename real, int LPR, int UNROLL = (LPR >= 16 ? 4 : 2), typename Fin>
 __device__ __forceinline__ void propagate_quads(const StepArgs<real>& a, int64_t base, int n,
                                                 const real* __restrict__ xs, Fin fin) {
@@ -819,6 +850,7 @@ inline StepArgs<real> make_args(nw_ctx* ctx, int k_steps) {
     a.qrow = ctx->q_rowptr.as<int64_t>(); a.qbase = ctx->q_base.as<uint16_t>(); a.qval = ctx->q_val.as<real>();
     a.neuron_narrow = (ctx->lanes_split > 0 && ctx->narrow_for == ctx->lanes_split)
                           ? ctx->neuron_narrow.as<uint8_t>() : nullptr;
+    a.rows_claimed = ctx->rows_claimed ? 1 : 0;
     if (ctx->win_ok) {
         a.wnrow = ctx->win_row.as<uint4>();
         a.wnbase = ctx->win_base.as<uint16_t>(); a.wnval = ctx->win_val.as<real>();

@@ -101,6 +101,26 @@ def test_conductance_cache_carries_over_calls_until_the_model_changes(precision)
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_claimed_rows_give_the_static_schedule_bits(precision):
+    """Quad rows taken by the warps from a shared counter: every row is summed by the
+    same lanes in the same order as under the static schedule."""
+    runs = []
+    for claimed in (0, 1):
+        m = _quad_case(precision)
+        m._ctx.set_option("fusion_depth", 7)
+        m._ctx.set_option("rows_claimed", claimed)
+        m._ctx.call("nw_set_tuning", 8, 256, 0)     # many rows per warp
+        m.advance(30)
+        m._ctx.call("nw_set_tuning", 16, 1024, 0)
+        m.advance(20)
+        assert m._ctx.get_option("rows_claimed") == claimed
+        runs.append(_state(m))
+        m.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+
+
 def test_graph_cache_follows_launch_shape():
     m, _ = _case(probes=())
     m._ctx.set_option("fusion_depth", 10)
