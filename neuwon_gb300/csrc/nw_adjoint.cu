@@ -67,10 +67,19 @@ __device__ __forceinline__ real* tape_slot(const AdjArgs<real>& A, int s, int sl
 
 // V_r-like sums of one neuron's rows applied to xs in the row format or, when the
 // model stores it, the quad format (the same entries); fin(r, row, xi, y).
+// Quad rows are claimed by the warps from the CTA's counters ctr[0..1], which
+// alternate from call to call (phase, the same in every thread): the call resets the
+// other counter, which no warp reads before the barrier that ends this call's phase.
 template <typename real, int LPR, bool QUAD, typename Fin>
-__device__ __forceinline__ void propagate_adj(const StepArgs<real>& a, int64_t base, int n, const real* xs, Fin fin) {
-    if constexpr (QUAD) propagate_quads<real, LPR>(a, base, n, xs, fin);
-    else propagate_rows<real, LPR>(a, base, n, xs, fin);
+__device__ __forceinline__ void propagate_adj(const StepArgs<real>& a, int64_t base, int n, const real* xs, Fin fin,
+                                              int* ctr, int& phase) {
+    if constexpr (QUAD) {
+        if (threadIdx.x == 0) ctr[(phase + 1) & 1] = 0;
+        propagate_quads_claimed<real, LPR>(a, base, n, xs, fin, ctr + (phase & 1));
+        ++phase;
+    } else {
+        propagate_rows<real, LPR>(a, base, n, xs, fin);
+    }
 }
 
 // Quad windows of a neuron of fewer than 4 segments reach past it: zeros there.
@@ -87,6 +96,9 @@ __global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<rea
     extern __shared__ __align__(16) unsigned char smem_raw[];
     real* xs = reinterpret_cast<real*>(smem_raw);
     __shared__ int s_job;
+    __shared__ int s_ctr[2];
+    if (threadIdx.x == 0) { s_ctr[0] = 0; s_ctr[1] = 0; }
+    int phase = 0;
     __shared__ int s_nclamp;
     __shared__ uint32_t s_cseg[kMaxClampsPerNeuron];
     __shared__ real s_camp[kMaxClampsPerNeuron];
@@ -152,7 +164,7 @@ __global__ void __launch_bounds__(1024) adjoint_forward_kernel(const AdjArgs<rea
                 propagate_adj<real, LPR, QUAD>(a, base, n, xs, [&](int64_t r, int, real, real vnew) {
                     if (!isfinite(vnew)) atomicOr(a.status, kStatusNonFinite);
                     a.V[r] = vnew;
-                });
+                }, s_ctr, phase);
                 __syncthreads();
                 if (half == 0) {
                     for (int li = tid; li < n; li += nthr) {
@@ -211,7 +223,8 @@ template <typename real, int LPR, bool QUAD>
 __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_t base, int n, real* xs,
                                                   const real* V_in, const real* V_out, const real* gm,
                                                   const real* gh, const real* gn, const real* lam_out,
-                                                  real* lam_in, bool gv, real& ra_s, real& ra_c) {
+                                                  real* lam_in, bool gv, real& ra_s, real& ra_c, int* ctr,
+                                                  int& phase) {
     const StepArgs<real>& a = A.a;
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int64_t ns = A.n_seg;
@@ -222,7 +235,8 @@ __device__ __forceinline__ void half_step_reverse(const AdjArgs<real>& A, int64_
     __syncthreads();
     // The rows leave lambda of x (C P^T applied) in lam_in; the membrane update's
     // adjoint follows per segment below, with every lane of the CTA.
-    propagate_adj<real, LPR, QUAD>(a, base, n, xs, [&](int64_t r, int, real, real nu) { lam_in[r] = nu * A.cap_r[r]; });
+    propagate_adj<real, LPR, QUAD>(a, base, n, xs, [&](int64_t r, int, real, real nu) { lam_in[r] = nu * A.cap_r[r]; },
+                                   ctr, phase);
     // xs still holds lambda / C of every segment of the neuron (the rows only read it).
     for (int li = tid; li < n; li += nthr) {
         const int64_t i = base + li;
@@ -276,6 +290,9 @@ __global__ void __launch_bounds__(1024, sizeof(real) == 4 ? 2 : 1) adjoint_rever
     real* xs = reinterpret_cast<real*>(smem_raw);
     __shared__ int s_job;
     __shared__ double s_red[1024];
+    __shared__ int s_ctr[2];
+    if (threadIdx.x == 0) { s_ctr[0] = 0; s_ctr[1] = 0; }
+    int phase = 0;
     const StepArgs<real>& a = A.a;
     const int tid = threadIdx.x, nthr = blockDim.x;
     for (;;) {
@@ -299,7 +316,7 @@ __global__ void __launch_bounds__(1024, sizeof(real) == 4 ? 2 : 1) adjoint_rever
             // Second half step: V_mid, gates(s+1) -> V(s+1).
             half_step_reverse<real, LPR, QUAD>(A, base, n, xs, tape_slot(A, s, 1), tape_slot(A, s + 1, 0),
                                          tape_slot(A, s + 1, 2), tape_slot(A, s + 1, 3), tape_slot(A, s + 1, 4),
-                                         A.lamV, A.lamV2, true, ra_s, ra_c);
+                                         A.lamV, A.lamV2, true, ra_s, ra_c, s_ctr, phase);
             // Mechanisms: gates(s+1) = f(gates(s), V_mid).
             for (int li = tid; li < n; li += nthr) {
                 const int64_t i = base + li;
@@ -320,7 +337,7 @@ __global__ void __launch_bounds__(1024, sizeof(real) == 4 ? 2 : 1) adjoint_rever
             const bool gv = (gs > 0) || A.g_valid_first;
             half_step_reverse<real, LPR, QUAD>(A, base, n, xs, tape_slot(A, s, 0), tape_slot(A, s, 1),
                                          tape_slot(A, s, 2), tape_slot(A, s, 3), tape_slot(A, s, 4),
-                                         A.lamV2, A.lamV, gv, ra_s, ra_c);
+                                         A.lamV2, A.lamV, gv, ra_s, ra_c, s_ctr, phase);
         }
         // Fixed-order reduction of the Ra partial sums, scaled by -h / Ra.
         s_red[tid] = (double)ra_s - (double)ra_c;
